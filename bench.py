@@ -1,0 +1,384 @@
+"""Throughput benchmark: attempted atom moves per second on one GB300.
+
+Default workload (the Cu55 EAM configuration): Sutton-Chen EAM Cu55
+(scripts/cu55.jl:39-48 parameters), icosahedral start, SphericalBC(14 bohr),
+32 replicas geometric over 200-1000 K, the chosen form = FP32 move rows with
+an FP64 running total resynchronised by a full FP64 recompute every 1000
+cycles, batched as B independent PT runs (different Philox streams) in one
+launch.  A step is `--cycles` MC cycles of every run (all walkers make N atom
+moves per cycle).  The plain FP64 form is timed on the same batch and reported
+as `plain_fp64`.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload cu55|ne13|npt108|batched]
+  python bench.py --impl reference ...   # the CPU oracle on all host cores
+
+Under torchrun (N>1) every rank runs its own batch on its own GPU (replicas
+only, weak scaling; no collective on the data path), timing is max over ranks.
+"""
+import argparse
+import ctypes
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
+        -56234083.4334278, 288738837.441765]
+CU_EAM = dict(n=8.482, m=4.692, eps=0.0367493 * 0.0370, C=27.561, a=0.25 * 18.8973)
+P_NE = 101325 * 3.398928944382626e-14
+
+
+# --------------------------------------------------------------- workloads
+def cu55_ico():
+    d = json.load(open(os.path.join(ROOT, "tests", "golden", "nn_cu55.json")))
+    return np.array(d["ico55_nm"]) * (d["cu_lattice_nm"] * d["nm_to_bohr"])
+
+
+def sphere_start(N, radius, min_sep, seed):
+    rng = np.random.default_rng(seed)
+    pos = []
+    while len(pos) < N:
+        v = rng.uniform(-radius, radius, 3)
+        if np.linalg.norm(v) < radius and all(np.linalg.norm(v - q) > min_sep for q in pos):
+            pos.append(v)
+    return np.array(pos)
+
+
+def fcc(ncell, a, jitter, seed):
+    rng = np.random.default_rng(seed)
+    basis = [(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)]
+    x = np.array([[(i + b[0]) * a, (j + b[1]) * a, (k + b[2]) * a]
+                  for i in range(ncell) for j in range(ncell) for k in range(ncell) for b in basis])
+    return x + rng.uniform(-jitter, jitter, x.shape) - ncell * a / 2
+
+
+def workload(name):
+    """(description, N list per run, R, T0, T1, potential kind, ensemble, bc, starts fn)."""
+    if name == "cu55":
+        return dict(name="cu55_eam", R=32, T=(200.0, 1000.0), pot="eam", ens="nvt",
+                    bc=("sphere", 14.0), sizes=lambda B: [55] * B,
+                    start=lambda n, k: cu55_ico(), resync=1000, flops_pair=17, mufu_pair=3)
+    if name == "ne13":
+        return dict(name="ne13_eljeven", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
+                    bc=("sphere", 11.0), sizes=lambda B: [13] * B,
+                    start=lambda n, k: sphere_start(13, 8.0, 4.5, 1234 + k), resync=1000,
+                    flops_pair=24, mufu_pair=1)
+    if name == "npt108":
+        return dict(name="ne108_npt", R=32, T=(10.0, 40.0), pot="elj", ens="npt",
+                    bc=("cubic", 25.2), sizes=lambda B: [108] * B,
+                    start=lambda n, k: fcc(3, 8.4, 0.05, 7 + k), resync=1000,
+                    flops_pair=33, mufu_pair=1)
+    if name == "batched":
+        ns = [13, 38, 55, 101, 147]
+
+        def sizes(B):
+            return [ns[k % 5] for k in range(B)]
+        return dict(name="batched_uneven_elj", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
+                    bc=("sphere", None), sizes=sizes,
+                    start=lambda n, k: sphere_start(n, 0.9 * n ** (1 / 3) * 3, 4.3, 500 + k),
+                    resync=1000, flops_pair=24, mufu_pair=1)
+    raise SystemExit("unknown workload " + name)
+
+
+def default_runs(name, n_sm=152):
+    return {"cu55": 2 * n_sm, "ne13": 4 * n_sm, "npt108": n_sm, "batched": 256}[name]
+
+
+# --------------------------------------------------------------- GPU arm
+def make_engine(pk, W, B, precision, cycles_per_launch, seed, device):
+    R = W["R"]
+    sizes = W["sizes"](B)
+    mp_ = pk.MCParams(mc_cycles=10 ** 6, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=sizes[0])
+    temp = pk.TempGrid(W["T"][0], W["T"][1], R)
+    if W["pot"] == "eam":
+        pot = pk.EmbeddedAtomPotential(**CU_EAM)
+    else:
+        pot = pk.ELJPotentialEven(C_NE)
+    ens = pk.NPT(sizes[0], P_NE) if W["ens"] == "npt" else pk.NVT(sizes[0])
+    eng = pk.Engine(mp_, temp, pot, ens, n_runs=B, precision=precision,
+                    resync_every=W["resync"], exch_prob=1.0, seed=seed,
+                    cycles_per_launch=cycles_per_launch, device=device)
+    for r, n in enumerate(sizes):
+        x = W["start"](n, r)
+        if W["bc"][0] == "cubic":
+            bc = pk.CubicBC(W["bc"][1])
+        else:
+            rad = W["bc"][1] if W["bc"][1] else 0.9 * n ** (1 / 3) * 3 + 3.0
+            bc = pk.SphericalBC(rad)
+        eng.set_configs(r, pk.Config(x, bc))
+    eng.init()
+    return eng, sizes
+
+
+def flush_l2(torch, dev):
+    buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    buf.fill_(1.0)
+    torch.cuda.synchronize(dev)
+
+
+class ClockSampler:
+    def __init__(self, out_path, device):
+        self.out_path, self.device, self.proc = out_path, device, None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.out_path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device),
+                                          "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.out_path).read().strip().split("\n") if r]
+        except Exception:
+            return None
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        if not sm:
+            return None
+        mx = max(float(r[2]) for r in rows if len(r) >= 9)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows if len(r) >= 9 for k in range(4)
+                          if r[5 + k].strip() == "Active"})
+        loaded = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def time_steps(torch, eng, steps, cycles, dev):
+    """K timed steps; L2 flushed between steps; device time from the engine's
+    own CUDA events on its stream."""
+    ms = []
+    for _ in range(steps):
+        flush_l2(torch, dev)
+        eng.cycles_nosample(cycles)
+        ms.append(eng.stats()["last_cycles_ms"])
+    return ms
+
+
+def gpu_arm(args, rank, world):
+    import torch
+    import __graft_entry__ as g
+    pk = g.load_package()
+    dev = torch.device("cuda", args.local_rank)
+    torch.cuda.set_device(dev)
+    L = pk._capi.load()
+    W = workload(args.workload)
+    B = args.runs or default_runs(args.workload, torch.cuda.get_device_properties(dev).multi_processor_count)
+    # measured in-situ peaks (FMA/MUFU-bound kernels)
+    f32, f64, mufu = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    pk._capi.check(L.ptmc_measure_peaks(args.local_rank, ctypes.byref(f32), ctypes.byref(f64),
+                                        ctypes.byref(mufu)))
+    res = {}
+    for form in (["fp64", "fp32"] if not args.only_chosen else ["fp32"]):
+        eng, sizes = make_engine(pk, W, B, form, args.cycles, 1234 + 7919 * rank, args.local_rank)
+        for _ in range(args.warmup):
+            eng.cycles_nosample(args.cycles)
+        st0 = eng.stats()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        clk = ClockSampler(os.path.join(args.outdir, "clocks_%s_r%d.csv" % (form, rank)), args.local_rank)
+        with clk:
+            ms = time_steps(torch, eng, args.steps, args.cycles, dev)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        st1 = eng.stats()
+        moves = sum(sizes) * W["R"] * args.cycles * args.steps
+        dev_s = sum(ms) / 1e3
+        if world > 1:
+            t = torch.tensor([dev_s], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            dev_s = float(t.item())
+            m = torch.tensor([float(moves)], device=dev)
+            torch.distributed.all_reduce(m)
+            moves_all = float(m.item())
+        else:
+            moves_all = float(moves)
+        res[form] = dict(value=moves_all / dev_s, ms_per_step=1e3 * dev_s / args.steps, wall=wall,
+                         launches=st1["kernel_launches"] - st0["kernel_launches"],
+                         drift=st1["max_drift"], clocks=clk.summary(), moves=moves,
+                         sizes=sizes)
+        eng.close()
+    # e2e through the public API with host buffers, one engine per step
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        form = "fp32"
+        ts = []
+        h2d = d2h = 0
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            eng, sizes = make_engine(pk, W, B, form, args.cycles, 99 + k, args.local_rank)
+            eng.cycles_nosample(args.cycles)
+            outs = [eng.states(r)["en_tot"] for r in range(B)]
+            eng.close()
+            t1 = time.perf_counter()
+            if k >= args.warmup:
+                ts.append(t1 - t0)
+            h2d = sum(n * 3 * 8 for n in sizes)  # start configurations (one per run)
+            d2h = sum(o.nbytes for o in outs)
+        e2e = dict(value=sum(sizes) * W["R"] * args.cycles / statistics.mean(ts),
+                   unit="atom-moves/s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h)
+    return res, dict(fp32_tflops=f32.value, fp64_tflops=f64.value, mufu_tops=mufu.value), B, e2e
+
+
+# --------------------------------------------------------------- CPU oracle arm
+def _cpu_worker(args_tuple):
+    wname, seed, budget_s, k = args_tuple
+    from oracle import oracle as orc
+    W = workload(wname)
+    n = W["sizes"](k + 1)[k]
+    x = W["start"](n, k)
+    R = W["R"]
+    T, _ = orc.tempgrid(W["T"][0], W["T"][1], R)
+    ens = orc.NPT if W["ens"] == "npt" else orc.NVT
+    bcp = W["bc"][1] if W["bc"][1] else 0.9 * n ** (1 / 3) * 3 + 3.0
+    run = orc.Run(n, R, np.stack([x] * R), T, ensemble=ens, pressure=P_NE,
+                  bc=orc.BC_CUBIC if W["bc"][0] == "cubic" else orc.BC_SPHERE, bc_param=bcp,
+                  exch_prob=1.0, seed=seed)
+    if W["pot"] == "eam":
+        E = CU_EAM
+        ean = E["eps"] * E["a"] ** E["n"] / 2
+        ecam = E["eps"] * E["C"] * E["a"] ** (E["m"] / 2)
+        run.set_eam(E["n"], E["m"], ean, ecam)
+    else:
+        run.set_elj(C_NE, True)
+    run.init()
+    cyc, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        run.cycles(cyc + 1, 1)
+        cyc += 1
+    dt = time.perf_counter() - t0
+    return n * R * cyc, dt, cyc
+
+
+def cpu_baseline(wname, cores, budget_s):
+    from oracle import oracle as orc
+    orc.build()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_cpu_worker, [(wname, 1000 + k, budget_s, k) for k in range(cores)])
+    moves = sum(o[0] for o in out)
+    dt = max(o[1] for o in out)
+    cyc = sum(o[2] for o in out)
+    return moves / dt, cyc
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cu55", choices=["cu55", "ne13", "npt108", "batched"])
+    ap.add_argument("--runs", type=int, default=0, help="independent PT runs batched (0 = fill the GPU)")
+    ap.add_argument("--cycles", type=int, default=200, help="MC cycles per step")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--only-chosen", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    os.makedirs(args.outdir, exist_ok=True)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    args.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    W = workload(args.workload)
+    cores = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        per_step = []
+        for _ in range(args.warmup + args.steps):
+            v, cyc = cpu_baseline(args.workload, cores, max(2.0, args.cpu_seconds / 4))
+            per_step.append(v)
+        v = statistics.mean(per_step[args.warmup:])
+        line = {"metric": "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error",
+                "value": v, "unit": "atom-moves/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": W["name"], "replicas": W["R"]},
+                "cpu_baseline": {"value": v, "unit": "atom-moves/s", "cores": cores, "kind": "port",
+                                 "sample": "each step: %d spawn workers x %.1f s of oracle cycles"
+                                           % (cores, max(2.0, args.cpu_seconds / 4))},
+                "e2e": {"value": v, "unit": "atom-moves/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    # CPU baseline first (spawned workers, before any GPU work in this process)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cyc = cpu_baseline(args.workload, cores, args.cpu_seconds)
+        cpu = {"value": v, "unit": "atom-moves/s", "cores": cores, "kind": "port",
+               "sample": "%d spawn workers, one %s PT run each (R=%d), %.0f s, %d cycles in total"
+                         % (cores, W["name"], W["R"], args.cpu_seconds, cyc)}
+    res, peaks, B, e2e = gpu_arm(args, rank, world)
+    if rank != 0:
+        return
+    ch = res["fp32"]
+    sizes = ch["sizes"]
+    # roofline of the dominant kernel (k_cycles): algorithmic FP32 ops per launch
+    pairs_per_move = [n - 1 for n in sizes]
+    flops_launch = sum((W["flops_pair"] * (n - 1) + 2 * n) * n * W["R"] for n in sizes) * args.cycles
+    per_launch_s = ch["ms_per_step"] / 1e3 / max(1, ch["launches"] // max(1, args.steps))
+    achieved = flops_launch / per_launch_s / 1e12
+    line = {
+        "metric": "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error",
+        "value": ch["value"], "unit": "atom-moves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ch["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": W["name"] + "_fp32resync_batched", "runs_per_gpu": B,
+                   "replicas": W["R"], "atoms": sorted(set(sizes)), "cycles_per_step": args.cycles,
+                   "resync_every": W["resync"], "exchange": "every cycle",
+                   "l2": "flushed between steps (256 MB write)"},
+        "plain_fp64": ({"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
+                        "chosen_over_plain": ch["value"] / res["fp64"]["value"]}
+                       if "fp64" in res else None),
+        "fp32_max_drift_eh": ch["drift"],
+        "roofline": {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
+                     "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"], "traffic": None,
+                     "peak_source": "measured in-situ by ptmc_measure_peaks (FFMA chains)",
+                     "ops_per_pair": W["flops_pair"], "mufu_per_pair": W["mufu_pair"],
+                     "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"]},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": ch["launches"],
+        "clocks": ch["clocks"],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

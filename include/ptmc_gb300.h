@@ -1,0 +1,191 @@
+/*
+ * ptmc_gb300.h — C ABI of the GB300 parallel-tempering Monte Carlo engine.
+ *
+ * One context holds a batch of independent PT runs that share the potential,
+ * the ensemble, the temperature grid and the MC parameters (each run may have
+ * its own atom count and start configurations).  All replica state lives on the
+ * GPU; every entry point takes plain host pointers owned by the caller
+ * (column-major Julia arrays map 1:1: xyz is 3 x N per configuration).  No entry
+ * point keeps a caller pointer after it returns.  Errors are negative return
+ * codes; ptmc_last_error() gives the message.  There is no CPU fallback: every
+ * compute entry point fails with PTMC_ERR_CUDA when no usable GPU is present.
+ *
+ * Each declaration names the reference interface it replaces
+ * (ParallelTemperingMonteCarlo.jl v0.3.5, paths relative to the package root).
+ */
+#ifndef PTMC_GB300_H
+#define PTMC_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTMC_OK 0
+#define PTMC_ERR_ARG -1      /* bad argument (ArgumentError in the reference) */
+#define PTMC_ERR_STATE -2    /* call out of order */
+#define PTMC_ERR_CUDA -3     /* CUDA failure or no GPU */
+#define PTMC_ERR_SPHERE -4   /* "too many moves out of binding sphere" (src/MCMoves.jl:132) */
+#define PTMC_ERR_IO -5       /* checkpoint file error */
+#define PTMC_ERR_LIMIT -6    /* size beyond a documented limit */
+
+/* ensembles: NVT (src/Ensembles.jl:42), NPT (src/Ensembles.jl:75) */
+#define PTMC_NVT 0
+#define PTMC_NPT 1
+/* boundary conditions: SphericalBC (src/BoundaryConditions.jl:44),
+ * CubicBC (src/BoundaryConditions.jl:72) */
+#define PTMC_BC_SPHERE 0
+#define PTMC_BC_CUBIC 1
+/* arithmetic forms */
+#define PTMC_FP64 0          /* plain form: FP64 everywhere */
+#define PTMC_FP32_RESYNC 1   /* FP32 move rows, FP64 running total, FP64 resync */
+/* temperature distributions (src/InputParams.jl:77-95) */
+#define PTMC_TGEOMETRIC 0
+#define PTMC_TLINEAR 1
+
+typedef struct ptmc_ctx ptmc_ctx;
+
+/* MCParams (src/InputParams.jl:35-63) + TempGrid (src/InputParams.jl:77-95)
+ * + ensemble + engine options. */
+typedef struct ptmc_params {
+  int n_runs;         /* independent PT runs batched in one context (>= 1) */
+  int n_traj;         /* replicas per run, MCParams.n_traj (1..32) */
+  long long mc_cycles;/* MCParams.mc_cycles */
+  long long eq_cycles;/* MCParams.eq_cycles (round(eq_percentage*cycles)) */
+  int mc_sample;      /* MCParams.mc_sample */
+  int n_adjust;       /* MCParams.n_adjust */
+  int n_bin;          /* MCParams.n_bin */
+  double min_acc;     /* MCParams.min_acc */
+  double max_acc;     /* MCParams.max_acc */
+  int ensemble;       /* PTMC_NVT or PTMC_NPT */
+  double pressure;    /* NPT.pressure (Eh/bohr^3) */
+  double t_i, t_f;    /* TempGrid end points (K) */
+  int tdistr;         /* PTMC_TGEOMETRIC or PTMC_TLINEAR */
+  double exch_prob;   /* exchange attempt probability per cycle: 0.1 in
+                         src/MCRun.jl:203; 1.0 attempts one exchange every cycle */
+  int precision;      /* PTMC_FP64 or PTMC_FP32_RESYNC */
+  int resync_every;   /* FP32 form: cycles between FP64 recomputes (0 = never) */
+  uint64_t seed;      /* Philox key for every draw stream of this context */
+  int cycles_per_launch; /* cycles fused in one kernel launch (0 = auto) */
+  int device;         /* CUDA device ordinal */
+} ptmc_params;
+
+/* Result bag, Output (src/InputParams.jl:114-176), for one run.  Every array
+ * is caller-allocated with the length given; NULL skips it. */
+typedef struct ptmc_output {
+  double* en_avg;          /* [R]  Output.en_avg */
+  double* heat_cap;        /* [R]  Output.heat_cap (C/kB convention of Sampling.jl:386) */
+  double* count_stat_atom; /* [R]  Output.count_stat_atom */
+  double* count_stat_vol;  /* [R]  accepted volume moves / mc_cycles */
+  double* count_stat_exc;  /* [R]  Output.count_stat_exc */
+  double* max_displ;       /* [2R] per slot: atom, volume step (MCState.max_displ[1:2]) */
+  double* en_histogram;    /* [R*(n_bin+2)]  NVT Output.en_histogram */
+  double* ev_histogram;    /* [R*(n_bin+2)^2] NPT Output.ev_histogram, [slot][e][v] */
+  double hist_params[6];   /* en_min, en_max, v_min, v_max, delta_en_hist, delta_v_hist */
+} ptmc_output;
+
+/* Engine counters for measurement. */
+typedef struct ptmc_stats {
+  long long kernel_launches;   /* kernels launched by this context so far */
+  long long graph_launches;    /* CUDA graph replays */
+  long long atom_moves;        /* attempted atom moves (all replicas, all runs) */
+  long long volume_moves;      /* attempted volume moves */
+  double max_drift;            /* FP32 form: largest |E_running - E_fp64| seen at a resync (Eh) */
+  double last_cycles_ms;       /* device time of the last ptmc_run_cycles / ptmc_equilibrate */
+} ptmc_stats;
+
+/* --- set-up (replaces MCParams/TempGrid/ensemble construction and
+ *     initialisation(), src/Initialization.jl:70-100) --- */
+int ptmc_create(ptmc_ctx** out, const ptmc_params* p);
+/* ELJPotential / ELJPotentialEven (src/EnergyEvaluation.jl:923-942);
+ * c has K <= 16 coefficients for powers 6,7,8,... (even=0) or 6,8,10,... (even=1) */
+int ptmc_set_potential_elj(ptmc_ctx* c, const double* coeff, int K, int even);
+/* EmbeddedAtomPotential(n, m, ean, eCam) (src/EnergyEvaluation.jl:1059-1073) */
+int ptmc_set_potential_eam(ptmc_ctx* c, double n, double m, double ean,
+                           double ecam);
+/* RuNNerPotential (src/EnergyEvaluation.jl:1182-1213) with the per-atom MLP of
+ * MachineLearningPotential/ForwardPass.jl:23-84 (which calls the closed
+ * librunnerjulia.so `forward`).  sf: nsf rows of 8 doubles {kind (0 radial
+ * G2, 1 angular G4), type (11/10 radial, 111/110/100 angular; only 11 and 111
+ * are active for one element, SymmFunc.jl:261,281), eta, lambda, zeta, r_cut,
+ * G_min, G_max}.  weights: per layer W[n_in][n_out] (input-major) then
+ * b[n_out].  nodes: n_layers counts, nodes[0] == nsf, last == 1, hidden tanh.
+ * boundary: hard-core distance (bohr), E = 100 below it
+ * (src/EnergyEvaluation.jl:1602-1606). */
+int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf,
+                          const double* weights, int nw, const int* nodes,
+                          int n_layers, double boundary);
+/* Start configurations of run `run`: n_start configs of N atoms (xyz 3 x N
+ * each, bohr); replica i starts from config (i mod n_start)
+ * (src/Initialization.jl:88-96).  bc_param: sphere radius or cube side. */
+int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N,
+                         int n_start, int bc_kind, double bc_param);
+/* Optional initial step sizes, 2 per slot (atom, volume); default 0.1, 0.1
+ * (src/MCStates.jl:104). */
+int ptmc_set_max_displ(ptmc_ctx* c, int run, const double* max_displ);
+/* Uploads everything and computes the initial energies on the GPU
+ * (MCState constructor, src/MCStates.jl:137-162). */
+int ptmc_init(ptmc_ctx* c);
+
+/* --- the hot loop (replaces equilibration/mc_cycle!/ptmc_run! main loop,
+ *     src/MCRun.jl:192-253, 282-344, 363-432) --- */
+/* equilibration_cycle! (src/MCRun.jl:282-313): eq_cycles/2 cycles, energy
+ * bounds from the final energies, counter reset, histogram set-up
+ * (src/Sampling.jl:141-194). */
+int ptmc_equilibrate(ptmc_ctx* c);
+/* n production cycles (mc_cycle! with sampling_step!, src/MCRun.jl:215-253),
+ * continuing the cycle index where the previous call stopped. */
+int ptmc_run_cycles(ptmc_ctx* c, long long n);
+/* plain cycles without sampling (mc_cycle!, src/MCRun.jl:192-213), advancing
+ * a separate cycle index starting at 1; used for parity tests. */
+int ptmc_cycles_nosample(ptmc_ctx* c, long long n);
+/* FP32 form: recompute every running total in FP64 now. */
+int ptmc_resync(ptmc_ctx* c);
+
+/* --- results (finalise_results, src/Sampling.jl:377-399) --- */
+int ptmc_get_output(ptmc_ctx* c, int run, ptmc_output* out);
+/* Slot-ordered replica state: xyz [R][N][3], en_tot [R], box [R] (cube side
+ * or sphere radius), max_displ [2R], counts [R][6] = count_atom[1:2],
+ * count_vol[1:2], count_exc[1:2] (src/MCStates.jl:33-53), ham [2R]. */
+int ptmc_get_states(ptmc_ctx* c, int run, double* xyz, double* en_tot,
+                    double* box, double* max_displ, long long* counts,
+                    double* ham);
+int ptmc_get_stats(ptmc_ctx* c, ptmc_stats* s);
+
+/* --- checkpoint / resume (src/ReadSave.jl:93-218, 330-481) --- */
+/* Writes the reference's text formats into dir (params.data, hist_info.data,
+ * histograms.data, volume_hist.data, index.txt, configT<i>.xyz) for run 0,
+ * plus engine.bin with the full binary state of every run (exact resume). */
+int ptmc_checkpoint(ptmc_ctx* c, const char* dir);
+/* Restores the full state written by ptmc_checkpoint into a context created
+ * with the same parameters and potential. */
+int ptmc_restore(ptmc_ctx* c, const char* dir);
+
+/* --- multihistogram reweighting on the GPU (FP64 log-sum-exp) --- */
+/* multihistogram_NVT (src/multihist_NVT.jl:95-221): en_hist [R][n_bin+2]
+ * counts, t_grid/beta [R]; T_out/cv_out [10R]; returns iterations in *iters. */
+int ptmc_multihist_nvt(int R, int n_bin, const double* en_hist,
+                       const double* t_grid, const double* beta, double en_min,
+                       double en_max, double thr, double* T_out, double* cv_out,
+                       int* iters);
+/* multihistogram_NPT (src/multihist_NPT.jl:113-338): ev_hist
+ * [R][n_bin+2][n_bin+2]; T_out/cp_out [10R]. */
+int ptmc_multihist_npt(int R, int n_bin, const double* ev_hist,
+                       const double* t_grid, const double* beta, double en_min,
+                       double en_max, double v_min, double v_max,
+                       double pressure, double thr, double* T_out,
+                       double* cp_out, int* iters);
+
+/* Engine utility, no counterpart in the reference: measured FP32 FMA, FP64
+ * FMA (TFLOP/s) and MUFU ex2 (Tops/s) peaks of `device`, the roofline
+ * denominators of the replica-cycle kernels. */
+int ptmc_measure_peaks(int device, double* fp32_tflops, double* fp64_tflops,
+                       double* mufu_tops);
+
+const char* ptmc_last_error(ptmc_ctx* c); /* c may be NULL (global last error) */
+void ptmc_destroy(ptmc_ctx* c);
+const char* ptmc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,263 @@
+"""ctypes binding of the CPU oracle (oracle/ptmc_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: the checker for the GPU engine and the timed CPU
+baseline.  Nothing in the product imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libptmc_oracle.so")
+SRC = os.path.join(HERE, "ptmc_oracle.cpp")
+
+POT_ELJ, POT_ELJEVEN, POT_EAM, POT_NN = 0, 1, 2, 3
+BC_SPHERE, BC_CUBIC = 0, 1
+NVT, NPT = 0, 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+
+def build(force=False):
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "ptmc_oracle.h"))):
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+               "-o", LIB + ".tmp", SRC]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                 ctypes.c_int, ctypes.c_double, _dp, _dp, _dp, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_uint64, ctypes.c_int]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_set_pot_elj.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]
+        L.orc_set_pot_eam.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 4
+        L.orc_set_pot_nn.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, ctypes.c_int,
+                                     _ip, ctypes.c_int, ctypes.c_double]
+        L.orc_init.argtypes = [ctypes.c_void_p]
+        L.orc_equilibrate.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_production.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_long]
+        L.orc_cycles.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_long]
+        L.orc_get_walkers.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc_get_slots.argtypes = [ctypes.c_void_p, _ip, _dp, _lp, _lp, _lp, _dp]
+        L.orc_get_hist.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc_finalise.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_int, _dp, _dp, _dp, _dp]
+        L.orc_get_nn_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+        L.orc_dimer_energy.restype = ctypes.c_double
+        L.orc_dimer_energy.argtypes = [ctypes.c_int, _dp, ctypes.c_int, ctypes.c_double]
+        L.orc_distance2.restype = ctypes.c_double
+        L.orc_distance2.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_double]
+        L.orc_lrc.restype = ctypes.c_double
+        L.orc_lrc.argtypes = [ctypes.c_int, ctypes.c_double, _dp, ctypes.c_int]
+        L.orc_eam_config_energy.restype = ctypes.c_double
+        L.orc_eam_config_energy.argtypes = [_dp, ctypes.c_int] + [ctypes.c_double] * 4
+        L.orc_elj_config_energy.restype = ctypes.c_double
+        L.orc_elj_config_energy.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_tempgrid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp]
+        L.orc_u01.restype = ctypes.c_double
+        L.orc_u01.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]
+        L.orc_philox4x32.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
+        L.orc_mlp_forward.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _ip,
+                                      ctypes.c_int, _dp]
+        L.orc_multihist_nvt.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, _dp, _dp, _ip]
+        L.orc_multihist_npt.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, _dp, _dp, _ip]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def P(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+
+
+def dimer_energy(kind, c, r2):
+    c = _d(c)
+    return lib().orc_dimer_energy(kind, P(c), len(c), float(r2))
+
+
+def distance2(a, b, bc=BC_SPHERE, L=0.0):
+    a, b = _d(a), _d(b)
+    return lib().orc_distance2(P(a), P(b), bc, float(L))
+
+
+def lrc(N, rc2, c):
+    c = _d(c)
+    return lib().orc_lrc(N, float(rc2), P(c), len(c))
+
+
+def eam_config_energy(xyz, n, m, ean, ecam):
+    x = _d(xyz)
+    return lib().orc_eam_config_energy(P(x), len(x), n, m, ean, ecam)
+
+
+def elj_config_energy(xyz, kind, c, bc=BC_SPHERE, L=0.0, rc2=0.0):
+    x, c = _d(xyz), _d(c)
+    return lib().orc_elj_config_energy(P(x), len(x), kind, P(c), len(c), bc, L, rc2)
+
+
+def tempgrid(ti, tf, R, tdistr=0):
+    T, B = np.zeros(R), np.zeros(R)
+    lib().orc_tempgrid(ti, tf, R, tdistr, P(T), P(B))
+    return T, B
+
+
+def u01(seed, stream, run, idx):
+    return lib().orc_u01(seed, stream, run, idx)
+
+
+def philox4x32(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    o = np.zeros(4, dtype=np.uint32)
+    u = ctypes.POINTER(ctypes.c_uint32)
+    lib().orc_philox4x32(c.ctypes.data_as(u), k.ctypes.data_as(u), o.ctypes.data_as(u))
+    return o
+
+
+def mlp_forward(x, weights, nodes):
+    x = _d(x)
+    w = _d(weights)
+    nd = np.ascontiguousarray(nodes, dtype=np.int32)
+    out = np.zeros(x.shape[0])
+    _check(lib().orc_mlp_forward(P(x), x.shape[1], x.shape[0], P(w), len(w),
+                                 nd.ctypes.data_as(_ip), len(nd), P(out)))
+    return out
+
+
+def multihist_nvt(hist, t_grid, beta, en_min, en_max, thr):
+    h = _d(hist)
+    R, nb = h.shape
+    T, cv, it = np.zeros(10 * R), np.zeros(10 * R), ctypes.c_int()
+    _check(lib().orc_multihist_nvt(R, nb - 2, P(h), P(_d(t_grid)), P(_d(beta)), en_min, en_max,
+                                   thr, P(T), P(cv), ctypes.byref(it)))
+    return T, cv, it.value
+
+
+def multihist_npt(hist, t_grid, beta, en_min, en_max, v_min, v_max, p, thr):
+    h = _d(hist)
+    R, nb = h.shape[0], h.shape[1]
+    T, cp, it = np.zeros(10 * R), np.zeros(10 * R), ctypes.c_int()
+    _check(lib().orc_multihist_npt(R, nb - 2, P(h), P(_d(t_grid)), P(_d(beta)), en_min, en_max,
+                                   v_min, v_max, p, thr, P(T), P(cp), ctypes.byref(it)))
+    return T, cp, it.value
+
+
+class Run:
+    """One PT run on the CPU oracle (walker/slot formulation, Philox draws)."""
+
+    def __init__(self, N, R, xyz, T, ensemble=NVT, pressure=0.0, bc=BC_SPHERE, bc_param=10.0,
+                 max_displ=None, n_bin=100, n_adjust=100, mc_sample=1, min_acc=0.4, max_acc=0.6,
+                 exch_prob=0.1, seed=1234, run_index=0):
+        self.N, self.R, self.ens = N, R, ensemble
+        xyz = _d(xyz).reshape(R, N, 3)
+        T = _d(T)
+        md = _d(max_displ if max_displ is not None else np.full(2 * R, 0.1))
+        self.n_bin = n_bin
+        h = lib().orc_create(N, R, ensemble, pressure, bc, bc_param, P(xyz), P(T), P(md), n_bin,
+                             n_adjust, mc_sample, min_acc, max_acc, exch_prob, seed, run_index)
+        if not h:
+            raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def set_elj(self, c, even):
+        c = _d(c)
+        _check(lib().orc_set_pot_elj(self.h, P(c), len(c), int(even)))
+
+    def set_eam(self, n, m, ean, ecam):
+        _check(lib().orc_set_pot_eam(self.h, n, m, ean, ecam))
+
+    def set_nn(self, sf, weights, nodes, boundary=0.0):
+        sf, w = _d(sf), _d(weights)
+        nd = np.ascontiguousarray(nodes, dtype=np.int32)
+        _check(lib().orc_set_pot_nn(self.h, P(sf), sf.shape[0], P(w), len(w),
+                                    nd.ctypes.data_as(_ip), len(nd), boundary))
+
+    def init(self):
+        _check(lib().orc_init(self.h))
+
+    def equilibrate(self, eq):
+        _check(lib().orc_equilibrate(self.h, eq))
+
+    def production(self, first, n):
+        _check(lib().orc_production(self.h, first, n))
+
+    def cycles(self, first, n):
+        _check(lib().orc_cycles(self.h, first, n))
+
+    def walkers(self):
+        x = np.zeros((self.R, self.N, 3))
+        e, b = np.zeros(self.R), np.zeros(self.R)
+        lib().orc_get_walkers(self.h, P(x), P(e), P(b))
+        return x, e, b
+
+    def slots(self):
+        R = self.R
+        wos = np.zeros(R, dtype=np.int32)
+        md = np.zeros(2 * R)
+        ca, cv, ce = (np.zeros(2 * R, dtype=np.int64) for _ in range(3))
+        ham = np.zeros(2 * R)
+        lp = lambda a: a.ctypes.data_as(_lp)
+        lib().orc_get_slots(self.h, wos.ctypes.data_as(_ip), P(md), lp(ca), lp(cv), lp(ce), P(ham))
+        return dict(wos=wos, max_displ=md.reshape(R, 2), count_atom=ca.reshape(R, 2),
+                    count_vol=cv.reshape(R, 2), count_exc=ce.reshape(R, 2), ham=ham.reshape(R, 2))
+
+    def slot_states(self):
+        """(xyz, en, box) in slot order, like the engine's ptmc_get_states."""
+        x, e, b = self.walkers()
+        wos = self.slots()["wos"]
+        return x[wos], e[wos], b[wos]
+
+    def hist(self):
+        nb = self.n_bin + 2
+        eh = np.zeros((self.R, nb))
+        ev = np.zeros((self.R, nb, nb)) if self.ens == NPT else np.zeros(1)
+        hp = np.zeros(6)
+        lib().orc_get_hist(self.h, P(eh), P(ev), P(hp))
+        return eh, ev, hp
+
+    def finalise(self, mc_cycles, mc_sample=1):
+        R = self.R
+        a, b, c, d = (np.zeros(R) for _ in range(4))
+        lib().orc_finalise(self.h, mc_cycles, mc_sample, P(a), P(b), P(c), P(d))
+        return dict(en_avg=a, heat_cap=b, count_stat_atom=c, count_stat_exc=d)
+
+    def nn_state(self, w, nsf):
+        G = np.zeros((nsf, self.N))
+        ea = np.zeros(self.N)
+        _check(lib().orc_get_nn_state(self.h, w, P(G), P(ea)))
+        return G, ea

@@ -1,0 +1,1091 @@
+// ptmc_oracle.cpp — CPU ORACLE (test infrastructure only; see ptmc_oracle.h).
+//
+// A plain FP64 restatement of ParallelTemperingMonteCarlo.jl's hot path.  Every
+// function cites the reference file:line it follows.  Arithmetic keeps the
+// reference's operation order (no fused multiply-add: build with
+// -ffp-contract=off) so that squared distances, proposals and ELJ pair energies
+// are bit-identical to what the reference computes for the same inputs.
+//
+// Walker/slot formulation: the reference swaps whole configurations between
+// temperature-indexed MCState objects on an accepted exchange
+// (src/Exchange.jl:115-124).  Here a "walker" owns the configuration-bound data
+// (positions, distance matrix, energy, potential variables, box, draw stream)
+// and a "slot" owns the temperature-bound data (beta, max_displ, counters,
+// E/E^2 accumulators, histogram row).  An accepted exchange swaps the
+// walker<->slot mapping, which is the same state transition.
+#include "ptmc_oracle.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+int fail(const std::string& m) {
+  g_err = m;
+  return -1;
+}
+
+// ---------------------------------------------------------------- Philox4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3"
+// (SC'11).  Counter = {idx lo, idx hi, stream, run}; key = seed.
+inline void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += W0;
+      k1 += W1;
+    }
+    uint64_t p0 = (uint64_t)M0 * c[0];
+    uint64_t p1 = (uint64_t)M1 * c[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c[1] ^ k0;
+    uint32_t n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+  }
+}
+// Draw k of a stream is half (k & 1) of Philox block k >> 1: half 0 takes 53
+// bits from words (0,1), half 1 from words (2,3).
+inline double u01(uint64_t seed, uint32_t stream, uint32_t run, uint64_t idx) {
+  uint64_t blk = idx >> 1;
+  uint32_t c[4] = {(uint32_t)blk, (uint32_t)(blk >> 32), stream, run};
+  philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  int h = (int)(idx & 1) * 2;
+  uint64_t b = ((uint64_t)c[h] << 21) | (uint64_t)(c[h + 1] >> 11);
+  return (double)b * 0x1.0p-53;
+}
+// rand(1:n) (0-based result): floor(u*n), clamped
+inline int randint(double u, int n) {
+  int k = (int)(u * (double)n);
+  return k >= n ? n - 1 : k;
+}
+
+const double kB = 3.16681196E-6;  // src/InputParams.jl:19
+
+// ---------------------------------------------------------------- distances
+// distance2 (src/Configurations.jl:101-109): (a-b).(a-b) summed left to right
+inline double dot3(double x, double y, double z) {
+  return (x * x + y * y) + z * z;
+}
+inline double dist2_sph(const double* a, const double* b) {
+  return dot3(a[0] - b[0], a[1] - b[1], a[2] - b[2]);
+}
+// cubic minimum image (src/Configurations.jl:103-109)
+inline double dist2_cub(const double* a, const double* b, double L) {
+  double bx = b[0] + L * std::nearbyint((a[0] - b[0]) / L);
+  double by = b[1] + L * std::nearbyint((a[1] - b[1]) / L);
+  double bz = b[2] + L * std::nearbyint((a[2] - b[2]) / L);
+  return dot3(a[0] - bx, a[1] - by, a[2] - bz);
+}
+
+// ---------------------------------------------------------------- potentials
+struct SF {
+  int kind, type;
+  double eta, lambda, zeta, rcut, gnorm, goffset, tpz;
+};
+
+struct Pot {
+  int kind = -1;
+  std::vector<double> c;  // ELJ coefficients
+  double n = 0, m = 0, ean = 0, ecam = 0;
+  // NN
+  std::vector<SF> sf;
+  std::vector<double> w;
+  std::vector<int> nodes;
+  double rcut = 0, boundary2 = 0;
+};
+
+// dimer_energy ELJPotential (EnergyEvaluation.jl:923-932)
+double elj_all(const double* c, int K, double r2) {
+  double r = std::sqrt(r2);
+  double r6inv = 1 / (r2 * r2 * r2);
+  double s = 0.0;
+  for (int i = 0; i < K; ++i) {
+    s += c[i] * r6inv;
+    r6inv /= r;
+  }
+  return s;
+}
+// dimer_energy ELJPotentialEven (EnergyEvaluation.jl:934-942)
+double elj_even(const double* c, int K, double r2) {
+  double r6inv = 1 / (r2 * r2 * r2);
+  double s = 0.0;
+  for (int i = 0; i < K; ++i) {
+    s += c[i] * r6inv;
+    r6inv /= r2;
+  }
+  return s;
+}
+inline double dimer(const Pot& p, double r2) {
+  return p.kind == ORC_POT_ELJ ? elj_all(p.c.data(), (int)p.c.size(), r2)
+                               : elj_even(p.c.data(), (int)p.c.size(), r2);
+}
+// lrc (EnergyEvaluation.jl:968-982); r_cut is the squared cut-off
+double lrc_even(int N, double r_cut, const double* c, int K) {
+  if (r_cut <= 50) return 0.0;
+  double rcs = std::sqrt(r_cut);  // r_cut^0.5, correctly rounded
+  double rc3 = r_cut * rcs;
+  double e = 0.0;
+  for (int i = 1; i <= K; ++i) {
+    e += c[i - 1] / rc3 / (2 * i + 1);
+    rc3 *= r_cut;
+  }
+  e *= M_PI * (double)(N * N) / 4 / (rcs * rcs * rcs);
+  return e;
+}
+// dimer_energy_atom (EnergyEvaluation.jl:313-345): sum over j != i in order
+double dimer_atom(const Pot& p, int i, const double* d2, int N, bool cut,
+                  double rc2) {
+  double s = 0.0;
+  for (int j = 0; j < N; ++j) {
+    if (j == i) continue;
+    if (cut && !(d2[j] <= rc2)) continue;
+    s += dimer(p, d2[j]);
+  }
+  return s;
+}
+// dimer_energy_config (EnergyEvaluation.jl:378-420)
+double dimer_config(const Pot& p, const double* d2, int N, bool cut,
+                    double rc2) {
+  double e = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int j = i + 1; j < N; ++j) {
+      double x = d2[(size_t)i * N + j];
+      if (cut && !(x <= rc2)) continue;
+      e += dimer(p, x);
+    }
+  if (cut) e = e + lrc_even(N, rc2, p.c.data(), (int)p.c.size());
+  return e;
+}
+// invrexp (EnergyEvaluation.jl:1088-1095)
+inline void invrexp(double r2, double n, double m, double& a, double& b) {
+  if (r2 != 0.0) {
+    double rt = 1 / std::sqrt(r2);
+    a = std::pow(rt, n);
+    b = std::pow(rt, m);
+  } else {
+    a = 0.0;
+    b = 0.0;
+  }
+}
+// calc_energies_from_components (EnergyEvaluation.jl:1156-1162)
+double eam_energy(const double* comp, int N, double ean, double ecam) {
+  double e = 0.0;
+  for (int i = 0; i < N; ++i)
+    e += ean * comp[2 * i] - ecam * std::sqrt(comp[2 * i + 1]);
+  return e;
+}
+
+// cutoff_function (MachineLearningPotential/Cutoff.jl:79-90)
+inline double cutoff(double r, double rc) {
+  return r < rc ? 0.5 * (std::cos(M_PI * (r / rc)) + 1) : 0.0;
+}
+// all_angular_measure (Cutoff.jl:48-57): the three cosines of triangle abc
+inline void angles(const double* a, const double* b, const double* c,
+                   double r2ab, double r2ac, double r2bc, double th[3]) {
+  double ab[3], ac[3], bc[3];
+  for (int k = 0; k < 3; ++k) {
+    ab[k] = a[k] - b[k];
+    ac[k] = a[k] - c[k];
+    bc[k] = b[k] - c[k];
+  }
+  double dab = std::sqrt(r2ab), dac = std::sqrt(r2ac), dbc = std::sqrt(r2bc);
+  th[0] = ((ab[0] * ac[0] + ab[1] * ac[1]) + ab[2] * ac[2]) / (dab * dac);
+  th[1] = (((-ab[0]) * bc[0] + (-ab[1]) * bc[1]) + (-ab[2]) * bc[2]) /
+          (dab * dbc);
+  th[2] = (((-ac[0]) * (-bc[0]) + (-ac[1]) * (-bc[1])) + (-ac[2]) * (-bc[2])) /
+          (dac * dbc);
+}
+inline double theta_part(double th, double lam, double zeta) {
+  return std::pow(1 + lam * th, zeta);  // SymmFunc.jl:166
+}
+
+// per-atom MLP forward (ForwardPass.jl:50-84 math: activations
+// linear/tanh/.../linear).  Weight layout (ours): per layer W[n_in][n_out]
+// input-major, then bias[n_out].
+double mlp_atom(const double* x, const double* w, const int* nodes, int nl) {
+  double buf0[256], buf1[256];
+  const double* in = x;
+  double* out = buf0;
+  size_t off = 0;
+  for (int l = 1; l < nl; ++l) {
+    int ni = nodes[l - 1], no = nodes[l];
+    const double* W = w + off;
+    const double* B = w + off + (size_t)ni * no;
+    for (int j = 0; j < no; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < ni; ++i) s += in[i] * W[(size_t)i * no + j];
+      s += B[j];
+      out[j] = (l < nl - 1) ? std::tanh(s) : s;
+    }
+    off += (size_t)ni * no + no;
+    in = out;
+    out = (out == buf0) ? buf1 : buf0;
+  }
+  return in[0];
+}
+
+}  // namespace
+
+// ================================================================ run state
+struct orc_run {
+  int N, R, ens, bc;
+  double pressure, exch_prob, min_acc, max_acc;
+  int n_bin, n_adjust, mc_sample;
+  uint64_t seed;
+  int run_index;
+  Pot pot;
+  // walker-bound
+  std::vector<double> pos;    // R*N*3
+  std::vector<double> d2;     // R*N*N
+  std::vector<double> en;     // R
+  std::vector<double> box;    // R (cubic side)
+  std::vector<double> rcut2;  // R
+  std::vector<double> comp;   // R*N*2 (EAM)
+  std::vector<double> G;      // R*nsf*N (NN, column per atom)
+  std::vector<double> F;      // R*N*N (NN cut-off matrix)
+  std::vector<double> eatom;  // R*N
+  std::vector<uint64_t> ctr;  // R
+  // slot-bound
+  std::vector<double> T, beta, maxd, ham, max_box;  // R, R, 2R, 2R, R
+  std::vector<long> cnt_atom, cnt_vol, cnt_exc;     // 2R each
+  std::vector<int> wos;                             // walker of slot
+  uint64_t run_ctr = 0;
+  // results
+  double en_min = 0, en_max = 0, v_min = 0, v_max = 0, dE = 0, dV = 0;
+  std::vector<double> en_hist, ev_hist;
+  bool inited = false;
+  // scratch
+  std::vector<double> trial_row, new_comp, newG, newF, new_eatom, sc_pos,
+      sc_d2;
+
+  double draw(int w) {
+    return u01(seed, (uint32_t)w, (uint32_t)run_index, ctr[w]++);
+  }
+  double draw_run() {
+    return u01(seed, 0xFFFFFFFFu, (uint32_t)run_index, run_ctr++);
+  }
+  double* P(int w) { return &pos[(size_t)w * N * 3]; }
+  double* D(int w) { return &d2[(size_t)w * N * N]; }
+};
+
+namespace {
+
+int nsf(const orc_run* r) { return (int)r->pot.sf.size(); }
+
+// get_distance2_mat! (Configurations.jl:146-162)
+void build_d2(orc_run* r, int w) {
+  int N = r->N;
+  double* p = r->P(w);
+  double* d = r->D(w);
+  for (int i = 0; i < N; ++i)
+    for (int j = i + 1; j < N; ++j) {
+      double x = r->bc == ORC_BC_CUBIC ? dist2_cub(p + 3 * i, p + 3 * j, r->box[w])
+                                       : dist2_sph(p + 3 * i, p + 3 * j);
+      d[(size_t)i * N + j] = x;
+      d[(size_t)j * N + i] = x;
+    }
+  for (int i = 0; i < N; ++i) d[(size_t)i * N + i] = 0;
+}
+
+// total_symm_calc (SymmFunc.jl:494-510), all angular rows computed (the
+// reference's (Nrad+1):Nang loop bound skips the last Nrad angular rows).
+void nn_full(orc_run* r, int w) {
+  int N = r->N, S = nsf(r);
+  const double* p = r->P(w);
+  const double* d = r->D(w);
+  double* F = &r->F[(size_t)w * N * N];
+  double* G = &r->G[(size_t)w * S * N];
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      F[(size_t)i * N + j] = cutoff(std::sqrt(d[(size_t)i * N + j]), r->pot.rcut);
+  std::fill(G, G + (size_t)S * N, 0.0);
+  for (int s = 0; s < S; ++s) {
+    const SF& f = r->pot.sf[s];
+    double* g = G + (size_t)s * N;
+    if (f.kind == 0) {
+      if (f.type != 11) continue;  // calc_symm_vals! :259-278 -> zeros(N)
+      for (int a = 0; a < N; ++a)
+        for (int b = a + 1; b < N; ++b) {
+          double fc = F[(size_t)a * N + b];
+          double gv = (fc != 0.0 && fc != 1.0)
+                          ? fc * std::exp(-f.eta * d[(size_t)a * N + b]) * f.gnorm
+                          : 0.0;  // calc_one_symm_val :234
+          g[a] += gv;
+          g[b] += gv;
+        }
+    } else {
+      if (f.type != 111) continue;  // :280-312
+      for (int a = 0; a < N; ++a)
+        for (int b = a + 1; b < N; ++b)
+          for (int c = b + 1; c < N; ++c) {
+            double rab = d[(size_t)a * N + b], rac = d[(size_t)a * N + c],
+                   rbc = d[(size_t)b * N + c];
+            double th[3];
+            angles(p + 3 * a, p + 3 * b, p + 3 * c, rab, rac, rbc, th);
+            double ex = std::exp(-f.eta * (rab + rac + rbc)) *
+                        F[(size_t)a * N + b] * F[(size_t)a * N + c] *
+                        F[(size_t)b * N + c];
+            g[a] += ex * theta_part(th[0], f.lambda, f.zeta) * f.tpz;
+            g[b] += ex * theta_part(th[1], f.lambda, f.zeta) * f.tpz;
+            g[c] += ex * theta_part(th[2], f.lambda, f.zeta) * f.tpz;
+          }
+    }
+    for (int a = 0; a < N; ++a) g[a] = g[a] + f.goffset;
+  }
+}
+
+double nn_energy(orc_run* r, const double* G, double* eatom) {
+  int N = r->N, S = nsf(r);
+  std::vector<double> x(S);
+  double e = 0.0;
+  for (int a = 0; a < N; ++a) {
+    for (int s = 0; s < S; ++s) x[s] = G[(size_t)s * N + a];
+    eatom[a] = mlp_atom(x.data(), r->pot.w.data(), r->pot.nodes.data(),
+                        (int)r->pot.nodes.size());
+    e += eatom[a];
+  }
+  return e;
+}
+
+// initialise_energy (EnergyEvaluation.jl:1662-1747) for walker w
+double init_energy(orc_run* r, int w) {
+  int N = r->N;
+  const Pot& p = r->pot;
+  if (p.kind == ORC_POT_EAM) {
+    double* comp = &r->comp[(size_t)w * N * 2];
+    const double* d = r->D(w);
+    for (int i = 0; i < N; ++i) {  // set_variables :1800-1810
+      double a = 0, b = 0;
+      for (int j = 0; j < N; ++j) {
+        double x, y;
+        invrexp(d[(size_t)i * N + j], p.n, p.m, x, y);
+        a += x;
+        b += y;
+      }
+      comp[2 * i] = a;
+      comp[2 * i + 1] = b;
+    }
+    return eam_energy(comp, N, p.ean, p.ecam);
+  }
+  if (p.kind == ORC_POT_NN) {
+    nn_full(r, w);
+    return nn_energy(r, &r->G[(size_t)w * nsf(r) * N], &r->eatom[(size_t)w * N]);
+  }
+  bool cut = r->ens == ORC_NPT;
+  return dimer_config(p, r->D(w), N, cut, r->rcut2[w]);
+}
+
+// ---------------------------------------------------------------- moves
+// atom move: mc_move! (MCRun.jl:142-162) with index < N
+int atom_move(orc_run* r, int w, int slot, int i) {
+  int N = r->N;
+  double md = r->maxd[2 * slot];
+  double* p = r->P(w);
+  double* xi = p + 3 * i;
+  double t[3];
+  // atom_displacement (MCMoves.jl:33-64, 100-143)
+  auto propose = [&]() {
+    double dx = (r->draw(w) - 0.5) * md;
+    double dy = (r->draw(w) - 0.5) * md;
+    double dz = (r->draw(w) - 0.5) * md;
+    t[0] = xi[0] + dx;
+    t[1] = xi[1] + dy;
+    t[2] = xi[2] + dz;
+  };
+  propose();
+  if (r->bc == ORC_BC_SPHERE) {
+    double R2 = r->box[w] * r->box[w];  // SphericalBC stores radius^2
+    int count = 0;
+    while (dot3(t[0], t[1], t[2]) > R2) {
+      ++count;
+      if (count == 50) {  // recentre!(config) (Configurations.jl:79-85)
+        double cx = 0, cy = 0, cz = 0;
+        for (int a = 0; a < N; ++a) {
+          cx += p[3 * a];
+          cy += p[3 * a + 1];
+          cz += p[3 * a + 2];
+        }
+        cx /= N;
+        cy /= N;
+        cz /= N;
+        for (int a = 0; a < N; ++a) {
+          p[3 * a] -= cx;
+          p[3 * a + 1] -= cy;
+          p[3 * a + 2] -= cz;
+        }
+      } else {
+        propose();
+        if (count == 100) return fail("Error: too many moves out of binding sphere");
+      }
+    }
+  } else {
+    double L = r->box[w];
+    for (int k = 0; k < 3; ++k) t[k] -= L * std::nearbyint(t[k] / L);
+  }
+  double* row = r->trial_row.data();
+  for (int j = 0; j < N; ++j)
+    row[j] = r->bc == ORC_BC_CUBIC ? dist2_cub(t, p + 3 * j, r->box[w])
+                                   : dist2_sph(t, p + 3 * j);
+  row[i] = 0.0;
+  const double* old = r->D(w) + (size_t)i * N;
+  const Pot& pot = r->pot;
+  double new_en;
+  bool hard = false;
+  if (pot.kind == ORC_POT_EAM) {  // energy_update! EAM (:1567-1591)
+    int S2 = 2 * N;
+    double* nc = r->new_comp.data();
+    std::memcpy(nc, &r->comp[(size_t)w * S2], sizeof(double) * S2);
+    for (int j = 0; j < N; ++j) {  // calc_components :1129-1148
+      double a1, b1, a0, b0;
+      invrexp(row[j], pot.n, pot.m, a1, b1);
+      invrexp(old[j], pot.n, pot.m, a0, b0);
+      double ja = a1 - a0, jb = b1 - b0;
+      nc[2 * j] += ja;
+      nc[2 * j + 1] += jb;
+      nc[2 * i] += ja;
+      nc[2 * i + 1] += jb;
+    }
+    new_en = eam_energy(nc, N, pot.ean, pot.ecam);
+  } else if (pot.kind == ORC_POT_NN) {  // energy_update! RuNNer (:1593-1621)
+    for (int j = 0; j < N; ++j)
+      if (j != i && row[j] < pot.boundary2) hard = true;
+    if (hard) {
+      new_en = 100.0;
+    } else {
+      int S = nsf(r);
+      double* nF = r->newF.data();
+      for (int j = 0; j < N; ++j) nF[j] = cutoff(std::sqrt(row[j]), pot.rcut);
+      double* nG = r->newG.data();
+      std::memcpy(nG, &r->G[(size_t)w * S * N], sizeof(double) * S * N);
+      const double* F = &r->F[(size_t)w * N * N];
+      const double* d = r->D(w);
+      for (int s = 0; s < S; ++s) {  // total_thr_symm! (DeltaMatrix.jl:933)
+        const SF& f = pot.sf[s];
+        double* g = nG + (size_t)s * N;
+        if (f.kind == 0) {
+          if (f.type != 11) continue;  // radial_symmetry_calculation! :794
+          for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            double gn = std::exp(-f.eta * row[j]) * (nF[j] * f.gnorm);
+            double go = std::exp(-f.eta * old[j]) * ((-F[(size_t)i * N + j]) * f.gnorm);
+            g[i] = g[i] + gn;
+            g[j] = g[j] + gn;
+            g[i] = g[i] + go;
+            g[j] = g[j] + go;
+          }
+        } else {
+          if (f.type != 111) continue;  // angular_symmetry_calculation! :827
+          for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            for (int k = j + 1; k < N; ++k) {
+              if (k == i) continue;
+              double rjk = d[(size_t)j * N + k];
+              double tn[3], to[3];
+              angles(t, p + 3 * j, p + 3 * k, row[j], row[k], rjk, tn);
+              angles(p + 3 * i, p + 3 * j, p + 3 * k, old[j], old[k], rjk, to);
+              double en_ = std::exp(-f.eta * (row[j] + row[k] + rjk)) * nF[j] *
+                           nF[k] * F[(size_t)j * N + k];
+              double eo_ = std::exp(-f.eta * (old[j] + old[k] + rjk)) *
+                           F[(size_t)i * N + j] * F[(size_t)i * N + k] *
+                           F[(size_t)j * N + k];
+              int idx[3] = {i, j, k};
+              for (int q = 0; q < 3; ++q) {
+                double vo = theta_part(to[q], f.lambda, f.zeta);
+                double vn = theta_part(tn[q], f.lambda, f.zeta);
+                double gv = g[idx[q]];
+                gv += en_ * vn * f.tpz;
+                gv -= eo_ * vo * f.tpz;
+                g[idx[q]] = gv;
+              }
+            }
+          }
+        }
+      }
+      new_en = nn_energy(r, nG, r->new_eatom.data());
+    }
+  } else {  // dimer_energy_update! (:804-821)
+    bool cut = r->ens == ORC_NPT;
+    double rc2 = r->rcut2[w];
+    double dE = dimer_atom(pot, i, row, N, cut, rc2) - dimer_atom(pot, i, old, N, cut, rc2);
+    new_en = dE + r->en[w];
+  }
+  // acc_test! (MCRun.jl:122-132), metropolis_condition (Exchange.jl:53-57)
+  double prob = std::exp(-(new_en - r->en[w]) * r->beta[slot]);
+  if (prob > 1) prob = 1.0;
+  double u = r->draw(w);
+  if (prob >= u) {  // swap_atom_config! (swap_config.jl:40-51)
+    xi[0] = t[0];
+    xi[1] = t[1];
+    xi[2] = t[2];
+    double* d = r->D(w);
+    for (int j = 0; j < N; ++j) {
+      d[(size_t)i * N + j] = row[j];
+      d[(size_t)j * N + i] = row[j];
+    }
+    r->en[w] = new_en;
+    r->cnt_atom[2 * slot] += 1;
+    r->cnt_atom[2 * slot + 1] += 1;
+    if (pot.kind == ORC_POT_EAM) {  // swap_vars! EAM (:208-211)
+      std::memcpy(&r->comp[(size_t)w * N * 2], r->new_comp.data(), sizeof(double) * 2 * N);
+    } else if (pot.kind == ORC_POT_NN && !hard) {  // swap_vars! NNP (:213-221)
+      int S = nsf(r);
+      std::memcpy(&r->G[(size_t)w * S * N], r->newG.data(), sizeof(double) * S * N);
+      std::memcpy(&r->eatom[(size_t)w * N], r->new_eatom.data(), sizeof(double) * N);
+      double* F = &r->F[(size_t)w * N * N];
+      for (int j = 0; j < N; ++j) {
+        F[(size_t)i * N + j] = r->newF[j];
+        F[(size_t)j * N + i] = r->newF[j];
+      }
+    }
+  }
+  return 0;
+}
+
+// volume move: volume_change_uniform (MCMoves.jl:277-287) with the NPT
+// energy (MCRun.jl:76-85) and metropolis_condition NPT (Exchange.jl:58-70)
+int volume_move(orc_run* r, int w, int slot) {
+  int N = r->N;
+  double L = r->box[w];
+  double u = r->draw(w);
+  double scale = std::pow(std::exp((u - 0.5) * r->maxd[2 * slot + 1]), 1.0 / 3.0);
+  if (L >= r->max_box[slot] && scale > 1.0) scale = 1.0;
+  double Ln = scale * L;
+  double rc_new = Ln * Ln / 4;
+  double s2 = scale * scale;
+  std::vector<double>& nd = r->sc_d2;
+  const double* d = r->D(w);
+  for (size_t k = 0; k < (size_t)N * N; ++k) nd[k] = d[k] * s2;
+  double new_en = dimer_config(r->pot, nd.data(), N, true, rc_new);
+  double Vn = Ln * Ln * Ln, Vo = L * L * L;
+  double dh = (new_en - r->en[w]) + r->pressure * (Vn - Vo);
+  double prob = std::exp(-dh * r->beta[slot] + (double)N * std::log(Vn / Vo));
+  if (prob > 1) prob = 1.0;
+  double ua = r->draw(w);
+  if (prob >= ua) {  // swap_config_v! (swap_config.jl:113-141)
+    double* p = r->P(w);
+    for (int k = 0; k < 3 * N; ++k) p[k] = scale * p[k];
+    r->box[w] = Ln;
+    std::memcpy(r->D(w), nd.data(), sizeof(double) * N * N);
+    r->en[w] = new_en;
+    r->cnt_vol[2 * slot] += 1;
+    r->cnt_vol[2 * slot + 1] += 1;
+    r->rcut2[w] = rc_new;
+  }
+  return 0;
+}
+
+// mc_cycle! (MCRun.jl:192-213)
+int cycle(orc_run* r, long index) {
+  int R = r->R, N = r->N;
+  int n_steps = r->ens == ORC_NPT ? N + 1 : N;
+  for (int s = 0; s < R; ++s) {  // mc_step! over states
+    int w = r->wos[s];
+    for (int k = 0; k < n_steps; ++k) {
+      int idx = randint(r->draw(w), n_steps);
+      int rc = idx < N ? atom_move(r, w, s, idx) : volume_move(r, w, s);
+      if (rc) return rc;
+    }
+  }
+  // parallel_tempering_exchange! (Exchange.jl:132-180)
+  if (R > 1 && r->draw_run() < r->exch_prob) {
+    int k = randint(r->draw_run(), R - 1);
+    r->cnt_exc[2 * k] += 1;
+    r->cnt_exc[2 * (k + 1)] += 1;
+    int w1 = r->wos[k], w2 = r->wos[k + 1];
+    double e1 = r->en[w1], e2 = r->en[w2];
+    if (r->ens == ORC_NPT) {
+      double L1 = r->box[w1], L2 = r->box[w2];
+      e1 = e1 + r->pressure * (L1 * L1 * L1);
+      e2 = e2 + r->pressure * (L2 * L2 * L2);
+    }
+    double acc = std::exp((r->beta[k] - r->beta[k + 1]) * (e1 - e2));
+    if (acc > 1.0) acc = 1.0;
+    if (acc > r->draw_run()) {
+      r->cnt_exc[2 * k + 1] += 1;
+      r->cnt_exc[2 * (k + 1) + 1] += 1;
+      r->wos[k] = w2;
+      r->wos[k + 1] = w1;
+    }
+  }
+  // update_max_stepsize! (Exchange.jl:198-257)
+  if (index % r->n_adjust == 0) {
+    for (int s = 0; s < R; ++s) {
+      double acc = (double)r->cnt_atom[2 * s + 1] / (double)(r->n_adjust * N);
+      if (acc < r->min_acc) r->maxd[2 * s] *= 0.9;
+      else if (acc > r->max_acc) r->maxd[2 * s] *= 1.1;
+      r->cnt_atom[2 * s + 1] = 0;
+      if (r->ens == ORC_NPT) {
+        double av = (double)r->cnt_vol[2 * s + 1] / (double)(r->n_adjust * 1);
+        if (av < r->min_acc) r->maxd[2 * s + 1] *= 0.9;
+        else if (av > r->max_acc) r->maxd[2 * s + 1] *= 1.1;
+        r->cnt_vol[2 * s + 1] = 0;
+      }
+    }
+  }
+  return 0;
+}
+
+// find_hist_index (Sampling.jl:53-62)
+inline long hist_index(double h, int n_bin) {
+  if (h < 1) return 1;
+  if (h > n_bin) return n_bin + 2;
+  return (long)std::floor(h) + 1;
+}
+
+// sampling_step! (Sampling.jl:330-371)
+void sample(orc_run* r) {
+  int R = r->R, nb = r->n_bin + 2;
+  for (int s = 0; s < R; ++s) {
+    int w = r->wos[s];
+    double e = r->en[w];
+    if (r->ens == ORC_NPT) {
+      double L = r->box[w];
+      double H = e + r->pressure * (L * L * L);  // update_energy_tot :35-46
+      r->ham[2 * s] += H;
+      r->ham[2 * s + 1] += H * H;
+      double he = std::floor((e - r->en_min) / r->dE) + 1;  // :98-110
+      double hv = std::floor((L * L * L - r->v_min) / r->dV) + 1;
+      long ie = hist_index(he, r->n_bin), iv = hist_index(hv, r->n_bin);
+      r->ev_hist[((size_t)s * nb + (ie - 1)) * nb + (iv - 1)] += 1;
+    } else {
+      r->ham[2 * s] += e;
+      r->ham[2 * s + 1] += e * e;
+      long ie = hist_index((e - r->en_min) / r->dE + 1, r->n_bin);
+      r->en_hist[(size_t)s * nb + (ie - 1)] += 1;
+    }
+  }
+}
+
+}  // namespace
+
+// ================================================================ C API
+extern "C" {
+
+const char* orc_last_error(void) { return g_err.c_str(); }
+
+double orc_u01(uint64_t seed, uint32_t stream, uint32_t run, uint64_t idx) {
+  return u01(seed, stream, run, idx);
+}
+void orc_philox4x32(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox(c, key[0], key[1]);
+  for (int k = 0; k < 4; ++k) out[k] = c[k];
+}
+
+orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
+                    double bc_param, const double* xyz, const double* T,
+                    const double* max_displ, int n_bin, int n_adjust,
+                    int mc_sample, double min_acc, double max_acc,
+                    double exch_prob, uint64_t seed, int run_index) {
+  if (N < 2 || R < 1) {
+    fail("orc_create: need N >= 2 and R >= 1");
+    return nullptr;
+  }
+  if (ensemble == ORC_NPT && bc_kind != ORC_BC_CUBIC) {
+    fail("SphericalBC cannot be used in an NPT ensemble.");  // Ensembles.jl:192
+    return nullptr;
+  }
+  orc_run* r = new orc_run();
+  r->N = N;
+  r->R = R;
+  r->ens = ensemble;
+  r->bc = bc_kind;
+  r->pressure = pressure;
+  r->exch_prob = exch_prob;
+  r->min_acc = min_acc;
+  r->max_acc = max_acc;
+  r->n_bin = n_bin;
+  r->n_adjust = n_adjust;
+  r->mc_sample = mc_sample;
+  r->seed = seed;
+  r->run_index = run_index;
+  r->pos.assign(xyz, xyz + (size_t)R * N * 3);
+  r->d2.assign((size_t)R * N * N, 0.0);
+  r->en.assign(R, 0.0);
+  r->box.assign(R, bc_param);
+  r->rcut2.assign(R, bc_kind == ORC_BC_CUBIC ? bc_param * bc_param / 4 : 0.0);
+  r->ctr.assign(R, 0);
+  r->T.assign(T, T + R);
+  r->beta.resize(R);
+  for (int s = 0; s < R; ++s) r->beta[s] = 1.0 / (kB * T[s]);  // InputParams.jl:93
+  r->maxd.assign(max_displ, max_displ + 2 * R);
+  r->max_box.assign(R, bc_param * 1.8);  // max_length (MCStates.jl:66-75)
+  r->ham.assign(2 * R, 0.0);
+  r->cnt_atom.assign(2 * R, 0);
+  r->cnt_vol.assign(2 * R, 0);
+  r->cnt_exc.assign(2 * R, 0);
+  r->wos.resize(R);
+  for (int s = 0; s < R; ++s) r->wos[s] = s;
+  r->trial_row.resize(N);
+  r->new_comp.resize(2 * N);
+  r->sc_d2.resize((size_t)N * N);
+  r->newF.resize(N);
+  r->new_eatom.resize(N);
+  return r;
+}
+
+void orc_destroy(orc_run* r) { delete r; }
+
+int orc_set_pot_elj(orc_run* r, const double* c, int K, int even) {
+  if (K < 1) return fail("ELJ needs at least one coefficient");
+  r->pot.kind = even ? ORC_POT_ELJEVEN : ORC_POT_ELJ;
+  r->pot.c.assign(c, c + K);
+  if (r->ens == ORC_NPT && !even)
+    return fail("NPT long-range correction is defined for ELJPotentialEven only");
+  return 0;
+}
+int orc_set_pot_eam(orc_run* r, double n, double m, double ean, double ecam) {
+  if (r->ens == ORC_NPT) return fail("EAM is supported in the NVT ensemble only");
+  r->pot.kind = ORC_POT_EAM;
+  r->pot.n = n;
+  r->pot.m = m;
+  r->pot.ean = ean;
+  r->pot.ecam = ecam;
+  return 0;
+}
+int orc_set_pot_nn(orc_run* r, const double* sf, int nsf_, const double* weights,
+                   int nw, const int* nodes, int n_layers, double boundary) {
+  if (r->ens == ORC_NPT) return fail("NN potential is supported in the NVT ensemble only");
+  if (n_layers < 2 || nodes[0] != nsf_ || nodes[n_layers - 1] != 1)
+    return fail("NN: node counts must start at the number of symmetry functions and end at 1");
+  long need = 0;
+  for (int l = 1; l < n_layers; ++l) need += (long)nodes[l - 1] * nodes[l] + nodes[l];
+  if (need != nw) return fail("NN: weight count does not match the layer sizes");
+  for (int l = 0; l < n_layers; ++l)
+    if (nodes[l] > 256) return fail("NN: layers wider than 256 are not supported");
+  r->pot.kind = ORC_POT_NN;
+  r->pot.sf.clear();
+  for (int s = 0; s < nsf_; ++s) {
+    const double* q = sf + 8 * s;
+    SF f;
+    f.kind = (int)q[0];
+    f.type = (int)q[1];
+    f.eta = q[2];
+    f.lambda = q[3];
+    f.zeta = q[4];
+    f.rcut = q[5];
+    double gmin = q[6], gmax = q[7];
+    // RadialType2 / AngularType3 with G_vals = [max, min] (SymmFunc.jl:37-44,104-112)
+    f.gnorm = 1 / (gmax - gmin);
+    f.goffset = -gmin * f.gnorm;
+    f.tpz = std::pow(2.0, 1 - f.zeta) * f.gnorm;
+    r->pot.sf.push_back(f);
+  }
+  r->pot.rcut = r->pot.sf.empty() ? 0.0 : r->pot.sf[0].rcut;
+  r->pot.w.assign(weights, weights + nw);
+  r->pot.nodes.assign(nodes, nodes + n_layers);
+  r->pot.boundary2 = boundary * boundary;
+  r->G.assign((size_t)r->R * nsf_ * r->N, 0.0);
+  r->F.assign((size_t)r->R * r->N * r->N, 0.0);
+  r->eatom.assign((size_t)r->R * r->N, 0.0);
+  r->newG.resize((size_t)nsf_ * r->N);
+  return 0;
+}
+
+int orc_init(orc_run* r) {
+  if (r->pot.kind < 0) return fail("no potential set");
+  if (r->pot.kind == ORC_POT_EAM) r->comp.assign((size_t)r->R * r->N * 2, 0.0);
+  for (int w = 0; w < r->R; ++w) {
+    build_d2(r, w);
+    r->en[w] = init_energy(r, w);
+  }
+  r->inited = true;
+  return 0;
+}
+
+int orc_cycles(orc_run* r, long first, long n) {
+  if (!r->inited) return fail("orc_init not called");
+  for (long i = first; i < first + n; ++i) {
+    int rc = cycle(r, i);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int orc_equilibrate(orc_run* r, int eq_cycles) {
+  if (!r->inited) return fail("orc_init not called");
+  for (long i = 1; i <= eq_cycles / 2; ++i) {
+    int rc = cycle(r, i);
+    if (rc) return rc;
+  }
+  double eb[2] = {100.0, -100.0};  // check_e_bounds (MCRun.jl:258-265)
+  for (long i = eq_cycles / 2 + 1; i <= eq_cycles; ++i)
+    for (int s = 0; s < r->R; ++s) {
+      double e = r->en[r->wos[s]];
+      if (e < eb[0]) eb[0] = e;
+      else if (e > eb[1]) eb[1] = e;
+    }
+  for (int k = 0; k < 2 * r->R; ++k) {  // reset_counters (MCRun.jl:271-277)
+    r->cnt_atom[k] = 0;
+    r->cnt_vol[k] = 0;
+    r->cnt_exc[k] = 0;
+  }
+  // initialise_histograms! (Sampling.jl:141-194)
+  r->en_min = eb[0];
+  r->en_max = eb[1];
+  r->dE = (r->en_max - r->en_min) / (r->n_bin - 1);
+  int nb = r->n_bin + 2;
+  r->en_hist.assign((size_t)r->R * nb, 0.0);
+  if (r->ens == ORC_NPT) {
+    double L = r->box[r->wos[0]];
+    double V = L * L * L;
+    r->v_min = V * 0.8;
+    r->v_max = V * 2.0;
+    r->dV = (r->v_max - r->v_min) / r->n_bin;
+    r->ev_hist.assign((size_t)r->R * nb * nb, 0.0);
+  }
+  return 0;
+}
+
+int orc_production(orc_run* r, long first, long n) {
+  if (r->en_hist.empty()) return fail("orc_equilibrate not called");
+  for (long i = first; i < first + n; ++i) {
+    int rc = cycle(r, i);
+    if (rc) return rc;
+    if (i % r->mc_sample == 0) sample(r);
+  }
+  return 0;
+}
+
+int orc_get_walkers(orc_run* r, double* xyz, double* en_tot, double* box) {
+  if (xyz) std::memcpy(xyz, r->pos.data(), sizeof(double) * r->pos.size());
+  if (en_tot) std::memcpy(en_tot, r->en.data(), sizeof(double) * r->R);
+  if (box) std::memcpy(box, r->box.data(), sizeof(double) * r->R);
+  return 0;
+}
+
+int orc_get_slots(orc_run* r, int* wos, double* max_displ, long* ca, long* cv,
+                  long* ce, double* ham) {
+  int R = r->R;
+  if (wos) std::memcpy(wos, r->wos.data(), sizeof(int) * R);
+  if (max_displ) std::memcpy(max_displ, r->maxd.data(), sizeof(double) * 2 * R);
+  if (ca) std::memcpy(ca, r->cnt_atom.data(), sizeof(long) * 2 * R);
+  if (cv) std::memcpy(cv, r->cnt_vol.data(), sizeof(long) * 2 * R);
+  if (ce) std::memcpy(ce, r->cnt_exc.data(), sizeof(long) * 2 * R);
+  if (ham) std::memcpy(ham, r->ham.data(), sizeof(double) * 2 * R);
+  return 0;
+}
+
+int orc_get_hist(orc_run* r, double* en_hist, double* ev_hist, double* hp) {
+  if (en_hist && !r->en_hist.empty() && r->ens == ORC_NVT)
+    std::memcpy(en_hist, r->en_hist.data(), sizeof(double) * r->en_hist.size());
+  if (ev_hist && !r->ev_hist.empty())
+    std::memcpy(ev_hist, r->ev_hist.data(), sizeof(double) * r->ev_hist.size());
+  if (hp) {
+    hp[0] = r->en_min;
+    hp[1] = r->en_max;
+    hp[2] = r->v_min;
+    hp[3] = r->v_max;
+    hp[4] = r->dE;
+    hp[5] = r->dV;
+  }
+  return 0;
+}
+
+int orc_finalise(orc_run* r, long mc_cycles, int mc_sample, double* en_avg,
+                 double* heat_cap, double* stat_atom, double* stat_exc) {
+  double n_sample = (double)mc_cycles / (double)mc_sample;
+  for (int s = 0; s < r->R; ++s) {
+    double ea = r->ham[2 * s] / n_sample;
+    double e2 = r->ham[2 * s + 1] / n_sample;
+    if (en_avg) en_avg[s] = ea;
+    if (heat_cap) heat_cap[s] = (e2 - ea * ea) * (r->beta[s] * r->beta[s]);
+    if (stat_atom) stat_atom[s] = (double)r->cnt_atom[2 * s] / (double)((long)r->N * mc_cycles);
+    if (stat_exc) stat_exc[s] = (double)r->cnt_exc[2 * s + 1] / (double)r->cnt_exc[2 * s];
+  }
+  return 0;
+}
+
+int orc_get_nn_state(orc_run* r, int w, double* G, double* eatom) {
+  if (r->pot.kind != ORC_POT_NN) return fail("not an NN run");
+  int S = nsf(r), N = r->N;
+  if (G) std::memcpy(G, &r->G[(size_t)w * S * N], sizeof(double) * S * N);
+  if (eatom) std::memcpy(eatom, &r->eatom[(size_t)w * N], sizeof(double) * N);
+  return 0;
+}
+
+double orc_dimer_energy(int kind, const double* c, int K, double r2) {
+  return kind == ORC_POT_ELJ ? elj_all(c, K, r2) : elj_even(c, K, r2);
+}
+double orc_distance2(const double* a, const double* b, int bc_kind, double L) {
+  return bc_kind == ORC_BC_CUBIC ? dist2_cub(a, b, L) : dist2_sph(a, b);
+}
+double orc_lrc(int N, double r_cut2, const double* c, int K) {
+  return lrc_even(N, r_cut2, c, K);
+}
+double orc_eam_config_energy(const double* xyz, int N, double n, double m,
+                             double ean, double ecam) {
+  std::vector<double> comp(2 * N, 0.0);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      double a, b;
+      invrexp(i == j ? 0.0 : dist2_sph(xyz + 3 * i, xyz + 3 * j), n, m, a, b);
+      comp[2 * i] += a;
+      comp[2 * i + 1] += b;
+    }
+  return eam_energy(comp.data(), N, ean, ecam);
+}
+double orc_elj_config_energy(const double* xyz, int N, int kind,
+                             const double* c, int K, int bc_kind, double L,
+                             double r_cut2) {
+  Pot p;
+  p.kind = kind;
+  p.c.assign(c, c + K);
+  std::vector<double> d((size_t)N * N, 0.0);
+  for (int i = 0; i < N; ++i)
+    for (int j = i + 1; j < N; ++j) {
+      double x = bc_kind == ORC_BC_CUBIC ? dist2_cub(xyz + 3 * i, xyz + 3 * j, L)
+                                         : dist2_sph(xyz + 3 * i, xyz + 3 * j);
+      d[(size_t)i * N + j] = d[(size_t)j * N + i] = x;
+    }
+  return dimer_config(p, d.data(), N, bc_kind == ORC_BC_CUBIC, r_cut2);
+}
+void orc_tempgrid(double ti, double tf, int R, int tdistr, double* T, double* beta) {
+  // TempGrid (InputParams.jl:77-95)
+  for (int i = 0; i < R; ++i) {
+    if (tdistr == 1) T[i] = ti + i * ((tf - ti) / (R - 1));
+    else T[i] = ti * std::pow(tf / ti, (double)i / (double)(R - 1));
+    beta[i] = 1.0 / (kB * T[i]);
+  }
+}
+int orc_mlp_forward(const double* input, int n_in, int batch,
+                    const double* weights, int nw, const int* nodes,
+                    int n_layers, double* eatom) {
+  (void)nw;
+  if (nodes[0] != n_in) return fail("input width mismatch");
+  for (int b = 0; b < batch; ++b)
+    eatom[b] = mlp_atom(input + (size_t)b * n_in, weights, nodes, n_layers);
+  return 0;
+}
+
+// ---------------------------------------------------------------- WHAM NVT
+// multihistogram_NVT (multihist_NVT.jl:11-221), restated literally.
+int orc_multihist_nvt(int R, int n_bin, const double* H, const double* t_grid,
+                      const double* beta, double en_min, double en_max,
+                      double thr, double* T_out, double* cv_out, int* iters) {
+  const double k = 3.166811429 / 1e6;  // :18
+  int nb = n_bin + 2;
+  double dE = (en_max - en_min) / n_bin;  // :24
+  std::vector<double> f(R, 0.0), nf(R, 0.0), nc(R, 0.0);
+  for (int i = 0; i < R; ++i)
+    for (int m = 1; m <= n_bin; ++m) nc[i] = nc[i] + H[(size_t)i * nb + m];
+  auto qp = [&](double bt, int m) {  // quasiprob :59-85
+    double E = en_min + (m - 0.5) * dE;
+    double q = 0, den = 0, off = -1e6;
+    for (int i = 0; i < R; ++i) off = std::fmax(off, -beta[i] * E - f[i]);
+    off = off + std::log(1e3);
+    for (int i = 0; i < R; ++i) {
+      q = q + H[(size_t)i * nb + m];
+      den = den + nc[i] * std::exp(-beta[i] * E - f[i] - off);
+    }
+    return q / den * std::exp(-bt * E - off);
+  };
+  int it = 0;
+  for (it = 1; it <= 1000; ++it) {
+    for (int i = 0; i < R; ++i) {
+      nf[i] = 0;
+      for (int m = 1; m <= n_bin; ++m) nf[i] = nf[i] + qp(beta[i], m);
+      nf[i] = std::log(nf[i]);
+    }
+    double delta = 0;
+    for (int i = 0; i < R; ++i) {
+      double dd = std::fabs(nf[i] - f[i]);
+      delta = delta + dd * dd;
+      f[i] = nf[i];
+    }
+    if (delta < thr) break;
+  }
+  if (iters) *iters = it > 1000 ? 1000 : it;
+  int RR = 10 * R;
+  std::vector<double> Tr(RR), Br(RR);
+  orc_tempgrid(t_grid[0], t_grid[R - 1], RR, 0, Tr.data(), Br.data());
+  for (int i = 0; i < RR; ++i) {
+    double norm = 0;
+    for (int m = 1; m <= n_bin; ++m) norm = norm + qp(Br[i], m);
+    double e1 = 0, e2 = 0;
+    for (int m = 1; m <= n_bin; ++m) {
+      double E = en_min + (m - 0.5) * dE;
+      e1 = e1 + qp(Br[i], m) / norm * E;
+      e2 = e2 + qp(Br[i], m) / norm * (E * E);
+    }
+    T_out[i] = Tr[i];
+    cv_out[i] = (e2 - e1 * e1) / (k * (Tr[i] * Tr[i]));
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- WHAM NPT
+// multihistogram_NPT (multihist_NPT.jl:11-338), restated literally.
+int orc_multihist_npt(int R, int n_bin, const double* H, const double* t_grid,
+                      const double* beta, double en_min, double en_max,
+                      double v_min, double v_max, double p, double thr,
+                      double* T_out, double* cp_out, int* iters) {
+  const double k = 3.166811429 / 1e6;
+  int nb = n_bin + 2;
+  double dE = (en_max - en_min) / n_bin, dV = (v_max - v_min) / n_bin;
+  auto h = [&](int i, int m, int n) { return H[((size_t)i * nb + m) * nb + n]; };
+  std::vector<double> f(R, 0.0), nf(R, 0.0), nc(R, 0.0);
+  for (int i = 0; i < R; ++i)
+    for (int m = 1; m <= n_bin; ++m)
+      for (int n = 1; n <= n_bin; ++n) nc[i] = nc[i] + h(i, m, n);
+  auto qp = [&](double bt, int m, int n) {  // quasiprob :70-103
+    double E = en_min + (m - 0.5) * dE;
+    double V = v_min + (n - 0.5) * dV;
+    double q = 0, den = 0, off = -1e6;
+    for (int i = 0; i < R; ++i) off = std::fmax(off, -beta[i] * (E + p * V) - f[i]);
+    off = off + std::log(1e3);
+    for (int i = 0; i < R; ++i) {
+      q = q + h(i, m, n);
+      den = den + nc[i] * std::exp(-beta[i] * (E + p * V) - f[i] - off);
+    }
+    return q / den * std::exp(-bt * (E + p * V) - off);
+  };
+  int it = 0;
+  for (it = 1; it <= 1000; ++it) {
+    for (int i = 0; i < R; ++i) {
+      nf[i] = 0;
+      for (int m = 1; m <= n_bin; ++m)
+        for (int n = 1; n <= n_bin; ++n) nf[i] = nf[i] + qp(beta[i], m, n);
+      nf[i] = std::log(nf[i]);
+    }
+    double delta = 0;
+    for (int i = 0; i < R; ++i) {
+      double dd = std::fabs(nf[i] - f[i]);
+      delta = delta + dd * dd;
+      f[i] = nf[i];
+    }
+    if (delta < thr) break;
+  }
+  if (iters) *iters = it > 1000 ? 1000 : it;
+  int RR = 10 * R;
+  std::vector<double> Tr(RR), Br(RR);
+  orc_tempgrid(t_grid[0], t_grid[R - 1], RR, 0, Tr.data(), Br.data());
+  for (int i = 0; i < RR; ++i) {
+    double norm = 0;
+    for (int m = 1; m <= n_bin; ++m)
+      for (int n = 1; n <= n_bin; ++n) norm = norm + qp(Br[i], m, n);
+    double h1 = 0, h2 = 0;
+    for (int m = 1; m <= n_bin; ++m)
+      for (int n = 1; n <= n_bin; ++n) {
+        double E = en_min + (m - 0.5) * dE;
+        double V = v_min + (n - 0.5) * dV;
+        double q = qp(Br[i], m, n) / norm;
+        h1 = h1 + q * (E + p * V);
+        h2 = h2 + q * ((E + p * V) * (E + p * V));
+      }
+    T_out[i] = Tr[i];
+    cp_out[i] = (h2 - h1 * h1) / (k * (Tr[i] * Tr[i]));
+  }
+  return 0;
+}
+
+}  // extern "C"

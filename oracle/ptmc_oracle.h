@@ -1,0 +1,122 @@
+/*
+ * ptmc_oracle.h — CPU ORACLE for the parallel-tempering Monte Carlo hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is a plain FP64 C++17 restatement of
+ * ParallelTemperingMonteCarlo.jl's replica cycle (moves, energies, Metropolis,
+ * exchange, step adaptation, sampling, multihistogram).  It is the checker the
+ * GPU engine is compared against; it is never linked into, loaded by or called
+ * from the product library.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline leg of bench.py may load it.
+ *
+ * Pinning: the deterministic known-answer tests of the reference
+ * (test/test_potentials.jl, test/runtests.jl, test/configurations.jl,
+ * test/test_runner_forward.jl) and the multihistogram golden vectors embedded in
+ * test/multihist_test.jl are checked against this library in tests/.  The
+ * reference's RNG-seeded pins (test/test_states.jl) need Julia's Xoshiro stream
+ * and cannot be reproduced; instead oracle and engine share one Philox4x32-10
+ * draw stream (same draw order as the reference, see src/MCRun.jl:142-162).
+ *
+ * All functions return 0 on success and a negative code on error;
+ * orc_last_error() gives the message.
+ */
+#ifndef PTMC_ORACLE_H
+#define PTMC_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_run orc_run;
+
+/* potential kinds (src/EnergyEvaluation.jl) */
+#define ORC_POT_ELJ 0      /* ELJPotential      :923 */
+#define ORC_POT_ELJEVEN 1  /* ELJPotentialEven  :934 */
+#define ORC_POT_EAM 2      /* EmbeddedAtomPotential :1059 */
+#define ORC_POT_NN 3       /* RuNNerPotential   :1182 */
+/* boundary kinds (src/BoundaryConditions.jl) */
+#define ORC_BC_SPHERE 0
+#define ORC_BC_CUBIC 1
+/* ensembles (src/Ensembles.jl) */
+#define ORC_NVT 0
+#define ORC_NPT 1
+
+/* One PT run of R replicas of N atoms.  xyz holds R start configurations
+ * (walker w starts from xyz[w*N*3 ...]); T holds the R temperatures (K);
+ * max_displ holds 2 values per slot (atom, volume).  bc_param is the sphere
+ * radius or the cubic side length.  run_index selects the Philox stream. */
+orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
+                    double bc_param, const double* xyz, const double* T,
+                    const double* max_displ, int n_bin, int n_adjust,
+                    int mc_sample, double min_acc, double max_acc,
+                    double exch_prob, uint64_t seed, int run_index);
+void orc_destroy(orc_run* r);
+const char* orc_last_error(void);
+
+int orc_set_pot_elj(orc_run* r, const double* c, int K, int even);
+int orc_set_pot_eam(orc_run* r, double n, double m, double ean, double ecam);
+/* sf: nsf rows of 8 doubles {kind(0 radial,1 angular), type, eta, lambda,
+ * zeta, rcut, gmin, gmax}; weights: our layout (per layer: W[n_in][n_out]
+ * input-major, then b[n_out]); nodes: n_layers node counts; boundary: hard-core
+ * distance (bohr) below which E = 100 (EnergyEvaluation.jl:1602). */
+int orc_set_pot_nn(orc_run* r, const double* sf, int nsf, const double* weights,
+                   int nw, const int* nodes, int n_layers, double boundary);
+int orc_init(orc_run* r);
+
+/* equilibration_cycle! (MCRun.jl:282): eq_cycles/2 cycles, ebounds, counters
+ * reset, histogram initialisation (Sampling.jl:141). */
+int orc_equilibrate(orc_run* r, int eq_cycles);
+/* production cycles i = first .. first+n-1 (MCRun.jl:397, mc_cycle! :215) */
+int orc_production(orc_run* r, long first, long n);
+/* plain cycles without sampling (mc_cycle! :192) */
+int orc_cycles(orc_run* r, long first, long n);
+
+/* walker-bound state (config order = walker order) */
+int orc_get_walkers(orc_run* r, double* xyz, double* en_tot, double* box);
+/* slot-bound state (slot = temperature index) */
+int orc_get_slots(orc_run* r, int* walker_of_slot, double* max_displ,
+                  long* count_atom, long* count_vol, long* count_exc,
+                  double* ham);
+/* histogram state: NVT en_hist R*(n_bin+2), NPT ev_hist R*(n_bin+2)^2
+ * (row-major [slot][e][v]); hp = {en_min, en_max, v_min, v_max, dE, dV} */
+int orc_get_hist(orc_run* r, double* en_hist, double* ev_hist, double* hp);
+/* finalise_results (Sampling.jl:377) */
+int orc_finalise(orc_run* r, long mc_cycles, int mc_sample, double* en_avg,
+                 double* heat_cap, double* stat_atom, double* stat_exc);
+/* NN only: G matrix (nsf x N, column per atom) of walker w */
+int orc_get_nn_state(orc_run* r, int w, double* G, double* eatom);
+
+/* ---- pure functions (known-answer tests) ---- */
+double orc_dimer_energy(int kind, const double* c, int K, double r2);
+double orc_distance2(const double* a, const double* b, int bc_kind,
+                     double L);
+double orc_lrc(int N, double r_cut2, const double* c, int K);
+double orc_eam_config_energy(const double* xyz, int N, double n, double m,
+                             double ean, double ecam);
+double orc_elj_config_energy(const double* xyz, int N, int kind,
+                             const double* c, int K, int bc_kind, double L,
+                             double r_cut2);
+void orc_tempgrid(double ti, double tf, int R, int tdistr, double* T,
+                  double* beta);
+double orc_u01(uint64_t seed, uint32_t stream, uint32_t run, uint64_t idx);
+/* raw Philox4x32-10 block (known-answer test) */
+void orc_philox4x32(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
+/* per-atom MLP forward (ForwardPass.jl:50-84 math), FP64 */
+int orc_mlp_forward(const double* input, int n_in, int batch,
+                    const double* weights, int nw, const int* nodes,
+                    int n_layers, double* eatom);
+
+/* ---- multihistogram (multihist_NVT.jl:95, multihist_NPT.jl:113) ---- */
+int orc_multihist_nvt(int R, int n_bin, const double* en_hist,
+                      const double* t_grid, const double* beta, double en_min,
+                      double en_max, double thr, double* T_out, double* cv_out,
+                      int* iters);
+int orc_multihist_npt(int R, int n_bin, const double* ev_hist,
+                      const double* t_grid, const double* beta, double en_min,
+                      double en_max, double v_min, double v_max,
+                      double pressure, double thr, double* T_out,
+                      double* cp_out, int* iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,553 @@
+"""GB300 parallel-tempering Monte Carlo engine — host-side mirror of the
+ParallelTemperingMonteCarlo.jl API for the replica-cycle hot path.
+
+Names, argument meaning and error behaviour follow the reference:
+MCParams / TempGrid (src/InputParams.jl:35-95), SphericalBC / CubicBC
+(src/BoundaryConditions.jl:44-80), Config (src/Configurations.jl:42),
+NVT / NPT (src/Ensembles.jl:42-86), ELJPotential / ELJPotentialEven /
+EmbeddedAtomPotential (src/EnergyEvaluation.jl:923-942, 1059-1073),
+ptmc_run! (src/MCRun.jl:363-481, here `ptmc_run`), Output
+(src/InputParams.jl:114-176), multihistogram_NVT / multihistogram_NPT
+(src/multihist_NVT.jl:95, src/multihist_NPT.jl:113) and the checkpoint
+directory of src/ReadSave.jl.
+
+Every computation runs in libptmc_gb300.so on the GPU through its C ABI
+(include/ptmc_gb300.h); this module only marshals arguments.  There is no CPU
+fallback: without the built library or a usable GPU every call raises.
+"""
+import ctypes
+import math
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _capi
+from ._capi import PTMCError
+
+kB = 3.16681196e-6  # Hartree/K, src/InputParams.jl:19
+
+__all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "Config", "NVT", "NPT",
+           "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "Output", "MCState",
+           "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
+           "distance2", "get_distance2_mat", "get_volume", "PTMCError"]
+
+
+# ------------------------------------------------------------------ parameters
+@dataclass
+class MCParams:
+    """MCParams (src/InputParams.jl:35-63)."""
+    mc_cycles: int
+    eq_cycles: int
+    mc_sample: int
+    n_traj: int
+    n_atoms: int
+    n_adjust: int = 100
+    n_bin: int = 100
+    min_acc: float = 0.4
+    max_acc: float = 0.6
+
+    @classmethod
+    def new(cls, cycles, n_traj, n_atoms, eq_percentage=0.2, mc_sample=1, n_adjust=100,
+            n_bin=100, min_acc=0.4, max_acc=0.6):
+        cycles = int(cycles)
+        return cls(cycles, int(round(eq_percentage * cycles)), mc_sample, n_traj, n_atoms,
+                   n_adjust, n_bin, min_acc, max_acc)
+
+
+def _mcparams(cycles, n_traj, n_atoms, **kw):
+    return MCParams.new(cycles, n_traj, n_atoms, **kw)
+
+
+class TempGrid:
+    """TempGrid{N}(ti, tf; tdistr) (src/InputParams.jl:77-95)."""
+
+    def __init__(self, ti, tf, N, tdistr="geometric"):
+        if tdistr not in ("geometric", "equally_spaced"):
+            raise ValueError("chosen temperature distribution %s does not exist" % tdistr)
+        i = np.arange(N, dtype=np.float64)
+        if tdistr == "equally_spaced":
+            delta = (tf - ti) / (N - 1)
+            self.t_grid = ti + i * delta
+        else:
+            self.t_grid = np.array([ti * (tf / ti) ** (k / (N - 1)) for k in range(N)])
+        self.beta_grid = 1.0 / (kB * self.t_grid)
+        self.ti, self.tf, self.N, self.tdistr = float(ti), float(tf), N, tdistr
+
+    def __len__(self):
+        return self.N
+
+
+@dataclass
+class SphericalBC:
+    """SphericalBC(radius) (src/BoundaryConditions.jl:44-49); stores radius^2."""
+    radius: float
+
+    @property
+    def radius2(self):
+        return self.radius * self.radius
+
+
+@dataclass
+class CubicBC:
+    """CubicBC(side_length) (src/BoundaryConditions.jl:72-78)."""
+    box_length: float
+
+
+class Config:
+    """Config(positions, boundary_condition) (src/Configurations.jl:42-56)."""
+
+    def __init__(self, positions, boundary_condition):
+        self.positions = np.array(positions, dtype=np.float64).reshape(-1, 3)
+        self.boundary_condition = boundary_condition
+
+    def __len__(self):
+        return len(self.positions)
+
+
+def distance2(a, b, bc=None):
+    """distance2 (src/Configurations.jl:101-109), with CubicBC minimum image."""
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    if isinstance(bc, CubicBC):
+        L = bc.box_length
+        b = b + L * np.round((a - b) / L)
+    d = a - b
+    return float((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+
+
+def get_distance2_mat(config):
+    """get_distance2_mat (src/Configurations.jl:135-162)."""
+    n = len(config)
+    m = np.zeros((n, n))
+    for i in range(n):
+        for j in range(i + 1, n):
+            m[i, j] = m[j, i] = distance2(config.positions[i], config.positions[j],
+                                          config.boundary_condition)
+    return m
+
+
+def get_volume(bc):
+    """get_volume (src/Configurations.jl:246-256)."""
+    if isinstance(bc, CubicBC):
+        return bc.box_length ** 3
+    raise TypeError("get_volume is defined for periodic boxes")
+
+
+@dataclass
+class NVT:
+    """NVT(n_atoms) (src/Ensembles.jl:42-50)."""
+    n_atoms: int
+
+    @property
+    def n_atom_moves(self):
+        return self.n_atoms
+
+
+@dataclass
+class NPT:
+    """NPT(n_atoms, pressure, separated_volume) (src/Ensembles.jl:75-86)."""
+    n_atoms: int
+    pressure: float
+    separated_volume: bool = False
+
+    def __post_init__(self):
+        if self.separated_volume:
+            raise NotImplementedError("separated volume moves are not part of this engine")
+
+
+@dataclass
+class ELJPotential:
+    """ELJPotential: V(r) = sum_i c_i r^-(5+i) (src/EnergyEvaluation.jl:923-932)."""
+    coeff: list
+
+    even = False
+
+
+@dataclass
+class ELJPotentialEven:
+    """ELJPotentialEven: V(r) = sum_i c_i r^-(4+2i) (src/EnergyEvaluation.jl:934-942)."""
+    coeff: list
+
+    even = True
+
+
+class EmbeddedAtomPotential:
+    """EmbeddedAtomPotential(n, m, eps, C, a) (src/EnergyEvaluation.jl:1059-1073)."""
+
+    def __init__(self, n, m, eps=None, C=None, a=None, *, ean=None, eCam=None):
+        self.n, self.m = float(n), float(m)
+        if ean is not None:
+            self.ean, self.eCam = float(ean), float(eCam)
+        else:
+            self.ean = eps * a ** n / 2
+            self.eCam = eps * C * a ** (m / 2)
+
+
+@dataclass
+class Output:
+    """Output{Float64} (src/InputParams.jl:114-176), one run."""
+    n_bin: int
+    en_min: float = 0.0
+    en_max: float = 0.0
+    v_min: float = 0.0
+    v_max: float = 0.0
+    delta_en_hist: float = 0.0
+    delta_v_hist: float = 0.0
+    delta_r2: float = 0.0
+    max_displ: np.ndarray = None
+    en_avg: np.ndarray = None
+    heat_cap: np.ndarray = None
+    en_histogram: np.ndarray = None
+    ev_histogram: np.ndarray = None
+    rdf: list = field(default_factory=list)
+    count_stat_atom: np.ndarray = None
+    count_stat_vol: np.ndarray = None
+    count_stat_exc: np.ndarray = None
+
+
+@dataclass
+class MCState:
+    """Slot-ordered replica state after a run (the host view of MCState,
+    src/MCStates.jl:33-53)."""
+    temp: float
+    beta: float
+    config: Config
+    en_tot: float
+    max_displ: np.ndarray
+    count_atom: np.ndarray
+    count_vol: np.ndarray
+    count_exc: np.ndarray
+    ham: np.ndarray
+
+
+# ------------------------------------------------------------------ engine
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Engine:
+    """A batch of `n_runs` independent PT runs on the GPU (one ptmc_ctx).
+
+    Every run shares the potential, the ensemble, the temperature grid and the
+    MC parameters; each run gets its own start configurations (and may have its
+    own atom count)."""
+
+    def __init__(self, mc_params, temp, potential, ensemble, *, n_runs=1, precision="fp64",
+                 resync_every=1000, exch_prob=0.1, seed=1234, cycles_per_launch=0, device=0):
+        self.L = _capi.load()
+        self.mc_params, self.temp, self.potential, self.ensemble = mc_params, temp, potential, ensemble
+        p = _capi.Params()
+        p.n_runs = n_runs
+        p.n_traj = mc_params.n_traj
+        p.mc_cycles = mc_params.mc_cycles
+        p.eq_cycles = mc_params.eq_cycles
+        p.mc_sample = mc_params.mc_sample
+        p.n_adjust = mc_params.n_adjust
+        p.n_bin = mc_params.n_bin
+        p.min_acc = mc_params.min_acc
+        p.max_acc = mc_params.max_acc
+        p.ensemble = _capi.NPT if isinstance(ensemble, NPT) else _capi.NVT
+        p.pressure = ensemble.pressure if isinstance(ensemble, NPT) else 0.0
+        p.t_i, p.t_f = temp.ti, temp.tf
+        p.tdistr = _capi.TLINEAR if temp.tdistr == "equally_spaced" else _capi.TGEOMETRIC
+        p.exch_prob = exch_prob
+        p.precision = {"fp64": _capi.FP64, "fp32": _capi.FP32_RESYNC,
+                       "fp32_resync": _capi.FP32_RESYNC}[precision]
+        p.resync_every = resync_every
+        p.seed = seed
+        p.cycles_per_launch = cycles_per_launch
+        p.device = device
+        self.params = p
+        h = ctypes.c_void_p()
+        _capi.check(self.L.ptmc_create(ctypes.byref(h), ctypes.byref(p)))
+        self.h = h
+        self.n_runs, self.R = n_runs, mc_params.n_traj
+        self.N = {}
+        self.bc = {}
+        if isinstance(potential, (ELJPotential, ELJPotentialEven)):
+            c = np.ascontiguousarray(potential.coeff, dtype=np.float64)
+            self._ck(self.L.ptmc_set_potential_elj(h, _dptr(c), len(c), int(potential.even)))
+        elif isinstance(potential, EmbeddedAtomPotential):
+            self._ck(self.L.ptmc_set_potential_eam(h, potential.n, potential.m, potential.ean,
+                                                   potential.eCam))
+        else:
+            raise TypeError("unsupported potential %r" % type(potential))
+
+    def _ck(self, rc):
+        return _capi.check(rc, self.h)
+
+    def set_configs(self, run, configs, max_displ=None):
+        """Start configurations of `run` (one Config or a sequence; replica i
+        starts from configs[i mod len], src/Initialization.jl:88-96)."""
+        if isinstance(configs, Config):
+            configs = [configs]
+        bc = configs[0].boundary_condition
+        N = len(configs[0])
+        xyz = np.ascontiguousarray(np.stack([c.positions for c in configs]), dtype=np.float64)
+        kind = _capi.BC_CUBIC if isinstance(bc, CubicBC) else _capi.BC_SPHERE
+        par = bc.box_length if kind == _capi.BC_CUBIC else bc.radius
+        self._ck(self.L.ptmc_set_run_configs(self.h, run, _dptr(xyz), N, len(configs), kind, par))
+        self.N[run], self.bc[run] = N, bc
+        if max_displ is not None:
+            md = np.ascontiguousarray(max_displ, dtype=np.float64).reshape(-1)
+            if md.size == self.R:
+                md = np.stack([md, np.full(self.R, 0.1)], 1).reshape(-1)
+            self._ck(self.L.ptmc_set_max_displ(self.h, run, _dptr(md)))
+
+    def init(self):
+        self._ck(self.L.ptmc_init(self.h))
+
+    def equilibrate(self):
+        self._ck(self.L.ptmc_equilibrate(self.h))
+
+    def run_cycles(self, n):
+        self._ck(self.L.ptmc_run_cycles(self.h, int(n)))
+
+    def cycles_nosample(self, n):
+        self._ck(self.L.ptmc_cycles_nosample(self.h, int(n)))
+
+    def resync(self):
+        self._ck(self.L.ptmc_resync(self.h))
+
+    def states(self, run=0):
+        """Slot-ordered (xyz [R,N,3], en_tot [R], box [R], max_displ [R,2],
+        counts [R,6], ham [R,2])."""
+        R, N = self.R, self.N[run]
+        xyz = np.zeros((R, N, 3))
+        en, box = np.zeros(R), np.zeros(R)
+        md, ham = np.zeros((R, 2)), np.zeros((R, 2))
+        cnt = np.zeros((R, 6), dtype=np.int64)
+        self._ck(self.L.ptmc_get_states(self.h, run, _dptr(xyz), _dptr(en), _dptr(box), _dptr(md),
+                                        cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                        _dptr(ham)))
+        return dict(xyz=xyz, en_tot=en, box=box, max_displ=md, counts=cnt, ham=ham)
+
+    def output(self, run=0):
+        R, nb = self.R, self.mc_params.n_bin + 2
+        npt = isinstance(self.ensemble, NPT)
+        arrs = dict(en_avg=np.zeros(R), heat_cap=np.zeros(R), count_stat_atom=np.zeros(R),
+                    count_stat_vol=np.zeros(R), count_stat_exc=np.zeros(R),
+                    max_displ=np.zeros((R, 2)))
+        eh = np.zeros((R, nb))
+        ev = np.zeros((R, nb, nb)) if npt else np.zeros(1)
+        o = _capi.Output()
+        for k, v in arrs.items():
+            setattr(o, k, _dptr(v))
+        o.en_histogram = _dptr(eh)
+        o.ev_histogram = _dptr(ev)
+        self._ck(self.L.ptmc_get_output(self.h, run, ctypes.byref(o)))
+        hp = list(o.hist_params)
+        return Output(n_bin=self.mc_params.n_bin, en_min=hp[0], en_max=hp[1], v_min=hp[2],
+                      v_max=hp[3], delta_en_hist=hp[4], delta_v_hist=hp[5],
+                      max_displ=arrs["max_displ"], en_avg=arrs["en_avg"],
+                      heat_cap=arrs["heat_cap"], en_histogram=eh,
+                      ev_histogram=ev if npt else None,
+                      count_stat_atom=arrs["count_stat_atom"],
+                      count_stat_vol=arrs["count_stat_vol"],
+                      count_stat_exc=arrs["count_stat_exc"])
+
+    def stats(self):
+        s = _capi.Stats()
+        self._ck(self.L.ptmc_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _capi.Stats._fields_}
+
+    def checkpoint(self, directory):
+        self._ck(self.L.ptmc_checkpoint(self.h, os.fsencode(directory)))
+
+    def restore(self, directory):
+        self._ck(self.L.ptmc_restore(self.h, os.fsencode(directory)))
+
+    def mc_states(self, run=0):
+        s = self.states(run)
+        out = []
+        for i in range(self.R):
+            bc = self.bc[run]
+            bci = CubicBC(s["box"][i]) if isinstance(bc, CubicBC) else SphericalBC(s["box"][i])
+            out.append(MCState(self.temp.t_grid[i], self.temp.beta_grid[i],
+                               Config(s["xyz"][i], bci), s["en_tot"][i], s["max_displ"][i],
+                               s["counts"][i, 0:2], s["counts"][i, 2:4], s["counts"][i, 4:6],
+                               s["ham"][i]))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ptmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def ptmc_run(mc_params, temp, start_config, potential, ensemble, *, rdfsave=False,
+             restart=False, save=False, saveconfigs=False, configsname="configuration",
+             workingdirectory=None, precision="fp64", resync_every=1000, exch_prob=0.1,
+             seed=1234, max_displ=None):
+    """ptmc_run! (src/MCRun.jl:363-432): initialise, equilibrate, run
+    mc_params.mc_cycles production cycles with optional checkpoints every
+    `save` cycles into <workingdirectory>/checkpoint, finalise.
+
+    Returns (mc_states, results) with slot-ordered states and an Output."""
+    if rdfsave:
+        raise NotImplementedError("the radial distribution sampler is not part of this engine")
+    wd = workingdirectory or os.getcwd()
+    ckdir = os.path.join(wd, "checkpoint")
+    eng = Engine(mc_params, temp, potential, ensemble, precision=precision,
+                 resync_every=resync_every, exch_prob=exch_prob, seed=seed)
+    try:
+        eng.set_configs(0, start_config, max_displ)
+        eng.init()
+        if restart:
+            eng.restore(ckdir)
+            done = _restored_index(ckdir)
+        else:
+            eng.equilibrate()
+            done = 0
+        total = mc_params.mc_cycles
+        marks = set()
+        if save:
+            marks.update(range(save, total + 1, save))
+        if saveconfigs:
+            marks.update(range(saveconfigs, total + 1, saveconfigs))
+        for m in sorted(x for x in marks if x > done):
+            eng.run_cycles(m - done)
+            done = m
+            if save and m % save == 0:
+                eng.checkpoint(ckdir)
+            if saveconfigs and m % saveconfigs == 0:
+                _save_configs(eng, ckdir, "%s%d" % (configsname, m))
+        if done < total:
+            eng.run_cycles(total - done)
+        if save and total % save != 0:
+            eng.checkpoint(ckdir)
+        results = eng.output(0)
+        states = eng.mc_states(0)
+        return states, results
+    finally:
+        eng.close()
+
+
+def _restored_index(ckdir):
+    with open(os.path.join(ckdir, "index.txt")) as f:
+        return int(float(f.read().split()[0]))
+
+
+def _save_configs(eng, ckdir, name):
+    """save_configs (src/ReadSave.jl:160-170) in the xyz format of checkpoint_config."""
+    os.makedirs(ckdir, exist_ok=True)
+    for i, st in enumerate(eng.mc_states(0)):
+        with open(os.path.join(ckdir, "%sT%d.xyz" % (name, i + 1)), "w") as f:
+            f.write("%d\n" % len(st.config))
+            bc = st.config.boundary_condition
+            hdr = ("SphericalBC{Float64} r2: %r" % bc.radius2 if isinstance(bc, SphericalBC)
+                   else "CubicBC{Float64} box_length: %r" % bc.box_length)
+            f.write("%s %r %r %r %d %d\n" % (hdr, st.max_displ[0], st.max_displ[1], 0.1,
+                                             st.count_atom[0], st.count_vol[0]))
+            for x in st.config.positions:
+                f.write("1  %r %r %r \n" % (x[0], x[1], x[2]))
+
+
+# ------------------------------------------------------------------ analysis
+def multihistogram_NVT(ensemble, temp, results, conv_threshold, readfile=False, debug=False):
+    """multihistogram_NVT (src/multihist_NVT.jl:95-221) on the GPU; returns
+    Cv on TempGrid{10R}(t_1, t_R)."""
+    T, cv, _ = multihist_nvt_arrays(results.en_histogram, temp.t_grid, temp.beta_grid,
+                                    results.en_min, results.en_max, conv_threshold)
+    return cv
+
+
+def multihistogram_NPT(ensemble, temp, results, conv_threshold, readfile=False, debug=False):
+    """multihistogram_NPT (src/multihist_NPT.jl:113-338) on the GPU; returns
+    (T, Cp) on TempGrid{10R}(t_1, t_R)."""
+    T, cp, _ = multihist_npt_arrays(results.ev_histogram, temp.t_grid, temp.beta_grid,
+                                    results.en_min, results.en_max, results.v_min,
+                                    results.v_max, ensemble.pressure, conv_threshold)
+    return T, cp
+
+
+def multihist_nvt_arrays(hist, t_grid, beta, en_min, en_max, thr):
+    L = _capi.load()
+    h = np.ascontiguousarray(hist, dtype=np.float64)
+    R, nb = h.shape
+    t, b = np.ascontiguousarray(t_grid, float), np.ascontiguousarray(beta, float)
+    T, cv, it = np.zeros(10 * R), np.zeros(10 * R), ctypes.c_int()
+    _capi.check(L.ptmc_multihist_nvt(R, nb - 2, _dptr(h), _dptr(t), _dptr(b), en_min, en_max,
+                                     thr, _dptr(T), _dptr(cv), ctypes.byref(it)))
+    return T, cv, it.value
+
+
+def multihist_npt_arrays(hist, t_grid, beta, en_min, en_max, v_min, v_max, p, thr):
+    L = _capi.load()
+    h = np.ascontiguousarray(hist, dtype=np.float64)
+    R, nb = h.shape[0], h.shape[1]
+    t, b = np.ascontiguousarray(t_grid, float), np.ascontiguousarray(beta, float)
+    T, cp, it = np.zeros(10 * R), np.zeros(10 * R), ctypes.c_int()
+    _capi.check(L.ptmc_multihist_npt(R, nb - 2, _dptr(h), _dptr(t), _dptr(b), en_min, en_max,
+                                     v_min, v_max, p, thr, _dptr(T), _dptr(cp), ctypes.byref(it)))
+    return T, cp, it.value
+
+
+# ------------------------------------------------------------------ checkpoints
+def read_checkpoint(directory):
+    """Read a reference checkpoint directory (src/ReadSave.jl:330-481):
+    params.data, hist_info.data, histograms.data, [volume_hist.data],
+    index.txt and configT<i>.xyz or config.<i>.  Returns a dict."""
+    def rows(path):
+        with open(path) as f:
+            return [ln.split() for ln in f.read().strip().split("\n")]
+
+    out = {}
+    p = rows(os.path.join(directory, "params.data"))
+    out["params"] = [float(x) for x in p[1]]
+    out["ensemble"] = p[3]
+    out["potential"] = p[4]
+    hi = rows(os.path.join(directory, "hist_info.data"))
+    out["hist_info"] = [float(x) for x in hi[1]]
+    out["histograms"] = np.array([[float(x) for x in r] for r in
+                                  rows(os.path.join(directory, "histograms.data"))])
+    vp = os.path.join(directory, "volume_hist.data")
+    if os.path.exists(vp):
+        v = np.array([[float(x) for x in r] for r in rows(vp)])
+        nb = int(round(math.sqrt(v.shape[1])))
+        out["volume_hist"] = v.reshape(v.shape[0], nb, nb).transpose(0, 2, 1)
+    ip = os.path.join(directory, "index.txt")
+    if os.path.exists(ip):
+        out["index"] = int(float(open(ip).read().split()[0]))
+    # one file per replica; the count is taken from the files present (the
+    # reference's own fixture holds 25 files for n_traj = 24)
+    configs = []
+    i = 0
+    while True:
+        i += 1
+        names = [n for n in ("configT%d.xyz" % i, "config.%d" % i)
+                 if os.path.exists(os.path.join(directory, n))]
+        if not names:
+            break
+        for name in names:
+            path = os.path.join(directory, name)
+            if os.path.exists(path):
+                r = rows(path)
+                n = int(r[0][0])
+                hdr = r[1]
+                xyz = np.array([[float(x) for x in ln[1:4]] for ln in r[2:2 + n]])
+                if hdr[0].startswith("SphericalBC"):
+                    bc = SphericalBC(math.sqrt(float(hdr[2])))
+                    md = [float(x) for x in hdr[3:6]]
+                    counts = [int(float(x)) for x in hdr[6:8]]
+                else:
+                    bc = CubicBC(float(hdr[2]))
+                    md = [float(x) for x in hdr[3:6]]
+                    counts = [int(float(x)) for x in hdr[6:8]]
+                configs.append(dict(config=Config(xyz, bc), max_displ=md, counts=counts))
+                break
+    out["configs"] = configs
+    return out

@@ -1,0 +1,1003 @@
+// ptmc_capi.cu — the C ABI (include/ptmc_gb300.h): context, HBM layout,
+// orchestration of the replica cycles, outputs and checkpoints.
+//
+// What replaces what: ptmc_create/ptmc_set_*/ptmc_init replace MCParams,
+// TempGrid, the ensemble/potential constructors and initialisation()
+// (src/Initialization.jl:70-100); ptmc_equilibrate replaces equilibration()
+// (src/MCRun.jl:322-344); ptmc_run_cycles replaces the main loop of
+// ptmc_run! (src/MCRun.jl:397-419); ptmc_get_output replaces
+// finalise_results (src/Sampling.jl:377-399); ptmc_checkpoint/ptmc_restore
+// replace checkpoint/save_configs/rebuild_states (src/ReadSave.jl:93-218,
+// 330-481).
+//
+// Runs are grouped by atom count.  One group = one kernel launch per chunk of
+// cycles (grid = runs of the group, block = 32 x replicas).  Groups run on
+// forked streams so uneven-N batches execute concurrently; a chunk sequence of
+// every group is captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <charconv>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/ptmc_gb300.h"
+#include "ptmc_engine.cuh"
+
+using namespace ptmc;
+
+namespace {
+thread_local std::string g_err;
+const double kB = 3.16681196E-6;  // src/InputParams.jl:19
+
+struct HostRun {
+  int N = 0;
+  int n_start = 0;
+  int bc = -1;
+  double bc_param = 0;
+  std::vector<double> xyz;   // n_start * N * 3
+  std::vector<double> maxd;  // 2R (optional)
+};
+
+struct Group {
+  int N;
+  int dev0;    // first device run index
+  int nruns;
+  cudaStream_t st = nullptr;
+};
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  int alloc(size_t count) {
+    n = count;
+    if (count == 0) count = 1;
+    return (int)cudaMalloc(&p, count * sizeof(T));
+  }
+  void free_() {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+};
+
+// Shortest round-trip text of a double in Julia's print style ("0.1",
+// "100.0", "1.0e6", "-5.62340834334278e7", "1.0e-5"), so that checkpoint files
+// read like the reference's writedlm output (src/ReadSave.jl).
+std::string fmt_double(double v) {
+  if (v == 0) return std::signbit(v) ? "-0.0" : "0.0";
+  if (std::isnan(v)) return "NaN";
+  if (std::isinf(v)) return v > 0 ? "Inf" : "-Inf";
+  char buf[64];
+  auto r = std::to_chars(buf, buf + sizeof(buf), v, std::chars_format::scientific);
+  std::string sc(buf, r.ptr);  // [-]d[.ddd]e(+|-)XX
+  bool neg = sc[0] == '-';
+  if (neg) sc = sc.substr(1);
+  size_t ep = sc.find('e');
+  std::string mant = sc.substr(0, ep);
+  int ex = std::stoi(sc.substr(ep + 1));
+  std::string digits;
+  for (char ch : mant)
+    if (ch != '.') digits += ch;
+  while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
+  std::string out;
+  if (ex >= -5 && ex < 6) {
+    if (ex >= 0) {
+      std::string ip = digits.substr(0, std::min<size_t>(digits.size(), ex + 1));
+      while ((int)ip.size() < ex + 1) ip += '0';
+      std::string fp = (int)digits.size() > ex + 1 ? digits.substr(ex + 1) : "0";
+      out = ip + "." + fp;
+    } else {
+      out = "0." + std::string(-ex - 1, '0') + digits;
+    }
+  } else {
+    out = digits.substr(0, 1) + "." + (digits.size() > 1 ? digits.substr(1) : "0") + "e" +
+          std::to_string(ex);
+  }
+  return neg ? "-" + out : out;
+}
+
+bool write_file_atomic(const std::string& path, const std::string& data) {
+  std::string tmp = path + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return false;
+  bool ok = std::fwrite(data.data(), 1, data.size(), f) == data.size();
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return false;
+  return std::rename(tmp.c_str(), path.c_str()) == 0;
+}
+}  // namespace
+
+struct ptmc_ctx {
+  ptmc_params p{};
+  std::string err;
+  int pot = -1;
+  std::vector<double> coeff;
+  double eam[4] = {0, 0, 0, 0};
+  std::vector<HostRun> runs;
+  // layout
+  std::vector<int> dev_of_run, run_of_dev;
+  std::vector<Group> groups;
+  std::vector<RunDesc> rd;  // device-ordered
+  int W = 0;                // total walkers
+  bool inited = false, equilibrated = false;
+  // device state
+  DBuf<RunDesc> d_runs;
+  DBuf<double> d_pos, d_mat, d_comp, d_en, d_box, d_rc2, d_drift, d_beta, d_maxd,
+      d_maxbox, d_ham;
+  DBuf<unsigned long long> d_ctr;
+  DBuf<int> d_status, d_wos;
+  DBuf<long long> d_cnt;
+  DBuf<unsigned int> d_hist;
+  KParams K{};
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evfork = nullptr;
+  std::vector<cudaEvent_t> evjoin;
+  std::map<long long, cudaGraphExec_t> graphs;  // key: phase*2^40 + chunk*2^8 + reps
+  ptmc_stats stats{};
+  std::vector<double> T, beta;
+
+  int fail(int code, const std::string& m) {
+    err = m;
+    g_err = m;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    return fail(PTMC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+  }
+  int R() const { return p.n_traj; }
+  int bc() const { return runs.empty() ? 0 : runs[0].bc; }
+  bool f32() const { return p.precision == PTMC_FP32_RESYNC; }
+};
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return c->cuda_fail(e_, #call);    \
+  } while (0)
+
+namespace {
+
+int check_status(ptmc_ctx* c) {
+  std::vector<int> st(c->W);
+  CK(cudaMemcpyAsync(st.data(), c->d_status.p, sizeof(int) * c->W, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int i = 0; i < c->W; ++i)
+    if (st[i] == ST_SPHERE)
+      return c->fail(PTMC_ERR_SPHERE, "Error: too many moves out of binding sphere");
+  return PTMC_OK;
+}
+
+int push_runs(ptmc_ctx* c) {
+  CK(cudaMemcpyAsync(c->d_runs.p, c->rd.data(), sizeof(RunDesc) * c->rd.size(),
+                     cudaMemcpyHostToDevice, c->st));
+  return PTMC_OK;
+}
+int pull_runs(ptmc_ctx* c) {
+  CK(cudaMemcpyAsync(c->rd.data(), c->d_runs.p, sizeof(RunDesc) * c->rd.size(),
+                     cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+// one chunk of `ncyc` cycles for every group, groups on forked streams
+int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
+  CK(cudaEventRecord(c->evfork, c->st));
+  for (size_t g = 0; g < c->groups.size(); ++g) {
+    Group& G = c->groups[g];
+    CK(cudaStreamWaitEvent(G.st, c->evfork, 0));
+    int rc = launch_cycles(c->pot, c->bc(), c->p.ensemble, c->f32(), c->K, G.dev0,
+                           G.nruns, c->R(), G.N, ncyc, phase, G.st);
+    if (rc) return c->cuda_fail((cudaError_t)rc, "k_cycles launch");
+    CK(cudaEventRecord(c->evjoin[g], G.st));
+    CK(cudaStreamWaitEvent(c->st, c->evjoin[g], 0));
+    c->stats.kernel_launches += 1;
+  }
+  return PTMC_OK;
+}
+
+int default_chunk(ptmc_ctx* c) {
+  if (c->p.cycles_per_launch > 0) return c->p.cycles_per_launch;
+  // aim at a few milliseconds of work per launch
+  int maxN = 0;
+  for (auto& G : c->groups) maxN = std::max(maxN, G.N);
+  long long per_cycle = (long long)maxN * maxN;  // pair terms per walker-cycle
+  long long chunk = std::max(1LL, 4000000LL / std::max(1LL, per_cycle));
+  return (int)std::min(chunk, 2000LL);
+}
+
+int run_phase(ptmc_ctx* c, long long n, int phase) {
+  if (n <= 0) return PTMC_OK;
+  int chunk = default_chunk(c);
+  CK(cudaEventRecord(c->ev0, c->st));
+  long long done = 0;
+  const int reps = 8;
+  long long nfull = n / ((long long)chunk * reps);
+  if (nfull > 0) {
+    long long key = ((long long)phase << 40) | ((long long)chunk << 8) | reps;
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      long long saved = c->stats.kernel_launches;
+      for (int r = 0; r < reps; ++r) {
+        int rc = enqueue_chunk(c, chunk, phase);
+        if (rc) {
+          cudaStreamEndCapture(c->st, &graph);
+          return rc;
+        }
+      }
+      c->stats.kernel_launches = saved;
+      CK(cudaStreamEndCapture(c->st, &graph));
+      cudaGraphExec_t ex;
+      CK(cudaGraphInstantiate(&ex, graph, 0));
+      cudaGraphDestroy(graph);
+      it = c->graphs.emplace(key, ex).first;
+    }
+    for (long long k = 0; k < nfull; ++k) {
+      CK(cudaGraphLaunch(it->second, c->st));
+      c->stats.graph_launches += 1;
+      c->stats.kernel_launches += (long long)reps * c->groups.size();
+    }
+    done = nfull * chunk * reps;
+  }
+  while (done < n) {
+    int m = (int)std::min<long long>(chunk, n - done);
+    int rc = enqueue_chunk(c, m, phase);
+    if (rc) return rc;
+    done += m;
+  }
+  CK(cudaEventRecord(c->ev1, c->st));
+  CK(cudaEventSynchronize(c->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->stats.last_cycles_ms = ms;
+  long long atom_slots = 0, vol_slots = 0;
+  for (auto& G : c->groups) {
+    atom_slots += (long long)G.nruns * c->R() * G.N;
+    if (c->p.ensemble == PTMC_NPT) vol_slots += (long long)G.nruns * c->R();
+  }
+  // attempted moves: n_steps per walker-cycle split by the slot draw; the
+  // expected split is exact on average, report the nominal counts
+  c->stats.atom_moves += atom_slots * n;
+  c->stats.volume_moves += vol_slots * n;
+  CK(cudaGetLastError());
+  return check_status(c);
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+const char* ptmc_version(void) { return "ptmc-gb300 0.1 (sm_103a)"; }
+
+const char* ptmc_last_error(ptmc_ctx* c) { return c ? c->err.c_str() : g_err.c_str(); }
+
+int ptmc_create(ptmc_ctx** out, const ptmc_params* p) {
+  if (!out || !p) {
+    g_err = "ptmc_create: null argument";
+    return PTMC_ERR_ARG;
+  }
+  *out = nullptr;
+  if (p->n_runs < 1 || p->n_traj < 1) {
+    g_err = "ptmc_create: need n_runs >= 1 and n_traj >= 1";
+    return PTMC_ERR_ARG;
+  }
+  if (p->n_traj > MAX_REPLICAS) {
+    g_err = "ptmc_create: at most 32 replicas per run (one warp per replica in one CTA)";
+    return PTMC_ERR_LIMIT;
+  }
+  if (p->n_bin < 2 || p->n_adjust < 1 || p->mc_sample < 1 || p->mc_cycles < 0 || p->eq_cycles < 0) {
+    g_err = "ptmc_create: invalid MCParams";
+    return PTMC_ERR_ARG;
+  }
+  if (p->ensemble != PTMC_NVT && p->ensemble != PTMC_NPT) {
+    g_err = "ptmc_create: unknown ensemble";
+    return PTMC_ERR_ARG;
+  }
+  if (p->tdistr != PTMC_TGEOMETRIC && p->tdistr != PTMC_TLINEAR) {
+    g_err = "chosen temperature distribution does not exist";  // InputParams.jl:91
+    return PTMC_ERR_ARG;
+  }
+  if (p->precision != PTMC_FP64 && p->precision != PTMC_FP32_RESYNC) {
+    g_err = "ptmc_create: unknown precision";
+    return PTMC_ERR_ARG;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    g_err = std::string("ptmc_create: no CUDA device: ") + cudaGetErrorString(e);
+    return PTMC_ERR_CUDA;
+  }
+  if (p->device < 0 || p->device >= ndev) {
+    g_err = "ptmc_create: bad device ordinal";
+    return PTMC_ERR_ARG;
+  }
+  e = cudaSetDevice(p->device);
+  if (e != cudaSuccess) {
+    g_err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return PTMC_ERR_CUDA;
+  }
+  ptmc_ctx* c = new ptmc_ctx();
+  c->p = *p;
+  c->runs.resize(p->n_runs);
+  // TempGrid (src/InputParams.jl:77-95)
+  int R = p->n_traj;
+  c->T.resize(R);
+  c->beta.resize(R);
+  for (int i = 0; i < R; ++i) {
+    if (R == 1) c->T[i] = p->t_i;
+    else if (p->tdistr == PTMC_TLINEAR) c->T[i] = p->t_i + i * ((p->t_f - p->t_i) / (R - 1));
+    else c->T[i] = p->t_i * std::pow(p->t_f / p->t_i, (double)i / (double)(R - 1));
+    c->beta[i] = 1.0 / (kB * c->T[i]);
+  }
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->evfork, cudaEventDisableTiming) != cudaSuccess) {
+    g_err = "ptmc_create: stream/event creation failed";
+    delete c;
+    return PTMC_ERR_CUDA;
+  }
+  *out = c;
+  return PTMC_OK;
+}
+
+int ptmc_set_potential_elj(ptmc_ctx* c, const double* coeff, int K, int even) {
+  if (!c || !coeff) return PTMC_ERR_ARG;
+  if (K < 1 || K > MAX_COEFF) return c->fail(PTMC_ERR_LIMIT, "ELJ: 1..16 coefficients supported");
+  if (c->p.ensemble == PTMC_NPT && !even)
+    return c->fail(PTMC_ERR_ARG, "NPT long-range correction is defined for ELJPotentialEven only");
+  c->pot = even ? POT_ELJEVEN : POT_ELJ;
+  c->coeff.assign(coeff, coeff + K);
+  return PTMC_OK;
+}
+
+int ptmc_set_potential_eam(ptmc_ctx* c, double n, double m, double ean, double ecam) {
+  if (!c) return PTMC_ERR_ARG;
+  if (c->p.ensemble == PTMC_NPT) return c->fail(PTMC_ERR_ARG, "EAM is supported in the NVT ensemble only");
+  c->pot = POT_EAM;
+  c->eam[0] = n;
+  c->eam[1] = m;
+  c->eam[2] = ean;
+  c->eam[3] = ecam;
+  return PTMC_OK;
+}
+
+int ptmc_set_potential_nn(ptmc_ctx* c, const double*, int, const double*, int,
+                          const int*, int, double) {
+  if (!c) return PTMC_ERR_ARG;
+  return c->fail(PTMC_ERR_STATE, "RuNNerPotential: use ptmc_nn_* entry points (not in this build)");
+}
+
+int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N, int n_start,
+                         int bc_kind, double bc_param) {
+  if (!c || !xyz) return PTMC_ERR_ARG;
+  if (c->inited) return c->fail(PTMC_ERR_STATE, "configurations must be set before ptmc_init");
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  if (N < 2) return c->fail(PTMC_ERR_ARG, "need at least 2 atoms");
+  if (N > 1024) return c->fail(PTMC_ERR_LIMIT, "at most 1024 atoms per configuration");
+  if (n_start < 1) return c->fail(PTMC_ERR_ARG, "need at least one start configuration");
+  if (bc_kind != PTMC_BC_SPHERE && bc_kind != PTMC_BC_CUBIC)
+    return c->fail(PTMC_ERR_ARG, "unknown boundary condition");
+  if (!(bc_param > 0)) return c->fail(PTMC_ERR_ARG, "boundary parameter must be positive");
+  if (c->p.ensemble == PTMC_NPT && bc_kind != PTMC_BC_CUBIC)
+    return c->fail(PTMC_ERR_ARG, "SphericalBC cannot be used in an NPT ensemble.");  // Ensembles.jl:192
+  for (auto& r : c->runs)
+    if (r.bc >= 0 && r.bc != bc_kind)
+      return c->fail(PTMC_ERR_ARG, "all runs of a context share one boundary kind");
+  HostRun& h = c->runs[run];
+  h.N = N;
+  h.n_start = n_start;
+  h.bc = bc_kind;
+  h.bc_param = bc_param;
+  h.xyz.assign(xyz, xyz + (size_t)n_start * N * 3);
+  return PTMC_OK;
+}
+
+int ptmc_set_max_displ(ptmc_ctx* c, int run, const double* md) {
+  if (!c || !md) return PTMC_ERR_ARG;
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  c->runs[run].maxd.assign(md, md + 2 * c->R());
+  return PTMC_OK;
+}
+
+int ptmc_init(ptmc_ctx* c) {
+  if (!c) return PTMC_ERR_ARG;
+  if (c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init called twice");
+  if (c->pot < 0) return c->fail(PTMC_ERR_STATE, "no potential set");
+  for (auto& r : c->runs)
+    if (r.N == 0) return c->fail(PTMC_ERR_STATE, "every run needs start configurations");
+  const int R = c->R();
+  const bool npt = c->p.ensemble == PTMC_NPT;
+  // group runs by N: device order sorted by N (stable)
+  int nr = c->p.n_runs;
+  c->run_of_dev.resize(nr);
+  for (int i = 0; i < nr; ++i) c->run_of_dev[i] = i;
+  std::stable_sort(c->run_of_dev.begin(), c->run_of_dev.end(),
+                   [&](int a, int b) { return c->runs[a].N < c->runs[b].N; });
+  c->dev_of_run.resize(nr);
+  for (int d = 0; d < nr; ++d) c->dev_of_run[c->run_of_dev[d]] = d;
+  c->groups.clear();
+  for (int d = 0; d < nr; ++d) {
+    int N = c->runs[c->run_of_dev[d]].N;
+    if (c->groups.empty() || c->groups.back().N != N) c->groups.push_back({N, d, 0, nullptr});
+    c->groups.back().nruns++;
+  }
+  for (auto& G : c->groups) {
+    long long smem = cycles_smem_bytes(c->pot, c->p.ensemble, c->f32(), R, G.N);
+    if (smem > 227 * 1024)
+      return c->fail(PTMC_ERR_LIMIT, "replica state of a run exceeds 227 KB of shared memory (R*N too large)");
+    CK(cudaStreamCreateWithFlags(&G.st, cudaStreamNonBlocking));
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->evjoin.push_back(e);
+  }
+  // offsets
+  c->rd.assign(nr, RunDesc{});
+  long long po = 0, mo = 0, co = 0, ho = 0;
+  int wk = 0;
+  int nb = c->p.n_bin + 2;
+  int hstride = npt ? nb * nb : nb;
+  for (int d = 0; d < nr; ++d) {
+    const HostRun& h = c->runs[c->run_of_dev[d]];
+    RunDesc& r = c->rd[d];
+    r.N = h.N;
+    r.R = R;
+    r.wk = wk;
+    r.run_id = c->run_of_dev[d];
+    r.pos_off = po;
+    r.mat_off = mo;
+    r.comp_off = co;
+    r.hist_off = ho;
+    r.hist_stride = hstride;
+    r.cyc[0] = r.cyc[1] = r.cyc[2] = 1;
+    r.run_ctr = 0;
+    po += (long long)R * h.N * 3;
+    if (npt && !c->f32()) mo += (long long)R * h.N * h.N;
+    if (c->pot == POT_EAM) co += (long long)R * h.N * 2;
+    ho += (long long)R * hstride;
+    wk += R;
+  }
+  c->W = wk;
+  int W = wk;
+  if (c->d_runs.alloc(nr) || c->d_pos.alloc(po) || c->d_mat.alloc(mo) || c->d_comp.alloc(co) ||
+      c->d_en.alloc(W) || c->d_box.alloc(W) || c->d_rc2.alloc(W) || c->d_drift.alloc(W) ||
+      c->d_beta.alloc(W) || c->d_maxd.alloc(2 * W) || c->d_maxbox.alloc(W) ||
+      c->d_ham.alloc(2 * W) || c->d_ctr.alloc(W) || c->d_status.alloc(W) ||
+      c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho))
+    return c->fail(PTMC_ERR_CUDA, "device allocation failed");
+  // host images
+  std::vector<double> pos(po), box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W);
+  std::vector<int> wos(W);
+  for (int d = 0; d < nr; ++d) {
+    const HostRun& h = c->runs[c->run_of_dev[d]];
+    const RunDesc& r = c->rd[d];
+    for (int w = 0; w < R; ++w) {
+      const double* src = &h.xyz[(size_t)(w % h.n_start) * h.N * 3];
+      std::copy(src, src + (size_t)h.N * 3, &pos[r.pos_off + (size_t)w * h.N * 3]);
+      int g = r.wk + w;
+      box[g] = h.bc_param;
+      rc2[g] = h.bc == PTMC_BC_CUBIC ? h.bc_param * h.bc_param / 4 : 0.0;  // get_r_cut (Ensembles.jl:118)
+      beta[g] = c->beta[w];
+      maxd[2 * g] = h.maxd.empty() ? 0.1 : h.maxd[2 * w];       // MCStates.jl:104
+      maxd[2 * g + 1] = h.maxd.empty() ? 0.1 : h.maxd[2 * w + 1];
+      maxbox[g] = h.bc == PTMC_BC_CUBIC ? h.bc_param * 1.8 : 30.0;  // max_length (MCStates.jl:63-75)
+      wos[g] = w;
+    }
+  }
+  cudaStream_t s = c->st;
+  CK(cudaMemcpyAsync(c->d_pos.p, pos.data(), sizeof(double) * po, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_box.p, box.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_rc2.p, rc2.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_beta.p, beta.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_maxd.p, maxd.data(), sizeof(double) * 2 * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_maxbox.p, maxbox.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_wos.p, wos.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(unsigned long long) * W, s));
+  CK(cudaMemsetAsync(c->d_ham.p, 0, sizeof(double) * 2 * W, s));
+  CK(cudaMemsetAsync(c->d_cnt.p, 0, sizeof(long long) * 6 * W, s));
+  CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned int) * std::max<long long>(ho, 1), s));
+  int rc = push_runs(c);
+  if (rc) return rc;
+  KParams& K = c->K;
+  K.runs = c->d_runs.p;
+  K.pos = c->d_pos.p;
+  K.mat = c->d_mat.p;
+  K.comp = c->d_comp.p;
+  K.en = c->d_en.p;
+  K.box = c->d_box.p;
+  K.rc2 = c->d_rc2.p;
+  K.drift = c->d_drift.p;
+  K.ctr = c->d_ctr.p;
+  K.status = c->d_status.p;
+  K.beta = c->d_beta.p;
+  K.maxd = c->d_maxd.p;
+  K.maxbox = c->d_maxbox.p;
+  K.ham = c->d_ham.p;
+  K.cnt = c->d_cnt.p;
+  K.wos = c->d_wos.p;
+  K.hist = c->d_hist.p;
+  K.K = (int)c->coeff.size();
+  for (int k = 0; k < MAX_COEFF; ++k) K.c[k] = k < K.K ? c->coeff[k] : 0.0;
+  K.eam_n = c->eam[0];
+  K.eam_m = c->eam[1];
+  K.eam_ean = c->eam[2];
+  K.eam_ecam = c->eam[3];
+  K.pressure = c->p.pressure;
+  K.exch_prob = c->p.exch_prob;
+  K.min_acc = c->p.min_acc;
+  K.max_acc = c->p.max_acc;
+  K.n_bin = c->p.n_bin;
+  K.n_adjust = c->p.n_adjust;
+  K.mc_sample = c->p.mc_sample;
+  K.resync_every = c->p.resync_every;
+  K.seed = c->p.seed;
+  for (auto& G : c->groups) {
+    int e = launch_init(c->pot, c->bc(), c->p.ensemble, c->f32(), K, G.dev0, G.nruns, R, s);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_init launch");
+    c->stats.kernel_launches += 1;
+  }
+  CK(cudaStreamSynchronize(s));
+  c->inited = true;
+  return PTMC_OK;
+}
+
+int ptmc_cycles_nosample(ptmc_ctx* c, long long n) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  return run_phase(c, n, PHASE_PLAIN);
+}
+
+int ptmc_equilibrate(ptmc_ctx* c) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (c->equilibrated) return c->fail(PTMC_ERR_STATE, "already equilibrated");
+  long long eq = c->p.eq_cycles;
+  int rc = run_phase(c, eq / 2, PHASE_EQ);  // only half is simulated (MCRun.jl:296-298)
+  if (rc) return rc;
+  int R = c->R(), W = c->W;
+  std::vector<double> en(W), box(W);
+  std::vector<int> wos(W);
+  CK(cudaMemcpyAsync(en.data(), c->d_en.p, sizeof(double) * W, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(box.data(), c->d_box.p, sizeof(double) * W, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(wos.data(), c->d_wos.p, sizeof(int) * W, cudaMemcpyDeviceToHost, c->st));
+  rc = pull_runs(c);
+  if (rc) return rc;
+  for (auto& r : c->rd) {
+    double eb[2] = {100.0, -100.0};  // check_e_bounds (MCRun.jl:258-265, 299-303)
+    for (long long i = eq / 2 + 1; i <= eq; ++i)
+      for (int s = 0; s < R; ++s) {
+        double e = en[r.wk + wos[r.wk + s]];
+        if (e < eb[0]) eb[0] = e;
+        else if (e > eb[1]) eb[1] = e;
+      }
+    // initialise_histograms! (Sampling.jl:141-194)
+    r.en_min = eb[0];
+    r.en_max = eb[1];
+    r.dE = (r.en_max - r.en_min) / (c->p.n_bin - 1);
+    if (c->p.ensemble == PTMC_NPT) {
+      double L = box[r.wk + wos[r.wk + 0]];
+      double V = L * L * L;
+      r.v_min = V * 0.8;
+      r.v_max = V * 2.0;
+      r.dV = (r.v_max - r.v_min) / c->p.n_bin;
+    }
+  }
+  c->equilibrated = true;
+  rc = push_runs(c);
+  if (rc) return rc;
+  // reset_counters (MCRun.jl:271-277)
+  CK(cudaMemsetAsync(c->d_cnt.p, 0, sizeof(long long) * 6 * W, c->st));
+  CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned int) * std::max<size_t>(c->d_hist.n, 1), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+int ptmc_run_cycles(ptmc_ctx* c, long long n) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->equilibrated) return c->fail(PTMC_ERR_STATE, "ptmc_equilibrate not called");
+  return run_phase(c, n, PHASE_PROD);
+}
+
+int ptmc_resync(ptmc_ctx* c) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  for (auto& G : c->groups) {
+    int e = launch_resync(c->pot, c->bc(), c->p.ensemble, c->f32(), c->K, G.dev0, G.nruns, c->R(), c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_resync launch");
+    c->stats.kernel_launches += 1;
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+int ptmc_get_states(ptmc_ctx* c, int run, double* xyz, double* en_tot, double* box,
+                    double* max_displ, long long* counts, double* ham) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  const RunDesc& r = c->rd[c->dev_of_run[run]];
+  int R = c->R(), N = r.N;
+  std::vector<double> pos((size_t)R * N * 3), en(R), bx(R), md(2 * R), hm(2 * R);
+  std::vector<int> wos(R);
+  std::vector<long long> cnt(6 * R);
+  cudaStream_t s = c->st;
+  CK(cudaMemcpyAsync(pos.data(), c->d_pos.p + r.pos_off, sizeof(double) * pos.size(), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(en.data(), c->d_en.p + r.wk, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(bx.data(), c->d_box.p + r.wk, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(md.data(), c->d_maxd.p + 2 * r.wk, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hm.data(), c->d_ham.p + 2 * r.wk, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(cnt.data(), c->d_cnt.p + 6 * (size_t)r.wk, sizeof(long long) * 6 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wos.data(), c->d_wos.p + r.wk, sizeof(int) * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int slot = 0; slot < R; ++slot) {
+    int w = wos[slot];
+    if (xyz) std::copy(&pos[(size_t)w * N * 3], &pos[(size_t)w * N * 3] + (size_t)N * 3, xyz + (size_t)slot * N * 3);
+    if (en_tot) en_tot[slot] = en[w];
+    if (box) box[slot] = bx[w];
+  }
+  if (max_displ) std::copy(md.begin(), md.end(), max_displ);
+  if (counts) std::copy(cnt.begin(), cnt.end(), counts);
+  if (ham) std::copy(hm.begin(), hm.end(), ham);
+  return PTMC_OK;
+}
+
+int ptmc_get_output(ptmc_ctx* c, int run, ptmc_output* o) {
+  if (!c || !o) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  int rc = pull_runs(c);
+  if (rc) return rc;
+  const RunDesc& r = c->rd[c->dev_of_run[run]];
+  int R = c->R();
+  std::vector<double> md(2 * R), hm(2 * R);
+  std::vector<long long> cnt(6 * R);
+  std::vector<unsigned int> h((size_t)R * r.hist_stride);
+  cudaStream_t s = c->st;
+  CK(cudaMemcpyAsync(md.data(), c->d_maxd.p + 2 * r.wk, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hm.data(), c->d_ham.p + 2 * r.wk, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(cnt.data(), c->d_cnt.p + 6 * (size_t)r.wk, sizeof(long long) * 6 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h.data(), c->d_hist.p + r.hist_off, sizeof(unsigned int) * h.size(), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  // finalise_results (Sampling.jl:377-399)
+  double n_sample = (double)c->p.mc_cycles / (double)c->p.mc_sample;
+  for (int i = 0; i < R; ++i) {
+    double ea = hm[2 * i] / n_sample, e2 = hm[2 * i + 1] / n_sample;
+    if (o->en_avg) o->en_avg[i] = ea;
+    if (o->heat_cap) o->heat_cap[i] = (e2 - ea * ea) * (c->beta[i] * c->beta[i]);
+    if (o->count_stat_atom)
+      o->count_stat_atom[i] = (double)cnt[6 * i] / (double)((long long)r.N * c->p.mc_cycles);
+    if (o->count_stat_vol) o->count_stat_vol[i] = (double)cnt[6 * i + 2] / (double)c->p.mc_cycles;
+    if (o->count_stat_exc) o->count_stat_exc[i] = (double)cnt[6 * i + 5] / (double)cnt[6 * i + 4];
+  }
+  if (o->max_displ) std::copy(md.begin(), md.end(), o->max_displ);
+  if (o->en_histogram && c->p.ensemble == PTMC_NVT)
+    for (size_t k = 0; k < h.size(); ++k) o->en_histogram[k] = (double)h[k];
+  if (o->ev_histogram && c->p.ensemble == PTMC_NPT)
+    for (size_t k = 0; k < h.size(); ++k) o->ev_histogram[k] = (double)h[k];
+  o->hist_params[0] = r.en_min;
+  o->hist_params[1] = r.en_max;
+  o->hist_params[2] = r.v_min;
+  o->hist_params[3] = r.v_max;
+  o->hist_params[4] = r.dE;
+  o->hist_params[5] = r.dV;
+  return PTMC_OK;
+}
+
+int ptmc_get_stats(ptmc_ctx* c, ptmc_stats* s) {
+  if (!c || !s) return PTMC_ERR_ARG;
+  *s = c->stats;
+  if (c->inited) {
+    std::vector<double> d(c->W);
+    CK(cudaMemcpy(d.data(), c->d_drift.p, sizeof(double) * c->W, cudaMemcpyDeviceToHost));
+    double m = 0;
+    for (double x : d) m = std::max(m, x);
+    s->max_drift = m;
+  }
+  return PTMC_OK;
+}
+
+void ptmc_destroy(ptmc_ctx* c) {
+  if (!c) return;
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& G : c->groups)
+    if (G.st) cudaStreamDestroy(G.st);
+  for (auto e : c->evjoin) cudaEventDestroy(e);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->evfork) cudaEventDestroy(c->evfork);
+  c->d_runs.free_();
+  c->d_pos.free_();
+  c->d_mat.free_();
+  c->d_comp.free_();
+  c->d_en.free_();
+  c->d_box.free_();
+  c->d_rc2.free_();
+  c->d_drift.free_();
+  c->d_beta.free_();
+  c->d_maxd.free_();
+  c->d_maxbox.free_();
+  c->d_ham.free_();
+  c->d_ctr.free_();
+  c->d_status.free_();
+  c->d_wos.free_();
+  c->d_cnt.free_();
+  c->d_hist.free_();
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- checkpoint
+// Reference text formats (src/ReadSave.jl) for run 0, plus engine.bin with the
+// complete binary state of every run for exact resume.
+namespace {
+template <typename T>
+void put(std::string& b, const T* p, size_t n) {
+  b.append((const char*)p, n * sizeof(T));
+}
+template <typename T>
+int dump(ptmc_ctx* c, std::string& b, const DBuf<T>& d) {
+  std::vector<T> h(d.n);
+  if (d.n) CK(cudaMemcpy(h.data(), d.p, sizeof(T) * d.n, cudaMemcpyDeviceToHost));
+  unsigned long long n = d.n;
+  put(b, &n, 1);
+  put(b, h.data(), h.size());
+  return PTMC_OK;
+}
+template <typename T>
+int undump(ptmc_ctx* c, const std::string& b, size_t& at, DBuf<T>& d) {
+  unsigned long long n = 0;
+  if (at + sizeof(n) > b.size()) return c->fail(PTMC_ERR_IO, "engine.bin truncated");
+  std::memcpy(&n, b.data() + at, sizeof(n));
+  at += sizeof(n);
+  if (n != d.n) return c->fail(PTMC_ERR_IO, "engine.bin does not match this context's layout");
+  if (at + n * sizeof(T) > b.size()) return c->fail(PTMC_ERR_IO, "engine.bin truncated");
+  if (n) CK(cudaMemcpy(d.p, b.data() + at, sizeof(T) * n, cudaMemcpyHostToDevice));
+  at += n * sizeof(T);
+  return PTMC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
+  if (!c || !dir) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  CK(cudaStreamSynchronize(c->st));
+  ::mkdir(dir, 0755);
+  std::string d(dir);
+  int rc = pull_runs(c);
+  if (rc) return rc;
+  const int R = c->R();
+  const RunDesc& r0 = c->rd[c->dev_of_run[0]];
+  const int N = r0.N;
+  const bool npt = c->p.ensemble == PTMC_NPT;
+  // params.data (save_init/writeparams/writeensemble/writepotential, :24-110)
+  std::string s = "cycles: sample_rate: n_traj: n_atoms: n_adjust n_bins min_acc: max_acc t_i: t_f\n";
+  double pv[10] = {(double)c->p.mc_cycles, (double)c->p.mc_sample, (double)R, (double)N,
+                   (double)c->p.n_adjust, (double)c->p.n_bin, c->p.min_acc, c->p.max_acc,
+                   c->T.front(), c->T.back()};
+  for (int k = 0; k < 10; ++k) s += fmt_double(pv[k]) + (k < 9 ? " " : "\n");
+  if (npt) {
+    s += "ensemble n_atom_moves n_volume_moves n_atom_swaps pressure separated_volume\n";
+    s += "NPT " + std::to_string(N) + " " + std::to_string(N) + " 1 0 " + fmt_double(c->p.pressure) + " false\n";
+  } else {
+    s += "ensemble n_atom_moves n_atom_swaps\n";
+    s += "NVT " + std::to_string(N) + " " + std::to_string(N) + " 0\n";
+  }
+  if (c->pot == POT_EAM) {
+    s += "EAM: " + fmt_double(c->eam[0]) + " " + fmt_double(c->eam[1]) + " " + fmt_double(c->eam[2]) +
+         " " + fmt_double(c->eam[3]) + " \n";
+  } else {
+    s += std::string(c->pot == POT_ELJEVEN ? "ELJPotentialEven{" : "ELJPotential{") +
+         std::to_string(c->coeff.size()) + ", Float64}";
+    for (double x : c->coeff) s += " " + fmt_double(x);
+    s += "\n";
+  }
+  if (!write_file_atomic(d + "/params.data", s)) return c->fail(PTMC_ERR_IO, "cannot write params.data");
+  // hist_info.data (save_histparams, :117-127)
+  s = "e_min e_max v_min v_max \xce\x94_E \xce\x94_V \xce\x94_r2\n";
+  double hv[7] = {r0.en_min, r0.en_max, r0.v_min, r0.v_max, r0.dE, r0.dV, 0.0};
+  for (int k = 0; k < 7; ++k) s += fmt_double(hv[k]) + (k < 6 ? " " : "\n");
+  if (!write_file_atomic(d + "/hist_info.data", s)) return c->fail(PTMC_ERR_IO, "cannot write hist_info.data");
+  // histograms (checkpoint, :178-218)
+  std::vector<unsigned int> h((size_t)R * r0.hist_stride);
+  CK(cudaMemcpy(h.data(), c->d_hist.p + r0.hist_off, sizeof(unsigned int) * h.size(), cudaMemcpyDeviceToHost));
+  int nb = c->p.n_bin + 2;
+  s.clear();
+  for (int i = 0; i < R; ++i) {
+    for (int m = 0; m < nb; ++m) {
+      double v = npt ? 0.0 : (double)h[(size_t)i * r0.hist_stride + m];
+      s += fmt_double(v) + (m < nb - 1 ? "\t" : "\n");
+    }
+  }
+  if (!write_file_atomic(d + "/histograms.data", s)) return c->fail(PTMC_ERR_IO, "cannot write histograms.data");
+  if (npt) {  // one row per replica, matrix flattened column-major (setresults :404-412)
+    s.clear();
+    for (int i = 0; i < R; ++i)
+      for (int col = 0; col < nb; ++col)
+        for (int rw = 0; rw < nb; ++rw) {
+          double v = (double)h[(size_t)i * r0.hist_stride + (size_t)rw * nb + col];
+          s += fmt_double(v) + ((col == nb - 1 && rw == nb - 1) ? "\n" : "\t");
+        }
+    if (!write_file_atomic(d + "/volume_hist.data", s)) return c->fail(PTMC_ERR_IO, "cannot write volume_hist.data");
+  }
+  long long index = r0.cyc[PHASE_PROD] - 1;
+  if (!write_file_atomic(d + "/index.txt", std::to_string(index) + "\n"))
+    return c->fail(PTMC_ERR_IO, "cannot write index.txt");
+  // configT<i>.xyz (checkpoint_config, :142-158)
+  std::vector<double> xyz((size_t)R * N * 3), en(R), box(R), md(2 * R), ham(2 * R);
+  std::vector<long long> cnt(6 * R);
+  rc = ptmc_get_states(c, 0, xyz.data(), en.data(), box.data(), md.data(), cnt.data(), ham.data());
+  if (rc) return rc;
+  for (int i = 0; i < R; ++i) {
+    std::string t = std::to_string(N) + "\n";
+    if (c->bc() == PTMC_BC_SPHERE) t += "SphericalBC{Float64} r2: " + fmt_double(box[i] * box[i]);
+    else t += "CubicBC{Float64} box_length: " + fmt_double(box[i]);
+    t += " " + fmt_double(md[2 * i]) + " " + fmt_double(md[2 * i + 1]) + " " + fmt_double(0.1) + " " +
+         std::to_string(cnt[6 * i]) + " " + std::to_string(cnt[6 * i + 2]) + "\n";
+    for (int a = 0; a < N; ++a) {
+      const double* x = &xyz[((size_t)i * N + a) * 3];
+      t += "1  " + fmt_double(x[0]) + " " + fmt_double(x[1]) + " " + fmt_double(x[2]) + " \n";
+    }
+    if (!write_file_atomic(d + "/configT" + std::to_string(i + 1) + ".xyz", t))
+      return c->fail(PTMC_ERR_IO, "cannot write configT.xyz");
+  }
+  // engine.bin: complete state
+  std::string b = "PTMCGB01";
+  unsigned long long hdr[4] = {(unsigned long long)c->p.n_runs, (unsigned long long)R,
+                               (unsigned long long)c->W, (unsigned long long)c->equilibrated};
+  put(b, hdr, 4);
+  put(b, c->rd.data(), c->rd.size());
+  if ((rc = dump(c, b, c->d_pos)) || (rc = dump(c, b, c->d_mat)) || (rc = dump(c, b, c->d_comp)) ||
+      (rc = dump(c, b, c->d_en)) || (rc = dump(c, b, c->d_box)) || (rc = dump(c, b, c->d_rc2)) ||
+      (rc = dump(c, b, c->d_drift)) || (rc = dump(c, b, c->d_beta)) || (rc = dump(c, b, c->d_maxd)) ||
+      (rc = dump(c, b, c->d_maxbox)) || (rc = dump(c, b, c->d_ham)) || (rc = dump(c, b, c->d_ctr)) ||
+      (rc = dump(c, b, c->d_status)) || (rc = dump(c, b, c->d_wos)) || (rc = dump(c, b, c->d_cnt)) ||
+      (rc = dump(c, b, c->d_hist)))
+    return rc;
+  put(b, "PTMCEND!", 8);
+  if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
+  return PTMC_OK;
+}
+
+int ptmc_restore(ptmc_ctx* c, const char* dir) {
+  if (!c || !dir) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "call ptmc_init before ptmc_restore");
+  std::string path = std::string(dir) + "/engine.bin";
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return c->fail(PTMC_ERR_IO, "cannot open " + path);
+  std::string b;
+  char buf[1 << 16];
+  size_t k;
+  while ((k = std::fread(buf, 1, sizeof(buf), f)) > 0) b.append(buf, k);
+  std::fclose(f);
+  if (b.size() < 8 + 32 || b.compare(0, 8, "PTMCGB01") != 0)
+    return c->fail(PTMC_ERR_IO, "engine.bin: bad magic");
+  if (b.size() < 8 || b.compare(b.size() - 8, 8, "PTMCEND!") != 0)
+    return c->fail(PTMC_ERR_IO, "engine.bin truncated (no end marker)");
+  unsigned long long hdr[4];
+  std::memcpy(hdr, b.data() + 8, sizeof(hdr));
+  if (hdr[0] != (unsigned long long)c->p.n_runs || hdr[1] != (unsigned long long)c->R() ||
+      hdr[2] != (unsigned long long)c->W)
+    return c->fail(PTMC_ERR_IO, "engine.bin was written by a context with other dimensions");
+  size_t at = 8 + sizeof(hdr);
+  if (at + sizeof(RunDesc) * c->rd.size() > b.size()) return c->fail(PTMC_ERR_IO, "engine.bin truncated");
+  std::vector<RunDesc> rd(c->rd.size());
+  std::memcpy(rd.data(), b.data() + at, sizeof(RunDesc) * rd.size());
+  at += sizeof(RunDesc) * rd.size();
+  for (size_t i = 0; i < rd.size(); ++i)
+    if (rd[i].N != c->rd[i].N || rd[i].pos_off != c->rd[i].pos_off)
+      return c->fail(PTMC_ERR_IO, "engine.bin run layout does not match");
+  int rc;
+  if ((rc = undump(c, b, at, c->d_pos)) || (rc = undump(c, b, at, c->d_mat)) ||
+      (rc = undump(c, b, at, c->d_comp)) || (rc = undump(c, b, at, c->d_en)) ||
+      (rc = undump(c, b, at, c->d_box)) || (rc = undump(c, b, at, c->d_rc2)) ||
+      (rc = undump(c, b, at, c->d_drift)) || (rc = undump(c, b, at, c->d_beta)) ||
+      (rc = undump(c, b, at, c->d_maxd)) || (rc = undump(c, b, at, c->d_maxbox)) ||
+      (rc = undump(c, b, at, c->d_ham)) || (rc = undump(c, b, at, c->d_ctr)) ||
+      (rc = undump(c, b, at, c->d_status)) || (rc = undump(c, b, at, c->d_wos)) ||
+      (rc = undump(c, b, at, c->d_cnt)) || (rc = undump(c, b, at, c->d_hist)))
+    return rc;
+  c->rd = rd;
+  c->equilibrated = hdr[3] != 0;
+  rc = push_runs(c);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// ---------------------------------------------------------------- WHAM
+static int wham_common(bool npt, int R, int n_bin, const double* hist,
+                       const double* t_grid, const double* beta, double en_min,
+                       double en_max, double v_min, double v_max, double pr,
+                       double thr, double* T_out, double* cv_out, int* iters) {
+  if (R < 1 || n_bin < 1 || !hist || !t_grid || !beta || !T_out || !cv_out) {
+    g_err = "multihistogram: bad arguments";
+    return PTMC_ERR_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    g_err = "multihistogram: no CUDA device";
+    return PTMC_ERR_CUDA;
+  }
+  int n_out = 10 * R;  // temp_trajectories (multihist_NVT.jl:11-15)
+  std::vector<double> tb(2 * n_out);
+  for (int i = 0; i < n_out; ++i) {  // TempGrid{10R}(t_1, t_R) geometric (:29-34)
+    double T = n_out == 1 ? t_grid[0]
+                          : t_grid[0] * std::pow(t_grid[R - 1] / t_grid[0], (double)i / (double)(n_out - 1));
+    tb[i] = 1.0 / (kB * T);
+    tb[n_out + i] = T;
+  }
+  long long nb = n_bin + 2;
+  long long hn = npt ? (long long)R * nb * nb : (long long)R * nb;
+  long long B = npt ? (long long)n_bin * n_bin : n_bin;
+  long long nwork = wham_work_doubles(R, (int)B);
+  double *dh = nullptr, *db = nullptr, *dtb = nullptr, *dw = nullptr, *dout = nullptr;
+  int* dit = nullptr;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+  chk(cudaMalloc(&dh, sizeof(double) * hn));
+  chk(cudaMalloc(&db, sizeof(double) * R));
+  chk(cudaMalloc(&dtb, sizeof(double) * 2 * n_out));
+  chk(cudaMalloc(&dw, sizeof(double) * nwork));
+  chk(cudaMalloc(&dout, sizeof(double) * n_out));
+  chk(cudaMalloc(&dit, sizeof(int)));
+  if (e == cudaSuccess) {
+    chk(cudaMemcpy(dh, hist, sizeof(double) * hn, cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(db, beta, sizeof(double) * R, cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(dtb, tb.data(), sizeof(double) * 2 * n_out, cudaMemcpyHostToDevice));
+  }
+  if (e == cudaSuccess) {
+    int rc = npt ? wham_npt_device(R, n_bin, dh, db, en_min, en_max, v_min, v_max, pr, thr, dtb,
+                                   n_out, dw, dout, dit, nullptr)
+                 : wham_nvt_device(R, n_bin, dh, db, en_min, en_max, thr, dtb, n_out, dw, dout,
+                                   dit, nullptr);
+    if (rc) e = (cudaError_t)rc;
+  }
+  if (e == cudaSuccess) chk(cudaMemcpy(cv_out, dout, sizeof(double) * n_out, cudaMemcpyDeviceToHost));
+  int it = 0;
+  if (e == cudaSuccess) chk(cudaMemcpy(&it, dit, sizeof(int), cudaMemcpyDeviceToHost));
+  cudaFree(dh);
+  cudaFree(db);
+  cudaFree(dtb);
+  cudaFree(dw);
+  cudaFree(dout);
+  cudaFree(dit);
+  if (e != cudaSuccess) {
+    g_err = std::string("multihistogram: ") + cudaGetErrorString(e);
+    return PTMC_ERR_CUDA;
+  }
+  for (int i = 0; i < n_out; ++i) T_out[i] = tb[n_out + i];
+  if (iters) *iters = it;
+  return PTMC_OK;
+}
+
+int ptmc_multihist_nvt(int R, int n_bin, const double* en_hist, const double* t_grid,
+                       const double* beta, double en_min, double en_max, double thr,
+                       double* T_out, double* cv_out, int* iters) {
+  return wham_common(false, R, n_bin, en_hist, t_grid, beta, en_min, en_max, 0, 0, 0, thr,
+                     T_out, cv_out, iters);
+}
+
+int ptmc_multihist_npt(int R, int n_bin, const double* ev_hist, const double* t_grid,
+                       const double* beta, double en_min, double en_max, double v_min,
+                       double v_max, double pressure, double thr, double* T_out,
+                       double* cp_out, int* iters) {
+  return wham_common(true, R, n_bin, ev_hist, t_grid, beta, en_min, en_max, v_min, v_max,
+                     pressure, thr, T_out, cp_out, iters);
+}
+
+}  // extern "C"

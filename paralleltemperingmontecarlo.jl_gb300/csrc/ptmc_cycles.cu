@@ -1,0 +1,782 @@
+// ptmc_cycles.cu — replica-cycle kernels of the GB300 PT-MC engine.
+//
+// Execution model.  One CTA runs one PT run; one warp owns one walker.  A
+// walker is the configuration-bound part of an MCState (positions, distance
+// matrix, energy, potential variables, box, draw stream); a slot is the
+// temperature-bound part (beta, max_displ, counters, E/E^2 sums, histogram
+// row).  The reference swaps whole configurations between temperature slots on
+// an accepted exchange (src/Exchange.jl:115-124); here the exchange swaps the
+// walker<->slot index, which is the same transition and moves no data.
+//
+// Per cycle (mc_cycle!, src/MCRun.jl:192-253): every warp makes n_steps moves
+// of its walker (mc_step!/mc_move!, src/MCRun.jl:142-182) with positions and
+// per-atom potential variables in shared memory and the move's pair terms
+// spread over the 32 lanes (warp-shuffle reductions give dE); then, after a
+// CTA barrier, thread 0 makes the exchange draw (parallel_tempering_exchange!,
+// src/Exchange.jl:132-180), threads 0..R-1 adapt step sizes
+// (update_max_stepsize!, src/Exchange.jl:198-257) and sample
+// (sampling_step!, src/Sampling.jl:330-371).  The loop runs `ncycles` cycles
+// per launch; there are no spin-waits and no inter-CTA communication.
+//
+// Draw order per move (both forms, identical to the CPU oracle): slot index
+// (rand(1:n_steps)), 3 displacement draws (+3 per spherical retry), the
+// acceptance draw; volume move: scale draw, acceptance draw.
+//
+// Forms.  FP64 (plain): every quantity in FP64; proposals and squared
+// distances use non-contracted IEEE operations, so they are bit-identical to
+// the reference's; pair energies use FMA Horner forms (agree to ~1e-16
+// relative).  FP32_RESYNC: positions stay FP64 (exact proposals), the pair
+// terms of a move are FP32 (MUFU lg2/ex2 for the EAM powers), the running
+// total is FP64, and every `resync_every` cycles each walker recomputes its
+// energy (and EAM components) in FP64, recording the drift.
+#include <cuda_runtime.h>
+
+#include "ptmc_device.cuh"
+#include "ptmc_engine.cuh"
+
+namespace ptmc {
+
+// ------------------------------------------------------------ pair energies
+// ELJPotentialEven (src/EnergyEvaluation.jl:934-942): sum_k c_k r^-(6+2k)
+__device__ __forceinline__ double v_even64(const double* c, int K, double r2) {
+  double inv = 1.0 / r2;
+  double v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fma(v, inv, c[k]);
+  return v * (inv * inv * inv);
+}
+// ELJPotential (src/EnergyEvaluation.jl:923-932): sum_k c_k r^-(6+k)
+__device__ __forceinline__ double v_all64(const double* c, int K, double r2) {
+  double ir = 1.0 / sqrt(r2);
+  double inv = ir * ir;
+  double v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fma(v, ir, c[k]);
+  return v * (inv * inv * inv);
+}
+__device__ __forceinline__ float v_even32(const float* c, int K, float r2) {
+  float inv = rcpf(r2);
+  float v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fmaf(v, inv, c[k]);
+  return v * (inv * inv * inv);
+}
+__device__ __forceinline__ float v_all32(const float* c, int K, float r2) {
+  float ir = rsqrtf(r2);
+  float inv = ir * ir;
+  float v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fmaf(v, ir, c[k]);
+  return v * (inv * inv * inv);
+}
+template <int POT>
+__device__ __forceinline__ double v64(const double* c, int K, double r2) {
+  return POT == POT_ELJ ? v_all64(c, K, r2) : v_even64(c, K, r2);
+}
+template <int POT>
+__device__ __forceinline__ float v32(const float* c, int K, float r2) {
+  return POT == POT_ELJ ? v_all32(c, K, r2) : v_even32(c, K, r2);
+}
+// lrc (src/EnergyEvaluation.jl:968-982); rc2 is the squared cut-off
+__device__ double lrc64(int N, double rc2, const double* c, int K) {
+  if (rc2 <= 50) return 0.0;
+  double rcs = sqrt(rc2);
+  double rc3 = rc2 * rcs;
+  double e = 0.0;
+  for (int i = 1; i <= K; ++i) {
+    e += c[i - 1] / rc3 / (2 * i + 1);
+    rc3 *= rc2;
+  }
+  e *= 3.141592653589793 * (double)(N * N) / 4 / (rcs * rcs * rcs);
+  return e;
+}
+// invrexp (src/EnergyEvaluation.jl:1088-1095): (r^-n, r^-m) from r^2
+__device__ __forceinline__ void invrexp64(double r2, double hn, double hm,
+                                          double& a, double& b) {
+  if (r2 != 0.0) {
+    double lg = log(r2);
+    a = exp(hn * lg);
+    b = exp(hm * lg);
+  } else {
+    a = 0.0;
+    b = 0.0;
+  }
+}
+
+template <int BC>
+__device__ __forceinline__ double pd2(double ax, double ay, double az,
+                                      const double* b, double L) {
+  return BC == BC_CUB ? d2_cub(ax, ay, az, b[0], b[1], b[2], L)
+                      : d2_sph(ax, ay, az, b[0], b[1], b[2]);
+}
+template <int BC>
+__device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
+  float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+  if (BC == BC_CUB) return f2_cub(dx, dy, dz, L, iL);
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// ------------------------------------------------------------ FP64 energy of
+// one walker from positions (init and resync).  ELJ: dimer_energy_config
+// (src/EnergyEvaluation.jl:378-420); EAM: set_variables + energy
+// (src/EnergyEvaluation.jl:1800-1810, 1156-1162).  Writes the NPT distance
+// matrix (plain form) and the EAM components when the pointers are given.
+template <int POT, int BC, int ENS>
+__device__ double walker_energy64(const double* X, int N, double L, double rc2,
+                                  const double* c, int K, double hn, double hm,
+                                  double ean, double ecam, double* M,
+                                  double* comp64, float2* comp32, int lane) {
+  double e = 0.0;
+  if (POT == POT_EAM) {
+    for (int k = lane; k < N; k += 32) {
+      double a = 0.0, b = 0.0;
+      for (int j = 0; j < N; ++j) {
+        if (j == k) continue;
+        double x = pd2<BC>(X[3 * k], X[3 * k + 1], X[3 * k + 2], X + 3 * j, L);
+        double pa, pb;
+        invrexp64(x, hn, hm, pa, pb);
+        a += pa;
+        b += pb;
+      }
+      if (comp64) {
+        comp64[2 * k] = a;
+        comp64[2 * k + 1] = b;
+      }
+      if (comp32) comp32[k] = make_float2((float)a, (float)b);
+      e += ean * a - ecam * sqrt(b);
+    }
+    return warp_sum(e);
+  }
+  for (int i = 0; i < N; ++i) {
+    double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+    for (int j = i + 1 + lane; j < N; j += 32) {
+      double x = pd2<BC>(xi, yi, zi, X + 3 * j, L);
+      if (M) {
+        M[(size_t)i * N + j] = x;
+        M[(size_t)j * N + i] = x;
+      }
+      if (ENS == ENS_NPT && !(x <= rc2)) continue;
+      e += v64<POT>(c, K, x);
+    }
+    if (M && lane == 0) M[(size_t)i * N + i] = 0.0;
+  }
+  e = warp_sum(e);
+  if (ENS == ENS_NPT) e = e + lrc64(N, rc2, c, K);
+  return e;
+}
+
+// ------------------------------------------------------------ init kernel
+// MCState constructor (src/MCStates.jl:137-162): distance matrix, potential
+// variables and initial energy of every walker, in FP64, from HBM positions.
+template <int POT, int BC, int ENS, bool F32>
+__global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
+  const RunDesc rd = P.runs[run0 + blockIdx.x];
+  const int N = rd.N, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w >= rd.R) return;
+  const int g = rd.wk + w;
+  const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
+  double* M = (ENS == ENS_NPT && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
+  double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
+  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.rc2[g], P.c, P.K,
+                                           -0.5 * P.eam_n, -0.5 * P.eam_m,
+                                           P.eam_ean, P.eam_ecam, M, comp,
+                                           nullptr, lane);
+  if (lane == 0) {
+    P.en[g] = e;
+    P.status[g] = ST_OK;
+    P.drift[g] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------ cycle kernel
+template <int POT, int BC, int ENS, bool F32>
+__global__ void __launch_bounds__(1024)
+    k_cycles(KParams P, int run0, int ncycles, int phase) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double s_c[MAX_COEFF];
+  __shared__ float s_cf[MAX_COEFF];
+  const RunDesc rd = P.runs[run0 + blockIdx.x];
+  const int N = rd.N, R = rd.R;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int nthr = blockDim.x;
+  const int K = P.K;
+  const int n_steps = ENS == ENS_NPT ? N + 1 : N;
+
+  // ---- carve shared memory (order matches cycles_smem_bytes) ----
+  unsigned char* sp = smem_raw;
+  auto carve = [&](long long bytes) {
+    unsigned char* p = sp;
+    sp += (bytes + 15) / 16 * 16;
+    return p;
+  };
+  double* s_pos = (double*)carve((long long)R * N * 3 * 8);
+  float4* s_p32 = F32 ? (float4*)carve((long long)R * N * 16) : nullptr;
+  double2* s_c64 = nullptr;
+  double2* s_d64 = nullptr;
+  float2* s_c32 = nullptr;
+  float2* s_d32 = nullptr;
+  if (POT == POT_EAM) {
+    if (F32) {
+      s_c32 = (float2*)carve((long long)R * N * 8);
+      s_d32 = (float2*)carve((long long)R * N * 8);
+    } else {
+      s_c64 = (double2*)carve((long long)R * N * 16);
+      s_d64 = (double2*)carve((long long)R * N * 16);
+    }
+  }
+  double* s_row = (ENS == ENS_NPT && !F32) ? (double*)carve((long long)R * N * 8) : nullptr;
+  double* s_drw = (double*)carve((long long)R * DRAW_BUF * 8);
+  double* s_beta = (double*)carve((long long)R * 8);
+  double* s_maxbox = (double*)carve((long long)R * 8);
+  double* s_en = (double*)carve((long long)R * 8);
+  double* s_box = (double*)carve((long long)R * 8);
+  double* s_ham = (double*)carve((long long)R * 16);
+  double* s_maxd = (double*)carve((long long)R * 16);
+  long long* s_cnt = (long long*)carve((long long)R * 48);
+  int* s_wos = (int*)carve((long long)R * 4);
+  int* s_sow = (int*)carve((long long)R * 4);
+
+  // ---- load the run into shared memory ----
+  if (tid < K) {
+    s_c[tid] = P.c[tid];
+    s_cf[tid] = (float)P.c[tid];
+  }
+  const double* gpos = P.pos + rd.pos_off;
+  for (int k = tid; k < R * N * 3; k += nthr) s_pos[k] = gpos[k];
+  if (POT == POT_EAM) {
+    const double* gc = P.comp + rd.comp_off;
+    for (int k = tid; k < R * N; k += nthr) {
+      if (F32) s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
+      else s_c64[k] = make_double2(gc[2 * k], gc[2 * k + 1]);
+    }
+  }
+  for (int s = tid; s < R; s += nthr) {
+    int g = rd.wk + s;
+    s_beta[s] = P.beta[g];
+    s_maxbox[s] = P.maxbox[g];
+    s_ham[2 * s] = P.ham[2 * g];
+    s_ham[2 * s + 1] = P.ham[2 * g + 1];
+    s_maxd[2 * s] = P.maxd[2 * g];
+    s_maxd[2 * s + 1] = P.maxd[2 * g + 1];
+    for (int q = 0; q < 6; ++q) s_cnt[6 * s + q] = P.cnt[6 * (size_t)g + q];
+    s_wos[s] = P.wos[g];
+  }
+  __syncthreads();
+  if (F32)
+    for (int k = tid; k < R * N; k += nthr)
+      s_p32[k] = make_float4((float)s_pos[3 * k], (float)s_pos[3 * k + 1],
+                             (float)s_pos[3 * k + 2], 0.f);
+  for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
+  __syncthreads();
+
+  // ---- walker registers (warp-uniform) ----
+  const int g = rd.wk + w;
+  double en = P.en[g];
+  double L = P.box[g];
+  double rc2 = P.rc2[g];
+  unsigned long long ctr = P.ctr[g];
+  unsigned long long base = ctr + DRAW_BUF;  // forces a refill on first draw
+  int status = P.status[g];
+  double drift = P.drift[g];
+  double* X = s_pos + (size_t)w * N * 3;
+  float4* X32 = F32 ? s_p32 + (size_t)w * N : nullptr;
+  double* drw = s_drw + w * DRAW_BUF;
+  double* M = (ENS == ENS_NPT && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
+  double* row = s_row ? s_row + (size_t)w * N : nullptr;
+  const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
+  const double ean = P.eam_ean, ecam = P.eam_ecam;
+  const float hnf = (float)hn, hmf = (float)hm, eanf = (float)ean, ecamf = (float)ecam;
+  const uint32_t run_word = (uint32_t)rd.run_id;
+
+  // draw from this walker's stream (all lanes in lockstep)
+  auto draw = [&]() -> double {
+    if (ctr - base >= (unsigned long long)DRAW_BUF) {
+      __syncwarp();
+      base = ctr & ~1ull;
+      if (lane < DRAW_BUF / 2) {
+        double u0, u1;
+        philox_pair(P.seed, (uint32_t)w, run_word, (base >> 1) + lane, u0, u1);
+        drw[2 * lane] = u0;
+        drw[2 * lane + 1] = u1;
+      }
+      __syncwarp();
+    }
+    double u = drw[ctr - base];
+    ++ctr;
+    return u;
+  };
+
+  // ---------------------------------------------------------- atom move
+  // mc_move! with an "atommove" slot (src/MCRun.jl:142-162)
+  auto atom_move = [&](int i, double beta, double md) -> int {
+    double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+    double tx, ty, tz;
+    auto propose = [&]() {  // atom_displacement (src/MCMoves.jl:33-64)
+      double ux = draw(), uy = draw(), uz = draw();
+      tx = dadd(xi, dmul(dsub(ux, 0.5), md));
+      ty = dadd(yi, dmul(dsub(uy, 0.5), md));
+      tz = dadd(zi, dmul(dsub(uz, 0.5), md));
+    };
+    propose();
+    if (BC == BC_SPH) {  // spherical retry loop (src/MCMoves.jl:117-136)
+      const double R2 = dmul(L, L);
+      int count = 0;
+      while (dot3(tx, ty, tz) > R2) {
+        ++count;
+        if (count == 50) {  // recentre! (src/Configurations.jl:79-85)
+          double sx = 0, sy = 0, sz = 0;
+          for (int a = lane; a < N; a += 32) {
+            sx += X[3 * a];
+            sy += X[3 * a + 1];
+            sz += X[3 * a + 2];
+          }
+          sx = warp_sum(sx) / N;
+          sy = warp_sum(sy) / N;
+          sz = warp_sum(sz) / N;
+          __syncwarp();
+          for (int a = lane; a < N; a += 32) {
+            X[3 * a] -= sx;
+            X[3 * a + 1] -= sy;
+            X[3 * a + 2] -= sz;
+            if (F32) X32[a] = make_float4((float)X[3 * a], (float)X[3 * a + 1], (float)X[3 * a + 2], 0.f);
+          }
+          __syncwarp();
+          xi = X[3 * i];
+          yi = X[3 * i + 1];
+          zi = X[3 * i + 2];
+        } else {
+          propose();
+          if (count == 100) {
+            status = ST_SPHERE;
+            return 0;
+          }
+        }
+      }
+    } else {  // periodic wrap (src/MCMoves.jl:50-64)
+      tx = dsub(tx, dmul(L, rint(ddiv(tx, L))));
+      ty = dsub(ty, dmul(L, rint(ddiv(ty, L))));
+      tz = dsub(tz, dmul(L, rint(ddiv(tz, L))));
+    }
+
+    double new_en;
+    double sa = 0.0, sb = 0.0;  // EAM FP64: sum of component deltas of atom i
+    float saf = 0.f, sbf = 0.f;
+    if (POT == POT_ELJ || POT == POT_ELJEVEN) {
+      if (!F32) {  // dimer_energy_update! (src/EnergyEvaluation.jl:804-821)
+        double e_n = 0.0, e_o = 0.0;
+        const double* Mi = M ? M + (size_t)i * N : nullptr;
+        for (int j = lane; j < N; j += 32) {
+          if (j == i) {
+            if (row) row[j] = 0.0;
+            continue;
+          }
+          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L);
+          double dol = Mi ? Mi[j] : pd2<BC>(xi, yi, zi, X + 3 * j, L);
+          if (ENS == ENS_NPT) {
+            row[j] = dn;
+            if (dn <= rc2) e_n += v64<POT>(s_c, K, dn);
+            if (dol <= rc2) e_o += v64<POT>(s_c, K, dol);
+          } else {
+            e_n += v64<POT>(s_c, K, dn);
+            e_o += v64<POT>(s_c, K, dol);
+          }
+        }
+        e_n = warp_sum(e_n);
+        e_o = warp_sum(e_o);
+        new_en = (e_n - e_o) + en;
+      } else {
+        const float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
+        float4 t4 = make_float4((float)tx, (float)ty, (float)tz, 0.f);
+        float4 x4 = X32[i];
+        float de = 0.f;
+        for (int j = lane; j < N; j += 32) {
+          if (j == i) continue;
+          float4 b = X32[j];
+          float dn = pf2<BC>(t4, b, Lf, iLf);
+          float dol = pf2<BC>(x4, b, Lf, iLf);
+          if (ENS == ENS_NPT) {
+            if (dn <= rcf) de += v32<POT>(s_cf, K, dn);
+            if (dol <= rcf) de -= v32<POT>(s_cf, K, dol);
+          } else {
+            de += v32<POT>(s_cf, K, dn) - v32<POT>(s_cf, K, dol);
+          }
+        }
+        de = warp_sum(de);
+        new_en = en + (double)de;
+      }
+    } else {  // EAM energy_update! (src/EnergyEvaluation.jl:1567-1591)
+      if (!F32) {
+        double2* C = s_c64 + (size_t)w * N;
+        double2* D = s_d64 + (size_t)w * N;
+        for (int j = lane; j < N; j += 32) {
+          if (j == i) {
+            D[j] = make_double2(0.0, 0.0);
+            continue;
+          }
+          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L);
+          double dol = pd2<BC>(xi, yi, zi, X + 3 * j, L);
+          double a1, b1, a0, b0;
+          invrexp64(dn, hn, hm, a1, b1);
+          invrexp64(dol, hn, hm, a0, b0);
+          double da = a1 - a0, db = b1 - b0;
+          D[j] = make_double2(da, db);
+          sa += da;
+          sb += db;
+        }
+        sa = warp_sum(sa);
+        sb = warp_sum(sb);
+        __syncwarp();
+        double e = 0.0;  // calc_energies_from_components (:1156-1162)
+        for (int k = lane; k < N; k += 32) {
+          double2 c = C[k];
+          double2 d = (k == i) ? make_double2(sa, sb) : D[k];
+          e += ean * (c.x + d.x) - ecam * sqrt(c.y + d.y);
+        }
+        new_en = warp_sum(e);
+      } else {
+        const float Lf = (float)L, iLf = (float)(1.0 / L);
+        float2* C = s_c32 + (size_t)w * N;
+        float2* D = s_d32 + (size_t)w * N;
+        float4 t4 = make_float4((float)tx, (float)ty, (float)tz, 0.f);
+        float4 x4 = X32[i];
+        float de = 0.f;
+        for (int j = lane; j < N; j += 32) {
+          if (j == i) continue;
+          float4 b = X32[j];
+          float ln_ = lg2f(pf2<BC>(t4, b, Lf, iLf));
+          float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
+          float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
+          float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
+          D[j] = make_float2(da, db);
+          saf += da;
+          sbf += db;
+          float2 c = C[j];
+          // sqrt(rho+d) - sqrt(rho) in the cancellation-free form
+          float s0 = sqrtf_approx(c.y), s1 = sqrtf_approx(c.y + db);
+          de += eanf * da - ecamf * __fdividef(db, s0 + s1);
+        }
+        saf = warp_sum(saf);
+        sbf = warp_sum(sbf);
+        de = warp_sum(de);
+        float2 ci = C[i];
+        float s0 = sqrtf_approx(ci.y), s1 = sqrtf_approx(ci.y + sbf);
+        de += eanf * saf - ecamf * __fdividef(sbf, s0 + s1);
+        new_en = en + (double)de;
+      }
+    }
+
+    // acc_test! / metropolis_condition (src/MCRun.jl:122-132, Exchange.jl:53-57)
+    double prob = exp(-(new_en - en) * beta);
+    if (prob > 1) prob = 1.0;
+    double u = draw();
+    if (!(prob >= u)) return 0;
+    // swap_atom_config! (src/swap_config.jl:40-51)
+    __syncwarp();
+    if (lane == 0) {
+      X[3 * i] = tx;
+      X[3 * i + 1] = ty;
+      X[3 * i + 2] = tz;
+      if (F32) X32[i] = make_float4((float)tx, (float)ty, (float)tz, 0.f);
+    }
+    if (M) {
+      for (int j = lane; j < N; j += 32) {
+        double v = row[j];
+        M[(size_t)i * N + j] = v;
+        M[(size_t)j * N + i] = v;
+      }
+    }
+    if (POT == POT_EAM) {  // swap_vars! EAM (src/swap_config.jl:208-211)
+      if (!F32) {
+        double2* C = s_c64 + (size_t)w * N;
+        const double2* D = s_d64 + (size_t)w * N;
+        for (int k = lane; k < N; k += 32) {
+          double2 d = (k == i) ? make_double2(sa, sb) : D[k];
+          double2 c = C[k];
+          C[k] = make_double2(c.x + d.x, c.y + d.y);
+        }
+      } else {
+        float2* C = s_c32 + (size_t)w * N;
+        const float2* D = s_d32 + (size_t)w * N;
+        for (int k = lane; k < N; k += 32) {
+          float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
+          float2 c = C[k];
+          C[k] = make_float2(c.x + d.x, c.y + d.y);
+        }
+      }
+    }
+    en = new_en;
+    __syncwarp();
+    return 1;
+  };
+
+  // ---------------------------------------------------------- volume move
+  // volume_change_uniform (src/MCMoves.jl:277-287), NPT energy
+  // (src/MCRun.jl:76-85), metropolis_condition NPT (src/Exchange.jl:58-70),
+  // swap_config_v! (src/swap_config.jl:113-141).  Always FP64.
+  auto volume_move = [&](double beta, double mdv, double maxbox) -> int {
+    double u = draw();
+    double scale = pow(exp((u - 0.5) * mdv), 1.0 / 3.0);
+    if (L >= maxbox && scale > 1.0) scale = 1.0;
+    double Ln = scale * L;
+    double rcn = Ln * Ln / 4;
+    double s2 = scale * scale;
+    double e = 0.0;
+    if (!F32) {
+      for (int i = 0; i < N; ++i)
+        for (int j = i + 1 + lane; j < N; j += 32) {
+          double x = M[(size_t)i * N + j] * s2;
+          if (x <= rcn) e += v64<POT>(s_c, K, x);
+        }
+    } else {
+      for (int i = 0; i < N; ++i) {
+        double xi = scale * X[3 * i], yi = scale * X[3 * i + 1], zi = scale * X[3 * i + 2];
+        for (int j = i + 1 + lane; j < N; j += 32) {
+          double x = d2_cub(xi, yi, zi, scale * X[3 * j], scale * X[3 * j + 1],
+                            scale * X[3 * j + 2], Ln);
+          if (x <= rcn) e += v64<POT>(s_c, K, x);
+        }
+      }
+    }
+    e = warp_sum(e) + lrc64(N, rcn, s_c, K);
+    double Vn = Ln * Ln * Ln, Vo = L * L * L;
+    double dh = dadd(dsub(e, en), dmul(P.pressure, dsub(Vn, Vo)));
+    double prob = exp(dadd(dmul(-dh, beta), dmul((double)N, log(Vn / Vo))));
+    if (prob > 1) prob = 1.0;
+    double ua = draw();
+    if (!(prob >= ua)) return 0;
+    __syncwarp();
+    for (int k = lane; k < 3 * N; k += 32) X[k] = scale * X[k];
+    if (!F32)
+      for (int k = lane; k < N * N; k += 32) M[k] = M[k] * s2;
+    __syncwarp();
+    if (F32)
+      for (int a = lane; a < N; a += 32)
+        X32[a] = make_float4((float)X[3 * a], (float)X[3 * a + 1], (float)X[3 * a + 2], 0.f);
+    L = Ln;
+    rc2 = rcn;
+    en = e;
+    __syncwarp();
+    return 1;
+  };
+
+  // ---------------------------------------------------------- cycles
+  const long long first = rd.cyc[phase];
+  unsigned long long run_ctr = rd.run_ctr;
+  for (int cyc = 0; cyc < ncycles; ++cyc) {
+    const long long idx = first + cyc;
+    const int slot = s_sow[w];
+    const double beta = s_beta[slot];
+    const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
+    const double maxbox = s_maxbox[slot];
+    long long acc_a = 0, acc_v = 0;
+    if (status == ST_OK) {
+      for (int st = 0; st < n_steps; ++st) {
+        int k = randint(draw(), n_steps);
+        if (k < N) acc_a += atom_move(k, beta, md);
+        else acc_v += volume_move(beta, mdv, maxbox);
+        if (status != ST_OK) break;
+      }
+      if (F32 && P.resync_every > 0 && idx % P.resync_every == 0) {
+        double e64 = walker_energy64<POT, BC, ENS>(
+            X, N, L, rc2, s_c, K, hn, hm, ean, ecam, nullptr, nullptr,
+            POT == POT_EAM ? s_c32 + (size_t)w * N : nullptr, lane);
+        drift = fmax(drift, fabs(en - e64));
+        en = e64;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) {
+      s_en[w] = en;
+      s_box[w] = L;
+      s_cnt[6 * slot + 0] += acc_a;
+      s_cnt[6 * slot + 1] += acc_a;
+      s_cnt[6 * slot + 2] += acc_v;
+      s_cnt[6 * slot + 3] += acc_v;
+    }
+    __syncthreads();
+    if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
+      double u = philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++);
+      if (u < P.exch_prob) {
+        int k = randint(philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++), R - 1);
+        s_cnt[6 * k + 4] += 1;
+        s_cnt[6 * (k + 1) + 4] += 1;
+        int w1 = s_wos[k], w2 = s_wos[k + 1];
+        double e1 = s_en[w1], e2 = s_en[w2];
+        if (ENS == ENS_NPT) {
+          double L1 = s_box[w1], L2 = s_box[w2];
+          e1 = dadd(e1, dmul(P.pressure, dmul(dmul(L1, L1), L1)));
+          e2 = dadd(e2, dmul(P.pressure, dmul(dmul(L2, L2), L2)));
+        }
+        double acc = exp((s_beta[k] - s_beta[k + 1]) * (e1 - e2));
+        if (acc > 1.0) acc = 1.0;
+        if (acc > philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++)) {
+          s_cnt[6 * k + 5] += 1;
+          s_cnt[6 * (k + 1) + 5] += 1;
+          s_wos[k] = w2;
+          s_wos[k + 1] = w1;
+          s_sow[w2] = k;
+          s_sow[w1] = k + 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < R) {
+      const int s = tid;
+      if (idx % P.n_adjust == 0) {  // update_max_stepsize!
+        double acc = (double)s_cnt[6 * s + 1] / (double)((long long)P.n_adjust * N);
+        if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
+        else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
+        s_cnt[6 * s + 1] = 0;
+        if (ENS == ENS_NPT) {
+          double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);
+          if (av < P.min_acc) s_maxd[2 * s + 1] *= 0.9;
+          else if (av > P.max_acc) s_maxd[2 * s + 1] *= 1.1;
+          s_cnt[6 * s + 3] = 0;
+        }
+      }
+      if (phase == PHASE_PROD && idx % P.mc_sample == 0) {  // sampling_step!
+        const int wk = s_wos[s];
+        const double e = s_en[wk];
+        const int nb = P.n_bin;
+        unsigned int* hrow = P.hist + rd.hist_off + (size_t)s * rd.hist_stride;
+        auto hidx = [&](double h) -> int {  // find_hist_index (Sampling.jl:53-62)
+          if (h < 1) return 1;
+          if (h > nb) return nb + 2;
+          return (int)floor(h) + 1;
+        };
+        if (ENS == ENS_NPT) {
+          double Lw = s_box[wk];
+          double V = dmul(dmul(Lw, Lw), Lw);
+          double H = dadd(e, dmul(P.pressure, V));
+          s_ham[2 * s] += H;
+          s_ham[2 * s + 1] = dadd(s_ham[2 * s + 1], dmul(H, H));
+          int ie = hidx(floor((e - rd.en_min) / rd.dE) + 1);
+          int iv = hidx(floor((V - rd.v_min) / rd.dV) + 1);
+          atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
+        } else {
+          s_ham[2 * s] += e;
+          s_ham[2 * s + 1] = dadd(s_ham[2 * s + 1], dmul(e, e));
+          int ie = hidx((e - rd.en_min) / rd.dE + 1);
+          atomicAdd(hrow + (ie - 1), 1u);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- store the run back to HBM ----
+  double* gpos_w = P.pos + rd.pos_off;
+  for (int k = tid; k < R * N * 3; k += nthr) gpos_w[k] = s_pos[k];
+  if (POT == POT_EAM) {
+    double* gc = P.comp + rd.comp_off;
+    for (int k = tid; k < R * N; k += nthr) {
+      if (F32) {
+        gc[2 * k] = s_c32[k].x;
+        gc[2 * k + 1] = s_c32[k].y;
+      } else {
+        gc[2 * k] = s_c64[k].x;
+        gc[2 * k + 1] = s_c64[k].y;
+      }
+    }
+  }
+  if (lane == 0) {
+    P.en[g] = en;
+    P.box[g] = L;
+    P.rc2[g] = rc2;
+    P.ctr[g] = ctr;
+    P.status[g] = status;
+    P.drift[g] = drift;
+  }
+  for (int s = tid; s < R; s += nthr) {
+    int gs = rd.wk + s;
+    P.ham[2 * gs] = s_ham[2 * s];
+    P.ham[2 * gs + 1] = s_ham[2 * s + 1];
+    P.maxd[2 * gs] = s_maxd[2 * s];
+    P.maxd[2 * gs + 1] = s_maxd[2 * s + 1];
+    for (int q = 0; q < 6; ++q) P.cnt[6 * (size_t)gs + q] = s_cnt[6 * s + q];
+    P.wos[gs] = s_wos[s];
+  }
+  if (tid == 0) {
+    P.runs[run0 + blockIdx.x].cyc[phase] = first + ncycles;
+    P.runs[run0 + blockIdx.x].run_ctr = run_ctr;
+  }
+}
+
+// FP32 form: explicit FP64 recompute of every walker (ptmc_resync)
+template <int POT, int BC, int ENS, bool F32>
+__global__ void __launch_bounds__(1024) k_resync(KParams P, int run0) {
+  const RunDesc rd = P.runs[run0 + blockIdx.x];
+  const int N = rd.N, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w >= rd.R) return;
+  const int g = rd.wk + w;
+  const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
+  double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
+  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.rc2[g], P.c, P.K,
+                                           -0.5 * P.eam_n, -0.5 * P.eam_m,
+                                           P.eam_ean, P.eam_ecam, nullptr, comp,
+                                           nullptr, lane);
+  if (lane == 0) {
+    P.drift[g] = fmax(P.drift[g], fabs(P.en[g] - e));
+    P.en[g] = e;
+  }
+}
+
+// ------------------------------------------------------------ dispatch
+template <int POT, int BC, int ENS, bool F32>
+static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
+                        int maxN, int ncycles, int phase, cudaStream_t st) {
+  dim3 grid(nruns), block(R * 32);
+  if (what == 0) {
+    long long smem = cycles_smem_bytes(POT, ENS, F32, R, maxN);
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_cycles<POT, BC, ENS, F32>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      attr_set = true;
+    }
+    k_cycles<POT, BC, ENS, F32><<<grid, block, (size_t)smem, st>>>(P, run0, ncycles, phase);
+  } else if (what == 1) {
+    k_init<POT, BC, ENS, F32><<<grid, block, 0, st>>>(P, run0);
+  } else {
+    k_resync<POT, BC, ENS, F32><<<grid, block, 0, st>>>(P, run0);
+  }
+  return (int)cudaGetLastError();
+}
+
+template <int POT, int BC, int ENS>
+static int run_prec(bool f32, int what, const KParams& P, int run0, int nruns,
+                    int R, int maxN, int ncycles, int phase, cudaStream_t st) {
+  return f32 ? run_instance<POT, BC, ENS, true>(what, P, run0, nruns, R, maxN, ncycles, phase, st)
+             : run_instance<POT, BC, ENS, false>(what, P, run0, nruns, R, maxN, ncycles, phase, st);
+}
+
+static int dispatch(int pot, int bc, int ens, bool f32, int what,
+                    const KParams& P, int run0, int nruns, int R, int maxN,
+                    int ncycles, int phase, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+#define PT_CASE(PO, B, E)                                                  \
+  if (pot == PO && bc == B && ens == E)                                    \
+    return run_prec<PO, B, E>(f32, what, P, run0, nruns, R, maxN, ncycles, \
+                              phase, st);
+  PT_CASE(POT_ELJ, BC_SPH, ENS_NVT)
+  PT_CASE(POT_ELJEVEN, BC_SPH, ENS_NVT)
+  PT_CASE(POT_EAM, BC_SPH, ENS_NVT)
+  PT_CASE(POT_ELJ, BC_CUB, ENS_NVT)
+  PT_CASE(POT_ELJEVEN, BC_CUB, ENS_NVT)
+  PT_CASE(POT_EAM, BC_CUB, ENS_NVT)
+  PT_CASE(POT_ELJEVEN, BC_CUB, ENS_NPT)
+#undef PT_CASE
+  return -1;
+}
+
+int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
+                  int run0, int nruns, int R, int maxN, int ncycles, int phase,
+                  void* stream) {
+  return dispatch(pot, bc, ens, f32, 0, P, run0, nruns, R, maxN, ncycles, phase, stream);
+}
+int launch_init(int pot, int bc, int ens, bool f32, const KParams& P, int run0,
+                int nruns, int R, void* stream) {
+  return dispatch(pot, bc, ens, f32, 1, P, run0, nruns, R, 0, 0, 0, stream);
+}
+int launch_resync(int pot, int bc, int ens, bool f32, const KParams& P,
+                  int run0, int nruns, int R, void* stream) {
+  return dispatch(pot, bc, ens, f32, 2, P, run0, nruns, R, 0, 0, 0, stream);
+}
+
+}  // namespace ptmc

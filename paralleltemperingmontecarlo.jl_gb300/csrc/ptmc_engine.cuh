@@ -1,0 +1,116 @@
+// ptmc_engine.cuh — structures shared between the host orchestration
+// (ptmc_capi.cu) and the replica-cycle kernels (ptmc_cycles.cu).
+//
+// HBM layout (structure of arrays, one allocation per field, walkers of all
+// runs concatenated; "walker" = configuration-bound data, "slot" =
+// temperature-bound data, see the walker/slot note in ptmc_cycles.cu):
+//   pos   f64 [sum_r R_r*N_r*3]   positions, walker-major, atom-major, xyz
+//   mat   f64 [sum_r R_r*N_r*N_r] NPT plain form: squared-distance matrix
+//   comp  f64 [sum_r R_r*N_r*2]   EAM (phi_i, rho_i) components
+//   en/box/rc2/drift f64 [W], ctr u64 [W], status i32 [W]   per walker
+//   beta/maxbox f64 [W], maxd f64 [2W], ham f64 [2W], cnt i64 [6W],
+//   wos i32 [W]                                              per slot
+//   hist u32 [sum_r R_r*stride_r]  NVT: (n_bin+2) per slot, NPT: (n_bin+2)^2
+#pragma once
+#include <cstdint>
+
+namespace ptmc {
+
+enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3 };
+enum { BC_SPH = 0, BC_CUB = 1 };
+enum { ENS_NVT = 0, ENS_NPT = 1 };
+enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
+enum { ST_OK = 0, ST_SPHERE = 1 };
+constexpr int MAX_COEFF = 16;
+constexpr int MAX_REPLICAS = 32;
+constexpr int DRAW_BUF = 16;
+
+struct RunDesc {
+  int N, R;                 // atoms, replicas
+  int wk;                   // first global walker (= slot) index of the run
+  int run_id;               // Philox run word (global run index)
+  long long pos_off;        // element offsets of walker 0 in pos / mat / comp
+  long long mat_off;
+  long long comp_off;
+  long long hist_off;       // element offset of slot 0 in hist
+  int hist_stride;          // hist elements per slot
+  int pad0;
+  double en_min, en_max, dE;  // energy histogram (Sampling.jl:141-194)
+  double v_min, v_max, dV;    // volume histogram (NPT)
+  long long cyc[3];         // next cycle index (1-based) per phase
+  unsigned long long run_ctr;  // run-level draw counter
+};
+
+struct KParams {
+  RunDesc* runs;
+  // walker-bound
+  double* pos;
+  double* mat;
+  double* comp;
+  double* en;
+  double* box;
+  double* rc2;
+  double* drift;
+  unsigned long long* ctr;
+  int* status;
+  // slot-bound
+  double* beta;
+  double* maxd;
+  double* maxbox;
+  double* ham;
+  long long* cnt;
+  int* wos;
+  unsigned int* hist;
+  // potential
+  double c[MAX_COEFF];
+  int K;
+  double eam_n, eam_m, eam_ean, eam_ecam;
+  // ensemble / MC parameters
+  double pressure;
+  double exch_prob;
+  double min_acc, max_acc;
+  int n_bin, n_adjust, mc_sample, resync_every;
+  unsigned long long seed;
+};
+
+// shared-memory bytes of one run CTA
+inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
+  auto al = [](long long b) { return (b + 15) / 16 * 16; };
+  long long b = 0;
+  b += al((long long)R * N * 3 * 8);                 // FP64 positions
+  if (f32) b += al((long long)R * N * 16);           // FP32 positions (float4)
+  if (pot == POT_EAM) {
+    b += al((long long)R * N * (f32 ? 8 : 16));      // components
+    b += al((long long)R * N * (f32 ? 8 : 16));      // per-move deltas
+  }
+  if (ens == ENS_NPT && !f32) b += al((long long)R * N * 8);  // trial row
+  b += al((long long)R * DRAW_BUF * 8);              // draw buffers
+  b += al((long long)R * 8) * 6;                     // beta, maxbox, en, box, ham(2)
+  b += al((long long)R * 16);                        // maxd
+  b += al((long long)R * 6 * 8);                     // counters
+  b += al((long long)R * 4) * 2;                     // wos, sow
+  return b;
+}
+
+}  // namespace ptmc
+
+// kernel launch entry points (ptmc_cycles.cu)
+namespace ptmc {
+int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
+                  int run0, int nruns, int R, int maxN, int ncycles, int phase,
+                  void* stream);
+int launch_init(int pot, int bc, int ens, bool f32, const KParams& P,
+                int run0, int nruns, int R, void* stream);
+int launch_resync(int pot, int bc, int ens, bool f32, const KParams& P,
+                  int run0, int nruns, int R, void* stream);
+// multihistogram (ptmc_wham.cu); scratch is caller-provided device memory
+int wham_nvt_device(int R, int n_bin, const double* d_hist, const double* d_beta,
+                    double en_min, double en_max, double thr,
+                    const double* d_beta_out, int n_out, double* d_work,
+                    double* d_out, int* d_iters, void* stream);
+int wham_npt_device(int R, int n_bin, const double* d_hist, const double* d_beta,
+                    double en_min, double en_max, double v_min, double v_max,
+                    double p, double thr, const double* d_beta_out, int n_out,
+                    double* d_work, double* d_out, int* d_iters, void* stream);
+long long wham_work_doubles(int R, int n_bins_total);
+}  // namespace ptmc

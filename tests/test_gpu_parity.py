@@ -1,0 +1,279 @@
+"""GPU parity tests: the CUDA engine through its C ABI against the CPU oracle.
+
+Both consume the same Philox draw streams in the reference's draw order, so the
+plain FP64 form must reproduce the oracle's accept/reject sequence exactly:
+accept counters, exchange counters, step sizes, walker permutation, positions
+and histograms are compared for equality, energies to 1e-10 relative (the
+tolerance north of FP64 rounding differences between the GPU's and the host's
+exp/log/pow and between warp-tree and sequential sums).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
+        -56234083.4334278, 288738837.441765]  # examples/ne13.jl:24-31
+REL = 1e-10
+
+
+def sphere_start(N, radius, min_sep, seed):
+    rng = np.random.default_rng(seed)
+    pos = []
+    tries = 0
+    while len(pos) < N:
+        tries += 1
+        assert tries < 200000
+        v = rng.uniform(-radius, radius, 3)
+        if np.linalg.norm(v) < radius and all(np.linalg.norm(v - q) > min_sep for q in pos):
+            pos.append(v)
+    return np.array(pos)
+
+
+def fcc(ncell, a, jitter, seed):
+    rng = np.random.default_rng(seed)
+    basis = [(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)]
+    x = np.array([[(i + b[0]) * a, (j + b[1]) * a, (k + b[2]) * a]
+                  for i in range(ncell) for j in range(ncell) for k in range(ncell) for b in basis])
+    x += rng.uniform(-jitter, jitter, x.shape)
+    return x - ncell * a / 2
+
+
+def cu55_ico():
+    d = json.load(open(os.path.join(GOLDEN, "nn_cu55.json")))
+    return np.array(d["ico55_nm"]) * (d["cu_lattice_nm"] * d["nm_to_bohr"])
+
+
+CU_EAM = dict(n=8.482, m=4.692, eps=0.0367493 * 0.0370, C=27.561, a=0.25 * 18.8973)  # scripts/cu55.jl:39-48
+
+
+def pair(pk, orc, *, N, R, x0, T0, T1, pot, ens="nvt", bc_param, exch_prob, seed, n_runs=1,
+         starts=None, cycles_per_launch=0, pressure=0.0, eq=0):
+    """An engine and matching oracle runs (one per engine run)."""
+    mp = pk.MCParams(mc_cycles=1000, eq_cycles=eq, mc_sample=1, n_traj=R, n_atoms=N)
+    temp = pk.TempGrid(T0, T1, R)
+    ensemble = pk.NPT(N, pressure) if ens == "npt" else pk.NVT(N)
+    bc = pk.CubicBC(bc_param) if ens == "npt" or ens == "nvt_cubic" else pk.SphericalBC(bc_param)
+    eng = pk.Engine(mp, temp, pot, ensemble, n_runs=n_runs, exch_prob=exch_prob, seed=seed,
+                    cycles_per_launch=cycles_per_launch)
+    oracles = []
+    for r in range(n_runs):
+        xr = x0 if starts is None else starts[r]
+        eng.set_configs(r, pk.Config(xr, bc))
+        o = orc.Run(len(xr), R, np.stack([xr] * R), temp.t_grid,
+                    ensemble=orc.NPT if ens == "npt" else orc.NVT, pressure=pressure,
+                    bc=orc.BC_CUBIC if isinstance(bc, pk.CubicBC) else orc.BC_SPHERE,
+                    bc_param=bc_param, exch_prob=exch_prob, seed=seed, run_index=r)
+        if isinstance(pot, pk.EmbeddedAtomPotential):
+            o.set_eam(pot.n, pot.m, pot.ean, pot.eCam)
+        else:
+            o.set_elj(pot.coeff, pot.even)
+        o.init()
+        oracles.append(o)
+    eng.init()
+    return eng, oracles
+
+
+def compare(eng, o, run=0, rel=REL, positions_exact=True):
+    g = eng.states(run)
+    xo, eo, bo = o.slot_states()
+    s = o.slots()
+    assert np.array_equal(g["counts"][:, 0:2], s["count_atom"]), "atom accept counters"
+    assert np.array_equal(g["counts"][:, 2:4], s["count_vol"]), "volume accept counters"
+    assert np.array_equal(g["counts"][:, 4:6], s["count_exc"]), "exchange counters"
+    assert np.array_equal(g["max_displ"], s["max_displ"]), "step sizes"
+    if positions_exact:
+        assert np.array_equal(g["xyz"], xo), "positions (bitwise)"
+    else:
+        np.testing.assert_allclose(g["xyz"], xo, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(g["box"], bo, rtol=1e-14)
+    np.testing.assert_allclose(g["en_tot"], eo, rtol=rel, atol=0)
+    np.testing.assert_allclose(g["ham"], s["ham"], rtol=rel, atol=1e-300)
+    return g
+
+
+def test_ne13_nvt_fp64_parity(pk, orc):
+    """Ne13 in a sphere of 11 bohr, 16 replicas 4-16 K (the Ne13 workload at
+    reduced cycle count): equilibration, production, sampling, exchange p = 0.1."""
+    x0 = sphere_start(13, 8.0, 4.5, 1234)
+    eng, (o,) = pair(pk, orc, N=13, R=16, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                     bc_param=11.0, exch_prob=0.1, seed=1234, eq=400)
+    eng.equilibrate()
+    o.equilibrate(400)
+    eng.run_cycles(600)
+    o.production(1, 600)
+    compare(eng, o)
+    out = eng.output(0)
+    eh, _, hp = o.hist()
+    assert out.en_min == hp[0] and out.en_max == hp[1]
+    assert np.array_equal(out.en_histogram, eh), "energy histograms"
+    eng.close()
+
+
+def test_ne13_exchange_every_cycle(pk, orc):
+    x0 = sphere_start(13, 8.0, 4.5, 77)
+    eng, (o,) = pair(pk, orc, N=13, R=8, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                     bc_param=11.0, exch_prob=1.0, seed=42)
+    eng.cycles_nosample(500)
+    o.cycles(1, 500)
+    g = compare(eng, o)
+    assert g["counts"][:, 5].sum() > 0, "some exchanges accepted"
+    eng.close()
+
+
+def test_elj_all_powers_parity(pk, orc):
+    x0 = sphere_start(13, 8.0, 4.5, 5)
+    c = C_NE[:3] + [0.0, 1.0e5]
+    eng, (o,) = pair(pk, orc, N=13, R=4, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotential(c),
+                     bc_param=11.0, exch_prob=1.0, seed=3)
+    eng.cycles_nosample(200)
+    o.cycles(1, 200)
+    compare(eng, o)
+    eng.close()
+
+
+def test_cu55_eam_fp64_parity(pk, orc):
+    """Cu55 Sutton-Chen EAM (scripts/cu55.jl:39-48), icosahedral start, sphere 14 bohr."""
+    pot = pk.EmbeddedAtomPotential(**CU_EAM)
+    eng, (o,) = pair(pk, orc, N=55, R=8, x0=cu55_ico(), T0=200.0, T1=1000.0, pot=pot,
+                     bc_param=14.0, exch_prob=1.0, seed=11)
+    eng.cycles_nosample(60)
+    o.cycles(1, 60)
+    compare(eng, o)
+    eng.close()
+
+
+def test_npt_fp64_parity(pk, orc):
+    """Bulk Ne NPT, fcc start with jitter, cubic box, cut-off L/2 + lrc, volume moves."""
+    x0 = fcc(2, 8.4, 0.05, 2)
+    p = 101325 * 3.398928944382626e-14  # test/test_states.jl:64
+    eng, (o,) = pair(pk, orc, N=32, R=4, x0=x0, T0=10.0, T1=40.0, pot=pk.ELJPotentialEven(C_NE),
+                     ens="npt", bc_param=16.8, exch_prob=1.0, seed=8, pressure=p, eq=40)
+    eng.equilibrate()
+    o.equilibrate(40)
+    eng.run_cycles(80)
+    o.production(1, 80)
+    g = compare(eng, o)
+    assert g["counts"][:, 2].sum() > 0, "some volume moves accepted"
+    out = eng.output(0)
+    _, ev, hp = o.hist()
+    assert np.array_equal(out.ev_histogram, ev)
+    eng.close()
+
+
+def test_nvt_cubic_parity(pk, orc):
+    x0 = fcc(2, 8.4, 0.05, 4)
+    eng, (o,) = pair(pk, orc, N=32, R=4, x0=x0, T0=10.0, T1=40.0, pot=pk.ELJPotentialEven(C_NE),
+                     ens="nvt_cubic", bc_param=16.8, exch_prob=1.0, seed=6)
+    eng.cycles_nosample(60)
+    o.cycles(1, 60)
+    # the NVT periodic form recomputes old distances from positions; the
+    # reference stores them, so ties in the minimum image may round 1 ulp apart
+    compare(eng, o, positions_exact=True)
+    eng.close()
+
+
+def test_batched_uneven_runs(pk, orc):
+    """Several independent runs of different N in one context (grouped launches)."""
+    sizes = [13, 38, 13, 20]
+    starts = [sphere_start(n, 0.9 * n ** (1 / 3) * 3, 4.3, 100 + k) for k, n in enumerate(sizes)]
+    radius = max(0.9 * n ** (1 / 3) * 3 for n in sizes) + 3
+    eng, os_ = pair(pk, orc, N=13, R=4, x0=None, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                    bc_param=radius, exch_prob=1.0, seed=21, n_runs=len(sizes), starts=starts,
+                    cycles_per_launch=7)
+    eng.cycles_nosample(50)
+    for r, o in enumerate(os_):
+        o.cycles(1, 50)
+        compare(eng, o, run=r)
+    st = eng.stats()
+    assert st["kernel_launches"] >= 8
+    eng.close()
+
+
+def test_graph_replay_matches_direct(pk, orc):
+    """CUDA-graph-replayed chunks give the same chain as the oracle."""
+    x0 = sphere_start(13, 8.0, 4.5, 9)
+    eng, (o,) = pair(pk, orc, N=13, R=4, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                     bc_param=11.0, exch_prob=1.0, seed=17, cycles_per_launch=5)
+    eng.cycles_nosample(5 * 8 * 3 + 7)   # 3 graph replays of 8 chunks + a remainder
+    o.cycles(1, 5 * 8 * 3 + 7)
+    compare(eng, o)
+    assert eng.stats()["graph_launches"] == 3
+    eng.close()
+
+
+def test_checkpoint_exact_resume(pk, orc, tmp_path):
+    x0 = sphere_start(13, 8.0, 4.5, 31)
+    kw = dict(N=13, R=4, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE), bc_param=11.0,
+              exch_prob=0.5, seed=5, eq=100)
+    a, _ = pair(pk, orc, **kw)
+    a.equilibrate()
+    a.run_cycles(300)
+    b, _ = pair(pk, orc, **kw)
+    b.equilibrate()
+    b.run_cycles(150)
+    b.checkpoint(str(tmp_path / "ck"))
+    b.close()
+    c, _ = pair(pk, orc, **kw)
+    c.restore(str(tmp_path / "ck"))
+    c.run_cycles(150)
+    sa, sc = a.states(0), c.states(0)
+    for k in sa:
+        assert np.array_equal(sa[k], sc[k]), k
+    assert np.array_equal(a.output(0).en_histogram, c.output(0).en_histogram)
+    # the reference-format files are readable by the reference-format reader
+    r = pk.read_checkpoint(str(tmp_path / "ck"))
+    assert r["index"] == 150 and len(r["configs"]) == 4
+    assert r["histograms"].shape == (4, 102)
+    assert r["histograms"].sum() == 4 * 150
+    a.close()
+    c.close()
+
+
+def test_sphere_error_is_reported(pk):
+    """An atom that cannot move back inside the sphere: 100 retries -> error
+    (src/MCMoves.jl:132), reported through the status word, no fault."""
+    x0 = sphere_start(13, 8.0, 4.5, 1) * 3.0   # every atom far outside radius 2
+    mp = pk.MCParams(mc_cycles=10, eq_cycles=0, mc_sample=1, n_traj=2, n_atoms=13)
+    eng = pk.Engine(mp, pk.TempGrid(4, 16, 2), pk.ELJPotentialEven(C_NE), pk.NVT(13))
+    eng.set_configs(0, pk.Config(x0, pk.SphericalBC(2.0)))
+    eng.init()
+    with pytest.raises(pk.PTMCError) as ei:
+        eng.cycles_nosample(2)
+    assert ei.value.code == -4
+    eng.close()
+
+
+@pytest.mark.parametrize("name", ["multihist_nvt", "multihist_npt"])
+def test_gpu_multihist_golden(pk, name):
+    """GPU WHAM against the reference's golden values (test/multihist_test.jl)."""
+    d = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    temp = pk.TempGrid(d["t_i"], d["t_f"], d["R"])
+    if name == "multihist_nvt":
+        T, cv, it = pk.multihist_nvt_arrays(np.array(d["en_histogram"]), temp.t_grid,
+                                            temp.beta_grid, d["en_min"], d["en_max"], d["thr"])
+    else:
+        T, cv, it = pk.multihist_npt_arrays(np.array(d["ev_histogram"]), temp.t_grid,
+                                            temp.beta_grid, d["en_min"], d["en_max"], d["v_min"],
+                                            d["v_max"], d["pressure"], d["thr"])
+    for k, v in d["expected"].items():
+        assert cv[int(k) - 1] == pytest.approx(v, rel=1e-9), k
+
+
+def test_gpu_multihist_matches_oracle(pk, orc):
+    d = json.load(open(os.path.join(GOLDEN, "checkpoint_ne13.json")))
+    h = np.array(d["histograms"])
+    p = d["params"]
+    temp = pk.TempGrid(p[8], p[9], h.shape[0])
+    T, cv, it = pk.multihist_nvt_arrays(h, temp.t_grid, temp.beta_grid, d["hist_info"][0],
+                                        d["hist_info"][1], 1e-3)
+    To, cvo, ito = orc.multihist_nvt(h, temp.t_grid, temp.beta_grid, d["hist_info"][0],
+                                     d["hist_info"][1], 1e-3)
+    assert it == ito
+    np.testing.assert_allclose(cv, cvo, rtol=1e-9)
+    np.testing.assert_allclose(T, To, rtol=1e-15)

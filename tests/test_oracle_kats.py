@@ -1,0 +1,209 @@
+"""CPU tests: the oracle against the reference's own known answers.
+
+Each test cites the reference test it restates (paths inside the reference
+package).  These pin the oracle before it is trusted as the GPU checker.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
+        -56234083.4334278, 288738837.441765]  # examples/ne13.jl:24-31
+
+
+def test_philox_known_answers(orc):
+    # Random123 published KAT vectors for philox4x32_10
+    assert list(orc.philox4x32([0, 0, 0, 0], [0, 0])) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert list(orc.philox4x32([0xffffffff] * 4, [0xffffffff] * 2)) == [
+        0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert list(orc.philox4x32([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                               [0xa4093822, 0x299f31d0])) == [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_u01_stream_layout(orc):
+    # draw k = half (k & 1) of Philox block k >> 1, 53 bits, in [0, 1)
+    blk = orc.philox4x32([3, 0, 5, 2], [0x1234, 0])
+    u0 = ((int(blk[0]) << 21) | (int(blk[1]) >> 11)) * 2.0 ** -53
+    u1 = ((int(blk[2]) << 21) | (int(blk[3]) >> 11)) * 2.0 ** -53
+    assert orc.u01(0x1234, 5, 2, 6) == u0
+    assert orc.u01(0x1234, 5, 2, 7) == u1
+    us = [orc.u01(1, 0, 0, k) for k in range(2000)]
+    assert 0.0 <= min(us) and max(us) < 1.0
+    assert abs(np.mean(us) - 0.5) < 0.03
+
+
+def test_elj_closed_forms(orc):
+    # test/test_potentials.jl:3-16
+    assert orc.dimer_energy(orc.POT_ELJ, [-2.0, 0.0, 1.0], 1.0) == -1.0
+    assert orc.dimer_energy(orc.POT_ELJEVEN, [-2.0, 1.0], 1.0) == -1.0
+    assert orc.dimer_energy(orc.POT_ELJEVEN, [-2.0, 1.0], 2.0) == orc.dimer_energy(orc.POT_ELJ, [-2.0, 0.0, 1.0], 2.0)
+    c = [-1.0, 2.0, 3.0, -4.0, 5.0]
+    assert orc.dimer_energy(orc.POT_ELJ, c, 1.0) == sum(c)
+
+
+def test_elj_config_consistency(orc):
+    # test/test_potentials.jl:17-39: three atoms, pair sum, cut-off sum
+    x = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [0.0, 1.0, 0.0]])
+    c = [-1.0, 2.0, 3.0, -4.0, 5.0]
+    e = orc.elj_config_energy(x, orc.POT_ELJ, c)
+    d = [orc.distance2(x[i], x[j]) for i, j in ((0, 1), (0, 2), (1, 2))]
+    ref = 0.0
+    for r2 in d:
+        ref += orc.dimer_energy(orc.POT_ELJ, c, r2)
+    assert e == ref
+    assert e < 0 or e > 0
+    # r_cut^2 = 4 excludes all three pairs (d2 = 14, 11, 49) and lrc(r_cut<=50) = 0
+    # (a box of 100 leaves the distances unchanged; only the cut-off acts)
+    assert orc.elj_config_energy(x, orc.POT_ELJEVEN, [-2.0, 1.0], orc.BC_CUBIC, 100.0, 4.0) == 0.0
+
+
+def test_eam_known_answer(orc):
+    # test/test_potentials.jl:41-56: n = m = eps = C = a = 1 -> ean = 0.5, eCam = 1
+    x = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [0.0, 1.0, 0.0]])
+    e = orc.eam_config_energy(x, 1.0, 1.0, 0.5, 1.0)
+    assert e == pytest.approx(-1.3495549581716526, rel=1e-15)
+
+
+def test_distances_and_min_image(orc):
+    # test/runtests.jl:87-125, test/configurations.jl
+    v1, v2, v3 = [1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [0.0, 1.0, 0.0]
+    assert orc.distance2(v1, v2) == 14.0
+    assert orc.distance2(v1, v3) == 11.0
+    assert orc.distance2(v1, v2, orc.BC_CUBIC, 10.0) == 14.0
+    w3 = [3.0, 6.0, 9.0]
+    assert orc.distance2(v1, w3) == 56.0
+    assert orc.distance2(v1, w3, orc.BC_CUBIC, 10.0) == 36.0
+
+
+def test_tempgrid(orc, pk):
+    # test/runtests.jl:216-235
+    T, B = orc.tempgrid(2.0, 16.0, 31)
+    assert len(T) == 31 and T.min() == 2.0 and T.max() == 16.0
+    T, B = orc.tempgrid(2.0, 16.0, 32)
+    assert 1.0 / (T[0] * B[0]) == pytest.approx(3.16681196e-6)
+    T1, _ = orc.tempgrid(2.0, 16.0, 32, 1)
+    assert (T1[1] - T1[0]) == pytest.approx(T1[-1] - T1[-2])
+    g = pk.TempGrid(2, 16, 31)
+    assert np.array_equal(g.t_grid, orc.tempgrid(2.0, 16.0, 31)[0])
+    with pytest.raises(ValueError):
+        pk.TempGrid(2, 16, 256, tdistr="test")
+
+
+def test_lrc_matches_formula(orc):
+    # lrc (src/EnergyEvaluation.jl:968-982), written out independently
+    rc2, N = (25.2 * 25.2) / 4, 108
+    rcs = math.sqrt(rc2)
+    rc3 = rc2 * rcs
+    e = 0.0
+    for i, c in enumerate(C_NE, start=1):
+        e += c / rc3 / (2 * i + 1)
+        rc3 *= rc2
+    e *= math.pi * N * N / 4 / (rcs ** 3)
+    assert orc.lrc(N, rc2, C_NE) == pytest.approx(e, rel=1e-14)
+    assert orc.lrc(N, 50.0, C_NE) == 0.0
+
+
+def test_mlp_all_ones(orc):
+    # test/test_runner_forward.jl:44-75: 88-20-20-1, all parameters and inputs 1 -> 21
+    nodes = [88, 20, 20, 1]
+    npar = sum(nodes[i - 1] * nodes[i] + nodes[i] for i in range(1, 4))
+    assert npar == 2221
+    out = orc.mlp_forward(np.ones((2, 88)), np.ones(npar), nodes)
+    assert list(out) == [21.0, 21.0]
+
+
+@pytest.mark.parametrize("name", ["multihist_nvt", "multihist_npt"])
+def test_multihist_golden(orc, name):
+    # test/multihist_test.jl:4-32 (golden Cv / Cp values of the reference)
+    d = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    T, B = orc.tempgrid(d["t_i"], d["t_f"], d["R"])
+    if name == "multihist_nvt":
+        Tout, cv, it = orc.multihist_nvt(np.array(d["en_histogram"]), T, B, d["en_min"],
+                                         d["en_max"], d["thr"])
+        assert len(cv) == 320
+    else:
+        Tout, cv, it = orc.multihist_npt(np.array(d["ev_histogram"]), T, B, d["en_min"],
+                                         d["en_max"], d["v_min"], d["v_max"], d["pressure"],
+                                         d["thr"])
+        assert len(cv) == 30
+    for k, v in d["expected"].items():
+        assert cv[int(k) - 1] == pytest.approx(v, rel=1e-12), k
+    assert 1 <= it < 1000
+
+
+def test_checkpoint_fixture_wham(orc):
+    # test/testing_data/checkpoint: Ne13, 25 replicas, 102-bin histograms
+    d = json.load(open(os.path.join(GOLDEN, "checkpoint_ne13.json")))
+    p = d["params"]
+    h = np.array(d["histograms"])
+    # the fixture holds 25 histogram rows although params.data says n_traj = 24
+    assert int(p[2]) == 24 and h.shape == (25, 102)
+    R = h.shape[0]
+    T, B = orc.tempgrid(p[8], p[9], R)
+    Tout, cv, it = orc.multihist_nvt(h, T, B, d["hist_info"][0], d["hist_info"][1], 1e-3)
+    assert np.all(np.isfinite(cv)) and np.all(cv > 0)
+    assert Tout[0] == pytest.approx(p[8]) and Tout[-1] == pytest.approx(p[9])
+
+
+def _ne13_start(seed=1234):
+    rng = np.random.default_rng(seed)
+    pos = []
+    while len(pos) < 13:
+        v = rng.uniform(-8, 8, 3)
+        if np.linalg.norm(v) < 8.0 and all(np.linalg.norm(v - q) > 4.5 for q in pos):
+            pos.append(v)
+    return np.array(pos)
+
+
+def test_oracle_run_invariants(orc):
+    """A short Ne13 PT run: detailed bookkeeping invariants of the restatement."""
+    N, R = 13, 8
+    x0 = _ne13_start()
+    T, _ = orc.tempgrid(4.0, 16.0, R)
+    run = orc.Run(N, R, np.stack([x0] * R), T, bc_param=11.0, exch_prob=1.0, seed=5)
+    run.set_elj(C_NE, True)
+    run.init()
+    run.equilibrate(200)
+    run.production(1, 300)
+    x, e, _ = run.slot_states()
+    s = run.slots()
+    # energies equal a fresh recomputation from the positions
+    for i in range(R):
+        assert e[i] == pytest.approx(orc.elj_config_energy(x[i], orc.POT_ELJEVEN, C_NE), rel=1e-12)
+        assert np.all(np.sum(x[i] ** 2, 1) <= 121.0)  # inside the sphere
+    eh, _, hp = run.hist()
+    assert eh.sum() == R * 300  # one histogram entry per slot per cycle
+    assert np.all(s["count_exc"][:, 1] <= s["count_exc"][:, 0])
+    assert sorted(s["wos"]) == list(range(R))
+    fin = run.finalise(300)
+    assert np.all(fin["heat_cap"] >= 0)
+
+
+def test_oracle_npt_invariants(orc):
+    N, R = 32, 4
+    a = 8.4
+    cells = [(i, j, k) for i in range(2) for j in range(2) for k in range(2)]
+    basis = [(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)]
+    x0 = np.array([[(c[d] + b[d]) * a for d in range(3)] for c in cells for b in basis]) - a
+    L = 2 * a
+    T, _ = orc.tempgrid(10.0, 40.0, R)
+    run = orc.Run(N, R, np.stack([x0] * R), T, ensemble=orc.NPT, pressure=3.4439647528956955e-9,
+                  bc=orc.BC_CUBIC, bc_param=L, exch_prob=1.0, seed=9)
+    run.set_elj(C_NE, True)
+    run.init()
+    run.equilibrate(40)
+    run.production(1, 60)
+    x, e, box = run.slot_states()
+    s = run.slots()
+    assert s["count_vol"][:, 0].sum() > 0
+    for i in range(R):
+        rc2 = box[i] * box[i] / 4
+        assert e[i] == pytest.approx(orc.elj_config_energy(x[i], orc.POT_ELJEVEN, C_NE, orc.BC_CUBIC,
+                                                           box[i], rc2), rel=1e-9)
+    _, ev, hp = run.hist()
+    assert ev.sum() == R * 60
