@@ -636,7 +636,7 @@ int cycle(orc_run* r, long index) {
 
 // find_hist_index (Sampling.jl:53-62)
 inline long hist_index(double h, int n_bin) {
-  if (h < 1) return 1;
+  if (!(h >= 1)) return 1;  // NaN lands in the underflow bin (the reference throws)
   if (h > n_bin) return n_bin + 2;
   return (long)std::floor(h) + 1;
 }

@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(1024)
         const int nb = P.n_bin;
         unsigned int* hrow = P.hist + rd.hist_off + (size_t)s * rd.hist_stride;
         auto hidx = [&](double h) -> int {  // find_hist_index (Sampling.jl:53-62)
-          if (h < 1) return 1;
+          if (!(h >= 1)) return 1;          // also catches NaN (the reference throws)
           if (h > nb) return nb + 2;
           return (int)floor(h) + 1;
         };
