@@ -45,21 +45,18 @@ def cu55_ico():
 
 
 def sphere_start(N, radius, min_sep, seed):
-    rng = np.random.default_rng(seed)
-    pos = []
-    while len(pos) < N:
-        v = rng.uniform(-radius, radius, 3)
-        if np.linalg.norm(v) < radius and all(np.linalg.norm(v - q) > min_sep for q in pos):
-            pos.append(v)
-    return np.array(pos)
+    return _starts().sphere_start(N, radius, min_sep, seed)
 
 
 def fcc(ncell, a, jitter, seed):
-    rng = np.random.default_rng(seed)
-    basis = [(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)]
-    x = np.array([[(i + b[0]) * a, (j + b[1]) * a, (k + b[2]) * a]
-                  for i in range(ncell) for j in range(ncell) for k in range(ncell) for b in basis])
-    return x + rng.uniform(-jitter, jitter, x.shape) - ncell * a / 2
+    return _starts().fcc_box(ncell, a, jitter, seed)
+
+
+def _starts():
+    import __graft_entry__ as g
+    g.load_package()
+    import ptmc_gb300.starts as st
+    return st
 
 
 def workload(name):

@@ -123,7 +123,7 @@ __device__ double walker_energy64(const double* X, int N, double L, double rc2,
                                   double ean, double ecam, double* M,
                                   double* comp64, float2* comp32, int lane) {
   double e = 0.0;
-  if (POT == POT_EAM) {
+  if constexpr (POT == POT_EAM) {
     for (int k = lane; k < N; k += 32) {
       double a = 0.0, b = 0.0;
       for (int j = 0; j < N; ++j) {
@@ -142,23 +142,24 @@ __device__ double walker_energy64(const double* X, int N, double L, double rc2,
       e += ean * a - ecam * sqrt(b);
     }
     return warp_sum(e);
-  }
-  for (int i = 0; i < N; ++i) {
-    double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
-    for (int j = i + 1 + lane; j < N; j += 32) {
-      double x = pd2<BC>(xi, yi, zi, X + 3 * j, L);
-      if (M) {
-        M[(size_t)i * N + j] = x;
-        M[(size_t)j * N + i] = x;
+  } else {
+    for (int i = 0; i < N; ++i) {
+      double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+      for (int j = i + 1 + lane; j < N; j += 32) {
+        double x = pd2<BC>(xi, yi, zi, X + 3 * j, L);
+        if (M) {
+          M[(size_t)i * N + j] = x;
+          M[(size_t)j * N + i] = x;
+        }
+        if (ENS == ENS_NPT && !(x <= rc2)) continue;
+        e += v64<POT>(c, K, x);
       }
-      if (ENS == ENS_NPT && !(x <= rc2)) continue;
-      e += v64<POT>(c, K, x);
+      if (M && lane == 0) M[(size_t)i * N + i] = 0.0;
     }
-    if (M && lane == 0) M[(size_t)i * N + i] = 0.0;
+    e = warp_sum(e);
+    if (ENS == ENS_NPT) e = e + lrc64(N, rc2, c, K);
+    return e;
   }
-  e = warp_sum(e);
-  if (ENS == ENS_NPT) e = e + lrc64(N, rc2, c, K);
-  return e;
 }
 
 // ------------------------------------------------------------ init kernel
@@ -722,16 +723,30 @@ template <int POT, int BC, int ENS, bool F32>
 static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
                         int maxN, int ncycles, int phase, cudaStream_t st) {
   dim3 grid(nruns), block(R * 32);
-  if (what == 0) {
+  if constexpr (F32) {
+    if (what == 0) return (int)cudaErrorInvalidValue;  // FP32 form: ptmc_cycles32.cu
+  } else if (what == 0) {
     long long smem = cycles_smem_bytes(POT, ENS, F32, R, maxN);
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(k_cycles<POT, BC, ENS, F32>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-      attr_set = true;
+    // opt in to more than 48 KB of dynamic shared memory when needed, within
+    // the device limit minus the kernel's static shared memory
+    static long long attr_set = 48 * 1024;
+    if (smem > attr_set) {
+      int dev = 0, optin = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      cudaFuncAttributes fa;
+      cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles<POT, BC, ENS, F32>);
+      if (e != cudaSuccess) return (int)e;
+      if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
+      e = cudaFuncSetAttribute(k_cycles<POT, BC, ENS, F32>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return (int)e;
+      attr_set = smem;
     }
     k_cycles<POT, BC, ENS, F32><<<grid, block, (size_t)smem, st>>>(P, run0, ncycles, phase);
-  } else if (what == 1) {
+    return (int)cudaGetLastError();
+  }
+  if (what == 1) {
     k_init<POT, BC, ENS, F32><<<grid, block, 0, st>>>(P, run0);
   } else {
     k_resync<POT, BC, ENS, F32><<<grid, block, 0, st>>>(P, run0);
@@ -768,7 +783,8 @@ static int dispatch(int pot, int bc, int ens, bool f32, int what,
 int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
                   int run0, int nruns, int R, int maxN, int ncycles, int phase,
                   void* stream) {
-  return dispatch(pot, bc, ens, f32, 0, P, run0, nruns, R, maxN, ncycles, phase, stream);
+  if (f32) return launch_cycles32(pot, bc, ens, P, run0, nruns, R, maxN, ncycles, phase, stream);
+  return dispatch(pot, bc, ens, false, 0, P, run0, nruns, R, maxN, ncycles, phase, stream);
 }
 int launch_init(int pot, int bc, int ens, bool f32, const KParams& P, int run0,
                 int nruns, int R, void* stream) {

@@ -1,0 +1,617 @@
+// ptmc_cycles32.cu — replica-cycle kernel of the FP32_RESYNC form.
+//
+// Same execution model as ptmc_cycles.cu (one CTA per PT run, one warp per
+// walker, exchange by slot permutation), but the per-move path issues no FP64
+// instruction: on GB300 the FP64 pipe runs at ~1/70 of the FP32 rate, and a
+// warp-wide FP64 instruction costs the same pipe time whether 1 or 32 lanes are
+// active, so every FP64 operation of the scalar move logic (proposal,
+// Metropolis exp) would cost as much as the whole FP32 pair loop.
+//
+//  * Master positions are int32 fixed point, x = k * q with q = 2^-qbits bohr:
+//    proposals k' = k + round((u - 1/2) * max_displ / q) are exact and exactly
+//    symmetric, and nothing drifts.  A float mirror x_f = fl(k * q) feeds the
+//    pair terms.
+//  * Draws are 32-bit Philox words (word k of a walker stream = word k & 3 of
+//    Philox block k >> 2); u = (w >> 8) * 2^-24, rand(1:n) = mulhi(w, n).
+//  * Metropolis: accept iff ex2(-beta * log2(e) * dE) >= u, dE in FP32.
+//  * The FP64 running total absorbs the FP32 dE sum once per cycle; every
+//    `resync_every` cycles each walker recomputes its energy (and EAM
+//    components) in FP64 from the exact fixed-point positions and records the
+//    drift |E_running - E_fp64|.
+//  * NPT volume moves (rare: one slot in N+1) are evaluated with FP32 pair
+//    terms, Kahan-compensated per lane, FP64 across lanes and for the
+//    enthalpy, long-range correction and acceptance.
+#include <cuda_runtime.h>
+
+#include "ptmc_device.cuh"
+#include "ptmc_engine.cuh"
+
+namespace ptmc {
+
+namespace {
+
+__device__ __forceinline__ float v_even32(const float* c, int K, float r2) {
+  float inv = rcpf(r2);
+  float v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fmaf(v, inv, c[k]);
+  return v * (inv * inv * inv);
+}
+__device__ __forceinline__ float v_all32(const float* c, int K, float r2) {
+  float ir = rsqrtf(r2);
+  float inv = ir * ir;
+  float v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fmaf(v, ir, c[k]);
+  return v * (inv * inv * inv);
+}
+template <int POT>
+__device__ __forceinline__ float v32(const float* c, int K, float r2) {
+  return POT == POT_ELJ ? v_all32(c, K, r2) : v_even32(c, K, r2);
+}
+__device__ __forceinline__ double v_even64(const double* c, int K, double r2) {
+  double inv = 1.0 / r2;
+  double v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fma(v, inv, c[k]);
+  return v * (inv * inv * inv);
+}
+__device__ __forceinline__ double v_all64(const double* c, int K, double r2) {
+  double ir = 1.0 / sqrt(r2);
+  double inv = ir * ir;
+  double v = c[K - 1];
+  for (int k = K - 2; k >= 0; --k) v = fma(v, ir, c[k]);
+  return v * (inv * inv * inv);
+}
+template <int POT>
+__device__ __forceinline__ double v64(const double* c, int K, double r2) {
+  return POT == POT_ELJ ? v_all64(c, K, r2) : v_even64(c, K, r2);
+}
+__device__ double lrc64(int N, double rc2, const double* c, int K) {
+  if (rc2 <= 50) return 0.0;
+  double rcs = sqrt(rc2);
+  double rc3 = rc2 * rcs;
+  double e = 0.0;
+  for (int i = 1; i <= K; ++i) {
+    e += c[i - 1] / rc3 / (2 * i + 1);
+    rc3 *= rc2;
+  }
+  e *= 3.141592653589793 * (double)(N * N) / 4 / (rcs * rcs * rcs);
+  return e;
+}
+
+template <int BC>
+__device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
+  float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+  if (BC == BC_CUB) return f2_cub(dx, dy, dz, L, iL);
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+__device__ __forceinline__ float4 to_f(int4 k, float q) {
+  return make_float4((float)k.x * q, (float)k.y * q, (float)k.z * q, 0.f);
+}
+
+// FP64 energy of one walker from its fixed-point positions (resync).
+template <int POT, int BC, int ENS>
+__device__ double energy64(const int4* Xi, int N, double q, double L, double rc2,
+                           const double* c, int K, double hn, double hm, double ean,
+                           double ecam, float2* comp32, int lane) {
+  auto P = [&](int a, double& x, double& y, double& z) {
+    int4 k = Xi[a];
+    x = k.x * q;
+    y = k.y * q;
+    z = k.z * q;
+  };
+  double e = 0.0;
+  if constexpr (POT == POT_EAM) {
+    for (int a = lane; a < N; a += 32) {
+      double xa, ya, za, A = 0.0, B = 0.0;
+      P(a, xa, ya, za);
+      for (int j = 0; j < N; ++j) {
+        if (j == a) continue;
+        double xj, yj, zj;
+        P(j, xj, yj, zj);
+        double r2 = BC == BC_CUB ? d2_cub(xa, ya, za, xj, yj, zj, L) : d2_sph(xa, ya, za, xj, yj, zj);
+        double lg = log(r2);
+        A += exp(hn * lg);
+        B += exp(hm * lg);
+      }
+      if (comp32) comp32[a] = make_float2((float)A, (float)B);
+      e += ean * A - ecam * sqrt(B);
+    }
+    return warp_sum(e);
+  } else {
+    for (int i = 0; i < N; ++i) {
+      double xi, yi, zi;
+      P(i, xi, yi, zi);
+      for (int j = i + 1 + lane; j < N; j += 32) {
+        double xj, yj, zj;
+        P(j, xj, yj, zj);
+        double r2 = BC == BC_CUB ? d2_cub(xi, yi, zi, xj, yj, zj, L) : d2_sph(xi, yi, zi, xj, yj, zj);
+        if (ENS == ENS_NPT && !(r2 <= rc2)) continue;
+        e += v64<POT>(c, K, r2);
+      }
+    }
+    e = warp_sum(e);
+    if (ENS == ENS_NPT) e += lrc64(N, rc2, c, K);
+    return e;
+  }
+}
+
+}  // namespace
+
+// shared memory bytes of one run CTA (FP32 form)
+long long cycles32_smem_bytes(int pot, int R, int N) {
+  auto al = [](long long b) { return (b + 15) / 16 * 16; };
+  long long b = 0;
+  b += al((long long)R * N * 16);  // int4 fixed-point positions
+  b += al((long long)R * N * 16);  // float4 mirrors
+  if (pot == POT_EAM) b += 2 * al((long long)R * N * 8);  // components, deltas
+  b += al((long long)R * 32 * 4);                         // draw words
+  b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 2;
+  return b;
+}
+
+template <int POT, int BC, int ENS>
+__global__ void __launch_bounds__(1024)
+    k_cycles32(KParams P, int run0, int ncycles, int phase) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double s_c[MAX_COEFF];
+  __shared__ float s_cf[MAX_COEFF];
+  const RunDesc rd = P.runs[run0 + blockIdx.x];
+  const int N = rd.N, R = rd.R;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int nthr = blockDim.x;
+  const int K = P.K;
+  const int n_steps = ENS == ENS_NPT ? N + 1 : N;
+  const double q = P.q;
+  const float qf = (float)P.q;
+  const double iq = 1.0 / P.q;
+
+  unsigned char* sp = smem_raw;
+  auto carve = [&](long long bytes) {
+    unsigned char* p = sp;
+    sp += (bytes + 15) / 16 * 16;
+    return p;
+  };
+  int4* s_xi = (int4*)carve((long long)R * N * 16);
+  float4* s_xf = (float4*)carve((long long)R * N * 16);
+  float2* s_c32 = nullptr;
+  float2* s_d32 = nullptr;
+  if (POT == POT_EAM) {
+    s_c32 = (float2*)carve((long long)R * N * 8);
+    s_d32 = (float2*)carve((long long)R * N * 8);
+  }
+  uint32_t* s_drw = (uint32_t*)carve((long long)R * 32 * 4);
+  double* s_beta = (double*)carve((long long)R * 8);
+  double* s_maxbox = (double*)carve((long long)R * 8);
+  double* s_en = (double*)carve((long long)R * 8);
+  double* s_box = (double*)carve((long long)R * 8);
+  double* s_ham = (double*)carve((long long)R * 16);
+  double* s_maxd = (double*)carve((long long)R * 16);
+  long long* s_cnt = (long long*)carve((long long)R * 48);
+  int* s_wos = (int*)carve((long long)R * 4);
+  int* s_sow = (int*)carve((long long)R * 4);
+
+  if (tid < K) {
+    s_c[tid] = P.c[tid];
+    s_cf[tid] = (float)P.c[tid];
+  }
+  const double* gpos = P.pos + rd.pos_off;
+  for (int k = tid; k < R * N; k += nthr) {
+    int4 v = make_int4(__double2int_rn(gpos[3 * k] * iq), __double2int_rn(gpos[3 * k + 1] * iq),
+                       __double2int_rn(gpos[3 * k + 2] * iq), 0);
+    s_xi[k] = v;
+    s_xf[k] = to_f(v, qf);
+  }
+  if (POT == POT_EAM) {
+    const double* gc = P.comp + rd.comp_off;
+    for (int k = tid; k < R * N; k += nthr) s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
+  }
+  for (int s = tid; s < R; s += nthr) {
+    int g = rd.wk + s;
+    s_beta[s] = P.beta[g];
+    s_maxbox[s] = P.maxbox[g];
+    s_ham[2 * s] = P.ham[2 * g];
+    s_ham[2 * s + 1] = P.ham[2 * g + 1];
+    s_maxd[2 * s] = P.maxd[2 * g];
+    s_maxd[2 * s + 1] = P.maxd[2 * g + 1];
+    for (int k = 0; k < 6; ++k) s_cnt[6 * s + k] = P.cnt[6 * (size_t)g + k];
+    s_wos[s] = P.wos[g];
+  }
+  __syncthreads();
+  for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
+  __syncthreads();
+
+  const int g = rd.wk + w;
+  double en = P.en[g];
+  double L = P.box[g];
+  double rc2 = P.rc2[g];
+  unsigned long long ctr = P.ctr[g];
+  unsigned long long base = ctr + 32;
+  int status = P.status[g];
+  double drift = P.drift[g];
+  int4* Xi = s_xi + (size_t)w * N;
+  float4* Xf = s_xf + (size_t)w * N;
+  uint32_t* drw = s_drw + w * 32;
+  const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
+  const float hnf = (float)hn, hmf = (float)hm, eanf = (float)P.eam_ean, ecamf = (float)P.eam_ecam;
+  const uint32_t run_word = (uint32_t)rd.run_id;
+  float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
+  int Lq = BC == BC_CUB ? __double2int_rn(L * iq) : 0;  // box in grid units
+
+  auto word = [&]() -> uint32_t {
+    if (ctr - base >= 32ull) {
+      __syncwarp();
+      base = ctr & ~3ull;
+      if (lane < 8) {
+        uint64_t blk = (base >> 2) + lane;
+        uint32_t c4[4] = {(uint32_t)blk, (uint32_t)(blk >> 32), (uint32_t)w, run_word};
+        philox4x32_10(c4, (uint32_t)P.seed, (uint32_t)(P.seed >> 32));
+        drw[4 * lane] = c4[0];
+        drw[4 * lane + 1] = c4[1];
+        drw[4 * lane + 2] = c4[2];
+        drw[4 * lane + 3] = c4[3];
+      }
+      __syncwarp();
+    }
+    uint32_t x = drw[ctr - base];
+    ++ctr;
+    return x;
+  };
+  auto uf = [&]() -> float { return (float)(word() >> 8) * 0x1.0p-24f; };
+
+  // ---------------------------------------------------------- atom move
+  auto atom_move = [&](int i, float beta_l2e, float mdq, float& de_acc) -> int {
+    int4 xi = Xi[i];
+    int4 t;
+    auto propose = [&]() {
+      float a = uf(), b = uf(), cc = uf();
+      t.x = xi.x + __float2int_rn((a - 0.5f) * mdq);
+      t.y = xi.y + __float2int_rn((b - 0.5f) * mdq);
+      t.z = xi.z + __float2int_rn((cc - 0.5f) * mdq);
+      t.w = 0;
+    };
+    propose();
+    float4 tf = to_f(t, qf);
+    if (BC == BC_SPH) {
+      const float R2 = Lf * Lf;
+      int count = 0;
+      while (fmaf(tf.x, tf.x, fmaf(tf.y, tf.y, tf.z * tf.z)) > R2) {
+        ++count;
+        if (count == 50) {  // recentre! (src/Configurations.jl:79-85), exact in grid units
+          long long sx = 0, sy = 0, sz = 0;
+          for (int a = lane; a < N; a += 32) {
+            sx += Xi[a].x;
+            sy += Xi[a].y;
+            sz += Xi[a].z;
+          }
+          for (int o = 16; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            sz += __shfl_xor_sync(0xffffffffu, sz, o);
+          }
+          int cx = (int)llrint((double)sx / N), cy = (int)llrint((double)sy / N),
+              cz = (int)llrint((double)sz / N);
+          __syncwarp();
+          for (int a = lane; a < N; a += 32) {
+            int4 v = Xi[a];
+            v.x -= cx;
+            v.y -= cy;
+            v.z -= cz;
+            Xi[a] = v;
+            Xf[a] = to_f(v, qf);
+          }
+          __syncwarp();
+          xi = Xi[i];
+        } else {
+          propose();
+          tf = to_f(t, qf);
+          if (count == 100) {
+            status = ST_SPHERE;
+            return 0;
+          }
+        }
+      }
+    } else {  // periodic wrap by the grid-quantised box
+      t.x -= (int)rintf(tf.x * iLf) * Lq;
+      t.y -= (int)rintf(tf.y * iLf) * Lq;
+      t.z -= (int)rintf(tf.z * iLf) * Lq;
+      tf = to_f(t, qf);
+    }
+    const float4 x4 = Xf[i];
+    float de = 0.f, saf = 0.f, sbf = 0.f;
+    if (POT == POT_EAM) {
+      const float2* C = s_c32 + (size_t)w * N;
+      float2* D = s_d32 + (size_t)w * N;
+      for (int j = lane; j < N; j += 32) {
+        if (j == i) continue;
+        float4 b = Xf[j];
+        float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
+        float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
+        float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
+        float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
+        D[j] = make_float2(da, db);
+        saf += da;
+        sbf += db;
+        float2 c = C[j];
+        float s0 = sqrtf_approx(c.y), s1 = sqrtf_approx(c.y + db);
+        de += eanf * da - ecamf * __fdividef(db, s0 + s1);  // sqrt(rho+d) - sqrt(rho), stable
+      }
+      saf = warp_sum(saf);
+      sbf = warp_sum(sbf);
+      de = warp_sum(de);
+      float2 ci = C[i];
+      float s0 = sqrtf_approx(ci.y), s1 = sqrtf_approx(ci.y + sbf);
+      de += eanf * saf - ecamf * __fdividef(sbf, s0 + s1);
+    } else {
+      for (int j = lane; j < N; j += 32) {
+        if (j == i) continue;
+        float4 b = Xf[j];
+        float dn = pf2<BC>(tf, b, Lf, iLf);
+        float dol = pf2<BC>(x4, b, Lf, iLf);
+        if (ENS == ENS_NPT) {
+          if (dn <= rcf) de += v32<POT>(s_cf, K, dn);
+          if (dol <= rcf) de -= v32<POT>(s_cf, K, dol);
+        } else {
+          de += v32<POT>(s_cf, K, dn) - v32<POT>(s_cf, K, dol);
+        }
+      }
+      de = warp_sum(de);
+    }
+    float u = uf();
+    if (!(ex2f(-beta_l2e * de) >= u)) return 0;
+    __syncwarp();
+    if (lane == 0) {
+      Xi[i] = t;
+      Xf[i] = tf;
+    }
+    if (POT == POT_EAM) {
+      float2* C = s_c32 + (size_t)w * N;
+      const float2* D = s_d32 + (size_t)w * N;
+      for (int k = lane; k < N; k += 32) {
+        float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
+        float2 c = C[k];
+        C[k] = make_float2(c.x + d.x, c.y + d.y);
+      }
+    }
+    de_acc += de;
+    __syncwarp();
+    return 1;
+  };
+
+  // ---------------------------------------------------------- volume move
+  auto volume_move = [&](double beta, double mdv, double maxbox) -> int {
+    double u = (double)uf();
+    double scale = pow(exp((u - 0.5) * mdv), 1.0 / 3.0);
+    if (L >= maxbox && scale > 1.0) scale = 1.0;
+    double Ln = scale * L;
+    double rcn = Ln * Ln / 4;
+    const float s2 = (float)(scale * scale), rcnf = (float)rcn;
+    float acc = 0.f, comp = 0.f;  // Kahan-compensated lane sum
+    for (int i = 0; i < N; ++i) {
+      float4 a = Xf[i];
+      for (int j = i + 1 + lane; j < N; j += 32) {
+        float x = pf2<BC>(a, Xf[j], Lf, iLf) * s2;
+        if (x <= rcnf) {
+          float y = v32<POT>(s_cf, K, x) - comp;
+          float tt = acc + y;
+          comp = (tt - acc) - y;
+          acc = tt;
+        }
+      }
+    }
+    double e = warp_sum((double)acc - (double)comp) + lrc64(N, rcn, s_c, K);
+    double Vn = Ln * Ln * Ln, Vo = L * L * L;
+    double dh = (e - en) + P.pressure * (Vn - Vo);
+    double prob = exp(-dh * beta + (double)N * log(Vn / Vo));
+    double ua = (double)uf();
+    if (!(prob >= ua)) return 0;
+    __syncwarp();
+    for (int a = lane; a < N; a += 32) {
+      int4 v = Xi[a];
+      v.x = __double2int_rn(v.x * scale);
+      v.y = __double2int_rn(v.y * scale);
+      v.z = __double2int_rn(v.z * scale);
+      Xi[a] = v;
+      Xf[a] = to_f(v, qf);
+    }
+    L = Ln;
+    rc2 = rcn;
+    en = e;
+    Lf = (float)L;
+    iLf = (float)(1.0 / L);
+    rcf = (float)rc2;
+    Lq = __double2int_rn(L * iq);
+    __syncwarp();
+    return 1;
+  };
+
+  // ---------------------------------------------------------- cycles
+  const long long first = rd.cyc[phase];
+  unsigned long long run_ctr = rd.run_ctr;
+  const float l2e = 1.4426950408889634f;
+  for (int cyc = 0; cyc < ncycles; ++cyc) {
+    const long long idx = first + cyc;
+    const int slot = s_sow[w];
+    const double beta = s_beta[slot];
+    const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
+    const double maxbox = s_maxbox[slot];
+    const float beta_l2e = (float)beta * l2e;
+    const float mdq = (float)(md * iq);
+    long long acc_a = 0, acc_v = 0;
+    if (status == ST_OK) {
+      float de_acc = 0.f;
+      for (int st = 0; st < n_steps; ++st) {
+        int k = (int)__umulhi(word(), (uint32_t)n_steps);
+        if (k < N) {
+          acc_a += atom_move(k, beta_l2e, mdq, de_acc);
+        } else {
+          en += (double)de_acc;  // fold the FP32 sum before the FP64 enthalpy
+          de_acc = 0.f;
+          acc_v += volume_move(beta, mdv, maxbox);
+        }
+        if (status != ST_OK) break;
+      }
+      en += (double)de_acc;
+      if (P.resync_every > 0 && idx % P.resync_every == 0) {
+        double e64 = energy64<POT, BC, ENS>(Xi, N, q, L, rc2, s_c, K, hn, hm, P.eam_ean,
+                                            P.eam_ecam, POT == POT_EAM ? s_c32 + (size_t)w * N : nullptr,
+                                            lane);
+        drift = fmax(drift, fabs(en - e64));
+        en = e64;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) {
+      s_en[w] = en;
+      s_box[w] = L;
+      s_cnt[6 * slot + 0] += acc_a;
+      s_cnt[6 * slot + 1] += acc_a;
+      s_cnt[6 * slot + 2] += acc_v;
+      s_cnt[6 * slot + 3] += acc_v;
+    }
+    __syncthreads();
+    if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
+      double u = philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++);
+      if (u < P.exch_prob) {
+        int k = randint(philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++), R - 1);
+        s_cnt[6 * k + 4] += 1;
+        s_cnt[6 * (k + 1) + 4] += 1;
+        int w1 = s_wos[k], w2 = s_wos[k + 1];
+        double e1 = s_en[w1], e2 = s_en[w2];
+        if (ENS == ENS_NPT) {
+          double L1 = s_box[w1], L2 = s_box[w2];
+          e1 += P.pressure * (L1 * L1 * L1);
+          e2 += P.pressure * (L2 * L2 * L2);
+        }
+        double acc = exp((s_beta[k] - s_beta[k + 1]) * (e1 - e2));
+        if (acc > 1.0) acc = 1.0;
+        if (acc > philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++)) {
+          s_cnt[6 * k + 5] += 1;
+          s_cnt[6 * (k + 1) + 5] += 1;
+          s_wos[k] = w2;
+          s_wos[k + 1] = w1;
+          s_sow[w2] = k;
+          s_sow[w1] = k + 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < R) {
+      const int s = tid;
+      if (idx % P.n_adjust == 0) {  // update_max_stepsize!
+        double acc = (double)s_cnt[6 * s + 1] / (double)((long long)P.n_adjust * N);
+        if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
+        else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
+        s_cnt[6 * s + 1] = 0;
+        if (ENS == ENS_NPT) {
+          double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);
+          if (av < P.min_acc) s_maxd[2 * s + 1] *= 0.9;
+          else if (av > P.max_acc) s_maxd[2 * s + 1] *= 1.1;
+          s_cnt[6 * s + 3] = 0;
+        }
+      }
+      if (phase == PHASE_PROD && idx % P.mc_sample == 0) {  // sampling_step!
+        const int wk = s_wos[s];
+        const double e = s_en[wk];
+        const int nb = P.n_bin;
+        unsigned int* hrow = P.hist + rd.hist_off + (size_t)s * rd.hist_stride;
+        auto hidx = [&](double h) -> int {
+          if (!(h >= 1)) return 1;
+          if (h > nb) return nb + 2;
+          return (int)floor(h) + 1;
+        };
+        if (ENS == ENS_NPT) {
+          double Lw = s_box[wk];
+          double V = Lw * Lw * Lw;
+          double H = e + P.pressure * V;
+          s_ham[2 * s] += H;
+          s_ham[2 * s + 1] += H * H;
+          int ie = hidx(floor((e - rd.en_min) / rd.dE) + 1);
+          int iv = hidx(floor((V - rd.v_min) / rd.dV) + 1);
+          atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
+        } else {
+          s_ham[2 * s] += e;
+          s_ham[2 * s + 1] += e * e;
+          int ie = hidx((e - rd.en_min) / rd.dE + 1);
+          atomicAdd(hrow + (ie - 1), 1u);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  double* gpos_w = P.pos + rd.pos_off;
+  for (int k = tid; k < R * N; k += nthr) {
+    int4 v = s_xi[k];
+    gpos_w[3 * k] = v.x * q;
+    gpos_w[3 * k + 1] = v.y * q;
+    gpos_w[3 * k + 2] = v.z * q;
+  }
+  if (POT == POT_EAM) {
+    double* gc = P.comp + rd.comp_off;
+    for (int k = tid; k < R * N; k += nthr) {
+      gc[2 * k] = s_c32[k].x;
+      gc[2 * k + 1] = s_c32[k].y;
+    }
+  }
+  if (lane == 0) {
+    P.en[g] = en;
+    P.box[g] = L;
+    P.rc2[g] = rc2;
+    P.ctr[g] = ctr;
+    P.status[g] = status;
+    P.drift[g] = drift;
+  }
+  for (int s = tid; s < R; s += nthr) {
+    int gs = rd.wk + s;
+    P.ham[2 * gs] = s_ham[2 * s];
+    P.ham[2 * gs + 1] = s_ham[2 * s + 1];
+    P.maxd[2 * gs] = s_maxd[2 * s];
+    P.maxd[2 * gs + 1] = s_maxd[2 * s + 1];
+    for (int k = 0; k < 6; ++k) P.cnt[6 * (size_t)gs + k] = s_cnt[6 * s + k];
+    P.wos[gs] = s_wos[s];
+  }
+  if (tid == 0) {
+    P.runs[run0 + blockIdx.x].cyc[phase] = first + ncycles;
+    P.runs[run0 + blockIdx.x].run_ctr = run_ctr;
+  }
+}
+
+template <int POT, int BC, int ENS>
+static int launch32(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
+                    int phase, cudaStream_t st) {
+  long long smem = cycles32_smem_bytes(POT, R, maxN);
+  static long long attr_set = 48 * 1024;
+  if (smem > attr_set) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles32<POT, BC, ENS>);
+    if (e != cudaSuccess) return (int)e;
+    if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    attr_set = smem;
+  }
+  k_cycles32<POT, BC, ENS><<<nruns, R * 32, (size_t)smem, st>>>(P, run0, ncycles, phase);
+  return (int)cudaGetLastError();
+}
+
+int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,
+                    int maxN, int ncycles, int phase, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+#define PT32(PO, B, E) \
+  if (pot == PO && bc == B && ens == E) return launch32<PO, B, E>(P, run0, nruns, R, maxN, ncycles, phase, st);
+  PT32(POT_ELJ, BC_SPH, ENS_NVT)
+  PT32(POT_ELJEVEN, BC_SPH, ENS_NVT)
+  PT32(POT_EAM, BC_SPH, ENS_NVT)
+  PT32(POT_ELJ, BC_CUB, ENS_NVT)
+  PT32(POT_ELJEVEN, BC_CUB, ENS_NVT)
+  PT32(POT_EAM, BC_CUB, ENS_NVT)
+  PT32(POT_ELJEVEN, BC_CUB, ENS_NPT)
+#undef PT32
+  return -1;
+}
+
+}  // namespace ptmc

@@ -71,6 +71,7 @@ struct KParams {
   double min_acc, max_acc;
   int n_bin, n_adjust, mc_sample, resync_every;
   unsigned long long seed;
+  double q;  // FP32 form: fixed-point quantum of the master positions (bohr)
 };
 
 // shared-memory bytes of one run CTA
@@ -94,8 +95,11 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
 
 }  // namespace ptmc
 
-// kernel launch entry points (ptmc_cycles.cu)
+// kernel launch entry points (ptmc_cycles.cu, ptmc_cycles32.cu)
 namespace ptmc {
+long long cycles32_smem_bytes(int pot, int R, int N);
+int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,
+                    int maxN, int ncycles, int phase, void* stream);
 int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
                   int run0, int nruns, int R, int maxN, int ncycles, int phase,
                   void* stream);

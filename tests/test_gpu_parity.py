@@ -17,31 +17,24 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(autouse=True)
+def _pkg(pk):
+    return pk
+
 C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
         -56234083.4334278, 288738837.441765]  # examples/ne13.jl:24-31
 REL = 1e-10
 
 
 def sphere_start(N, radius, min_sep, seed):
-    rng = np.random.default_rng(seed)
-    pos = []
-    tries = 0
-    while len(pos) < N:
-        tries += 1
-        assert tries < 200000
-        v = rng.uniform(-radius, radius, 3)
-        if np.linalg.norm(v) < radius and all(np.linalg.norm(v - q) > min_sep for q in pos):
-            pos.append(v)
-    return np.array(pos)
+    import ptmc_gb300.starts as st
+    return st.sphere_start(N, radius, min_sep, seed)
 
 
 def fcc(ncell, a, jitter, seed):
-    rng = np.random.default_rng(seed)
-    basis = [(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)]
-    x = np.array([[(i + b[0]) * a, (j + b[1]) * a, (k + b[2]) * a]
-                  for i in range(ncell) for j in range(ncell) for k in range(ncell) for b in basis])
-    x += rng.uniform(-jitter, jitter, x.shape)
-    return x - ncell * a / 2
+    import ptmc_gb300.starts as st
+    return st.fcc_box(ncell, a, jitter, seed)
 
 
 def cu55_ico():
