@@ -492,24 +492,6 @@ int ptmc_init(ptmc_ctx* c) {
       wos[g] = w;
     }
   }
-  // FP32 form: master positions are int32 multiples of q = 2^-qbits bohr with
-  // |x| / q < 2^30 for every position the run can reach (sphere radius, or
-  // 1.8 x the box side for NPT); start positions are snapped to the grid.
-  double q = 0.0;
-  if (c->f32()) {
-    double ext = 1.0;
-    for (int d = 0; d < nr; ++d) {
-      const HostRun& h = c->runs[c->run_of_dev[d]];
-      ext = std::max(ext, h.bc == PTMC_BC_CUBIC ? 1.8 * h.bc_param : h.bc_param);
-      for (double x : h.xyz) ext = std::max(ext, std::fabs(x));
-    }
-    int qbits = (int)std::floor(std::log2(std::ldexp(1.0, 30) / (2.0 * ext)));
-    qbits = std::min(qbits, 26);
-    if (qbits < 8) return c->fail(PTMC_ERR_LIMIT, "FP32 form: configuration extent too large for the fixed-point grid");
-    q = std::ldexp(1.0, -qbits);
-    for (double& x : pos) x = std::nearbyint(x / q) * q;
-  }
-  c->K.q = q;
   cudaStream_t s = c->st;
   CK(cudaMemcpyAsync(c->d_pos.p, pos.data(), sizeof(double) * po, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->d_box.p, box.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));

@@ -7,17 +7,20 @@
 // active, so every FP64 operation of the scalar move logic (proposal,
 // Metropolis exp) would cost as much as the whole FP32 pair loop.
 //
-//  * Master positions are int32 fixed point, x = k * q with q = 2^-qbits bohr:
-//    proposals k' = k + round((u - 1/2) * max_displ / q) are exact and exactly
-//    symmetric, and nothing drifts.  A float mirror x_f = fl(k * q) feeds the
-//    pair terms.
+//  * Positions are float-float pairs (hi + lo, ~48 significant bits).  A
+//    proposal adds an FP32 displacement d to (hi, lo) with an error-free
+//    two-sum, so x' - x = d to ~2^-48 relative and the proposal stays
+//    symmetric; the pair terms read hi only.  No int<->float conversion
+//    appears in the move path: on GB300 conversions issue to the FP64 pipe.
 //  * Draws are 32-bit Philox words (word k of a walker stream = word k & 3 of
-//    Philox block k >> 2); u = (w >> 8) * 2^-24, rand(1:n) = mulhi(w, n).
+//    Philox block k >> 2).  Uniforms are built by bit assembly,
+//    u = float(1.m23) - 1, displacements use the symmetric grid
+//    u - 1/2 + 2^-24, and rand(1:n) = mulhi(w, n).
 //  * Metropolis: accept iff ex2(-beta * log2(e) * dE) >= u, dE in FP32.
 //  * The FP64 running total absorbs the FP32 dE sum once per cycle; every
 //    `resync_every` cycles each walker recomputes its energy (and EAM
-//    components) in FP64 from the exact fixed-point positions and records the
-//    drift |E_running - E_fp64|.
+//    components) in FP64 from hi + lo and records the drift
+//    |E_running - E_fp64|.
 //  * NPT volume moves (rare: one slot in N+1) are evaluated with FP32 pair
 //    terms, Kahan-compensated per lane, FP64 across lanes and for the
 //    enthalpy, long-range correction and acceptance.
@@ -84,20 +87,34 @@ __device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
-__device__ __forceinline__ float4 to_f(int4 k, float q) {
-  return make_float4((float)k.x * q, (float)k.y * q, (float)k.z * q, 0.f);
+// (hi, lo) += d, error-free two-sum followed by renormalisation
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
+  float s = hi + d;
+  float bp = s - hi;
+  float err = (hi - (s - bp)) + (d - bp);
+  float l = lo + err;
+  hi = s + l;
+  lo = l - (hi - s);
+}
+// uniform in [0, 1) from the top 23 bits of a Philox word
+__device__ __forceinline__ float u01f(uint32_t w) {
+  return __uint_as_float(0x3F800000u | (w >> 9)) - 1.0f;
+}
+// symmetric uniform in (-1/2, 1/2): (k + 1/2) 2^-23 - 1/2
+__device__ __forceinline__ float usymf(uint32_t w) {
+  return (u01f(w) - 0.5f) + 0x1.0p-24f;
 }
 
 // FP64 energy of one walker from its fixed-point positions (resync).
 template <int POT, int BC, int ENS>
-__device__ double energy64(const int4* Xi, int N, double q, double L, double rc2,
+__device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, double rc2,
                            const double* c, int K, double hn, double hm, double ean,
-                           double ecam, float2* comp32, int lane) {
+                           double ecam, float2* comp32, float* sq32, int lane) {
   auto P = [&](int a, double& x, double& y, double& z) {
-    int4 k = Xi[a];
-    x = k.x * q;
-    y = k.y * q;
-    z = k.z * q;
+    float4 h = Xh[a], l = Xl[a];
+    x = (double)h.x + (double)l.x;
+    y = (double)h.y + (double)l.y;
+    z = (double)h.z + (double)l.z;
   };
   double e = 0.0;
   if constexpr (POT == POT_EAM) {
@@ -114,6 +131,7 @@ __device__ double energy64(const int4* Xi, int N, double q, double L, double rc2
         B += exp(hm * lg);
       }
       if (comp32) comp32[a] = make_float2((float)A, (float)B);
+      if (sq32) sq32[a] = (float)sqrt(B);
       e += ean * A - ecam * sqrt(B);
     }
     return warp_sum(e);
@@ -141,9 +159,9 @@ __device__ double energy64(const int4* Xi, int N, double q, double L, double rc2
 long long cycles32_smem_bytes(int pot, int R, int N) {
   auto al = [](long long b) { return (b + 15) / 16 * 16; };
   long long b = 0;
-  b += al((long long)R * N * 16);  // int4 fixed-point positions
-  b += al((long long)R * N * 16);  // float4 mirrors
-  if (pot == POT_EAM) b += 2 * al((long long)R * N * 8);  // components, deltas
+  b += al((long long)R * N * 16);  // float4 hi positions
+  b += al((long long)R * N * 16);  // float4 lo positions
+  if (pot == POT_EAM) b += 2 * al((long long)R * N * 8) + al((long long)R * N * 4);  // comps, deltas, sqrt(rho)
   b += al((long long)R * 32 * 4);                         // draw words
   b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 2;
   return b;
@@ -155,15 +173,12 @@ __global__ void __launch_bounds__(1024)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
   __shared__ float s_cf[MAX_COEFF];
-  const RunDesc rd = P.runs[run0 + blockIdx.x];
-  const int N = rd.N, R = rd.R;
+  const RunDesc* rdp = P.runs + run0 + blockIdx.x;  // fields read on demand
+  const int N = rdp->N, R = rdp->R;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   const int nthr = blockDim.x;
   const int K = P.K;
   const int n_steps = ENS == ENS_NPT ? N + 1 : N;
-  const double q = P.q;
-  const float qf = (float)P.q;
-  const double iq = 1.0 / P.q;
 
   unsigned char* sp = smem_raw;
   auto carve = [&](long long bytes) {
@@ -171,13 +186,15 @@ __global__ void __launch_bounds__(1024)
     sp += (bytes + 15) / 16 * 16;
     return p;
   };
-  int4* s_xi = (int4*)carve((long long)R * N * 16);
-  float4* s_xf = (float4*)carve((long long)R * N * 16);
+  float4* s_xh = (float4*)carve((long long)R * N * 16);
+  float4* s_xl = (float4*)carve((long long)R * N * 16);
   float2* s_c32 = nullptr;
   float2* s_d32 = nullptr;
+  float* s_sq = nullptr;
   if (POT == POT_EAM) {
     s_c32 = (float2*)carve((long long)R * N * 8);
     s_d32 = (float2*)carve((long long)R * N * 8);
+    s_sq = (float*)carve((long long)R * N * 4);
   }
   uint32_t* s_drw = (uint32_t*)carve((long long)R * 32 * 4);
   double* s_beta = (double*)carve((long long)R * 8);
@@ -194,19 +211,24 @@ __global__ void __launch_bounds__(1024)
     s_c[tid] = P.c[tid];
     s_cf[tid] = (float)P.c[tid];
   }
-  const double* gpos = P.pos + rd.pos_off;
+  const double* gpos = P.pos + rdp->pos_off;
   for (int k = tid; k < R * N; k += nthr) {
-    int4 v = make_int4(__double2int_rn(gpos[3 * k] * iq), __double2int_rn(gpos[3 * k + 1] * iq),
-                       __double2int_rn(gpos[3 * k + 2] * iq), 0);
-    s_xi[k] = v;
-    s_xf[k] = to_f(v, qf);
+    double x = gpos[3 * k], y = gpos[3 * k + 1], z = gpos[3 * k + 2];
+    float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
+    s_xh[k] = h;
+    s_xl[k] = make_float4((float)(x - (double)h.x), (float)(y - (double)h.y),
+                          (float)(z - (double)h.z), 0.f);
   }
   if (POT == POT_EAM) {
-    const double* gc = P.comp + rd.comp_off;
-    for (int k = tid; k < R * N; k += nthr) s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
+    const double* gc = P.comp + rdp->comp_off;
+    for (int k = tid; k < R * N; k += nthr) {
+      s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
+      s_sq[k] = (float)sqrt(gc[2 * k + 1]);
+    }
   }
+  const int wk0 = rdp->wk;
   for (int s = tid; s < R; s += nthr) {
-    int g = rd.wk + s;
+    int g = wk0 + s;
     s_beta[s] = P.beta[g];
     s_maxbox[s] = P.maxbox[g];
     s_ham[2 * s] = P.ham[2 * g];
@@ -220,7 +242,7 @@ __global__ void __launch_bounds__(1024)
   for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
   __syncthreads();
 
-  const int g = rd.wk + w;
+  const int g = wk0 + w;
   double en = P.en[g];
   double L = P.box[g];
   double rc2 = P.rc2[g];
@@ -228,14 +250,15 @@ __global__ void __launch_bounds__(1024)
   unsigned long long base = ctr + 32;
   int status = P.status[g];
   double drift = P.drift[g];
-  int4* Xi = s_xi + (size_t)w * N;
-  float4* Xf = s_xf + (size_t)w * N;
+  float4* Xh = s_xh + (size_t)w * N;
+  float4* Xl = s_xl + (size_t)w * N;
+  float* SQ = s_sq ? s_sq + (size_t)w * N : nullptr;
   uint32_t* drw = s_drw + w * 32;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const float hnf = (float)hn, hmf = (float)hm, eanf = (float)P.eam_ean, ecamf = (float)P.eam_ecam;
-  const uint32_t run_word = (uint32_t)rd.run_id;
+  const uint32_t run_word = (uint32_t)rdp->run_id;
   float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
-  int Lq = BC == BC_CUB ? __double2int_rn(L * iq) : 0;  // box in grid units
+  float Llo = (float)(L - (double)Lf);
 
   auto word = [&]() -> uint32_t {
     if (ctr - base >= 32ull) {
@@ -256,74 +279,71 @@ __global__ void __launch_bounds__(1024)
     ++ctr;
     return x;
   };
-  auto uf = [&]() -> float { return (float)(word() >> 8) * 0x1.0p-24f; };
 
   // ---------------------------------------------------------- atom move
-  auto atom_move = [&](int i, float beta_l2e, float mdq, float& de_acc) -> int {
-    int4 xi = Xi[i];
-    int4 t;
+  auto atom_move = [&](int i, float beta_l2e, float mdf, float& de_acc) -> int {
+    float4 h0 = Xh[i], l0 = Xl[i];
+    float th[3], tl[3];
     auto propose = [&]() {
-      float a = uf(), b = uf(), cc = uf();
-      t.x = xi.x + __float2int_rn((a - 0.5f) * mdq);
-      t.y = xi.y + __float2int_rn((b - 0.5f) * mdq);
-      t.z = xi.z + __float2int_rn((cc - 0.5f) * mdq);
-      t.w = 0;
+      float d0 = usymf(word()) * mdf, d1 = usymf(word()) * mdf, d2 = usymf(word()) * mdf;
+      th[0] = h0.x; tl[0] = l0.x; ff_add(th[0], tl[0], d0);
+      th[1] = h0.y; tl[1] = l0.y; ff_add(th[1], tl[1], d1);
+      th[2] = h0.z; tl[2] = l0.z; ff_add(th[2], tl[2], d2);
     };
     propose();
-    float4 tf = to_f(t, qf);
     if (BC == BC_SPH) {
       const float R2 = Lf * Lf;
       int count = 0;
-      while (fmaf(tf.x, tf.x, fmaf(tf.y, tf.y, tf.z * tf.z)) > R2) {
+      while (fmaf(th[0], th[0], fmaf(th[1], th[1], th[2] * th[2])) > R2) {
         ++count;
-        if (count == 50) {  // recentre! (src/Configurations.jl:79-85), exact in grid units
-          long long sx = 0, sy = 0, sz = 0;
+        if (count == 50) {  // recentre! (src/Configurations.jl:79-85), in FP64
+          double sx = 0, sy = 0, sz = 0;
           for (int a = lane; a < N; a += 32) {
-            sx += Xi[a].x;
-            sy += Xi[a].y;
-            sz += Xi[a].z;
+            sx += (double)Xh[a].x + Xl[a].x;
+            sy += (double)Xh[a].y + Xl[a].y;
+            sz += (double)Xh[a].z + Xl[a].z;
           }
-          for (int o = 16; o > 0; o >>= 1) {
-            sx += __shfl_xor_sync(0xffffffffu, sx, o);
-            sy += __shfl_xor_sync(0xffffffffu, sy, o);
-            sz += __shfl_xor_sync(0xffffffffu, sz, o);
-          }
-          int cx = (int)llrint((double)sx / N), cy = (int)llrint((double)sy / N),
-              cz = (int)llrint((double)sz / N);
+          sx = warp_sum(sx) / N;
+          sy = warp_sum(sy) / N;
+          sz = warp_sum(sz) / N;
           __syncwarp();
           for (int a = lane; a < N; a += 32) {
-            int4 v = Xi[a];
-            v.x -= cx;
-            v.y -= cy;
-            v.z -= cz;
-            Xi[a] = v;
-            Xf[a] = to_f(v, qf);
+            double x = (double)Xh[a].x + Xl[a].x - sx, y = (double)Xh[a].y + Xl[a].y - sy,
+                   z = (double)Xh[a].z + Xl[a].z - sz;
+            float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
+            Xh[a] = h;
+            Xl[a] = make_float4((float)(x - h.x), (float)(y - h.y), (float)(z - h.z), 0.f);
           }
           __syncwarp();
-          xi = Xi[i];
+          h0 = Xh[i];
+          l0 = Xl[i];
         } else {
           propose();
-          tf = to_f(t, qf);
           if (count == 100) {
             status = ST_SPHERE;
             return 0;
           }
         }
       }
-    } else {  // periodic wrap by the grid-quantised box
-      t.x -= (int)rintf(tf.x * iLf) * Lq;
-      t.y -= (int)rintf(tf.y * iLf) * Lq;
-      t.z -= (int)rintf(tf.z * iLf) * Lq;
-      tf = to_f(t, qf);
+    } else {  // periodic wrap t -= L * round(t / L)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float m = rintf(th[k] * iLf);
+        if (m != 0.f) {
+          ff_add(th[k], tl[k], -m * Lf);
+          ff_add(th[k], tl[k], -m * Llo);
+        }
+      }
     }
-    const float4 x4 = Xf[i];
+    const float4 tf = make_float4(th[0], th[1], th[2], 0.f);
+    const float4 x4 = h0;
     float de = 0.f, saf = 0.f, sbf = 0.f;
     if (POT == POT_EAM) {
       const float2* C = s_c32 + (size_t)w * N;
       float2* D = s_d32 + (size_t)w * N;
       for (int j = lane; j < N; j += 32) {
         if (j == i) continue;
-        float4 b = Xf[j];
+        float4 b = Xh[j];
         float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
         float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
         float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
@@ -331,20 +351,19 @@ __global__ void __launch_bounds__(1024)
         D[j] = make_float2(da, db);
         saf += da;
         sbf += db;
-        float2 c = C[j];
-        float s0 = sqrtf_approx(c.y), s1 = sqrtf_approx(c.y + db);
-        de += eanf * da - ecamf * __fdividef(db, s0 + s1);  // sqrt(rho+d) - sqrt(rho), stable
+        float rho = C[j].y;
+        // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
+        de += eanf * da - ecamf * db * rcpf(SQ[j] + sqrtf_approx(rho + db));
       }
       saf = warp_sum(saf);
       sbf = warp_sum(sbf);
       de = warp_sum(de);
-      float2 ci = C[i];
-      float s0 = sqrtf_approx(ci.y), s1 = sqrtf_approx(ci.y + sbf);
-      de += eanf * saf - ecamf * __fdividef(sbf, s0 + s1);
+      float rhoi = C[i].y;
+      de += eanf * saf - ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(rhoi + sbf));
     } else {
       for (int j = lane; j < N; j += 32) {
         if (j == i) continue;
-        float4 b = Xf[j];
+        float4 b = Xh[j];
         float dn = pf2<BC>(tf, b, Lf, iLf);
         float dol = pf2<BC>(x4, b, Lf, iLf);
         if (ENS == ENS_NPT) {
@@ -356,12 +375,12 @@ __global__ void __launch_bounds__(1024)
       }
       de = warp_sum(de);
     }
-    float u = uf();
+    float u = u01f(word());
     if (!(ex2f(-beta_l2e * de) >= u)) return 0;
     __syncwarp();
     if (lane == 0) {
-      Xi[i] = t;
-      Xf[i] = tf;
+      Xh[i] = tf;
+      Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
     }
     if (POT == POT_EAM) {
       float2* C = s_c32 + (size_t)w * N;
@@ -369,7 +388,9 @@ __global__ void __launch_bounds__(1024)
       for (int k = lane; k < N; k += 32) {
         float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
         float2 c = C[k];
-        C[k] = make_float2(c.x + d.x, c.y + d.y);
+        float rho = c.y + d.y;
+        C[k] = make_float2(c.x + d.x, rho);
+        SQ[k] = sqrtf_approx(rho);
       }
     }
     de_acc += de;
@@ -379,7 +400,7 @@ __global__ void __launch_bounds__(1024)
 
   // ---------------------------------------------------------- volume move
   auto volume_move = [&](double beta, double mdv, double maxbox) -> int {
-    double u = (double)uf();
+    double u = (double)u01f(word());
     double scale = pow(exp((u - 0.5) * mdv), 1.0 / 3.0);
     if (L >= maxbox && scale > 1.0) scale = 1.0;
     double Ln = scale * L;
@@ -387,9 +408,9 @@ __global__ void __launch_bounds__(1024)
     const float s2 = (float)(scale * scale), rcnf = (float)rcn;
     float acc = 0.f, comp = 0.f;  // Kahan-compensated lane sum
     for (int i = 0; i < N; ++i) {
-      float4 a = Xf[i];
+      float4 a = Xh[i];
       for (int j = i + 1 + lane; j < N; j += 32) {
-        float x = pf2<BC>(a, Xf[j], Lf, iLf) * s2;
+        float x = pf2<BC>(a, Xh[j], Lf, iLf) * s2;
         if (x <= rcnf) {
           float y = v32<POT>(s_cf, K, x) - comp;
           float tt = acc + y;
@@ -402,31 +423,30 @@ __global__ void __launch_bounds__(1024)
     double Vn = Ln * Ln * Ln, Vo = L * L * L;
     double dh = (e - en) + P.pressure * (Vn - Vo);
     double prob = exp(-dh * beta + (double)N * log(Vn / Vo));
-    double ua = (double)uf();
+    double ua = (double)u01f(word());
     if (!(prob >= ua)) return 0;
     __syncwarp();
     for (int a = lane; a < N; a += 32) {
-      int4 v = Xi[a];
-      v.x = __double2int_rn(v.x * scale);
-      v.y = __double2int_rn(v.y * scale);
-      v.z = __double2int_rn(v.z * scale);
-      Xi[a] = v;
-      Xf[a] = to_f(v, qf);
+      double x = ((double)Xh[a].x + Xl[a].x) * scale, y = ((double)Xh[a].y + Xl[a].y) * scale,
+             z = ((double)Xh[a].z + Xl[a].z) * scale;
+      float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
+      Xh[a] = h;
+      Xl[a] = make_float4((float)(x - h.x), (float)(y - h.y), (float)(z - h.z), 0.f);
     }
     L = Ln;
     rc2 = rcn;
     en = e;
     Lf = (float)L;
+    Llo = (float)(L - (double)Lf);
     iLf = (float)(1.0 / L);
     rcf = (float)rc2;
-    Lq = __double2int_rn(L * iq);
     __syncwarp();
     return 1;
   };
 
   // ---------------------------------------------------------- cycles
-  const long long first = rd.cyc[phase];
-  unsigned long long run_ctr = rd.run_ctr;
+  const long long first = rdp->cyc[phase];
+  unsigned long long run_ctr = rdp->run_ctr;
   const float l2e = 1.4426950408889634f;
   for (int cyc = 0; cyc < ncycles; ++cyc) {
     const long long idx = first + cyc;
@@ -435,14 +455,14 @@ __global__ void __launch_bounds__(1024)
     const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
     const double maxbox = s_maxbox[slot];
     const float beta_l2e = (float)beta * l2e;
-    const float mdq = (float)(md * iq);
+    const float mdf = (float)md;
     long long acc_a = 0, acc_v = 0;
     if (status == ST_OK) {
       float de_acc = 0.f;
       for (int st = 0; st < n_steps; ++st) {
-        int k = (int)__umulhi(word(), (uint32_t)n_steps);
+        int k = (int)__umulhi(word(), (uint32_t)n_steps);  // rand(1:n_steps)
         if (k < N) {
-          acc_a += atom_move(k, beta_l2e, mdq, de_acc);
+          acc_a += atom_move(k, beta_l2e, mdf, de_acc);
         } else {
           en += (double)de_acc;  // fold the FP32 sum before the FP64 enthalpy
           de_acc = 0.f;
@@ -452,9 +472,9 @@ __global__ void __launch_bounds__(1024)
       }
       en += (double)de_acc;
       if (P.resync_every > 0 && idx % P.resync_every == 0) {
-        double e64 = energy64<POT, BC, ENS>(Xi, N, q, L, rc2, s_c, K, hn, hm, P.eam_ean,
+        double e64 = energy64<POT, BC, ENS>(Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean,
                                             P.eam_ecam, POT == POT_EAM ? s_c32 + (size_t)w * N : nullptr,
-                                            lane);
+                                            SQ, lane);
         drift = fmax(drift, fabs(en - e64));
         en = e64;
         __syncwarp();
@@ -513,7 +533,7 @@ __global__ void __launch_bounds__(1024)
         const int wk = s_wos[s];
         const double e = s_en[wk];
         const int nb = P.n_bin;
-        unsigned int* hrow = P.hist + rd.hist_off + (size_t)s * rd.hist_stride;
+        unsigned int* hrow = P.hist + rdp->hist_off + (size_t)s * rdp->hist_stride;
         auto hidx = [&](double h) -> int {
           if (!(h >= 1)) return 1;
           if (h > nb) return nb + 2;
@@ -525,13 +545,13 @@ __global__ void __launch_bounds__(1024)
           double H = e + P.pressure * V;
           s_ham[2 * s] += H;
           s_ham[2 * s + 1] += H * H;
-          int ie = hidx(floor((e - rd.en_min) / rd.dE) + 1);
-          int iv = hidx(floor((V - rd.v_min) / rd.dV) + 1);
+          int ie = hidx(floor((e - rdp->en_min) / rdp->dE) + 1);
+          int iv = hidx(floor((V - rdp->v_min) / rdp->dV) + 1);
           atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
         } else {
           s_ham[2 * s] += e;
           s_ham[2 * s + 1] += e * e;
-          int ie = hidx((e - rd.en_min) / rd.dE + 1);
+          int ie = hidx((e - rdp->en_min) / rdp->dE + 1);
           atomicAdd(hrow + (ie - 1), 1u);
         }
       }
@@ -539,15 +559,15 @@ __global__ void __launch_bounds__(1024)
     __syncthreads();
   }
 
-  double* gpos_w = P.pos + rd.pos_off;
+  double* gpos_w = P.pos + rdp->pos_off;
   for (int k = tid; k < R * N; k += nthr) {
-    int4 v = s_xi[k];
-    gpos_w[3 * k] = v.x * q;
-    gpos_w[3 * k + 1] = v.y * q;
-    gpos_w[3 * k + 2] = v.z * q;
+    float4 h = s_xh[k], l = s_xl[k];
+    gpos_w[3 * k] = (double)h.x + (double)l.x;
+    gpos_w[3 * k + 1] = (double)h.y + (double)l.y;
+    gpos_w[3 * k + 2] = (double)h.z + (double)l.z;
   }
   if (POT == POT_EAM) {
-    double* gc = P.comp + rd.comp_off;
+    double* gc = P.comp + rdp->comp_off;
     for (int k = tid; k < R * N; k += nthr) {
       gc[2 * k] = s_c32[k].x;
       gc[2 * k + 1] = s_c32[k].y;
@@ -562,7 +582,7 @@ __global__ void __launch_bounds__(1024)
     P.drift[g] = drift;
   }
   for (int s = tid; s < R; s += nthr) {
-    int gs = rd.wk + s;
+    int gs = wk0 + s;
     P.ham[2 * gs] = s_ham[2 * s];
     P.ham[2 * gs + 1] = s_ham[2 * s + 1];
     P.maxd[2 * gs] = s_maxd[2 * s];
@@ -570,6 +590,7 @@ __global__ void __launch_bounds__(1024)
     for (int k = 0; k < 6; ++k) P.cnt[6 * (size_t)gs + k] = s_cnt[6 * s + k];
     P.wos[gs] = s_wos[s];
   }
+  __syncthreads();  // every thread has read the run descriptor
   if (tid == 0) {
     P.runs[run0 + blockIdx.x].cyc[phase] = first + ncycles;
     P.runs[run0 + blockIdx.x].run_ctr = run_ctr;

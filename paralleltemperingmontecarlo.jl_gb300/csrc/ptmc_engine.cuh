@@ -71,7 +71,6 @@ struct KParams {
   double min_acc, max_acc;
   int n_bin, n_adjust, mc_sample, resync_every;
   unsigned long long seed;
-  double q;  // FP32 form: fixed-point quantum of the master positions (bohr)
 };
 
 // shared-memory bytes of one run CTA

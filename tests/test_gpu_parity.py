@@ -152,7 +152,9 @@ def test_npt_fp64_parity(pk, orc):
     o.equilibrate(40)
     eng.run_cycles(80)
     o.production(1, 80)
-    g = compare(eng, o)
+    # the volume scale exp(...)^(1/3) comes from the device's exp/pow and the
+    # host's: they may round 1 ulp apart, so positions agree to ~1e-15 here
+    g = compare(eng, o, positions_exact=False)
     assert g["counts"][:, 2].sum() > 0, "some volume moves accepted"
     out = eng.output(0)
     _, ev, hp = o.hist()
