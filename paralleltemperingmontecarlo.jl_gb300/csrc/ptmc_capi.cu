@@ -530,6 +530,10 @@ int ptmc_init(ptmc_ctx* c) {
   K.eam_m = c->eam[1];
   K.eam_ean = c->eam[2];
   K.eam_ecam = c->eam[3];
+  K.f_hn = (float)(-0.5 * c->eam[0]);
+  K.f_hm = (float)(-0.5 * c->eam[1]);
+  K.f_ean = (float)c->eam[2];
+  K.f_ecam = (float)c->eam[3];
   K.pressure = c->p.pressure;
   K.exch_prob = c->p.exch_prob;
   K.min_acc = c->p.min_acc;

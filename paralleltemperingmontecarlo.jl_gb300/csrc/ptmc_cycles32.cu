@@ -163,7 +163,7 @@ long long cycles32_smem_bytes(int pot, int R, int N) {
   b += al((long long)R * N * 16);  // float4 lo positions
   if (pot == POT_EAM) b += 2 * al((long long)R * N * 8) + al((long long)R * N * 4);  // comps, deltas, sqrt(rho)
   b += al((long long)R * 32 * 4);                         // draw words
-  b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 2;
+  b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 4;
   return b;
 }
 
@@ -206,6 +206,8 @@ __global__ void __launch_bounds__(1024)
   long long* s_cnt = (long long*)carve((long long)R * 48);
   int* s_wos = (int*)carve((long long)R * 4);
   int* s_sow = (int*)carve((long long)R * 4);
+  float* s_bl2e = (float*)carve((long long)R * 4);  // beta * log2(e) per slot
+  float* s_mdf = (float*)carve((long long)R * 4);   // atom step size per slot
 
   if (tid < K) {
     s_c[tid] = P.c[tid];
@@ -237,6 +239,8 @@ __global__ void __launch_bounds__(1024)
     s_maxd[2 * s + 1] = P.maxd[2 * g + 1];
     for (int k = 0; k < 6; ++k) s_cnt[6 * s + k] = P.cnt[6 * (size_t)g + k];
     s_wos[s] = P.wos[g];
+    s_bl2e[s] = (float)(P.beta[g] * 1.4426950408889634);
+    s_mdf[s] = (float)P.maxd[2 * g];
   }
   __syncthreads();
   for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(1024)
   float* SQ = s_sq ? s_sq + (size_t)w * N : nullptr;
   uint32_t* drw = s_drw + w * 32;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
-  const float hnf = (float)hn, hmf = (float)hm, eanf = (float)P.eam_ean, ecamf = (float)P.eam_ecam;
+  const float hnf = P.f_hn, hmf = P.f_hm, eanf = P.f_ean, ecamf = P.f_ecam;
   const uint32_t run_word = (uint32_t)rdp->run_id;
   float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
   float Llo = (float)(L - (double)Lf);
@@ -447,15 +451,14 @@ __global__ void __launch_bounds__(1024)
   // ---------------------------------------------------------- cycles
   const long long first = rdp->cyc[phase];
   unsigned long long run_ctr = rdp->run_ctr;
-  const float l2e = 1.4426950408889634f;
   for (int cyc = 0; cyc < ncycles; ++cyc) {
     const long long idx = first + cyc;
     const int slot = s_sow[w];
     const double beta = s_beta[slot];
-    const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
+    const double mdv = s_maxd[2 * slot + 1];
     const double maxbox = s_maxbox[slot];
-    const float beta_l2e = (float)beta * l2e;
-    const float mdf = (float)md;
+    const float beta_l2e = s_bl2e[slot];
+    const float mdf = s_mdf[slot];
     long long acc_a = 0, acc_v = 0;
     if (status == ST_OK) {
       float de_acc = 0.f;
@@ -521,6 +524,7 @@ __global__ void __launch_bounds__(1024)
         double acc = (double)s_cnt[6 * s + 1] / (double)((long long)P.n_adjust * N);
         if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
         else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
+        s_mdf[s] = (float)s_maxd[2 * s];
         s_cnt[6 * s + 1] = 0;
         if (ENS == ENS_NPT) {
           double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);

@@ -71,6 +71,11 @@ struct KParams {
   double min_acc, max_acc;
   int n_bin, n_adjust, mc_sample, resync_every;
   unsigned long long seed;
+  // FP32 copies of the potential constants (FP32 form).  Precomputed on the
+  // host so that no use inside the move loop converts from FP64: under
+  // register pressure the compiler rematerialises constants from their source
+  // expression, and an FP64 -> FP32 conversion issues to the FP64 pipe.
+  float f_hn, f_hm, f_ean, f_ecam;  // -n/2, -m/2, ean, eCam
 };
 
 // shared-memory bytes of one run CTA
