@@ -175,6 +175,28 @@ int ptmc_multihist_npt(int R, int n_bin, const double* ev_hist,
                        double pressure, double thr, double* T_out,
                        double* cp_out, int* iters);
 
+/* Allocation-free multihistogram_NVT, no counterpart in the reference (which
+ * has no device memory at all).  For callers that cannot call cudaMalloc: a
+ * Julia program whose GPU memory belongs to CUDA.jl's pool, code enqueueing
+ * inside a stream capture, or a service that reserves all device memory up
+ * front.  Every pointer is caller-owned DEVICE memory: d_hist [R][n_bin+2],
+ * d_t_grid and d_beta [R] in, d_T_out and d_cv_out [10R] and d_iters [1] out.
+ * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream) and
+ * the call returns without waiting.  The iteration's scratch is a fixed
+ * file-scope device array of PTMC_NOALLOC_SCRATCH_DOUBLES doubles (128 KiB,
+ * held by every GPU that loads the library until exit); inputs that need more
+ * (3R + 3 n_bin + 20R + 2 doubles) return PTMC_ERR_LIMIT.  All calls share
+ * that array, so calls that overlap on the GPU race.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  Results equal
+ * ptmc_multihist_nvt's to rounding. */
+#define PTMC_NOALLOC_SCRATCH_DOUBLES 16384
+int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist,
+                               const double* d_t_grid, const double* d_beta,
+                               double en_min, double en_max, double thr,
+                               double* d_T_out, double* d_cv_out, int* d_iters,
+                               void* stream);
+
 /* Engine utility, no counterpart in the reference: measured FP32 FMA, FP64
  * FMA (TFLOP/s) and MUFU ex2 (Tops/s) peaks of `device`, the roofline
  * denominators of the replica-cycle kernels. */

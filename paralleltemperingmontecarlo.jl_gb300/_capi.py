@@ -74,6 +74,12 @@ SIGNATURES = {
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                           _dp, _dp, _ip]),
+    "ptmc_multihist_nvt_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_double, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
     "ptmc_measure_peaks": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "ptmc_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "ptmc_destroy": (None, [ctypes.c_void_p]),
