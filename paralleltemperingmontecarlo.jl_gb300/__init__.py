@@ -29,7 +29,8 @@ from ._capi import PTMCError
 kB = 3.16681196e-6  # Hartree/K, src/InputParams.jl:19
 
 __all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "Config", "NVT", "NPT",
-           "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "Output", "MCState",
+           "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "RuNNerPotential",
+           "Output", "MCState",
            "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
            "distance2", "get_distance2_mat", "get_volume", "PTMCError"]
 
@@ -184,6 +185,51 @@ class EmbeddedAtomPotential:
             self.eCam = eps * C * a ** (m / 2)
 
 
+class RuNNerPotential:
+    """RuNNerPotential (src/EnergyEvaluation.jl:1182-1213): Behler-Parrinello
+    symmetry functions + per-atom MLP {n_sf, H1, H2, 1} with tanh hidden layers
+    (MachineLearningPotential/ForwardPass.jl:21-41).
+
+    sf: rows {kind (0 radial, 1 angular), type, eta, lambda, zeta, r_cut,
+    G_min, G_max}; weights: per layer W[n_in][n_out] (input-major), then the
+    biases; boundary: hard-core distance (bohr), E = 100 below it
+    (src/EnergyEvaluation.jl:1602-1606)."""
+
+    def __init__(self, sf, weights, nodes=(88, 20, 20, 1), boundary=0.0):
+        self.sf = np.ascontiguousarray(sf, dtype=np.float64).reshape(-1, 8)
+        self.weights = np.ascontiguousarray(weights, dtype=np.float64)
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        self.boundary = float(boundary)
+
+    @staticmethod
+    def sf_table(tables, r_cut=None):
+        """The (n_sf, 8) table from the symmetry-function list of scripts/cu55.jl
+        (as stored in tests/golden/nn_cu55.json), optionally with another cut-off."""
+        rows = []
+        for f in tables["sf"]:
+            rows.append([f["kind"], f["type"], f["eta"], f["lambda"], f["zeta"],
+                         r_cut if r_cut is not None else f["rcut"], f["gmin"], f["gmax"]])
+        return np.array(rows)
+
+    @staticmethod
+    def random_weights(nodes, seed, out_scale=1.0):
+        """FP32-valued weights and biases ~ U(-1/sqrt(fan_in), 1/sqrt(fan_in)),
+        seeded; the last layer is multiplied by out_scale (sets the energy scale)."""
+        rng = np.random.default_rng(seed)
+        w = []
+        for l in range(1, len(nodes)):
+            ni, no = nodes[l - 1], nodes[l]
+            lim = 1.0 / np.sqrt(ni)
+            W = rng.uniform(-lim, lim, (ni, no)).astype(np.float32)
+            bvec = rng.uniform(-lim, lim, no).astype(np.float32)
+            if l == len(nodes) - 1:
+                W = (W * out_scale).astype(np.float32)
+                bvec = (bvec * out_scale).astype(np.float32)
+            w.append(W.astype(np.float64).reshape(-1))
+            w.append(bvec.astype(np.float64))
+        return np.concatenate(w)
+
+
 @dataclass
 class Output:
     """Output{Float64} (src/InputParams.jl:114-176), one run."""
@@ -271,6 +317,11 @@ class Engine:
         elif isinstance(potential, EmbeddedAtomPotential):
             self._ck(self.L.ptmc_set_potential_eam(h, potential.n, potential.m, potential.ean,
                                                    potential.eCam))
+        elif isinstance(potential, RuNNerPotential):
+            self._ck(self.L.ptmc_set_potential_nn(
+                h, _dptr(potential.sf), potential.sf.shape[0], _dptr(potential.weights),
+                len(potential.weights), potential.nodes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                len(potential.nodes), potential.boundary))
         else:
             raise TypeError("unsupported potential %r" % type(potential))
 

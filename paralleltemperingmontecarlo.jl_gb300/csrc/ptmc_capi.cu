@@ -28,6 +28,7 @@
 
 #include "../../include/ptmc_gb300.h"
 #include "ptmc_engine.cuh"
+#include "ptmc_nn.cuh"
 
 using namespace ptmc;
 
@@ -135,6 +136,15 @@ struct ptmc_ctx {
   DBuf<long long> d_cnt;
   DBuf<unsigned int> d_hist;
   KParams K{};
+  // neural-network potential
+  std::vector<NNSF> nn_sf;    // active functions (radial, then angular sorted by eta)
+  std::vector<double> nn_W;   // gathered MLP parameters
+  int nn_H1 = 0, nn_H2 = 0, nn_Nmax = 0;
+  double nn_rcut = 0, nn_boundary2 = 0;
+  DBuf<NNSF> d_nn_sf;
+  DBuf<double> d_nn_W, d_nn_G;
+  DBuf<int> d_nn_row, d_nn_sow;
+  NNParams Q{};
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evfork = nullptr;
   std::vector<cudaEvent_t> evjoin;
@@ -187,6 +197,15 @@ int pull_runs(ptmc_ctx* c) {
 
 // one chunk of `ncyc` cycles for every group, groups on forked streams
 int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
+  if (c->pot == POT_NN) {  // one cycle kernel + one run epilogue per cycle
+    for (int k = 0; k < ncyc; ++k) {
+      int rc = nn_launch_cycle(c->K, c->Q, c->W, (int)c->rd.size(), c->R(), c->nn_Nmax,
+                               !c->f32(), phase, c->st);
+      if (rc) return c->cuda_fail((cudaError_t)rc, "k_nn_cycle launch");
+      c->stats.kernel_launches += 2;
+    }
+    return PTMC_OK;
+  }
   CK(cudaEventRecord(c->evfork, c->st));
   for (size_t g = 0; g < c->groups.size(); ++g) {
     Group& G = c->groups[g];
@@ -203,6 +222,7 @@ int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
 
 int default_chunk(ptmc_ctx* c) {
   if (c->p.cycles_per_launch > 0) return c->p.cycles_per_launch;
+  if (c->pot == POT_NN) return 16;  // cycles per chunk (each cycle is 2 launches)
   // aim at a few milliseconds of work per launch
   int maxN = 0;
   for (auto& G : c->groups) maxN = std::max(maxN, G.N);
@@ -242,7 +262,8 @@ int run_phase(ptmc_ctx* c, long long n, int phase) {
     for (long long k = 0; k < nfull; ++k) {
       CK(cudaGraphLaunch(it->second, c->st));
       c->stats.graph_launches += 1;
-      c->stats.kernel_launches += (long long)reps * c->groups.size();
+      c->stats.kernel_launches +=
+          c->pot == POT_NN ? 2LL * reps * chunk : (long long)reps * c->groups.size();
     }
     done = nfull * chunk * reps;
   }
@@ -289,8 +310,8 @@ int ptmc_create(ptmc_ctx** out, const ptmc_params* p) {
     g_err = "ptmc_create: need n_runs >= 1 and n_traj >= 1";
     return PTMC_ERR_ARG;
   }
-  if (p->n_traj > MAX_REPLICAS) {
-    g_err = "ptmc_create: at most 32 replicas per run (one warp per replica in one CTA)";
+  if (p->n_traj > 1024) {
+    g_err = "ptmc_create: at most 1024 replicas per run";
     return PTMC_ERR_LIMIT;
   }
   if (p->n_bin < 2 || p->n_adjust < 1 || p->mc_sample < 1 || p->mc_cycles < 0 || p->eq_cycles < 0) {
@@ -369,10 +390,61 @@ int ptmc_set_potential_eam(ptmc_ctx* c, double n, double m, double ean, double e
   return PTMC_OK;
 }
 
-int ptmc_set_potential_nn(ptmc_ctx* c, const double*, int, const double*, int,
-                          const int*, int, double) {
-  if (!c) return PTMC_ERR_ARG;
-  return c->fail(PTMC_ERR_STATE, "RuNNerPotential: use ptmc_nn_* entry points (not in this build)");
+int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf, const double* weights, int nw,
+                          const int* nodes, int n_layers, double boundary) {
+  if (!c || !sf || !weights || !nodes) return PTMC_ERR_ARG;
+  if (c->p.ensemble == PTMC_NPT) return c->fail(PTMC_ERR_ARG, "NN potential is supported in the NVT ensemble only");
+  if (n_layers != 4 || nodes[0] != nsf || nodes[3] != 1)
+    return c->fail(PTMC_ERR_ARG, "NN: layers must be {n_sf, H1, H2, 1} (ForwardPass.jl:21)");
+  int H1 = nodes[1], H2 = nodes[2];
+  if (H1 < 1 || H2 < 1 || H1 > 64 || H2 > 64) return c->fail(PTMC_ERR_LIMIT, "NN: hidden layers of 1..64 nodes");
+  long long need = (long long)nsf * H1 + H1 + (long long)H1 * H2 + H2 + H2 + 1;
+  if (need != nw) return c->fail(PTMC_ERR_ARG, "NN: weight count does not match the layer sizes");
+  // active functions: radial type 11 in table order, angular type 111 sorted by eta
+  std::vector<int> rad, ang;
+  double rc = -1;
+  for (int k = 0; k < nsf; ++k) {
+    const double* q = sf + 8 * k;
+    int kind = (int)q[0], type = (int)q[1];
+    if (rc < 0) rc = q[5];
+    if (q[5] != rc) return c->fail(PTMC_ERR_ARG, "NN: all symmetry functions must share one cut-off");
+    if (kind == 0 && type == 11) rad.push_back(k);
+    if (kind == 1 && type == 111) ang.push_back(k);
+  }
+  std::stable_sort(ang.begin(), ang.end(), [&](int a, int b) { return sf[8 * a + 2] < sf[8 * b + 2]; });
+  if ((int)ang.size() > MAX_NN_ANG) return c->fail(PTMC_ERR_LIMIT, "NN: at most 32 active angular functions");
+  std::vector<int> act(rad);
+  act.insert(act.end(), ang.begin(), ang.end());
+  c->nn_sf.clear();
+  for (int k : act) {
+    const double* q = sf + 8 * k;
+    NNSF f{};
+    f.eta = q[2];
+    f.lambda = q[3];
+    f.zeta = q[4];
+    double gmin = q[6], gmax = q[7];
+    f.gnorm = 1 / (gmax - gmin);  // RadialType2 / AngularType3 with [max, min]
+    f.goffset = -gmin * f.gnorm;
+    f.tpz = std::pow(2.0, 1 - f.zeta) * f.gnorm;
+    f.zc = f.zeta == 1 ? 1 : f.zeta == 2 ? 2 : f.zeta == 4 ? 3 : f.zeta == 8 ? 4 : f.zeta == 16 ? 5 : 0;
+    c->nn_sf.push_back(f);
+  }
+  // gather the MLP: W1 rows of the active inputs, the rest unchanged
+  int S = (int)act.size();
+  std::vector<double>& W = c->nn_W;
+  W.clear();
+  for (int q = 0; q < S; ++q)
+    for (int h = 0; h < H1; ++h) W.push_back(weights[(size_t)act[q] * H1 + h]);
+  const double* rest = weights + (size_t)nsf * H1;
+  W.insert(W.end(), rest, rest + (H1 + (size_t)H1 * H2 + H2 + H2 + 1));
+  c->nn_H1 = H1;
+  c->nn_H2 = H2;
+  c->nn_rcut = rc;
+  c->nn_boundary2 = boundary * boundary;
+  c->Q.SR = (int)rad.size();
+  c->Q.SA = (int)ang.size();
+  c->pot = POT_NN;
+  return PTMC_OK;
 }
 
 int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N, int n_start,
@@ -414,6 +486,15 @@ int ptmc_init(ptmc_ctx* c) {
   for (auto& r : c->runs)
     if (r.N == 0) return c->fail(PTMC_ERR_STATE, "every run needs start configurations");
   const int R = c->R();
+  const bool nn = c->pot == POT_NN;
+  if (!nn && R > MAX_REPLICAS)
+    return c->fail(PTMC_ERR_LIMIT, "at most 32 replicas per run (one warp per replica in one CTA)");
+  if (nn) {
+    for (auto& r : c->runs) {
+      if (r.N > MAX_NN_ATOMS) return c->fail(PTMC_ERR_LIMIT, "NN potential: at most 64 atoms");
+      if (r.bc != PTMC_BC_SPHERE) return c->fail(PTMC_ERR_ARG, "NN potential: SphericalBC only");
+    }
+  }
   const bool npt = c->p.ensemble == PTMC_NPT;
   // group runs by N: device order sorted by N (stable)
   int nr = c->p.n_runs;
@@ -430,7 +511,8 @@ int ptmc_init(ptmc_ctx* c) {
     c->groups.back().nruns++;
   }
   for (auto& G : c->groups) {
-    long long smem = c->f32() ? cycles32_smem_bytes(c->pot, R, G.N)
+    long long smem = nn ? 0
+                     : c->f32() ? cycles32_smem_bytes(c->pot, R, G.N)
                               : cycles_smem_bytes(c->pot, c->p.ensemble, false, R, G.N);
     if (smem > 227 * 1024)
       return c->fail(PTMC_ERR_LIMIT, "replica state of a run exceeds 227 KB of shared memory (R*N too large)");
@@ -543,10 +625,48 @@ int ptmc_init(ptmc_ctx* c) {
   K.mc_sample = c->p.mc_sample;
   K.resync_every = c->p.resync_every;
   K.seed = c->p.seed;
-  for (auto& G : c->groups) {
-    int e = launch_init(c->pot, c->bc(), c->p.ensemble, c->f32(), K, G.dev0, G.nruns, R, s);
-    if (e) return c->cuda_fail((cudaError_t)e, "k_init launch");
+  if (nn) {
+    int S = (int)c->nn_sf.size();
+    int Nmax = 0;
+    for (auto& G : c->groups) Nmax = std::max(Nmax, G.N);
+    c->nn_Nmax = Nmax;
+    std::vector<int> row(W), sow(W);
+    for (int d = 0; d < nr; ++d)
+      for (int w = 0; w < R; ++w) {
+        row[c->rd[d].wk + w] = d;
+        sow[c->rd[d].wk + w] = w;
+      }
+    if (c->d_nn_sf.alloc(S) || c->d_nn_W.alloc(c->nn_W.size()) ||
+        c->d_nn_G.alloc((size_t)W * S * Nmax) || c->d_nn_row.alloc(W) || c->d_nn_sow.alloc(W))
+      return c->fail(PTMC_ERR_CUDA, "device allocation failed");
+    CK(cudaMemcpyAsync(c->d_nn_sf.p, c->nn_sf.data(), sizeof(NNSF) * S, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_nn_W.p, c->nn_W.data(), sizeof(double) * c->nn_W.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_nn_row.p, row.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_nn_sow.p, sow.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s));
+    NNParams& Q = c->Q;
+    Q.S = S;
+    Q.H1 = c->nn_H1;
+    Q.H2 = c->nn_H2;
+    Q.nW = (int)c->nn_W.size();
+    Q.Nmax = Nmax;
+    Q.rcut = c->nn_rcut;
+    Q.boundary2 = c->nn_boundary2;
+    Q.sf = c->d_nn_sf.p;
+    Q.W = c->d_nn_W.p;
+    Q.G = c->d_nn_G.p;
+    Q.run_of_walker = c->d_nn_row.p;
+    Q.sow = c->d_nn_sow.p;
+    if (nn_smem_bytes(Q, Nmax, !c->f32()) > 227 * 1024)
+      return c->fail(PTMC_ERR_LIMIT, "NN walker state exceeds 227 KB of shared memory");
+    int e = nn_launch_init(K, Q, W, Nmax, !c->f32(), s);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_nn_init launch");
     c->stats.kernel_launches += 1;
+  } else {
+    for (auto& G : c->groups) {
+      int e = launch_init(c->pot, c->bc(), c->p.ensemble, c->f32(), K, G.dev0, G.nruns, R, s);
+      if (e) return c->cuda_fail((cudaError_t)e, "k_init launch");
+      c->stats.kernel_launches += 1;
+    }
   }
   CK(cudaStreamSynchronize(s));
   c->inited = true;
@@ -613,6 +733,13 @@ int ptmc_run_cycles(ptmc_ctx* c, long long n) {
 int ptmc_resync(ptmc_ctx* c) {
   if (!c) return PTMC_ERR_ARG;
   if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (c->pot == POT_NN) {  // recompute G and the energies from the positions
+    int e = nn_launch_init(c->K, c->Q, c->W, c->nn_Nmax, !c->f32(), c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_nn_init launch");
+    c->stats.kernel_launches += 1;
+    CK(cudaStreamSynchronize(c->st));
+    return PTMC_OK;
+  }
   for (auto& G : c->groups) {
     int e = launch_resync(c->pot, c->bc(), c->p.ensemble, c->f32(), c->K, G.dev0, G.nruns, c->R(), c->st);
     if (e) return c->cuda_fail((cudaError_t)e, "k_resync launch");
@@ -734,6 +861,11 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_wos.free_();
   c->d_cnt.free_();
   c->d_hist.free_();
+  c->d_nn_sf.free_();
+  c->d_nn_W.free_();
+  c->d_nn_G.free_();
+  c->d_nn_row.free_();
+  c->d_nn_sow.free_();
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -867,7 +999,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       (rc = dump(c, b, c->d_drift)) || (rc = dump(c, b, c->d_beta)) || (rc = dump(c, b, c->d_maxd)) ||
       (rc = dump(c, b, c->d_maxbox)) || (rc = dump(c, b, c->d_ham)) || (rc = dump(c, b, c->d_ctr)) ||
       (rc = dump(c, b, c->d_status)) || (rc = dump(c, b, c->d_wos)) || (rc = dump(c, b, c->d_cnt)) ||
-      (rc = dump(c, b, c->d_hist)))
+      (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)))
     return rc;
   put(b, "PTMCEND!", 8);
   if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
@@ -910,7 +1042,8 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
       (rc = undump(c, b, at, c->d_maxd)) || (rc = undump(c, b, at, c->d_maxbox)) ||
       (rc = undump(c, b, at, c->d_ham)) || (rc = undump(c, b, at, c->d_ctr)) ||
       (rc = undump(c, b, at, c->d_status)) || (rc = undump(c, b, at, c->d_wos)) ||
-      (rc = undump(c, b, at, c->d_cnt)) || (rc = undump(c, b, at, c->d_hist)))
+      (rc = undump(c, b, at, c->d_cnt)) || (rc = undump(c, b, at, c->d_hist)) ||
+      (rc = undump(c, b, at, c->d_nn_G)) || (rc = undump(c, b, at, c->d_nn_sow)))
     return rc;
   c->rd = rd;
   c->equilibrated = hdr[3] != 0;

@@ -1,0 +1,681 @@
+// ptmc_nn.cu — RuNNer (Behler-Parrinello) neural-network potential path.
+//
+// RuNNerPotential (src/EnergyEvaluation.jl:1182-1275): per-atom symmetry
+// functions G (radial G2 and angular G4, MachineLearningPotential/SymmFunc.jl
+// :184-312, min/max scaled), updated incrementally when one atom moves
+// (MachineLearningPotential/DeltaMatrix.jl:794-975), fed to a per-atom MLP
+// (ForwardPass.jl:23-84, linear/tanh/.../linear).  Only the active symmetry
+// functions of one element (radial type 11, angular type 111; the others are
+// identically zero, SymmFunc.jl:261,281) are stored; their MLP input rows are
+// gathered on the host.
+//
+// Execution: one CTA of 256 threads per walker (a move is ~10^5 FLOP, far too
+// much for one warp), one launch per MC cycle (N moves per walker), then a
+// per-run epilogue kernel does the exchange, step adaptation and sampling of
+// the cycle.  The host captures [cycle, epilogue] x C in one CUDA graph.
+//
+// Per move:
+//   1. warp 0 draws the proposal (walker stream, reference draw order),
+//   2. threads over j: new/old distance rows, cut-off rows, hard-core test,
+//   3. radial deltas: threads over (sf, j),
+//   4. angular deltas: threads over (j, k-chunk); each ordered pair (j, k)
+//      evaluates the old and new triangle (i, j, k) once and adds the centre-j
+//      term; pairs with j < k also add the centre-i term.  Exponentials are
+//      shared by the functions with equal eta, powers (1 + lambda cos)^zeta by
+//      repeated squaring for zeta in {1, 2, 4, 8, 16},
+//   5. the MLP on every atom (every column of G changes): threads over
+//      (atom, hidden unit), layer by layer, block sum of the atom energies,
+//   6. Metropolis on thread 0, commit (positions, distance and cut-off
+//      matrices, G += dG) on acceptance.
+#include <cuda_runtime.h>
+
+#include "ptmc_device.cuh"
+#include "ptmc_engine.cuh"
+#include "ptmc_nn.cuh"
+
+namespace ptmc {
+
+namespace {
+
+constexpr int NN_THREADS = 256;
+constexpr int NCH = 4;  // k chunks of the angular work items
+
+template <typename Real>
+__device__ __forceinline__ Real rexp(Real x);
+template <>
+__device__ __forceinline__ double rexp<double>(double x) { return exp(x); }
+template <>
+__device__ __forceinline__ float rexp<float>(float x) { return __expf(x); }
+
+template <typename Real>
+__device__ __forceinline__ Real rtanh(Real x);
+template <>
+__device__ __forceinline__ double rtanh<double>(double x) { return tanh(x); }
+template <>
+__device__ __forceinline__ float rtanh<float>(float x) { return tanhf(x); }
+
+// cutoff_function (MachineLearningPotential/Cutoff.jl:79-90)
+template <typename Real>
+__device__ __forceinline__ Real cutoff(Real r, Real rc) {
+  return r < rc ? Real(0.5) * (cos(Real(3.141592653589793) * (r / rc)) + Real(1)) : Real(0);
+}
+
+// (1 + lam*c)^zeta for zeta in {1,2,4,8,16}, general zeta via pow
+template <typename Real>
+__device__ __forceinline__ Real tpow(Real b, int zc, Real zeta) {
+  if (zc == 0) return pow(b, zeta);
+  Real p = b;
+  if (zc >= 2) p = p * p;
+  if (zc >= 3) p = p * p;
+  if (zc >= 4) p = p * p;
+  if (zc >= 5) p = p * p;
+  return p;
+}
+
+template <typename Real>
+struct NNSmem {
+  double* Xd;  // [N][3] positions (FP64 master: proposals and commits)
+  Real* X;     // [N][3] positions in the arithmetic type
+  Real* D2;    // [N][N]
+  Real* F;     // [N][N]
+  Real* G;     // [S][N]
+  Real* dG;    // [S][N]
+  Real* part;  // [NCH][SA][64]
+  Real* rows;  // d2n, fn, rn, d2o, fo, ro [6][64]
+  Real* vn;    // [64][3] t - x_j
+  Real* vo;    // [64][3] x_i - x_j
+  Real* W;     // MLP parameters (gathered layout)
+  Real* h1;    // [N][H1]
+  Real* h2;    // [N][H2]
+  Real* red;   // block-reduction scratch [NN_THREADS/32 + 8]
+  Real* dGi;   // [S] centre-i deltas
+  double* drw; // draw buffer [16]
+  double* tpos;// trial position [3]
+  int* flags;  // [4]
+};
+
+template <typename Real>
+__device__ size_t nn_carve(NNSmem<Real>& s, unsigned char* base, int N, int S, int SA, int H1,
+                           int H2, int nW) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = base + off;
+    off += (bytes + 15) / 16 * 16;
+    return p;
+  };
+  s.Xd = (double*)take(sizeof(double) * N * 3);
+  s.X = (Real*)take(sizeof(Real) * N * 3);
+  s.D2 = (Real*)take(sizeof(Real) * N * N);
+  s.F = (Real*)take(sizeof(Real) * N * N);
+  s.G = (Real*)take(sizeof(Real) * S * N);
+  s.dG = (Real*)take(sizeof(Real) * S * N);
+  s.part = (Real*)take(sizeof(Real) * NCH * (SA > 0 ? SA : 1) * 64);
+  s.rows = (Real*)take(sizeof(Real) * 6 * 64);
+  s.vn = (Real*)take(sizeof(Real) * 64 * 3);
+  s.vo = (Real*)take(sizeof(Real) * 64 * 3);
+  s.W = (Real*)take(sizeof(Real) * nW);
+  s.h1 = (Real*)take(sizeof(Real) * N * H1);
+  s.h2 = (Real*)take(sizeof(Real) * N * H2);
+  s.red = (Real*)take(sizeof(Real) * 64);
+  s.dGi = (Real*)take(sizeof(Real) * (S > 0 ? S : 1));
+  s.drw = (double*)take(sizeof(double) * DRAW_BUF);
+  s.tpos = (double*)take(sizeof(double) * 4);
+  s.flags = (int*)take(sizeof(int) * 4);
+  return off;
+}
+
+template <typename Real>
+__device__ Real block_sum(Real v, Real* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  Real t = 0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : Real(0);
+    t = warp_sum(t);
+    if (threadIdx.x == 0) red[32] = t;
+  }
+  __syncthreads();
+  t = red[32];
+  __syncthreads();
+  return t;
+}
+
+// E = sum_a MLP(G[:, a] + (dG ? dG[:, a] : 0))
+template <typename Real>
+__device__ Real mlp_energy(const NNParams& Q, NNSmem<Real>& s, int N, bool with_delta) {
+  const int S = Q.S, H1 = Q.H1, H2 = Q.H2;
+  const Real* W1 = s.W;               // [S][H1]
+  const Real* B1 = W1 + S * H1;       // [H1]
+  const Real* W2 = B1 + H1;           // [H1][H2]
+  const Real* B2 = W2 + H1 * H2;      // [H2]
+  const Real* W3 = B2 + H2;           // [H2]
+  const Real b3 = W3[H2];
+  for (int t = threadIdx.x; t < N * H1; t += blockDim.x) {
+    int a = t / H1, h = t % H1;
+    Real z = 0;
+    for (int q = 0; q < S; ++q) {
+      Real g = s.G[q * N + a];
+      if (with_delta) g += s.dG[q * N + a];
+      z += g * W1[q * H1 + h];
+    }
+    s.h1[a * H1 + h] = rtanh<Real>(z + B1[h]);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < N * H2; t += blockDim.x) {
+    int a = t / H2, h = t % H2;
+    Real z = 0;
+    for (int q = 0; q < H1; ++q) z += s.h1[a * H1 + q] * W2[q * H2 + h];
+    s.h2[a * H2 + h] = rtanh<Real>(z + B2[h]);
+  }
+  __syncthreads();
+  Real e = 0;
+  for (int a = threadIdx.x; a < N; a += blockDim.x) {
+    Real z = 0;
+    for (int q = 0; q < H2; ++q) z += s.h2[a * H2 + q] * W3[q];
+    e += z + b3;
+  }
+  return block_sum(e, s.red);
+}
+
+template <typename Real>
+__device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X, const double* Gg,
+                            int N) {
+  for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) {
+    s.Xd[k] = X[k];
+    s.X[k] = (Real)X[k];
+  }
+  for (int k = threadIdx.x; k < Q.nW; k += blockDim.x) s.W[k] = (Real)Q.W[k];
+  if (Gg)
+    for (int k = threadIdx.x; k < Q.S * N; k += blockDim.x) s.G[k] = (Real)Gg[k];
+  __syncthreads();
+  for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+    int a = t / N, b = t % N;
+    Real dx = s.X[3 * a] - s.X[3 * b], dy = s.X[3 * a + 1] - s.X[3 * b + 1],
+         dz = s.X[3 * a + 2] - s.X[3 * b + 2];
+    Real d2 = (dx * dx + dy * dy) + dz * dz;
+    s.D2[t] = a == b ? Real(0) : d2;
+    s.F[t] = cutoff<Real>(sqrt(s.D2[t]), (Real)Q.rcut);
+  }
+  __syncthreads();
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- init kernel
+// set_variables + initialise_energy (src/EnergyEvaluation.jl:1812-1822,
+// 1737-1747; total_symm_calc, SymmFunc.jl:494-510, with every angular row).
+template <typename Real>
+__global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int gw = blockIdx.x;  // global walker
+  const int run = Q.run_of_walker[gw];
+  const RunDesc* rd = P.runs + run;
+  const int N = rd->N, w = gw - rd->wk;
+  NNSmem<Real> s;
+  nn_carve(s, smem_raw, N, Q.S, Q.SA, Q.H1, Q.H2, Q.nW);
+  const double* X = P.pos + rd->pos_off + (size_t)w * N * 3;
+  load_walker(Q, s, X, nullptr, N);
+  const int S = Q.S, SR = Q.SR;
+  for (int t = threadIdx.x; t < S * N; t += blockDim.x) s.G[t] = 0;
+  __syncthreads();
+  // radial: G_s[a] = sum_b gnorm f_ab exp(-eta r2_ab) (fc != 0, 1 excluded, SymmFunc.jl:234)
+  for (int t = threadIdx.x; t < SR * N; t += blockDim.x) {
+    int q = t / N, a = t % N;
+    const NNSF& f = Q.sf[q];
+    Real g = 0;
+    for (int b = 0; b < N; ++b) {
+      if (b == a) continue;
+      Real fc = s.F[a * N + b];
+      if (fc != Real(0) && fc != Real(1))
+        g += fc * rexp<Real>(-(Real)f.eta * s.D2[a * N + b]) * (Real)f.gnorm;
+    }
+    s.G[q * N + a] = g + (Real)f.goffset;
+  }
+  // angular: centre a, pairs b < c
+  for (int t = threadIdx.x; t < (S - SR) * N; t += blockDim.x) {
+    int q = SR + t / N, a = t % N;
+    const NNSF& f = Q.sf[q];
+    Real g = 0;
+    for (int b = 0; b < N; ++b) {
+      if (b == a) continue;
+      for (int c = b + 1; c < N; ++c) {
+        if (c == a) continue;
+        Real rab = s.D2[a * N + b], rac = s.D2[a * N + c], rbc = s.D2[b * N + c];
+        Real ex = rexp<Real>(-(Real)f.eta * (rab + rac + rbc)) * s.F[a * N + b] * s.F[a * N + c] *
+                  s.F[b * N + c];
+        if (ex == Real(0)) continue;
+        Real abx = s.X[3 * a] - s.X[3 * b], aby = s.X[3 * a + 1] - s.X[3 * b + 1],
+             abz = s.X[3 * a + 2] - s.X[3 * b + 2];
+        Real acx = s.X[3 * a] - s.X[3 * c], acy = s.X[3 * a + 1] - s.X[3 * c + 1],
+             acz = s.X[3 * a + 2] - s.X[3 * c + 2];
+        Real cs = ((abx * acx + aby * acy) + abz * acz) / (sqrt(rab) * sqrt(rac));
+        g += ex * tpow<Real>(Real(1) + (Real)f.lambda * cs, f.zc, (Real)f.zeta) * (Real)f.tpz;
+      }
+    }
+    s.G[q * N + a] = g + (Real)f.goffset;
+  }
+  __syncthreads();
+  Real e = mlp_energy<Real>(Q, s, N, false);
+  double* Gg = Q.G + (size_t)gw * S * Q.Nmax;
+  for (int t = threadIdx.x; t < S * N; t += blockDim.x) Gg[t] = (double)s.G[t];
+  if (threadIdx.x == 0) {
+    P.en[rd->wk + w] = (double)e;
+    P.status[rd->wk + w] = ST_OK;
+    P.drift[rd->wk + w] = 0.0;
+  }
+}
+
+// --------------------------------------------------------------- cycle kernel
+template <typename Real>
+__global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, int phase) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int gw = blockIdx.x;
+  const int run = Q.run_of_walker[gw];
+  const RunDesc* rd = P.runs + run;
+  const int N = rd->N, w = gw - rd->wk, g = rd->wk + w;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int S = Q.S, SR = Q.SR, SA = Q.SA;
+  NNSmem<Real> s;
+  nn_carve(s, smem_raw, N, S, SA, Q.H1, Q.H2, Q.nW);
+  double* Xg = P.pos + rd->pos_off + (size_t)w * N * 3;
+  double* Gg = Q.G + (size_t)gw * S * Q.Nmax;
+  load_walker(Q, s, Xg, Gg, N);
+  if (P.status[g] != ST_OK) return;
+  const int slot = Q.sow[g];
+  const int gs = rd->wk + slot;
+  const double beta = P.beta[gs];
+  const double md = P.maxd[2 * gs];
+  double en = P.en[g];
+  unsigned long long ctr = P.ctr[g];
+  unsigned long long base = ctr + DRAW_BUF;
+  int status = ST_OK;
+  long long acc = 0;
+  const Real rc = (Real)Q.rcut;
+  const uint32_t run_word = (uint32_t)rd->run_id;
+  const double R2 = P.box[g] * P.box[g];
+
+  auto draw = [&]() -> double {  // warp 0 only, lanes in lockstep
+    if (ctr - base >= (unsigned long long)DRAW_BUF) {
+      __syncwarp();
+      base = ctr & ~1ull;
+      if (lane < DRAW_BUF / 2) {
+        double u0, u1;
+        philox_pair(P.seed, (uint32_t)w, run_word, (base >> 1) + lane, u0, u1);
+        s.drw[2 * lane] = u0;
+        s.drw[2 * lane + 1] = u1;
+      }
+      __syncwarp();
+    }
+    double u = s.drw[ctr - base];
+    ++ctr;
+    return u;
+  };
+
+  for (int step = 0; step < N; ++step) {
+    // ---- 1. proposal (atom_displacement, src/MCMoves.jl:33-48, 115-143)
+    if (warp == 0) {
+      int i = randint(draw(), N);
+      double xi = s.Xd[3 * i], yi = s.Xd[3 * i + 1], zi = s.Xd[3 * i + 2];
+      double tx, ty, tz;
+      auto propose = [&]() {
+        double ux = draw(), uy = draw(), uz = draw();
+        tx = dadd(xi, dmul(dsub(ux, 0.5), md));
+        ty = dadd(yi, dmul(dsub(uy, 0.5), md));
+        tz = dadd(zi, dmul(dsub(uz, 0.5), md));
+      };
+      propose();
+      int count = 0, err = 0, rec = 0;
+      while (dot3(tx, ty, tz) > R2) {
+        ++count;
+        if (count == 50) {
+          rec = 1;  // recentre handled by the whole CTA below (rare path)
+          break;
+        }
+        propose();
+        if (count == 100) {
+          err = 1;
+          break;
+        }
+      }
+      if (lane == 0) {
+        s.tpos[0] = tx;
+        s.tpos[1] = ty;
+        s.tpos[2] = tz;
+        s.flags[0] = i;
+        s.flags[1] = err;
+        s.flags[2] = rec;
+        s.flags[3] = 0;
+      }
+    }
+    __syncthreads();
+    if (s.flags[2]) {
+      // recentre! at the 50th retry (src/MCMoves.jl:126-128): the rare path
+      // shifts the configuration and the move continues with fresh proposals
+      if (tid == 0) {  // mean of the positions, in order (src/Configurations.jl:64-85)
+        double cx = 0, cy = 0, cz = 0;
+        for (int a = 0; a < N; ++a) {
+          cx += s.Xd[3 * a];
+          cy += s.Xd[3 * a + 1];
+          cz += s.Xd[3 * a + 2];
+        }
+        cx /= N;
+        cy /= N;
+        cz /= N;
+        for (int a = 0; a < N; ++a) {
+          s.Xd[3 * a] -= cx;
+          s.Xd[3 * a + 1] -= cy;
+          s.Xd[3 * a + 2] -= cz;
+          s.X[3 * a] = (Real)s.Xd[3 * a];
+          s.X[3 * a + 1] = (Real)s.Xd[3 * a + 1];
+          s.X[3 * a + 2] = (Real)s.Xd[3 * a + 2];
+        }
+      }
+      __syncthreads();
+      if (warp == 0) {
+        int i = s.flags[0];
+        double xi = s.Xd[3 * i], yi = s.Xd[3 * i + 1], zi = s.Xd[3 * i + 2];
+        double tx = 0, ty = 0, tz = 0;
+        int err = 1;
+        for (int count = 51; count <= 100; ++count) {
+          double ux = draw(), uy = draw(), uz = draw();
+          tx = dadd(xi, dmul(dsub(ux, 0.5), md));
+          ty = dadd(yi, dmul(dsub(uy, 0.5), md));
+          tz = dadd(zi, dmul(dsub(uz, 0.5), md));
+          if (count == 100) break;
+          if (!(dot3(tx, ty, tz) > R2)) {
+            err = 0;
+            break;
+          }
+        }
+        if (lane == 0) {
+          s.tpos[0] = tx;
+          s.tpos[1] = ty;
+          s.tpos[2] = tz;
+          s.flags[1] = err;
+        }
+      }
+      __syncthreads();
+    }
+    if (s.flags[1]) {
+      status = ST_SPHERE;
+      break;
+    }
+    const int i = s.flags[0];
+    const Real tx = (Real)s.tpos[0], ty = (Real)s.tpos[1], tz = (Real)s.tpos[2];
+    Real* d2n = s.rows;
+    Real* fn = s.rows + 64;
+    Real* rn = s.rows + 128;
+    Real* d2o = s.rows + 192;
+    Real* fo = s.rows + 256;
+    Real* ro = s.rows + 320;
+    // ---- 2. rows and hard core (energy_update! RuNNer, src/EnergyEvaluation.jl:1593-1606)
+    int hard = 0;
+    for (int j = tid; j < N; j += blockDim.x) {
+      Real vx = tx - s.X[3 * j], vy = ty - s.X[3 * j + 1], vz = tz - s.X[3 * j + 2];
+      Real d = (vx * vx + vy * vy) + vz * vz;
+      if (j == i) d = 0;
+      d2n[j] = d;
+      rn[j] = sqrt(d);
+      fn[j] = cutoff<Real>(rn[j], rc);
+      s.vn[3 * j] = vx;
+      s.vn[3 * j + 1] = vy;
+      s.vn[3 * j + 2] = vz;
+      Real ox = s.X[3 * i] - s.X[3 * j], oy = s.X[3 * i + 1] - s.X[3 * j + 1],
+           oz = s.X[3 * i + 2] - s.X[3 * j + 2];
+      s.vo[3 * j] = ox;
+      s.vo[3 * j + 1] = oy;
+      s.vo[3 * j + 2] = oz;
+      d2o[j] = s.D2[i * N + j];
+      ro[j] = sqrt(d2o[j]);
+      fo[j] = s.F[i * N + j];
+      if (j != i && d < (Real)Q.boundary2) hard = 1;
+    }
+    hard = __syncthreads_or(hard);
+    Real new_en;
+    if (hard) {
+      new_en = Real(100.0);
+    } else {
+      for (int q = tid; q < S; q += blockDim.x) s.dGi[q] = 0;
+      __syncthreads();
+      // ---- 3. radial deltas (radial_symmetry_calculation!, DeltaMatrix.jl:794-822)
+      for (int t = tid; t < SR * N; t += blockDim.x) {
+        int q = t / N, j = t % N;
+        Real d = 0;
+        if (j != i) {
+          const NNSF& f = Q.sf[q];
+          Real eta = (Real)f.eta, gn = (Real)f.gnorm;
+          d = rexp<Real>(-eta * d2n[j]) * (fn[j] * gn) - rexp<Real>(-eta * d2o[j]) * (fo[j] * gn);
+          atomicAdd(&s.dGi[q], d);
+        }
+        s.dG[q * N + j] = d;
+      }
+      // ---- 4. angular deltas (angular_symmetry_calculation!, DeltaMatrix.jl:827-871)
+      {
+        const int j = tid % 64, c = tid / 64;
+        Real accj[MAX_NN_ANG], acci[MAX_NN_ANG];
+        for (int q = 0; q < SA; ++q) {
+          accj[q] = 0;
+          acci[q] = 0;
+        }
+        if (j < N && j != i) {
+          const int k0 = (c * N) / NCH, k1 = ((c + 1) * N) / NCH;
+          const Real vnx = s.vn[3 * j], vny = s.vn[3 * j + 1], vnz = s.vn[3 * j + 2];
+          const Real vox = s.vo[3 * j], voy = s.vo[3 * j + 1], voz = s.vo[3 * j + 2];
+          const Real rnj = rn[j], roj = ro[j], fnj = fn[j], foj = fo[j];
+          for (int k = k0; k < k1; ++k) {
+            if (k == i || k == j) continue;
+            const Real rjk2 = s.D2[j * N + k], fjk = s.F[j * N + k];
+            const Real fpn = fnj * fn[k] * fjk, fpo = foj * fo[k] * fjk;
+            if (fpn == Real(0) && fpo == Real(0)) continue;
+            const Real rjk = sqrt(rjk2);
+            // x_k - x_j
+            const Real ux = s.X[3 * k] - s.X[3 * j], uy = s.X[3 * k + 1] - s.X[3 * j + 1],
+                       uz = s.X[3 * k + 2] - s.X[3 * j + 2];
+            // angle at j: (t - x_j).(x_k - x_j) / (|t - x_j| |x_k - x_j|)
+            const Real cjn = ((vnx * ux + vny * uy) + vnz * uz) / (rnj * rjk);
+            const Real cjo = ((vox * ux + voy * uy) + voz * uz) / (roj * rjk);
+            const Real sn = (d2n[j] + d2n[k]) + rjk2, so = (d2o[j] + d2o[k]) + rjk2;
+            const bool ci_on = j < k;
+            Real cin = 0, cio = 0;
+            if (ci_on) {  // angle at the moved atom: (x_j - t).(x_k - t) / (r_j r_k)
+              cin = ((vnx * s.vn[3 * k] + vny * s.vn[3 * k + 1]) + vnz * s.vn[3 * k + 2]) / (rnj * rn[k]);
+              cio = ((vox * s.vo[3 * k] + voy * s.vo[3 * k + 1]) + voz * s.vo[3 * k + 2]) / (roj * ro[k]);
+            }
+            Real en_e = 0, eo_e = 0, last_eta = -1;
+            for (int q = 0; q < SA; ++q) {
+              const NNSF& f = Q.sf[SR + q];
+              const Real eta = (Real)f.eta;
+              if (eta != last_eta) {  // functions are sorted by eta: one exp pair per distinct eta
+                en_e = rexp<Real>(-eta * sn) * fpn;
+                eo_e = rexp<Real>(-eta * so) * fpo;
+                last_eta = eta;
+              }
+              const Real lam = (Real)f.lambda, tpz = (Real)f.tpz;
+              accj[q] += (en_e * tpow<Real>(Real(1) + lam * cjn, f.zc, (Real)f.zeta) -
+                          eo_e * tpow<Real>(Real(1) + lam * cjo, f.zc, (Real)f.zeta)) * tpz;
+              if (ci_on)
+                acci[q] += (en_e * tpow<Real>(Real(1) + lam * cin, f.zc, (Real)f.zeta) -
+                            eo_e * tpow<Real>(Real(1) + lam * cio, f.zc, (Real)f.zeta)) * tpz;
+            }
+          }
+        }
+        for (int q = 0; q < SA; ++q) {
+          s.part[(c * SA + q) * 64 + j] = accj[q];
+          Real v = warp_sum(acci[q]);
+          if (lane == 0 && v != Real(0)) atomicAdd(&s.dGi[SR + q], v);
+        }
+      }
+      __syncthreads();
+      for (int t = tid; t < SA * N; t += blockDim.x) {
+        int q = t / N, j = t % N;
+        Real v = 0;
+        if (j != i)
+          for (int c = 0; c < NCH; ++c) v += s.part[(c * SA + q) * 64 + j];
+        s.dG[(SR + q) * N + j] = v;
+      }
+      __syncthreads();
+      for (int q = tid; q < S; q += blockDim.x) s.dG[q * N + i] = s.dGi[q];
+      __syncthreads();
+      // ---- 5. MLP on every atom (calc_new_runner_energy!, src/EnergyEvaluation.jl:1269-1275)
+      new_en = mlp_energy<Real>(Q, s, N, true);
+    }
+    // ---- 6. Metropolis (src/MCRun.jl:122-132) and commit (swap_vars!, swap_config.jl:213-221)
+    if (warp == 0) {
+      double prob = exp(-((double)new_en - en) * beta);
+      if (prob > 1) prob = 1.0;
+      double u = draw();
+      if (lane == 0) s.flags[3] = (prob >= u) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s.flags[3]) {
+      for (int j = tid; j < N; j += blockDim.x) {
+        Real d = d2n[j];
+        s.D2[i * N + j] = d;
+        s.D2[j * N + i] = d;
+        if (!hard) {  // the hard-core branch computes no new cut-off row or G
+          Real f = fn[j];
+          s.F[i * N + j] = f;
+          s.F[j * N + i] = f;
+        }
+      }
+      if (!hard)
+        for (int t = tid; t < S * N; t += blockDim.x) s.G[t] += s.dG[t];
+      __syncthreads();
+      if (tid == 0) {
+        for (int k = 0; k < 3; ++k) {
+          s.Xd[3 * i + k] = s.tpos[k];
+          s.X[3 * i + k] = (Real)s.tpos[k];
+        }
+      }
+      en = (double)new_en;
+      ++acc;
+    }
+    __syncthreads();
+  }
+  // store back
+  for (int k = tid; k < 3 * N; k += blockDim.x) Xg[k] = s.Xd[k];
+  for (int t = tid; t < S * N; t += blockDim.x) Gg[t] = (double)s.G[t];
+  if (tid == 0) {
+    P.en[g] = en;
+    P.status[g] = status;
+    P.cnt[6 * (size_t)gs + 0] += acc;
+    P.cnt[6 * (size_t)gs + 1] += acc;
+  }
+  if (warp == 0 && lane == 0) P.ctr[g] = ctr;
+}
+
+// --------------------------------------------------------------- run epilogue
+// After every walker finished its cycle: exchange (src/Exchange.jl:132-154),
+// step adaptation (src/Exchange.jl:250-257) and sampling (src/Sampling.jl:330-371)
+// of one run, on global slot tables.  One CTA per run, one thread per slot.
+__global__ void k_run_epilogue(KParams P, NNParams Q, int run0, int phase) {
+  RunDesc* rd = P.runs + run0 + blockIdx.x;
+  const int R = rd->R, N = rd->N, wk = rd->wk, s = threadIdx.x;
+  const long long idx = rd->cyc[phase];
+  const uint32_t run_word = (uint32_t)rd->run_id;
+  if (s == 0 && R > 1) {
+    unsigned long long rc = rd->run_ctr;
+    double u = philox_u01(P.seed, 0xFFFFFFFFu, run_word, rc++);
+    if (u < P.exch_prob) {
+      int k = randint(philox_u01(P.seed, 0xFFFFFFFFu, run_word, rc++), R - 1);
+      P.cnt[6 * (size_t)(wk + k) + 4] += 1;
+      P.cnt[6 * (size_t)(wk + k + 1) + 4] += 1;
+      int w1 = P.wos[wk + k], w2 = P.wos[wk + k + 1];
+      double e1 = P.en[wk + w1], e2 = P.en[wk + w2];
+      double a = exp((P.beta[wk + k] - P.beta[wk + k + 1]) * (e1 - e2));
+      if (a > 1.0) a = 1.0;
+      if (a > philox_u01(P.seed, 0xFFFFFFFFu, run_word, rc++)) {
+        P.cnt[6 * (size_t)(wk + k) + 5] += 1;
+        P.cnt[6 * (size_t)(wk + k + 1) + 5] += 1;
+        P.wos[wk + k] = w2;
+        P.wos[wk + k + 1] = w1;
+        Q.sow[wk + w2] = k;
+        Q.sow[wk + w1] = k + 1;
+      }
+    }
+    rd->run_ctr = rc;
+  }
+  __syncthreads();
+  if (s < R) {
+    const int gs = wk + s;
+    if (idx % P.n_adjust == 0) {
+      double acc = (double)P.cnt[6 * (size_t)gs + 1] / (double)((long long)P.n_adjust * N);
+      if (acc < P.min_acc) P.maxd[2 * gs] *= 0.9;
+      else if (acc > P.max_acc) P.maxd[2 * gs] *= 1.1;
+      P.cnt[6 * (size_t)gs + 1] = 0;
+    }
+    if (phase == PHASE_PROD && idx % P.mc_sample == 0) {
+      const double e = P.en[wk + P.wos[gs]];
+      P.ham[2 * gs] += e;
+      P.ham[2 * gs + 1] = dadd(P.ham[2 * gs + 1], dmul(e, e));
+      const int nb = P.n_bin;
+      double h = (e - rd->en_min) / rd->dE + 1;
+      int ie = !(h >= 1) ? 1 : (h > nb ? nb + 2 : (int)floor(h) + 1);
+      atomicAdd(P.hist + rd->hist_off + (size_t)s * rd->hist_stride + (ie - 1), 1u);
+    }
+  }
+  __syncthreads();
+  if (s == 0) rd->cyc[phase] = idx + 1;
+}
+
+// --------------------------------------------------------------- launchers
+size_t nn_smem_bytes(const NNParams& Q, int N, bool f64) {
+  size_t es = f64 ? 8 : 4;
+  auto al = [](size_t b) { return (b + 15) / 16 * 16; };
+  size_t b = 0;
+  b += al(8 * N * 3) + al(es * N * 3) + 2 * al(es * N * N) + 2 * al(es * Q.S * N);
+  b += al(es * NCH * (Q.SA > 0 ? Q.SA : 1) * 64) + al(es * 6 * 64) + 2 * al(es * 64 * 3);
+  b += al(es * Q.nW) + al(es * N * Q.H1) + al(es * N * Q.H2) + al(es * 64) + al(es * (Q.S > 0 ? Q.S : 1));
+  b += al(8 * DRAW_BUF) + al(8 * 4) + al(4 * 4);
+  return b;
+}
+
+template <typename K>
+static int set_smem(K kern, size_t smem) {
+  if (smem <= 48 * 1024) return 0;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+  if (e != cudaSuccess) return (int)e;
+  if ((long long)smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
+  return (int)cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+int nn_launch_init(const KParams& P, const NNParams& Q, int n_walkers, int maxN, bool f64,
+                   void* stream) {
+  size_t smem = nn_smem_bytes(Q, maxN, f64);
+  cudaStream_t st = (cudaStream_t)stream;
+  int e;
+  if (f64) {
+    if ((e = set_smem(k_nn_init<double>, smem))) return e;
+    k_nn_init<double><<<n_walkers, NN_THREADS, smem, st>>>(P, Q);
+  } else {
+    if ((e = set_smem(k_nn_init<float>, smem))) return e;
+    k_nn_init<float><<<n_walkers, NN_THREADS, smem, st>>>(P, Q);
+  }
+  return (int)cudaGetLastError();
+}
+
+int nn_launch_cycle(const KParams& P, const NNParams& Q, int n_walkers, int n_runs, int R,
+                    int maxN, bool f64, int phase, void* stream) {
+  size_t smem = nn_smem_bytes(Q, maxN, f64);
+  cudaStream_t st = (cudaStream_t)stream;
+  int e;
+  if (f64) {
+    if ((e = set_smem(k_nn_cycle<double>, smem))) return e;
+    k_nn_cycle<double><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
+  } else {
+    if ((e = set_smem(k_nn_cycle<float>, smem))) return e;
+    k_nn_cycle<float><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
+  }
+  if ((e = (int)cudaGetLastError())) return e;
+  k_run_epilogue<<<n_runs, ((R + 31) / 32) * 32, 0, st>>>(P, Q, 0, phase);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace ptmc

@@ -53,8 +53,8 @@ def _create(pk, p):
 
 
 def test_argument_validation(pk):
-    rc, h, msg = _create(pk, _params(pk, n_traj=33))
-    assert rc == -6 and "32 replicas" in msg
+    rc, h, msg = _create(pk, _params(pk, n_traj=1025))
+    assert rc == -6 and "1024 replicas" in msg
     rc, h, msg = _create(pk, _params(pk, tdistr=7))
     assert rc == -1 and "temperature distribution" in msg
     rc, h, msg = _create(pk, _params(pk, n_runs=0))
