@@ -75,6 +75,12 @@ def workload(name):
                     bc=("cubic", 25.2), sizes=lambda B: [108] * B,
                     start=lambda n, k: fcc(3, 8.4, 0.05, 7 + k), resync=1000,
                     flops_pair=33, mufu_pair=1)
+    if name == "nn55":
+        return dict(name="nn55_runner", R=64, T=(300.0, 900.0), pot="nn", ens="nvt",
+                    bc=("sphere", 14.0), sizes=lambda B: [55] * B,
+                    start=lambda n, k: cu55_ico(), resync=1000,
+                    # per move: 74.4 k angular triple terms x ~30 ops + 239 k MLP flops
+                    flops_move=74400 * 30 + 239000, flops_pair=0, mufu_pair=0)
     if name == "batched":
         ns = [13, 38, 55, 101, 147]
 
@@ -88,7 +94,17 @@ def workload(name):
 
 
 def default_runs(name, n_sm=152):
-    return {"cu55": 2 * n_sm, "ne13": 4 * n_sm, "npt108": n_sm, "batched": 256}[name]
+    return {"cu55": 2 * n_sm, "ne13": 4 * n_sm, "npt108": n_sm, "batched": 256,
+            "nn55": max(1, (2 * n_sm) // 64)}[name]
+
+
+def nn_potential(pk):
+    """88 G2/G4 functions of scripts/cu55.jl with r_c = 12 bohr, MLP 88-20-20-1
+    with seeded FP32 weights (output layer x0.01 to give energies of ~1e-2 Eh)."""
+    tables = json.load(open(os.path.join(ROOT, "tests", "golden", "nn_cu55.json")))
+    nodes = [88, 20, 20, 1]
+    return pk.RuNNerPotential(pk.RuNNerPotential.sf_table(tables, 12.0),
+                              pk.RuNNerPotential.random_weights(nodes, 3, 0.01), nodes)
 
 
 # --------------------------------------------------------------- GPU arm
@@ -99,6 +115,8 @@ def make_engine(pk, W, B, precision, cycles_per_launch, seed, device):
     temp = pk.TempGrid(W["T"][0], W["T"][1], R)
     if W["pot"] == "eam":
         pot = pk.EmbeddedAtomPotential(**CU_EAM)
+    elif W["pot"] == "nn":
+        pot = nn_potential(pk)
     else:
         pot = pk.ELJPotentialEven(C_NE)
     ens = pk.NPT(sizes[0], P_NE) if W["ens"] == "npt" else pk.NVT(sizes[0])
@@ -264,6 +282,10 @@ def _cpu_worker(args_tuple):
         ean = E["eps"] * E["a"] ** E["n"] / 2
         ecam = E["eps"] * E["C"] * E["a"] ** (E["m"] / 2)
         run.set_eam(E["n"], E["m"], ean, ecam)
+    elif W["pot"] == "nn":
+        import __graft_entry__ as g
+        pot = nn_potential(g.load_package())
+        run.set_nn(pot.sf, pot.weights, pot.nodes, pot.boundary)
     else:
         run.set_elj(C_NE, True)
     run.init()
@@ -293,7 +315,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="cu55", choices=["cu55", "ne13", "npt108", "batched"])
+    ap.add_argument("--workload", default="cu55", choices=["cu55", "ne13", "npt108", "batched", "nn55"])
     ap.add_argument("--runs", type=int, default=0, help="independent PT runs batched (0 = fill the GPU)")
     ap.add_argument("--cycles", type=int, default=200, help="MC cycles per step")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -348,9 +370,12 @@ def main():
     sizes = ch["sizes"]
     # roofline of the dominant kernel (k_cycles): algorithmic FP32 ops per launch
     pairs_per_move = [n - 1 for n in sizes]
-    flops_launch = sum((W["flops_pair"] * (n - 1) + 2 * n) * n * W["R"] for n in sizes) * args.cycles
-    per_launch_s = ch["ms_per_step"] / 1e3 / max(1, ch["launches"] // max(1, args.steps))
-    achieved = flops_launch / per_launch_s / 1e12
+    if W.get("flops_move"):
+        flops_launch = W["flops_move"] * sum(sizes) * W["R"] * args.cycles
+    else:
+        flops_launch = sum((W["flops_pair"] * (n - 1) + 2 * n) * n * W["R"] for n in sizes) * args.cycles
+    # the cycle kernels are ~all of a step's device time (launch list in profiles/)
+    achieved = flops_launch / (ch["ms_per_step"] / 1e3) / 1e12
     line = {
         "metric": "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error",
         "value": ch["value"], "unit": "atom-moves/s", "n_gpus": world, "steps": args.steps,
