@@ -71,6 +71,17 @@ __device__ __forceinline__ Real tpow(Real b, int zc, Real zeta) {
   if (zc >= 5) p = p * p;
   return p;
 }
+// same with the code stored as a real: > 0 code, <= 0 minus a general zeta
+template <typename Real>
+__device__ __forceinline__ Real tpowc(Real b, Real code) {
+  if (code <= Real(0)) return pow(b, -code);
+  Real p = b;
+  if (code >= Real(2)) p = p * p;
+  if (code >= Real(3)) p = p * p;
+  if (code >= Real(4)) p = p * p;
+  if (code >= Real(5)) p = p * p;
+  return p;
+}
 
 template <typename Real>
 struct NNSmem {
@@ -89,6 +100,7 @@ struct NNSmem {
   Real* h2;    // [N][H2]
   Real* red;   // block-reduction scratch [NN_THREADS/32 + 8]
   Real* dGi;   // [S] centre-i deltas
+  Real* sfp;   // [SA][4] angular parameters: eta, lambda, tpz, zeta code
   double* drw; // draw buffer [16]
   double* tpos;// trial position [3]
   int* flags;  // [4]
@@ -118,6 +130,7 @@ __device__ size_t nn_carve(NNSmem<Real>& s, unsigned char* base, int N, int S, i
   s.h2 = (Real*)take(sizeof(Real) * N * H2);
   s.red = (Real*)take(sizeof(Real) * 64);
   s.dGi = (Real*)take(sizeof(Real) * (S > 0 ? S : 1));
+  s.sfp = (Real*)take(sizeof(Real) * 4 * MAX_NN_ANG);
   s.drw = (double*)take(sizeof(double) * DRAW_BUF);
   s.tpos = (double*)take(sizeof(double) * 4);
   s.flags = (int*)take(sizeof(int) * 4);
@@ -188,6 +201,13 @@ __device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X,
     s.X[k] = (Real)X[k];
   }
   for (int k = threadIdx.x; k < Q.nW; k += blockDim.x) s.W[k] = (Real)Q.W[k];
+  for (int q = threadIdx.x; q < Q.SA; q += blockDim.x) {
+    const NNSF& f = Q.sf[Q.SR + q];
+    s.sfp[4 * q] = (Real)f.eta;
+    s.sfp[4 * q + 1] = (Real)f.lambda;
+    s.sfp[4 * q + 2] = (Real)f.tpz;
+    s.sfp[4 * q + 3] = (Real)(f.zc == 0 ? -f.zeta : (double)f.zc);  // >0: code, <=0: -zeta
+  }
   if (Gg)
     for (int k = threadIdx.x; k < Q.S * N; k += blockDim.x) s.G[k] = (Real)Gg[k];
   __syncthreads();
@@ -456,7 +476,8 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
       {
         const int j = tid % 64, c = tid / 64;
         Real accj[MAX_NN_ANG], acci[MAX_NN_ANG];
-        for (int q = 0; q < SA; ++q) {
+#pragma unroll
+        for (int q = 0; q < MAX_NN_ANG; ++q) {
           accj[q] = 0;
           acci[q] = 0;
         }
@@ -485,27 +506,32 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
               cio = ((vox * s.vo[3 * k] + voy * s.vo[3 * k + 1]) + voz * s.vo[3 * k + 2]) / (roj * ro[k]);
             }
             Real en_e = 0, eo_e = 0, last_eta = -1;
-            for (int q = 0; q < SA; ++q) {
-              const NNSF& f = Q.sf[SR + q];
-              const Real eta = (Real)f.eta;
-              if (eta != last_eta) {  // functions are sorted by eta: one exp pair per distinct eta
-                en_e = rexp<Real>(-eta * sn) * fpn;
-                eo_e = rexp<Real>(-eta * so) * fpo;
-                last_eta = eta;
+#pragma unroll
+            for (int q = 0; q < MAX_NN_ANG; ++q) {  // unrolled: accumulators stay in registers
+              if (q < SA) {
+                const Real eta = s.sfp[4 * q], lam = s.sfp[4 * q + 1], tpz = s.sfp[4 * q + 2],
+                           zc = s.sfp[4 * q + 3];
+                if (eta != last_eta) {  // sorted by eta: one exp pair per distinct eta
+                  en_e = rexp<Real>(-eta * sn) * fpn;
+                  eo_e = rexp<Real>(-eta * so) * fpo;
+                  last_eta = eta;
+                }
+                accj[q] += (en_e * tpowc<Real>(Real(1) + lam * cjn, zc) -
+                            eo_e * tpowc<Real>(Real(1) + lam * cjo, zc)) * tpz;
+                if (ci_on)
+                  acci[q] += (en_e * tpowc<Real>(Real(1) + lam * cin, zc) -
+                              eo_e * tpowc<Real>(Real(1) + lam * cio, zc)) * tpz;
               }
-              const Real lam = (Real)f.lambda, tpz = (Real)f.tpz;
-              accj[q] += (en_e * tpow<Real>(Real(1) + lam * cjn, f.zc, (Real)f.zeta) -
-                          eo_e * tpow<Real>(Real(1) + lam * cjo, f.zc, (Real)f.zeta)) * tpz;
-              if (ci_on)
-                acci[q] += (en_e * tpow<Real>(Real(1) + lam * cin, f.zc, (Real)f.zeta) -
-                            eo_e * tpow<Real>(Real(1) + lam * cio, f.zc, (Real)f.zeta)) * tpz;
             }
           }
         }
-        for (int q = 0; q < SA; ++q) {
-          s.part[(c * SA + q) * 64 + j] = accj[q];
-          Real v = warp_sum(acci[q]);
-          if (lane == 0 && v != Real(0)) atomicAdd(&s.dGi[SR + q], v);
+#pragma unroll
+        for (int q = 0; q < MAX_NN_ANG; ++q) {
+          if (q < SA) {
+            s.part[(c * SA + q) * 64 + j] = accj[q];
+            Real v = warp_sum(acci[q]);
+            if (lane == 0 && v != Real(0)) atomicAdd(&s.dGi[SR + q], v);
+          }
         }
       }
       __syncthreads();
@@ -629,6 +655,7 @@ size_t nn_smem_bytes(const NNParams& Q, int N, bool f64) {
   b += al(8 * N * 3) + al(es * N * 3) + 2 * al(es * N * N) + 2 * al(es * Q.S * N);
   b += al(es * NCH * (Q.SA > 0 ? Q.SA : 1) * 64) + al(es * 6 * 64) + 2 * al(es * 64 * 3);
   b += al(es * Q.nW) + al(es * N * Q.H1) + al(es * N * Q.H2) + al(es * 64) + al(es * (Q.S > 0 ? Q.S : 1));
+  b += al(es * 4 * MAX_NN_ANG);
   b += al(8 * DRAW_BUF) + al(8 * 4) + al(4 * 4);
   return b;
 }
