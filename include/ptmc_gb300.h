@@ -175,6 +175,64 @@ int ptmc_multihist_npt(int R, int n_bin, const double* ev_hist,
                        double pressure, double thr, double* T_out,
                        double* cp_out, int* iters);
 
+/* --- delayed acceptance with a learned pair surrogate (no counterpart in the
+ *     reference; Christen & Fox 2005 two-stage Metropolis-Hastings) ---
+ * Surrogate: E_s = sum over pairs phi(r), phi = escale*(w3.h2 + b3),
+ * h2 = tanh(W2^T h1 + b2), h1 = tanh(W1^T g + b1), g_k = fc(r)*exp(-gamma
+ * (r - mu_k)^2) with 16 centres mu_k evenly spaced on [r_lo, r_hi] and the
+ * cosine cut-off fc at r_cut.  Parameters: PTMC_SUR_NPARAMS floats W1[16][32]
+ * (input-major), b1[32], W2[32][32], b2[32], w3[32], b3.  A move record is 128
+ * floats: [0..63] new distances |t - x_j|, [64..127] old distances |x_i - x_j|
+ * (negative = no pair); dE_s = sum phi(new) - sum phi(old).  The two matrix
+ * products per record run on the tensor cores (BF16 operands, FP32
+ * accumulation).  A delayed-acceptance atom move draws, after the proposal,
+ * u1 and accepts stage 1 iff min(1, exp(-beta dE_s)) >= u1; only then is the
+ * exact NN energy computed and the move accepted iff
+ * min(1, exp(-beta (dE - dE_s))) >= u2 (a second draw).  The chain stays exact
+ * for any fixed surrogate: train, then freeze, then enable. */
+typedef struct ptmc_surrogate_cfg {
+  double r_lo, r_hi;  /* first and last Gaussian centre (bohr) */
+  double gamma;       /* Gaussian width parameter (1/bohr^2) */
+  double r_cut;       /* cosine cut-off of the features (bohr) */
+  double escale;      /* output scale (Eh); 0 = set from the recorded dE at the first training */
+} ptmc_surrogate_cfg;
+#define PTMC_SUR_NPARAMS 1633
+/* dE_s of n move records on `device` (host arrays in and out). */
+int ptmc_surrogate_eval(const ptmc_surrogate_cfg* cfg, const float* params,
+                        const float* rows, int n, double* dEs_out, int device);
+/* Huber loss (delta 1) of (dE_s - targets)/escale averaged over the n records
+ * and its gradient grad[PTMC_SUR_NPARAMS] (host arrays), computed on `device`
+ * by the training kernels (tensor-core forward, FP32 backward). */
+int ptmc_surrogate_loss_grad(const ptmc_surrogate_cfg* cfg, const float* params,
+                             const float* rows, const float* targets, int n,
+                             double* loss, float* grad, int device);
+/* Attach a surrogate to an NN context (after ptmc_init): cfg, initial
+ * parameters (NULL = seeded uniform(+-1/sqrt(fan_in)) weights, zero biases),
+ * a ring of `capacity` training records, and the capture stride: move m of a
+ * walker in cycle c is recorded when (c*N + m) % record_every == 0.  Calling
+ * it again re-initialises the parameters, the optimiser and the counters and
+ * keeps the captured records when the capacity is unchanged. */
+int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg,
+                       const float* params, int capacity, int record_every);
+/* Record (config, dE) pairs from the exact chain during the following cycle
+ * calls (on = 1) or stop (0).  Not allowed while delayed acceptance is on. */
+int ptmc_surrogate_record(ptmc_ctx* c, int on);
+/* `steps` Adam steps (learning rate lr) on minibatches of `batch` records drawn
+ * from the ring; *loss_out = mean minibatch loss of the last 10 % of steps. */
+int ptmc_surrogate_train(ptmc_ctx* c, int steps, int batch, double lr,
+                         double* loss_out);
+/* Switch delayed-acceptance moves on (1) or off (0); the surrogate is frozen
+ * while on. */
+int ptmc_surrogate_enable(ptmc_ctx* c, int on);
+/* Current parameters (params may be NULL), the configuration in use (cfg may
+ * be NULL) and counters stats[4] = {records captured, first-stage
+ * rejections, exact evaluations, 0} summed over every walker. */
+int ptmc_surrogate_get(ptmc_ctx* c, float* params, ptmc_surrogate_cfg* cfg,
+                       long long* stats);
+/* Copy up to max_n captured records (rows [n][128], targets [n]); *n_out = count. */
+int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n,
+                           int* n_out);
+
 /* Allocation-free multihistogram_NVT, no counterpart in the reference (which
  * has no device memory at all).  For callers that cannot call cudaMalloc: a
  * Julia program whose GPU memory belongs to CUDA.jl's pool, code enqueueing

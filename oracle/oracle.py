@@ -83,6 +83,12 @@ def lib():
         L.orc_multihist_npt.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, _dp, _dp, _ip]
+        _fp = ctypes.POINTER(ctypes.c_float)
+        L.orc_sur_nparams.restype = ctypes.c_int
+        L.orc_sur_forward.argtypes = [_dp, _dp, _fp, ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_sur_loss_grad.argtypes = [_dp, _dp, _fp, _fp, ctypes.c_int, ctypes.c_int, _dp, _dp]
+        L.orc_set_surrogate.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int]
+        L.orc_get_sur_stats.argtypes = [ctypes.c_void_p, _lp]
         _lib = L
     return _lib
 
@@ -256,8 +262,52 @@ class Run:
         lib().orc_finalise(self.h, mc_cycles, mc_sample, P(a), P(b), P(c), P(d))
         return dict(en_avg=a, heat_cap=b, count_stat_atom=c, count_stat_exc=d)
 
+    def set_surrogate(self, cfg, params, bf16=True):
+        """Delayed-acceptance atom moves with the pair surrogate (None: off)."""
+        if params is None:
+            _check(lib().orc_set_surrogate(self.h, None, None, 0))
+            return
+        self._sur = (_d(cfg), _d(params))
+        _check(lib().orc_set_surrogate(self.h, P(self._sur[0]), P(self._sur[1]), int(bf16)))
+
+    def sur_stats(self):
+        out = (ctypes.c_long * 2)()
+        lib().orc_get_sur_stats(self.h, out)
+        return dict(stage1_rejects=out[0], exact_evals=out[1])
+
     def nn_state(self, w, nsf):
         G = np.zeros((nsf, self.N))
         ea = np.zeros(self.N)
         _check(lib().orc_get_nn_state(self.h, w, P(G), P(ea)))
         return G, ea
+
+
+# ---------------------------------------------------------------- surrogate
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def sur_nparams():
+    return lib().orc_sur_nparams()
+
+
+def sur_forward(cfg, params, rows, bf16=True):
+    """dE_s of every record (rows: (n, 128) distances, negative = no pair)."""
+    cfg, params, rows = _d(cfg), _d(params), _f(rows)
+    out = np.zeros(rows.shape[0])
+    _check(lib().orc_sur_forward(P(cfg), P(params), _fptr(rows), rows.shape[0], int(bf16), P(out)))
+    return out
+
+
+def sur_loss_grad(cfg, params, rows, targets, bf16=True):
+    cfg, params, rows, targets = _d(cfg), _d(params), _f(rows), _f(targets)
+    loss = np.zeros(1)
+    g = np.zeros(sur_nparams())
+    _check(lib().orc_sur_loss_grad(P(cfg), P(params), _fptr(rows), _fptr(targets), rows.shape[0],
+                                   int(bf16), P(loss), P(g)))
+    return float(loss[0]), g
+

@@ -233,6 +233,129 @@ double mlp_atom(const double* x, const double* w, const int* nodes, int nl) {
   return in[0];
 }
 
+
+// ---------------------------------------------------------------- surrogate
+// Learned pair surrogate of the delayed-acceptance move (no counterpart in the
+// reference; Christen & Fox, J. Comput. Graph. Stat. 14 (2005) 795, two-stage
+// Metropolis-Hastings).  E_s(x) = sum_{i<j} phi(r_ij) with
+//   g_k(r) = fc(r) exp(-gamma (r - mu_k)^2),  mu_k = r_lo + k (r_hi - r_lo)/15,
+//   h1 = tanh(W1^T g + b1),  h2 = tanh(W2^T h1 + b2),
+//   phi = escale (w3 . h2 + b3)
+// (16 features, 32 + 32 hidden units).  A move of atom i has the record
+// rows[0..63] = |t - x_j| (new), rows[64..127] = |x_i - x_j| (old), negative =
+// no pair; dE_s = sum_new phi - sum_old phi.  With `bf` set, the operands of
+// the two matrix products (g, W1, h1, W2) are rounded to BF16 as the tensor
+// cores see them; sums and activations stay FP64 here.
+struct SurCfg {
+  double r_lo = 0, r_hi = 0, gamma = 0, r_cut = 0, escale = 1;
+};
+constexpr int SUR_F = 16, SUR_H = 32, SUR_ROWS = 128;
+constexpr int SUR_B1 = SUR_F * SUR_H, SUR_W2 = SUR_B1 + SUR_H, SUR_B2 = SUR_W2 + SUR_H * SUR_H,
+              SUR_W3 = SUR_B2 + SUR_H, SUR_B3 = SUR_W3 + SUR_H, SUR_NP = SUR_B3 + 1;
+
+// round to float, then to the nearest BF16 (ties to even)
+inline double bf16r(double x) {
+  float f = (float)x;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+  std::memcpy(&f, &u, 4);
+  return (double)f;
+}
+
+struct SurRow {
+  double g[SUR_F], h1[SUR_H], h2[SUR_H], phi;
+};
+
+void sur_row(const SurCfg& c, const double* P, double r, bool bf, SurRow& st) {
+  const double fc = r < c.r_cut ? 0.5 * (std::cos(3.141592653589793 * (r / c.r_cut)) + 1) : 0.0;
+  for (int k = 0; k < SUR_F; ++k) {
+    double mu = c.r_lo + k * ((c.r_hi - c.r_lo) / (SUR_F - 1));
+    double d = r - mu;
+    double g = fc * std::exp(-c.gamma * (d * d));
+    st.g[k] = bf ? bf16r(g) : g;
+  }
+  for (int n = 0; n < SUR_H; ++n) {
+    double z = 0;
+    for (int k = 0; k < SUR_F; ++k) {
+      double w = P[k * SUR_H + n];
+      z += st.g[k] * (bf ? bf16r(w) : w);
+    }
+    st.h1[n] = std::tanh(z + P[SUR_B1 + n]);
+  }
+  double phi = 0;
+  for (int n = 0; n < SUR_H; ++n) {
+    double z = 0;
+    for (int k = 0; k < SUR_H; ++k) {
+      double w = P[SUR_W2 + k * SUR_H + n];
+      z += (bf ? bf16r(st.h1[k]) : st.h1[k]) * (bf ? bf16r(w) : w);
+    }
+    st.h2[n] = std::tanh(z + P[SUR_B2 + n]);
+    phi += P[SUR_W3 + n] * st.h2[n];
+  }
+  st.phi = c.escale * (phi + P[SUR_B3]);
+}
+
+double sur_delta(const SurCfg& c, const double* P, const float* rows, bool bf) {
+  SurRow st;
+  double e = 0;
+  for (int q = 0; q < SUR_ROWS; ++q) {
+    if (!(rows[q] >= 0)) continue;
+    sur_row(c, P, rows[q], bf, st);
+    e += q < SUR_ROWS / 2 ? st.phi : -st.phi;
+  }
+  return e;
+}
+
+// Huber loss (delta 1) of the scaled residual (dE_s - y)/escale, averaged
+// over the n records, and its gradient with respect to the parameters (the
+// BF16 rounding, when on, is treated as the identity in the backward pass).
+double sur_loss_grad(const SurCfg& c, const double* P, const float* rows, const float* y, int n,
+                     bool bf, double* grad) {
+  std::vector<SurRow> st(SUR_ROWS);
+  double L = 0;
+  if (grad) std::fill(grad, grad + SUR_NP, 0.0);
+  for (int b = 0; b < n; ++b) {
+    const float* rr = rows + (size_t)b * SUR_ROWS;
+    double e = 0;
+    for (int q = 0; q < SUR_ROWS; ++q) {
+      if (!(rr[q] >= 0)) continue;
+      sur_row(c, P, rr[q], bf, st[q]);
+      e += q < SUR_ROWS / 2 ? st[q].phi : -st[q].phi;
+    }
+    double res = (e - (double)y[b]) / c.escale;
+    double a = std::fabs(res);
+    L += a <= 1 ? 0.5 * res * res : a - 0.5;
+    if (!grad) continue;
+    double G = (res > 1 ? 1.0 : res < -1 ? -1.0 : res) / (c.escale * n);  // dL/d dE_s
+    for (int q = 0; q < SUR_ROWS; ++q) {
+      if (!(rr[q] >= 0)) continue;
+      const SurRow& s = st[q];
+      double dphi = (q < SUR_ROWS / 2 ? G : -G) * c.escale;
+      grad[SUR_B3] += dphi;
+      double dz2[SUR_H];
+      for (int m = 0; m < SUR_H; ++m) {
+        grad[SUR_W3 + m] += dphi * s.h2[m];
+        dz2[m] = dphi * P[SUR_W3 + m] * (1 - s.h2[m] * s.h2[m]);
+        grad[SUR_B2 + m] += dz2[m];
+      }
+      for (int k = 0; k < SUR_H; ++k) {
+        double h1k = bf ? bf16r(s.h1[k]) : s.h1[k];
+        double dh = 0;
+        for (int m = 0; m < SUR_H; ++m) {
+          double w = P[SUR_W2 + k * SUR_H + m];
+          grad[SUR_W2 + k * SUR_H + m] += h1k * dz2[m];
+          dh += (bf ? bf16r(w) : w) * dz2[m];
+        }
+        double dz1 = dh * (1 - s.h1[k] * s.h1[k]);
+        grad[SUR_B1 + k] += dz1;
+        for (int f = 0; f < SUR_F; ++f) grad[f * SUR_H + k] += s.g[f] * dz1;
+      }
+    }
+  }
+  return L / n;
+}
+
 }  // namespace
 
 // ================================================================ run state
@@ -259,6 +382,11 @@ struct orc_run {
   std::vector<long> cnt_atom, cnt_vol, cnt_exc;     // 2R each
   std::vector<int> wos;                             // walker of slot
   uint64_t run_ctr = 0;
+  // delayed acceptance (NN only): surrogate parameters, stage counters
+  bool da = false, da_bf = true;
+  SurCfg sc;
+  std::vector<double> sp;
+  long da_reject1 = 0, da_exact = 0;
   // results
   double en_min = 0, en_max = 0, v_min = 0, v_max = 0, dE = 0, dV = 0;
   std::vector<double> en_hist, ev_hist;
@@ -440,6 +568,27 @@ int atom_move(orc_run* r, int w, int slot, int i) {
   const Pot& pot = r->pot;
   double new_en;
   bool hard = false;
+  // delayed acceptance, stage 1: the surrogate screens the proposal; the
+  // first-stage draw follows the proposal draws (a rejected proposal costs no
+  // exact energy evaluation)
+  double dEs = 0.0;
+  if (r->da) {
+    float rows[SUR_ROWS];
+    for (int q = 0; q < SUR_ROWS; ++q) rows[q] = -1.0f;
+    for (int j = 0; j < N; ++j) {
+      if (j == i) continue;
+      rows[j] = (float)std::sqrt(row[j]);
+      rows[SUR_ROWS / 2 + j] = (float)std::sqrt(old[j]);
+    }
+    dEs = sur_delta(r->sc, r->sp.data(), rows, r->da_bf);
+    double p1 = std::exp(-dEs * r->beta[slot]);
+    if (p1 > 1) p1 = 1.0;
+    if (!(p1 >= r->draw(w))) {
+      r->da_reject1 += 1;
+      return 0;
+    }
+    r->da_exact += 1;
+  }
   if (pot.kind == ORC_POT_EAM) {  // energy_update! EAM (:1567-1591)
     int S2 = 2 * N;
     double* nc = r->new_comp.data();
@@ -518,8 +667,9 @@ int atom_move(orc_run* r, int w, int slot, int i) {
     double dE = dimer_atom(pot, i, row, N, cut, rc2) - dimer_atom(pot, i, old, N, cut, rc2);
     new_en = dE + r->en[w];
   }
-  // acc_test! (MCRun.jl:122-132), metropolis_condition (Exchange.jl:53-57)
-  double prob = std::exp(-(new_en - r->en[w]) * r->beta[slot]);
+  // acc_test! (MCRun.jl:122-132), metropolis_condition (Exchange.jl:53-57);
+  // with delayed acceptance the second stage uses exp(-beta (dE - dE_s))
+  double prob = std::exp(-((new_en - r->en[w]) - dEs) * r->beta[slot]);
   if (prob > 1) prob = 1.0;
   double u = r->draw(w);
   if (prob >= u) {  // swap_atom_config! (swap_config.jl:40-51)
@@ -964,6 +1114,48 @@ int orc_mlp_forward(const double* input, int n_in, int batch,
   if (nodes[0] != n_in) return fail("input width mismatch");
   for (int b = 0; b < batch; ++b)
     eatom[b] = mlp_atom(input + (size_t)b * n_in, weights, nodes, n_layers);
+  return 0;
+}
+
+// ---------------------------------------------------------------- surrogate
+static SurCfg sur_cfg(const double* cfg) {
+  SurCfg c;
+  c.r_lo = cfg[0];
+  c.r_hi = cfg[1];
+  c.gamma = cfg[2];
+  c.r_cut = cfg[3];
+  c.escale = cfg[4];
+  return c;
+}
+int orc_sur_nparams(void) { return SUR_NP; }
+int orc_sur_forward(const double* cfg, const double* params, const float* rows, int n, int bf16,
+                    double* dEs) {
+  SurCfg c = sur_cfg(cfg);
+  for (int b = 0; b < n; ++b) dEs[b] = sur_delta(c, params, rows + (size_t)b * SUR_ROWS, bf16 != 0);
+  return 0;
+}
+int orc_sur_loss_grad(const double* cfg, const double* params, const float* rows,
+                      const float* targets, int n, int bf16, double* loss, double* grad) {
+  if (n < 1) return fail("need at least one record");
+  *loss = sur_loss_grad(sur_cfg(cfg), params, rows, targets, n, bf16 != 0, grad);
+  return 0;
+}
+int orc_set_surrogate(orc_run* r, const double* cfg, const double* params, int bf16) {
+  if (!params) {
+    r->da = false;
+    return 0;
+  }
+  if (r->pot.kind != ORC_POT_NN) return fail("delayed acceptance needs the NN potential");
+  if (r->N > SUR_ROWS / 2) return fail("delayed acceptance: at most 64 atoms");
+  r->sc = sur_cfg(cfg);
+  r->sp.assign(params, params + SUR_NP);
+  r->da_bf = bf16 != 0;
+  r->da = true;
+  return 0;
+}
+int orc_get_sur_stats(orc_run* r, long* out) {
+  out[0] = r->da_reject1;
+  out[1] = r->da_exact;
   return 0;
 }
 

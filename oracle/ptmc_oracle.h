@@ -105,6 +105,26 @@ int orc_mlp_forward(const double* input, int n_in, int batch,
                     const double* weights, int nw, const int* nodes,
                     int n_layers, double* eatom);
 
+/* ---- learned pair surrogate of the delayed-acceptance move (no counterpart
+ * in the reference).  cfg = {r_lo, r_hi, gamma, r_cut, escale}; params: the
+ * orc_sur_nparams() values W1[16][32], b1[32], W2[32][32], b2[32], w3[32], b3;
+ * rows: n records of 128 floats (0..63 new distances |t - x_j|, 64..127 old
+ * |x_i - x_j|, negative = no pair).  bf16 != 0 rounds the matrix-product
+ * operands to BF16 as the GPU's tensor cores see them. ---- */
+int orc_sur_nparams(void);
+int orc_sur_forward(const double* cfg, const double* params, const float* rows,
+                    int n, int bf16, double* dEs);
+/* Huber (delta 1) loss of (dE_s - target)/escale averaged over the records,
+ * and its gradient (grad may be NULL) */
+int orc_sur_loss_grad(const double* cfg, const double* params,
+                      const float* rows, const float* targets, int n, int bf16,
+                      double* loss, double* grad);
+/* delayed-acceptance atom moves for an NN run (params NULL switches it off);
+ * stats: {first-stage rejections, exact evaluations} */
+int orc_set_surrogate(orc_run* r, const double* cfg, const double* params,
+                      int bf16);
+int orc_get_sur_stats(orc_run* r, long* out);
+
 /* ---- multihistogram (multihist_NVT.jl:95, multihist_NPT.jl:113) ---- */
 int orc_multihist_nvt(int R, int n_bin, const double* en_hist,
                       const double* t_grid, const double* beta, double en_min,

@@ -30,7 +30,7 @@ kB = 3.16681196e-6  # Hartree/K, src/InputParams.jl:19
 
 __all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "Config", "NVT", "NPT",
            "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "RuNNerPotential",
-           "Output", "MCState",
+           "Output", "MCState", "PairSurrogate",
            "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
            "distance2", "get_distance2_mat", "get_volume", "PTMCError"]
 
@@ -268,8 +268,57 @@ class MCState:
 
 
 # ------------------------------------------------------------------ engine
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
 def _dptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class PairSurrogate:
+    """Configuration of the learned pair surrogate of delayed-acceptance moves
+    (no counterpart in the reference): 16 Gaussian radial features with centres
+    evenly spaced on [r_lo, r_hi], width parameter gamma, cosine cut-off r_cut,
+    MLP 16 -> 32 -> 32 -> 1 (tanh), output scale escale (0: set from the
+    recorded energy changes at the first training)."""
+
+    def __init__(self, r_lo=2.0, r_hi=12.0, gamma=None, r_cut=12.0, escale=0.0):
+        self.r_lo, self.r_hi, self.r_cut, self.escale = float(r_lo), float(r_hi), float(r_cut), float(escale)
+        dmu = (self.r_hi - self.r_lo) / 15.0
+        self.gamma = float(gamma) if gamma is not None else 1.0 / (2.0 * dmu * dmu)
+
+    def cfg(self):
+        c = _capi.SurrogateCfg()
+        c.r_lo, c.r_hi, c.gamma, c.r_cut, c.escale = self.r_lo, self.r_hi, self.gamma, self.r_cut, self.escale
+        return c
+
+    def as_array(self):
+        return np.array([self.r_lo, self.r_hi, self.gamma, self.r_cut, self.escale])
+
+    def eval(self, params, rows, device=0):
+        """dE_s of move records (n, 128) on the GPU (tensor-core forward)."""
+        L = _capi.load()
+        rows = np.ascontiguousarray(rows, dtype=np.float32)
+        P = np.ascontiguousarray(params, dtype=np.float32)
+        out = np.zeros(rows.shape[0])
+        c = self.cfg()
+        _capi.check(L.ptmc_surrogate_eval(ctypes.byref(c), _fptr(P), _fptr(rows), rows.shape[0],
+                                          _dptr(out), device))
+        return out
+
+    def loss_grad(self, params, rows, targets, device=0):
+        """Huber loss of (dE_s - targets)/escale and its gradient, on the GPU."""
+        L = _capi.load()
+        rows = np.ascontiguousarray(rows, dtype=np.float32)
+        y = np.ascontiguousarray(targets, dtype=np.float32)
+        P = np.ascontiguousarray(params, dtype=np.float32)
+        g = np.zeros(_capi.SUR_NPARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        c = self.cfg()
+        _capi.check(L.ptmc_surrogate_loss_grad(ctypes.byref(c), _fptr(P), _fptr(rows), _fptr(y),
+                                               rows.shape[0], ctypes.byref(loss), _fptr(g), device))
+        return loss.value, g
 
 
 class Engine:
@@ -360,6 +409,49 @@ class Engine:
 
     def resync(self):
         self._ck(self.L.ptmc_resync(self.h))
+
+    # ---- delayed acceptance with the learned pair surrogate (NN potential)
+    def surrogate_set(self, surrogate, capacity=100000, record_every=1, params=None):
+        """Attach a PairSurrogate (configuration and, unless `params` is given,
+        seeded initial weights) with a ring of `capacity` training records."""
+        cfg = surrogate.cfg()
+        p = None if params is None else _fptr(np.ascontiguousarray(params, dtype=np.float32))
+        self._ck(self.L.ptmc_surrogate_set(self.h, ctypes.byref(cfg), p, int(capacity),
+                                           int(record_every)))
+
+    def surrogate_record(self, on=True):
+        self._ck(self.L.ptmc_surrogate_record(self.h, int(bool(on))))
+
+    def surrogate_train(self, steps, batch=512, lr=1e-3):
+        """Adam on the GPU over minibatches of the captured records; returns the
+        mean minibatch loss of the last 10 % of steps."""
+        loss = ctypes.c_double()
+        self._ck(self.L.ptmc_surrogate_train(self.h, int(steps), int(batch), float(lr),
+                                             ctypes.byref(loss)))
+        return loss.value
+
+    def surrogate_enable(self, on=True):
+        self._ck(self.L.ptmc_surrogate_enable(self.h, int(bool(on))))
+
+    def surrogate_state(self):
+        """(parameters, PairSurrogate config, stats dict)."""
+        P = np.zeros(_capi.SUR_NPARAMS, dtype=np.float32)
+        cfg = _capi.SurrogateCfg()
+        st = np.zeros(4, dtype=np.int64)
+        self._ck(self.L.ptmc_surrogate_get(self.h, _fptr(P), ctypes.byref(cfg),
+                                           st.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
+        sur = PairSurrogate(cfg.r_lo, cfg.r_hi, cfg.gamma, cfg.r_cut, cfg.escale)
+        return P, sur, dict(records=int(st[0]), stage1_rejects=int(st[1]), exact_evals=int(st[2]))
+
+    def surrogate_records(self, max_n=None):
+        _, _, st = self.surrogate_state()
+        n = st["records"] if max_n is None else max_n
+        n = max(0, int(n))
+        rows = np.zeros((max(n, 1), 128), dtype=np.float32)
+        y = np.zeros(max(n, 1), dtype=np.float32)
+        got = ctypes.c_int()
+        self._ck(self.L.ptmc_surrogate_records(self.h, _fptr(rows), _fptr(y), n, ctypes.byref(got)))
+        return rows[:got.value], y[:got.value]
 
     def states(self, run=0):
         """Slot-ordered (xyz [R,N,3], en_tot [R], box [R], max_displ [R,2],

@@ -46,6 +46,14 @@ class Stats(ctypes.Structure):
                 ("max_drift", ctypes.c_double), ("last_cycles_ms", ctypes.c_double)]
 
 
+class SurrogateCfg(ctypes.Structure):
+    _fields_ = [("r_lo", ctypes.c_double), ("r_hi", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("r_cut", ctypes.c_double), ("escale", ctypes.c_double)]
+
+
+SUR_NPARAMS = 1633
+_fp = ctypes.POINTER(ctypes.c_float)
+
 # every symbol include/ptmc_gb300.h declares, with its ctypes signature
 SIGNATURES = {
     "ptmc_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Params)]),
@@ -81,6 +89,19 @@ SIGNATURES = {
                                                   ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p]),
     "ptmc_measure_peaks": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
+    "ptmc_surrogate_eval": (ctypes.c_int, [ctypes.POINTER(SurrogateCfg), _fp, _fp, ctypes.c_int,
+                                           _dp, ctypes.c_int]),
+    "ptmc_surrogate_loss_grad": (ctypes.c_int, [ctypes.POINTER(SurrogateCfg), _fp, _fp, _fp,
+                                                ctypes.c_int, _dp, _fp, ctypes.c_int]),
+    "ptmc_surrogate_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SurrogateCfg), _fp,
+                                          ctypes.c_int, ctypes.c_int]),
+    "ptmc_surrogate_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "ptmc_surrogate_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, _dp]),
+    "ptmc_surrogate_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "ptmc_surrogate_get": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.POINTER(SurrogateCfg),
+                                          _llp]),
+    "ptmc_surrogate_records": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int, _ip]),
     "ptmc_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "ptmc_destroy": (None, [ctypes.c_void_p]),
     "ptmc_version": (ctypes.c_char_p, []),

@@ -29,6 +29,7 @@
 #include "../../include/ptmc_gb300.h"
 #include "ptmc_engine.cuh"
 #include "ptmc_nn.cuh"
+#include "ptmc_surrogate.cuh"
 
 using namespace ptmc;
 
@@ -145,6 +146,15 @@ struct ptmc_ctx {
   DBuf<double> d_nn_W, d_nn_G;
   DBuf<int> d_nn_row, d_nn_sow;
   NNParams Q{};
+  // delayed-acceptance surrogate (ptmc_surrogate.cuh)
+  bool sur_set = false;
+  ptmc_surrogate_cfg sur_cfg{};
+  DBuf<float> d_sur_P, d_sur_m, d_sur_v, d_sur_g, d_rec_rows, d_rec_y;
+  DBuf<double> d_sur_loss;
+  DBuf<unsigned long long> d_rec_n;
+  DBuf<long long> d_da_cnt;
+  DBuf<int> d_sur_err;
+  int sur_step = 0;  // Adam steps taken
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evfork = nullptr;
   std::vector<cudaEvent_t> evjoin;
@@ -177,9 +187,12 @@ int check_status(ptmc_ctx* c) {
   std::vector<int> st(c->W);
   CK(cudaMemcpyAsync(st.data(), c->d_status.p, sizeof(int) * c->W, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  for (int i = 0; i < c->W; ++i)
+  for (int i = 0; i < c->W; ++i) {
     if (st[i] == ST_SPHERE)
       return c->fail(PTMC_ERR_SPHERE, "Error: too many moves out of binding sphere");
+    if (st[i] == ST_TIMEOUT)
+      return c->fail(PTMC_ERR_CUDA, "a tensor-core completion wait ran out (surrogate stage)");
+  }
   return PTMC_OK;
 }
 
@@ -866,6 +879,12 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_nn_G.free_();
   c->d_nn_row.free_();
   c->d_nn_sow.free_();
+  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_rec_rows, &c->d_rec_y})
+    b->free_();
+  c->d_sur_loss.free_();
+  c->d_rec_n.free_();
+  c->d_da_cnt.free_();
+  c->d_sur_err.free_();
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1136,6 +1155,373 @@ int ptmc_multihist_npt(int R, int n_bin, const double* ev_hist, const double* t_
                        double* cp_out, int* iters) {
   return wham_common(true, R, n_bin, ev_hist, t_grid, beta, en_min, en_max, v_min, v_max,
                      pressure, thr, T_out, cp_out, iters);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- surrogate
+// Delayed-acceptance pair surrogate (ptmc_surrogate.cuh, ptmc_surrogate.cu):
+// record capture from the exact chain, training on the GPU, frozen use as the
+// first stage of two-stage moves in the NN cycle kernel.
+namespace {
+
+SurCfgDev sur_dev(const ptmc_surrogate_cfg& c) {
+  SurCfgDev d;
+  d.r_lo = (float)c.r_lo;
+  d.dmu = (float)((c.r_hi - c.r_lo) / (SUR_F - 1));
+  d.gamma = (float)c.gamma;
+  d.r_cut = (float)c.r_cut;
+  d.escale = (float)c.escale;
+  return d;
+}
+
+bool sur_cfg_ok(const ptmc_surrogate_cfg* c, bool allow_auto_scale) {
+  if (!c) return false;
+  if (!(c->r_hi > c->r_lo) || !(c->gamma > 0) || !(c->r_cut > 0)) return false;
+  return c->escale > 0 || (allow_auto_scale && c->escale == 0);
+}
+
+// seeded initial parameters: W ~ U(-1/sqrt(fan_in), 1/sqrt(fan_in)), zero biases
+void sur_init_params(std::vector<float>& P, uint64_t seed) {
+  uint64_t x = seed ^ 0x9E3779B97F4A7C15ull;
+  auto u = [&]() {  // splitmix64 -> [0, 1)
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  P.assign(SUR_NP, 0.0f);
+  for (int k = 0; k < SUR_B1; ++k) P[k] = (float)((2 * u() - 1) / std::sqrt((double)SUR_F));
+  for (int k = 0; k < SUR_H * SUR_H; ++k)
+    P[SUR_W2 + k] = (float)((2 * u() - 1) / std::sqrt((double)SUR_H));
+  for (int k = 0; k < SUR_H; ++k) P[SUR_W3 + k] = (float)((2 * u() - 1) / std::sqrt((double)SUR_H));
+}
+
+void drop_graphs(ptmc_ctx* c) {
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+}
+
+int sur_err_check(ptmc_ctx* c) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, c->d_sur_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (e) return c->fail(PTMC_ERR_CUDA, "a tensor-core completion wait ran out (surrogate kernels)");
+  return PTMC_OK;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+// standalone helpers: device buffers owned by one call
+struct Scratch {
+  std::vector<void*> ptrs;
+  template <typename T>
+  T* get(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return (T*)p;
+  }
+  ~Scratch() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
+
+int standalone_device(int device) {
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    g_err = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return PTMC_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    g_err = "bad device ordinal";
+    return PTMC_ERR_ARG;
+  }
+  if ((e = cudaSetDevice(device)) != cudaSuccess) {
+    g_err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return PTMC_ERR_CUDA;
+  }
+  return PTMC_OK;
+}
+
+#define SCK(call)                                                           \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) {                                                \
+      g_err = std::string(#call) + ": " + cudaGetErrorString(e_);           \
+      return PTMC_ERR_CUDA;                                                 \
+    }                                                                       \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int ptmc_surrogate_eval(const ptmc_surrogate_cfg* cfg, const float* params, const float* rows,
+                        int n, double* dEs_out, int device) {
+  if (!sur_cfg_ok(cfg, false) || !params || (n > 0 && (!rows || !dEs_out)) || n < 0) {
+    g_err = "ptmc_surrogate_eval: bad argument";
+    return PTMC_ERR_ARG;
+  }
+  int rc = standalone_device(device);
+  if (rc) return rc;
+  if (n == 0) return PTMC_OK;
+  Scratch sc;
+  float* dP = sc.get<float>(SUR_NP);
+  float* dR = sc.get<float>((size_t)n * SUR_ROWS);
+  double* dO = sc.get<double>(n);
+  int* dE = sc.get<int>(1);
+  if (!dP || !dR || !dO || !dE) {
+    g_err = "ptmc_surrogate_eval: device allocation failed";
+    return PTMC_ERR_CUDA;
+  }
+  SCK(cudaMemcpy(dP, params, sizeof(float) * SUR_NP, cudaMemcpyHostToDevice));
+  SCK(cudaMemcpy(dR, rows, sizeof(float) * n * SUR_ROWS, cudaMemcpyHostToDevice));
+  SCK(cudaMemset(dE, 0, sizeof(int)));
+  int e = sur_launch_eval(sur_dev(*cfg), dP, dR, n, dO, dE, 8 * sm_count(), nullptr);
+  if (e) {
+    g_err = std::string("k_sur_eval launch: ") + cudaGetErrorString((cudaError_t)e);
+    return PTMC_ERR_CUDA;
+  }
+  SCK(cudaDeviceSynchronize());
+  int herr = 0;
+  SCK(cudaMemcpy(&herr, dE, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) {
+    g_err = "a tensor-core completion wait ran out (k_sur_eval)";
+    return PTMC_ERR_CUDA;
+  }
+  SCK(cudaMemcpy(dEs_out, dO, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_loss_grad(const ptmc_surrogate_cfg* cfg, const float* params, const float* rows,
+                             const float* targets, int n, double* loss, float* grad, int device) {
+  if (!sur_cfg_ok(cfg, false) || !params || !rows || !targets || !loss || !grad || n < 1) {
+    g_err = "ptmc_surrogate_loss_grad: bad argument";
+    return PTMC_ERR_ARG;
+  }
+  int rc = standalone_device(device);
+  if (rc) return rc;
+  Scratch sc;
+  float* dP = sc.get<float>(SUR_NP);
+  float* dR = sc.get<float>((size_t)n * SUR_ROWS);
+  float* dY = sc.get<float>(n);
+  int* dI = sc.get<int>(n);
+  float* dG = sc.get<float>(SUR_NP);
+  double* dL = sc.get<double>(1);
+  int* dE = sc.get<int>(1);
+  if (!dP || !dR || !dY || !dI || !dG || !dL || !dE) {
+    g_err = "ptmc_surrogate_loss_grad: device allocation failed";
+    return PTMC_ERR_CUDA;
+  }
+  std::vector<int> idx(n);
+  for (int k = 0; k < n; ++k) idx[k] = k;
+  SCK(cudaMemcpy(dP, params, sizeof(float) * SUR_NP, cudaMemcpyHostToDevice));
+  SCK(cudaMemcpy(dR, rows, sizeof(float) * n * SUR_ROWS, cudaMemcpyHostToDevice));
+  SCK(cudaMemcpy(dY, targets, sizeof(float) * n, cudaMemcpyHostToDevice));
+  SCK(cudaMemcpy(dI, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  SCK(cudaMemset(dG, 0, sizeof(float) * SUR_NP));
+  SCK(cudaMemset(dL, 0, sizeof(double)));
+  SCK(cudaMemset(dE, 0, sizeof(int)));
+  int e = sur_launch_grad(sur_dev(*cfg), dP, dR, dY, n, dI, n, 0, 0, dG, dL, dE, 3 * sm_count(),
+                          nullptr);
+  if (e) {
+    g_err = std::string("k_sur_grad launch: ") + cudaGetErrorString((cudaError_t)e);
+    return PTMC_ERR_CUDA;
+  }
+  SCK(cudaDeviceSynchronize());
+  int herr = 0;
+  SCK(cudaMemcpy(&herr, dE, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) {
+    g_err = "a tensor-core completion wait ran out (k_sur_grad)";
+    return PTMC_ERR_CUDA;
+  }
+  SCK(cudaMemcpy(grad, dG, sizeof(float) * SUR_NP, cudaMemcpyDeviceToHost));
+  SCK(cudaMemcpy(loss, dL, sizeof(double), cudaMemcpyDeviceToHost));
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg, const float* params,
+                       int capacity, int record_every) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (c->pot != POT_NN) return c->fail(PTMC_ERR_ARG, "delayed acceptance needs the NN potential");
+  if (!sur_cfg_ok(cfg, true)) return c->fail(PTMC_ERR_ARG, "surrogate: bad configuration");
+  if (capacity < 1 || record_every < 1)
+    return c->fail(PTMC_ERR_ARG, "surrogate: capacity and record_every must be >= 1");
+  if ((long long)capacity * SUR_ROWS > (1LL << 31))
+    return c->fail(PTMC_ERR_LIMIT, "surrogate: at most 2^24 records");
+  const int W = c->W;
+  // the record ring survives a new set-up with the same capacity (re-training
+  // from other initial parameters on the same records)
+  const bool keep_ring = c->sur_set && c->Q.rec_cap == capacity;
+  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g}) b->free_();
+  c->d_sur_loss.free_();
+  c->d_da_cnt.free_();
+  c->d_sur_err.free_();
+  if (!keep_ring) {
+    c->d_rec_rows.free_();
+    c->d_rec_y.free_();
+    c->d_rec_n.free_();
+  }
+  if (c->d_sur_P.alloc(SUR_NP) || c->d_sur_m.alloc(SUR_NP) || c->d_sur_v.alloc(SUR_NP) ||
+      c->d_sur_g.alloc(SUR_NP) || c->d_sur_loss.alloc(1) || c->d_da_cnt.alloc(2 * (size_t)W) ||
+      c->d_sur_err.alloc(1))
+    return c->fail(PTMC_ERR_CUDA, "surrogate: device allocation failed");
+  if (!keep_ring && (c->d_rec_rows.alloc((size_t)capacity * SUR_ROWS) ||
+                     c->d_rec_y.alloc(capacity) || c->d_rec_n.alloc(1)))
+    return c->fail(PTMC_ERR_CUDA, "surrogate: device allocation failed");
+  std::vector<float> P;
+  if (params) P.assign(params, params + SUR_NP);
+  else sur_init_params(P, c->p.seed);
+  CK(cudaMemcpyAsync(c->d_sur_P.p, P.data(), sizeof(float) * SUR_NP, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->d_sur_m.p, 0, sizeof(float) * SUR_NP, c->st));
+  CK(cudaMemsetAsync(c->d_sur_v.p, 0, sizeof(float) * SUR_NP, c->st));
+  CK(cudaMemsetAsync(c->d_sur_g.p, 0, sizeof(float) * SUR_NP, c->st));
+  CK(cudaMemsetAsync(c->d_sur_loss.p, 0, sizeof(double), c->st));
+  if (!keep_ring) CK(cudaMemsetAsync(c->d_rec_n.p, 0, sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(c->d_da_cnt.p, 0, sizeof(long long) * 2 * W, c->st));
+  CK(cudaMemsetAsync(c->d_sur_err.p, 0, sizeof(int), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->sur_cfg = *cfg;
+  c->sur_set = true;
+  c->sur_step = 0;
+  NNParams& Q = c->Q;
+  Q.da = 0;
+  Q.sc = sur_dev(*cfg);
+  Q.surP = c->d_sur_P.p;
+  Q.da_cnt = c->d_da_cnt.p;
+  Q.rec_rows = nullptr;
+  Q.rec_y = c->d_rec_y.p;
+  Q.rec_n = c->d_rec_n.p;
+  Q.rec_cap = capacity;
+  Q.rec_every = record_every;
+  drop_graphs(c);
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_record(ptmc_ctx* c, int on) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  if (on && c->Q.da)
+    return c->fail(PTMC_ERR_STATE, "records come from the exact chain: switch delayed acceptance off first");
+  c->Q.rec_rows = on ? c->d_rec_rows.p : nullptr;
+  drop_graphs(c);
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_train(ptmc_ctx* c, int steps, int batch, double lr, double* loss_out) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  if (c->Q.da) return c->fail(PTMC_ERR_STATE, "the surrogate is frozen while delayed acceptance is on");
+  if (steps < 0 || batch < 1 || !(lr > 0)) return c->fail(PTMC_ERR_ARG, "surrogate: bad training arguments");
+  unsigned long long nrec = 0;
+  CK(cudaMemcpyAsync(&nrec, c->d_rec_n.p, sizeof(nrec), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  const int n = (int)std::min<unsigned long long>(nrec, (unsigned long long)c->Q.rec_cap);
+  if (n < 1) return c->fail(PTMC_ERR_STATE, "surrogate: no training records captured");
+  if (c->sur_cfg.escale == 0) {  // output scale from the data: 1.4826 x median |dE - median|
+    std::vector<float> y(n);
+    CK(cudaMemcpyAsync(y.data(), c->d_rec_y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    std::vector<float> t(y);
+    std::nth_element(t.begin(), t.begin() + n / 2, t.end());
+    const float med = t[n / 2];
+    for (auto& v : t) v = std::fabs(v - med);
+    std::nth_element(t.begin(), t.begin() + n / 2, t.end());
+    double sc = 1.4826 * t[n / 2];
+    if (!(sc > 0)) sc = 1e-3;
+    c->sur_cfg.escale = sc;
+    c->Q.sc.escale = (float)sc;
+  }
+  const SurCfgDev sd = sur_dev(c->sur_cfg);
+  const int k0 = steps - std::max(1, steps / 10);
+  const int grid = std::min(batch, 3 * sm_count());
+  for (int k = 0; k < steps; ++k) {
+    if (k == k0) CK(cudaMemsetAsync(c->d_sur_loss.p, 0, sizeof(double), c->st));
+    int e = sur_launch_grad(sd, c->d_sur_P.p, c->d_rec_rows.p, c->d_rec_y.p, n, nullptr, batch,
+                            c->p.seed ^ 0x5A17ull, c->sur_step, c->d_sur_g.p, c->d_sur_loss.p,
+                            c->d_sur_err.p, grid, c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_sur_grad launch");
+    c->sur_step += 1;
+    e = sur_launch_adam(c->d_sur_P.p, c->d_sur_g.p, c->d_sur_m.p, c->d_sur_v.p, c->sur_step,
+                        (float)lr, c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_sur_adam launch");
+    c->stats.kernel_launches += 2;
+  }
+  int rc = sur_err_check(c);
+  if (rc) return rc;
+  if (loss_out) {
+    double L = 0;
+    CK(cudaMemcpyAsync(&L, c->d_sur_loss.p, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    *loss_out = steps > 0 ? L / (steps - k0) : 0.0;
+  }
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_enable(ptmc_ctx* c, int on) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  if (on) {
+    if (c->Q.rec_rows) return c->fail(PTMC_ERR_STATE, "stop recording before enabling delayed acceptance");
+    if (!(c->sur_cfg.escale > 0))
+      return c->fail(PTMC_ERR_STATE, "surrogate output scale unset: train first or give escale");
+    NNParams Q = c->Q;
+    Q.da = 1;
+    if (nn_smem_bytes(Q, c->nn_Nmax, !c->f32()) > 227 * 1024)
+      return c->fail(PTMC_ERR_LIMIT, "NN walker state plus surrogate tiles exceed 227 KB of shared memory");
+  }
+  c->Q.da = on ? 1 : 0;
+  drop_graphs(c);
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_get(ptmc_ctx* c, float* params, ptmc_surrogate_cfg* cfg, long long* stats) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  if (params)
+    CK(cudaMemcpyAsync(params, c->d_sur_P.p, sizeof(float) * SUR_NP, cudaMemcpyDeviceToHost, c->st));
+  std::vector<long long> cnt(2 * (size_t)c->W);
+  unsigned long long nrec = 0;
+  CK(cudaMemcpyAsync(cnt.data(), c->d_da_cnt.p, sizeof(long long) * cnt.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(&nrec, c->d_rec_n.p, sizeof(nrec), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (cfg) *cfg = c->sur_cfg;
+  if (stats) {
+    stats[0] = (long long)nrec;
+    stats[1] = stats[2] = stats[3] = 0;
+    for (int g = 0; g < c->W; ++g) {
+      stats[1] += cnt[2 * (size_t)g];
+      stats[2] += cnt[2 * (size_t)g + 1];
+    }
+  }
+  return PTMC_OK;
+}
+
+int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n, int* n_out) {
+  if (!c || !n_out || max_n < 0) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  unsigned long long nrec = 0;
+  CK(cudaMemcpyAsync(&nrec, c->d_rec_n.p, sizeof(nrec), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  int n = (int)std::min<unsigned long long>(std::min<unsigned long long>(nrec, c->Q.rec_cap),
+                                            (unsigned long long)max_n);
+  if (n > 0 && rows)
+    CK(cudaMemcpyAsync(rows, c->d_rec_rows.p, sizeof(float) * SUR_ROWS * n, cudaMemcpyDeviceToHost, c->st));
+  if (n > 0 && targets)
+    CK(cudaMemcpyAsync(targets, c->d_rec_y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *n_out = n;
+  return PTMC_OK;
 }
 
 }  // extern "C"

@@ -20,7 +20,7 @@ enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3 };
 enum { BC_SPH = 0, BC_CUB = 1 };
 enum { ENS_NVT = 0, ENS_NPT = 1 };
 enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
-enum { ST_OK = 0, ST_SPHERE = 1 };
+enum { ST_OK = 0, ST_SPHERE = 1, ST_TIMEOUT = 2 };  // TIMEOUT: a bounded tensor-core wait ran out
 constexpr int MAX_COEFF = 16;
 constexpr int MAX_REPLICAS = 32;
 constexpr int DRAW_BUF = 16;

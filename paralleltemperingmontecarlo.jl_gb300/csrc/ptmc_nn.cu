@@ -20,9 +20,11 @@
 //   3. radial deltas: threads over (sf, j),
 //   4. angular deltas: threads over (j, k-chunk); each ordered pair (j, k)
 //      evaluates the old and new triangle (i, j, k) once and adds the centre-j
-//      term; pairs with j < k also add the centre-i term.  Exponentials are
-//      shared by the functions with equal eta, powers (1 + lambda cos)^zeta by
-//      repeated squaring for zeta in {1, 2, 4, 8, 16},
+//      term; one of (j, k) and (k, j) also adds the centre-i term.  FP64:
+//      exponentials shared by the functions with equal eta, powers
+//      (1 + lambda cos)^zeta by repeated squaring for zeta in {1, 2, 4, 8, 16};
+//      FP32: one ex2(zeta lg2(1 + lambda cos) + lg2(tpz) - eta log2(e) s) per
+//      function and term, branch-free,
 //   5. the MLP on every atom (every column of G changes): threads over
 //      (atom, hidden unit), layer by layer, block sum of the atom energies,
 //   6. Metropolis on thread 0, commit (positions, distance and cut-off
@@ -92,7 +94,7 @@ struct NNSmem {
   Real* G;     // [S][N]
   Real* dG;    // [S][N]
   Real* part;  // [NCH][SA][64]
-  Real* rows;  // d2n, fn, rn, d2o, fo, ro [6][64]
+  Real* rows;  // d2n, fn, rn, d2o, fo, ro, 1/rn, 1/ro [8][64]
   Real* vn;    // [64][3] t - x_j
   Real* vo;    // [64][3] x_i - x_j
   Real* W;     // MLP parameters (gathered layout)
@@ -100,7 +102,8 @@ struct NNSmem {
   Real* h2;    // [N][H2]
   Real* red;   // block-reduction scratch [NN_THREADS/32 + 8]
   Real* dGi;   // [S] centre-i deltas
-  Real* sfp;   // [SA][4] angular parameters: eta, lambda, tpz, zeta code
+  Real* sfp;   // [SA][4] angular parameters: FP64 eta, lambda, tpz, zeta code;
+               // FP32 -eta*log2(e), zeta, log2(tpz), lambda
   double* drw; // draw buffer [16]
   double* tpos;// trial position [3]
   int* flags;  // [4]
@@ -122,7 +125,7 @@ __device__ size_t nn_carve(NNSmem<Real>& s, unsigned char* base, int N, int S, i
   s.G = (Real*)take(sizeof(Real) * S * N);
   s.dG = (Real*)take(sizeof(Real) * S * N);
   s.part = (Real*)take(sizeof(Real) * NCH * (SA > 0 ? SA : 1) * 64);
-  s.rows = (Real*)take(sizeof(Real) * 6 * 64);
+  s.rows = (Real*)take(sizeof(Real) * 8 * 64);
   s.vn = (Real*)take(sizeof(Real) * 64 * 3);
   s.vo = (Real*)take(sizeof(Real) * 64 * 3);
   s.W = (Real*)take(sizeof(Real) * nW);
@@ -203,10 +206,17 @@ __device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X,
   for (int k = threadIdx.x; k < Q.nW; k += blockDim.x) s.W[k] = (Real)Q.W[k];
   for (int q = threadIdx.x; q < Q.SA; q += blockDim.x) {
     const NNSF& f = Q.sf[Q.SR + q];
-    s.sfp[4 * q] = (Real)f.eta;
-    s.sfp[4 * q + 1] = (Real)f.lambda;
-    s.sfp[4 * q + 2] = (Real)f.tpz;
-    s.sfp[4 * q + 3] = (Real)(f.zc == 0 ? -f.zeta : (double)f.zc);  // >0: code, <=0: -zeta
+    if constexpr (sizeof(Real) == 4) {  // exponent form of the FP32 path
+      s.sfp[4 * q] = (Real)(-f.eta * 1.4426950408889634);
+      s.sfp[4 * q + 1] = (Real)f.zeta;
+      s.sfp[4 * q + 2] = (Real)log2(f.tpz);
+      s.sfp[4 * q + 3] = (Real)f.lambda;
+    } else {
+      s.sfp[4 * q] = (Real)f.eta;
+      s.sfp[4 * q + 1] = (Real)f.lambda;
+      s.sfp[4 * q + 2] = (Real)f.tpz;
+      s.sfp[4 * q + 3] = (Real)(f.zc == 0 ? -f.zeta : (double)f.zc);  // >0: code, <=0: -zeta
+    }
   }
   if (Gg)
     for (int k = threadIdx.x; k < Q.S * N; k += blockDim.x) s.G[k] = (Real)Gg[k];
@@ -304,6 +314,22 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
   double* Gg = Q.G + (size_t)gw * S * Q.Nmax;
   load_walker(Q, s, Xg, Gg, N);
   if (P.status[g] != ST_OK) return;
+  // delayed acceptance: surrogate tiles after the walker state, 128-byte aligned
+  SurSmem ss{};
+  uint32_t tbase = 0, mphase = 0;
+  long long n_rej1 = 0, n_exact = 0;
+  if (Q.da) {
+    size_t off = nn_carve(s, smem_raw, N, S, SA, Q.H1, Q.H2, Q.nW);
+    uint32_t a = smem_u32(smem_raw) + (uint32_t)off;
+    off += (128u - (a & 127u)) & 127u;
+    sur_carve(ss, smem_raw + off);
+    sur_stage(ss, Q.surP);
+    if (warp == 0) tmem_alloc(smem_u32(ss.tslot), SUR_TMEM_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    tbase = *ss.tslot;
+  }
   const int slot = Q.sow[g];
   const int gs = rd->wk + slot;
   const double beta = P.beta[gs];
@@ -431,6 +457,8 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
     Real* d2o = s.rows + 192;
     Real* fo = s.rows + 256;
     Real* ro = s.rows + 320;
+    Real* rin = s.rows + 384;
+    Real* rio = s.rows + 448;
     // ---- 2. rows and hard core (energy_update! RuNNer, src/EnergyEvaluation.jl:1593-1606)
     int hard = 0;
     for (int j = tid; j < N; j += blockDim.x) {
@@ -450,10 +478,43 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
       s.vo[3 * j + 2] = oz;
       d2o[j] = s.D2[i * N + j];
       ro[j] = sqrt(d2o[j]);
+      rin[j] = Real(1) / rn[j];
+      rio[j] = Real(1) / ro[j];
       fo[j] = s.F[i * N + j];
       if (j != i && d < (Real)Q.boundary2) hard = 1;
     }
     hard = __syncthreads_or(hard);
+    // ---- delayed acceptance, stage 1 (Christen & Fox 2005): the surrogate
+    // dE_s screens the proposal with its own draw; a rejection here costs no
+    // exact evaluation
+    double dEs = 0.0;
+    if (Q.da) {
+      float r = -1.f;
+      if (tid < SUR_ROWS) {
+        const int j = tid & (SUR_ROWS / 2 - 1);
+        if (j < N && j != i) r = (float)(tid < SUR_ROWS / 2 ? rn[j] : ro[j]);
+      }
+      float phi = 0.f;
+      if (!sur_tile_forward(ss, Q.sc, tbase, mphase, r, phi, nullptr, nullptr)) {
+        status = ST_TIMEOUT;
+        break;
+      }
+      float v = warp_sum(r >= 0.f ? (tid < SUR_ROWS / 2 ? phi : -phi) : 0.f);
+      if (lane == 0 && warp < SUR_ROWS / 32) ss.vec[100 + warp] = v;
+      __syncthreads();
+      dEs = (double)((ss.vec[100] + ss.vec[101]) + (ss.vec[102] + ss.vec[103]));
+      int pass = 0;
+      if (warp == 0) {
+        double p1 = exp(-dEs * beta);
+        if (p1 > 1) p1 = 1.0;
+        pass = p1 >= draw();
+      }
+      if (!__syncthreads_or(warp == 0 && lane == 0 && pass)) {
+        ++n_rej1;
+        continue;
+      }
+      ++n_exact;
+    }
     Real new_en;
     if (hard) {
       new_en = Real(100.0);
@@ -468,7 +529,6 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
           const NNSF& f = Q.sf[q];
           Real eta = (Real)f.eta, gn = (Real)f.gnorm;
           d = rexp<Real>(-eta * d2n[j]) * (fn[j] * gn) - rexp<Real>(-eta * d2o[j]) * (fo[j] * gn);
-          atomicAdd(&s.dGi[q], d);
         }
         s.dG[q * N + j] = d;
       }
@@ -486,6 +546,54 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
           const Real vnx = s.vn[3 * j], vny = s.vn[3 * j + 1], vnz = s.vn[3 * j + 2];
           const Real vox = s.vo[3 * j], voy = s.vo[3 * j + 1], voz = s.vo[3 * j + 2];
           const Real rnj = rn[j], roj = ro[j], fnj = fn[j], foj = fo[j];
+          if constexpr (sizeof(Real) == 4) {
+            // FP32: every term is one ex2 of zeta*lg2(1 + lambda cos) + lg2(tpz) -
+            // eta*log2(e)*s (no per-function branches); the centre-i term of an
+            // unordered pair {j, k} is taken by exactly one of (j, k) and (k, j),
+            // chosen by the parity of j + k so that the threads share it evenly
+            const float rnji = rin[j], roji = rio[j], d2nj = d2n[j], d2oj = d2o[j];
+            const float4* sf4 = reinterpret_cast<const float4*>(s.sfp);
+            for (int k = k0; k < k1; ++k) {
+              if (k == i || k == j) continue;
+              const float rjk2 = s.D2[j * N + k], fjk = s.F[j * N + k];
+              const float fpn = fnj * fn[k] * fjk, fpo = foj * fo[k] * fjk;
+              if (fpn == 0.f && fpo == 0.f) continue;
+              const float rjki = rsqrtf(rjk2);
+              const float ux = s.X[3 * k] - s.X[3 * j], uy = s.X[3 * k + 1] - s.X[3 * j + 1],
+                          uz = s.X[3 * k + 2] - s.X[3 * j + 2];
+              const float cjn = ((vnx * ux + vny * uy) + vnz * uz) * (rnji * rjki);
+              const float cjo = ((vox * ux + voy * uy) + voz * uz) * (roji * rjki);
+              const float sn = (d2nj + d2n[k]) + rjk2, so = (d2oj + d2o[k]) + rjk2;
+              const bool ci_on = (j < k) == (((j + k) & 1) != 0);
+              const float ljn_p = lg2f(fmaxf(1.f + cjn, 0.f)), ljn_m = lg2f(fmaxf(1.f - cjn, 0.f));
+              const float ljo_p = lg2f(fmaxf(1.f + cjo, 0.f)), ljo_m = lg2f(fmaxf(1.f - cjo, 0.f));
+              float lin_p = 0.f, lin_m = 0.f, lio_p = 0.f, lio_m = 0.f;
+              if (ci_on) {
+                const float cin = ((vnx * s.vn[3 * k] + vny * s.vn[3 * k + 1]) + vnz * s.vn[3 * k + 2]) *
+                                  (rnji * rin[k]);
+                const float cio = ((vox * s.vo[3 * k] + voy * s.vo[3 * k + 1]) + voz * s.vo[3 * k + 2]) *
+                                  (roji * rio[k]);
+                lin_p = lg2f(fmaxf(1.f + cin, 0.f));
+                lin_m = lg2f(fmaxf(1.f - cin, 0.f));
+                lio_p = lg2f(fmaxf(1.f + cio, 0.f));
+                lio_m = lg2f(fmaxf(1.f - cio, 0.f));
+              }
+#pragma unroll
+              for (int q = 0; q < MAX_NN_ANG; ++q) {
+                if (q < SA) {
+                  const float4 pr = sf4[q];  // -eta*log2e, zeta, lg2(tpz), lambda
+                  const float tn = fmaf(pr.x, sn, pr.z), to = fmaf(pr.x, so, pr.z);
+                  const bool lp = pr.w > 0.f;
+                  accj[q] = fmaf(fpn, ex2f(fmaf(pr.y, lp ? ljn_p : ljn_m, tn)), accj[q]);
+                  accj[q] = fmaf(-fpo, ex2f(fmaf(pr.y, lp ? ljo_p : ljo_m, to)), accj[q]);
+                  if (ci_on) {
+                    acci[q] = fmaf(fpn, ex2f(fmaf(pr.y, lp ? lin_p : lin_m, tn)), acci[q]);
+                    acci[q] = fmaf(-fpo, ex2f(fmaf(pr.y, lp ? lio_p : lio_m, to)), acci[q]);
+                  }
+                }
+              }
+            }
+          } else
           for (int k = k0; k < k1; ++k) {
             if (k == i || k == j) continue;
             const Real rjk2 = s.D2[j * N + k], fjk = s.F[j * N + k];
@@ -542,15 +650,38 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
           for (int c = 0; c < NCH; ++c) v += s.part[(c * SA + q) * 64 + j];
         s.dG[(SR + q) * N + j] = v;
       }
+      for (int q = warp; q < SR; q += NN_THREADS / 32) {  // centre-i radial deltas
+        Real v = 0;
+        for (int j = lane; j < N; j += 32) v += s.dG[q * N + j];
+        v = warp_sum(v);
+        if (lane == 0) s.dGi[q] = v;
+      }
       __syncthreads();
       for (int q = tid; q < S; q += blockDim.x) s.dG[q * N + i] = s.dGi[q];
       __syncthreads();
       // ---- 5. MLP on every atom (calc_new_runner_energy!, src/EnergyEvaluation.jl:1269-1275)
       new_en = mlp_energy<Real>(Q, s, N, true);
     }
-    // ---- 6. Metropolis (src/MCRun.jl:122-132) and commit (swap_vars!, swap_config.jl:213-221)
+    // ---- training record of this exact move (proposal rows and exact dE)
+    if (Q.rec_rows && !hard) {
+      const long long m = (rd->cyc[phase]) * (long long)N + step;
+      if (m % Q.rec_every == 0) {
+        if (tid == 0) s.flags[2] = (int)(atomicAdd(Q.rec_n, 1ull) % (unsigned long long)Q.rec_cap);
+        __syncthreads();
+        const size_t at = (size_t)s.flags[2];
+        if (tid < SUR_ROWS) {
+          const int j = tid & (SUR_ROWS / 2 - 1);
+          float r = -1.f;
+          if (j < N && j != i) r = (float)(tid < SUR_ROWS / 2 ? rn[j] : ro[j]);
+          Q.rec_rows[at * SUR_ROWS + tid] = r;
+        }
+        if (tid == 0) Q.rec_y[at] = (float)((double)new_en - en);
+      }
+    }
+    // ---- 6. Metropolis (src/MCRun.jl:122-132) and commit (swap_vars!, swap_config.jl:213-221);
+    // with delayed acceptance this is the second stage, exp(-beta (dE - dE_s))
     if (warp == 0) {
-      double prob = exp(-((double)new_en - en) * beta);
+      double prob = exp(-(((double)new_en - en) - dEs) * beta);
       if (prob > 1) prob = 1.0;
       double u = draw();
       if (lane == 0) s.flags[3] = (prob >= u) ? 1 : 0;
@@ -589,8 +720,18 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
     P.status[g] = status;
     P.cnt[6 * (size_t)gs + 0] += acc;
     P.cnt[6 * (size_t)gs + 1] += acc;
+    if (Q.da) {
+      Q.da_cnt[2 * (size_t)g] += n_rej1;
+      Q.da_cnt[2 * (size_t)g + 1] += n_exact;
+    }
   }
   if (warp == 0 && lane == 0) P.ctr[g] = ctr;
+  if (Q.da) {  // free the tensor memory (every path out of the move loop comes here)
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tbase, SUR_TMEM_COLS);
+  }
 }
 
 // --------------------------------------------------------------- run epilogue
@@ -653,10 +794,11 @@ size_t nn_smem_bytes(const NNParams& Q, int N, bool f64) {
   auto al = [](size_t b) { return (b + 15) / 16 * 16; };
   size_t b = 0;
   b += al(8 * N * 3) + al(es * N * 3) + 2 * al(es * N * N) + 2 * al(es * Q.S * N);
-  b += al(es * NCH * (Q.SA > 0 ? Q.SA : 1) * 64) + al(es * 6 * 64) + 2 * al(es * 64 * 3);
+  b += al(es * NCH * (Q.SA > 0 ? Q.SA : 1) * 64) + al(es * 8 * 64) + 2 * al(es * 64 * 3);
   b += al(es * Q.nW) + al(es * N * Q.H1) + al(es * N * Q.H2) + al(es * 64) + al(es * (Q.S > 0 ? Q.S : 1));
   b += al(es * 4 * MAX_NN_ANG);
   b += al(8 * DRAW_BUF) + al(8 * 4) + al(4 * 4);
+  if (Q.da) b += 128 + SUR_SMEM_BYTES;  // 128-byte alignment slack + tiles
   return b;
 }
 

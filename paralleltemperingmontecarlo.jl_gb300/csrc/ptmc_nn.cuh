@@ -1,6 +1,7 @@
 // ptmc_nn.cuh — parameters of the neural-network potential path (ptmc_nn.cu).
 #pragma once
 #include "ptmc_engine.cuh"
+#include "ptmc_surrogate.cuh"
 
 namespace ptmc {
 
@@ -27,6 +28,17 @@ struct NNParams {
   double* G;          // [walkers][S][Nmax]
   const int* run_of_walker;
   int* sow;           // slot of walker (global walker index -> slot within its run)
+  // delayed acceptance (two-stage moves screened by the pair surrogate)
+  int da;             // 1: on
+  SurCfgDev sc;
+  const float* surP;  // [SUR_NP] surrogate parameters
+  long long* da_cnt;  // [walkers][2]: first-stage rejections, exact evaluations
+  // training-record capture (exact moves only): move m of a walker in cycle c
+  // is recorded when (c * N + m) % rec_every == 0, into a ring of rec_cap
+  float* rec_rows;    // [rec_cap][128] distances (ptmc_surrogate.cuh row layout), NULL = off
+  float* rec_y;       // [rec_cap] exact dE
+  unsigned long long* rec_n;  // records written so far
+  int rec_cap, rec_every;
 };
 
 size_t nn_smem_bytes(const NNParams& Q, int N, bool f64);

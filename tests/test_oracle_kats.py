@@ -207,3 +207,76 @@ def test_oracle_npt_invariants(orc):
                                                            box[i], rc2), rel=1e-9)
     _, ev, hp = run.hist()
     assert ev.sum() == R * 60
+
+
+# ---------------------------------------------------------------- surrogate oracle
+SUR_CFG = [2.0, 12.0, 1.125, 12.0, 0.02]
+
+
+def _sur_case(orc, n=6, seed=0):
+    rng = np.random.default_rng(seed)
+    P = rng.normal(0, 0.3, orc.sur_nparams())
+    rows = rng.uniform(3.0, 14.0, (n, 128)).astype(np.float32)
+    rows[:, 50:64] = -1.0
+    rows[:, 114:128] = -1.0
+    y = rng.normal(0, 0.02, n).astype(np.float32)
+    return P, rows, y
+
+
+def test_surrogate_oracle_gradient_finite_differences(orc):
+    """The oracle's analytic gradient of the Huber loss (FP64, no BF16 rounding)
+    against central differences, on every parameter block."""
+    P, rows, y = _sur_case(orc)
+    L, g = orc.sur_loss_grad(SUR_CFG, P, rows, y, bf16=False)
+    h = 1e-6
+    idx = np.r_[0:5, 511, 512, 540, 544, 1000, 1567, 1568, 1599, 1600, 1631, 1632]
+    for k in idx:
+        Pp, Pm = P.copy(), P.copy()
+        Pp[k] += h
+        Pm[k] -= h
+        fd = (orc.sur_loss_grad(SUR_CFG, Pp, rows, y, bf16=False)[0] -
+              orc.sur_loss_grad(SUR_CFG, Pm, rows, y, bf16=False)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * np.abs(g).max() + 1e-9, (k, fd, g[k])
+
+
+def test_surrogate_oracle_antisymmetry_and_bf16(orc):
+    """dE_s of the reverse move (new and old rows swapped) is -dE_s; BF16
+    rounding of the matrix operands changes dE_s by a small relative amount."""
+    P, rows, _ = _sur_case(orc, n=10, seed=1)
+    rev = np.concatenate([rows[:, 64:], rows[:, :64]], axis=1)
+    for bf in (False, True):
+        a = orc.sur_forward(SUR_CFG, P, rows, bf16=bf)
+        b = orc.sur_forward(SUR_CFG, P, rev, bf16=bf)
+        np.testing.assert_allclose(a, -b, rtol=1e-12, atol=1e-15)
+    a = orc.sur_forward(SUR_CFG, P, rows, bf16=False)
+    b = orc.sur_forward(SUR_CFG, P, rows, bf16=True)
+    assert np.max(np.abs(a - b)) < 0.05 * np.max(np.abs(a)) and np.max(np.abs(a - b)) > 0
+
+
+def test_oracle_delayed_acceptance_zero_surrogate_is_exact_chain(orc):
+    """With dE_s = 0 the first stage always passes; the chain makes the same
+    accept decisions as the plain chain but consumes one more draw per move,
+    so it is a valid, different chain with the same statistics."""
+    import json
+    tables = json.load(open(os.path.join(GOLDEN, "nn_cu55.json")))
+    rows = []
+    for f in tables["sf"]:
+        rows.append([f["kind"], f["type"], f["eta"], f["lambda"], f["zeta"], 12.0, f["gmin"], f["gmax"]])
+    sf = np.array(rows)
+    rng = np.random.default_rng(3)
+    nodes = [88, 20, 20, 1]
+    w = []
+    for l in range(1, 4):
+        lim = 1 / np.sqrt(nodes[l - 1])
+        w += [rng.uniform(-lim, lim, nodes[l - 1] * nodes[l]), rng.uniform(-lim, lim, nodes[l])]
+    w = np.concatenate(w) * 0.01
+    N, R = 6, 2
+    x0 = np.array([[0, 0, 0], [4.5, 0, 0], [0, 4.5, 0], [0, 0, 4.5], [4.5, 4.5, 0], [0, 4.5, 4.5]], float)
+    T, _ = orc.tempgrid(300.0, 900.0, R)
+    run = orc.Run(N, R, np.stack([x0] * R), T, bc=orc.BC_SPHERE, bc_param=10.0, exch_prob=1.0, seed=4)
+    run.set_nn(sf, w, nodes, 0.0)
+    run.init()
+    run.set_surrogate(SUR_CFG, np.zeros(orc.sur_nparams()))
+    run.cycles(1, 5)
+    st = run.sur_stats()
+    assert st["stage1_rejects"] == 0 and st["exact_evals"] == 5 * N * R
