@@ -80,7 +80,8 @@ def workload(name):
                     bc=("sphere", 14.0), sizes=lambda B: [55] * B,
                     start=lambda n, k: cu55_ico(), resync=1000,
                     # per move: 74.4 k angular triple terms x ~30 ops + 239 k MLP flops
-                    flops_move=74400 * 30 + 239000, flops_pair=0, mufu_pair=0)
+                    flops_move=74400 * 30 + 239000, flops_pair=0, mufu_pair=0,
+                    da=True, cycles=20)
     if name == "batched":
         ns = [13, 38, 55, 101, 147]
 
@@ -100,15 +101,45 @@ def default_runs(name, n_sm=152):
 
 def nn_potential(pk):
     """88 G2/G4 functions of scripts/cu55.jl with r_c = 12 bohr, MLP 88-20-20-1
-    with seeded FP32 weights (output layer x0.01 to give energies of ~1e-2 Eh)."""
+    with seeded FP32 weights; the output layer is scaled by 0.3 so that the
+    exact chain accepts ~20-40 % of the default 0.1-bohr moves at 300-900 K, and
+    a 3-bohr hard core (E = 100 below it) keeps atoms apart."""
     tables = json.load(open(os.path.join(ROOT, "tests", "golden", "nn_cu55.json")))
     nodes = [88, 20, 20, 1]
     return pk.RuNNerPotential(pk.RuNNerPotential.sf_table(tables, 12.0),
-                              pk.RuNNerPotential.random_weights(nodes, 3, 0.01), nodes)
+                              pk.RuNNerPotential.random_weights(nodes, 3, 0.3), nodes, boundary=3.0)
+
+
+def train_surrogate(pk, eng, sizes, R, cycles=300, capacity=40000, steps=4000):
+    """Delayed acceptance set-up (outside the timed region): capture moves of
+    the exact chain, train the pair surrogate on the GPU, freeze, enable."""
+    every = max(1, (cycles * sum(sizes) * R) // capacity)
+    eng.surrogate_set(pk.PairSurrogate(2.0, 12.0, None, 12.0, 0.0), capacity=capacity,
+                      record_every=every)
+    eng.surrogate_record(True)
+    t0 = time.perf_counter()
+    eng.cycles_nosample(cycles)
+    eng.surrogate_record(False)
+    t1 = time.perf_counter()
+    loss = eng.surrogate_train(steps, batch=512, lr=2e-3)
+    t2 = time.perf_counter()
+    rows, y = eng.surrogate_records()
+    P, sur, _ = eng.surrogate_state()
+    held = slice(-min(5000, len(y) // 5), None)
+    corr = float(np.corrcoef(sur.eval(P, rows[held]), y[held])[0, 1])
+    t3 = time.perf_counter()
+    kappa = eng.surrogate_calibrate(0.0, 10)
+    t4 = time.perf_counter()
+    eng.surrogate_enable(True)
+    return dict(records=int(len(y)), record_s=t1 - t0, train_s=t2 - t1, train_steps=steps,
+                loss=loss, heldout_corr=corr, escale=sur.escale, calibrate_s=t4 - t3,
+                kappa=[round(float(k), 4) for k in kappa])
 
 
 # --------------------------------------------------------------- GPU arm
-def make_engine(pk, W, B, precision, cycles_per_launch, seed, device):
+def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=None):
+    """Engine of B runs of workload W.  `starts`: per run, the slot-ordered
+    states of an earlier engine (configurations and step sizes) to start from."""
     R = W["R"]
     sizes = W["sizes"](B)
     mp_ = pk.MCParams(mc_cycles=10 ** 6, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=sizes[0])
@@ -124,13 +155,16 @@ def make_engine(pk, W, B, precision, cycles_per_launch, seed, device):
                     resync_every=W["resync"], exch_prob=1.0, seed=seed,
                     cycles_per_launch=cycles_per_launch, device=device)
     for r, n in enumerate(sizes):
-        x = W["start"](n, r)
         if W["bc"][0] == "cubic":
             bc = pk.CubicBC(W["bc"][1])
         else:
             rad = W["bc"][1] if W["bc"][1] else 0.9 * n ** (1 / 3) * 3 + 3.0
             bc = pk.SphericalBC(rad)
-        eng.set_configs(r, pk.Config(x, bc))
+        if starts is None:
+            eng.set_configs(r, pk.Config(W["start"](n, r), bc))
+        else:
+            st = starts[r]
+            eng.set_configs(r, [pk.Config(x, bc) for x in st["xyz"]], max_displ=st["max_displ"])
     eng.init()
     return eng, sizes
 
@@ -209,11 +243,11 @@ def gpu_arm(args, rank, world):
     pk._capi.check(L.ptmc_measure_peaks(args.local_rank, ctypes.byref(f32), ctypes.byref(f64),
                                         ctypes.byref(mufu)))
     res = {}
-    for form in (["fp64", "fp32"] if not args.only_chosen else ["fp32"]):
-        eng, sizes = make_engine(pk, W, B, form, args.cycles, 1234 + 7919 * rank, args.local_rank)
-        for _ in range(args.warmup):
-            eng.cycles_nosample(args.cycles)
+
+    def timed(eng, form, sizes):
+        """K timed steps of `eng` (barrier + synchronize on both sides)."""
         st0 = eng.stats()
+        acc0 = sum(int(eng.states(r)["counts"][:, 0].sum()) for r in range(B))
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
@@ -235,28 +269,74 @@ def gpu_arm(args, rank, world):
             moves_all = float(m.item())
         else:
             moves_all = float(moves)
-        res[form] = dict(value=moves_all / dev_s, ms_per_step=1e3 * dev_s / args.steps, wall=wall,
-                         launches=st1["kernel_launches"] - st0["kernel_launches"],
-                         drift=st1["max_drift"], clocks=clk.summary(), moves=moves,
-                         sizes=sizes)
+        acc = sum(int(eng.states(r)["counts"][:, 0].sum()) for r in range(B))
+        return dict(value=moves_all / dev_s, ms_per_step=1e3 * dev_s / args.steps, wall=wall,
+                    launches=st1["kernel_launches"] - st0["kernel_launches"],
+                    drift=st1["max_drift"], clocks=clk.summary(), moves=moves, sizes=sizes,
+                    acceptance=(acc - acc0) / moves)
+
+    seed = 1234 + 7919 * rank
+    if W.get("da"):
+        # delayed acceptance: one FP32 chain is equilibrated and its surrogate
+        # trained (untimed); then the exact FP32 form, the surrogate-screened form
+        # and (from the same configurations and step sizes) the plain FP64 form
+        # are timed from the same chain state
+        eng, sizes = make_engine(pk, W, B, "fp32", args.cycles, seed, args.local_rank)
+        for _ in range(args.warmup):
+            eng.cycles_nosample(args.cycles)
+        da = train_surrogate(pk, eng, sizes, W["R"])
+        trained = eng.surrogate_state()[:2]
+        starts = [eng.states(r) for r in range(B)]
+        if not args.only_chosen:
+            eng.surrogate_enable(False)
+            res["fp32"] = timed(eng, "fp32", sizes)
+            eng.surrogate_enable(True)
+        sur0 = eng.surrogate_state()[2]
+        res["fp32_da"] = timed(eng, "fp32_da", sizes)
+        sur1 = eng.surrogate_state()[2]
+        moves = res["fp32_da"]["moves"]
+        da.update(stage1_reject_frac=(sur1["stage1_rejects"] - sur0["stage1_rejects"]) / moves,
+                  exact_eval_frac=(sur1["exact_evals"] - sur0["exact_evals"]) / moves,
+                  acceptance=res["fp32_da"]["acceptance"],
+                  acceptance_exact=res["fp32"]["acceptance"] if "fp32" in res else None)
+        res["fp32_da"]["da"] = da
         eng.close()
+        if not args.only_chosen:
+            eng, _ = make_engine(pk, W, B, "fp64", args.cycles, seed + 1, args.local_rank, starts=starts)
+            eng.cycles_nosample(args.cycles)
+            res["fp64"] = timed(eng, "fp64", sizes)
+            eng.close()
+    else:
+        for form in (["fp64", "fp32"] if not args.only_chosen else ["fp32"]):
+            eng, sizes = make_engine(pk, W, B, form, args.cycles, seed, args.local_rank)
+            for _ in range(args.warmup):
+                eng.cycles_nosample(args.cycles)
+            res[form] = timed(eng, form, sizes)
+            eng.close()
     # e2e through the public API with host buffers, one engine per step
     e2e = None
     if rank == 0 and not args.no_e2e:
-        form = "fp32"
+        # per step: a context from host arrays (start configurations; with delayed
+        # acceptance also the trained surrogate's parameters), the step's cycles,
+        # every run's energies read back
         ts = []
         h2d = d2h = 0
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
-            eng, sizes = make_engine(pk, W, B, form, args.cycles, 99 + k, args.local_rank)
+            eng, sizes = make_engine(pk, W, B, "fp32", args.cycles, 99 + k, args.local_rank)
+            h2d = sum(n * 3 * 8 for n in sizes)  # start configurations (one per run)
+            if W.get("da"):
+                P, sur = trained
+                eng.surrogate_set(sur, capacity=1, params=P)
+                eng.surrogate_enable(True)
+                h2d += P.nbytes
             eng.cycles_nosample(args.cycles)
             outs = [eng.states(r)["en_tot"] for r in range(B)]
             eng.close()
             t1 = time.perf_counter()
             if k >= args.warmup:
                 ts.append(t1 - t0)
-            h2d = sum(n * 3 * 8 for n in sizes)  # start configurations (one per run)
             d2h = sum(o.nbytes for o in outs)
         e2e = dict(value=sum(sizes) * W["R"] * args.cycles / statistics.mean(ts),
                    unit="atom-moves/s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h)
@@ -317,7 +397,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cu55", choices=["cu55", "ne13", "npt108", "batched", "nn55"])
     ap.add_argument("--runs", type=int, default=0, help="independent PT runs batched (0 = fill the GPU)")
-    ap.add_argument("--cycles", type=int, default=200, help="MC cycles per step")
+    ap.add_argument("--cycles", type=int, default=0, help="MC cycles per step (0: 200, NN: 20)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
     ap.add_argument("--only-chosen", action="store_true")
@@ -329,6 +409,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     args.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     W = workload(args.workload)
+    if args.cycles <= 0:
+        args.cycles = W.get("cycles", 200)
     cores = os.cpu_count() or 1
 
     if args.impl == "reference":
@@ -366,7 +448,8 @@ def main():
     res, peaks, B, e2e = gpu_arm(args, rank, world)
     if rank != 0:
         return
-    ch = res["fp32"]
+    chosen = "fp32_da" if "fp32_da" in res else "fp32"
+    ch = res[chosen]
     sizes = ch["sizes"]
     # roofline of the dominant kernel (k_cycles): algorithmic FP32 ops per launch
     pairs_per_move = [n - 1 for n in sizes]
@@ -380,14 +463,19 @@ def main():
         "metric": "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error",
         "value": ch["value"], "unit": "atom-moves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ch["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": W["name"] + "_fp32resync_batched", "runs_per_gpu": B,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64+bf16" if chosen == "fp32_da" else "f32+f64", "data": "synthetic",
+        "config": {"workload": W["name"] + ("_fp32resync_batched_da" if chosen == "fp32_da"
+                                            else "_fp32resync_batched"), "runs_per_gpu": B,
                    "replicas": W["R"], "atoms": sorted(set(sizes)), "cycles_per_step": args.cycles,
                    "resync_every": W["resync"], "exchange": "every cycle",
                    "l2": "flushed between steps (256 MB write)"},
         "plain_fp64": ({"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
                         "chosen_over_plain": ch["value"] / res["fp64"]["value"]}
                        if "fp64" in res else None),
+        "fp32_exact": ({"value": res["fp32"]["value"], "ms_per_step": res["fp32"]["ms_per_step"]}
+                       if chosen != "fp32" and "fp32" in res else None),
+        "delayed_acceptance": ch.get("da"),
         "fp32_max_drift_eh": ch["drift"],
         "roofline": {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
                      "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"], "traffic": None,

@@ -229,6 +229,20 @@ int ptmc_surrogate_enable(ptmc_ctx* c, int on);
  * rejections, exact evaluations, 0} summed over every walker. */
 int ptmc_surrogate_get(ptmc_ctx* c, float* params, ptmc_surrogate_cfg* cfg,
                        long long* stats);
+/* Screening strength per temperature slot.  With kappa_s the first stage
+ * accepts iff min(1, exp(-kappa_s beta_s dE_s)) >= u1 and the second iff
+ * min(1, exp(-beta_s (dE - kappa_s dE_s))) >= u2 (exact for any fixed kappa);
+ * kappa_s = 0 skips the surrogate for that slot (no first-stage draw).  The
+ * default after ptmc_surrogate_set is 1.  This call picks kappa_s in
+ * {0, 1/16, ..., 1} per slot to maximise accepted moves per unit cost,
+ * a(kappa)/(r + p1(kappa)), estimated on the slot's captured records (exact dE
+ * and the surrogate's dE_s), where r is the cost of a surrogate stage relative
+ * to an exact evaluation: cost_ratio if > 0, else measured by timing
+ * timing_cycles plain cycles without and with screening (these cycles advance
+ * the chain, without sampling).  kappa_out [R] (may be NULL) receives the
+ * choice.  The delayed-acceptance on/off state is left as it was. */
+int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles,
+                             double* kappa_out);
 /* Copy up to max_n captured records (rows [n][128], targets [n]); *n_out = count. */
 int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n,
                            int* n_out);

@@ -433,6 +433,16 @@ class Engine:
     def surrogate_enable(self, on=True):
         self._ck(self.L.ptmc_surrogate_enable(self.h, int(bool(on))))
 
+    def surrogate_calibrate(self, cost_ratio=0.0, timing_cycles=20):
+        """Per-temperature screening strength kappa (returned, one per slot),
+        chosen from the captured records; cost_ratio <= 0 measures the cost of
+        a surrogate stage relative to an exact evaluation by timing
+        `timing_cycles` plain cycles without and with screening."""
+        k = np.zeros(self.R)
+        self._ck(self.L.ptmc_surrogate_calibrate(self.h, float(cost_ratio), int(timing_cycles),
+                                                 _dptr(k)))
+        return k
+
     def surrogate_state(self):
         """(parameters, PairSurrogate config, stats dict)."""
         P = np.zeros(_capi.SUR_NPARAMS, dtype=np.float32)

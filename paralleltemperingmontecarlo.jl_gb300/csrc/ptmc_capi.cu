@@ -153,7 +153,9 @@ struct ptmc_ctx {
   DBuf<double> d_sur_loss;
   DBuf<unsigned long long> d_rec_n;
   DBuf<long long> d_da_cnt;
-  DBuf<int> d_sur_err;
+  DBuf<int> d_sur_err, d_rec_slot;
+  DBuf<float> d_da_kappa;
+  std::vector<double> sur_kappa;  // per slot index
   int sur_step = 0;  // Adam steps taken
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evfork = nullptr;
@@ -879,12 +881,14 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_nn_G.free_();
   c->d_nn_row.free_();
   c->d_nn_sow.free_();
-  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_rec_rows, &c->d_rec_y})
+  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_rec_rows, &c->d_rec_y,
+                  &c->d_da_kappa})
     b->free_();
   c->d_sur_loss.free_();
   c->d_rec_n.free_();
   c->d_da_cnt.free_();
   c->d_sur_err.free_();
+  c->d_rec_slot.free_();
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1363,7 +1367,7 @@ int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg, const float* 
   // the record ring survives a new set-up with the same capacity (re-training
   // from other initial parameters on the same records)
   const bool keep_ring = c->sur_set && c->Q.rec_cap == capacity;
-  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g}) b->free_();
+  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_da_kappa}) b->free_();
   c->d_sur_loss.free_();
   c->d_da_cnt.free_();
   c->d_sur_err.free_();
@@ -1371,14 +1375,21 @@ int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg, const float* 
     c->d_rec_rows.free_();
     c->d_rec_y.free_();
     c->d_rec_n.free_();
+    c->d_rec_slot.free_();
   }
   if (c->d_sur_P.alloc(SUR_NP) || c->d_sur_m.alloc(SUR_NP) || c->d_sur_v.alloc(SUR_NP) ||
       c->d_sur_g.alloc(SUR_NP) || c->d_sur_loss.alloc(1) || c->d_da_cnt.alloc(2 * (size_t)W) ||
-      c->d_sur_err.alloc(1))
+      c->d_sur_err.alloc(1) || c->d_da_kappa.alloc(W))
     return c->fail(PTMC_ERR_CUDA, "surrogate: device allocation failed");
   if (!keep_ring && (c->d_rec_rows.alloc((size_t)capacity * SUR_ROWS) ||
-                     c->d_rec_y.alloc(capacity) || c->d_rec_n.alloc(1)))
+                     c->d_rec_y.alloc(capacity) || c->d_rec_n.alloc(1) ||
+                     c->d_rec_slot.alloc(capacity)))
     return c->fail(PTMC_ERR_CUDA, "surrogate: device allocation failed");
+  c->sur_kappa.assign(c->R(), 1.0);
+  {
+    std::vector<float> k1(W, 1.0f);
+    CK(cudaMemcpyAsync(c->d_da_kappa.p, k1.data(), sizeof(float) * W, cudaMemcpyHostToDevice, c->st));
+  }
   std::vector<float> P;
   if (params) P.assign(params, params + SUR_NP);
   else sur_init_params(P, c->p.seed);
@@ -1399,8 +1410,10 @@ int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg, const float* 
   Q.sc = sur_dev(*cfg);
   Q.surP = c->d_sur_P.p;
   Q.da_cnt = c->d_da_cnt.p;
+  Q.da_kappa = c->d_da_kappa.p;
   Q.rec_rows = nullptr;
   Q.rec_y = c->d_rec_y.p;
+  Q.rec_slot = c->d_rec_slot.p;
   Q.rec_n = c->d_rec_n.p;
   Q.rec_cap = capacity;
   Q.rec_every = record_every;
@@ -1521,6 +1534,114 @@ int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n, 
     CK(cudaMemcpyAsync(targets, c->d_rec_y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   *n_out = n;
+  return PTMC_OK;
+}
+
+
+int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, double* kappa_out) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  if (c->Q.rec_rows) return c->fail(PTMC_ERR_STATE, "stop recording before calibrating");
+  if (!(c->sur_cfg.escale > 0)) return c->fail(PTMC_ERR_STATE, "train the surrogate before calibrating");
+  unsigned long long nrec = 0;
+  CK(cudaMemcpyAsync(&nrec, c->d_rec_n.p, sizeof(nrec), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  const int n = (int)std::min<unsigned long long>(nrec, (unsigned long long)c->Q.rec_cap);
+  if (n < 1) return c->fail(PTMC_ERR_STATE, "surrogate: no records to calibrate on");
+  const int R = c->R(), W = c->W;
+  const int da_before = c->Q.da;
+  auto set_kappa = [&](const std::vector<double>& k) -> int {
+    std::vector<float> kw(W);
+    for (const auto& r : c->rd)
+      for (int s2 = 0; s2 < R; ++s2) kw[r.wk + s2] = (float)k[s2];
+    CK(cudaMemcpyAsync(c->d_da_kappa.p, kw.data(), sizeof(float) * W, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return PTMC_OK;
+  };
+  double r = cost_ratio;
+  if (!(r > 0)) {  // cost of a surrogate stage relative to an exact evaluation, measured
+    if (timing_cycles < 1) return c->fail(PTMC_ERR_ARG, "need timing_cycles >= 1 to measure the cost ratio");
+    int rc = set_kappa(std::vector<double>(R, 1.0));
+    if (rc) return rc;
+    c->Q.da = 0;
+    drop_graphs(c);
+    rc = run_phase(c, timing_cycles, PHASE_PLAIN);
+    if (rc) return rc;
+    const double t_ex = c->stats.last_cycles_ms;
+    std::vector<long long> k0(2 * (size_t)W), k1(2 * (size_t)W);
+    CK(cudaMemcpyAsync(k0.data(), c->d_da_cnt.p, sizeof(long long) * k0.size(), cudaMemcpyDeviceToHost, c->st));
+    c->Q.da = 1;
+    drop_graphs(c);
+    rc = run_phase(c, timing_cycles, PHASE_PLAIN);
+    if (rc) return rc;
+    const double t_da = c->stats.last_cycles_ms;
+    CK(cudaMemcpyAsync(k1.data(), c->d_da_cnt.p, sizeof(long long) * k1.size(), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    double rej = 0, ex = 0;
+    for (int g = 0; g < W; ++g) {
+      rej += (double)(k1[2 * (size_t)g] - k0[2 * (size_t)g]);
+      ex += (double)(k1[2 * (size_t)g + 1] - k0[2 * (size_t)g + 1]);
+    }
+    const double f = ex / std::max(1.0, rej + ex);
+    r = t_ex > 0 ? t_da / t_ex - f : 0.05;
+    r = std::min(2.0, std::max(0.002, r));
+  }
+  // dE_s of every record on the GPU, then the choice per slot on the host
+  double* d_out = nullptr;
+  CK(cudaMalloc(&d_out, sizeof(double) * n));
+  int e = sur_launch_eval(sur_dev(c->sur_cfg), c->d_sur_P.p, c->d_rec_rows.p, n, d_out,
+                          c->d_sur_err.p, 8 * sm_count(), c->st);
+  std::vector<double> des(n);
+  std::vector<float> y(n);
+  std::vector<int> sl(n);
+  cudaError_t ce = e ? (cudaError_t)e
+                     : cudaMemcpyAsync(des.data(), d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(y.data(), c->d_rec_y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->st);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(sl.data(), c->d_rec_slot.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->st);
+  cudaFree(d_out);
+  if (ce != cudaSuccess) return c->cuda_fail(ce, "surrogate calibration");
+  int rc = sur_err_check(c);
+  if (rc) return rc;
+  // per slot: kappa in {0, 1/16, ..., 1} maximising accepted moves per unit cost,
+  // a(kappa) / (r + p1(kappa)) with p1 the first-stage and a the two-stage
+  // acceptance estimated on the slot's records; kappa = 0 (no screening, cost 1)
+  // competes with the exact acceptance
+  std::vector<double> kap(R, 0.0);
+  for (int s2 = 0; s2 < R; ++s2) {
+    const double b = c->beta[s2];
+    double best = -1, bk = 0;
+    for (int q = 0; q <= 16; ++q) {
+      const double k = q / 16.0;
+      double a = 0, p1s = 0;
+      long cnt = 0;
+      for (int m = 0; m < n; ++m) {
+        if (sl[m] != s2) continue;
+        const double d = (double)y[m], ds = des[m];
+        const double p1 = std::min(1.0, std::exp(-k * b * ds));
+        const double p2 = std::min(1.0, std::exp(-b * (d - k * ds)));
+        a += p1 * p2;
+        p1s += p1;
+        ++cnt;
+      }
+      if (cnt == 0) break;
+      const double eff = q == 0 ? a / cnt : (a / cnt) / (r + p1s / cnt);
+      if (eff > best) {
+        best = eff;
+        bk = k;
+      }
+    }
+    kap[s2] = bk;
+  }
+  rc = set_kappa(kap);
+  if (rc) return rc;
+  c->sur_kappa = kap;
+  c->Q.da = da_before;
+  drop_graphs(c);
+  if (kappa_out)
+    for (int s2 = 0; s2 < R; ++s2) kappa_out[s2] = kap[s2];
   return PTMC_OK;
 }
 

@@ -332,6 +332,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
   }
   const int slot = Q.sow[g];
   const int gs = rd->wk + slot;
+  const float kap = Q.da ? Q.da_kappa[gs] : 0.f;
   const double beta = P.beta[gs];
   const double md = P.maxd[2 * gs];
   double en = P.en[g];
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
     // dE_s screens the proposal with its own draw; a rejection here costs no
     // exact evaluation
     double dEs = 0.0;
-    if (Q.da) {
+    if (kap > 0.f) {
       float r = -1.f;
       if (tid < SUR_ROWS) {
         const int j = tid & (SUR_ROWS / 2 - 1);
@@ -502,7 +503,9 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
       float v = warp_sum(r >= 0.f ? (tid < SUR_ROWS / 2 ? phi : -phi) : 0.f);
       if (lane == 0 && warp < SUR_ROWS / 32) ss.vec[100 + warp] = v;
       __syncthreads();
-      dEs = (double)((ss.vec[100] + ss.vec[101]) + (ss.vec[102] + ss.vec[103]));
+      // screening strength kappa: stage 1 on exp(-kappa beta dE_s), stage 2 on
+      // exp(-beta (dE - kappa dE_s)); exact for any fixed kappa
+      dEs = (double)(kap * ((ss.vec[100] + ss.vec[101]) + (ss.vec[102] + ss.vec[103])));
       int pass = 0;
       if (warp == 0) {
         double p1 = exp(-dEs * beta);
@@ -514,6 +517,8 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
         continue;
       }
       ++n_exact;
+    } else if (Q.da) {
+      ++n_exact;  // an unscreened slot: every move is evaluated exactly
     }
     Real new_en;
     if (hard) {
@@ -675,7 +680,10 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
           if (j < N && j != i) r = (float)(tid < SUR_ROWS / 2 ? rn[j] : ro[j]);
           Q.rec_rows[at * SUR_ROWS + tid] = r;
         }
-        if (tid == 0) Q.rec_y[at] = (float)((double)new_en - en);
+        if (tid == 0) {
+          Q.rec_y[at] = (float)((double)new_en - en);
+          Q.rec_slot[at] = slot;
+        }
       }
     }
     // ---- 6. Metropolis (src/MCRun.jl:122-132) and commit (swap_vars!, swap_config.jl:213-221);

@@ -33,10 +33,12 @@ struct NNParams {
   SurCfgDev sc;
   const float* surP;  // [SUR_NP] surrogate parameters
   long long* da_cnt;  // [walkers][2]: first-stage rejections, exact evaluations
+  const float* da_kappa;  // [slots] screening strength per temperature slot (0 = no screening)
   // training-record capture (exact moves only): move m of a walker in cycle c
   // is recorded when (c * N + m) % rec_every == 0, into a ring of rec_cap
   float* rec_rows;    // [rec_cap][128] distances (ptmc_surrogate.cuh row layout), NULL = off
   float* rec_y;       // [rec_cap] exact dE
+  int* rec_slot;      // [rec_cap] temperature slot (within its run) of the move
   unsigned long long* rec_n;  // records written so far
   int rec_cap, rec_every;
 };

@@ -156,7 +156,9 @@ def test_trained_surrogate_gain_and_exactness(pk):
     does not) and rejects a large share of proposals without an exact
     evaluation, at fewer exact evaluations per accepted move than the exact
     chain.  Exactness: per-temperature mean energies of the measured windows
-    agree within 5 combined standard errors (independent runs as samples)."""
+    (fixed screening strength 1, then the per-temperature strengths chosen by
+    ptmc_surrogate_calibrate) agree with the exact chain's within 5 combined
+    standard errors (independent runs as samples)."""
     pot = nn_potential(pk, out_scale=0.3)
     pot.boundary = 3.0
     runs, N, R = 24, 13, 8
@@ -191,6 +193,11 @@ def test_trained_surrogate_gain_and_exactness(pk):
     eng.surrogate_enable(True)
     e_da, acc_da = window(eng)
     _, _, st = eng.surrogate_state()
+    # per-temperature screening strength from the records, then a second window
+    kappa = eng.surrogate_calibrate(0.05)
+    assert kappa.shape == (R,) and np.all((kappa >= 0) & (kappa <= 1))
+    assert np.all(np.abs(kappa * 16 - np.round(kappa * 16)) < 1e-9)
+    e_cal, acc_cal = window(eng)
     eng.close()
 
     moves = 200 * N * R * runs
@@ -198,8 +205,10 @@ def test_trained_surrogate_gain_and_exactness(pk):
     assert st["stage1_rejects"] / moves > 0.15, st
     # exact evaluations per accepted move: every move for the exact chain
     assert st["exact_evals"] / acc_da < moves / acc_ref, (st, acc_da, acc_ref)
-    m_ref, m_da = e_ref.mean(axis=(0, 1)), e_da.mean(axis=(0, 1))
+    m_ref = e_ref.mean(axis=(0, 1))
     se_ref = e_ref.mean(axis=0).std(axis=0, ddof=1) / np.sqrt(runs)
-    se_da = e_da.mean(axis=0).std(axis=0, ddof=1) / np.sqrt(runs)
-    z = np.abs(m_ref - m_da) / np.sqrt(se_ref ** 2 + se_da ** 2)
-    assert np.all(z < 5), z
+    for e_x in (e_da, e_cal):
+        m_x = e_x.mean(axis=(0, 1))
+        se_x = e_x.mean(axis=0).std(axis=0, ddof=1) / np.sqrt(runs)
+        z = np.abs(m_ref - m_x) / np.sqrt(se_ref ** 2 + se_x ** 2)
+        assert np.all(z < 5), z
