@@ -54,6 +54,15 @@ struct PTMCOutput
     hist_params::NTuple{6,Cdouble}
 end
 
+# mirrors `struct ptmc_surrogate_cfg`
+struct PTMCSurrogateCfg
+    r_lo::Cdouble
+    r_hi::Cdouble
+    gamma::Cdouble
+    r_cut::Cdouble
+    escale::Cdouble
+end
+
 check(rc, ctx) = rc == 0 || error(unsafe_string(ccall((:ptmc_last_error, libptmc), Cstring, (Ptr{Cvoid},), ctx)))
 
 """
@@ -168,6 +177,30 @@ function multihistogram_NVT(ensemble, temp::TempGrid, results::Output, conv_thre
                results.en_min, results.en_max, conv_threshold, T, cv, it)
     rc == 0 || error(unsafe_string(ccall((:ptmc_last_error, libptmc), Cstring, (Ptr{Cvoid},), C_NULL)))
     return cv
+end
+
+"""
+    train_surrogate!(ctx; cycles=300, capacity=40000, steps=4000, batch=512, lr=2e-3)
+
+Delayed-acceptance set-up on an initialised NN context (no counterpart in the
+reference): capture `cycles` of exact moves, train the pair surrogate on the
+GPU, calibrate the per-temperature screening strength, enable screening.
+"""
+function train_surrogate!(ctx::Ptr{Cvoid}; cycles=300, capacity=40000, steps=4000, batch=512,
+                          lr=2e-3, cfg=PTMCSurrogateCfg(2.0, 12.0, 0.5625, 12.0, 0.0))
+    check(ccall((:ptmc_surrogate_set, libptmc), Cint,
+                (Ptr{Cvoid}, Ref{PTMCSurrogateCfg}, Ptr{Cfloat}, Cint, Cint),
+                ctx, cfg, C_NULL, capacity, 1), ctx)
+    check(ccall((:ptmc_surrogate_record, libptmc), Cint, (Ptr{Cvoid}, Cint), ctx, 1), ctx)
+    check(ccall((:ptmc_cycles_nosample, libptmc), Cint, (Ptr{Cvoid}, Clonglong), ctx, cycles), ctx)
+    check(ccall((:ptmc_surrogate_record, libptmc), Cint, (Ptr{Cvoid}, Cint), ctx, 0), ctx)
+    loss = Ref{Cdouble}(0)
+    check(ccall((:ptmc_surrogate_train, libptmc), Cint, (Ptr{Cvoid}, Cint, Cint, Cdouble, Ref{Cdouble}),
+                ctx, steps, batch, lr, loss), ctx)
+    check(ccall((:ptmc_surrogate_calibrate, libptmc), Cint, (Ptr{Cvoid}, Cdouble, Cint, Ptr{Cdouble}),
+                ctx, 0.0, 10, C_NULL), ctx)
+    check(ccall((:ptmc_surrogate_enable, libptmc), Cint, (Ptr{Cvoid}, Cint), ctx, 1), ctx)
+    return loss[]
 end
 
 end
