@@ -13,6 +13,18 @@
 // iteration inside one CTA (no host round trips, no spin-waits: the loop is
 // bounded by 1000 iterations and every barrier is a __syncthreads).
 //
+// Energy origin: the iteration first runs with the reference's arithmetic
+// (absolute energies).  The per-bin offset is set by the replica with the
+// largest -beta_i X - f_i, so with large |E| (Cu55 EAM: E ~ -9 Eh, beta up to
+// 1580 / Eh) the other replicas' terms exp(-(beta_j - beta_1) X) underflow to
+// zero in the first iteration, their f_j become -inf and every Cv is NaN (on
+// the CPU restatement as in the reference).  When the iteration ends with a
+// non-finite free energy, it is repeated with energies measured from en_min
+// (X = E - en_min (+ pV)); Cv/Cp are unchanged by a constant shift of the
+// energy (the free energies absorb -beta_i * shift), and |beta X| then stays
+// below beta * (en_max - en_min).  Cases the reference handles keep its exact
+// iteration.
+//
 // Scratch (caller-provided device memory, wham_work_doubles() doubles):
 //   f[R], nf[R], nc[R], num[B], w[B], off[B], red[2] where B = n_bin (NVT) or
 //   n_bin^2 (NPT).
@@ -77,9 +89,10 @@ __device__ double warp_qsum(const BinGeo& G, int B, double bt, const double* w,
 }
 
 __global__ void __launch_bounds__(WHAM_THREADS)
-    k_wham(BinGeo G, int R, const double* hist, const double* beta, double thr,
+    k_wham(BinGeo G0, int R, const double* hist, const double* beta, double thr,
            const double* tb_out, int n_out, double* work, double* out,
            int* iters) {
+  BinGeo G = G0;
   const int B = G.npt ? G.n_bin * G.n_bin : G.n_bin;
   double* f = work;
   double* nf = f + R;
@@ -87,42 +100,52 @@ __global__ void __launch_bounds__(WHAM_THREADS)
   double* num = nc + R;
   double* w = num + B;
   double* off = w + B;
-  __shared__ int s_stop;
+  __shared__ int s_stop, s_finite;
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
   const int nw = blockDim.x >> 5;
-  // free_energy_initialise (:37-57): f = 0, ncycles_i = sum of interior bins
-  for (int i = tid; i < R; i += blockDim.x) {
-    f[i] = 0.0;
-    double s = 0.0;
-    for (int m = 0; m < B; ++m) s = s + hist[G.hidx(i, m)];
-    nc[i] = s;
-  }
-  for (int m = tid; m < B; m += blockDim.x) {  // sum_i n_im, order i = 1..R
-    double q = 0.0;
-    for (int i = 0; i < R; ++i) q = q + hist[G.hidx(i, m)];
-    num[m] = q;
-  }
-  __syncthreads();
   int it = 0;
-  for (it = 1; it <= 1000; ++it) {
-    bin_pass(G, R, B, hist, beta, f, nc, num, w, off);
-    __syncthreads();
-    for (int i = wid; i < R; i += nw) {
-      double s = warp_qsum(G, B, beta[i], w, off, lane);
-      if (lane == 0) nf[i] = log(s);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if (attempt == 1) G.en_min = 0.0;  // energies measured from en_min
+    // free_energy_initialise (:37-57): f = 0, ncycles_i = sum of interior bins
+    for (int i = tid; i < R; i += blockDim.x) {
+      f[i] = 0.0;
+      double s = 0.0;
+      for (int m = 0; m < B; ++m) s = s + hist[G.hidx(i, m)];
+      nc[i] = s;
+    }
+    for (int m = tid; m < B; m += blockDim.x) {  // sum_i n_im, order i = 1..R
+      double q = 0.0;
+      for (int i = 0; i < R; ++i) q = q + hist[G.hidx(i, m)];
+      num[m] = q;
     }
     __syncthreads();
-    if (tid == 0) {
-      double delta = 0.0;
-      for (int i = 0; i < R; ++i) {
-        double d = fabs(nf[i] - f[i]);
-        delta = delta + d * d;
-        f[i] = nf[i];
+    for (it = 1; it <= 1000; ++it) {
+      bin_pass(G, R, B, hist, beta, f, nc, num, w, off);
+      __syncthreads();
+      for (int i = wid; i < R; i += nw) {
+        double s = warp_qsum(G, B, beta[i], w, off, lane);
+        if (lane == 0) nf[i] = log(s);
       }
-      s_stop = delta < thr;
+      __syncthreads();
+      if (tid == 0) {
+        double delta = 0.0;
+        for (int i = 0; i < R; ++i) {
+          double d = fabs(nf[i] - f[i]);
+          delta = delta + d * d;
+          f[i] = nf[i];
+        }
+        s_stop = delta < thr;
+      }
+      __syncthreads();
+      if (s_stop) break;
+    }
+    if (tid == 0) {
+      int ok = 1;
+      for (int i = 0; i < R; ++i) ok &= isfinite(f[i]) ? 1 : 0;
+      s_finite = ok;
     }
     __syncthreads();
-    if (s_stop) break;
+    if (s_finite) break;
   }
   // reweighting with the final free energies (:158-216)
   bin_pass(G, R, B, hist, beta, f, nc, num, w, off);

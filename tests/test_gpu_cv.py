@@ -1,0 +1,126 @@
+"""Cv(T) of the chosen forms against the plain FP64 form (GPU).
+
+For each workload, independent runs (separate Philox streams, batched in one
+context per form) go through the reference protocol: equilibration
+(eq_cycles/2 cycles, histogram range from the final energies), production with
+sampling, then the multihistogram reweighting (multihistogram_NVT on the GPU)
+gives Cv on the 10R-temperature grid of every run.  With sigma_T the
+run-to-run standard deviation of the plain FP64 form's Cv(T), the chosen
+form's mean curve must lie within 2 sigma_T of the FP64 mean at every
+temperature, and the two means must agree within 5 combined standard errors.
+
+  * Ne13 (ELJEven, the neon coefficients of examples/ne13.jl), FP32 move rows
+    + FP64 resync
+  * Cu55 (Sutton-Chen EAM of scripts/cu55.jl), FP32 move rows + FP64 resync;
+    both forms start from the same configurations, relaxed beforehand by the
+    FP32 form (the icosahedral start relaxes for longer than a short
+    equilibration, and the reference protocol fixes the histogram range at the
+    end of equilibration: energies that keep dropping land in the underflow
+    bin).  Cu55's energies (~ -9 Eh at beta up to 1580 / Eh) are where the
+    GPU multihistogram's energy origin at en_min matters: the reference's
+    formulation overflows there.
+  * NN13 (RuNNer potential, random FP32 weights), FP32 + delayed acceptance
+    with a GPU-trained surrogate and calibrated screening strength
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
+        -56234083.4334278, 288738837.441765]
+
+
+def run_form(pk, pot, starts, bc, R, T, eq, prod, precision, seed, da=None):
+    """starts: per run, one configuration or a list of R (one per replica)."""
+    n_runs = len(starts)
+    first = starts[0][0] if isinstance(starts[0], list) else starts[0]
+    N = len(first)
+    mp = pk.MCParams(mc_cycles=prod, eq_cycles=eq, mc_sample=1, n_traj=R, n_atoms=N)
+    temp = pk.TempGrid(T[0], T[1], R)
+    eng = pk.Engine(mp, temp, pot, pk.NVT(N), n_runs=n_runs, precision=precision,
+                    exch_prob=1.0, seed=seed, resync_every=1000)
+    for r, x in enumerate(starts):
+        cfg = [pk.Config(c, bc) for c in x] if isinstance(x, list) else pk.Config(x, bc)
+        eng.set_configs(r, cfg)
+    eng.init()
+    if da is not None:
+        da(eng)
+    eng.equilibrate()
+    eng.run_cycles(prod)
+    cv = np.array([pk.multihistogram_NVT(None, temp, eng.output(r), 1e-4) for r in range(n_runs)])
+    eng.close()
+    return cv
+
+
+def compare(cv_ref, cv_x, label):
+    assert np.all(np.isfinite(cv_ref)) and np.all(np.isfinite(cv_x)), label
+    n_ref, n_x = len(cv_ref), len(cv_x)
+    m_ref, m_x = cv_ref.mean(0), cv_x.mean(0)
+    sig = cv_ref.std(0, ddof=1)
+    se = np.sqrt(sig ** 2 / n_ref + cv_x.std(0, ddof=1) ** 2 / n_x)
+    dev = np.abs(m_x - m_ref)
+    print("%s: max |dCv|/sigma_fp64 = %.3f, max z = %.3f, peak Cv %.4g vs %.4g" % (
+        label, np.max(dev / sig), np.max(dev / se), m_x.max(), m_ref.max()))
+    assert np.all(dev <= 2 * sig), (label, np.max(dev / sig))
+    assert np.all(dev <= 5 * se), (label, np.max(dev / se))
+
+
+def test_cv_ne13_fp32_vs_fp64(pk):
+    import ptmc_gb300.starts as S
+    R = 16
+    starts = [S.sphere_start(13, 8.0, 4.5, 1234 + r) for r in range(16)]
+    args = (pk, pk.ELJPotentialEven(C_NE), starts, pk.SphericalBC(11.0), R, (4.0, 16.0), 4000, 20000)
+    compare(run_form(*args, "fp64", 11), run_form(*args, "fp32", 12), "Ne13 FP32+resync")
+
+
+def test_cv_cu55_eam_fp32_vs_fp64(pk):
+    d = json.load(open(os.path.join(GOLDEN, "nn_cu55.json")))
+    x0 = np.array(d["ico55_nm"]) * (d["cu_lattice_nm"] * d["nm_to_bohr"])
+    n_runs, R, T = 16, 32, (200.0, 1000.0)
+    pot = pk.EmbeddedAtomPotential(8.482, 4.692, 0.0367493 * 0.0370, 27.561, 0.25 * 18.8973)
+    bc = pk.SphericalBC(14.0)
+    # relax every replica of every run with the FP32 form first
+    mp = pk.MCParams(mc_cycles=1, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=55)
+    pre = pk.Engine(mp, pk.TempGrid(*T, R), pot, pk.NVT(55), n_runs=n_runs, precision="fp32",
+                    exch_prob=1.0, seed=20)
+    for r in range(n_runs):
+        pre.set_configs(r, pk.Config(x0, bc))
+    pre.init()
+    pre.cycles_nosample(4000)
+    starts = [list(pre.states(r)["xyz"]) for r in range(n_runs)]
+    pre.close()
+    args = (pk, pot, starts, bc, R, T, 400, 1500)
+    compare(run_form(*args, "fp64", 21), run_form(*args, "fp32", 22), "Cu55 EAM FP32+resync")
+
+
+def test_cv_nn13_delayed_acceptance_vs_fp64(pk):
+    import ptmc_gb300.starts as S
+    tables = json.load(open(os.path.join(GOLDEN, "nn_cu55.json")))
+    nodes = [88, 20, 20, 1]
+    pot = pk.RuNNerPotential(pk.RuNNerPotential.sf_table(tables, 12.0),
+                             pk.RuNNerPotential.random_weights(nodes, 3, 0.3), nodes, boundary=3.0)
+    starts = [S.sphere_start(13, 7.0, 4.0, 100 + r) for r in range(8)]
+
+    def pre(eng):  # the same cycles before equilibration as the screened form
+        eng.cycles_nosample(920)
+
+    def da(eng):
+        eng.cycles_nosample(600)
+        eng.surrogate_set(pk.PairSurrogate(2.0, 12.0, None, 12.0, 0.0), capacity=40000,
+                          record_every=2)
+        eng.surrogate_record(True)
+        eng.cycles_nosample(300)
+        eng.surrogate_record(False)
+        eng.surrogate_train(4000, batch=512, lr=2e-3)
+        eng.surrogate_calibrate(0.0, 10)
+        eng.surrogate_enable(True)
+
+    args = (pk, pot, starts, pk.SphericalBC(10.0), 8, (300.0, 900.0), 2000, 4000)
+    compare(run_form(*args, "fp64", 31, da=pre), run_form(*args, "fp32", 32, da=da),
+            "NN13 FP32+delayed acceptance")
