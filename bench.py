@@ -309,9 +309,20 @@ def gpu_arm(args, rank, world):
     else:
         for form in (["fp64", "fp32"] if not args.only_chosen else ["fp32"]):
             eng, sizes = make_engine(pk, W, B, form, args.cycles, seed, args.local_rank)
+            shapes = None
+            if form == "fp32" and not args.no_tune:
+                # launch shape per atom count (CTAs per run), untimed set-up; the
+                # autotuner restores the chain after its trials
+                t0 = time.perf_counter()
+                shapes = eng.autotune(trial_cycles=max(2, min(20, args.cycles // 4)),
+                                      cache=os.path.join(args.outdir, "autotune_r%d.json" % rank))
+                tune_s = time.perf_counter() - t0
             for _ in range(args.warmup):
                 eng.cycles_nosample(args.cycles)
             res[form] = timed(eng, form, sizes)
+            if shapes is not None:
+                res[form]["launch_shapes"] = {"ctas_per_run": {str(k): v for k, v in sorted(shapes.items())},
+                                              "autotune_s": round(tune_s, 3)}
             eng.close()
     # e2e through the public API with host buffers, one engine per step
     e2e = None
@@ -403,6 +414,7 @@ def main():
     ap.add_argument("--only-chosen", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep one CTA per run (no autotuning)")
     args = ap.parse_args()
     os.makedirs(args.outdir, exist_ok=True)
     rank = int(os.environ.get("RANK", "0"))
@@ -469,6 +481,7 @@ def main():
                                             else "_fp32resync_batched"), "runs_per_gpu": B,
                    "replicas": W["R"], "atoms": sorted(set(sizes)), "cycles_per_step": args.cycles,
                    "resync_every": W["resync"], "exchange": "every cycle",
+                   "launch_shapes": ch.get("launch_shapes"),
                    "l2": "flushed between steps (256 MB write)"},
         "plain_fp64": ({"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
                         "chosen_over_plain": ch["value"] / res["fp64"]["value"]}

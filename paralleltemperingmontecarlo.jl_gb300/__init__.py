@@ -410,6 +410,20 @@ class Engine:
     def resync(self):
         self._ck(self.L.ptmc_resync(self.h))
 
+    # ---- launch shapes (FP32 form)
+    def set_launch_shape(self, N, ctas_per_run):
+        """Spread each run with N atoms over a cluster of `ctas_per_run` CTAs."""
+        self._ck(self.L.ptmc_set_launch_shape(self.h, int(N), int(ctas_per_run)))
+
+    def autotune(self, trial_cycles=20, cache=None):
+        """Pick CTAs per run for every atom count by timed trials (the chain is
+        restored after each); returns {N: ctas_per_run}."""
+        out = np.zeros(self.n_runs, dtype=np.int32)
+        path = None if cache is None else os.fsencode(cache)
+        self._ck(self.L.ptmc_autotune(self.h, int(trial_cycles), path,
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return {int(self.N[r]): int(out[r]) for r in range(self.n_runs)}
+
     # ---- delayed acceptance with the learned pair surrogate (NN potential)
     def surrogate_set(self, surrogate, capacity=100000, record_every=1, params=None):
         """Attach a PairSurrogate (configuration and, unless `params` is given,

@@ -21,7 +21,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
+#include <sstream>
 #include <string>
 #include <sys/stat.h>
 #include <vector>
@@ -51,6 +53,7 @@ struct Group {
   int dev0;    // first device run index
   int nruns;
   cudaStream_t st = nullptr;
+  int ncta = 1;  // CTAs per run (thread-block cluster size; FP32 form), set by ptmc_autotune
 };
 
 template <typename T>
@@ -226,7 +229,7 @@ int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
     Group& G = c->groups[g];
     CK(cudaStreamWaitEvent(G.st, c->evfork, 0));
     int rc = launch_cycles(c->pot, c->bc(), c->p.ensemble, c->f32(), c->K, G.dev0,
-                           G.nruns, c->R(), G.N, ncyc, phase, G.st);
+                           G.nruns, c->R(), G.N, ncyc, phase, G.st, c->f32() ? G.ncta : 1);
     if (rc) return c->cuda_fail((cudaError_t)rc, "k_cycles launch");
     CK(cudaEventRecord(c->evjoin[g], G.st));
     CK(cudaStreamWaitEvent(c->st, c->evjoin[g], 0));
@@ -527,7 +530,7 @@ int ptmc_init(ptmc_ctx* c) {
   }
   for (auto& G : c->groups) {
     long long smem = nn ? 0
-                     : c->f32() ? cycles32_smem_bytes(c->pot, R, G.N)
+                     : c->f32() ? cycles32_smem_bytes(c->pot, R, G.N, 1)
                               : cycles_smem_bytes(c->pot, c->p.ensemble, false, R, G.N);
     if (smem > 227 * 1024)
       return c->fail(PTMC_ERR_LIMIT, "replica state of a run exceeds 227 KB of shared memory (R*N too large)");
@@ -623,6 +626,7 @@ int ptmc_init(ptmc_ctx* c) {
   K.hist = c->d_hist.p;
   K.K = (int)c->coeff.size();
   for (int k = 0; k < MAX_COEFF; ++k) K.c[k] = k < K.K ? c->coeff[k] : 0.0;
+  for (int k = 0; k < MAX_COEFF; ++k) K.cf[k] = (float)K.c[k];
   K.eam_n = c->eam[0];
   K.eam_m = c->eam[1];
   K.eam_ean = c->eam[2];
@@ -1646,3 +1650,208 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- autotuner
+// Launch shape per atom-count group: CTAs per run C (a thread-block cluster of
+// C CTAs on C SMs holds the R walkers of a run, R/C per CTA; FP32 form).
+// Coordinate descent on the whole batch's device time: starting from C = 1
+// everywhere, each group in turn (largest N first) tries every C in
+// {1, 2, 4, 8} (R % C == 0, shared memory permitting) with the other groups
+// fixed, and takes the best if it cuts the batch time of `trial_cycles`
+// cycles by more than 2 %; at most 3 passes.  Every trial
+// runs on a snapshot of the device state that is restored afterwards, so the
+// chain continues as if no trial had run.  Results are cached by key (device
+// name, potential, boundary, ensemble, R, the (N, runs) multiset) as JSON
+// lines {"key": "...", "ncta": {"N": C, ...}}.
+namespace {
+
+std::string tune_key(ptmc_ctx* c) {
+  cudaDeviceProp prop{};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaGetDeviceProperties(&prop, dev);
+  std::ostringstream k;
+  k << prop.name << "|sm" << prop.multiProcessorCount << "|pot" << c->pot << "|bc" << c->bc()
+    << "|ens" << c->p.ensemble << "|R" << c->R() << "|groups";
+  for (auto& G : c->groups) k << ":" << G.N << "x" << G.nruns;
+  return k.str();
+}
+
+bool tune_cache_read(const char* path, const std::string& key, std::map<int, int>& out) {
+  if (!path) return false;
+  std::ifstream f(path);
+  if (!f) return false;
+  std::string line, want = "{\"key\": \"" + key + "\"";
+  while (std::getline(f, line)) {
+    if (line.compare(0, want.size(), want) != 0) continue;
+    size_t at = line.find("\"ncta\": {");
+    if (at == std::string::npos) continue;
+    out.clear();
+    const char* p = line.c_str() + at + 9;
+    int n = 0, v = 0, used = 0;
+    while (std::sscanf(p, " \"%d\": %d%n", &n, &v, &used) == 2) {
+      out[n] = v;
+      p += used;
+      while (*p == ',' || *p == ' ') ++p;
+    }
+    return !out.empty();
+  }
+  return false;
+}
+
+void tune_cache_write(const char* path, const std::string& key, const std::map<int, int>& m) {
+  if (!path) return;
+  std::ofstream f(path, std::ios::app);
+  if (!f) return;
+  f << "{\"key\": \"" << key << "\", \"ncta\": {";
+  bool first = true;
+  for (auto& kv : m) {
+    f << (first ? "" : ", ") << "\"" << kv.first << "\": " << kv.second;
+    first = false;
+  }
+  f << "}}\n";
+}
+
+struct Snapshot {
+  std::vector<std::pair<void*, std::vector<unsigned char>>> bufs;  // device ptr, host copy
+};
+
+template <typename T>
+int snap_one(ptmc_ctx* c, Snapshot& s, DBuf<T>& d) {
+  if (!d.p || d.n == 0) return PTMC_OK;
+  std::vector<unsigned char> h(d.n * sizeof(T));
+  CK(cudaMemcpyAsync(h.data(), d.p, h.size(), cudaMemcpyDeviceToHost, c->st));
+  s.bufs.emplace_back((void*)d.p, std::move(h));
+  return PTMC_OK;
+}
+
+int snapshot(ptmc_ctx* c, Snapshot& s) {
+  int rc = 0;
+  rc |= snap_one(c, s, c->d_runs);
+  for (auto* b : {&c->d_pos, &c->d_mat, &c->d_comp, &c->d_en, &c->d_box, &c->d_rc2, &c->d_drift,
+                  &c->d_beta, &c->d_maxd, &c->d_maxbox, &c->d_ham})
+    rc |= snap_one(c, s, *b);
+  rc |= snap_one(c, s, c->d_ctr);
+  rc |= snap_one(c, s, c->d_status);
+  rc |= snap_one(c, s, c->d_wos);
+  rc |= snap_one(c, s, c->d_cnt);
+  rc |= snap_one(c, s, c->d_hist);
+  if (rc) return PTMC_ERR_CUDA;
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+int restore_snapshot(ptmc_ctx* c, const Snapshot& s) {
+  for (auto& b : s.bufs)
+    CK(cudaMemcpyAsync(b.first, b.second.data(), b.second.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+}  // namespace
+
+extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_path,
+                             int* ctas_per_run) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (trial_cycles < 1) return c->fail(PTMC_ERR_ARG, "trial_cycles must be >= 1");
+  const int R = c->R();
+  std::map<int, int> best;  // N -> C
+  for (auto& G : c->groups) best[G.N] = 1;
+  auto apply = [&](const std::map<int, int>& m) {
+    for (auto& G : c->groups) G.ncta = m.at(G.N);
+    drop_graphs(c);
+  };
+  if (c->f32() && c->pot != POT_NN) {
+    const std::string key = tune_key(c);
+    std::map<int, int> cached;
+    if (tune_cache_read(cache_path, key, cached) && cached.size() == best.size()) {
+      best = cached;
+    } else {
+      int optin = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      Snapshot snap;
+      int rc = snapshot(c, snap);
+      if (rc) return rc;
+      const ptmc_stats saved = c->stats;
+      auto trial = [&](const std::map<int, int>& m, double& ms) -> int {
+        apply(m);
+        int r = run_phase(c, 2, PHASE_PLAIN);  // warm-up (attributes, first launch)
+        if (!r) r = run_phase(c, trial_cycles, PHASE_PLAIN);
+        ms = c->stats.last_cycles_ms;
+        int r2 = restore_snapshot(c, snap);
+        return r ? r : r2;
+      };
+      double t_best = 0;
+      rc = trial(best, t_best);
+      if (rc) return rc;
+      std::vector<int> order;
+      for (auto& kv : best) order.push_back(kv.first);
+      std::sort(order.rbegin(), order.rend());  // largest N first
+      // coordinate descent: every candidate C of one group with the others
+      // fixed (the batch time is not monotonic in C: co-residency of the
+      // groups' CTAs on the SMs changes with the shape), at most 3 passes
+      for (int pass = 0; pass < 3; ++pass) {
+        bool improved = false;
+        for (int N : order) {
+          int pick = best[N];
+          double t_pick = t_best;
+          for (int cand_c : {1, 2, 4, 8}) {
+            if (cand_c == best[N] || R % cand_c != 0 || cand_c > R) continue;
+            if (cycles32_smem_bytes(c->pot, R, N, cand_c) > optin) continue;
+            std::map<int, int> cand = best;
+            cand[N] = cand_c;
+            double t = 0;
+            rc = trial(cand, t);
+            if (rc) {  // a shape the device cannot launch: skip it
+              apply(best);
+              cudaGetLastError();
+              continue;
+            }
+            if (t < 0.98 * t_pick) {
+              pick = cand_c;
+              t_pick = t;
+            }
+          }
+          if (pick != best[N]) {
+            best[N] = pick;
+            t_best = t_pick;
+            improved = true;
+          }
+        }
+        if (!improved) break;
+      }
+      c->stats = saved;
+      tune_cache_write(cache_path, key, best);
+    }
+  }
+  apply(best);
+  if (ctas_per_run)
+    for (int r = 0; r < c->p.n_runs; ++r) ctas_per_run[r] = best[c->runs[r].N];
+  return PTMC_OK;
+}
+
+extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (!c->f32() || c->pot == POT_NN)
+    return c->fail(PTMC_ERR_ARG, "launch shapes apply to the FP32 form of the pair/EAM potentials");
+  const int R = c->R();
+  if (ctas_per_run < 1 || ctas_per_run > 8 || R % ctas_per_run != 0)
+    return c->fail(PTMC_ERR_ARG, "ctas_per_run must divide the replica count and be <= 8");
+  int optin = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  bool found = false;
+  for (auto& G : c->groups) {
+    if (G.N != N) continue;
+    if (cycles32_smem_bytes(c->pot, R, N, ctas_per_run) > optin)
+      return c->fail(PTMC_ERR_LIMIT, "launch shape exceeds the shared memory of a CTA");
+    G.ncta = ctas_per_run;
+    found = true;
+  }
+  if (!found) return c->fail(PTMC_ERR_ARG, "no run with that atom count");
+  drop_graphs(c);
+  return PTMC_OK;
+}

@@ -24,6 +24,17 @@
 //  * NPT volume moves (rare: one slot in N+1) are evaluated with FP32 pair
 //    terms, Kahan-compensated per lane, FP64 across lanes and for the
 //    enthalpy, long-range correction and acceptance.
+//  * A run may be split over a thread-block cluster of C CTAs (C SMs): CTA
+//    rank q holds walkers q*R/C .. (q+1)*R/C - 1.  After the moves of a cycle
+//    every CTA gathers all walkers' energies, boxes and acceptance counts
+//    through distributed shared memory (cluster barrier, DSMEM reads, cluster
+//    barrier) and then runs the exchange, step adaptation and sampling on its
+//    own full copy of the slot tables; the inputs and the run-level draws are
+//    the same in every CTA, so the copies stay identical and rank 0 alone
+//    writes them back.  Walker arithmetic and draw streams do not depend on C:
+//    results are bit-identical for every C.  C is chosen per atom count by
+//    ptmc_autotune (C = 1: a plain CTA launch, no cluster barrier).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "ptmc_device.cuh"
@@ -49,6 +60,44 @@ __device__ __forceinline__ float v_all32(const float* c, int K, float r2) {
 template <int POT>
 __device__ __forceinline__ float v32(const float* c, int K, float r2) {
   return POT == POT_ELJ ? v_all32(c, K, r2) : v_even32(c, K, r2);
+}
+// Same polynomial with the coefficients read as kernel-parameter (constant
+// bank) operands and the Horner recurrence unrolled for the coefficient count
+// KK: no shared-memory loads and no loop overhead per pair term (a runtime-K
+// loop over shared-memory coefficients costs ~5 instructions per term).
+template <int KK>
+__device__ __forceinline__ float horner_p(const KParams& P, float x) {
+  float v = P.cf[KK - 1];
+#pragma unroll
+  for (int k = KK - 2; k >= 0; --k) v = fmaf(v, x, P.cf[k]);
+  return v;
+}
+template <int POT>
+__device__ __forceinline__ float v32p(const KParams& P, const float* c, int K, float r2) {
+  float x, s;
+  if (POT == POT_ELJ) {
+    const float ir = rsqrtf(r2);
+    const float inv = ir * ir;
+    x = ir;
+    s = inv * inv * inv;
+  } else {
+    const float inv = rcpf(r2);
+    x = inv;
+    s = inv * inv * inv;
+  }
+  float v;
+  switch (K) {  // uniform across the grid
+    case 4: v = horner_p<4>(P, x); break;
+    case 5: v = horner_p<5>(P, x); break;
+    case 6: v = horner_p<6>(P, x); break;
+    case 7: v = horner_p<7>(P, x); break;
+    case 8: v = horner_p<8>(P, x); break;
+    case 10: v = horner_p<10>(P, x); break;
+    default:
+      v = c[K - 1];
+      for (int k = K - 2; k >= 0; --k) v = fmaf(v, x, c[k]);
+  }
+  return v * s;
 }
 __device__ __forceinline__ double v_even64(const double* c, int K, double r2) {
   double inv = 1.0 / r2;
@@ -155,27 +204,35 @@ __device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, 
 
 }  // namespace
 
-// shared memory bytes of one run CTA (FP32 form)
-long long cycles32_smem_bytes(int pot, int R, int N) {
+// shared memory bytes of one run CTA (FP32 form) holding Rl = R / C walkers
+long long cycles32_smem_bytes(int pot, int R, int N, int C) {
   auto al = [](long long b) { return (b + 15) / 16 * 16; };
+  const long long Rl = R / C;
   long long b = 0;
-  b += al((long long)R * N * 16);  // float4 hi positions
-  b += al((long long)R * N * 16);  // float4 lo positions
-  if (pot == POT_EAM) b += 2 * al((long long)R * N * 8) + al((long long)R * N * 4);  // comps, deltas, sqrt(rho)
-  b += al((long long)R * 32 * 4);                         // draw words
+  b += al(Rl * N * 16);  // float4 hi positions
+  b += al(Rl * N * 16);  // float4 lo positions
+  if (pot == POT_EAM) b += 2 * al(Rl * N * 8) + al(Rl * N * 4);  // comps, deltas, sqrt(rho)
+  b += al(Rl * 32 * 4);                                          // draw words
   b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 4;
+  b += al((long long)R * 8);                                     // per-walker accepted counts
   return b;
 }
 
-template <int POT, int BC, int ENS>
+template <int POT, int BC, int ENS, bool SPLIT>
 __global__ void __launch_bounds__(1024)
-    k_cycles32(KParams P, int run0, int ncycles, int phase) {
+    k_cycles32(KParams P, int run0, int ncycles, int phase, int ncta) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
   __shared__ float s_cf[MAX_COEFF];
-  const RunDesc* rdp = P.runs + run0 + blockIdx.x;  // fields read on demand
+  namespace cg = cooperative_groups;
+  const int CL = SPLIT ? ncta : 1;          // CTAs of this run (cluster size)
+  const int q = SPLIT ? (int)cg::this_cluster().block_rank() : 0;
+  const int run_local = blockIdx.x / CL;
+  const RunDesc* rdp = P.runs + run0 + run_local;  // fields read on demand
   const int N = rdp->N, R = rdp->R;
-  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int Rl = R / CL;                    // walkers held by this CTA
+  const int tid = threadIdx.x, wl = tid >> 5, lane = tid & 31;
+  const int w = q * Rl + wl;                // walker index within the run
   const int nthr = blockDim.x;
   const int K = P.K;
   const int n_steps = ENS == ENS_NPT ? N + 1 : N;
@@ -186,17 +243,17 @@ __global__ void __launch_bounds__(1024)
     sp += (bytes + 15) / 16 * 16;
     return p;
   };
-  float4* s_xh = (float4*)carve((long long)R * N * 16);
-  float4* s_xl = (float4*)carve((long long)R * N * 16);
+  float4* s_xh = (float4*)carve((long long)Rl * N * 16);
+  float4* s_xl = (float4*)carve((long long)Rl * N * 16);
   float2* s_c32 = nullptr;
   float2* s_d32 = nullptr;
   float* s_sq = nullptr;
   if (POT == POT_EAM) {
-    s_c32 = (float2*)carve((long long)R * N * 8);
-    s_d32 = (float2*)carve((long long)R * N * 8);
-    s_sq = (float*)carve((long long)R * N * 4);
+    s_c32 = (float2*)carve((long long)Rl * N * 8);
+    s_d32 = (float2*)carve((long long)Rl * N * 8);
+    s_sq = (float*)carve((long long)Rl * N * 4);
   }
-  uint32_t* s_drw = (uint32_t*)carve((long long)R * 32 * 4);
+  uint32_t* s_drw = (uint32_t*)carve((long long)Rl * 32 * 4);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_maxbox = (double*)carve((long long)R * 8);
   double* s_en = (double*)carve((long long)R * 8);
@@ -208,13 +265,14 @@ __global__ void __launch_bounds__(1024)
   int* s_sow = (int*)carve((long long)R * 4);
   float* s_bl2e = (float*)carve((long long)R * 4);  // beta * log2(e) per slot
   float* s_mdf = (float*)carve((long long)R * 4);   // atom step size per slot
+  int2* s_acc = (int2*)carve((long long)R * 8);     // this cycle's accepted atom/volume moves per walker
 
   if (tid < K) {
     s_c[tid] = P.c[tid];
     s_cf[tid] = (float)P.c[tid];
   }
-  const double* gpos = P.pos + rdp->pos_off;
-  for (int k = tid; k < R * N; k += nthr) {
+  const double* gpos = P.pos + rdp->pos_off + (size_t)q * Rl * N * 3;
+  for (int k = tid; k < Rl * N; k += nthr) {
     double x = gpos[3 * k], y = gpos[3 * k + 1], z = gpos[3 * k + 2];
     float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
     s_xh[k] = h;
@@ -222,8 +280,8 @@ __global__ void __launch_bounds__(1024)
                           (float)(z - (double)h.z), 0.f);
   }
   if (POT == POT_EAM) {
-    const double* gc = P.comp + rdp->comp_off;
-    for (int k = tid; k < R * N; k += nthr) {
+    const double* gc = P.comp + rdp->comp_off + (size_t)q * Rl * N * 2;
+    for (int k = tid; k < Rl * N; k += nthr) {
       s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
       s_sq[k] = (float)sqrt(gc[2 * k + 1]);
     }
@@ -254,10 +312,10 @@ __global__ void __launch_bounds__(1024)
   unsigned long long base = ctr + 32;
   int status = P.status[g];
   double drift = P.drift[g];
-  float4* Xh = s_xh + (size_t)w * N;
-  float4* Xl = s_xl + (size_t)w * N;
-  float* SQ = s_sq ? s_sq + (size_t)w * N : nullptr;
-  uint32_t* drw = s_drw + w * 32;
+  float4* Xh = s_xh + (size_t)wl * N;
+  float4* Xl = s_xl + (size_t)wl * N;
+  float* SQ = s_sq ? s_sq + (size_t)wl * N : nullptr;
+  uint32_t* drw = s_drw + wl * 32;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const float hnf = P.f_hn, hmf = P.f_hm, eanf = P.f_ean, ecamf = P.f_ecam;
   const uint32_t run_word = (uint32_t)rdp->run_id;
@@ -343,8 +401,8 @@ __global__ void __launch_bounds__(1024)
     const float4 x4 = h0;
     float de = 0.f, saf = 0.f, sbf = 0.f;
     if (POT == POT_EAM) {
-      const float2* C = s_c32 + (size_t)w * N;
-      float2* D = s_d32 + (size_t)w * N;
+      const float2* C = s_c32 + (size_t)wl * N;
+      float2* D = s_d32 + (size_t)wl * N;
       for (int j = lane; j < N; j += 32) {
         if (j == i) continue;
         float4 b = Xh[j];
@@ -371,10 +429,10 @@ __global__ void __launch_bounds__(1024)
         float dn = pf2<BC>(tf, b, Lf, iLf);
         float dol = pf2<BC>(x4, b, Lf, iLf);
         if (ENS == ENS_NPT) {
-          if (dn <= rcf) de += v32<POT>(s_cf, K, dn);
-          if (dol <= rcf) de -= v32<POT>(s_cf, K, dol);
+          if (dn <= rcf) de += v32p<POT>(P, s_cf, K, dn);
+          if (dol <= rcf) de -= v32p<POT>(P, s_cf, K, dol);
         } else {
-          de += v32<POT>(s_cf, K, dn) - v32<POT>(s_cf, K, dol);
+          de += v32p<POT>(P, s_cf, K, dn) - v32p<POT>(P, s_cf, K, dol);
         }
       }
       de = warp_sum(de);
@@ -387,8 +445,8 @@ __global__ void __launch_bounds__(1024)
       Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
     }
     if (POT == POT_EAM) {
-      float2* C = s_c32 + (size_t)w * N;
-      const float2* D = s_d32 + (size_t)w * N;
+      float2* C = s_c32 + (size_t)wl * N;
+      const float2* D = s_d32 + (size_t)wl * N;
       for (int k = lane; k < N; k += 32) {
         float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
         float2 c = C[k];
@@ -476,7 +534,7 @@ __global__ void __launch_bounds__(1024)
       en += (double)de_acc;
       if (P.resync_every > 0 && idx % P.resync_every == 0) {
         double e64 = energy64<POT, BC, ENS>(Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean,
-                                            P.eam_ecam, POT == POT_EAM ? s_c32 + (size_t)w * N : nullptr,
+                                            P.eam_ecam, POT == POT_EAM ? s_c32 + (size_t)wl * N : nullptr,
                                             SQ, lane);
         drift = fmax(drift, fabs(en - e64));
         en = e64;
@@ -486,10 +544,30 @@ __global__ void __launch_bounds__(1024)
     if (lane == 0) {
       s_en[w] = en;
       s_box[w] = L;
-      s_cnt[6 * slot + 0] += acc_a;
-      s_cnt[6 * slot + 1] += acc_a;
-      s_cnt[6 * slot + 2] += acc_v;
-      s_cnt[6 * slot + 3] += acc_v;
+      s_acc[w] = make_int2((int)acc_a, (int)acc_v);
+    }
+    if constexpr (SPLIT) {  // gather the other CTAs' walkers through distributed shared memory
+      cg::cluster_group cl = cg::this_cluster();
+      cl.sync();
+      for (int v = tid; v < R; v += nthr) {
+        const int owner = v / Rl;
+        if (owner != q) {
+          s_en[v] = *cl.map_shared_rank(s_en + v, owner);
+          s_box[v] = *cl.map_shared_rank(s_box + v, owner);
+          s_acc[v] = *cl.map_shared_rank(s_acc + v, owner);
+        }
+      }
+      cl.sync();  // every remote read is done before any CTA writes its next results
+    } else {
+      __syncthreads();
+    }
+    for (int v = tid; v < R; v += nthr) {  // counters of the slot each walker occupied
+      const int sl = s_sow[v];
+      const int2 a = s_acc[v];
+      s_cnt[6 * sl + 0] += a.x;
+      s_cnt[6 * sl + 1] += a.x;
+      s_cnt[6 * sl + 2] += a.y;
+      s_cnt[6 * sl + 3] += a.y;
     }
     __syncthreads();
     if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
@@ -551,28 +629,28 @@ __global__ void __launch_bounds__(1024)
           s_ham[2 * s + 1] += H * H;
           int ie = hidx(floor((e - rdp->en_min) / rdp->dE) + 1);
           int iv = hidx(floor((V - rdp->v_min) / rdp->dV) + 1);
-          atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
+          if (q == 0) atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
         } else {
           s_ham[2 * s] += e;
           s_ham[2 * s + 1] += e * e;
           int ie = hidx((e - rdp->en_min) / rdp->dE + 1);
-          atomicAdd(hrow + (ie - 1), 1u);
+          if (q == 0) atomicAdd(hrow + (ie - 1), 1u);
         }
       }
     }
     __syncthreads();
   }
 
-  double* gpos_w = P.pos + rdp->pos_off;
-  for (int k = tid; k < R * N; k += nthr) {
+  double* gpos_w = P.pos + rdp->pos_off + (size_t)q * Rl * N * 3;
+  for (int k = tid; k < Rl * N; k += nthr) {
     float4 h = s_xh[k], l = s_xl[k];
     gpos_w[3 * k] = (double)h.x + (double)l.x;
     gpos_w[3 * k + 1] = (double)h.y + (double)l.y;
     gpos_w[3 * k + 2] = (double)h.z + (double)l.z;
   }
   if (POT == POT_EAM) {
-    double* gc = P.comp + rdp->comp_off;
-    for (int k = tid; k < R * N; k += nthr) {
+    double* gc = P.comp + rdp->comp_off + (size_t)q * Rl * N * 2;
+    for (int k = tid; k < Rl * N; k += nthr) {
       gc[2 * k] = s_c32[k].x;
       gc[2 * k + 1] = s_c32[k].y;
     }
@@ -585,7 +663,7 @@ __global__ void __launch_bounds__(1024)
     P.status[g] = status;
     P.drift[g] = drift;
   }
-  for (int s = tid; s < R; s += nthr) {
+  for (int s = tid; s < R && q == 0; s += nthr) {  // slot tables: identical in every CTA
     int gs = wk0 + s;
     P.ham[2 * gs] = s_ham[2 * s];
     P.ham[2 * gs + 1] = s_ham[2 * s + 1];
@@ -595,39 +673,60 @@ __global__ void __launch_bounds__(1024)
     P.wos[gs] = s_wos[s];
   }
   __syncthreads();  // every thread has read the run descriptor
-  if (tid == 0) {
-    P.runs[run0 + blockIdx.x].cyc[phase] = first + ncycles;
-    P.runs[run0 + blockIdx.x].run_ctr = run_ctr;
+  if (tid == 0 && q == 0) {
+    P.runs[run0 + run_local].cyc[phase] = first + ncycles;
+    P.runs[run0 + run_local].run_ctr = run_ctr;
   }
 }
 
 template <int POT, int BC, int ENS>
 static int launch32(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
-                    int phase, cudaStream_t st) {
-  long long smem = cycles32_smem_bytes(POT, R, maxN);
+                    int phase, int ncta, cudaStream_t st) {
+  if (ncta < 1 || ncta > 8 || R % ncta != 0) return (int)cudaErrorInvalidValue;
+  long long smem = cycles32_smem_bytes(POT, R, maxN, ncta);
   static long long attr_set = 48 * 1024;
   if (smem > attr_set) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles32<POT, BC, ENS>);
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles32<POT, BC, ENS, false>);
     if (e != cudaSuccess) return (int)e;
     if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
-    e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+    e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     attr_set = smem;
   }
-  k_cycles32<POT, BC, ENS><<<nruns, R * 32, (size_t)smem, st>>>(P, run0, ncycles, phase);
+  if (ncta == 1) {
+    k_cycles32<POT, BC, ENS, false><<<nruns, R * 32, (size_t)smem, st>>>(P, run0, ncycles, phase, 1);
+    return (int)cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nruns * ncta), 1, 1);
+  cfg.blockDim = dim3((unsigned)(R / ncta * 32), 1, 1);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)ncta;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_cycles32<POT, BC, ENS, true>, P, run0, ncycles, phase, ncta);
+  if (e != cudaSuccess) return (int)e;
   return (int)cudaGetLastError();
 }
 
 int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,
-                    int maxN, int ncycles, int phase, void* stream) {
+                    int maxN, int ncycles, int phase, int ncta, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
 #define PT32(PO, B, E) \
-  if (pot == PO && bc == B && ens == E) return launch32<PO, B, E>(P, run0, nruns, R, maxN, ncycles, phase, st);
+  if (pot == PO && bc == B && ens == E) return launch32<PO, B, E>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st);
   PT32(POT_ELJ, BC_SPH, ENS_NVT)
   PT32(POT_ELJEVEN, BC_SPH, ENS_NVT)
   PT32(POT_EAM, BC_SPH, ENS_NVT)

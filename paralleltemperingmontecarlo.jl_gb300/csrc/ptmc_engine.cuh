@@ -76,6 +76,7 @@ struct KParams {
   // register pressure the compiler rematerialises constants from their source
   // expression, and an FP64 -> FP32 conversion issues to the FP64 pipe.
   float f_hn, f_hm, f_ean, f_ecam;  // -n/2, -m/2, ean, eCam
+  float cf[MAX_COEFF];              // ELJ coefficients in FP32 (constant-bank operands)
 };
 
 // shared-memory bytes of one run CTA
@@ -101,12 +102,13 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
 
 // kernel launch entry points (ptmc_cycles.cu, ptmc_cycles32.cu)
 namespace ptmc {
-long long cycles32_smem_bytes(int pot, int R, int N);
+long long cycles32_smem_bytes(int pot, int R, int N, int ncta);
+// ncta: CTAs per run (a thread-block cluster when > 1; FP32 form only)
 int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,
-                    int maxN, int ncycles, int phase, void* stream);
+                    int maxN, int ncycles, int phase, int ncta, void* stream);
 int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
                   int run0, int nruns, int R, int maxN, int ncycles, int phase,
-                  void* stream);
+                  void* stream, int ncta = 1);
 int launch_init(int pot, int bc, int ens, bool f32, const KParams& P,
                 int run0, int nruns, int R, void* stream);
 int launch_resync(int pot, int bc, int ens, bool f32, const KParams& P,

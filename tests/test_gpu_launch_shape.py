@@ -1,0 +1,131 @@
+"""Launch shapes of the FP32 form: a run spread over a thread-block cluster of
+C CTAs (walkers split across SMs, exchange/adaptation/sampling on the gathered
+walkers via distributed shared memory) must give bit-identical results for
+every C, and the autotuner must leave the chain where it found it.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
+        -56234083.4334278, 288738837.441765]
+
+
+def engine(pk, pot, ens, starts, bc, R, T, seed):
+    N = len(starts[0])
+    mp = pk.MCParams(mc_cycles=200, eq_cycles=100, mc_sample=1, n_traj=R, n_atoms=N)
+    eng = pk.Engine(mp, pk.TempGrid(T[0], T[1], R), pot, ens, n_runs=len(starts),
+                    precision="fp32", exch_prob=1.0, seed=seed, resync_every=40)
+    for r, x in enumerate(starts):
+        eng.set_configs(r, pk.Config(x, bc))
+    eng.init()
+    return eng
+
+
+def snapshot(eng):
+    out = []
+    for r in range(eng.n_runs):
+        st = eng.states(r)
+        o = eng.output(r)
+        out.append((st["xyz"], st["en_tot"], st["box"], st["counts"], st["ham"], st["max_displ"],
+                    o.en_histogram, o.ev_histogram))
+    return out
+
+
+def assert_identical(a, b):
+    for ra, rb in zip(a, b):
+        for x, y in zip(ra, rb):
+            assert np.array_equal(x, y)
+
+
+def protocol(eng):
+    eng.equilibrate()
+    eng.run_cycles(120)
+    return snapshot(eng)
+
+
+@pytest.mark.parametrize("ctas", [2, 4, 8])
+def test_cluster_split_ne13_bit_identical(pk, ctas):
+    import ptmc_gb300.starts as S
+    starts = [S.sphere_start(13, 8.0, 4.5, 40 + r) for r in range(3)]
+    args = (pk, pk.ELJPotentialEven(C_NE), pk.NVT(13), starts, pk.SphericalBC(11.0), 16, (4.0, 16.0), 5)
+    ref = engine(*args)
+    a = protocol(ref)
+    ref.close()
+    eng = engine(*args)
+    eng.set_launch_shape(13, ctas)
+    b = protocol(eng)
+    eng.close()
+    assert_identical(a, b)
+    assert a[0][3][:, 0].sum() > 0
+
+
+def test_cluster_split_eam_and_npt_bit_identical(pk):
+    d = json.load(open(os.path.join(GOLDEN, "nn_cu55.json")))
+    x0 = np.array(d["ico55_nm"]) * (d["cu_lattice_nm"] * d["nm_to_bohr"])
+    eam = pk.EmbeddedAtomPotential(8.482, 4.692, 0.0367493 * 0.0370, 27.561, 0.25 * 18.8973)
+    args = (pk, eam, pk.NVT(55), [x0, x0], pk.SphericalBC(14.0), 8, (200.0, 1000.0), 6)
+    ref = engine(*args)
+    a = protocol(ref)
+    ref.close()
+    eng = engine(*args)
+    eng.set_launch_shape(55, 4)
+    b = protocol(eng)
+    eng.close()
+    assert_identical(a, b)
+    import ptmc_gb300.starts as S
+    x = S.fcc_box(2, 8.4, 0.05, 3)
+    n = len(x)
+    nargs = (pk, pk.ELJPotentialEven(C_NE), pk.NPT(n, 101325 * 3.398928944382626e-14), [x, x],
+             pk.CubicBC(16.8), 8, (10.0, 40.0), 7)
+    ref = engine(*nargs)
+    a = protocol(ref)
+    ref.close()
+    eng = engine(*nargs)
+    eng.set_launch_shape(n, 2)
+    b = protocol(eng)
+    eng.close()
+    assert_identical(a, b)
+    assert a[0][3][:, 2].sum() > 0  # volume moves accepted
+
+
+def test_autotune_uneven_batch_restores_chain(pk, tmp_path):
+    """Autotuning an uneven batch picks a valid shape per atom count, caches it,
+    and does not advance the chain: the tuned run equals an untuned one."""
+    import ptmc_gb300.starts as S
+    sizes = [13, 38, 55, 101, 147] * 2
+    starts = [S.sphere_start(n, 0.9 * n ** (1 / 3) * 3, 4.3, 500 + k) for k, n in enumerate(sizes)]
+
+    def make(seed):
+        mp = pk.MCParams(mc_cycles=100, eq_cycles=0, mc_sample=1, n_traj=16, n_atoms=13)
+        eng = pk.Engine(mp, pk.TempGrid(4.0, 16.0, 16), pk.ELJPotentialEven(C_NE), pk.NVT(13),
+                        n_runs=len(sizes), precision="fp32", exch_prob=1.0, seed=seed)
+        for r, (n, x) in enumerate(zip(sizes, starts)):
+            eng.set_configs(r, pk.Config(x, pk.SphericalBC(0.9 * n ** (1 / 3) * 3 + 3.0)))
+        eng.init()
+        return eng
+
+    cache = str(tmp_path / "tune.json")
+    eng = make(9)
+    shapes = eng.autotune(trial_cycles=5, cache=cache)
+    assert set(shapes) == set(sizes)
+    assert all(c in (1, 2, 4, 8) for c in shapes.values())
+    eng.cycles_nosample(30)
+    a = snapshot(eng)
+    eng.close()
+    ref = make(9)
+    ref.cycles_nosample(30)
+    b = snapshot(ref)
+    ref.close()
+    assert_identical(a, b)
+    # a cache hit gives the same shapes without trials
+    eng = make(9)
+    assert eng.autotune(trial_cycles=5, cache=cache) == shapes
+    eng.close()
+    assert len(open(cache).read().strip().split("\n")) == 1
