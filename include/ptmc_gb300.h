@@ -234,12 +234,14 @@ int ptmc_surrogate_get(ptmc_ctx* c, float* params, ptmc_surrogate_cfg* cfg,
  * min(1, exp(-beta_s (dE - kappa_s dE_s))) >= u2 (exact for any fixed kappa);
  * kappa_s = 0 skips the surrogate for that slot (no first-stage draw).  The
  * default after ptmc_surrogate_set is 1.  This call picks kappa_s in
- * {0, 1/16, ..., 1} per slot to maximise accepted moves per unit cost,
- * a(kappa)/(r + p1(kappa)), estimated on the slot's captured records (exact dE
- * and the surrogate's dE_s), where r is the cost of a surrogate stage relative
- * to an exact evaluation: cost_ratio if > 0, else measured by timing
- * timing_cycles plain cycles without and with screening (these cycles advance
- * the chain, without sampling).  kappa_out [R] (may be NULL) receives the
+ * {0, 1/16, ..., 1} per slot to maximise accepted moves per unit time: the sum
+ * over slots of the two-stage acceptance a_s(kappa_s) divided by the summed
+ * cost per move, r + p1_s(kappa_s) (1 for kappa_s = 0; the walker CTAs share
+ * the SMs, so a cycle's time follows the total cost); a and p1 are estimated on the slot's captured
+ * records (exact dE and the surrogate's dE_s), r is the cost of a surrogate
+ * stage relative to an exact evaluation: cost_ratio if > 0, else measured by
+ * timing timing_cycles plain cycles without, with and again without screening
+ * (these cycles advance the chain, without sampling).  kappa_out [R] (may be NULL) receives the
  * choice.  The delayed-acceptance on/off state is left as it was. */
 int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles,
                              double* kappa_out);

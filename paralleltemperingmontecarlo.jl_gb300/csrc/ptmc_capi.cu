@@ -677,6 +677,10 @@ int ptmc_init(ptmc_ctx* c) {
     Q.sow = c->d_nn_sow.p;
     if (nn_smem_bytes(Q, Nmax, !c->f32()) > 227 * 1024)
       return c->fail(PTMC_ERR_LIMIT, "NN walker state exceeds 227 KB of shared memory");
+    if (c->f32() && (S > 32 || Q.H1 > 32 || Q.H2 > 32))
+      return c->fail(PTMC_ERR_LIMIT,
+                     "FP32 NN form: at most 32 active symmetry functions and 32 units per hidden "
+                     "layer (one tensor-core tile)");
     int e = nn_launch_init(K, Q, W, Nmax, !c->f32(), s);
     if (e) return c->cuda_fail((cudaError_t)e, "k_nn_init launch");
     c->stats.kernel_launches += 1;
@@ -1571,7 +1575,7 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
     drop_graphs(c);
     rc = run_phase(c, timing_cycles, PHASE_PLAIN);
     if (rc) return rc;
-    const double t_ex = c->stats.last_cycles_ms;
+    double t_ex = c->stats.last_cycles_ms;
     std::vector<long long> k0(2 * (size_t)W), k1(2 * (size_t)W);
     CK(cudaMemcpyAsync(k0.data(), c->d_da_cnt.p, sizeof(long long) * k0.size(), cudaMemcpyDeviceToHost, c->st));
     c->Q.da = 1;
@@ -1581,6 +1585,11 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
     const double t_da = c->stats.last_cycles_ms;
     CK(cudaMemcpyAsync(k1.data(), c->d_da_cnt.p, sizeof(long long) * k1.size(), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    c->Q.da = 0;  // a second exact segment after the screened one (the chain drifts)
+    drop_graphs(c);
+    rc = run_phase(c, timing_cycles, PHASE_PLAIN);
+    if (rc) return rc;
+    t_ex = 0.5 * (t_ex + c->stats.last_cycles_ms);
     double rej = 0, ex = 0;
     for (int g = 0; g < W; ++g) {
       rej += (double)(k1[2 * (size_t)g] - k0[2 * (size_t)g]);
@@ -1609,15 +1618,20 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
   if (ce != cudaSuccess) return c->cuda_fail(ce, "surrogate calibration");
   int rc = sur_err_check(c);
   if (rc) return rc;
-  // per slot: kappa in {0, 1/16, ..., 1} maximising accepted moves per unit cost,
-  // a(kappa) / (r + p1(kappa)) with p1 the first-stage and a the two-stage
-  // acceptance estimated on the slot's records; kappa = 0 (no screening, cost 1)
-  // competes with the exact acceptance
-  std::vector<double> kap(R, 0.0);
+  // Per slot and kappa in {0, 1/16, ..., 1}: the two-stage acceptance a and the
+  // cost per move c (r + p1 with p1 the first-stage acceptance; 1 for kappa = 0,
+  // no screening), estimated on the slot's records.  The walker CTAs share the
+  // SMs and the cycle kernel is throughput-bound, so a cycle's time follows the
+  // summed cost of all walkers (measured: uniform kappa = 1 ran in r + mean p1
+  // of the exact time).  Objective: accepted moves per unit time,
+  // sum_s a_s / sum_s c_s, maximised over the per-slot choices by Dinkelbach's
+  // iteration (each step maximises sum_s (a_s - lambda c_s) slot by slot, then
+  // lambda = sum a / sum c).
+  constexpr int NK = 17;
+  std::vector<double> A((size_t)R * NK, -1.0), Cc((size_t)R * NK, 0.0);
   for (int s2 = 0; s2 < R; ++s2) {
     const double b = c->beta[s2];
-    double best = -1, bk = 0;
-    for (int q = 0; q <= 16; ++q) {
+    for (int q = 0; q < NK; ++q) {
       const double k = q / 16.0;
       double a = 0, p1s = 0;
       long cnt = 0;
@@ -1630,15 +1644,43 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
         p1s += p1;
         ++cnt;
       }
-      if (cnt == 0) break;
-      const double eff = q == 0 ? a / cnt : (a / cnt) / (r + p1s / cnt);
-      if (eff > best) {
-        best = eff;
-        bk = k;
+      if (cnt == 0) break;  // no records for this slot: it keeps kappa = 1
+      A[(size_t)s2 * NK + q] = a / cnt;
+      Cc[(size_t)s2 * NK + q] = q == 0 ? 1.0 : r + p1s / cnt;
+    }
+  }
+  std::vector<double> kap(R, 1.0);
+  std::vector<int> pick(R, NK - 1);
+  auto totals = [&](double& sa, double& sc) {
+    sa = sc = 0;
+    for (int s2 = 0; s2 < R; ++s2) {
+      if (A[(size_t)s2 * NK] < 0) continue;
+      sa += A[(size_t)s2 * NK + pick[s2]];
+      sc += Cc[(size_t)s2 * NK + pick[s2]];
+    }
+  };
+  double sa = 0, sc = 0;
+  totals(sa, sc);
+  double lambda = sc > 0 ? sa / sc : 0;
+  for (int it = 0; it < 50; ++it) {
+    for (int s2 = 0; s2 < R; ++s2) {
+      if (A[(size_t)s2 * NK] < 0) continue;
+      double bv = -1e300;
+      for (int q = 0; q < NK; ++q) {
+        const double v = A[(size_t)s2 * NK + q] - lambda * Cc[(size_t)s2 * NK + q];
+        if (v > bv + 1e-15) {
+          bv = v;
+          pick[s2] = q;
+        }
       }
     }
-    kap[s2] = bk;
+    totals(sa, sc);
+    const double nl = sc > 0 ? sa / sc : 0;
+    if (std::fabs(nl - lambda) <= 1e-12 * std::max(1.0, nl)) break;
+    lambda = nl;
   }
+  for (int s2 = 0; s2 < R; ++s2)
+    if (A[(size_t)s2 * NK] >= 0) kap[s2] = pick[s2] / 16.0;
   rc = set_kappa(kap);
   if (rc) return rc;
   c->sur_kappa = kap;

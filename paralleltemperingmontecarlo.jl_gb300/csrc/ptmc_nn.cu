@@ -232,6 +232,214 @@ __device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X,
   __syncthreads();
 }
 
+// ---------------------------------------------------------------- tensor-core MLP
+// FP32 form: the per-atom MLP (ForwardPass.jl:23-84) of all N <= 64 atoms as
+// two tcgen05 GEMMs, rows = atoms (M = 128, rows >= N zero), K = 32 (active
+// symmetry functions, then the first hidden layer, zero-padded), N = 32
+// (hidden units, zero-padded).  Operands are split into TF32 hi + lo parts
+// (hi = x with the low 13 mantissa bits cleared, lo = x - hi) and each product
+// is hi*hi + hi*lo + lo*hi (3xTF32, ~1e-6 relative like an FP32 GEMM); accumulators in 32 TMEM columns, read back by warps 0-1 (one
+// atom per thread), tanh and the output layer on the CUDA cores.  The FP64
+// form keeps the CUDA-core MLP.
+constexpr uint32_t MLP_LBO = 128, MLP_SBO = 1024;  // K = 32 TF32: 8 core matrices per row group
+constexpr size_t MLP_TC_BYTES = 2 * 16384 + 4 * 4096 + 512 + 16;
+
+struct MlpSmem {
+  unsigned char *Ah, *Al;              // 128 x 32 TF32 inputs (hi, lo)
+  unsigned char *B1h, *B1l, *B2h, *B2l;  // W1^T, W2^T: 32 x 32 TF32 (hi, lo)
+  float* vec;                          // b1[32], b2[32], w3[32], b3
+  unsigned long long* mbar;
+  uint32_t* tslot;
+};
+
+__device__ __forceinline__ void mlp_carve(MlpSmem& m, unsigned char* base) {
+  m.Ah = base;
+  m.Al = base + 16384;
+  m.B1h = base + 32768;
+  m.B1l = base + 36864;
+  m.B2h = base + 40960;
+  m.B2l = base + 45056;
+  m.vec = (float*)(base + 49152);
+  m.mbar = (unsigned long long*)(base + 49152 + 512);
+  m.tslot = (uint32_t*)(base + 49152 + 520);
+}
+
+// W: gathered parameters W1[S][H1], b1, W2[H1][H2], b2, w3[H2], b3
+__device__ void mlp_stage(const MlpSmem& m, const float* W, int S, int H1, int H2) {
+  const float* W2 = W + S * H1 + H1;
+  for (int e = threadIdx.x; e < 2 * 16384 / 4; e += blockDim.x) ((float*)m.Ah)[e] = 0.f;
+  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+    const int n = e / 32, k = e % 32;
+    const float x1 = (k < S && n < H1) ? W[k * H1 + n] : 0.f;
+    const float x2 = (k < H1 && n < H2) ? W2[k * H2 + n] : 0.f;
+    const uint32_t o = umma_off32(n, k, MLP_LBO, MLP_SBO);
+    const float h1 = tf32_hi(x1), h2 = tf32_hi(x2);
+    *(float*)(m.B1h + o) = h1;
+    *(float*)(m.B1l + o) = x1 - h1;
+    *(float*)(m.B2h + o) = h2;
+    *(float*)(m.B2l + o) = x2 - h2;
+  }
+  for (int n = threadIdx.x; n < 32; n += blockDim.x) {
+    m.vec[n] = n < H1 ? W[S * H1 + n] : 0.f;
+    m.vec[32 + n] = n < H2 ? W2[H1 * H2 + n] : 0.f;
+    m.vec[64 + n] = n < H2 ? W2[H1 * H2 + H2 + n] : 0.f;
+  }
+  if (threadIdx.x == 0) {
+    m.vec[96] = W2[H1 * H2 + 2 * H2];
+    mbar_init(smem_u32(m.mbar), 1);
+  }
+  fence_async_smem();
+}
+
+// three TF32 products per K = 8 step: hi*hi, hi*lo, lo*hi
+__device__ __forceinline__ void mlp_issue(uint32_t tbase, const unsigned char* Ah,
+                                          const unsigned char* Al, const unsigned char* Bh,
+                                          const unsigned char* Bl) {
+  const uint32_t id = umma_idesc_tf32(128, 32);
+  const uint32_t ah = smem_u32(Ah), al = smem_u32(Al), bh = smem_u32(Bh), bl = smem_u32(Bl);
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    const uint32_t o = 2u * MLP_LBO * ks;
+    umma_tf32(tbase, umma_sdesc(ah + o, MLP_LBO, MLP_SBO), umma_sdesc(bh + o, MLP_LBO, MLP_SBO), id,
+              ks > 0);
+    umma_tf32(tbase, umma_sdesc(ah + o, MLP_LBO, MLP_SBO), umma_sdesc(bl + o, MLP_LBO, MLP_SBO), id, 1);
+    umma_tf32(tbase, umma_sdesc(al + o, MLP_LBO, MLP_SBO), umma_sdesc(bh + o, MLP_LBO, MLP_SBO), id, 1);
+  }
+}
+
+// E = sum_a MLP(G[:, a] (+ dG[:, a])); every thread calls it.  `ph` is the
+// mbarrier parity (flipped twice); *bad is set (uniformly) when a
+// tensor-core wait ran out.
+__device__ float mlp_energy_tc(const NNSmem<float>& s, const MlpSmem& m, int N, int S, int H1,
+                               int H2, bool with_delta, uint32_t tbase, uint32_t& ph, int* bad) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t mb = smem_u32(m.mbar);
+  for (int t = tid; t < 32 * N; t += blockDim.x) {  // inputs, columns S..31 zero
+    const int q = t / N, a = t % N;
+    float x = 0.f;
+    if (q < S) {
+      x = s.G[q * N + a];
+      if (with_delta) x += s.dG[q * N + a];
+    }
+    const uint32_t o = umma_off32(a, q, MLP_LBO, MLP_SBO);
+    const float h = tf32_hi(x);
+    *(float*)(m.Ah + o) = h;
+    *(float*)(m.Al + o) = x - h;
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0) {
+    tc_fence_after();
+    mlp_issue(tbase, m.Ah, m.Al, m.B1h, m.B1l);
+    umma_commit(mb);
+  }
+  int b = 0;
+  float acc[16];
+  if (warp < 2) {
+    if (!mbar_wait(mb, ph)) b = 1;
+    tc_fence_after();
+    const int a = tid;
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {  // 16 columns at a time (register pressure)
+      tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 16u * half, acc);
+      if (a < N) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {  // first hidden layer -> second GEMM's input (hi, lo)
+          const int n = 16 * half + c;
+          const float h = n < H1 ? tanhf(acc[c] + m.vec[n]) : 0.f;
+          const uint32_t o = umma_off32(a, n, MLP_LBO, MLP_SBO);
+          const float hh = tf32_hi(h);
+          *(float*)(m.Ah + o) = hh;
+          *(float*)(m.Al + o) = h - hh;
+        }
+      }
+    }
+  }
+  ph ^= 1u;
+  fence_async_smem();
+  tc_fence_before();
+  if (__syncthreads_or(b)) {
+    *bad = 1;
+    return 0.f;
+  }
+  if (tid == 0) {
+    tc_fence_after();
+    mlp_issue(tbase, m.Ah, m.Al, m.B2h, m.B2l);
+    umma_commit(mb);
+  }
+  float e = 0.f;
+  if (warp < 2) {
+    if (!mbar_wait(mb, ph)) b = 1;
+    tc_fence_after();
+    const int a = tid;
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 16u * half, acc);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int n = 16 * half + c;
+        if (a < N && n < H2) e += m.vec[64 + n] * tanhf(acc[c] + m.vec[32 + n]);
+      }
+    }
+    if (a < N) e += m.vec[96];
+  }
+  ph ^= 1u;
+  tc_fence_before();
+  if (__syncthreads_or(b)) {
+    *bad = 1;
+    return 0.f;
+  }
+  return block_sum(e, s.red);
+}
+
+// tensor-core state of a walker CTA: MLP tiles (FP32 form), surrogate tiles
+// (delayed acceptance), one 32-column TMEM allocation shared by both (they are
+// used one after the other within a move)
+template <typename Real>
+struct TcState {
+  MlpSmem m{};
+  SurSmem ss{};
+  uint32_t tbase = 0, mph = 0, sph = 0;
+  bool on = false;
+};
+
+template <typename Real>
+__device__ void tc_setup(TcState<Real>& t, unsigned char* smem_raw, size_t off, const NNParams& Q,
+                         const NNSmem<Real>& s, bool want_sur) {
+  const uint32_t a = smem_u32(smem_raw) + (uint32_t)off;
+  off += (128u - (a & 127u)) & 127u;
+  uint32_t* slot = nullptr;
+  if constexpr (sizeof(Real) == 4) {
+    mlp_carve(t.m, smem_raw + off);
+    off += MLP_TC_BYTES;
+    mlp_stage(t.m, s.W, Q.S, Q.H1, Q.H2);
+    slot = t.m.tslot;
+  }
+  if (want_sur) {
+    sur_carve(t.ss, smem_raw + off);
+    sur_stage(t.ss, Q.surP);
+    if (!slot) slot = t.ss.tslot;
+  }
+  t.on = slot != nullptr;
+  if (t.on) {
+    if ((threadIdx.x >> 5) == 0) tmem_alloc(smem_u32(slot), 32);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    t.tbase = *slot;
+  }
+}
+
+template <typename Real>
+__device__ void tc_teardown(const TcState<Real>& t) {
+  if (!t.on) return;
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if ((threadIdx.x >> 5) == 0) tmem_dealloc(t.tbase, 32);
+}
+
 }  // namespace
 
 // --------------------------------------------------------------- init kernel
@@ -245,9 +453,11 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
   const RunDesc* rd = P.runs + run;
   const int N = rd->N, w = gw - rd->wk;
   NNSmem<Real> s;
-  nn_carve(s, smem_raw, N, Q.S, Q.SA, Q.H1, Q.H2, Q.nW);
+  const size_t nn_off = nn_carve(s, smem_raw, N, Q.S, Q.SA, Q.H1, Q.H2, Q.nW);
   const double* X = P.pos + rd->pos_off + (size_t)w * N * 3;
   load_walker(Q, s, X, nullptr, N);
+  TcState<Real> tc;
+  tc_setup(tc, smem_raw, nn_off, Q, s, false);
   const int S = Q.S, SR = Q.SR;
   for (int t = threadIdx.x; t < S * N; t += blockDim.x) s.G[t] = 0;
   __syncthreads();
@@ -288,19 +498,26 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
     s.G[q * N + a] = g + (Real)f.goffset;
   }
   __syncthreads();
-  Real e = mlp_energy<Real>(Q, s, N, false);
+  Real e;
+  int bad = 0;
+  if constexpr (sizeof(Real) == 4)
+    e = mlp_energy_tc(s, tc.m, N, S, Q.H1, Q.H2, false, tc.tbase, tc.mph, &bad);
+  else
+    e = mlp_energy<Real>(Q, s, N, false);
   double* Gg = Q.G + (size_t)gw * S * Q.Nmax;
   for (int t = threadIdx.x; t < S * N; t += blockDim.x) Gg[t] = (double)s.G[t];
   if (threadIdx.x == 0) {
     P.en[rd->wk + w] = (double)e;
-    P.status[rd->wk + w] = ST_OK;
+    P.status[rd->wk + w] = bad ? ST_TIMEOUT : ST_OK;
     P.drift[rd->wk + w] = 0.0;
   }
+  tc_teardown(tc);
 }
 
 // --------------------------------------------------------------- cycle kernel
 template <typename Real>
-__global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, int phase) {
+__global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
+    k_nn_cycle(KParams P, NNParams Q, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int gw = blockIdx.x;
   const int run = Q.run_of_walker[gw];
@@ -309,27 +526,18 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int S = Q.S, SR = Q.SR, SA = Q.SA;
   NNSmem<Real> s;
-  nn_carve(s, smem_raw, N, S, SA, Q.H1, Q.H2, Q.nW);
+  const size_t nn_off = nn_carve(s, smem_raw, N, S, SA, Q.H1, Q.H2, Q.nW);
   double* Xg = P.pos + rd->pos_off + (size_t)w * N * 3;
   double* Gg = Q.G + (size_t)gw * S * Q.Nmax;
   load_walker(Q, s, Xg, Gg, N);
   if (P.status[g] != ST_OK) return;
-  // delayed acceptance: surrogate tiles after the walker state, 128-byte aligned
-  SurSmem ss{};
-  uint32_t tbase = 0, mphase = 0;
+  // tensor-core tiles after the walker state: MLP (FP32 form), surrogate (delayed acceptance)
+  TcState<Real> tc;
+  tc_setup(tc, smem_raw, nn_off, Q, s, Q.da != 0);
+  const SurSmem& ss = tc.ss;
+  const uint32_t tbase = tc.tbase;
+  uint32_t& mphase = tc.sph;
   long long n_rej1 = 0, n_exact = 0;
-  if (Q.da) {
-    size_t off = nn_carve(s, smem_raw, N, S, SA, Q.H1, Q.H2, Q.nW);
-    uint32_t a = smem_u32(smem_raw) + (uint32_t)off;
-    off += (128u - (a & 127u)) & 127u;
-    sur_carve(ss, smem_raw + off);
-    sur_stage(ss, Q.surP);
-    if (warp == 0) tmem_alloc(smem_u32(ss.tslot), SUR_TMEM_COLS);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    tbase = *ss.tslot;
-  }
   const int slot = Q.sow[g];
   const int gs = rd->wk + slot;
   const float kap = Q.da ? Q.da_kappa[gs] : 0.f;
@@ -496,7 +704,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
         if (j < N && j != i) r = (float)(tid < SUR_ROWS / 2 ? rn[j] : ro[j]);
       }
       float phi = 0.f;
-      if (!sur_tile_forward(ss, Q.sc, tbase, mphase, r, phi, nullptr, nullptr)) {
+      if (!sur_tile_forward<true>(ss, Q.sc, tbase, mphase, r, phi, nullptr, nullptr)) {
         status = ST_TIMEOUT;
         break;
       }
@@ -665,7 +873,16 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
       for (int q = tid; q < S; q += blockDim.x) s.dG[q * N + i] = s.dGi[q];
       __syncthreads();
       // ---- 5. MLP on every atom (calc_new_runner_energy!, src/EnergyEvaluation.jl:1269-1275)
-      new_en = mlp_energy<Real>(Q, s, N, true);
+      if constexpr (sizeof(Real) == 4) {
+        int bad = 0;
+        new_en = mlp_energy_tc(s, tc.m, N, S, Q.H1, Q.H2, true, tbase, tc.mph, &bad);
+        if (bad) {
+          status = ST_TIMEOUT;
+          break;
+        }
+      } else {
+        new_en = mlp_energy<Real>(Q, s, N, true);
+      }
     }
     // ---- training record of this exact move (proposal rows and exact dE)
     if (Q.rec_rows && !hard) {
@@ -734,12 +951,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_cycle(KParams P, NNParams Q, 
     }
   }
   if (warp == 0 && lane == 0) P.ctr[g] = ctr;
-  if (Q.da) {  // free the tensor memory (every path out of the move loop comes here)
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (warp == 0) tmem_dealloc(tbase, SUR_TMEM_COLS);
-  }
+  tc_teardown(tc);  // free the tensor memory (every path out of the move loop comes here)
 }
 
 // --------------------------------------------------------------- run epilogue
@@ -806,7 +1018,9 @@ size_t nn_smem_bytes(const NNParams& Q, int N, bool f64) {
   b += al(es * Q.nW) + al(es * N * Q.H1) + al(es * N * Q.H2) + al(es * 64) + al(es * (Q.S > 0 ? Q.S : 1));
   b += al(es * 4 * MAX_NN_ANG);
   b += al(8 * DRAW_BUF) + al(8 * 4) + al(4 * 4);
-  if (Q.da) b += 128 + SUR_SMEM_BYTES;  // 128-byte alignment slack + tiles
+  b += 128;                                 // alignment of the tensor-core tiles
+  if (!f64) b += MLP_TC_BYTES;              // FP32 form: tensor-core MLP tiles
+  if (Q.da) b += SUR_SMEM_BYTES;            // surrogate tiles
   return b;
 }
 

@@ -94,23 +94,41 @@ __device__ __forceinline__ void sur_stage(const SurSmem& s, const float* __restr
   fence_async_smem();
 }
 
-// 16 features of one distance (r < 0: no pair -> zeros)
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+template <bool FAST>
+__device__ __forceinline__ float sur_tanh(float x) {
+  return FAST ? tanh_fast(x) : tanhf(x);
+}
+
+// 16 features of one distance (r < 0: no pair -> zeros).  FAST uses the MUFU
+// approximations (first stage of a move); training and evaluation use the
+// accurate functions the oracle restates.
+template <bool FAST>
 __device__ __forceinline__ void sur_features(const SurCfgDev& c, float r, float (&g)[SUR_F]) {
   float fc = 0.f;
-  if (r >= 0.f && r < c.r_cut) fc = 0.5f * (cosf(3.14159265358979f * (r / c.r_cut)) + 1.f);
+  if (r >= 0.f && r < c.r_cut)
+    fc = 0.5f * ((FAST ? __cosf(3.14159265358979f * (r / c.r_cut))
+                       : cosf(3.14159265358979f * (r / c.r_cut))) + 1.f);
 #pragma unroll
   for (int k = 0; k < SUR_F; ++k) {
     float d = r - (c.r_lo + (float)k * c.dmu);
-    g[k] = fc * expf(-c.gamma * (d * d));
+    g[k] = fc * (FAST ? __expf(-c.gamma * (d * d)) : expf(-c.gamma * (d * d)));
   }
 }
 
 // Forward pass of one 128-row tile, called by every thread of the CTA
-// (blockDim >= 128).  Threads 0..127 pass their row's distance in `r` and get
+// (blockDim >= 128).  FAST: MUFU tanh/exp/cos (the first stage of a move: any
+// deterministic pair function keeps dE_s an exact difference of a state
+// function, so the chain stays exact); otherwise the accurate functions.  Threads 0..127 pass their row's distance in `r` and get
 // phi back (garbage for rows with r < 0, which the caller masks); with
 // `keep` they also get h1 (FP32, before BF16 rounding) and h2.  `phase` is the
 // mbarrier parity, flipped twice per call.  Returns false (every thread) if a
 // tensor-core completion wait ran out; the caller must then stop issuing.
+template <bool FAST = false>
 __device__ __forceinline__ bool sur_tile_forward(const SurSmem& s, const SurCfgDev& c,
                                                  uint32_t tbase, uint32_t& phase, float r,
                                                  float& phi, float* h1keep, float* h2keep) {
@@ -120,7 +138,7 @@ __device__ __forceinline__ bool sur_tile_forward(const SurSmem& s, const SurCfgD
   const uint32_t lane_addr = tbase + ((uint32_t)(32 * (tid >> 5)) << 16);
   if (tid < SUR_ROWS) {
     float g[SUR_F];
-    sur_features(c, r, g);
+    sur_features<FAST>(c, r, g);
 #pragma unroll
     for (int k = 0; k < SUR_F; k += 2) {
       __nv_bfloat162 v = __floats2bfloat162_rn(g[k], g[k + 1]);
@@ -144,7 +162,7 @@ __device__ __forceinline__ bool sur_tile_forward(const SurSmem& s, const SurCfgD
     tmem_ld32(lane_addr, acc);
 #pragma unroll
     for (int n = 0; n < SUR_H; n += 2) {
-      float a = tanhf(acc[n] + s.vec[n]), b = tanhf(acc[n + 1] + s.vec[n + 1]);
+      float a = sur_tanh<FAST>(acc[n] + s.vec[n]), b = sur_tanh<FAST>(acc[n + 1] + s.vec[n + 1]);
       if (h1keep) {
         h1keep[n] = a;
         h1keep[n + 1] = b;
@@ -173,7 +191,7 @@ __device__ __forceinline__ bool sur_tile_forward(const SurSmem& s, const SurCfgD
     float e = 0.f;
 #pragma unroll
     for (int n = 0; n < SUR_H; ++n) {
-      float h = tanhf(acc[n] + s.vec[SUR_H + n]);
+      float h = sur_tanh<FAST>(acc[n] + s.vec[SUR_H + n]);
       if (h2keep) h2keep[n] = h;
       e += s.vec[2 * SUR_H + n] * h;
     }

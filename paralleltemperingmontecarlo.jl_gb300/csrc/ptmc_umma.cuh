@@ -52,6 +52,39 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
          ((uint32_t)(M >> 4) << 24);
 }
 
+// byte offset of element (row, k) of a no-swizzle K-major operand with 4-byte
+// elements (TF32): a core matrix row holds 4 elements
+__host__ __device__ __forceinline__ uint32_t umma_off32(int row, int k, uint32_t lbo, uint32_t sbo) {
+  return (uint32_t)(row >> 3) * sbo + (uint32_t)(k >> 2) * lbo + (uint32_t)(row & 7) * 16u +
+         (uint32_t)(k & 3) * 4u;
+}
+
+// instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A TF32 (bits
+// 7-9 = 2), B TF32 (bits 10-12 = 2), both K-major, dense, N >> 3 at bit 17,
+// M >> 4 at bit 24; one MMA covers K = 8
+__host__ __device__ constexpr uint32_t umma_idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// TF32 part of an FP32 value by truncation (the tensor core reads only the top
+// 19 bits of a TF32 operand): one integer AND instead of a conversion, which on
+// this GPU would issue to the FP64 pipe.  For the 3xTF32 split, hi = tf32_hi(x)
+// and lo = x - hi is exact in FP32; the tensor core truncates lo in turn.
+__device__ __forceinline__ float tf32_hi(float x) {
+  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+
+// D (+)= A * B with TF32 operands, issued by one thread
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // D (+)= A * B, issued by one thread
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                           uint32_t idesc, uint32_t accumulate) {
@@ -112,6 +145,22 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     if (ok) return true;
   }
   return false;
+}
+
+// 32 TMEM lanes x 16 consecutive FP32 columns -> 16 registers per thread
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
 // 32 TMEM lanes x 32 consecutive FP32 columns -> 32 registers per thread
