@@ -64,7 +64,11 @@ def workload(name):
     if name == "cu55":
         return dict(name="cu55_eam", R=32, T=(200.0, 1000.0), pot="eam", ens="nvt",
                     bc=("sphere", 14.0), sizes=lambda B: [55] * B,
-                    start=lambda n, k: cu55_ico(), resync=1000, flops_pair=17, mufu_pair=3)
+                    start=lambda n, k: cu55_ico(), resync=1000, flops_pair=17, mufu_pair=3,
+                    # DRAM bytes (read + write) of one k_cycles32 launch per run: ncu capture
+                    # of a 16-run launch, 1.30 MB (profiles/k_cycles32_cu55_eam.md); the
+                    # state moved per launch grows with the runs
+                    dram_bytes_per_run=1.30e6 / 16)
     if name == "ne13":
         return dict(name="ne13_eljeven", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
                     bc=("sphere", 11.0), sizes=lambda B: [13] * B,
@@ -492,7 +496,8 @@ def main():
         "delayed_acceptance": ch.get("da"),
         "fp32_max_drift_eh": ch["drift"],
         "roofline": {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
-                     "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"], "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"],
+                     "traffic": (W["dram_bytes_per_run"] * B if W.get("dram_bytes_per_run") else None),
                      "peak_source": "measured in-situ by ptmc_measure_peaks (FFMA chains)",
                      "ops_per_pair": W["flops_pair"], "mufu_per_pair": W["mufu_pair"],
                      "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"]},
