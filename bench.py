@@ -239,6 +239,8 @@ def gpu_arm(args, rank, world):
     torch.cuda.set_device(dev)
     L = pk._capi.load()
     W = workload(args.workload)
+    if args.atoms > 0 and args.workload == "batched":
+        W["sizes"] = lambda B, n=args.atoms: [n] * B
     B = args.runs or default_runs(args.workload, torch.cuda.get_device_properties(dev).multi_processor_count)
     # measured in-situ peaks (FMA/MUFU-bound kernels)
     f32, f64, mufu = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
@@ -420,12 +422,16 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep one CTA per run (no autotuning)")
+    ap.add_argument("--atoms", type=int, default=0,
+                    help="batched workload: every run with this atom count (profiling one group)")
     args = ap.parse_args()
     os.makedirs(args.outdir, exist_ok=True)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     args.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     W = workload(args.workload)
+    if args.atoms > 0 and args.workload == "batched":
+        W["sizes"] = lambda B, n=args.atoms: [n] * B
     if args.cycles <= 0:
         args.cycles = W.get("cycles", 200)
     cores = os.cpu_count() or 1
