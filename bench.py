@@ -328,8 +328,10 @@ def gpu_arm(args, rank, world):
                 eng.cycles_nosample(args.cycles)
             res[form] = timed(eng, form, sizes)
             if shapes is not None:
-                res[form]["launch_shapes"] = {"ctas_per_run": {str(k): v for k, v in sorted(shapes.items())},
-                                              "autotune_s": round(tune_s, 3)}
+                res[form]["launch_shapes"] = {
+                    "ctas_per_run": {str(k): v[0] for k, v in sorted(shapes.items())},
+                    "lanes_per_walker": {str(k): v[1] for k, v in sorted(shapes.items())},
+                    "autotune_s": round(tune_s, 3)}
             eng.close()
     # e2e through the public API with host buffers, one engine per step
     e2e = None

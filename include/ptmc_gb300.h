@@ -273,23 +273,26 @@ int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist,
 
 /* --- launch shapes (no counterpart in the reference: the reference runs one
  *     replica per Julia task) ---
- * FP32 form of the pair and EAM potentials: the R walkers of a run may be
+ * FP32 form of the pair and EAM potentials.  C: the R walkers of a run may be
  * spread over a thread-block cluster of C CTAs (C SMs, R/C walkers each); the
  * replica exchange, step adaptation and sampling then read the other CTAs'
- * walkers through distributed shared memory.  Results are bit-identical for
- * every C; only the speed changes.  Default C = 1. */
-/* Set C for the runs with N atoms (C <= 8, R % C == 0). */
-int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run);
-/* Pick C per atom count by timing `trial_cycles` plain cycles of the whole
- * batch for candidate shapes (coordinate descent over C in {1, 2, 4, 8} per
- * atom count, largest N first) on a snapshot of the
- * device state that is restored after every trial, so the chain is not
- * advanced.  cache_path (may be NULL): JSON-lines file of earlier choices,
- * keyed by device, potential, boundary, ensemble, R and the (N, runs) mix; a
- * hit skips the trials, a miss appends the result.  ctas_per_run [n_runs]
- * (may be NULL) receives the choice per run.  Other forms keep C = 1. */
+ * walkers through distributed shared memory; results are bit-identical for
+ * every C.  L: lanes per walker, 32 (one warp per walker) or 16 (two walkers
+ * per warp, for small N); the pair sums then add in another order (FP32
+ * rounding), the chains stay statistically equivalent.  Default C = 1, L = 32. */
+/* Set (C, L) for the runs with N atoms (C <= 8, R % C == 0, L in {32, 16},
+ * (R / C) % (32 / L) == 0). */
+int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run, int lanes_per_walker);
+/* Pick (C, L) per atom count by timing `trial_cycles` plain cycles of the whole
+ * batch for candidate shapes (coordinate descent over C in {1, 2, 4, 8} x L
+ * in {32, 16} per atom count, largest N first) on a snapshot of the device
+ * state that is restored after every trial, so the chain is not advanced.
+ * cache_path (may be NULL): JSON-lines file of earlier choices, keyed by
+ * device, potential, boundary, ensemble, R and the (N, runs) mix; a hit skips
+ * the trials, a miss appends the result.  shape_out [2 n_runs] (may be NULL)
+ * receives (C, L) per run.  Other forms keep C = 1, L = 32. */
 int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_path,
-                  int* ctas_per_run);
+                  int* shape_out);
 
 /* Engine utility, no counterpart in the reference: measured FP32 FMA, FP64
  * FMA (TFLOP/s) and MUFU ex2 (Tops/s) peaks of `device`, the roofline

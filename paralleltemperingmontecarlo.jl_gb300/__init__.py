@@ -411,18 +411,20 @@ class Engine:
         self._ck(self.L.ptmc_resync(self.h))
 
     # ---- launch shapes (FP32 form)
-    def set_launch_shape(self, N, ctas_per_run):
-        """Spread each run with N atoms over a cluster of `ctas_per_run` CTAs."""
-        self._ck(self.L.ptmc_set_launch_shape(self.h, int(N), int(ctas_per_run)))
+    def set_launch_shape(self, N, ctas_per_run, lanes_per_walker=32):
+        """Runs with N atoms: spread over a cluster of `ctas_per_run` CTAs, with
+        `lanes_per_walker` lanes (32, or 16 = two walkers per warp) per walker."""
+        self._ck(self.L.ptmc_set_launch_shape(self.h, int(N), int(ctas_per_run),
+                                              int(lanes_per_walker)))
 
     def autotune(self, trial_cycles=20, cache=None):
-        """Pick CTAs per run for every atom count by timed trials (the chain is
-        restored after each); returns {N: ctas_per_run}."""
-        out = np.zeros(self.n_runs, dtype=np.int32)
+        """Pick (CTAs per run, lanes per walker) for every atom count by timed
+        trials (the chain is restored after each); returns {N: (C, L)}."""
+        out = np.zeros(2 * self.n_runs, dtype=np.int32)
         path = None if cache is None else os.fsencode(cache)
         self._ck(self.L.ptmc_autotune(self.h, int(trial_cycles), path,
                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
-        return {int(self.N[r]): int(out[r]) for r in range(self.n_runs)}
+        return {int(self.N[r]): (int(out[2 * r]), int(out[2 * r + 1])) for r in range(self.n_runs)}
 
     # ---- delayed acceptance with the learned pair surrogate (NN potential)
     def surrogate_set(self, surrogate, capacity=100000, record_every=1, params=None):

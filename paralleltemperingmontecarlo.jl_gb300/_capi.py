@@ -104,7 +104,8 @@ SIGNATURES = {
     "ptmc_surrogate_records": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int, _ip]),
     "ptmc_surrogate_calibrate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                                 _dp]),
-    "ptmc_set_launch_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "ptmc_set_launch_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int]),
     "ptmc_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, _ip]),
     "ptmc_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "ptmc_destroy": (None, [ctypes.c_void_p]),

@@ -54,6 +54,7 @@ struct Group {
   int nruns;
   cudaStream_t st = nullptr;
   int ncta = 1;  // CTAs per run (thread-block cluster size; FP32 form), set by ptmc_autotune
+  int lpr = 32;  // lanes per walker (32 or 16; FP32 form)
 };
 
 template <typename T>
@@ -229,7 +230,8 @@ int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
     Group& G = c->groups[g];
     CK(cudaStreamWaitEvent(G.st, c->evfork, 0));
     int rc = launch_cycles(c->pot, c->bc(), c->p.ensemble, c->f32(), c->K, G.dev0,
-                           G.nruns, c->R(), G.N, ncyc, phase, G.st, c->f32() ? G.ncta : 1);
+                           G.nruns, c->R(), G.N, ncyc, phase, G.st, c->f32() ? G.ncta : 1,
+                           c->f32() ? G.lpr : 32);
     if (rc) return c->cuda_fail((cudaError_t)rc, "k_cycles launch");
     CK(cudaEventRecord(c->evjoin[g], G.st));
     CK(cudaStreamWaitEvent(c->st, c->evjoin[g], 0));
@@ -1695,16 +1697,17 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
 
 // ---------------------------------------------------------------- autotuner
 // Launch shape per atom-count group: CTAs per run C (a thread-block cluster of
-// C CTAs on C SMs holds the R walkers of a run, R/C per CTA; FP32 form).
+// C CTAs on C SMs holds the R walkers of a run, R/C per CTA) and lanes per
+// walker L (32, or 16 with two walkers per warp); FP32 form.
 // Coordinate descent on the whole batch's device time: starting from C = 1
 // everywhere, each group in turn (largest N first) tries every C in
-// {1, 2, 4, 8} (R % C == 0, shared memory permitting) with the other groups
-// fixed, and takes the best if it cuts the batch time of `trial_cycles`
+// {1, 2, 4, 8} x L in {32, 16} (R % C == 0, shared memory permitting) with
+// the other groups fixed, and takes the best if it cuts the batch time of `trial_cycles`
 // cycles by more than 2 %; at most 3 passes.  Every trial
 // runs on a snapshot of the device state that is restored afterwards, so the
 // chain continues as if no trial had run.  Results are cached by key (device
 // name, potential, boundary, ensemble, R, the (N, runs) multiset) as JSON
-// lines {"key": "...", "ncta": {"N": C, ...}}.
+// lines {"key": "...", "ncta": {"N": 100 C + L, ...}} (L = lanes per walker).
 namespace {
 
 std::string tune_key(ptmc_ctx* c) {
@@ -1713,7 +1716,7 @@ std::string tune_key(ptmc_ctx* c) {
   cudaGetDevice(&dev);
   cudaGetDeviceProperties(&prop, dev);
   std::ostringstream k;
-  k << prop.name << "|sm" << prop.multiProcessorCount << "|pot" << c->pot << "|bc" << c->bc()
+  k << prop.name << "|sm" << prop.multiProcessorCount << "|shape=100C+L|pot" << c->pot << "|bc" << c->bc()
     << "|ens" << c->p.ensemble << "|R" << c->R() << "|groups";
   for (auto& G : c->groups) k << ":" << G.N << "x" << G.nruns;
   return k.str();
@@ -1793,15 +1796,19 @@ int restore_snapshot(ptmc_ctx* c, const Snapshot& s) {
 }  // namespace
 
 extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_path,
-                             int* ctas_per_run) {
+                             int* shape_out) {
   if (!c) return PTMC_ERR_ARG;
   if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
   if (trial_cycles < 1) return c->fail(PTMC_ERR_ARG, "trial_cycles must be >= 1");
   const int R = c->R();
-  std::map<int, int> best;  // N -> C
-  for (auto& G : c->groups) best[G.N] = 1;
+  // shape code: 100 * CTAs per run + lanes per walker
+  std::map<int, int> best;  // N -> shape code
+  for (auto& G : c->groups) best[G.N] = 100 + 32;
   auto apply = [&](const std::map<int, int>& m) {
-    for (auto& G : c->groups) G.ncta = m.at(G.N);
+    for (auto& G : c->groups) {
+      G.ncta = m.at(G.N) / 100;
+      G.lpr = m.at(G.N) % 100;
+    }
     drop_graphs(c);
   };
   if (c->f32() && c->pot != POT_NN) {
@@ -1831,31 +1838,33 @@ extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_pa
       std::vector<int> order;
       for (auto& kv : best) order.push_back(kv.first);
       std::sort(order.rbegin(), order.rend());  // largest N first
-      // coordinate descent: every candidate C of one group with the others
-      // fixed (the batch time is not monotonic in C: co-residency of the
-      // groups' CTAs on the SMs changes with the shape), at most 3 passes
+      // coordinate descent: every candidate shape of one group with the others
+      // fixed (the batch time is not monotonic in the shape: co-residency of the
+      // groups' CTAs on the SMs changes with it), at most 3 passes
       for (int pass = 0; pass < 3; ++pass) {
         bool improved = false;
         for (int N : order) {
           int pick = best[N];
           double t_pick = t_best;
-          for (int cand_c : {1, 2, 4, 8}) {
-            if (cand_c == best[N] || R % cand_c != 0 || cand_c > R) continue;
-            if (cycles32_smem_bytes(c->pot, R, N, cand_c) > optin) continue;
-            std::map<int, int> cand = best;
-            cand[N] = cand_c;
-            double t = 0;
-            rc = trial(cand, t);
-            if (rc) {  // a shape the device cannot launch: skip it
-              apply(best);
-              cudaGetLastError();
-              continue;
+          for (int cc : {1, 2, 4, 8})
+            for (int ll : {32, 16}) {
+              const int code = 100 * cc + ll;
+              if (code == best[N] || R % cc != 0 || (R / cc) % (32 / ll) != 0) continue;
+              if (cycles32_smem_bytes(c->pot, R, N, cc) > optin) continue;
+              std::map<int, int> cand = best;
+              cand[N] = code;
+              double t = 0;
+              rc = trial(cand, t);
+              if (rc) {  // a shape the device cannot launch: skip it
+                apply(best);
+                cudaGetLastError();
+                continue;
+              }
+              if (t < 0.98 * t_pick) {
+                pick = code;
+                t_pick = t;
+              }
             }
-            if (t < 0.98 * t_pick) {
-              pick = cand_c;
-              t_pick = t;
-            }
-          }
           if (pick != best[N]) {
             best[N] = pick;
             t_best = t_pick;
@@ -1869,12 +1878,15 @@ extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_pa
     }
   }
   apply(best);
-  if (ctas_per_run)
-    for (int r = 0; r < c->p.n_runs; ++r) ctas_per_run[r] = best[c->runs[r].N];
+  if (shape_out)
+    for (int r = 0; r < c->p.n_runs; ++r) {
+      shape_out[2 * r] = best[c->runs[r].N] / 100;
+      shape_out[2 * r + 1] = best[c->runs[r].N] % 100;
+    }
   return PTMC_OK;
 }
 
-extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run) {
+extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run, int lanes_per_walker) {
   if (!c) return PTMC_ERR_ARG;
   if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
   if (!c->f32() || c->pot == POT_NN)
@@ -1882,6 +1894,10 @@ extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run) {
   const int R = c->R();
   if (ctas_per_run < 1 || ctas_per_run > 8 || R % ctas_per_run != 0)
     return c->fail(PTMC_ERR_ARG, "ctas_per_run must divide the replica count and be <= 8");
+  if (lanes_per_walker != 32 && lanes_per_walker != 16)
+    return c->fail(PTMC_ERR_ARG, "lanes_per_walker must be 32 or 16");
+  if ((R / ctas_per_run) % (32 / lanes_per_walker) != 0)
+    return c->fail(PTMC_ERR_ARG, "16 lanes per walker need an even number of walkers per CTA");
   int optin = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -1891,6 +1907,7 @@ extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run) {
     if (cycles32_smem_bytes(c->pot, R, N, ctas_per_run) > optin)
       return c->fail(PTMC_ERR_LIMIT, "launch shape exceeds the shared memory of a CTA");
     G.ncta = ctas_per_run;
+    G.lpr = lanes_per_walker;
     found = true;
   }
   if (!found) return c->fail(PTMC_ERR_ARG, "no run with that atom count");

@@ -782,8 +782,8 @@ static int dispatch(int pot, int bc, int ens, bool f32, int what,
 
 int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
                   int run0, int nruns, int R, int maxN, int ncycles, int phase,
-                  void* stream, int ncta) {
-  if (f32) return launch_cycles32(pot, bc, ens, P, run0, nruns, R, maxN, ncycles, phase, ncta, stream);
+                  void* stream, int ncta, int lpr) {
+  if (f32) return launch_cycles32(pot, bc, ens, P, run0, nruns, R, maxN, ncycles, phase, ncta, lpr, stream);
   return dispatch(pot, bc, ens, false, 0, P, run0, nruns, R, maxN, ncycles, phase, stream);
 }
 int launch_init(int pot, int bc, int ens, bool f32, const KParams& P, int run0,

@@ -34,6 +34,11 @@
 //    writes them back.  Walker arithmetic and draw streams do not depend on C:
 //    results are bit-identical for every C.  C is chosen per atom count by
 //    ptmc_autotune (C = 1: a plain CTA launch, no cluster barrier).
+//  * LPR lanes per walker (32 or 16): with 16, the two halves of a warp hold two
+//    walkers; pair loops stride by LPR, reductions are segmented shuffles under
+//    the walker's lane mask, and every warp-level barrier takes that mask, so
+//    the halves may diverge (accept vs reject, refills) without waiting on each
+//    other.  Small N wastes fewer lanes and shares the per-move fixed work.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -154,11 +159,20 @@ __device__ __forceinline__ float usymf(uint32_t w) {
   return (u01f(w) - 0.5f) + 0x1.0p-24f;
 }
 
-// FP64 energy of one walker from its fixed-point positions (resync).
-template <int POT, int BC, int ENS>
+// sum over the LPR lanes of one walker (xor partners stay inside the group)
+template <int LPR, typename T>
+__device__ __forceinline__ T seg_sum(T v, unsigned mask) {
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+
+// FP64 energy of one walker from its fixed-point positions (resync); the
+// walker's LPR lanes share the work (glane = lane within the walker's group).
+template <int POT, int BC, int ENS, int LPR>
 __device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, double rc2,
                            const double* c, int K, double hn, double hm, double ean,
-                           double ecam, float2* comp32, float* sq32, int lane) {
+                           double ecam, float2* comp32, float* sq32, int lane, unsigned gmask) {
   auto P = [&](int a, double& x, double& y, double& z) {
     float4 h = Xh[a], l = Xl[a];
     x = (double)h.x + (double)l.x;
@@ -167,7 +181,7 @@ __device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, 
   };
   double e = 0.0;
   if constexpr (POT == POT_EAM) {
-    for (int a = lane; a < N; a += 32) {
+    for (int a = lane; a < N; a += LPR) {
       double xa, ya, za, A = 0.0, B = 0.0;
       P(a, xa, ya, za);
       for (int j = 0; j < N; ++j) {
@@ -183,12 +197,12 @@ __device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, 
       if (sq32) sq32[a] = (float)sqrt(B);
       e += ean * A - ecam * sqrt(B);
     }
-    return warp_sum(e);
+    return seg_sum<LPR>(e, gmask);
   } else {
     for (int i = 0; i < N; ++i) {
       double xi, yi, zi;
       P(i, xi, yi, zi);
-      for (int j = i + 1 + lane; j < N; j += 32) {
+      for (int j = i + 1 + lane; j < N; j += LPR) {
         double xj, yj, zj;
         P(j, xj, yj, zj);
         double r2 = BC == BC_CUB ? d2_cub(xi, yi, zi, xj, yj, zj, L) : d2_sph(xi, yi, zi, xj, yj, zj);
@@ -196,7 +210,7 @@ __device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, 
         e += v64<POT>(c, K, r2);
       }
     }
-    e = warp_sum(e);
+    e = seg_sum<LPR>(e, gmask);
     if (ENS == ENS_NPT) e += lrc64(N, rc2, c, K);
     return e;
   }
@@ -218,7 +232,7 @@ long long cycles32_smem_bytes(int pot, int R, int N, int C) {
   return b;
 }
 
-template <int POT, int BC, int ENS, bool SPLIT>
+template <int POT, int BC, int ENS, bool SPLIT, int LPR>
 __global__ void __launch_bounds__(1024)
     k_cycles32(KParams P, int run0, int ncycles, int phase, int ncta) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -231,7 +245,11 @@ __global__ void __launch_bounds__(1024)
   const RunDesc* rdp = P.runs + run0 + run_local;  // fields read on demand
   const int N = rdp->N, R = rdp->R;
   const int Rl = R / CL;                    // walkers held by this CTA
-  const int tid = threadIdx.x, wl = tid >> 5, lane = tid & 31;
+  // LPR lanes per walker, 32 / LPR walkers per warp; gmask = the walker's lanes
+  constexpr int WPW = 32 / LPR;
+  const int tid = threadIdx.x, lane = tid & (LPR - 1);
+  const int wl = (tid >> 5) * WPW + (tid & 31) / LPR;  // walker within this CTA
+  const unsigned gmask = LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << ((tid & 31) & ~(LPR - 1)));
   const int w = q * Rl + wl;                // walker index within the run
   const int nthr = blockDim.x;
   const int K = P.K;
@@ -324,7 +342,7 @@ __global__ void __launch_bounds__(1024)
 
   auto word = [&]() -> uint32_t {
     if (ctr - base >= 32ull) {
-      __syncwarp();
+      __syncwarp(gmask);
       base = ctr & ~3ull;
       if (lane < 8) {
         uint64_t blk = (base >> 2) + lane;
@@ -335,7 +353,7 @@ __global__ void __launch_bounds__(1024)
         drw[4 * lane + 2] = c4[2];
         drw[4 * lane + 3] = c4[3];
       }
-      __syncwarp();
+      __syncwarp(gmask);
     }
     uint32_t x = drw[ctr - base];
     ++ctr;
@@ -360,23 +378,23 @@ __global__ void __launch_bounds__(1024)
         ++count;
         if (count == 50) {  // recentre! (src/Configurations.jl:79-85), in FP64
           double sx = 0, sy = 0, sz = 0;
-          for (int a = lane; a < N; a += 32) {
+          for (int a = lane; a < N; a += LPR) {
             sx += (double)Xh[a].x + Xl[a].x;
             sy += (double)Xh[a].y + Xl[a].y;
             sz += (double)Xh[a].z + Xl[a].z;
           }
-          sx = warp_sum(sx) / N;
-          sy = warp_sum(sy) / N;
-          sz = warp_sum(sz) / N;
-          __syncwarp();
-          for (int a = lane; a < N; a += 32) {
+          sx = seg_sum<LPR>(sx, gmask) / N;
+          sy = seg_sum<LPR>(sy, gmask) / N;
+          sz = seg_sum<LPR>(sz, gmask) / N;
+          __syncwarp(gmask);
+          for (int a = lane; a < N; a += LPR) {
             double x = (double)Xh[a].x + Xl[a].x - sx, y = (double)Xh[a].y + Xl[a].y - sy,
                    z = (double)Xh[a].z + Xl[a].z - sz;
             float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
             Xh[a] = h;
             Xl[a] = make_float4((float)(x - h.x), (float)(y - h.y), (float)(z - h.z), 0.f);
           }
-          __syncwarp();
+          __syncwarp(gmask);
           h0 = Xh[i];
           l0 = Xl[i];
         } else {
@@ -403,7 +421,7 @@ __global__ void __launch_bounds__(1024)
     if (POT == POT_EAM) {
       const float2* C = s_c32 + (size_t)wl * N;
       float2* D = s_d32 + (size_t)wl * N;
-      for (int j = lane; j < N; j += 32) {
+      for (int j = lane; j < N; j += LPR) {
         if (j == i) continue;
         float4 b = Xh[j];
         float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
@@ -417,13 +435,13 @@ __global__ void __launch_bounds__(1024)
         // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
         de += eanf * da - ecamf * db * rcpf(SQ[j] + sqrtf_approx(rho + db));
       }
-      saf = warp_sum(saf);
-      sbf = warp_sum(sbf);
-      de = warp_sum(de);
+      saf = seg_sum<LPR>(saf, gmask);
+      sbf = seg_sum<LPR>(sbf, gmask);
+      de = seg_sum<LPR>(de, gmask);
       float rhoi = C[i].y;
       de += eanf * saf - ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(rhoi + sbf));
     } else {
-      for (int j = lane; j < N; j += 32) {
+      for (int j = lane; j < N; j += LPR) {
         if (j == i) continue;
         float4 b = Xh[j];
         float dn = pf2<BC>(tf, b, Lf, iLf);
@@ -435,11 +453,11 @@ __global__ void __launch_bounds__(1024)
           de += v32p<POT>(P, s_cf, K, dn) - v32p<POT>(P, s_cf, K, dol);
         }
       }
-      de = warp_sum(de);
+      de = seg_sum<LPR>(de, gmask);
     }
     float u = u01f(word());
     if (!(ex2f(-beta_l2e * de) >= u)) return 0;
-    __syncwarp();
+    __syncwarp(gmask);
     if (lane == 0) {
       Xh[i] = tf;
       Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
@@ -447,7 +465,7 @@ __global__ void __launch_bounds__(1024)
     if (POT == POT_EAM) {
       float2* C = s_c32 + (size_t)wl * N;
       const float2* D = s_d32 + (size_t)wl * N;
-      for (int k = lane; k < N; k += 32) {
+      for (int k = lane; k < N; k += LPR) {
         float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
         float2 c = C[k];
         float rho = c.y + d.y;
@@ -456,7 +474,7 @@ __global__ void __launch_bounds__(1024)
       }
     }
     de_acc += de;
-    __syncwarp();
+    __syncwarp(gmask);
     return 1;
   };
 
@@ -471,7 +489,7 @@ __global__ void __launch_bounds__(1024)
     float acc = 0.f, comp = 0.f;  // Kahan-compensated lane sum
     for (int i = 0; i < N; ++i) {
       float4 a = Xh[i];
-      for (int j = i + 1 + lane; j < N; j += 32) {
+      for (int j = i + 1 + lane; j < N; j += LPR) {
         float x = pf2<BC>(a, Xh[j], Lf, iLf) * s2;
         if (x <= rcnf) {
           float y = v32<POT>(s_cf, K, x) - comp;
@@ -481,14 +499,14 @@ __global__ void __launch_bounds__(1024)
         }
       }
     }
-    double e = warp_sum((double)acc - (double)comp) + lrc64(N, rcn, s_c, K);
+    double e = seg_sum<LPR>((double)acc - (double)comp, gmask) + lrc64(N, rcn, s_c, K);
     double Vn = Ln * Ln * Ln, Vo = L * L * L;
     double dh = (e - en) + P.pressure * (Vn - Vo);
     double prob = exp(-dh * beta + (double)N * log(Vn / Vo));
     double ua = (double)u01f(word());
     if (!(prob >= ua)) return 0;
-    __syncwarp();
-    for (int a = lane; a < N; a += 32) {
+    __syncwarp(gmask);
+    for (int a = lane; a < N; a += LPR) {
       double x = ((double)Xh[a].x + Xl[a].x) * scale, y = ((double)Xh[a].y + Xl[a].y) * scale,
              z = ((double)Xh[a].z + Xl[a].z) * scale;
       float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
@@ -502,7 +520,7 @@ __global__ void __launch_bounds__(1024)
     Llo = (float)(L - (double)Lf);
     iLf = (float)(1.0 / L);
     rcf = (float)rc2;
-    __syncwarp();
+    __syncwarp(gmask);
     return 1;
   };
 
@@ -533,12 +551,12 @@ __global__ void __launch_bounds__(1024)
       }
       en += (double)de_acc;
       if (P.resync_every > 0 && idx % P.resync_every == 0) {
-        double e64 = energy64<POT, BC, ENS>(Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean,
+        double e64 = energy64<POT, BC, ENS, LPR>(Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean,
                                             P.eam_ecam, POT == POT_EAM ? s_c32 + (size_t)wl * N : nullptr,
-                                            SQ, lane);
+                                            SQ, lane, gmask);
         drift = fmax(drift, fabs(en - e64));
         en = e64;
-        __syncwarp();
+        __syncwarp(gmask);
       }
     }
     if (lane == 0) {
@@ -679,35 +697,45 @@ __global__ void __launch_bounds__(1024)
   }
 }
 
-template <int POT, int BC, int ENS>
-static int launch32(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
-                    int phase, int ncta, cudaStream_t st) {
-  if (ncta < 1 || ncta > 8 || R % ncta != 0) return (int)cudaErrorInvalidValue;
+template <int POT, int BC, int ENS, int LPR>
+static int set_smem32(long long smem) {
+  static long long attr_set = 48 * 1024;  // per instantiation
+  if (smem <= attr_set) return 0;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles32<POT, BC, ENS, false, LPR>);
+  if (e != cudaSuccess) return (int)e;
+  if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS, false, LPR>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS, true, LPR>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  attr_set = smem;
+  return 0;
+}
+
+template <int POT, int BC, int ENS, int LPR>
+static int launch32l(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
+                     int phase, int ncta, cudaStream_t st) {
+  constexpr int WPW = 32 / LPR;
+  if (ncta < 1 || ncta > 8 || R % ncta != 0 || (R / ncta) % WPW != 0)
+    return (int)cudaErrorInvalidValue;
   long long smem = cycles32_smem_bytes(POT, R, maxN, ncta);
-  static long long attr_set = 48 * 1024;
-  if (smem > attr_set) {
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles32<POT, BC, ENS, false>);
-    if (e != cudaSuccess) return (int)e;
-    if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
-    e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    e = cudaFuncSetAttribute(k_cycles32<POT, BC, ENS, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    attr_set = smem;
-  }
+  int e = set_smem32<POT, BC, ENS, LPR>(smem);
+  if (e) return e;
+  const unsigned threads = (unsigned)(R / ncta * LPR);
   if (ncta == 1) {
-    k_cycles32<POT, BC, ENS, false><<<nruns, R * 32, (size_t)smem, st>>>(P, run0, ncycles, phase, 1);
+    k_cycles32<POT, BC, ENS, false, LPR><<<nruns, threads, (size_t)smem, st>>>(P, run0, ncycles,
+                                                                               phase, 1);
     return (int)cudaGetLastError();
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nruns * ncta), 1, 1);
-  cfg.blockDim = dim3((unsigned)(R / ncta * 32), 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
   cfg.dynamicSmemBytes = (size_t)smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -717,16 +745,25 @@ static int launch32(const KParams& P, int run0, int nruns, int R, int maxN, int 
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, k_cycles32<POT, BC, ENS, true>, P, run0, ncycles, phase, ncta);
-  if (e != cudaSuccess) return (int)e;
+  cudaError_t ce =
+      cudaLaunchKernelEx(&cfg, k_cycles32<POT, BC, ENS, true, LPR>, P, run0, ncycles, phase, ncta);
+  if (ce != cudaSuccess) return (int)ce;
   return (int)cudaGetLastError();
 }
 
+template <int POT, int BC, int ENS>
+static int launch32(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
+                    int phase, int ncta, int lpr, cudaStream_t st) {
+  if (lpr == 16) return launch32l<POT, BC, ENS, 16>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st);
+  if (lpr == 32) return launch32l<POT, BC, ENS, 32>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st);
+  return (int)cudaErrorInvalidValue;
+}
+
 int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,
-                    int maxN, int ncycles, int phase, int ncta, void* stream) {
+                    int maxN, int ncycles, int phase, int ncta, int lpr, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
 #define PT32(PO, B, E) \
-  if (pot == PO && bc == B && ens == E) return launch32<PO, B, E>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st);
+  if (pot == PO && bc == B && ens == E) return launch32<PO, B, E>(P, run0, nruns, R, maxN, ncycles, phase, ncta, lpr, st);
   PT32(POT_ELJ, BC_SPH, ENS_NVT)
   PT32(POT_ELJEVEN, BC_SPH, ENS_NVT)
   PT32(POT_EAM, BC_SPH, ENS_NVT)

@@ -104,11 +104,12 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
 namespace ptmc {
 long long cycles32_smem_bytes(int pot, int R, int N, int ncta);
 // ncta: CTAs per run (a thread-block cluster when > 1; FP32 form only)
+// lpr: lanes per walker (32 or 16; FP32 form only)
 int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,
-                    int maxN, int ncycles, int phase, int ncta, void* stream);
+                    int maxN, int ncycles, int phase, int ncta, int lpr, void* stream);
 int launch_cycles(int pot, int bc, int ens, bool f32, const KParams& P,
                   int run0, int nruns, int R, int maxN, int ncycles, int phase,
-                  void* stream, int ncta = 1);
+                  void* stream, int ncta = 1, int lpr = 32);
 int launch_init(int pot, int bc, int ens, bool f32, const KParams& P,
                 int run0, int nruns, int R, void* stream);
 int launch_resync(int pot, int bc, int ens, bool f32, const KParams& P,

@@ -97,7 +97,9 @@ def test_cluster_split_eam_and_npt_bit_identical(pk):
 
 def test_autotune_uneven_batch_restores_chain(pk, tmp_path):
     """Autotuning an uneven batch picks a valid shape per atom count, caches it,
-    and does not advance the chain: the tuned run equals an untuned one."""
+    and leaves the whole device state (positions, energies, draw counters,
+    counters, histograms) as it found it: with the default shape set back, the
+    chain continues bit for bit like an untuned one."""
     import ptmc_gb300.starts as S
     sizes = [13, 38, 55, 101, 147] * 2
     starts = [S.sphere_start(n, 0.9 * n ** (1 / 3) * 3, 4.3, 500 + k) for k, n in enumerate(sizes)]
@@ -115,7 +117,9 @@ def test_autotune_uneven_batch_restores_chain(pk, tmp_path):
     eng = make(9)
     shapes = eng.autotune(trial_cycles=5, cache=cache)
     assert set(shapes) == set(sizes)
-    assert all(c in (1, 2, 4, 8) for c in shapes.values())
+    assert all(c in (1, 2, 4, 8) and l in (16, 32) for c, l in shapes.values())
+    for n in set(sizes):  # back to one full warp per walker: the chain must continue bit for bit
+        eng.set_launch_shape(n, 1, 32)
     eng.cycles_nosample(30)
     a = snapshot(eng)
     eng.close()
@@ -129,3 +133,44 @@ def test_autotune_uneven_batch_restores_chain(pk, tmp_path):
     assert eng.autotune(trial_cycles=5, cache=cache) == shapes
     eng.close()
     assert len(open(cache).read().strip().split("\n")) == 1
+
+
+def test_half_warp_walkers(pk, orc):
+    """16 lanes per walker (two walkers per warp): the running FP32 energy tracks
+    the oracle's FP64 energy of the positions; the result does not depend on the
+    cluster size at L = 16 (bit for bit); per-temperature mean energies agree
+    with the 32-lane layout within 5 combined standard errors."""
+    import ptmc_gb300.starts as S
+    pot = pk.ELJPotentialEven(C_NE)
+    starts = [S.sphere_start(13, 8.0, 4.5, 40 + r) for r in range(3)]
+    args = (pk, pot, pk.NVT(13), starts, pk.SphericalBC(11.0), 16, (4.0, 16.0), 5)
+    ref = engine(*args)
+    ref.set_launch_shape(13, 1, 16)
+    a = protocol(ref)
+    for r in range(3):
+        st = ref.states(r)
+        e64 = np.array([orc.elj_config_energy(x, orc.POT_ELJEVEN, C_NE) for x in st["xyz"]])
+        assert np.all(np.abs(st["en_tot"] - e64) <= 1e-6 * np.abs(e64))
+    ref.close()
+    eng = engine(*args)
+    eng.set_launch_shape(13, 2, 16)
+    b = protocol(eng)
+    eng.close()
+    assert_identical(a, b)
+    # statistics against the 32-lane layout: 16 independent runs each
+    st16 = [S.sphere_start(13, 8.0, 4.5, 60 + r) for r in range(16)]
+
+    def means(lanes, seed):
+        e = engine(pk, pot, pk.NVT(13), st16, pk.SphericalBC(11.0), 16, (4.0, 16.0), seed)
+        e.set_launch_shape(13, 1, lanes)
+        e.cycles_nosample(2000)
+        m = []
+        for _ in range(20):
+            e.cycles_nosample(100)
+            m.append([e.states(r)["en_tot"] for r in range(16)])
+        e.close()
+        return np.array(m).mean(axis=0)  # [runs, R]
+    m16, m32 = means(16, 71), means(32, 72)
+    se = np.sqrt(m16.var(axis=0, ddof=1) / 16 + m32.var(axis=0, ddof=1) / 16)
+    z = np.abs(m16.mean(axis=0) - m32.mean(axis=0)) / se
+    assert np.all(z < 5), z
