@@ -81,6 +81,8 @@ typedef struct ptmc_output {
   double* en_histogram;    /* [R*(n_bin+2)]  NVT Output.en_histogram */
   double* ev_histogram;    /* [R*(n_bin+2)^2] NPT Output.ev_histogram, [slot][e][v] */
   double hist_params[6];   /* en_min, en_max, v_min, v_max, delta_en_hist, delta_v_hist */
+  double* rdf;             /* [R*5*n_bin] Output.rdf (needs ptmc_set_rdf), NULL skips it */
+  double delta_r2;         /* Output.delta_r2, the rdf bin width in r^2 */
 } ptmc_output;
 
 /* Engine counters for measurement. */
@@ -122,6 +124,12 @@ int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N,
 /* Optional initial step sizes, 2 per slot (atom, volume); default 0.1, 0.1
  * (src/MCStates.jl:104). */
 int ptmc_set_max_displ(ptmc_ctx* c, int run, const double* max_displ);
+/* Radial distribution sampling, the rdfsave option of ptmc_run! (update_rdf!,
+ * src/Sampling.jl:282-316): every 1000th production cycle each slot's
+ * configuration adds its pair distances to 5 n_bin bins of width
+ * delta_r2 = 4 r^2 / n_bin / 5 (sphere) or 3/4 L^2 / n_bin / 5 (cube).  Set it
+ * before ptmc_init. */
+int ptmc_set_rdf(ptmc_ctx* c, int on);
 /* Uploads everything and computes the initial energies on the GPU
  * (MCState constructor, src/MCStates.jl:137-162). */
 int ptmc_init(ptmc_ctx* c);

@@ -83,6 +83,8 @@ def lib():
         L.orc_multihist_npt.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, _dp, _dp, _ip]
+        L.orc_set_rdf.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_get_rdf.argtypes = [ctypes.c_void_p, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.orc_sur_nparams.restype = ctypes.c_int
         L.orc_sur_forward.argtypes = [_dp, _dp, _fp, ctypes.c_int, ctypes.c_int, _dp]
@@ -261,6 +263,15 @@ class Run:
         a, b, c, d = (np.zeros(R) for _ in range(4))
         lib().orc_finalise(self.h, mc_cycles, mc_sample, P(a), P(b), P(c), P(d))
         return dict(en_avg=a, heat_cap=b, count_stat_atom=c, count_stat_exc=d)
+
+    def set_rdf(self, on=True):
+        _check(lib().orc_set_rdf(self.h, int(bool(on))))
+
+    def rdf(self):
+        out = np.zeros((self.R, 5 * self.n_bin))
+        dr2 = np.zeros(1)
+        _check(lib().orc_get_rdf(self.h, P(out), P(dr2)))
+        return out, float(dr2[0])
 
     def set_surrogate(self, cfg, params, bf16=True):
         """Delayed-acceptance atom moves with the pair surrogate (None: off)."""

@@ -390,6 +390,9 @@ struct orc_run {
   // results
   double en_min = 0, en_max = 0, v_min = 0, v_max = 0, dE = 0, dV = 0;
   std::vector<double> en_hist, ev_hist;
+  bool rdf_on = false;       // rdfsave
+  double dr2 = 0;            // delta_r2
+  std::vector<double> rdf;   // R * 5 n_bin
   bool inited = false;
   // scratch
   std::vector<double> trial_row, new_comp, newG, newF, new_eatom, sc_pos,
@@ -792,7 +795,24 @@ inline long hist_index(double h, int n_bin) {
 }
 
 // sampling_step! (Sampling.jl:330-371)
-void sample(orc_run* r) {
+// update_rdf! (Sampling.jl:282, 301-316): dist2_mat[i, k], k <= i, of each
+// slot's configuration; rdf_index = floor(r2 / delta_r2), kept when != 0 and
+// <= 5 n_bin (1-based)
+void update_rdf(orc_run* r) {
+  const int N = r->N, nb5 = 5 * r->n_bin;
+  for (int s = 0; s < r->R; ++s) {
+    const double* d = r->D(r->wos[s]);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k <= i; ++k) {
+        const double idx = std::floor(d[(size_t)i * N + k] / r->dr2);
+        if (idx != 0 && idx <= nb5) r->rdf[(size_t)s * nb5 + (size_t)idx - 1] += 1;
+      }
+  }
+}
+
+// sampling_step! (Sampling.jl:330-371) of production cycle `idx`
+void sample(orc_run* r, long idx) {
+  if (r->rdf_on && idx % 1000 == 0) update_rdf(r);
   int R = r->R, nb = r->n_bin + 2;
   for (int s = 0; s < R; ++s) {
     int w = r->wos[s];
@@ -993,6 +1013,21 @@ int orc_equilibrate(orc_run* r, int eq_cycles) {
     r->dV = (r->v_max - r->v_min) / r->n_bin;
     r->ev_hist.assign((size_t)r->R * nb * nb, 0.0);
   }
+  {  // delta_r2 (Sampling.jl:151 sphere, :185 cube) of the first state's boundary
+    double b = r->box[r->wos[0]];
+    r->dr2 = r->bc == ORC_BC_CUBIC ? 3.0 / 4.0 * (b * b) / r->n_bin / 5 : 4 * (b * b) / r->n_bin / 5;
+    r->rdf.assign((size_t)r->R * 5 * r->n_bin, 0.0);
+  }
+  return 0;
+}
+
+int orc_set_rdf(orc_run* r, int on) {
+  r->rdf_on = on != 0;
+  return 0;
+}
+int orc_get_rdf(orc_run* r, double* rdf, double* dr2) {
+  if (rdf && !r->rdf.empty()) std::memcpy(rdf, r->rdf.data(), sizeof(double) * r->rdf.size());
+  if (dr2) *dr2 = r->dr2;
   return 0;
 }
 
@@ -1001,7 +1036,7 @@ int orc_production(orc_run* r, long first, long n) {
   for (long i = first; i < first + n; ++i) {
     int rc = cycle(r, i);
     if (rc) return rc;
-    if (i % r->mc_sample == 0) sample(r);
+    if (i % r->mc_sample == 0) sample(r, i);
   }
   return 0;
 }

@@ -82,6 +82,10 @@ int orc_get_hist(orc_run* r, double* en_hist, double* ev_hist, double* hp);
 /* finalise_results (Sampling.jl:377) */
 int orc_finalise(orc_run* r, long mc_cycles, int mc_sample, double* en_avg,
                  double* heat_cap, double* stat_atom, double* stat_exc);
+/* radial distribution sampling (rdfsave, Sampling.jl:282-345): on/off, and
+ * the R x 5 n_bin histogram with its bin width delta_r2 */
+int orc_set_rdf(orc_run* r, int on);
+int orc_get_rdf(orc_run* r, double* rdf, double* dr2);
 /* NN only: G matrix (nsf x N, column per atom) of walker w */
 int orc_get_nn_state(orc_run* r, int w, double* G, double* eatom);
 

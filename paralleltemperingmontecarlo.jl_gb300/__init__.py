@@ -329,8 +329,10 @@ class Engine:
     own atom count)."""
 
     def __init__(self, mc_params, temp, potential, ensemble, *, n_runs=1, precision="fp64",
-                 resync_every=1000, exch_prob=0.1, seed=1234, cycles_per_launch=0, device=0):
+                 resync_every=1000, exch_prob=0.1, seed=1234, cycles_per_launch=0, device=0,
+                 rdfsave=False):
         self.L = _capi.load()
+        self.rdfsave = bool(rdfsave)
         self.mc_params, self.temp, self.potential, self.ensemble = mc_params, temp, potential, ensemble
         p = _capi.Params()
         p.n_runs = n_runs
@@ -357,6 +359,8 @@ class Engine:
         h = ctypes.c_void_p()
         _capi.check(self.L.ptmc_create(ctypes.byref(h), ctypes.byref(p)))
         self.h = h
+        if self.rdfsave:
+            self._ck(self.L.ptmc_set_rdf(h, 1))
         self.n_runs, self.R = n_runs, mc_params.n_traj
         self.N = {}
         self.bc = {}
@@ -505,10 +509,14 @@ class Engine:
             setattr(o, k, _dptr(v))
         o.en_histogram = _dptr(eh)
         o.ev_histogram = _dptr(ev)
+        rdf = np.zeros((R, 5 * self.mc_params.n_bin)) if self.rdfsave else None
+        if rdf is not None:
+            o.rdf = _dptr(rdf)
         self._ck(self.L.ptmc_get_output(self.h, run, ctypes.byref(o)))
         hp = list(o.hist_params)
         return Output(n_bin=self.mc_params.n_bin, en_min=hp[0], en_max=hp[1], v_min=hp[2],
                       v_max=hp[3], delta_en_hist=hp[4], delta_v_hist=hp[5],
+                      delta_r2=o.delta_r2, rdf=list(rdf) if rdf is not None else [],
                       max_displ=arrs["max_displ"], en_avg=arrs["en_avg"],
                       heat_cap=arrs["heat_cap"], en_histogram=eh,
                       ev_histogram=ev if npt else None,
@@ -565,13 +573,13 @@ def ptmc_run(mc_params, temp, start_config, potential, ensemble, *, rdfsave=Fals
     mc_params.mc_cycles production cycles with optional checkpoints every
     `save` cycles into <workingdirectory>/checkpoint, finalise.
 
-    Returns (mc_states, results) with slot-ordered states and an Output."""
-    if rdfsave:
-        raise NotImplementedError("the radial distribution sampler is not part of this engine")
+    Returns (mc_states, results) with slot-ordered states and an Output; with
+    rdfsave the radial distribution (Output.rdf) is sampled every 1000th
+    production cycle (src/Sampling.jl:341-345)."""
     wd = workingdirectory or os.getcwd()
     ckdir = os.path.join(wd, "checkpoint")
     eng = Engine(mc_params, temp, potential, ensemble, precision=precision,
-                 resync_every=resync_every, exch_prob=exch_prob, seed=seed)
+                 resync_every=resync_every, exch_prob=exch_prob, seed=seed, rdfsave=rdfsave)
     try:
         eng.set_configs(0, start_config, max_displ)
         eng.init()

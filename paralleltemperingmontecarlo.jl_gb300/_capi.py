@@ -37,7 +37,7 @@ class Output(ctypes.Structure):
     _fields_ = [("en_avg", _dp), ("heat_cap", _dp), ("count_stat_atom", _dp),
                 ("count_stat_vol", _dp), ("count_stat_exc", _dp), ("max_displ", _dp),
                 ("en_histogram", _dp), ("ev_histogram", _dp),
-                ("hist_params", ctypes.c_double * 6)]
+                ("hist_params", ctypes.c_double * 6), ("rdf", _dp), ("delta_r2", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -64,6 +64,7 @@ SIGNATURES = {
     "ptmc_set_run_configs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_int, ctypes.c_double]),
     "ptmc_set_max_displ": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "ptmc_set_rdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ptmc_init": (ctypes.c_int, [ctypes.c_void_p]),
     "ptmc_equilibrate": (ctypes.c_int, [ctypes.c_void_p]),
     "ptmc_run_cycles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),

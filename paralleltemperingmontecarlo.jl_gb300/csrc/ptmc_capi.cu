@@ -140,6 +140,8 @@ struct ptmc_ctx {
   DBuf<int> d_status, d_wos;
   DBuf<long long> d_cnt;
   DBuf<unsigned int> d_hist;
+  bool rdf_on = false;         // radial distribution sampling (rdfsave of ptmc_run!)
+  DBuf<unsigned int> d_rdf;    // [W][5 n_bin]
   KParams K{};
   // neural-network potential
   std::vector<NNSF> nn_sf;    // active functions (radial, then angular sorted by eta)
@@ -499,6 +501,13 @@ int ptmc_set_max_displ(ptmc_ctx* c, int run, const double* md) {
   return PTMC_OK;
 }
 
+int ptmc_set_rdf(ptmc_ctx* c, int on) {
+  if (!c) return PTMC_ERR_ARG;
+  if (c->inited) return c->fail(PTMC_ERR_STATE, "radial distribution sampling is set before ptmc_init");
+  c->rdf_on = on != 0;
+  return PTMC_OK;
+}
+
 int ptmc_init(ptmc_ctx* c) {
   if (!c) return PTMC_ERR_ARG;
   if (c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init called twice");
@@ -573,7 +582,8 @@ int ptmc_init(ptmc_ctx* c) {
       c->d_en.alloc(W) || c->d_box.alloc(W) || c->d_rc2.alloc(W) || c->d_drift.alloc(W) ||
       c->d_beta.alloc(W) || c->d_maxd.alloc(2 * W) || c->d_maxbox.alloc(W) ||
       c->d_ham.alloc(2 * W) || c->d_ctr.alloc(W) || c->d_status.alloc(W) ||
-      c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho))
+      c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho) ||
+      (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)))
     return c->fail(PTMC_ERR_CUDA, "device allocation failed");
   // host images
   std::vector<double> pos(po), box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W);
@@ -606,6 +616,7 @@ int ptmc_init(ptmc_ctx* c) {
   CK(cudaMemsetAsync(c->d_ham.p, 0, sizeof(double) * 2 * W, s));
   CK(cudaMemsetAsync(c->d_cnt.p, 0, sizeof(long long) * 6 * W, s));
   CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned int) * std::max<long long>(ho, 1), s));
+  if (c->rdf_on) CK(cudaMemsetAsync(c->d_rdf.p, 0, sizeof(unsigned int) * c->d_rdf.n, s));
   int rc = push_runs(c);
   if (rc) return rc;
   KParams& K = c->K;
@@ -626,6 +637,7 @@ int ptmc_init(ptmc_ctx* c) {
   K.cnt = c->d_cnt.p;
   K.wos = c->d_wos.p;
   K.hist = c->d_hist.p;
+  K.rdf = c->rdf_on ? c->d_rdf.p : nullptr;
   K.K = (int)c->coeff.size();
   for (int k = 0; k < MAX_COEFF; ++k) K.c[k] = k < K.K ? c->coeff[k] : 0.0;
   for (int k = 0; k < MAX_COEFF; ++k) K.cf[k] = (float)K.c[k];
@@ -738,6 +750,11 @@ int ptmc_equilibrate(ptmc_ctx* c) {
       r.v_max = V * 2.0;
       r.dV = (r.v_max - r.v_min) / c->p.n_bin;
     }
+    {  // delta_r2 of the first state's boundary (Sampling.jl:151, 185)
+      const double b = box[r.wk + wos[r.wk + 0]];
+      r.dr2 = c->bc() == PTMC_BC_CUBIC ? 3.0 / 4.0 * (b * b) / c->p.n_bin / 5
+                                       : 4 * (b * b) / c->p.n_bin / 5;
+    }
   }
   c->equilibrated = true;
   rc = push_runs(c);
@@ -745,6 +762,7 @@ int ptmc_equilibrate(ptmc_ctx* c) {
   // reset_counters (MCRun.jl:271-277)
   CK(cudaMemsetAsync(c->d_cnt.p, 0, sizeof(long long) * 6 * W, c->st));
   CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned int) * std::max<size_t>(c->d_hist.n, 1), c->st));
+  if (c->rdf_on) CK(cudaMemsetAsync(c->d_rdf.p, 0, sizeof(unsigned int) * c->d_rdf.n, c->st));
   CK(cudaStreamSynchronize(c->st));
   return PTMC_OK;
 }
@@ -844,6 +862,15 @@ int ptmc_get_output(ptmc_ctx* c, int run, ptmc_output* o) {
   o->hist_params[3] = r.v_max;
   o->hist_params[4] = r.dE;
   o->hist_params[5] = r.dV;
+  o->delta_r2 = r.dr2;
+  if (o->rdf && c->rdf_on) {  // Output.rdf: 5 n_bin bins per slot
+    const size_t nb5 = (size_t)5 * c->p.n_bin;
+    std::vector<unsigned int> rh((size_t)R * nb5);
+    CK(cudaMemcpyAsync(rh.data(), c->d_rdf.p + (size_t)r.wk * nb5, sizeof(unsigned int) * rh.size(),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (size_t k = 0; k < rh.size(); ++k) o->rdf[k] = (double)rh[k];
+  }
   return PTMC_OK;
 }
 
@@ -886,6 +913,7 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_wos.free_();
   c->d_cnt.free_();
   c->d_hist.free_();
+  c->d_rdf.free_();
   c->d_nn_sf.free_();
   c->d_nn_W.free_();
   c->d_nn_G.free_();
@@ -975,7 +1003,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
   if (!write_file_atomic(d + "/params.data", s)) return c->fail(PTMC_ERR_IO, "cannot write params.data");
   // hist_info.data (save_histparams, :117-127)
   s = "e_min e_max v_min v_max \xce\x94_E \xce\x94_V \xce\x94_r2\n";
-  double hv[7] = {r0.en_min, r0.en_max, r0.v_min, r0.v_max, r0.dE, r0.dV, 0.0};
+  double hv[7] = {r0.en_min, r0.en_max, r0.v_min, r0.v_max, r0.dE, r0.dV, r0.dr2};
   for (int k = 0; k < 7; ++k) s += fmt_double(hv[k]) + (k < 6 ? " " : "\n");
   if (!write_file_atomic(d + "/hist_info.data", s)) return c->fail(PTMC_ERR_IO, "cannot write hist_info.data");
   // histograms (checkpoint, :178-218)
@@ -999,6 +1027,17 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
           s += fmt_double(v) + ((col == nb - 1 && rw == nb - 1) ? "\n" : "\t");
         }
     if (!write_file_atomic(d + "/volume_hist.data", s)) return c->fail(PTMC_ERR_IO, "cannot write volume_hist.data");
+  }
+  if (c->rdf_on) {  // rdf.data (checkpoint with rdfsave, :192-196): one row per replica
+    const size_t nb5 = (size_t)5 * c->p.n_bin;
+    std::vector<unsigned int> rh((size_t)R * nb5);
+    CK(cudaMemcpy(rh.data(), c->d_rdf.p + (size_t)r0.wk * nb5, sizeof(unsigned int) * rh.size(),
+                  cudaMemcpyDeviceToHost));
+    s.clear();
+    for (int i = 0; i < R; ++i)
+      for (size_t m = 0; m < nb5; ++m)
+        s += fmt_double((double)rh[(size_t)i * nb5 + m]) + (m < nb5 - 1 ? "\t" : "\n");
+    if (!write_file_atomic(d + "/rdf.data", s)) return c->fail(PTMC_ERR_IO, "cannot write rdf.data");
   }
   long long index = r0.cyc[PHASE_PROD] - 1;
   if (!write_file_atomic(d + "/index.txt", std::to_string(index) + "\n"))
@@ -1032,7 +1071,8 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       (rc = dump(c, b, c->d_drift)) || (rc = dump(c, b, c->d_beta)) || (rc = dump(c, b, c->d_maxd)) ||
       (rc = dump(c, b, c->d_maxbox)) || (rc = dump(c, b, c->d_ham)) || (rc = dump(c, b, c->d_ctr)) ||
       (rc = dump(c, b, c->d_status)) || (rc = dump(c, b, c->d_wos)) || (rc = dump(c, b, c->d_cnt)) ||
-      (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)))
+      (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)) ||
+      (rc = dump(c, b, c->d_rdf)))
     return rc;
   put(b, "PTMCEND!", 8);
   if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
@@ -1076,7 +1116,8 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
       (rc = undump(c, b, at, c->d_ham)) || (rc = undump(c, b, at, c->d_ctr)) ||
       (rc = undump(c, b, at, c->d_status)) || (rc = undump(c, b, at, c->d_wos)) ||
       (rc = undump(c, b, at, c->d_cnt)) || (rc = undump(c, b, at, c->d_hist)) ||
-      (rc = undump(c, b, at, c->d_nn_G)) || (rc = undump(c, b, at, c->d_nn_sow)))
+      (rc = undump(c, b, at, c->d_nn_G)) || (rc = undump(c, b, at, c->d_nn_sow)) ||
+      (rc = undump(c, b, at, c->d_rdf)))
     return rc;
   c->rd = rd;
   c->equilibrated = hdr[3] != 0;

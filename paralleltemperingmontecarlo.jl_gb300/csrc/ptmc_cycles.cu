@@ -659,6 +659,21 @@ __global__ void __launch_bounds__(1024)
       }
     }
     __syncthreads();
+    if (P.rdf && phase == PHASE_PROD && idx % P.mc_sample == 0 && idx % RDF_EVERY == 0) {
+      // update_rdf!: pairs k < i of this walker into the row of its slot; NPT
+      // reads the distance matrix (scaled on volume moves, as the reference's)
+      unsigned int* row = P.rdf + (size_t)(rd.wk + s_sow[w]) * 5 * P.n_bin;
+      for (int i = 1; i < N; ++i)
+        for (int k = lane; k < i; k += 32) {
+          double r2;
+          if (M) r2 = M[(size_t)i * N + k];
+          else if (BC == BC_CUB)
+            r2 = d2_cub(X[3 * i], X[3 * i + 1], X[3 * i + 2], X[3 * k], X[3 * k + 1], X[3 * k + 2], L);
+          else
+            r2 = d2_sph(X[3 * i], X[3 * i + 1], X[3 * i + 2], X[3 * k], X[3 * k + 1], X[3 * k + 2]);
+          rdf_add(row, 5 * P.n_bin, r2, rd.dr2);
+        }
+    }
   }
 
   // ---- store the run back to HBM ----

@@ -657,6 +657,13 @@ __global__ void __launch_bounds__(1024)
       }
     }
     __syncthreads();
+    if (P.rdf && phase == PHASE_PROD && idx % P.mc_sample == 0 && idx % RDF_EVERY == 0) {
+      // update_rdf! (src/Sampling.jl:301-316) from the FP32 positions
+      unsigned int* row = P.rdf + (size_t)(wk0 + s_sow[w]) * 5 * P.n_bin;
+      for (int i = 1; i < N; ++i)
+        for (int k = lane; k < i; k += LPR)
+          rdf_add(row, 5 * P.n_bin, (double)pf2<BC>(Xh[i], Xh[k], Lf, iLf), rdp->dr2);
+    }
   }
 
   double* gpos_w = P.pos + rdp->pos_off + (size_t)q * Rl * N * 3;

@@ -39,7 +39,18 @@ struct RunDesc {
   double v_min, v_max, dV;    // volume histogram (NPT)
   long long cyc[3];         // next cycle index (1-based) per phase
   unsigned long long run_ctr;  // run-level draw counter
+  double dr2;               // radial-distribution bin width in r^2 (Sampling.jl:151,185)
+  double pad1;
 };
+
+// update_rdf! (src/Sampling.jl:282, 301-316): bin = floor(r2 / delta_r2), kept
+// when 1 <= bin <= 5 n_bin (1-based; the diagonal, r2 = 0, falls in bin 0)
+__device__ __forceinline__ void rdf_add(unsigned int* row, int nb5, double r2, double dr2) {
+  const double b = floor(r2 / dr2);
+  if (b >= 1.0 && b <= (double)nb5) atomicAdd(row + ((int)b - 1), 1u);
+}
+// every 1000th production cycle (Sampling.jl:341-345)
+constexpr int RDF_EVERY = 1000;
 
 struct KParams {
   RunDesc* runs;
@@ -61,6 +72,7 @@ struct KParams {
   long long* cnt;
   int* wos;
   unsigned int* hist;
+  unsigned int* rdf;        // [slots][5 n_bin] radial distribution (NULL = off)
   // potential
   double c[MAX_COEFF];
   int K;

@@ -1005,6 +1005,21 @@ __global__ void k_run_epilogue(KParams P, NNParams Q, int run0, int phase) {
     }
   }
   __syncthreads();
+  if (P.rdf && phase == PHASE_PROD && idx % P.mc_sample == 0 && idx % RDF_EVERY == 0) {
+    // update_rdf! (src/Sampling.jl:301-316): every slot's walker, pairs k < i
+    for (int sl = 0; sl < R; ++sl) {
+      const double* X = P.pos + rd->pos_off + (size_t)P.wos[wk + sl] * N * 3;
+      unsigned int* row = P.rdf + (size_t)(wk + sl) * 5 * P.n_bin;
+      for (int p = threadIdx.x; p < N * N; p += blockDim.x) {
+        const int i = p / N, k = p % N;
+        if (k >= i) continue;
+        rdf_add(row, 5 * P.n_bin,
+                d2_sph(X[3 * i], X[3 * i + 1], X[3 * i + 2], X[3 * k], X[3 * k + 1], X[3 * k + 2]),
+                rd->dr2);
+      }
+    }
+  }
+  __syncthreads();
   if (s == 0) rd->cyc[phase] = idx + 1;
 }
 

@@ -52,6 +52,8 @@ struct PTMCOutput
     en_histogram::Ptr{Cdouble}
     ev_histogram::Ptr{Cdouble}
     hist_params::NTuple{6,Cdouble}
+    rdf::Ptr{Cdouble}
+    delta_r2::Cdouble
 end
 
 # mirrors `struct ptmc_surrogate_cfg`
@@ -75,7 +77,7 @@ max_displ)` and `results::Output`.
 """
 function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential, ensemble;
                    save=false, precision=:fp64, exch_prob=0.1, seed=1234, resync_every=1000,
-                   workingdirectory=pwd())
+                   rdfsave=false, workingdirectory=pwd())
     configs = start_config isa Config ? (start_config,) : Tuple(start_config)
     R = mc_params.n_traj
     N = length(configs[1])
@@ -104,6 +106,7 @@ function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential,
         xyz = reduce(hcat, [reduce(hcat, cf.positions) for cf in configs])
         bc = configs[1].boundary_condition
         kind, par = bc isa SphericalBC ? (0, sqrt(bc.radius2)) : (1, bc.box_length)
+        rdfsave && check(ccall((:ptmc_set_rdf, libptmc), Cint, (Ptr{Cvoid}, Cint), c, 1), c)
         check(ccall((:ptmc_set_run_configs, libptmc), Cint,
                     (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cint, Cint, Cdouble),
                     c, 0, xyz, N, length(configs), kind, par), c)
@@ -126,15 +129,21 @@ function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential,
         md = zeros(2R)
         eh = zeros(nb * R)
         ev = npt ? zeros(nb * nb * R) : zeros(1)
+        rd = zeros(rdfsave ? 5 * mc_params.n_bin * R : 1)
         o = Ref(PTMCOutput(pointer(en_avg), pointer(heat_cap), pointer(sa), pointer(sv),
-                           pointer(se), pointer(md), pointer(eh), pointer(ev), ntuple(_ -> 0.0, 6)))
-        GC.@preserve en_avg heat_cap sa sv se md eh ev begin
+                           pointer(se), pointer(md), pointer(eh), pointer(ev), ntuple(_ -> 0.0, 6),
+                           rdfsave ? pointer(rd) : C_NULL, 0.0))
+        GC.@preserve en_avg heat_cap sa sv se md eh ev rd begin
             check(ccall((:ptmc_get_output, libptmc), Cint, (Ptr{Cvoid}, Cint, Ref{PTMCOutput}), c, 0, o), c)
         end
         hp = o[].hist_params
         results = Output{Float64}(mc_params.n_bin)
         results.en_min, results.en_max, results.v_min, results.v_max = hp[1], hp[2], hp[3], hp[4]
         results.delta_en_hist, results.delta_v_hist = hp[5], hp[6]
+        if rdfsave
+            results.delta_r2 = o[].delta_r2
+            results.rdf = [rd[(k - 1) * 5 * mc_params.n_bin + 1:k * 5 * mc_params.n_bin] for k in 1:R]
+        end
         results.en_avg, results.heat_cap = en_avg, heat_cap
         results.count_stat_atom, results.count_stat_exc = sa, se
         results.max_displ = md[1:2:end]

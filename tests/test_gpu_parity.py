@@ -46,14 +46,14 @@ CU_EAM = dict(n=8.482, m=4.692, eps=0.0367493 * 0.0370, C=27.561, a=0.25 * 18.89
 
 
 def pair(pk, orc, *, N, R, x0, T0, T1, pot, ens="nvt", bc_param, exch_prob, seed, n_runs=1,
-         starts=None, cycles_per_launch=0, pressure=0.0, eq=0):
+         starts=None, cycles_per_launch=0, pressure=0.0, eq=0, rdfsave=False, precision="fp64"):
     """An engine and matching oracle runs (one per engine run)."""
     mp = pk.MCParams(mc_cycles=1000, eq_cycles=eq, mc_sample=1, n_traj=R, n_atoms=N)
     temp = pk.TempGrid(T0, T1, R)
     ensemble = pk.NPT(N, pressure) if ens == "npt" else pk.NVT(N)
     bc = pk.CubicBC(bc_param) if ens == "npt" or ens == "nvt_cubic" else pk.SphericalBC(bc_param)
     eng = pk.Engine(mp, temp, pot, ensemble, n_runs=n_runs, exch_prob=exch_prob, seed=seed,
-                    cycles_per_launch=cycles_per_launch)
+                    cycles_per_launch=cycles_per_launch, rdfsave=rdfsave, precision=precision)
     oracles = []
     for r in range(n_runs):
         xr = x0 if starts is None else starts[r]
@@ -66,6 +66,8 @@ def pair(pk, orc, *, N, R, x0, T0, T1, pot, ens="nvt", bc_param, exch_prob, seed
             o.set_eam(pot.n, pot.m, pot.ean, pot.eCam)
         else:
             o.set_elj(pot.coeff, pot.even)
+        if rdfsave:
+            o.set_rdf(True)
         o.init()
         oracles.append(o)
     eng.init()
@@ -273,3 +275,49 @@ def test_gpu_multihist_matches_oracle(pk, orc):
     assert it == ito
     np.testing.assert_allclose(cv, cvo, rtol=1e-9)
     np.testing.assert_allclose(T, To, rtol=1e-15)
+
+
+def test_rdf_sampler_parity(pk, orc, tmp_path):
+    """rdfsave (update_rdf!, src/Sampling.jl:282-345): every 1000th production
+    cycle each slot's configuration adds its pair distances.  FP64 sphere: the
+    histograms equal the oracle's exactly (the distances are recomputed from
+    positions that are bitwise identical).  NPT reads the scaled distance matrix;
+    positions agree to ~1 ulp there, so a few pairs may fall in a neighbouring
+    bin.  The FP32 form samples the same number of pairs."""
+    x0 = sphere_start(13, 8.0, 4.5, 1234)
+    args = dict(N=13, R=8, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE), bc_param=11.0,
+                exch_prob=1.0, seed=21, eq=400, rdfsave=True)
+    eng, (o,) = pair(pk, orc, **args)
+    eng.equilibrate()
+    o.equilibrate(400)
+    eng.run_cycles(3000)
+    o.production(1, 3000)
+    out = eng.output(0)
+    ro, dr2 = o.rdf()
+    assert out.delta_r2 == dr2 == 4 * 11.0 ** 2 / 100 / 5
+    g = np.array(out.rdf)
+    assert np.array_equal(g, ro), "radial distribution histograms"
+    assert g.sum() == 3 * 8 * 13 * 12 / 2
+    ck = str(tmp_path / "ck")  # the reference's rdf.data: one row per replica
+    eng.checkpoint(ck)
+    np.testing.assert_array_equal(np.loadtxt(os.path.join(ck, "rdf.data")), ro)
+    assert float(open(os.path.join(ck, "hist_info.data")).read().split("\n")[1].split()[6]) == dr2
+    eng.close()
+    e32, _ = pair(pk, orc, **dict(args, precision="fp32"))
+    e32.equilibrate()
+    e32.run_cycles(3000)
+    assert np.array(e32.output(0).rdf).sum() == 3 * 8 * 13 * 12 / 2
+    e32.close()
+    p = 101325 * 3.398928944382626e-14
+    eng, (o,) = pair(pk, orc, N=32, R=4, x0=fcc(2, 8.4, 0.05, 2), T0=10.0, T1=40.0,
+                     pot=pk.ELJPotentialEven(C_NE), ens="npt", bc_param=16.8, exch_prob=1.0, seed=8,
+                     pressure=p, eq=40, rdfsave=True)
+    eng.equilibrate()
+    o.equilibrate(40)
+    eng.run_cycles(2000)
+    o.production(1, 2000)
+    g = np.array(eng.output(0).rdf)
+    ro, _ = o.rdf()
+    assert ro.sum() > 0 and abs(g.sum() - ro.sum()) <= 2
+    assert np.abs(g - ro).sum() <= 0.001 * ro.sum() + 4
+    eng.close()
