@@ -257,6 +257,20 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles,
 int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n,
                            int* n_out);
 
+/* multihistogram(output, Tvec) of src/multihist.jl (the linear-solve
+ * multihistogram, used by postprocess): histograms en_hist [R][n_bin+2]
+ * (interior bins used, divided by n_bin, empty bins dropped), beta [R].
+ * Outputs: energies and S_E [n_bin] (entropy per kept bin, the first *n_kept
+ * are set), alpha [R], and on npoints temperatures T_1 + k (T_R - T_1)/npoints:
+ * T, Z, U, Cv, dCv, S_T [npoints] (analysis, :292-375, with the reference's
+ * rescaling of Z into [1, 100]).  The system A alpha = b is singular; the
+ * reference's A \ b fixes the free constant by LAPACK's rounding, this call by
+ * alpha[R-1] = 0: U, Cv and dCv are unaffected, Z and S_T scale / shift. */
+int ptmc_multihist_linear(int R, int n_bin, const double* en_hist, const double* beta,
+                          double en_min, double en_max, int npoints, double* energies,
+                          double* S_E, int* n_kept, double* alpha, double* T, double* Z,
+                          double* U, double* Cv, double* dCv, double* S_T);
+
 /* Allocation-free multihistogram_NVT, no counterpart in the reference (which
  * has no device memory at all).  For callers that cannot call cudaMalloc: a
  * Julia program whose GPU memory belongs to CUDA.jl's pool, code enqueueing

@@ -83,6 +83,9 @@ def lib():
         L.orc_multihist_npt.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, _dp, _dp, _ip]
+        L.orc_multihist_linear.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int, _dp, _dp, _ip, _dp, _dp,
+                                           _dp, _dp, _dp, _dp, _dp]
         L.orc_set_rdf.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_get_rdf.argtypes = [ctypes.c_void_p, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
@@ -322,3 +325,20 @@ def sur_loss_grad(cfg, params, rows, targets, bf16=True):
                                    int(bf16), P(loss), P(g)))
     return float(loss[0]), g
 
+
+def multihist_linear(en_hist, beta, en_min, en_max, npoints=1000):
+    """Linear-solve multihistogram (src/multihist.jl); returns a dict."""
+    h = _d(en_hist)
+    R, nb = h.shape
+    n_bin = nb - 2
+    beta = _d(beta)
+    E, S = np.zeros(n_bin), np.zeros(n_bin)
+    nk = (ctypes.c_int * 1)()
+    al = np.zeros(R)
+    out = {k: np.zeros(npoints) for k in ("T", "Z", "U", "Cv", "dCv", "S_T")}
+    _check(lib().orc_multihist_linear(R, n_bin, P(h), P(beta), en_min, en_max, npoints, P(E), P(S),
+                                      ctypes.cast(nk, _ip), P(al), P(out["T"]), P(out["Z"]),
+                                      P(out["U"]), P(out["Cv"]), P(out["dCv"]), P(out["S_T"])))
+    k = nk[0]
+    out.update(energies=E[:k], S_E=S[:k], alpha=al)
+    return out

@@ -1194,6 +1194,143 @@ int orc_get_sur_stats(orc_run* r, long* out) {
   return 0;
 }
 
+// ---------------------------------------------------------------- linear multihistogram
+// multihistogram(output, Tvec) of src/multihist.jl:25-487: readfile (:55-79),
+// processhist! (:89-114), bvector (:166-210), amatrix (:215-232), systemsolver
+// (:237-270), Entropycalc (:275-283), analysis (:292-375).  The matrix A is
+// singular (its rows sum to zero; b is consistent), so the reference's A \ b
+// returns alpha up to an additive constant chosen by LAPACK's rounding; here
+// the last equation is replaced by alpha[R-1] = 0 (Gaussian elimination with
+// partial pivoting).  A constant in alpha shifts S(E) by a constant, which
+// leaves U, Cv and dCv unchanged (Z and S(T) change by the factor / offset).
+int orc_multihist_linear(int R, int n_bin, const double* en_hist, const double* beta,
+                         double en_min, double en_max, int npoints, double* energies,
+                         double* S_E, int* n_kept, double* alpha, double* T_out, double* Z,
+                         double* U, double* Cv, double* dCv, double* S_T) {
+  const double kB = 3.16681196E-6;  // multihist.jl:57
+  const int nb = n_bin + 2;
+  const double de = (en_max - en_min) / (n_bin - 1);
+  std::vector<double> H((size_t)R * n_bin), E(n_bin);
+  for (int j = 0; j < n_bin; ++j) E[j] = j * de + en_min;
+  for (int i = 0; i < R; ++i)
+    for (int j = 0; j < n_bin; ++j) H[(size_t)i * n_bin + j] = en_hist[(size_t)i * nb + j + 1] / n_bin;
+  // processhist!: drop bins with no counts
+  std::vector<int> keep;
+  std::vector<double> nsum;
+  for (int j = 0; j < n_bin; ++j) {
+    double t = 0;
+    for (int i = 0; i < R; ++i) t += H[(size_t)i * n_bin + j];
+    if (t != 0) {
+      keep.push_back(j);
+      nsum.push_back(t);
+    }
+  }
+  const int B = (int)keep.size();
+  if (B == 0) return fail("multihistogram: empty histograms");
+  std::vector<double> h((size_t)R * B), ev(B), bmat((size_t)R * B), rh(B, 0.0), b(R, 0.0);
+  for (int k = 0; k < B; ++k) {
+    ev[k] = E[keep[k]];
+    for (int i = 0; i < R; ++i) h[(size_t)i * B + k] = H[(size_t)i * n_bin + keep[k]];
+  }
+  for (int i = 0; i < R; ++i)  // bvector
+    for (int k = 0; k < B; ++k) {
+      double x = h[(size_t)i * B + k];
+      bmat[(size_t)i * B + k] = x == 0.0 ? 0.0 : x * (std::log(x) + beta[i] * ev[k]);
+    }
+  for (int k = 0; k < B; ++k)
+    for (int i = 0; i < R; ++i) rh[k] += bmat[(size_t)i * B + k];
+  for (int i = 0; i < R; ++i)
+    for (int k = 0; k < B; ++k) b[i] += bmat[(size_t)i * B + k] - h[(size_t)i * B + k] * rh[k] / nsum[k];
+  std::vector<double> A((size_t)R * R, 0.0);  // amatrix
+  for (int i = 0; i < R; ++i)
+    for (int ip = 0; ip < R; ++ip) {
+      double t = 0;
+      for (int k = 0; k < B; ++k) t += h[(size_t)i * B + k] * h[(size_t)ip * B + k] / nsum[k];
+      A[(size_t)i * R + ip] = -t;
+      if (i == ip) {
+        double d = 0;
+        for (int k = 0; k < B; ++k) d += h[(size_t)i * B + k];
+        A[(size_t)i * R + ip] += d;
+      }
+    }
+  // gauge: alpha[R-1] = 0 in place of the last (dependent) equation
+  for (int ip = 0; ip < R; ++ip) A[(size_t)(R - 1) * R + ip] = ip == R - 1 ? 1.0 : 0.0;
+  b[R - 1] = 0.0;
+  std::vector<double> x(b);
+  for (int col = 0; col < R; ++col) {  // Gaussian elimination, partial pivoting
+    int piv = col;
+    for (int rr = col + 1; rr < R; ++rr)
+      if (std::fabs(A[(size_t)rr * R + col]) > std::fabs(A[(size_t)piv * R + col])) piv = rr;
+    if (A[(size_t)piv * R + col] == 0.0) return fail("multihistogram: singular system");
+    if (piv != col) {
+      for (int cc = 0; cc < R; ++cc) std::swap(A[(size_t)piv * R + cc], A[(size_t)col * R + cc]);
+      std::swap(x[piv], x[col]);
+    }
+    for (int rr = col + 1; rr < R; ++rr) {
+      const double f = A[(size_t)rr * R + col] / A[(size_t)col * R + col];
+      for (int cc = col; cc < R; ++cc) A[(size_t)rr * R + cc] -= f * A[(size_t)col * R + cc];
+      x[rr] -= f * x[col];
+    }
+  }
+  for (int rr = R - 1; rr >= 0; --rr) {
+    double t = x[rr];
+    for (int cc = rr + 1; cc < R; ++cc) t -= A[(size_t)rr * R + cc] * x[cc];
+    x[rr] = t / A[(size_t)rr * R + rr];
+  }
+  std::vector<double> S(B);  // Entropycalc
+  for (int k = 0; k < B; ++k) {
+    double t = 0;
+    for (int i = 0; i < R; ++i) t += bmat[(size_t)i * B + k] - h[(size_t)i * B + k] * x[i];
+    S[k] = t / nsum[k];
+  }
+  // analysis
+  const double T0 = 1 / (kB * beta[0]), T1 = 1 / (kB * beta[R - 1]);
+  const double dT = (T1 - T0) / npoints;
+  double nexp = 0;
+  std::vector<double> XP(B);
+  for (int p = 0; p < npoints; ++p) {
+    const double T = p * dT + T0;
+    double z = 0;
+    for (long guard = 0;; ++guard) {
+      if (guard > 10000000) return fail("multihistogram: partition-function scaling did not settle");
+      z = 0;
+      for (int k = 0; k < B; ++k) {
+        XP[k] = std::exp((S[k] - ev[k] / (T * kB)) - nexp);
+        z += XP[k];
+      }
+      if (z < 1.0) nexp -= 1.0;
+      else if (z > 100.0) nexp += 0.7;
+      else break;
+    }
+    double u = 0, u2 = 0;
+    for (int k = 0; k < B; ++k) {
+      u += XP[k] * ev[k];
+      u2 += XP[k] * ev[k] * ev[k];
+    }
+    u /= z;
+    u2 /= z;
+    double r2 = 0, r3 = 0;
+    for (int k = 0; k < B; ++k) {
+      const double d = ev[k] - u;
+      r2 += XP[k] * d * d;
+      r3 += XP[k] * d * d * d;
+    }
+    r2 /= z;
+    r3 /= z;
+    if (T_out) T_out[p] = T;
+    if (Z) Z[p] = z;
+    if (U) U[p] = u;
+    if (Cv) Cv[p] = (u2 - u * u) / kB / (T * T);
+    if (S_T) S_T[p] = u / T + kB * std::log(z);
+    if (dCv) dCv[p] = r3 / (kB * kB) / (T * T * T * T) - 2 * r2 / kB / (T * T * T);
+  }
+  if (n_kept) *n_kept = B;
+  if (energies) std::copy(ev.begin(), ev.end(), energies);
+  if (S_E) std::copy(S.begin(), S.end(), S_E);
+  if (alpha) std::copy(x.begin(), x.end(), alpha);
+  return 0;
+}
+
 // ---------------------------------------------------------------- WHAM NVT
 // multihistogram_NVT (multihist_NVT.jl:11-221), restated literally.
 int orc_multihist_nvt(int R, int n_bin, const double* H, const double* t_grid,

@@ -140,6 +140,15 @@ int orc_multihist_npt(int R, int n_bin, const double* ev_hist,
                       double pressure, double thr, double* T_out,
                       double* cp_out, int* iters);
 
+/* linear-solve multihistogram (multihistogram(output, Tvec), src/multihist.jl):
+ * en_hist [R][n_bin+2]; outputs energies/S_E [n_bin] (the first *n_kept are
+ * used), alpha [R], and T/Z/U/Cv/dCv/S_T [npoints].  The gauge alpha[R-1] = 0
+ * replaces the singular system's last equation. */
+int orc_multihist_linear(int R, int n_bin, const double* en_hist, const double* beta,
+                         double en_min, double en_max, int npoints, double* energies,
+                         double* S_E, int* n_kept, double* alpha, double* T_out,
+                         double* Z, double* U, double* Cv, double* dCv, double* S_T);
+
 #ifdef __cplusplus
 }
 #endif

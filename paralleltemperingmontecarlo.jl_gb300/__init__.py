@@ -32,6 +32,7 @@ __all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "Config", "NV
            "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "RuNNerPotential",
            "Output", "MCState", "PairSurrogate",
            "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
+           "multihistogram", "postprocess",
            "distance2", "get_distance2_mat", "get_volume", "PTMCError"]
 
 
@@ -674,6 +675,114 @@ def multihist_npt_arrays(hist, t_grid, beta, en_min, en_max, v_min, v_max, p, th
 
 
 # ------------------------------------------------------------------ checkpoints
+def multihist_linear_arrays(hist, beta, en_min, en_max, npoints=1000):
+    """The linear-solve multihistogram on the GPU (ptmc_multihist_linear)."""
+    L = _capi.load()
+    h = np.ascontiguousarray(hist, dtype=np.float64)
+    R, nb = h.shape
+    n_bin = nb - 2
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    E, S, al = np.zeros(n_bin), np.zeros(n_bin), np.zeros(R)
+    nk = ctypes.c_int()
+    out = {k: np.zeros(npoints) for k in ("T", "Z", "U", "Cv", "dCv", "S_T")}
+    _capi.check(L.ptmc_multihist_linear(R, n_bin, _dptr(h), _dptr(b), en_min, en_max, int(npoints),
+                                        _dptr(E), _dptr(S), ctypes.byref(nk), _dptr(al),
+                                        _dptr(out["T"]), _dptr(out["Z"]), _dptr(out["U"]),
+                                        _dptr(out["Cv"]), _dptr(out["dCv"]), _dptr(out["S_T"])))
+    k = nk.value
+    out.update(energies=E[:k], S_E=S[:k], alpha=al)
+    return out
+
+
+def _jl(x):
+    """A float as Julia prints it ("0.1", "100.0", "1.0e-5", "-5.6e7")."""
+    x = float(x)
+    if x == 0:
+        return "-0.0" if math.copysign(1, x) < 0 else "0.0"
+    if not math.isfinite(x):
+        return "NaN" if x != x else ("Inf" if x > 0 else "-Inf")
+    r = repr(abs(x))  # shortest round-trip digits
+    if "e" in r:
+        mant, ex = r.split("e")
+        ex = int(ex)
+    else:
+        mant, ex = r, 0
+        if "." in mant:
+            ip, fp = mant.split(".")
+        else:
+            ip, fp = mant, ""
+        # normalise to d.ddd x 10^ex
+        if ip.strip("0"):
+            ex = len(ip.lstrip("0")) - 1
+            digits = (ip.lstrip("0") + fp).rstrip("0") or "0"
+        else:
+            lead = len(fp) - len(fp.lstrip("0"))
+            ex = -lead - 1
+            digits = fp.lstrip("0").rstrip("0") or "0"
+        mant = digits[0] + ("." + digits[1:] if len(digits) > 1 else "")
+    digits = mant.replace(".", "").rstrip("0") or "0"
+    if -4 <= ex < 6:  # Julia: 0.0001 fixed, 1.0e-5 and 1.0e6 scientific
+        if ex >= 0:
+            ip = digits[:ex + 1].ljust(ex + 1, "0")
+            fp = digits[ex + 1:] or "0"
+            txt = ip + "." + fp
+        else:
+            txt = "0." + "0" * (-ex - 1) + digits
+    else:
+        txt = digits[0] + "." + (digits[1:] or "0") + "e" + str(ex)
+    return ("-" if x < 0 else "") + txt
+
+
+def multihistogram(output, temp, outdir=None, npoints=1000):
+    """multihistogram(output, Tvec; outdir, NPoints) (src/multihist.jl:437-455):
+    the linear-solve multihistogram on the GPU.  Writes histograms.data, Sol.X,
+    S.data and analysis.NVT (T, Z, Cv, dCv, U(T)) into `outdir` (default: the
+    current directory) and returns the arrays (dict)."""
+    res = multihist_linear_arrays(output.en_histogram, temp.beta_grid, output.en_min,
+                                  output.en_max, npoints)
+    h = np.asarray(output.en_histogram, dtype=float)[:, 1:-1] / output.n_bin
+    h = h[:, h.sum(axis=0) != 0]
+    res["histograms"] = h
+    d = outdir or os.getcwd()
+    os.makedirs(d, exist_ok=True)
+
+    def row(v):
+        return "\t".join(_jl(x) for x in v) + "\n"
+    with open(os.path.join(d, "histograms.data"), "w") as f:
+        f.write(row(res["energies"]))
+        for r in h:
+            f.write(row(r))
+    with open(os.path.join(d, "Sol.X"), "w") as f:
+        f.write("alpha\n" + row(res["alpha"]))
+    with open(os.path.join(d, "S.data"), "w") as f:
+        f.write("E\tEntropy\n")
+        for e, s_ in zip(res["energies"], res["S_E"]):
+            f.write(row((e, s_)))
+    with open(os.path.join(d, "analysis.NVT"), "w") as f:
+        f.write("T\tZ\tCv\tdCv\tU(T)\n")
+        for k in range(npoints):
+            f.write(row((res["T"][k], res["Z"][k], res["Cv"][k], res["dCv"][k], res["U"][k])))
+    return res
+
+
+def postprocess(xdir=None, npoints=1000):
+    """postprocess(; xdir) (src/multihist.jl:457-485): the linear-solve
+    multihistogram of the run whose checkpoint is <xdir>/checkpoint (its
+    histograms and temperature grid); the four output files are written into
+    xdir, the checkpoint is left as it is.  Returns (energies, histogramdata,
+    T, Z, Cv, dCv, U) as the reference (its last column is U(T))."""
+    d = xdir or os.getcwd()
+    ck = read_checkpoint(os.path.join(d, "checkpoint"))
+    p = ck["params"]
+    R, n_bin = int(p[2]), int(p[5])
+    temp = TempGrid(p[8], p[9], R)
+    hi = ck["hist_info"]
+    out = Output(n_bin=n_bin, en_min=hi[0], en_max=hi[1], en_histogram=ck["histograms"][:R])
+    res = multihistogram(out, temp, outdir=d, npoints=npoints)
+    return (res["energies"], list(res["histograms"]), res["T"], res["Z"], res["Cv"], res["dCv"],
+            res["U"])
+
+
 def read_checkpoint(directory):
     """Read a reference checkpoint directory (src/ReadSave.jl:330-481):
     params.data, hist_info.data, histograms.data, [volume_hist.data],

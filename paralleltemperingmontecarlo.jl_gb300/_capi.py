@@ -90,6 +90,9 @@ SIGNATURES = {
                                                   ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p]),
     "ptmc_measure_peaks": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
+    "ptmc_multihist_linear": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                                             ctypes.c_double, ctypes.c_int, _dp, _dp, _ip, _dp, _dp,
+                                             _dp, _dp, _dp, _dp, _dp]),
     "ptmc_surrogate_eval": (ctypes.c_int, [ctypes.POINTER(SurrogateCfg), _fp, _fp, ctypes.c_int,
                                            _dp, ctypes.c_int]),
     "ptmc_surrogate_loss_grad": (ctypes.c_int, [ctypes.POINTER(SurrogateCfg), _fp, _fp, _fp,

@@ -92,7 +92,7 @@ std::string fmt_double(double v) {
     if (ch != '.') digits += ch;
   while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
   std::string out;
-  if (ex >= -5 && ex < 6) {
+  if (ex >= -4 && ex < 6) {  // Julia: 0.0001 fixed, 1.0e-5 and 1.0e6 scientific
     if (ex >= 0) {
       std::string ip = digits.substr(0, std::min<size_t>(digits.size(), ex + 1));
       while ((int)ip.size() < ex + 1) ip += '0';
@@ -314,6 +314,10 @@ int run_phase(ptmc_ctx* c, long long n, int phase) {
 }
 
 }  // namespace
+
+namespace ptmc {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace ptmc
 
 // ================================================================ C ABI
 extern "C" {

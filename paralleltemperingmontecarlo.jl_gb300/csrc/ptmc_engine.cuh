@@ -13,6 +13,7 @@
 //   hist u32 [sum_r R_r*stride_r]  NVT: (n_bin+2) per slot, NPT: (n_bin+2)^2
 #pragma once
 #include <cstdint>
+#include <string>
 
 namespace ptmc {
 
@@ -136,4 +137,6 @@ int wham_npt_device(int R, int n_bin, const double* d_hist, const double* d_beta
                     double p, double thr, const double* d_beta_out, int n_out,
                     double* d_work, double* d_out, int* d_iters, void* stream);
 long long wham_work_doubles(int R, int n_bins_total);
+// sets the message returned by ptmc_last_error(NULL) (ptmc_capi.cu)
+void set_last_error(const std::string& msg);
 }  // namespace ptmc

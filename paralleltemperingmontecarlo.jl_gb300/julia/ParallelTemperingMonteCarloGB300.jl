@@ -14,6 +14,7 @@ calls is exercised through Python ctypes in `tests/`.
 module ParallelTemperingMonteCarloGB300
 
 using ParallelTemperingMonteCarlo
+using DelimitedFiles
 
 const libptmc = joinpath(@__DIR__, "..", "_build", "libptmc_gb300.so")
 
@@ -186,6 +187,52 @@ function multihistogram_NVT(ensemble, temp::TempGrid, results::Output, conv_thre
                results.en_min, results.en_max, conv_threshold, T, cv, it)
     rc == 0 || error(unsafe_string(ccall((:ptmc_last_error, libptmc), Cstring, (Ptr{Cvoid},), C_NULL)))
     return cv
+end
+
+"""
+    multihistogram(output, temp; outdir=pwd(), NPoints=1000)
+
+Linear-solve multihistogram (`src/multihist.jl:437-455`) on the GPU
+(`ptmc_multihist_linear`, gauge alpha[R] = 0); writes histograms.data, Sol.X,
+S.data and analysis.NVT into `outdir` like the reference and returns
+(energies, T, Z, Cv, dCv, U).
+"""
+function multihistogram(output::Output, temp::TempGrid; outdir=pwd(), NPoints=1000)
+    R = length(temp.beta_grid)
+    nb = output.n_bin
+    h = reduce(vcat, output.en_histogram)            # row-major [slot][bin], n_bin + 2 bins
+    E, S, alpha = zeros(nb), zeros(nb), zeros(R)
+    T, Z, U, Cv, dCv, ST = (zeros(NPoints) for _ in 1:6)
+    nk = Ref{Cint}(0)
+    rc = ccall((:ptmc_multihist_linear, libptmc), Cint,
+               (Cint, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cdouble, Cint, Ptr{Cdouble},
+                Ptr{Cdouble}, Ref{Cint}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+                Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+               R, nb, Float64.(h), collect(temp.beta_grid), output.en_min, output.en_max, NPoints,
+               E, S, nk, alpha, T, Z, U, Cv, dCv, ST)
+    rc == 0 || error(unsafe_string(ccall((:ptmc_last_error, libptmc), Cstring, (Ptr{Cvoid},), C_NULL)))
+    E, S = E[1:nk[]], S[1:nk[]]
+    H = [Float64.(output.en_histogram[i][2:end-1]) ./ nb for i in 1:R]
+    keep = findall(!iszero, sum(H))
+    open(joinpath(outdir, "histograms.data"), "w") do f
+        writedlm(f, permutedims(E))
+        for i in 1:R
+            writedlm(f, permutedims(H[i][keep]))
+        end
+    end
+    open(joinpath(outdir, "Sol.X"), "w") do f
+        writedlm(f, ["alpha"])
+        writedlm(f, permutedims(alpha))
+    end
+    open(joinpath(outdir, "S.data"), "w") do f
+        writedlm(f, ["E" "Entropy"])
+        writedlm(f, [E S])
+    end
+    open(joinpath(outdir, "analysis.NVT"), "w") do f
+        writedlm(f, ["T" "Z" "Cv" "dCv" "U(T)"])
+        writedlm(f, [T Z Cv dCv U])
+    end
+    return E, T, Z, Cv, dCv, U
 end
 
 """

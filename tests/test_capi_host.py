@@ -123,3 +123,13 @@ def test_read_reference_checkpoint(pk, tmp_path):
     assert c0["max_displ"][0] == pytest.approx(0.3138428376721002)
     assert c0["counts"] == [9758, 0]
     assert len(c0["config"]) == 13
+
+
+def test_julia_float_text(pk):
+    """Floats in checkpoint and multihistogram files are printed as Julia prints
+    them (writedlm / print): fixed notation from 1e-4 to below 1e6."""
+    cases = {0.1: "0.1", 100.0: "100.0", 1e6: "1.0e6", 1e-5: "1.0e-5", 1e-4: "0.0001",
+             -5.62340834334278e7: "-5.62340834334278e7", 123456.5: "123456.5", 0.0: "0.0",
+             3.166811429e-6: "3.166811429e-6", -0.00123: "-0.00123"}
+    for x, t in cases.items():
+        assert pk._jl(x) == t, (x, pk._jl(x), t)

@@ -321,3 +321,35 @@ def test_rdf_sampler_parity(pk, orc, tmp_path):
     assert ro.sum() > 0 and abs(g.sum() - ro.sum()) <= 2
     assert np.abs(g - ro).sum() <= 0.001 * ro.sum() + 4
     eng.close()
+
+
+def test_gpu_linear_multihistogram(pk, orc, tmp_path):
+    """The linear-solve multihistogram (src/multihist.jl) on the GPU against the
+    oracle's restatement (same gauge alpha[R-1] = 0) on the reference's golden
+    NVT histograms; postprocess() of a checkpoint directory writes the
+    reference's four files."""
+    d = json.load(open(os.path.join(GOLDEN, "multihist_nvt.json")))
+    h = np.array(d["en_histogram"])
+    temp = pk.TempGrid(d["t_i"], d["t_f"], d["R"])
+    g = pk.multihist_linear_arrays(h, temp.beta_grid, d["en_min"], d["en_max"])
+    o = orc.multihist_linear(h, temp.beta_grid, d["en_min"], d["en_max"])
+    assert np.array_equal(g["energies"], o["energies"])
+    np.testing.assert_allclose(g["alpha"], o["alpha"], rtol=1e-9, atol=1e-9 * np.abs(o["alpha"]).max())
+    np.testing.assert_allclose(g["S_E"], o["S_E"], rtol=1e-9, atol=1e-12)
+    for k in ("T", "U", "Cv", "dCv", "Z", "S_T"):
+        np.testing.assert_allclose(g[k], o[k], rtol=1e-8, err_msg=k)
+    # postprocess of a checkpoint written by ptmc_run
+    x0 = sphere_start(13, 8.0, 4.5, 1234)
+    mp = pk.MCParams.new(2000, 8, 13, eq_percentage=0.5)
+    pk.ptmc_run(mp, pk.TempGrid(4.0, 16.0, 8), pk.Config(x0, pk.SphericalBC(11.0)),
+                pk.ELJPotentialEven(C_NE), pk.NVT(13), save=2000, exch_prob=1.0,
+                workingdirectory=str(tmp_path))
+    wd = str(tmp_path)
+    ck_hist = open(os.path.join(wd, "checkpoint", "histograms.data")).read()
+    E, hd, T, Z, Cv, dCv, U = pk.postprocess(wd, npoints=200)
+    for f in ("histograms.data", "Sol.X", "S.data", "analysis.NVT"):
+        assert os.path.exists(os.path.join(wd, f))
+    assert open(os.path.join(wd, "checkpoint", "histograms.data")).read() == ck_hist
+    a = np.loadtxt(os.path.join(wd, "analysis.NVT"), skiprows=1)
+    np.testing.assert_allclose(a[:, 2], Cv, rtol=1e-12)
+    assert np.all(np.isfinite(Cv)) and Cv.max() > 0 and len(hd) == 8

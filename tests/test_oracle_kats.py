@@ -280,3 +280,48 @@ def test_oracle_delayed_acceptance_zero_surrogate_is_exact_chain(orc):
     run.cycles(1, 5)
     st = run.sur_stats()
     assert st["stage1_rejects"] == 0 and st["exact_evals"] == 5 * N * R
+
+
+def _ref_linear_cv(h, beta, en_min, en_max, npoints=1000):
+    """src/multihist.jl restated in numpy with the singular A alpha = b solved by
+    least squares (minimum norm): another choice of the free constant."""
+    kB = 3.16681196e-6
+    R, nb = h.shape
+    n_bin = nb - 2
+    de = (en_max - en_min) / (n_bin - 1)
+    E = np.arange(n_bin) * de + en_min
+    H = h[:, 1:-1] / n_bin
+    keep = H.sum(axis=0) != 0
+    H, E = H[:, keep], E[keep]
+    nsum = H.sum(axis=0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        bmat = np.where(H == 0, 0.0, H * (np.log(H) + beta[:, None] * E[None, :]))
+    b = (bmat - H * bmat.sum(axis=0) / nsum).sum(axis=1)
+    A = -(H / nsum) @ H.T + np.diag(H.sum(axis=1))
+    alpha = np.linalg.lstsq(A, b, rcond=None)[0]
+    S = (bmat - H * alpha[:, None]).sum(axis=0) / nsum
+    T0, T1 = 1 / (kB * beta[0]), 1 / (kB * beta[-1])
+    T = np.arange(npoints) * ((T1 - T0) / npoints) + T0
+    y = S[None, :] - E[None, :] / (T[:, None] * kB)
+    y -= y.max(axis=1, keepdims=True)
+    w = np.exp(y)
+    w /= w.sum(axis=1, keepdims=True)
+    U = (w * E).sum(axis=1)
+    U2 = (w * E * E).sum(axis=1)
+    return T, U, (U2 - U * U) / kB / T ** 2
+
+
+def test_linear_multihistogram_gauge(orc):
+    """The linear-solve multihistogram (src/multihist.jl) has a singular system;
+    the oracle fixes alpha[R-1] = 0, a least-squares solve picks another constant:
+    U(T) and Cv(T) must agree (they do not depend on the constant)."""
+    d = json.load(open(os.path.join(GOLDEN, "multihist_nvt.json")))
+    h = np.array(d["en_histogram"])
+    _, beta = orc.tempgrid(d["t_i"], d["t_f"], d["R"])
+    r = orc.multihist_linear(h, beta, d["en_min"], d["en_max"])
+    T, U, Cv = _ref_linear_cv(h, beta, d["en_min"], d["en_max"])
+    np.testing.assert_allclose(r["T"], T, rtol=1e-13)
+    np.testing.assert_allclose(r["U"], U, rtol=1e-9)
+    np.testing.assert_allclose(r["Cv"], Cv, rtol=1e-6)
+    assert abs(r["alpha"][-1]) == 0.0
+    assert len(r["energies"]) == int((h[:, 1:-1].sum(axis=0) != 0).sum())
