@@ -32,9 +32,12 @@ extern "C" {
 #define PTMC_NVT 0
 #define PTMC_NPT 1
 /* boundary conditions: SphericalBC (src/BoundaryConditions.jl:44),
- * CubicBC (src/BoundaryConditions.jl:72) */
+ * CubicBC (src/BoundaryConditions.jl:72), RectangularBC (:89) and RhombicBC
+ * (:110), the last two with a box length (x, y) and a height (z) */
 #define PTMC_BC_SPHERE 0
 #define PTMC_BC_CUBIC 1
+#define PTMC_BC_RECTANGULAR 2
+#define PTMC_BC_RHOMBIC 3
 /* arithmetic forms */
 #define PTMC_FP64 0          /* plain form: FP64 everywhere */
 #define PTMC_FP32_RESYNC 1   /* FP32 move rows, FP64 running total, FP64 resync */
@@ -121,9 +124,27 @@ int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf,
  * (src/Initialization.jl:88-96).  bc_param: sphere radius or cube side. */
 int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N,
                          int n_start, int bc_kind, double bc_param);
+/* Start configurations in a RectangularBC or RhombicBC box
+ * (src/BoundaryConditions.jl:80-116): box_length (x, y side; for the rhombic
+ * box the side of the rhombus) and box_height (z).  For the sphere and the cube
+ * box_height is ignored (ptmc_set_run_configs is this call with
+ * box_height = bc_param).  These boxes run in the plain FP64 form with the ELJ
+ * potentials. */
+int ptmc_set_run_configs_box(ptmc_ctx* c, int run, const double* xyz, int N,
+                             int n_start, int bc_kind, double box_length,
+                             double box_height);
+/* NPT(n_atoms, pressure, separated_volume) (src/Ensembles.jl:75-86): volume
+ * moves change z (probability 1/6), x and y (1/3) or all directions (1/2)
+ * (volume_change_separated, src/MCMoves.jl:298-343) with their own step sizes
+ * max_displ[3:4] and counters count_vol_xy / count_vol_z.  RectangularBC or
+ * RhombicBC boxes only.  Set it before ptmc_init. */
+int ptmc_set_separated_volume(ptmc_ctx* c, int on);
 /* Optional initial step sizes, 2 per slot (atom, volume); default 0.1, 0.1
  * (src/MCStates.jl:104). */
 int ptmc_set_max_displ(ptmc_ctx* c, int run, const double* max_displ);
+/* Optional initial separated-volume step sizes max_displ[3:4], 2 per slot
+ * (xy, z); default 0.1, 0.1 (src/MCStates.jl:101). */
+int ptmc_set_max_displ_sep(ptmc_ctx* c, int run, const double* max_displ_sep);
 /* Radial distribution sampling, the rdfsave option of ptmc_run! (update_rdf!,
  * src/Sampling.jl:282-316): every 1000th production cycle each slot's
  * configuration adds its pair distances to 5 n_bin bins of width
@@ -157,6 +178,11 @@ int ptmc_get_output(ptmc_ctx* c, int run, ptmc_output* out);
 int ptmc_get_states(ptmc_ctx* c, int run, double* xyz, double* en_tot,
                     double* box, double* max_displ, long long* counts,
                     double* ham);
+/* Slot-ordered box state of RectangularBC / RhombicBC runs: box_height [R],
+ * max_displ_sep [2R] = max_displ[3:4], counts_sep [R][4] = count_vol_xy[1:2],
+ * count_vol_z[1:2] (src/MCStates.jl:33-47).  NULL skips an array. */
+int ptmc_get_box_states(ptmc_ctx* c, int run, double* box_height,
+                        double* max_displ_sep, long long* counts_sep);
 int ptmc_get_stats(ptmc_ctx* c, ptmc_stats* s);
 
 /* --- checkpoint / resume (src/ReadSave.jl:93-218, 330-481) --- */

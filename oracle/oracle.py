@@ -14,7 +14,7 @@ LIB = os.path.join(HERE, "_build", "libptmc_oracle.so")
 SRC = os.path.join(HERE, "ptmc_oracle.cpp")
 
 POT_ELJ, POT_ELJEVEN, POT_EAM, POT_NN = 0, 1, 2, 3
-BC_SPHERE, BC_CUBIC = 0, 1
+BC_SPHERE, BC_CUBIC, BC_RECT, BC_RHOMBIC = 0, 1, 2, 3
 NVT, NPT = 0, 1
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -67,6 +67,18 @@ def lib():
         L.orc_distance2.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_double]
         L.orc_lrc.restype = ctypes.c_double
         L.orc_lrc.argtypes = [ctypes.c_int, ctypes.c_double, _dp, ctypes.c_int]
+        L.orc_distance2_box.restype = ctypes.c_double
+        L.orc_distance2_box.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_box_rcut.restype = ctypes.c_double
+        L.orc_box_rcut.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_box_volume.restype = ctypes.c_double
+        L.orc_box_volume.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_elj_config_energy_box.restype = ctypes.c_double
+        L.orc_elj_config_energy_box.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_int]
+        L.orc_set_box.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, _dp]
+        L.orc_get_box.argtypes = [ctypes.c_void_p, _dp, _dp, _lp, _lp]
         L.orc_eam_config_energy.restype = ctypes.c_double
         L.orc_eam_config_energy.argtypes = [_dp, ctypes.c_int] + [ctypes.c_double] * 4
         L.orc_elj_config_energy.restype = ctypes.c_double
@@ -119,6 +131,26 @@ def dimer_energy(kind, c, r2):
 def distance2(a, b, bc=BC_SPHERE, L=0.0):
     a, b = _d(a), _d(b)
     return lib().orc_distance2(P(a), P(b), bc, float(L))
+
+
+def distance2_box(a, b, bc, L, H):
+    """distance2 for a box of length L and height H (RectangularBC, RhombicBC)."""
+    a, b = _d(a), _d(b)
+    return lib().orc_distance2_box(P(a), P(b), bc, float(L), float(H))
+
+
+def box_rcut(bc, L, H):
+    return lib().orc_box_rcut(bc, float(L), float(H))
+
+
+def box_volume(bc, L, H):
+    return lib().orc_box_volume(bc, float(L), float(H))
+
+
+def elj_config_energy_box(xyz, kind, c, bc, L, H, cut=True):
+    x, c = _d(xyz), _d(c)
+    return lib().orc_elj_config_energy_box(P(x), len(x), kind, P(c), len(c), bc, float(L),
+                                           float(H), int(bool(cut)))
 
 
 def lrc(N, rc2, c):
@@ -199,6 +231,24 @@ class Run:
         if not h:
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         self.h = h
+
+    def set_box(self, height, separated=False, max_displ_sep=None):
+        """RectangularBC / RhombicBC: box height (bc_param is the length),
+        NPT separated volume moves, initial max_displ[3:4] (2 per slot)."""
+        md = None if max_displ_sep is None else _d(max_displ_sep)
+        self._mds = md
+        _check(lib().orc_set_box(self.h, float(height), int(bool(separated)),
+                                 None if md is None else P(md)))
+
+    def box(self):
+        """walker heights [R]; per slot max_displ[3:4] [R,2], count_vol_xy [R,2], count_vol_z [R,2]"""
+        R = self.R
+        h, md = np.zeros(R), np.zeros(2 * R)
+        cxy, cz = np.zeros(2 * R, dtype=np.int64), np.zeros(2 * R, dtype=np.int64)
+        lp = lambda a: a.ctypes.data_as(_lp)
+        _check(lib().orc_get_box(self.h, P(h), P(md), lp(cxy), lp(cz)))
+        return dict(height=h, max_displ_sep=md.reshape(R, 2), count_xy=cxy.reshape(R, 2),
+                    count_z=cz.reshape(R, 2))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -15,6 +15,7 @@
 // walker<->slot mapping, which is the same state transition.
 #include "ptmc_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -85,6 +86,47 @@ inline double dist2_cub(const double* a, const double* b, double L) {
   double bz = b[2] + L * std::nearbyint((a[2] - b[2]) / L);
   return dot3(a[0] - bx, a[1] - by, a[2] - bz);
 }
+// RectangularBC minimum image: side L in x and y, height H in z
+// (src/Configurations.jl:121-126)
+inline double dist2_rect(const double* a, const double* b, double L, double H) {
+  double bx = b[0] + L * std::nearbyint((a[0] - b[0]) / L);
+  double by = b[1] + L * std::nearbyint((a[1] - b[1]) / L);
+  double bz = b[2] + H * std::nearbyint((a[2] - b[2]) / H);
+  return dot3(a[0] - bx, a[1] - by, a[2] - bz);
+}
+// RhombicBC minimum image (src/Configurations.jl:110-120): y on the rhombus
+// height sqrt(3)/2 L, x on the sheared axis, z as the rectangular box.  3^0.5
+// is the double nearest sqrt(3) (Julia's pow is within 0.05 ulp of it there).
+const double S3 = 1.7320508075688772;
+inline double dist2_rhb(const double* a, const double* b, double L, double H) {
+  const double hy = S3 / 2 * L, is3 = 1 / S3;
+  double by = b[1] + hy * std::nearbyint((a[1] - b[1]) / hy);
+  double bx = ((b[0] - b[1] / S3) + L * std::nearbyint(((a[0] - b[0]) - is3 * (a[1] - b[1])) / L)) +
+              is3 * by;
+  double bz = b[2] + H * std::nearbyint((a[2] - b[2]) / H);
+  return dot3(a[0] - bx, a[1] - by, a[2] - bz);
+}
+inline double dist2_bc(int bc, const double* a, const double* b, double L, double H) {
+  switch (bc) {
+    case ORC_BC_CUBIC: return dist2_cub(a, b, L);
+    case ORC_BC_RECT: return dist2_rect(a, b, L, H);
+    case ORC_BC_RHOMBIC: return dist2_rhb(a, b, L, H);
+    default: return dist2_sph(a, b);
+  }
+}
+// get_r_cut (src/Ensembles.jl:118-155): squared cut-off implied by the box
+inline double box_rcut(int bc, double L, double H) {
+  if (bc == ORC_BC_RHOMBIC) return std::min(L * L * 3 / 16, H * H / 4);
+  if (bc == ORC_BC_RECT) return std::min(L * L / 4, H * H / 4);
+  if (bc == ORC_BC_CUBIC) return L * L / 4;
+  return 0.0;
+}
+// get_volume (src/Configurations.jl:246-256)
+inline double box_volume(int bc, double L, double H) {
+  if (bc == ORC_BC_RHOMBIC) return L * L * H * S3 / 2;
+  if (bc == ORC_BC_RECT) return L * L * H;
+  return L * L * L;
+}
 
 // ---------------------------------------------------------------- potentials
 struct SF {
@@ -152,9 +194,11 @@ double dimer_atom(const Pot& p, int i, const double* d2, int N, bool cut,
   }
   return s;
 }
-// dimer_energy_config (EnergyEvaluation.jl:378-420)
+// dimer_energy_config (EnergyEvaluation.jl:378-473); with a cut-off the long-range
+// correction, which assumes a cube, is rescaled for the other boxes
+// (:444, :469-472)
 double dimer_config(const Pot& p, const double* d2, int N, bool cut,
-                    double rc2) {
+                    double rc2, int bc = ORC_BC_CUBIC, double L = 0, double H = 0) {
   double e = 0.0;
   for (int i = 0; i < N; ++i)
     for (int j = i + 1; j < N; ++j) {
@@ -162,7 +206,12 @@ double dimer_config(const Pot& p, const double* d2, int N, bool cut,
       if (cut && !(x <= rc2)) continue;
       e += dimer(p, x);
     }
-  if (cut) e = e + lrc_even(N, rc2, p.c.data(), (int)p.c.size());
+  if (cut) {
+    double l = lrc_even(N, rc2, p.c.data(), (int)p.c.size());
+    if (bc == ORC_BC_RHOMBIC) l = l * 3 / 4 * L / H;
+    else if (bc == ORC_BC_RECT) l = L < H ? l * L / H : l * (H * H) / (L * L);
+    e = e + l;
+  }
   return e;
 }
 // invrexp (EnergyEvaluation.jl:1088-1095)
@@ -370,7 +419,8 @@ struct orc_run {
   std::vector<double> pos;    // R*N*3
   std::vector<double> d2;     // R*N*N
   std::vector<double> en;     // R
-  std::vector<double> box;    // R (cubic side)
+  std::vector<double> box;    // R (cubic side, box_length of the other boxes)
+  std::vector<double> boxh;   // R (box_height of RectangularBC / RhombicBC)
   std::vector<double> rcut2;  // R
   std::vector<double> comp;   // R*N*2 (EAM)
   std::vector<double> G;      // R*nsf*N (NN, column per atom)
@@ -380,6 +430,11 @@ struct orc_run {
   // slot-bound
   std::vector<double> T, beta, maxd, ham, max_box;  // R, R, 2R, 2R, R
   std::vector<long> cnt_atom, cnt_vol, cnt_exc;     // 2R each
+  // separated volume moves (NPT separated_volume): max_displ[3:4] (xy, z),
+  // max_boxheight, count_vol_xy, count_vol_z (MCStates.jl:33-47)
+  bool sep = false;
+  std::vector<double> maxd_sep, max_boxh;          // 2R, R
+  std::vector<long> cnt_xy, cnt_z;                 // 2R each
   std::vector<int> wos;                             // walker of slot
   uint64_t run_ctr = 0;
   // delayed acceptance (NN only): surrogate parameters, stage counters
@@ -419,8 +474,7 @@ void build_d2(orc_run* r, int w) {
   double* d = r->D(w);
   for (int i = 0; i < N; ++i)
     for (int j = i + 1; j < N; ++j) {
-      double x = r->bc == ORC_BC_CUBIC ? dist2_cub(p + 3 * i, p + 3 * j, r->box[w])
-                                       : dist2_sph(p + 3 * i, p + 3 * j);
+      double x = dist2_bc(r->bc, p + 3 * i, p + 3 * j, r->box[w], r->boxh[w]);
       d[(size_t)i * N + j] = x;
       d[(size_t)j * N + i] = x;
     }
@@ -512,7 +566,7 @@ double init_energy(orc_run* r, int w) {
     return nn_energy(r, &r->G[(size_t)w * nsf(r) * N], &r->eatom[(size_t)w * N]);
   }
   bool cut = r->ens == ORC_NPT;
-  return dimer_config(p, r->D(w), N, cut, r->rcut2[w]);
+  return dimer_config(p, r->D(w), N, cut, r->rcut2[w], r->bc, r->box[w], r->boxh[w]);
 }
 
 // ---------------------------------------------------------------- moves
@@ -558,14 +612,23 @@ int atom_move(orc_run* r, int w, int slot, int i) {
         if (count == 100) return fail("Error: too many moves out of binding sphere");
       }
     }
-  } else {
-    double L = r->box[w];
-    for (int k = 0; k < 3; ++k) t[k] -= L * std::nearbyint(t[k] / L);
+  } else if (r->bc == ORC_BC_RHOMBIC) {  // rhombic wrap (MCMoves.jl:66-83)
+    double L = r->box[w], H = r->boxh[w];
+    double ky = std::nearbyint((t[1] - L * S3 / 4) / (L * S3 / 2));
+    double sx = L * std::nearbyint((t[0] - t[1] / S3 - L / 2) / L) + L / 2 * ky;
+    double sy = L * S3 / 2 * ky;
+    double sz = H * std::nearbyint((t[2] - H / 2) / H);
+    t[0] -= sx;
+    t[1] -= sy;
+    t[2] -= sz;
+  } else {  // cubic / rectangular wrap (MCMoves.jl:50-64, 85-98)
+    double L = r->box[w], H = r->bc == ORC_BC_RECT ? r->boxh[w] : L;
+    t[0] -= L * std::nearbyint(t[0] / L);
+    t[1] -= L * std::nearbyint(t[1] / L);
+    t[2] -= H * std::nearbyint(t[2] / H);
   }
   double* row = r->trial_row.data();
-  for (int j = 0; j < N; ++j)
-    row[j] = r->bc == ORC_BC_CUBIC ? dist2_cub(t, p + 3 * j, r->box[w])
-                                   : dist2_sph(t, p + 3 * j);
+  for (int j = 0; j < N; ++j) row[j] = dist2_bc(r->bc, t, p + 3 * j, r->box[w], r->boxh[w]);
   row[i] = 0.0;
   const double* old = r->D(w) + (size_t)i * N;
   const Pot& pot = r->pot;
@@ -703,34 +766,99 @@ int atom_move(orc_run* r, int w, int slot, int i) {
   return 0;
 }
 
-// volume move: volume_change_uniform (MCMoves.jl:277-287) with the NPT
-// energy (MCRun.jl:76-85) and metropolis_condition NPT (Exchange.jl:58-70)
+// volume move: volume_change (MCMoves.jl:350-356) with the NPT energy
+// (MCRun.jl:76-85) and metropolis_condition NPT (Exchange.jl:58-70).
+// Uniform (volume_change_uniform, :277-287): positions and box scaled by
+// exp((u - 1/2) max_displ[2])^(1/3), distances scaled by scale^2.  Separated
+// (volume_change_separated, :298-343): rand(1:6) picks z (1), xy (2-3) or all
+// directions (4-6); the trial distance matrix is recomputed from the scaled
+// positions in every case.
 int volume_move(orc_run* r, int w, int slot) {
   int N = r->N;
-  double L = r->box[w];
-  double u = r->draw(w);
-  double scale = std::pow(std::exp((u - 0.5) * r->maxd[2 * slot + 1]), 1.0 / 3.0);
-  if (L >= r->max_box[slot] && scale > 1.0) scale = 1.0;
-  double Ln = scale * L;
-  double rc_new = Ln * Ln / 4;
-  double s2 = scale * scale;
+  const double L = r->box[w], H = r->boxh[w];
+  int xy_or_z = 0;
+  double fx = 1.0, fz = 1.0;  // trial factors of x, y and of z
+  double Ln = L, Hn = H;
+  const bool rect = r->bc == ORC_BC_RECT || r->bc == ORC_BC_RHOMBIC;
+  auto change_xyz = [&]() {  // volume_change_xyz (:169-177)
+    double u = r->draw(w);
+    double scale = std::pow(std::exp((u - 0.5) * r->maxd[2 * slot + 1]), 1.0 / 3.0);
+    if (L >= r->max_box[slot] && scale > 1.0) scale = 1.0;
+    fx = fz = scale;
+    Ln = scale * L;
+    Hn = rect ? scale * H : Ln;
+  };
+  if (r->sep) {
+    const double lh = r->max_box[slot] / r->max_boxh[slot];  // lh_ratio (MCStates.jl:103)
+    int ra = randint(r->draw(w), 6) + 1;
+    if (ra == 1) {  // volume_change_z (:257-271)
+      xy_or_z = 2;
+      double u = r->draw(w);
+      double scale = std::exp((u - 0.5) * r->maxd_sep[2 * slot + 1]);
+      if (L / H <= lh * 1.1 && scale > 1.0) scale = 1 / scale;
+      else if (L / H >= lh * 0.909 && scale < 1.0) scale = 1 / scale;
+      if (H >= r->max_boxh[slot] && scale > 1.0) scale = 1 / scale;
+      fz = scale;
+      Hn = H * scale;
+    } else if (ra <= 3) {  // volume_change_xy (:231-247)
+      xy_or_z = 1;
+      double u = r->draw(w);
+      double scale = std::pow(std::exp((u - 0.5) * r->maxd_sep[2 * slot]), 0.5);
+      if (L / H >= lh * 1.1 && scale > 1.0) scale = 1 / scale;
+      else if (L / H <= lh * 0.909 && scale < 1.0) scale = 1 / scale;
+      if (L >= r->max_box[slot] && scale > 1.0) scale = 1 / scale;
+      fx = scale;
+      Ln = L * scale;
+    } else {
+      change_xyz();
+    }
+  } else {
+    change_xyz();
+  }
+  const double rc_new = box_rcut(r->bc, Ln, Hn);
   std::vector<double>& nd = r->sc_d2;
-  const double* d = r->D(w);
-  for (size_t k = 0; k < (size_t)N * N; ++k) nd[k] = d[k] * s2;
-  double new_en = dimer_config(r->pot, nd.data(), N, true, rc_new);
-  double Vn = Ln * Ln * Ln, Vo = L * L * L;
+  std::vector<double>& np = r->sc_pos;
+  const double* p = r->P(w);
+  if (r->sep) {  // get_distance2_mat! of the trial configuration
+    np.resize((size_t)3 * N);
+    for (int a = 0; a < N; ++a) {
+      np[3 * a] = p[3 * a] * fx;
+      np[3 * a + 1] = p[3 * a + 1] * fx;
+      np[3 * a + 2] = p[3 * a + 2] * fz;
+    }
+    for (int i = 0; i < N; ++i) {
+      nd[(size_t)i * N + i] = 0.0;
+      for (int j = i + 1; j < N; ++j) {
+        double x = dist2_bc(r->bc, &np[3 * i], &np[3 * j], Ln, Hn);
+        nd[(size_t)i * N + j] = x;
+        nd[(size_t)j * N + i] = x;
+      }
+    }
+  } else {  // dist2_mat .* scale^2
+    const double s2 = fx * fx;
+    const double* d = r->D(w);
+    for (size_t k = 0; k < (size_t)N * N; ++k) nd[k] = d[k] * s2;
+  }
+  double new_en = dimer_config(r->pot, nd.data(), N, true, rc_new, r->bc, Ln, Hn);
+  double Vn = box_volume(r->bc, Ln, Hn), Vo = box_volume(r->bc, L, H);
   double dh = (new_en - r->en[w]) + r->pressure * (Vn - Vo);
   double prob = std::exp(-dh * r->beta[slot] + (double)N * std::log(Vn / Vo));
   if (prob > 1) prob = 1.0;
   double ua = r->draw(w);
   if (prob >= ua) {  // swap_config_v! (swap_config.jl:113-141)
-    double* p = r->P(w);
-    for (int k = 0; k < 3 * N; ++k) p[k] = scale * p[k];
+    double* pw = r->P(w);
+    if (r->sep) {
+      std::memcpy(pw, np.data(), sizeof(double) * 3 * N);
+    } else {
+      for (int k = 0; k < 3 * N; ++k) pw[k] = fx * pw[k];
+    }
     r->box[w] = Ln;
+    r->boxh[w] = Hn;
     std::memcpy(r->D(w), nd.data(), sizeof(double) * N * N);
     r->en[w] = new_en;
-    r->cnt_vol[2 * slot] += 1;
-    r->cnt_vol[2 * slot + 1] += 1;
+    std::vector<long>& cv = xy_or_z == 0 ? r->cnt_vol : xy_or_z == 1 ? r->cnt_xy : r->cnt_z;
+    cv[2 * slot] += 1;
+    cv[2 * slot + 1] += 1;
     r->rcut2[w] = rc_new;
   }
   return 0;
@@ -756,9 +884,8 @@ int cycle(orc_run* r, long index) {
     int w1 = r->wos[k], w2 = r->wos[k + 1];
     double e1 = r->en[w1], e2 = r->en[w2];
     if (r->ens == ORC_NPT) {
-      double L1 = r->box[w1], L2 = r->box[w2];
-      e1 = e1 + r->pressure * (L1 * L1 * L1);
-      e2 = e2 + r->pressure * (L2 * L2 * L2);
+      e1 = e1 + r->pressure * box_volume(r->bc, r->box[w1], r->boxh[w1]);
+      e2 = e2 + r->pressure * box_volume(r->bc, r->box[w2], r->boxh[w2]);
     }
     double acc = std::exp((r->beta[k] - r->beta[k + 1]) * (e1 - e2));
     if (acc > 1.0) acc = 1.0;
@@ -776,11 +903,22 @@ int cycle(orc_run* r, long index) {
       if (acc < r->min_acc) r->maxd[2 * s] *= 0.9;
       else if (acc > r->max_acc) r->maxd[2 * s] *= 1.1;
       r->cnt_atom[2 * s + 1] = 0;
-      if (r->ens == ORC_NPT) {
+      if (r->ens == ORC_NPT && !r->sep) {
         double av = (double)r->cnt_vol[2 * s + 1] / (double)(r->n_adjust * 1);
         if (av < r->min_acc) r->maxd[2 * s + 1] *= 0.9;
         else if (av > r->max_acc) r->maxd[2 * s + 1] *= 1.1;
         r->cnt_vol[2 * s + 1] = 0;
+      } else if (r->ens == ORC_NPT) {  // separated: all, xy, z (Exchange.jl:221-244)
+        auto adapt = [&](std::vector<long>& cv, double& md, double den) {
+          double av = (double)cv[2 * s + 1] / den;
+          if (av < r->min_acc) md *= 0.9;
+          else if (av > r->max_acc) md *= 1.1;
+          cv[2 * s + 1] = 0;
+        };
+        const double nu = (double)(r->n_adjust * 1);
+        adapt(r->cnt_vol, r->maxd[2 * s + 1], nu * 1 / 2);
+        adapt(r->cnt_xy, r->maxd_sep[2 * s], nu * 1 / 3);
+        adapt(r->cnt_z, r->maxd_sep[2 * s + 1], nu / 6);
       }
     }
   }
@@ -818,12 +956,17 @@ void sample(orc_run* r, long idx) {
     int w = r->wos[s];
     double e = r->en[w];
     if (r->ens == ORC_NPT) {
-      double L = r->box[w];
-      double H = e + r->pressure * (L * L * L);  // update_energy_tot :35-46
+      double L = r->box[w], Hb = r->boxh[w];
+      double H = e + r->pressure * box_volume(r->bc, L, Hb);  // update_energy_tot :35-46
       r->ham[2 * s] += H;
       r->ham[2 * s + 1] += H * H;
-      double he = std::floor((e - r->en_min) / r->dE) + 1;  // :98-110
-      double hv = std::floor((L * L * L - r->v_min) / r->dV) + 1;
+      double he = std::floor((e - r->en_min) / r->dE) + 1;  // :98-130
+      // the volume of the histogram index: L^3, L^2 H, and for the rhombic
+      // box L^2 * 3 H^0.5 / 2 as written at Sampling.jl:119-121
+      double vh = r->bc == ORC_BC_RECT      ? L * L * Hb
+                  : r->bc == ORC_BC_RHOMBIC ? L * L * (3 * std::sqrt(Hb)) / 2
+                                            : L * L * L;
+      double hv = std::floor((vh - r->v_min) / r->dV) + 1;
       long ie = hist_index(he, r->n_bin), iv = hist_index(hv, r->n_bin);
       r->ev_hist[((size_t)s * nb + (ie - 1)) * nb + (iv - 1)] += 1;
     } else {
@@ -860,7 +1003,7 @@ orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
     fail("orc_create: need N >= 2 and R >= 1");
     return nullptr;
   }
-  if (ensemble == ORC_NPT && bc_kind != ORC_BC_CUBIC) {
+  if (ensemble == ORC_NPT && bc_kind == ORC_BC_SPHERE) {
     fail("SphericalBC cannot be used in an NPT ensemble.");  // Ensembles.jl:192
     return nullptr;
   }
@@ -882,17 +1025,22 @@ orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
   r->d2.assign((size_t)R * N * N, 0.0);
   r->en.assign(R, 0.0);
   r->box.assign(R, bc_param);
-  r->rcut2.assign(R, bc_kind == ORC_BC_CUBIC ? bc_param * bc_param / 4 : 0.0);
+  r->boxh.assign(R, bc_param);
+  r->rcut2.assign(R, box_rcut(bc_kind, bc_param, bc_param));
   r->ctr.assign(R, 0);
   r->T.assign(T, T + R);
   r->beta.resize(R);
   for (int s = 0; s < R; ++s) r->beta[s] = 1.0 / (kB * T[s]);  // InputParams.jl:93
   r->maxd.assign(max_displ, max_displ + 2 * R);
   r->max_box.assign(R, bc_param * 1.8);  // max_length (MCStates.jl:66-75)
+  r->max_boxh.assign(R, bc_param * 1.8);  // max_height (MCStates.jl:79-87)
+  r->maxd_sep.assign(2 * R, 0.1);         // max_displ[3:4] (MCStates.jl:101)
   r->ham.assign(2 * R, 0.0);
   r->cnt_atom.assign(2 * R, 0);
   r->cnt_vol.assign(2 * R, 0);
   r->cnt_exc.assign(2 * R, 0);
+  r->cnt_xy.assign(2 * R, 0);
+  r->cnt_z.assign(2 * R, 0);
   r->wos.resize(R);
   for (int s = 0; s < R; ++s) r->wos[s] = s;
   r->trial_row.resize(N);
@@ -904,6 +1052,32 @@ orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
 }
 
 void orc_destroy(orc_run* r) { delete r; }
+
+int orc_set_box(orc_run* r, double height, int separated, const double* max_displ_sep) {
+  if (r->inited) return fail("orc_set_box: call before orc_init");
+  if (r->bc != ORC_BC_RECT && r->bc != ORC_BC_RHOMBIC) {
+    if (separated) return fail("separated volume moves need a RectangularBC or RhombicBC");
+    return 0;
+  }
+  if (!(height > 0)) return fail("box height must be positive");
+  if (separated && r->ens != ORC_NPT) return fail("separated volume moves are NPT moves");
+  for (int w = 0; w < r->R; ++w) {
+    r->boxh[w] = height;
+    r->rcut2[w] = box_rcut(r->bc, r->box[w], height);
+    r->max_boxh[w] = height * 1.8;
+  }
+  r->sep = separated != 0;
+  if (max_displ_sep) r->maxd_sep.assign(max_displ_sep, max_displ_sep + 2 * r->R);
+  return 0;
+}
+int orc_get_box(orc_run* r, double* height, double* max_displ_sep, long* count_xy, long* count_z) {
+  int R = r->R;
+  if (height) std::memcpy(height, r->boxh.data(), sizeof(double) * R);
+  if (max_displ_sep) std::memcpy(max_displ_sep, r->maxd_sep.data(), sizeof(double) * 2 * R);
+  if (count_xy) std::memcpy(count_xy, r->cnt_xy.data(), sizeof(long) * 2 * R);
+  if (count_z) std::memcpy(count_z, r->cnt_z.data(), sizeof(long) * 2 * R);
+  return 0;
+}
 
 int orc_set_pot_elj(orc_run* r, const double* c, int K, int even) {
   if (K < 1) return fail("ELJ needs at least one coefficient");
@@ -998,6 +1172,8 @@ int orc_equilibrate(orc_run* r, int eq_cycles) {
     r->cnt_atom[k] = 0;
     r->cnt_vol[k] = 0;
     r->cnt_exc[k] = 0;
+    r->cnt_xy[k] = 0;
+    r->cnt_z[k] = 0;
   }
   // initialise_histograms! (Sampling.jl:141-194)
   r->en_min = eb[0];
@@ -1005,19 +1181,20 @@ int orc_equilibrate(orc_run* r, int eq_cycles) {
   r->dE = (r->en_max - r->en_min) / (r->n_bin - 1);
   int nb = r->n_bin + 2;
   r->en_hist.assign((size_t)r->R * nb, 0.0);
+  const double b = r->box[r->wos[0]], bh = r->boxh[r->wos[0]];  // the first state's box
   if (r->ens == ORC_NPT) {
-    double L = r->box[r->wos[0]];
-    double V = L * L * L;
+    const double V = box_volume(r->bc, b, bh);
     r->v_min = V * 0.8;
     r->v_max = V * 2.0;
     r->dV = (r->v_max - r->v_min) / r->n_bin;
     r->ev_hist.assign((size_t)r->R * nb * nb, 0.0);
   }
-  {  // delta_r2 (Sampling.jl:151 sphere, :185 cube) of the first state's boundary
-    double b = r->box[r->wos[0]];
-    r->dr2 = r->bc == ORC_BC_CUBIC ? 3.0 / 4.0 * (b * b) / r->n_bin / 5 : 4 * (b * b) / r->n_bin / 5;
-    r->rdf.assign((size_t)r->R * 5 * r->n_bin, 0.0);
-  }
+  // delta_r2 (Sampling.jl:151 sphere, :185 cube, :210 rhombic, :240 rectangular)
+  if (r->bc == ORC_BC_CUBIC) r->dr2 = 3.0 / 4.0 * (b * b) / r->n_bin / 5;
+  else if (r->bc == ORC_BC_RHOMBIC) r->dr2 = (3.0 / 8.0 * (b * b) + 1.0 / 4.0 * (bh * bh)) / r->n_bin / 5;
+  else if (r->bc == ORC_BC_RECT) r->dr2 = (1.0 / 2.0 * (b * b) + 1.0 / 4.0 * (bh * bh)) / r->n_bin / 5;
+  else r->dr2 = 4 * (b * b) / r->n_bin / 5;
+  r->rdf.assign((size_t)r->R * 5 * r->n_bin, 0.0);
   return 0;
 }
 
@@ -1102,8 +1279,13 @@ double orc_dimer_energy(int kind, const double* c, int K, double r2) {
   return kind == ORC_POT_ELJ ? elj_all(c, K, r2) : elj_even(c, K, r2);
 }
 double orc_distance2(const double* a, const double* b, int bc_kind, double L) {
-  return bc_kind == ORC_BC_CUBIC ? dist2_cub(a, b, L) : dist2_sph(a, b);
+  return dist2_bc(bc_kind, a, b, L, L);
 }
+double orc_distance2_box(const double* a, const double* b, int bc_kind, double L, double H) {
+  return dist2_bc(bc_kind, a, b, L, H);
+}
+double orc_box_rcut(int bc_kind, double L, double H) { return box_rcut(bc_kind, L, H); }
+double orc_box_volume(int bc_kind, double L, double H) { return box_volume(bc_kind, L, H); }
 double orc_lrc(int N, double r_cut2, const double* c, int K) {
   return lrc_even(N, r_cut2, c, K);
 }
@@ -1128,11 +1310,23 @@ double orc_elj_config_energy(const double* xyz, int N, int kind,
   std::vector<double> d((size_t)N * N, 0.0);
   for (int i = 0; i < N; ++i)
     for (int j = i + 1; j < N; ++j) {
-      double x = bc_kind == ORC_BC_CUBIC ? dist2_cub(xyz + 3 * i, xyz + 3 * j, L)
-                                         : dist2_sph(xyz + 3 * i, xyz + 3 * j);
+      double x = dist2_bc(bc_kind, xyz + 3 * i, xyz + 3 * j, L, L);
       d[(size_t)i * N + j] = d[(size_t)j * N + i] = x;
     }
   return dimer_config(p, d.data(), N, bc_kind == ORC_BC_CUBIC, r_cut2);
+}
+double orc_elj_config_energy_box(const double* xyz, int N, int kind, const double* c, int K,
+                                 int bc_kind, double L, double H, int cut) {
+  Pot p;
+  p.kind = kind;
+  p.c.assign(c, c + K);
+  std::vector<double> d((size_t)N * N, 0.0);
+  for (int i = 0; i < N; ++i)
+    for (int j = i + 1; j < N; ++j) {
+      double x = dist2_bc(bc_kind, xyz + 3 * i, xyz + 3 * j, L, H);
+      d[(size_t)i * N + j] = d[(size_t)j * N + i] = x;
+    }
+  return dimer_config(p, d.data(), N, cut != 0, box_rcut(bc_kind, L, H), bc_kind, L, H);
 }
 void orc_tempgrid(double ti, double tf, int R, int tdistr, double* T, double* beta) {
   // TempGrid (InputParams.jl:77-95)

@@ -36,6 +36,8 @@ typedef struct orc_run orc_run;
 /* boundary kinds (src/BoundaryConditions.jl) */
 #define ORC_BC_SPHERE 0
 #define ORC_BC_CUBIC 1
+#define ORC_BC_RECT 2      /* RectangularBC :89 */
+#define ORC_BC_RHOMBIC 3   /* RhombicBC     :110 */
 /* ensembles (src/Ensembles.jl) */
 #define ORC_NVT 0
 #define ORC_NPT 1
@@ -50,6 +52,13 @@ orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
                     int mc_sample, double min_acc, double max_acc,
                     double exch_prob, uint64_t seed, int run_index);
 void orc_destroy(orc_run* r);
+/* RectangularBC / RhombicBC (bc_param of orc_create is box_length): box
+ * height, NPT separated volume moves and the initial max_displ[3:4] (2 per
+ * slot: xy, z; NULL = 0.1).  Before orc_init. */
+int orc_set_box(orc_run* r, double height, int separated, const double* max_displ_sep);
+/* walker box heights [R]; slot max_displ[3:4] [2R]; count_vol_xy, count_vol_z [2R] */
+int orc_get_box(orc_run* r, double* height, double* max_displ_sep, long* count_xy,
+                long* count_z);
 const char* orc_last_error(void);
 
 int orc_set_pot_elj(orc_run* r, const double* c, int K, int even);
@@ -94,6 +103,14 @@ double orc_dimer_energy(int kind, const double* c, int K, double r2);
 double orc_distance2(const double* a, const double* b, int bc_kind,
                      double L);
 double orc_lrc(int N, double r_cut2, const double* c, int K);
+/* distance2, get_r_cut, get_volume of a box with length L and height H */
+double orc_distance2_box(const double* a, const double* b, int bc_kind, double L, double H);
+double orc_box_rcut(int bc_kind, double L, double H);
+double orc_box_volume(int bc_kind, double L, double H);
+/* dimer_energy_config over all pairs; cut != 0 applies get_r_cut and the
+ * box-scaled long-range correction */
+double orc_elj_config_energy_box(const double* xyz, int N, int kind, const double* c, int K,
+                                 int bc_kind, double L, double H, int cut);
 double orc_eam_config_energy(const double* xyz, int N, double n, double m,
                              double ean, double ecam);
 double orc_elj_config_energy(const double* xyz, int N, int kind,

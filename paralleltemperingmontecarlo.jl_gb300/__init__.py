@@ -28,12 +28,13 @@ from ._capi import PTMCError
 
 kB = 3.16681196e-6  # Hartree/K, src/InputParams.jl:19
 
-__all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "Config", "NVT", "NPT",
+__all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "RectangularBC", "RhombicBC",
+           "Config", "NVT", "NPT",
            "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "RuNNerPotential",
            "Output", "MCState", "PairSurrogate",
            "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
            "multihistogram", "postprocess",
-           "distance2", "get_distance2_mat", "get_volume", "PTMCError"]
+           "distance2", "get_distance2_mat", "get_volume", "get_r_cut", "PTMCError"]
 
 
 # ------------------------------------------------------------------ parameters
@@ -97,6 +98,25 @@ class CubicBC:
     box_length: float
 
 
+@dataclass
+class RectangularBC:
+    """RectangularBC(box_length, box_height) (src/BoundaryConditions.jl:80-92):
+    square side box_length in x and y, box_height in z."""
+    box_length: float
+    box_height: float
+
+
+@dataclass
+class RhombicBC:
+    """RhombicBC(box_length, box_height) (src/BoundaryConditions.jl:95-116): a
+    rhombus of side box_length (60 degrees) in the xy plane, box_height in z."""
+    box_length: float
+    box_height: float
+
+
+SQRT3 = 1.7320508075688772  # 3^0.5
+
+
 class Config:
     """Config(positions, boundary_condition) (src/Configurations.jl:42-56)."""
 
@@ -109,11 +129,23 @@ class Config:
 
 
 def distance2(a, b, bc=None):
-    """distance2 (src/Configurations.jl:101-109), with CubicBC minimum image."""
+    """distance2 (src/Configurations.jl:101-126) with the minimum image of
+    CubicBC, RectangularBC and RhombicBC."""
     a, b = np.asarray(a, float), np.asarray(b, float)
     if isinstance(bc, CubicBC):
         L = bc.box_length
         b = b + L * np.round((a - b) / L)
+    elif isinstance(bc, RectangularBC):
+        L, H = bc.box_length, bc.box_height
+        b = b + np.array([L, L, H]) * np.round((a - b) / np.array([L, L, H]))
+    elif isinstance(bc, RhombicBC):
+        L, H = bc.box_length, bc.box_height
+        hy = SQRT3 / 2 * L
+        by = b[1] + hy * np.round((a[1] - b[1]) / hy)
+        bx = (b[0] - b[1] / SQRT3 + L * np.round(((a[0] - b[0]) - 1 / SQRT3 * (a[1] - b[1])) / L)
+              + 1 / SQRT3 * by)
+        bz = b[2] + H * np.round((a[2] - b[2]) / H)
+        b = np.array([bx, by, bz])
     d = a - b
     return float((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
 
@@ -133,7 +165,35 @@ def get_volume(bc):
     """get_volume (src/Configurations.jl:246-256)."""
     if isinstance(bc, CubicBC):
         return bc.box_length ** 3
+    if isinstance(bc, RhombicBC):
+        return bc.box_length * bc.box_length * bc.box_height * SQRT3 / 2
+    if isinstance(bc, RectangularBC):
+        return bc.box_length * bc.box_length * bc.box_height
     raise TypeError("get_volume is defined for periodic boxes")
+
+
+def get_r_cut(bc):
+    """get_r_cut (src/Ensembles.jl:118-155): the squared cut-off of a periodic box."""
+    if isinstance(bc, CubicBC):
+        return bc.box_length * bc.box_length / 4
+    if isinstance(bc, RhombicBC):
+        L, H = bc.box_length, bc.box_height
+        return min(L * L * 3 / 16, H * H / 4)
+    if isinstance(bc, RectangularBC):
+        L, H = bc.box_length, bc.box_height
+        return min(L * L / 4, H * H / 4)
+    raise TypeError("get_r_cut is defined for periodic boxes")
+
+
+def _bc_kind(bc):
+    """(C ABI kind, box_length or radius, box_height) of a boundary condition."""
+    if isinstance(bc, CubicBC):
+        return _capi.BC_CUBIC, bc.box_length, bc.box_length
+    if isinstance(bc, RectangularBC):
+        return _capi.BC_RECTANGULAR, bc.box_length, bc.box_height
+    if isinstance(bc, RhombicBC):
+        return _capi.BC_RHOMBIC, bc.box_length, bc.box_height
+    return _capi.BC_SPHERE, bc.radius, bc.radius
 
 
 @dataclass
@@ -152,10 +212,6 @@ class NPT:
     n_atoms: int
     pressure: float
     separated_volume: bool = False
-
-    def __post_init__(self):
-        if self.separated_volume:
-            raise NotImplementedError("separated volume moves are not part of this engine")
 
 
 @dataclass
@@ -266,6 +322,8 @@ class MCState:
     count_vol: np.ndarray
     count_exc: np.ndarray
     ham: np.ndarray
+    count_vol_xy: np.ndarray = None   # separated volume moves (RectangularBC, RhombicBC)
+    count_vol_z: np.ndarray = None
 
 
 # ------------------------------------------------------------------ engine
@@ -362,6 +420,8 @@ class Engine:
         self.h = h
         if self.rdfsave:
             self._ck(self.L.ptmc_set_rdf(h, 1))
+        if isinstance(ensemble, NPT) and ensemble.separated_volume:
+            self._ck(self.L.ptmc_set_separated_volume(h, 1))
         self.n_runs, self.R = n_runs, mc_params.n_traj
         self.N = {}
         self.bc = {}
@@ -390,15 +450,18 @@ class Engine:
         bc = configs[0].boundary_condition
         N = len(configs[0])
         xyz = np.ascontiguousarray(np.stack([c.positions for c in configs]), dtype=np.float64)
-        kind = _capi.BC_CUBIC if isinstance(bc, CubicBC) else _capi.BC_SPHERE
-        par = bc.box_length if kind == _capi.BC_CUBIC else bc.radius
-        self._ck(self.L.ptmc_set_run_configs(self.h, run, _dptr(xyz), N, len(configs), kind, par))
+        kind, par, height = _bc_kind(bc)
+        self._ck(self.L.ptmc_set_run_configs_box(self.h, run, _dptr(xyz), N, len(configs), kind,
+                                                 par, height))
         self.N[run], self.bc[run] = N, bc
-        if max_displ is not None:
-            md = np.ascontiguousarray(max_displ, dtype=np.float64).reshape(-1)
-            if md.size == self.R:
-                md = np.stack([md, np.full(self.R, 0.1)], 1).reshape(-1)
-            self._ck(self.L.ptmc_set_max_displ(self.h, run, _dptr(md)))
+        if max_displ is not None:  # per slot: [atom], [atom, volume] or [atom, volume, xy, z]
+            md = np.ascontiguousarray(max_displ, dtype=np.float64).reshape(self.R, -1)
+            if md.shape[1] == 1:
+                md = np.concatenate([md, np.full((self.R, 1), 0.1)], 1)
+            self._ck(self.L.ptmc_set_max_displ(self.h, run, _dptr(np.ascontiguousarray(md[:, :2]))))
+            if md.shape[1] == 4:
+                self._ck(self.L.ptmc_set_max_displ_sep(
+                    self.h, run, _dptr(np.ascontiguousarray(md[:, 2:]))))
 
     def init(self):
         self._ck(self.L.ptmc_init(self.h))
@@ -497,6 +560,17 @@ class Engine:
                                         _dptr(ham)))
         return dict(xyz=xyz, en_tot=en, box=box, max_displ=md, counts=cnt, ham=ham)
 
+    def box_states(self, run=0):
+        """Slot-ordered box state of RectangularBC / RhombicBC runs: box_height
+        [R], max_displ_sep [R,2] (max_displ[3:4]), counts_sep [R,4]
+        (count_vol_xy[1:2], count_vol_z[1:2])."""
+        R = self.R
+        h, md = np.zeros(R), np.zeros((R, 2))
+        cnt = np.zeros((R, 4), dtype=np.int64)
+        self._ck(self.L.ptmc_get_box_states(self.h, run, _dptr(h), _dptr(md),
+                                            cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
+        return dict(box_height=h, max_displ_sep=md, counts_sep=cnt)
+
     def output(self, run=0):
         R, nb = self.R, self.mc_params.n_bin + 2
         npt = isinstance(self.ensemble, NPT)
@@ -538,14 +612,23 @@ class Engine:
 
     def mc_states(self, run=0):
         s = self.states(run)
+        bc = self.bc[run]
+        boxed = isinstance(bc, (RectangularBC, RhombicBC))
+        b = self.box_states(run) if boxed else None
         out = []
         for i in range(self.R):
-            bc = self.bc[run]
-            bci = CubicBC(s["box"][i]) if isinstance(bc, CubicBC) else SphericalBC(s["box"][i])
+            if boxed:
+                bci = type(bc)(s["box"][i], b["box_height"][i])
+                md = np.concatenate([s["max_displ"][i], b["max_displ_sep"][i]])
+            else:
+                bci = CubicBC(s["box"][i]) if isinstance(bc, CubicBC) else SphericalBC(s["box"][i])
+                md = s["max_displ"][i]
             out.append(MCState(self.temp.t_grid[i], self.temp.beta_grid[i],
-                               Config(s["xyz"][i], bci), s["en_tot"][i], s["max_displ"][i],
+                               Config(s["xyz"][i], bci), s["en_tot"][i], md,
                                s["counts"][i, 0:2], s["counts"][i, 2:4], s["counts"][i, 4:6],
-                               s["ham"][i]))
+                               s["ham"][i],
+                               b["counts_sep"][i, 0:2] if boxed else None,
+                               b["counts_sep"][i, 2:4] if boxed else None))
         return out
 
     def close(self):
@@ -626,12 +709,18 @@ def _save_configs(eng, ckdir, name):
         with open(os.path.join(ckdir, "%sT%d.xyz" % (name, i + 1)), "w") as f:
             f.write("%d\n" % len(st.config))
             bc = st.config.boundary_condition
-            hdr = ("SphericalBC{Float64} r2: %r" % bc.radius2 if isinstance(bc, SphericalBC)
-                   else "CubicBC{Float64} box_length: %r" % bc.box_length)
-            f.write("%s %r %r %r %d %d\n" % (hdr, st.max_displ[0], st.max_displ[1], 0.1,
-                                             st.count_atom[0], st.count_vol[0]))
+            if isinstance(bc, SphericalBC):
+                hdr = "SphericalBC{Float64} r2: %s" % _jl(bc.radius2)
+            elif isinstance(bc, CubicBC):
+                hdr = "CubicBC{Float64} box_length: %s" % _jl(bc.box_length)
+            else:  # bc_info (src/ReadSave.jl:133-135)
+                hdr = "%s{Float64} box_dims: %s, %s" % (type(bc).__name__, _jl(bc.box_length),
+                                                        _jl(bc.box_height))
+            md3 = st.max_displ[2] if len(st.max_displ) > 2 else 0.1
+            f.write("%s %s %s %s %d %d\n" % (hdr, _jl(st.max_displ[0]), _jl(st.max_displ[1]),
+                                             _jl(md3), st.count_atom[0], st.count_vol[0]))
             for x in st.config.positions:
-                f.write("1  %r %r %r \n" % (x[0], x[1], x[2]))
+                f.write("1  %s %s %s \n" % (_jl(x[0]), _jl(x[1]), _jl(x[2])))
 
 
 # ------------------------------------------------------------------ analysis
@@ -829,6 +918,12 @@ def read_checkpoint(directory):
                     bc = SphericalBC(math.sqrt(float(hdr[2])))
                     md = [float(x) for x in hdr[3:6]]
                     counts = [int(float(x)) for x in hdr[6:8]]
+                elif hdr[0].startswith(("RhombicBC", "RectangularBC")):
+                    # bc_info "box_dims: L, H" (src/ReadSave.jl:133-135)
+                    cls = RhombicBC if hdr[0].startswith("RhombicBC") else RectangularBC
+                    bc = cls(float(hdr[2].rstrip(",")), float(hdr[3]))
+                    md = [float(x) for x in hdr[4:7]]
+                    counts = [int(float(x)) for x in hdr[7:9]]
                 else:
                     bc = CubicBC(float(hdr[2]))
                     md = [float(x) for x in hdr[3:6]]

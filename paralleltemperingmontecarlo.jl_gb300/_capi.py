@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libptmc_gb300.so")
 PTMC_OK = 0
 ERRORS = {-1: "argument", -2: "state", -3: "cuda", -4: "sphere", -5: "io", -6: "limit"}
 NVT, NPT = 0, 1
-BC_SPHERE, BC_CUBIC = 0, 1
+BC_SPHERE, BC_CUBIC, BC_RECTANGULAR, BC_RHOMBIC = 0, 1, 2, 3
 FP64, FP32_RESYNC = 0, 1
 TGEOMETRIC, TLINEAR = 0, 1
 
@@ -63,7 +63,12 @@ SIGNATURES = {
                                              ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double]),
     "ptmc_set_run_configs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    "ptmc_set_run_configs_box": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                ctypes.c_double]),
+    "ptmc_set_separated_volume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ptmc_set_max_displ": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "ptmc_set_max_displ_sep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "ptmc_set_rdf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ptmc_init": (ctypes.c_int, [ctypes.c_void_p]),
     "ptmc_equilibrate": (ctypes.c_int, [ctypes.c_void_p]),
@@ -73,6 +78,7 @@ SIGNATURES = {
     "ptmc_get_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Output)]),
     "ptmc_get_states": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp,
                                        _llp, _dp]),
+    "ptmc_get_box_states": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _llp]),
     "ptmc_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "ptmc_checkpoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "ptmc_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),

@@ -43,9 +43,11 @@ struct HostRun {
   int N = 0;
   int n_start = 0;
   int bc = -1;
-  double bc_param = 0;
+  double bc_param = 0;       // sphere radius, cube side, box_length
+  double bc_height = 0;      // box_height (RectangularBC, RhombicBC)
   std::vector<double> xyz;   // n_start * N * 3
   std::vector<double> maxd;  // 2R (optional)
+  std::vector<double> maxd_sep;  // 2R (optional): max_displ[3:4]
 };
 
 struct Group {
@@ -136,6 +138,9 @@ struct ptmc_ctx {
   DBuf<RunDesc> d_runs;
   DBuf<double> d_pos, d_mat, d_comp, d_en, d_box, d_rc2, d_drift, d_beta, d_maxd,
       d_maxbox, d_ham;
+  bool sep_vol = false;        // NPT.separated_volume
+  DBuf<double> d_boxh, d_maxboxh, d_maxd_sep;  // box height, max_boxheight, max_displ[3:4]
+  DBuf<long long> d_cnt_sep;   // count_vol_xy[1:2], count_vol_z[1:2] per slot
   DBuf<unsigned long long> d_ctr;
   DBuf<int> d_status, d_wos;
   DBuf<long long> d_cnt;
@@ -180,6 +185,7 @@ struct ptmc_ctx {
   }
   int R() const { return p.n_traj; }
   int bc() const { return runs.empty() ? 0 : runs[0].bc; }
+  bool boxh() const { return bc() == PTMC_BC_RECTANGULAR || bc() == PTMC_BC_RHOMBIC; }
   bool f32() const { return p.precision == PTMC_FP32_RESYNC; }
 };
 
@@ -475,16 +481,24 @@ int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf, const double* 
 
 int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N, int n_start,
                          int bc_kind, double bc_param) {
+  return ptmc_set_run_configs_box(c, run, xyz, N, n_start, bc_kind, bc_param, bc_param);
+}
+
+int ptmc_set_run_configs_box(ptmc_ctx* c, int run, const double* xyz, int N, int n_start,
+                             int bc_kind, double box_length, double box_height) {
+  const double bc_param = box_length;
   if (!c || !xyz) return PTMC_ERR_ARG;
   if (c->inited) return c->fail(PTMC_ERR_STATE, "configurations must be set before ptmc_init");
   if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
   if (N < 2) return c->fail(PTMC_ERR_ARG, "need at least 2 atoms");
   if (N > 1024) return c->fail(PTMC_ERR_LIMIT, "at most 1024 atoms per configuration");
   if (n_start < 1) return c->fail(PTMC_ERR_ARG, "need at least one start configuration");
-  if (bc_kind != PTMC_BC_SPHERE && bc_kind != PTMC_BC_CUBIC)
+  if (bc_kind != PTMC_BC_SPHERE && bc_kind != PTMC_BC_CUBIC && bc_kind != PTMC_BC_RECTANGULAR &&
+      bc_kind != PTMC_BC_RHOMBIC)
     return c->fail(PTMC_ERR_ARG, "unknown boundary condition");
   if (!(bc_param > 0)) return c->fail(PTMC_ERR_ARG, "boundary parameter must be positive");
-  if (c->p.ensemble == PTMC_NPT && bc_kind != PTMC_BC_CUBIC)
+  if (!(box_height > 0)) return c->fail(PTMC_ERR_ARG, "box height must be positive");
+  if (c->p.ensemble == PTMC_NPT && bc_kind == PTMC_BC_SPHERE)
     return c->fail(PTMC_ERR_ARG, "SphericalBC cannot be used in an NPT ensemble.");  // Ensembles.jl:192
   for (auto& r : c->runs)
     if (r.bc >= 0 && r.bc != bc_kind)
@@ -494,7 +508,22 @@ int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N, int n_s
   h.n_start = n_start;
   h.bc = bc_kind;
   h.bc_param = bc_param;
+  h.bc_height = (bc_kind == PTMC_BC_RECTANGULAR || bc_kind == PTMC_BC_RHOMBIC) ? box_height : bc_param;
   h.xyz.assign(xyz, xyz + (size_t)n_start * N * 3);
+  return PTMC_OK;
+}
+
+int ptmc_set_separated_volume(ptmc_ctx* c, int on) {
+  if (!c) return PTMC_ERR_ARG;
+  if (c->inited) return c->fail(PTMC_ERR_STATE, "separated volume moves are set before ptmc_init");
+  c->sep_vol = on != 0;
+  return PTMC_OK;
+}
+
+int ptmc_set_max_displ_sep(ptmc_ctx* c, int run, const double* md) {
+  if (!c || !md) return PTMC_ERR_ARG;
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  c->runs[run].maxd_sep.assign(md, md + 2 * c->R());
   return PTMC_OK;
 }
 
@@ -529,6 +558,19 @@ int ptmc_init(ptmc_ctx* c) {
     }
   }
   const bool npt = c->p.ensemble == PTMC_NPT;
+  if (c->boxh()) {  // RectangularBC / RhombicBC: the plain FP64 form with the ELJ potentials
+    if (c->f32())
+      return c->fail(PTMC_ERR_ARG,
+                     "RectangularBC/RhombicBC run in the plain FP64 form (precision PTMC_FP64)");
+    if (c->pot != POT_ELJ && c->pot != POT_ELJEVEN)
+      return c->fail(PTMC_ERR_ARG, "RectangularBC/RhombicBC: ELJPotential or ELJPotentialEven only");
+  }
+  if (c->sep_vol && (!npt || !c->boxh()))
+    return c->fail(PTMC_ERR_ARG,
+                   "separated volume moves need the NPT ensemble with a RectangularBC or RhombicBC");
+  if (npt && c->pot != POT_ELJEVEN)
+    return c->fail(PTMC_ERR_ARG, "NPT: ELJPotentialEven only (its long-range correction, "
+                                 "src/EnergyEvaluation.jl:968)");
   // group runs by N: device order sorted by N (stable)
   int nr = c->p.n_runs;
   c->run_of_dev.resize(nr);
@@ -587,10 +629,12 @@ int ptmc_init(ptmc_ctx* c) {
       c->d_beta.alloc(W) || c->d_maxd.alloc(2 * W) || c->d_maxbox.alloc(W) ||
       c->d_ham.alloc(2 * W) || c->d_ctr.alloc(W) || c->d_status.alloc(W) ||
       c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho) ||
-      (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)))
+      (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)) || c->d_boxh.alloc(W) ||
+      c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W))
     return c->fail(PTMC_ERR_CUDA, "device allocation failed");
   // host images
-  std::vector<double> pos(po), box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W);
+  std::vector<double> pos(po), box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W), boxh(W),
+      maxboxh(W), maxd_sep(2 * W);
   std::vector<int> wos(W);
   for (int d = 0; d < nr; ++d) {
     const HostRun& h = c->runs[c->run_of_dev[d]];
@@ -599,12 +643,22 @@ int ptmc_init(ptmc_ctx* c) {
       const double* src = &h.xyz[(size_t)(w % h.n_start) * h.N * 3];
       std::copy(src, src + (size_t)h.N * 3, &pos[r.pos_off + (size_t)w * h.N * 3]);
       int g = r.wk + w;
-      box[g] = h.bc_param;
-      rc2[g] = h.bc == PTMC_BC_CUBIC ? h.bc_param * h.bc_param / 4 : 0.0;  // get_r_cut (Ensembles.jl:118)
+      const double Lb = h.bc_param, Hb = h.bc_height;
+      box[g] = Lb;
+      boxh[g] = Hb;
+      // get_r_cut (Ensembles.jl:118-155)
+      rc2[g] = h.bc == PTMC_BC_CUBIC         ? Lb * Lb / 4
+               : h.bc == PTMC_BC_RECTANGULAR ? std::min(Lb * Lb / 4, Hb * Hb / 4)
+               : h.bc == PTMC_BC_RHOMBIC     ? std::min(Lb * Lb * 3 / 16, Hb * Hb / 4)
+                                             : 0.0;
       beta[g] = c->beta[w];
       maxd[2 * g] = h.maxd.empty() ? 0.1 : h.maxd[2 * w];       // MCStates.jl:104
       maxd[2 * g + 1] = h.maxd.empty() ? 0.1 : h.maxd[2 * w + 1];
-      maxbox[g] = h.bc == PTMC_BC_CUBIC ? h.bc_param * 1.8 : 30.0;  // max_length (MCStates.jl:63-75)
+      maxd_sep[2 * g] = h.maxd_sep.empty() ? 0.1 : h.maxd_sep[2 * w];
+      maxd_sep[2 * g + 1] = h.maxd_sep.empty() ? 0.1 : h.maxd_sep[2 * w + 1];
+      // max_length / max_height (MCStates.jl:63-87)
+      maxbox[g] = h.bc == PTMC_BC_SPHERE ? 30.0 : Lb * 1.8;
+      maxboxh[g] = h.bc == PTMC_BC_SPHERE ? 30.0 : Hb * 1.8;
       wos[g] = w;
     }
   }
@@ -615,6 +669,10 @@ int ptmc_init(ptmc_ctx* c) {
   CK(cudaMemcpyAsync(c->d_beta.p, beta.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->d_maxd.p, maxd.data(), sizeof(double) * 2 * W, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->d_maxbox.p, maxbox.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_boxh.p, boxh.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_maxboxh.p, maxboxh.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_maxd_sep.p, maxd_sep.data(), sizeof(double) * 2 * W, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(c->d_cnt_sep.p, 0, sizeof(long long) * 4 * W, s));
   CK(cudaMemcpyAsync(c->d_wos.p, wos.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(unsigned long long) * W, s));
   CK(cudaMemsetAsync(c->d_ham.p, 0, sizeof(double) * 2 * W, s));
@@ -642,6 +700,11 @@ int ptmc_init(ptmc_ctx* c) {
   K.wos = c->d_wos.p;
   K.hist = c->d_hist.p;
   K.rdf = c->rdf_on ? c->d_rdf.p : nullptr;
+  K.boxh = c->d_boxh.p;
+  K.maxboxh = c->d_maxboxh.p;
+  K.maxd_sep = c->d_maxd_sep.p;
+  K.cnt_sep = c->d_cnt_sep.p;
+  K.sep_vol = c->sep_vol ? 1 : 0;
   K.K = (int)c->coeff.size();
   for (int k = 0; k < MAX_COEFF; ++k) K.c[k] = k < K.K ? c->coeff[k] : 0.0;
   for (int k = 0; k < MAX_COEFF; ++k) K.cf[k] = (float)K.c[k];
@@ -728,10 +791,11 @@ int ptmc_equilibrate(ptmc_ctx* c) {
   int rc = run_phase(c, eq / 2, PHASE_EQ);  // only half is simulated (MCRun.jl:296-298)
   if (rc) return rc;
   int R = c->R(), W = c->W;
-  std::vector<double> en(W), box(W);
+  std::vector<double> en(W), box(W), boxh(W);
   std::vector<int> wos(W);
   CK(cudaMemcpyAsync(en.data(), c->d_en.p, sizeof(double) * W, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(box.data(), c->d_box.p, sizeof(double) * W, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(boxh.data(), c->d_boxh.p, sizeof(double) * W, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(wos.data(), c->d_wos.p, sizeof(int) * W, cudaMemcpyDeviceToHost, c->st));
   rc = pull_runs(c);
   if (rc) return rc;
@@ -747,24 +811,29 @@ int ptmc_equilibrate(ptmc_ctx* c) {
     r.en_min = eb[0];
     r.en_max = eb[1];
     r.dE = (r.en_max - r.en_min) / (c->p.n_bin - 1);
+    // the first state's box (Sampling.jl:141-245)
+    const double b = box[r.wk + wos[r.wk + 0]], bh = boxh[r.wk + wos[r.wk + 0]];
+    const int bc = c->bc();
     if (c->p.ensemble == PTMC_NPT) {
-      double L = box[r.wk + wos[r.wk + 0]];
-      double V = L * L * L;
+      double V = bc == PTMC_BC_RECTANGULAR ? b * b * bh
+                 : bc == PTMC_BC_RHOMBIC   ? b * b * bh * 1.7320508075688772 / 2
+                                           : b * b * b;
       r.v_min = V * 0.8;
       r.v_max = V * 2.0;
       r.dV = (r.v_max - r.v_min) / c->p.n_bin;
     }
-    {  // delta_r2 of the first state's boundary (Sampling.jl:151, 185)
-      const double b = box[r.wk + wos[r.wk + 0]];
-      r.dr2 = c->bc() == PTMC_BC_CUBIC ? 3.0 / 4.0 * (b * b) / c->p.n_bin / 5
-                                       : 4 * (b * b) / c->p.n_bin / 5;
-    }
+    // delta_r2 (Sampling.jl:151 sphere, :185 cube, :210 rhombic, :240 rectangular)
+    if (bc == PTMC_BC_CUBIC) r.dr2 = 3.0 / 4.0 * (b * b) / c->p.n_bin / 5;
+    else if (bc == PTMC_BC_RHOMBIC) r.dr2 = (3.0 / 8.0 * (b * b) + 1.0 / 4.0 * (bh * bh)) / c->p.n_bin / 5;
+    else if (bc == PTMC_BC_RECTANGULAR) r.dr2 = (1.0 / 2.0 * (b * b) + 1.0 / 4.0 * (bh * bh)) / c->p.n_bin / 5;
+    else r.dr2 = 4 * (b * b) / c->p.n_bin / 5;
   }
   c->equilibrated = true;
   rc = push_runs(c);
   if (rc) return rc;
   // reset_counters (MCRun.jl:271-277)
   CK(cudaMemsetAsync(c->d_cnt.p, 0, sizeof(long long) * 6 * W, c->st));
+  CK(cudaMemsetAsync(c->d_cnt_sep.p, 0, sizeof(long long) * 4 * W, c->st));
   CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned int) * std::max<size_t>(c->d_hist.n, 1), c->st));
   if (c->rdf_on) CK(cudaMemsetAsync(c->d_rdf.p, 0, sizeof(unsigned int) * c->d_rdf.n, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -824,6 +893,30 @@ int ptmc_get_states(ptmc_ctx* c, int run, double* xyz, double* en_tot, double* b
   if (max_displ) std::copy(md.begin(), md.end(), max_displ);
   if (counts) std::copy(cnt.begin(), cnt.end(), counts);
   if (ham) std::copy(hm.begin(), hm.end(), ham);
+  return PTMC_OK;
+}
+
+int ptmc_get_box_states(ptmc_ctx* c, int run, double* box_height, double* max_displ_sep,
+                        long long* counts_sep) {
+  if (!c) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  const RunDesc& r = c->rd[c->dev_of_run[run]];
+  const int R = c->R();
+  std::vector<double> bh(R), md(2 * R);
+  std::vector<long long> cnt(4 * R);
+  std::vector<int> wos(R);
+  cudaStream_t s = c->st;
+  CK(cudaMemcpyAsync(bh.data(), c->d_boxh.p + r.wk, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(md.data(), c->d_maxd_sep.p + 2 * r.wk, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(cnt.data(), c->d_cnt_sep.p + 4 * (size_t)r.wk, sizeof(long long) * 4 * R,
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wos.data(), c->d_wos.p + r.wk, sizeof(int) * R, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int slot = 0; slot < R; ++slot)
+    if (box_height) box_height[slot] = bh[wos[slot]];
+  if (max_displ_sep) std::copy(md.begin(), md.end(), max_displ_sep);
+  if (counts_sep) std::copy(cnt.begin(), cnt.end(), counts_sep);
   return PTMC_OK;
 }
 
@@ -918,6 +1011,10 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_cnt.free_();
   c->d_hist.free_();
   c->d_rdf.free_();
+  c->d_boxh.free_();
+  c->d_maxboxh.free_();
+  c->d_maxd_sep.free_();
+  c->d_cnt_sep.free_();
   c->d_nn_sf.free_();
   c->d_nn_W.free_();
   c->d_nn_G.free_();
@@ -990,7 +1087,8 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
   for (int k = 0; k < 10; ++k) s += fmt_double(pv[k]) + (k < 9 ? " " : "\n");
   if (npt) {
     s += "ensemble n_atom_moves n_volume_moves n_atom_swaps pressure separated_volume\n";
-    s += "NPT " + std::to_string(N) + " " + std::to_string(N) + " 1 0 " + fmt_double(c->p.pressure) + " false\n";
+    s += "NPT " + std::to_string(N) + " " + std::to_string(N) + " 1 0 " + fmt_double(c->p.pressure) +
+         (c->sep_vol ? " true\n" : " false\n");
   } else {
     s += "ensemble n_atom_moves n_atom_swaps\n";
     s += "NVT " + std::to_string(N) + " " + std::to_string(N) + " 0\n";
@@ -1047,16 +1145,22 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
   if (!write_file_atomic(d + "/index.txt", std::to_string(index) + "\n"))
     return c->fail(PTMC_ERR_IO, "cannot write index.txt");
   // configT<i>.xyz (checkpoint_config, :142-158)
-  std::vector<double> xyz((size_t)R * N * 3), en(R), box(R), md(2 * R), ham(2 * R);
+  std::vector<double> xyz((size_t)R * N * 3), en(R), box(R), md(2 * R), ham(2 * R), bh(R), mds(2 * R);
   std::vector<long long> cnt(6 * R);
   rc = ptmc_get_states(c, 0, xyz.data(), en.data(), box.data(), md.data(), cnt.data(), ham.data());
   if (rc) return rc;
+  rc = ptmc_get_box_states(c, 0, bh.data(), mds.data(), nullptr);
+  if (rc) return rc;
   for (int i = 0; i < R; ++i) {
     std::string t = std::to_string(N) + "\n";
+    // bc_info (ReadSave.jl:131-135)
     if (c->bc() == PTMC_BC_SPHERE) t += "SphericalBC{Float64} r2: " + fmt_double(box[i] * box[i]);
-    else t += "CubicBC{Float64} box_length: " + fmt_double(box[i]);
-    t += " " + fmt_double(md[2 * i]) + " " + fmt_double(md[2 * i + 1]) + " " + fmt_double(0.1) + " " +
-         std::to_string(cnt[6 * i]) + " " + std::to_string(cnt[6 * i + 2]) + "\n";
+    else if (c->bc() == PTMC_BC_CUBIC) t += "CubicBC{Float64} box_length: " + fmt_double(box[i]);
+    else
+      t += std::string(c->bc() == PTMC_BC_RHOMBIC ? "RhombicBC" : "RectangularBC") +
+           "{Float64} box_dims: " + fmt_double(box[i]) + ", " + fmt_double(bh[i]);
+    t += " " + fmt_double(md[2 * i]) + " " + fmt_double(md[2 * i + 1]) + " " + fmt_double(mds[2 * i]) +
+         " " + std::to_string(cnt[6 * i]) + " " + std::to_string(cnt[6 * i + 2]) + "\n";
     for (int a = 0; a < N; ++a) {
       const double* x = &xyz[((size_t)i * N + a) * 3];
       t += "1  " + fmt_double(x[0]) + " " + fmt_double(x[1]) + " " + fmt_double(x[2]) + " \n";
@@ -1065,7 +1169,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       return c->fail(PTMC_ERR_IO, "cannot write configT.xyz");
   }
   // engine.bin: complete state
-  std::string b = "PTMCGB01";
+  std::string b = "PTMCGB02";
   unsigned long long hdr[4] = {(unsigned long long)c->p.n_runs, (unsigned long long)R,
                                (unsigned long long)c->W, (unsigned long long)c->equilibrated};
   put(b, hdr, 4);
@@ -1076,7 +1180,8 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       (rc = dump(c, b, c->d_maxbox)) || (rc = dump(c, b, c->d_ham)) || (rc = dump(c, b, c->d_ctr)) ||
       (rc = dump(c, b, c->d_status)) || (rc = dump(c, b, c->d_wos)) || (rc = dump(c, b, c->d_cnt)) ||
       (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)) ||
-      (rc = dump(c, b, c->d_rdf)))
+      (rc = dump(c, b, c->d_rdf)) || (rc = dump(c, b, c->d_boxh)) || (rc = dump(c, b, c->d_maxboxh)) ||
+      (rc = dump(c, b, c->d_maxd_sep)) || (rc = dump(c, b, c->d_cnt_sep)))
     return rc;
   put(b, "PTMCEND!", 8);
   if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
@@ -1094,7 +1199,9 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
   size_t k;
   while ((k = std::fread(buf, 1, sizeof(buf), f)) > 0) b.append(buf, k);
   std::fclose(f);
-  if (b.size() < 8 + 32 || b.compare(0, 8, "PTMCGB01") != 0)
+  if (b.size() >= 8 && b.compare(0, 8, "PTMCGB01") == 0)
+    return c->fail(PTMC_ERR_IO, "engine.bin: written by an earlier format (PTMCGB01), not restorable");
+  if (b.size() < 8 + 32 || b.compare(0, 8, "PTMCGB02") != 0)
     return c->fail(PTMC_ERR_IO, "engine.bin: bad magic");
   if (b.size() < 8 || b.compare(b.size() - 8, 8, "PTMCEND!") != 0)
     return c->fail(PTMC_ERR_IO, "engine.bin truncated (no end marker)");
@@ -1121,7 +1228,9 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
       (rc = undump(c, b, at, c->d_status)) || (rc = undump(c, b, at, c->d_wos)) ||
       (rc = undump(c, b, at, c->d_cnt)) || (rc = undump(c, b, at, c->d_hist)) ||
       (rc = undump(c, b, at, c->d_nn_G)) || (rc = undump(c, b, at, c->d_nn_sow)) ||
-      (rc = undump(c, b, at, c->d_rdf)))
+      (rc = undump(c, b, at, c->d_rdf)) || (rc = undump(c, b, at, c->d_boxh)) ||
+      (rc = undump(c, b, at, c->d_maxboxh)) || (rc = undump(c, b, at, c->d_maxd_sep)) ||
+      (rc = undump(c, b, at, c->d_cnt_sep)))
     return rc;
   c->rd = rd;
   c->equilibrated = hdr[3] != 0;
@@ -1819,8 +1928,10 @@ int snapshot(ptmc_ctx* c, Snapshot& s) {
   int rc = 0;
   rc |= snap_one(c, s, c->d_runs);
   for (auto* b : {&c->d_pos, &c->d_mat, &c->d_comp, &c->d_en, &c->d_box, &c->d_rc2, &c->d_drift,
-                  &c->d_beta, &c->d_maxd, &c->d_maxbox, &c->d_ham})
+                  &c->d_beta, &c->d_maxd, &c->d_maxbox, &c->d_ham, &c->d_boxh, &c->d_maxboxh,
+                  &c->d_maxd_sep})
     rc |= snap_one(c, s, *b);
+  rc |= snap_one(c, s, c->d_cnt_sep);
   rc |= snap_one(c, s, c->d_ctr);
   rc |= snap_one(c, s, c->d_status);
   rc |= snap_one(c, s, c->d_wos);

@@ -86,6 +86,16 @@ __device__ double lrc64(int N, double rc2, const double* c, int K) {
   e *= 3.141592653589793 * (double)(N * N) / 4 / (rcs * rcs * rcs);
   return e;
 }
+// long-range correction of dimer_energy_config for the box
+// (src/EnergyEvaluation.jl:419, 444, 469-472): lrc assumes a cube, the other
+// boxes rescale it
+template <int BC>
+__device__ double lrc_box(int N, double rc2, const double* c, int K, double L, double H) {
+  const double l = lrc64(N, rc2, c, K);
+  if (BC == BC_RHB) return l * 3 / 4 * L / H;
+  if (BC == BC_RECT) return L < H ? l * L / H : l * (H * H) / (L * L);
+  return l;
+}
 // invrexp (src/EnergyEvaluation.jl:1088-1095): (r^-n, r^-m) from r^2
 __device__ __forceinline__ void invrexp64(double r2, double hn, double hm,
                                           double& a, double& b) {
@@ -101,9 +111,35 @@ __device__ __forceinline__ void invrexp64(double r2, double hn, double hm,
 
 template <int BC>
 __device__ __forceinline__ double pd2(double ax, double ay, double az,
-                                      const double* b, double L) {
-  return BC == BC_CUB ? d2_cub(ax, ay, az, b[0], b[1], b[2], L)
-                      : d2_sph(ax, ay, az, b[0], b[1], b[2]);
+                                      const double* b, double L, double H) {
+  if (BC == BC_CUB) return d2_cub(ax, ay, az, b[0], b[1], b[2], L);
+  if (BC == BC_RECT) return d2_rect(ax, ay, az, b[0], b[1], b[2], L, H);
+  if (BC == BC_RHB) return d2_rhb(ax, ay, az, b[0], b[1], b[2], L, H);
+  return d2_sph(ax, ay, az, b[0], b[1], b[2]);
+}
+// boxes with a separate height (RectangularBC, RhombicBC)
+template <int BC>
+__host__ __device__ constexpr bool has_height() { return BC == BC_RECT || BC == BC_RHB; }
+// get_r_cut (src/Ensembles.jl:118-155)
+template <int BC>
+__device__ __forceinline__ double box_rcut(double L, double H) {
+  if (BC == BC_RHB) return fmin(L * L * 3 / 16, H * H / 4);
+  if (BC == BC_RECT) return fmin(L * L / 4, H * H / 4);
+  return L * L / 4;
+}
+// get_volume (src/Configurations.jl:246-256)
+template <int BC>
+__device__ __forceinline__ double box_volume(double L, double H) {
+  if (BC == BC_RHB) return L * L * H * SQRT3 / 2;
+  if (BC == BC_RECT) return dmul(dmul(L, L), H);
+  return dmul(dmul(L, L), L);
+}
+// the volume the NPT histogram index is taken from (src/Sampling.jl:64-130):
+// the box volume, except that the rhombic branch computes L^2 * 3 H^0.5 / 2
+template <int BC>
+__device__ __forceinline__ double hist_volume(double L, double H) {
+  if (BC == BC_RHB) return dmul(dmul(L, L), dmul(3.0, sqrt(H))) / 2;
+  return box_volume<BC>(L, H);
 }
 template <int BC>
 __device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
@@ -118,7 +154,7 @@ __device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
 // (src/EnergyEvaluation.jl:1800-1810, 1156-1162).  Writes the NPT distance
 // matrix (plain form) and the EAM components when the pointers are given.
 template <int POT, int BC, int ENS>
-__device__ double walker_energy64(const double* X, int N, double L, double rc2,
+__device__ double walker_energy64(const double* X, int N, double L, double H, double rc2,
                                   const double* c, int K, double hn, double hm,
                                   double ean, double ecam, double* M,
                                   double* comp64, float2* comp32, int lane) {
@@ -128,7 +164,7 @@ __device__ double walker_energy64(const double* X, int N, double L, double rc2,
       double a = 0.0, b = 0.0;
       for (int j = 0; j < N; ++j) {
         if (j == k) continue;
-        double x = pd2<BC>(X[3 * k], X[3 * k + 1], X[3 * k + 2], X + 3 * j, L);
+        double x = pd2<BC>(X[3 * k], X[3 * k + 1], X[3 * k + 2], X + 3 * j, L, H);
         double pa, pb;
         invrexp64(x, hn, hm, pa, pb);
         a += pa;
@@ -146,7 +182,7 @@ __device__ double walker_energy64(const double* X, int N, double L, double rc2,
     for (int i = 0; i < N; ++i) {
       double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
       for (int j = i + 1 + lane; j < N; j += 32) {
-        double x = pd2<BC>(xi, yi, zi, X + 3 * j, L);
+        double x = pd2<BC>(xi, yi, zi, X + 3 * j, L, H);
         if (M) {
           M[(size_t)i * N + j] = x;
           M[(size_t)j * N + i] = x;
@@ -157,7 +193,7 @@ __device__ double walker_energy64(const double* X, int N, double L, double rc2,
       if (M && lane == 0) M[(size_t)i * N + i] = 0.0;
     }
     e = warp_sum(e);
-    if (ENS == ENS_NPT) e = e + lrc64(N, rc2, c, K);
+    if (ENS == ENS_NPT) e = e + lrc_box<BC>(N, rc2, c, K, L, H);
     return e;
   }
 }
@@ -174,7 +210,7 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
   const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
   double* M = (ENS == ENS_NPT && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
   double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
-  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.rc2[g], P.c, P.K,
+  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
                                            -0.5 * P.eam_n, -0.5 * P.eam_m,
                                            P.eam_ean, P.eam_ecam, M, comp,
                                            nullptr, lane);
@@ -232,6 +268,10 @@ __global__ void __launch_bounds__(1024)
   long long* s_cnt = (long long*)carve((long long)R * 48);
   int* s_wos = (int*)carve((long long)R * 4);
   int* s_sow = (int*)carve((long long)R * 4);
+  double* s_boxh = (double*)carve((long long)R * 8);
+  double* s_maxboxh = (double*)carve((long long)R * 8);
+  double* s_maxd_sep = (double*)carve((long long)R * 16);
+  long long* s_cnt_sep = (long long*)carve((long long)R * 32);
 
   // ---- load the run into shared memory ----
   if (tid < K) {
@@ -257,6 +297,12 @@ __global__ void __launch_bounds__(1024)
     s_maxd[2 * s + 1] = P.maxd[2 * g + 1];
     for (int q = 0; q < 6; ++q) s_cnt[6 * s + q] = P.cnt[6 * (size_t)g + q];
     s_wos[s] = P.wos[g];
+    if (has_height<BC>()) {
+      s_maxboxh[s] = P.maxboxh[g];
+      s_maxd_sep[2 * s] = P.maxd_sep[2 * g];
+      s_maxd_sep[2 * s + 1] = P.maxd_sep[2 * g + 1];
+      for (int q = 0; q < 4; ++q) s_cnt_sep[4 * s + q] = P.cnt_sep[4 * (size_t)g + q];
+    }
   }
   __syncthreads();
   if (F32)
@@ -270,6 +316,7 @@ __global__ void __launch_bounds__(1024)
   const int g = rd.wk + w;
   double en = P.en[g];
   double L = P.box[g];
+  double H = has_height<BC>() ? P.boxh[g] : L;  // box height (RectangularBC, RhombicBC)
   double rc2 = P.rc2[g];
   unsigned long long ctr = P.ctr[g];
   unsigned long long base = ctr + DRAW_BUF;  // forces a refill on first draw
@@ -349,10 +396,19 @@ __global__ void __launch_bounds__(1024)
           }
         }
       }
-    } else {  // periodic wrap (src/MCMoves.jl:50-64)
+    } else if (BC == BC_RHB) {  // rhombic wrap (src/MCMoves.jl:66-83)
+      const double ky = rint(ddiv(dsub(ty, ddiv(dmul(L, SQRT3), 4.0)), ddiv(dmul(L, SQRT3), 2.0)));
+      const double sx = dadd(dmul(L, rint(ddiv(dsub(dsub(tx, ddiv(ty, SQRT3)), ddiv(L, 2.0)), L))),
+                             dmul(ddiv(L, 2.0), ky));
+      const double sy = dmul(ddiv(dmul(L, SQRT3), 2.0), ky);
+      const double sz = dmul(H, rint(ddiv(dsub(tz, ddiv(H, 2.0)), H)));
+      tx = dsub(tx, sx);
+      ty = dsub(ty, sy);
+      tz = dsub(tz, sz);
+    } else {  // periodic wrap (src/MCMoves.jl:50-64, 85-98)
       tx = dsub(tx, dmul(L, rint(ddiv(tx, L))));
       ty = dsub(ty, dmul(L, rint(ddiv(ty, L))));
-      tz = dsub(tz, dmul(L, rint(ddiv(tz, L))));
+      tz = dsub(tz, dmul(H, rint(ddiv(tz, H))));
     }
 
     double new_en;
@@ -367,8 +423,8 @@ __global__ void __launch_bounds__(1024)
             if (row) row[j] = 0.0;
             continue;
           }
-          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L);
-          double dol = Mi ? Mi[j] : pd2<BC>(xi, yi, zi, X + 3 * j, L);
+          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
+          double dol = Mi ? Mi[j] : pd2<BC>(xi, yi, zi, X + 3 * j, L, H);
           if (ENS == ENS_NPT) {
             row[j] = dn;
             if (dn <= rc2) e_n += v64<POT>(s_c, K, dn);
@@ -410,8 +466,8 @@ __global__ void __launch_bounds__(1024)
             D[j] = make_double2(0.0, 0.0);
             continue;
           }
-          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L);
-          double dol = pd2<BC>(xi, yi, zi, X + 3 * j, L);
+          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
+          double dol = pd2<BC>(xi, yi, zi, X + 3 * j, L, H);
           double a1, b1, a0, b0;
           invrexp64(dn, hn, hm, a1, b1);
           invrexp64(dol, hn, hm, a0, b0);
@@ -507,18 +563,60 @@ __global__ void __launch_bounds__(1024)
   };
 
   // ---------------------------------------------------------- volume move
-  // volume_change_uniform (src/MCMoves.jl:277-287), NPT energy
-  // (src/MCRun.jl:76-85), metropolis_condition NPT (src/Exchange.jl:58-70),
-  // swap_config_v! (src/swap_config.jl:113-141).  Always FP64.
-  auto volume_move = [&](double beta, double mdv, double maxbox) -> int {
-    double u = draw();
-    double scale = pow(exp((u - 0.5) * mdv), 1.0 / 3.0);
-    if (L >= maxbox && scale > 1.0) scale = 1.0;
-    double Ln = scale * L;
-    double rcn = Ln * Ln / 4;
-    double s2 = scale * scale;
+  // volume_change (src/MCMoves.jl:350-356), NPT energy (src/MCRun.jl:76-85),
+  // metropolis_condition NPT (src/Exchange.jl:58-70), swap_config_v!
+  // (src/swap_config.jl:113-141).  Always FP64.  Uniform moves
+  // (volume_change_uniform, :277-287) scale the distance matrix by scale^2;
+  // separated moves (volume_change_separated, :298-343; RectangularBC and
+  // RhombicBC) draw rand(1:6) for z (1), xy (2-3) or all directions (4-6) and
+  // evaluate the trial energy from the scaled positions; the distance matrix is
+  // rebuilt from the new positions when the move is accepted.  Returns the
+  // accepted kind + 1 (1 all directions, 2 xy, 3 z), 0 when rejected.
+  auto volume_move = [&](double beta, int slot, double mdv, double maxbox) -> int {
+    int kind = 0;
+    double fx = 1.0, fz = 1.0, Ln = L, Hn = H;
+    auto change_xyz = [&]() {  // volume_change_xyz (src/MCMoves.jl:169-177)
+      double u = draw();
+      double scale = pow(exp((u - 0.5) * mdv), 1.0 / 3.0);
+      if (L >= maxbox && scale > 1.0) scale = 1.0;
+      fx = fz = scale;
+      Ln = scale * L;
+      Hn = has_height<BC>() ? scale * H : Ln;
+    };
+    const bool sep = has_height<BC>() && P.sep_vol;
+    if (sep) {
+      const double maxboxh = s_maxboxh[slot];
+      const double lh = maxbox / maxboxh;  // lh_ratio (src/MCStates.jl:103)
+      const double ratio = L / H;
+      const int ra = randint(draw(), 6) + 1;
+      if (ra == 1) {  // volume_change_z (src/MCMoves.jl:257-271)
+        kind = 2;
+        double u = draw();
+        double scale = exp((u - 0.5) * s_maxd_sep[2 * slot + 1]);
+        if (ratio <= lh * 1.1 && scale > 1.0) scale = 1 / scale;
+        else if (ratio >= lh * 0.909 && scale < 1.0) scale = 1 / scale;
+        if (H >= maxboxh && scale > 1.0) scale = 1 / scale;
+        fz = scale;
+        Hn = H * scale;
+      } else if (ra <= 3) {  // volume_change_xy (src/MCMoves.jl:231-247)
+        kind = 1;
+        double u = draw();
+        double scale = pow(exp((u - 0.5) * s_maxd_sep[2 * slot]), 0.5);
+        if (ratio >= lh * 1.1 && scale > 1.0) scale = 1 / scale;
+        else if (ratio <= lh * 0.909 && scale < 1.0) scale = 1 / scale;
+        if (L >= maxbox && scale > 1.0) scale = 1 / scale;
+        fx = scale;
+        Ln = L * scale;
+      } else {
+        change_xyz();
+      }
+    } else {
+      change_xyz();
+    }
+    const double rcn = box_rcut<BC>(Ln, Hn);
+    const double s2 = fx * fx;
     double e = 0.0;
-    if (!F32) {
+    if (!F32 && !sep) {
       for (int i = 0; i < N; ++i)
         for (int j = i + 1 + lane; j < N; j += 32) {
           double x = M[(size_t)i * N + j] * s2;
@@ -526,34 +624,52 @@ __global__ void __launch_bounds__(1024)
         }
     } else {
       for (int i = 0; i < N; ++i) {
-        double xi = scale * X[3 * i], yi = scale * X[3 * i + 1], zi = scale * X[3 * i + 2];
+        const double xi = X[3 * i] * fx, yi = X[3 * i + 1] * fx, zi = X[3 * i + 2] * fz;
         for (int j = i + 1 + lane; j < N; j += 32) {
-          double x = d2_cub(xi, yi, zi, scale * X[3 * j], scale * X[3 * j + 1],
-                            scale * X[3 * j + 2], Ln);
+          const double b[3] = {X[3 * j] * fx, X[3 * j + 1] * fx, X[3 * j + 2] * fz};
+          double x = pd2<BC>(xi, yi, zi, b, Ln, Hn);
           if (x <= rcn) e += v64<POT>(s_c, K, x);
         }
       }
     }
-    e = warp_sum(e) + lrc64(N, rcn, s_c, K);
-    double Vn = Ln * Ln * Ln, Vo = L * L * L;
+    e = warp_sum(e) + lrc_box<BC>(N, rcn, s_c, K, Ln, Hn);
+    const double Vn = box_volume<BC>(Ln, Hn), Vo = box_volume<BC>(L, H);
     double dh = dadd(dsub(e, en), dmul(P.pressure, dsub(Vn, Vo)));
     double prob = exp(dadd(dmul(-dh, beta), dmul((double)N, log(Vn / Vo))));
     if (prob > 1) prob = 1.0;
     double ua = draw();
     if (!(prob >= ua)) return 0;
     __syncwarp();
-    for (int k = lane; k < 3 * N; k += 32) X[k] = scale * X[k];
-    if (!F32)
-      for (int k = lane; k < N * N; k += 32) M[k] = M[k] * s2;
+    for (int a = lane; a < N; a += 32) {
+      X[3 * a] = X[3 * a] * fx;
+      X[3 * a + 1] = X[3 * a + 1] * fx;
+      X[3 * a + 2] = X[3 * a + 2] * fz;
+    }
+    __syncwarp();
+    if (!F32) {
+      if (sep) {  // get_distance2_mat! of the accepted configuration
+        for (int i = 0; i < N; ++i) {
+          for (int j = i + 1 + lane; j < N; j += 32) {
+            double x = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
+            M[(size_t)i * N + j] = x;
+            M[(size_t)j * N + i] = x;
+          }
+          if (lane == 0) M[(size_t)i * N + i] = 0.0;
+        }
+      } else {
+        for (int k = lane; k < N * N; k += 32) M[k] = M[k] * s2;
+      }
+    }
     __syncwarp();
     if (F32)
       for (int a = lane; a < N; a += 32)
         X32[a] = make_float4((float)X[3 * a], (float)X[3 * a + 1], (float)X[3 * a + 2], 0.f);
     L = Ln;
+    H = Hn;
     rc2 = rcn;
     en = e;
     __syncwarp();
-    return 1;
+    return kind + 1;
   };
 
   // ---------------------------------------------------------- cycles
@@ -565,17 +681,23 @@ __global__ void __launch_bounds__(1024)
     const double beta = s_beta[slot];
     const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
     const double maxbox = s_maxbox[slot];
-    long long acc_a = 0, acc_v = 0;
+    long long acc_a = 0, acc_v = 0, acc_xy = 0, acc_z = 0;
     if (status == ST_OK) {
       for (int st = 0; st < n_steps; ++st) {
         int k = randint(draw(), n_steps);
-        if (k < N) acc_a += atom_move(k, beta, md);
-        else acc_v += volume_move(beta, mdv, maxbox);
+        if (k < N) {
+          acc_a += atom_move(k, beta, md);
+        } else {
+          const int v = volume_move(beta, slot, mdv, maxbox);
+          acc_v += v == 1;
+          acc_xy += v == 2;
+          acc_z += v == 3;
+        }
         if (status != ST_OK) break;
       }
       if (F32 && P.resync_every > 0 && idx % P.resync_every == 0) {
         double e64 = walker_energy64<POT, BC, ENS>(
-            X, N, L, rc2, s_c, K, hn, hm, ean, ecam, nullptr, nullptr,
+            X, N, L, H, rc2, s_c, K, hn, hm, ean, ecam, nullptr, nullptr,
             POT == POT_EAM ? s_c32 + (size_t)w * N : nullptr, lane);
         drift = fmax(drift, fabs(en - e64));
         en = e64;
@@ -585,10 +707,17 @@ __global__ void __launch_bounds__(1024)
     if (lane == 0) {
       s_en[w] = en;
       s_box[w] = L;
+      s_boxh[w] = H;
       s_cnt[6 * slot + 0] += acc_a;
       s_cnt[6 * slot + 1] += acc_a;
       s_cnt[6 * slot + 2] += acc_v;
       s_cnt[6 * slot + 3] += acc_v;
+      if (has_height<BC>()) {  // count_vol_xy, count_vol_z
+        s_cnt_sep[4 * slot + 0] += acc_xy;
+        s_cnt_sep[4 * slot + 1] += acc_xy;
+        s_cnt_sep[4 * slot + 2] += acc_z;
+        s_cnt_sep[4 * slot + 3] += acc_z;
+      }
     }
     __syncthreads();
     if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
@@ -599,10 +728,9 @@ __global__ void __launch_bounds__(1024)
         s_cnt[6 * (k + 1) + 4] += 1;
         int w1 = s_wos[k], w2 = s_wos[k + 1];
         double e1 = s_en[w1], e2 = s_en[w2];
-        if (ENS == ENS_NPT) {
-          double L1 = s_box[w1], L2 = s_box[w2];
-          e1 = dadd(e1, dmul(P.pressure, dmul(dmul(L1, L1), L1)));
-          e2 = dadd(e2, dmul(P.pressure, dmul(dmul(L2, L2), L2)));
+        if (ENS == ENS_NPT) {  // enthalpies with get_volume (src/Exchange.jl:166-176)
+          e1 = dadd(e1, dmul(P.pressure, box_volume<BC>(s_box[w1], s_boxh[w1])));
+          e2 = dadd(e2, dmul(P.pressure, box_volume<BC>(s_box[w2], s_boxh[w2])));
         }
         double acc = exp((s_beta[k] - s_beta[k + 1]) * (e1 - e2));
         if (acc > 1.0) acc = 1.0;
@@ -624,11 +752,22 @@ __global__ void __launch_bounds__(1024)
         if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
         else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
         s_cnt[6 * s + 1] = 0;
-        if (ENS == ENS_NPT) {
+        if (ENS == ENS_NPT && !(has_height<BC>() && P.sep_vol)) {
           double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);
           if (av < P.min_acc) s_maxd[2 * s + 1] *= 0.9;
           else if (av > P.max_acc) s_maxd[2 * s + 1] *= 1.1;
           s_cnt[6 * s + 3] = 0;
+        } else if (ENS == ENS_NPT) {  // separated: all, xy, z (src/Exchange.jl:221-244)
+          const double nu = (double)(P.n_adjust * 1);
+          auto adapt = [&](long long& c, double& mdx, double den) {
+            double av = (double)c / den;
+            if (av < P.min_acc) mdx *= 0.9;
+            else if (av > P.max_acc) mdx *= 1.1;
+            c = 0;
+          };
+          adapt(s_cnt[6 * s + 3], s_maxd[2 * s + 1], nu * 1 / 2);
+          adapt(s_cnt_sep[4 * s + 1], s_maxd_sep[2 * s], nu * 1 / 3);
+          adapt(s_cnt_sep[4 * s + 3], s_maxd_sep[2 * s + 1], nu / 6);
         }
       }
       if (phase == PHASE_PROD && idx % P.mc_sample == 0) {  // sampling_step!
@@ -642,13 +781,13 @@ __global__ void __launch_bounds__(1024)
           return (int)floor(h) + 1;
         };
         if (ENS == ENS_NPT) {
-          double Lw = s_box[wk];
-          double V = dmul(dmul(Lw, Lw), Lw);
-          double H = dadd(e, dmul(P.pressure, V));
-          s_ham[2 * s] += H;
-          s_ham[2 * s + 1] = dadd(s_ham[2 * s + 1], dmul(H, H));
+          const double Lw = s_box[wk], Hw = s_boxh[wk];
+          double V = box_volume<BC>(Lw, Hw);
+          double Hs = dadd(e, dmul(P.pressure, V));
+          s_ham[2 * s] += Hs;
+          s_ham[2 * s + 1] = dadd(s_ham[2 * s + 1], dmul(Hs, Hs));
           int ie = hidx(floor((e - rd.en_min) / rd.dE) + 1);
-          int iv = hidx(floor((V - rd.v_min) / rd.dV) + 1);
+          int iv = hidx(floor((hist_volume<BC>(Lw, Hw) - rd.v_min) / rd.dV) + 1);
           atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
         } else {
           s_ham[2 * s] += e;
@@ -667,10 +806,8 @@ __global__ void __launch_bounds__(1024)
         for (int k = lane; k < i; k += 32) {
           double r2;
           if (M) r2 = M[(size_t)i * N + k];
-          else if (BC == BC_CUB)
-            r2 = d2_cub(X[3 * i], X[3 * i + 1], X[3 * i + 2], X[3 * k], X[3 * k + 1], X[3 * k + 2], L);
           else
-            r2 = d2_sph(X[3 * i], X[3 * i + 1], X[3 * i + 2], X[3 * k], X[3 * k + 1], X[3 * k + 2]);
+            r2 = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * k, L, H);
           rdf_add(row, 5 * P.n_bin, r2, rd.dr2);
         }
     }
@@ -694,6 +831,7 @@ __global__ void __launch_bounds__(1024)
   if (lane == 0) {
     P.en[g] = en;
     P.box[g] = L;
+    if (has_height<BC>()) P.boxh[g] = H;
     P.rc2[g] = rc2;
     P.ctr[g] = ctr;
     P.status[g] = status;
@@ -707,6 +845,11 @@ __global__ void __launch_bounds__(1024)
     P.maxd[2 * gs + 1] = s_maxd[2 * s + 1];
     for (int q = 0; q < 6; ++q) P.cnt[6 * (size_t)gs + q] = s_cnt[6 * s + q];
     P.wos[gs] = s_wos[s];
+    if (has_height<BC>()) {
+      P.maxd_sep[2 * gs] = s_maxd_sep[2 * s];
+      P.maxd_sep[2 * gs + 1] = s_maxd_sep[2 * s + 1];
+      for (int q = 0; q < 4; ++q) P.cnt_sep[4 * (size_t)gs + q] = s_cnt_sep[4 * s + q];
+    }
   }
   if (tid == 0) {
     P.runs[run0 + blockIdx.x].cyc[phase] = first + ncycles;
@@ -723,7 +866,7 @@ __global__ void __launch_bounds__(1024) k_resync(KParams P, int run0) {
   const int g = rd.wk + w;
   const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
   double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
-  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.rc2[g], P.c, P.K,
+  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
                                            -0.5 * P.eam_n, -0.5 * P.eam_m,
                                            P.eam_ean, P.eam_ecam, nullptr, comp,
                                            nullptr, lane);
@@ -792,6 +935,19 @@ static int dispatch(int pot, int bc, int ens, bool f32, int what,
   PT_CASE(POT_EAM, BC_CUB, ENS_NVT)
   PT_CASE(POT_ELJEVEN, BC_CUB, ENS_NPT)
 #undef PT_CASE
+  // RectangularBC / RhombicBC: plain FP64 form only
+#define PT_CASE64(PO, B, E)                                                              \
+  if (pot == PO && bc == B && ens == E)                                                  \
+    return f32 ? (int)cudaErrorInvalidValue                                              \
+               : run_instance<PO, B, E, false>(what, P, run0, nruns, R, maxN, ncycles,   \
+                                               phase, st);
+  PT_CASE64(POT_ELJ, BC_RECT, ENS_NVT)
+  PT_CASE64(POT_ELJEVEN, BC_RECT, ENS_NVT)
+  PT_CASE64(POT_ELJ, BC_RHB, ENS_NVT)
+  PT_CASE64(POT_ELJEVEN, BC_RHB, ENS_NVT)
+  PT_CASE64(POT_ELJEVEN, BC_RECT, ENS_NPT)
+  PT_CASE64(POT_ELJEVEN, BC_RHB, ENS_NPT)
+#undef PT_CASE64
   return -1;
 }
 

@@ -83,6 +83,31 @@ __device__ __forceinline__ double d2_cub(double ax, double ay, double az,
   return dot3(dsub(ax, ix), dsub(ay, iy), dsub(az, iz));
 }
 
+// RectangularBC minimum image, side L in x and y, height H in z
+// (src/Configurations.jl:121-126)
+__device__ __forceinline__ double d2_rect(double ax, double ay, double az,
+                                          double bx, double by, double bz,
+                                          double L, double H) {
+  double ix = dadd(bx, dmul(L, rint(ddiv(dsub(ax, bx), L))));
+  double iy = dadd(by, dmul(L, rint(ddiv(dsub(ay, by), L))));
+  double iz = dadd(bz, dmul(H, rint(ddiv(dsub(az, bz), H))));
+  return dot3(dsub(ax, ix), dsub(ay, iy), dsub(az, iz));
+}
+// sqrt(3) as a double (the value of 3^0.5 in the reference)
+constexpr double SQRT3 = 1.7320508075688772;
+// RhombicBC minimum image (src/Configurations.jl:110-120): y on the rhombus
+// height sqrt(3)/2 L, x along the sheared axis, z on the height H
+__device__ __forceinline__ double d2_rhb(double ax, double ay, double az,
+                                         double bx, double by, double bz,
+                                         double L, double H) {
+  const double hy = dmul(SQRT3 / 2, L), is3 = 1.0 / SQRT3;
+  double iy = dadd(by, dmul(hy, rint(ddiv(dsub(ay, by), hy))));
+  double q = ddiv(dsub(dsub(ax, bx), dmul(is3, dsub(ay, by))), L);
+  double ix = dadd(dadd(dsub(bx, ddiv(by, SQRT3)), dmul(L, rint(q))), dmul(is3, iy));
+  double iz = dadd(bz, dmul(H, rint(ddiv(dsub(az, bz), H))));
+  return dot3(dsub(ax, ix), dsub(ay, iy), dsub(az, iz));
+}
+
 // FP32 minimum image for the FP32 form
 __device__ __forceinline__ float f2_cub(float dx, float dy, float dz, float L,
                                         float iL) {

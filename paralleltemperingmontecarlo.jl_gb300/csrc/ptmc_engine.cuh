@@ -8,8 +8,11 @@
 //   mat   f64 [sum_r R_r*N_r*N_r] NPT plain form: squared-distance matrix
 //   comp  f64 [sum_r R_r*N_r*2]   EAM (phi_i, rho_i) components
 //   en/box/rc2/drift f64 [W], ctr u64 [W], status i32 [W]   per walker
+//   boxh f64 [W]  box height (RectangularBC / RhombicBC)     per walker
 //   beta/maxbox f64 [W], maxd f64 [2W], ham f64 [2W], cnt i64 [6W],
 //   wos i32 [W]                                              per slot
+//   maxboxh f64 [W], maxd_sep f64 [2W], cnt_sep i64 [4W]     per slot,
+//   separated volume moves (max_displ[3:4], count_vol_xy/_z)
 //   hist u32 [sum_r R_r*stride_r]  NVT: (n_bin+2) per slot, NPT: (n_bin+2)^2
 #pragma once
 #include <cstdint>
@@ -18,7 +21,7 @@
 namespace ptmc {
 
 enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3 };
-enum { BC_SPH = 0, BC_CUB = 1 };
+enum { BC_SPH = 0, BC_CUB = 1, BC_RECT = 2, BC_RHB = 3 };  // RECT/RHB: length L, height H
 enum { ENS_NVT = 0, ENS_NPT = 1 };
 enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
 enum { ST_OK = 0, ST_SPHERE = 1, ST_TIMEOUT = 2 };  // TIMEOUT: a bounded tensor-core wait ran out
@@ -74,6 +77,12 @@ struct KParams {
   int* wos;
   unsigned int* hist;
   unsigned int* rdf;        // [slots][5 n_bin] radial distribution (NULL = off)
+  // RectangularBC / RhombicBC and NPT separated volume moves
+  double* boxh;             // [W] walker box height
+  double* maxboxh;          // [W] slot max_boxheight (MCStates.jl:79-87)
+  double* maxd_sep;         // [2W] slot max_displ[3] (xy), max_displ[4] (z)
+  long long* cnt_sep;       // [4W] slot count_vol_xy[1:2], count_vol_z[1:2]
+  int sep_vol;              // NPT.separated_volume
   // potential
   double c[MAX_COEFF];
   int K;
@@ -107,6 +116,9 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
   b += al((long long)R * 8) * 6;                     // beta, maxbox, en, box, ham(2)
   b += al((long long)R * 16);                        // maxd
   b += al((long long)R * 6 * 8);                     // counters
+  b += al((long long)R * 8) * 2;                     // boxh, maxboxh
+  b += al((long long)R * 16);                        // maxd_sep
+  b += al((long long)R * 4 * 8);                     // cnt_sep
   b += al((long long)R * 4) * 2;                     // wos, sow
   return b;
 }

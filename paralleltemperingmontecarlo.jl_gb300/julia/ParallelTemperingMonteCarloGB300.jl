@@ -106,11 +106,17 @@ function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential,
         # 3 x N x n_start, column-major: exactly the layout of Vector{SVector{3}}
         xyz = reduce(hcat, [reduce(hcat, cf.positions) for cf in configs])
         bc = configs[1].boundary_condition
-        kind, par = bc isa SphericalBC ? (0, sqrt(bc.radius2)) : (1, bc.box_length)
+        kind, len, hgt = bc isa SphericalBC ? (0, sqrt(bc.radius2), sqrt(bc.radius2)) :
+                         bc isa CubicBC ? (1, bc.box_length, bc.box_length) :
+                         bc isa RectangularBC ? (2, bc.box_length, bc.box_height) :
+                         (3, bc.box_length, bc.box_height)   # RhombicBC
         rdfsave && check(ccall((:ptmc_set_rdf, libptmc), Cint, (Ptr{Cvoid}, Cint), c, 1), c)
-        check(ccall((:ptmc_set_run_configs, libptmc), Cint,
-                    (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cint, Cint, Cdouble),
-                    c, 0, xyz, N, length(configs), kind, par), c)
+        if npt && ensemble.separated_volume
+            check(ccall((:ptmc_set_separated_volume, libptmc), Cint, (Ptr{Cvoid}, Cint), c, 1), c)
+        end
+        check(ccall((:ptmc_set_run_configs_box, libptmc), Cint,
+                    (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cint, Cint, Cdouble, Cdouble),
+                    c, 0, xyz, N, length(configs), kind, len, hgt), c)
         check(ccall((:ptmc_init, libptmc), Cint, (Ptr{Cvoid},), c), c)
         check(ccall((:ptmc_equilibrate, libptmc), Cint, (Ptr{Cvoid},), c), c)
         done = 0

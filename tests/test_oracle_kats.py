@@ -209,6 +209,100 @@ def test_oracle_npt_invariants(orc):
     assert ev.sum() == R * 60
 
 
+def test_rhombic_box_known_answers(orc):
+    """test/runtests.jl:119-129, 186-215: rhombic distances (minimum image across
+    the sheared face), get_r_cut and get_volume, bit for bit."""
+    s3 = 3 ** 0.5
+    bc = orc.BC_RHOMBIC
+    v1, v2, v3 = [1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [3.0, 6.0, 9.0]
+    assert orc.distance2_box(v1, v2, bc, 10.0, 10.0) == 14.0
+    assert orc.distance2(v1, v3) == 56.0
+    assert orc.distance2_box(v1, v3, bc, 10.0, 10.0) == 36.0
+    assert orc.distance2_box(v1, [15.0, 5.0 * s3, 2.0], bc, 10.0, 10.0) == 6.0
+    assert orc.box_rcut(bc, 10.0, 10.0) == 10.0 ** 2 * 3 / 16
+    assert orc.box_rcut(bc, 10.0, 5.0) == 5.0 ** 2 / 4
+    assert orc.box_volume(bc, 10.0, 10.0) == s3 / 2 * 1000.0
+    assert orc.box_volume(orc.BC_CUBIC, 10.0, 10.0) == 1000.0
+    # rectangular: min(L^2/4, H^2/4), L^2 H, per-axis minimum image
+    assert orc.box_rcut(orc.BC_RECT, 10.0, 6.0) == 9.0
+    assert orc.box_volume(orc.BC_RECT, 10.0, 6.0) == 600.0
+    assert orc.distance2_box([0.0, 0.0, 0.0], [9.0, 1.0, 5.0], orc.BC_RECT, 10.0, 6.0) == 3.0
+
+
+def rhombic_hcp(n, m, a):
+    """n x n triangular layers (side a) stacked ABAB in z (spacing a sqrt(2/3))
+    inside RhombicBC(n a, m c): x - y/sqrt(3) in [0, L), y in [0, L sqrt(3)/2)."""
+    s3 = 3 ** 0.5
+    c = a * (2.0 / 3.0) ** 0.5
+    pts = []
+    for k in range(m):
+        ox, oy = (a / 2, a / (2 * s3)) if k % 2 else (0.0, 0.0)
+        for j in range(n):
+            for i in range(n):
+                pts.append((i * a + j * a / 2 + ox, j * a * s3 / 2 + oy, k * c + 0.25 * c))
+    return np.array(pts), n * a, m * c
+
+
+def test_oracle_separated_volume_rhombic(orc):
+    """NPT with separated volume moves in a RhombicBC (volume_change_separated,
+    src/MCMoves.jl:298-343): xy, z and uniform moves are all accepted, the box
+    aspect changes, every walker's energy equals dimer_energy_config with the
+    rhombic cut-off and long-range correction, and atoms stay in the cell."""
+    x0, L, H = rhombic_hcp(3, 4, 5.9)
+    N, R = len(x0), 4
+    T, _ = orc.tempgrid(10.0, 30.0, R)
+    run = orc.Run(N, R, np.stack([x0] * R), T, ensemble=orc.NPT, pressure=3.4439647528956955e-9,
+                  bc=orc.BC_RHOMBIC, bc_param=L, exch_prob=1.0, seed=21)
+    run.set_box(H, separated=True)
+    run.set_elj(C_NE, True)
+    run.init()
+    run.equilibrate(100)
+    run.production(1, 200)
+    x, e, Lw = run.slot_states()
+    b = run.box()
+    wos = run.slots()["wos"]
+    Hw = b["height"][wos]
+    s = run.slots()
+    assert s["count_vol"][:, 0].sum() > 0
+    assert b["count_xy"][:, 0].sum() > 0 and b["count_z"][:, 0].sum() > 0
+    assert np.any(np.abs(Lw / Hw - L / H) > 1e-6)
+    s3 = 3 ** 0.5
+    for i in range(R):
+        ref = orc.elj_config_energy_box(x[i], orc.POT_ELJEVEN, C_NE, orc.BC_RHOMBIC, Lw[i], Hw[i])
+        assert e[i] == pytest.approx(ref, rel=1e-9)
+        u = x[i][:, 0] - x[i][:, 1] / s3
+        assert np.all(u > -0.6 * Lw[i]) and np.all(u < 1.6 * Lw[i])
+        assert np.all(x[i][:, 2] > -0.6 * Hw[i]) and np.all(x[i][:, 2] < 1.6 * Hw[i])
+    _, ev, hp = run.hist()
+    assert ev.sum() == R * 200
+
+
+def test_oracle_rectangular_uniform_npt(orc):
+    """RectangularBC with uniform volume moves: L and H scale together (the
+    aspect is kept to rounding), energies follow dimer_energy_config."""
+    a = 8.4
+    cells = [(i, j, k) for i in range(2) for j in range(2) for k in range(3)]
+    basis = [(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)]
+    x0 = np.array([[(c[d] + b[d]) * a for d in range(3)] for c in cells for b in basis])
+    x0 -= np.array([a, a, 1.5 * a])
+    N, R = len(x0), 3
+    T, _ = orc.tempgrid(10.0, 30.0, R)
+    run = orc.Run(N, R, np.stack([x0] * R), T, ensemble=orc.NPT, pressure=3.4439647528956955e-9,
+                  bc=orc.BC_RECT, bc_param=2 * a, exch_prob=1.0, seed=5)
+    run.set_box(3 * a)
+    run.set_elj(C_NE, True)
+    run.init()
+    run.cycles(1, 150)
+    x, e, Lw = run.slot_states()
+    Hw = run.box()["height"][run.slots()["wos"]]
+    assert run.slots()["count_vol"][:, 0].sum() > 0
+    np.testing.assert_allclose(Lw / Hw, 2.0 / 3.0, rtol=1e-12)
+    assert np.any(Lw != 2 * a)
+    for i in range(R):
+        ref = orc.elj_config_energy_box(x[i], orc.POT_ELJEVEN, C_NE, orc.BC_RECT, Lw[i], Hw[i])
+        assert e[i] == pytest.approx(ref, rel=1e-9)
+
+
 # ---------------------------------------------------------------- surrogate oracle
 SUR_CFG = [2.0, 12.0, 1.125, 12.0, 0.02]
 
