@@ -104,6 +104,21 @@ int ptmc_create(ptmc_ctx** out, const ptmc_params* p);
 /* ELJPotential / ELJPotentialEven (src/EnergyEvaluation.jl:923-942);
  * c has K <= 16 coefficients for powers 6,7,8,... (even=0) or 6,8,10,... (even=1) */
 int ptmc_set_potential_elj(ptmc_ctx* c, const double* coeff, int K, int even);
+/* ELJPotentialB(a, b, c) (src/EnergyEvaluation.jl:161-183): the extended
+ * Lennard-Jones dimer in a magnetic field, c_k r^-p_k (1 + a_k cos 2theta +
+ * b_k cos 4theta) with theta the pair angle to z (dimer_energy, :943-958);
+ * K = 2..16.  Plain FP64 form; NVT with SphericalBC/CubicBC, NPT with
+ * CubicBC/RectangularBC/RhombicBC. */
+int ptmc_set_potential_eljb(ptmc_ctx* c, const double* a, const double* b,
+                            const double* coeff_c, int K);
+/* LookupTablePotential (src/EnergyEvaluation.jl:210-298): the fields of the
+ * reference's struct; table is its Matrix{Float64}(l_angle, l_dist) in Julia's
+ * column-major order (entry (angle a, distance d) at (d-1)*l_angle + (a-1)),
+ * so a Julia caller passes pot.table as is.  Same ensembles and boxes as
+ * ELJPotentialB. */
+int ptmc_set_potential_lookup(ptmc_ctx* c, const double* table, int l_angle,
+                              int l_dist, double start_dist, double start_angle,
+                              double d_dist, double d_angle, double c6coeff);
 /* EmbeddedAtomPotential(n, m, ean, eCam) (src/EnergyEvaluation.jl:1059-1073) */
 int ptmc_set_potential_eam(ptmc_ctx* c, double n, double m, double ean,
                            double ecam);

@@ -15,6 +15,7 @@ SRC = os.path.join(HERE, "ptmc_oracle.cpp")
 
 POT_ELJ, POT_ELJEVEN, POT_EAM, POT_NN = 0, 1, 2, 3
 BC_SPHERE, BC_CUBIC, BC_RECT, BC_RHOMBIC = 0, 1, 2, 3
+POT_ELJB, POT_LUT = 4, 5
 NVT, NPT = 0, 1
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -77,6 +78,15 @@ def lib():
         L.orc_elj_config_energy_box.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                 ctypes.c_int]
+        L.orc_get_tan.restype = ctypes.c_double
+        L.orc_get_tan.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_eljb_energy.restype = ctypes.c_double
+        L.orc_eljb_energy.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_lut_energy.restype = ctypes.c_double
+        L.orc_lut_energy.argtypes = [_dp, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6
+        L.orc_set_pot_eljb.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int]
+        L.orc_set_pot_lut.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int] + \
+            [ctypes.c_double] * 5
         L.orc_set_box.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, _dp]
         L.orc_get_box.argtypes = [ctypes.c_void_p, _dp, _dp, _lp, _lp]
         L.orc_eam_config_energy.restype = ctypes.c_double
@@ -151,6 +161,26 @@ def elj_config_energy_box(xyz, kind, c, bc, L, H, cut=True):
     x, c = _d(xyz), _d(c)
     return lib().orc_elj_config_energy_box(P(x), len(x), kind, P(c), len(c), bc, float(L),
                                            float(H), int(bool(cut)))
+
+
+def get_tan(a, b, bc=BC_SPHERE, L=0.0, H=None):
+    """get_tan (src/Configurations.jl:181-215)."""
+    a, b = _d(a), _d(b)
+    return lib().orc_get_tan(P(a), P(b), bc, float(L), float(L if H is None else H))
+
+
+def eljb_energy(a, b, c, r2, tn):
+    a, b, c = _d(a), _d(b), _d(c)
+    return lib().orc_eljb_energy(P(a), P(b), P(c), len(c), float(r2), float(tn))
+
+
+def lut_energy(lut, r2, tn):
+    """lut: dict(table [l_angle, l_dist], start_dist, d_dist, d_angle, c6coeff)."""
+    t = np.asfortranarray(lut["table"], dtype=np.float64)
+    flat = np.ascontiguousarray(t.reshape(-1, order="F"))
+    la, ld = t.shape
+    return lib().orc_lut_energy(P(flat), la, ld, lut["start_dist"], lut["d_dist"], lut["d_angle"],
+                                lut["c6coeff"], float(r2), float(tn))
 
 
 def lrc(N, rc2, c):
@@ -258,6 +288,19 @@ class Run:
     def set_elj(self, c, even):
         c = _d(c)
         _check(lib().orc_set_pot_elj(self.h, P(c), len(c), int(even)))
+
+    def set_eljb(self, a, b, c):
+        self._eljb = (_d(a), _d(b), _d(c))
+        _check(lib().orc_set_pot_eljb(self.h, *(P(x) for x in self._eljb), len(self._eljb[2])))
+
+    def set_lut(self, lut):
+        """lut: dict(table [l_angle, l_dist], start_dist, start_angle, d_dist, d_angle, c6coeff)."""
+        t = np.asarray(lut["table"], dtype=np.float64)
+        self._lut = np.ascontiguousarray(t.reshape(-1, order="F"))
+        la, ld = t.shape
+        _check(lib().orc_set_pot_lut(self.h, P(self._lut), la, ld, lut["start_dist"],
+                                     lut.get("start_angle", 0.0), lut["d_dist"], lut["d_angle"],
+                                     lut["c6coeff"]))
 
     def set_eam(self, n, m, ean, ecam):
         _check(lib().orc_set_pot_eam(self.h, n, m, ean, ecam))

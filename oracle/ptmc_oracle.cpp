@@ -128,6 +128,26 @@ inline double box_volume(int bc, double L, double H) {
   return L * L * L;
 }
 
+// get_tan (src/Configurations.jl:181-215): |tan| of the angle between the
+// (minimum-image) pair vector and z, sqrt(dx^2 + dy^2) / dz
+inline double tan_bc(int bc, const double* a, const double* b, double L, double H) {
+  double bx = b[0], by = b[1], bz = b[2];
+  if (bc == ORC_BC_CUBIC || bc == ORC_BC_RECT) {
+    const double Hz = bc == ORC_BC_RECT ? H : L;
+    bx = b[0] + L * std::nearbyint((a[0] - b[0]) / L);
+    by = b[1] + L * std::nearbyint((a[1] - b[1]) / L);
+    bz = b[2] + Hz * std::nearbyint((a[2] - b[2]) / Hz);
+  } else if (bc == ORC_BC_RHOMBIC) {
+    const double hy = S3 / 2 * L, is3 = 1 / S3;
+    by = b[1] + hy * std::nearbyint((a[1] - b[1]) / hy);
+    bx = ((b[0] - b[1] / S3) + L * std::nearbyint(((a[0] - b[0]) - is3 * (a[1] - b[1])) / L)) +
+         is3 * by;
+    bz = b[2] + H * std::nearbyint((a[2] - b[2]) / H);
+  }
+  const double dx = a[0] - bx, dy = a[1] - by;
+  return std::fabs(std::sqrt(dx * dx + dy * dy) / (a[2] - bz));
+}
+
 // ---------------------------------------------------------------- potentials
 struct SF {
   int kind, type;
@@ -136,7 +156,13 @@ struct SF {
 
 struct Pot {
   int kind = -1;
-  std::vector<double> c;  // ELJ coefficients
+  std::vector<double> c;  // ELJ coefficients (ELJPotentialB: coeff_c)
+  std::vector<double> a, b;  // ELJPotentialB coeff_a, coeff_b
+  // LookupTablePotential: table [l_dist][l_angle] (Julia's column-major
+  // Matrix(l_angle, l_dist)), first distance, steps, c6 tail coefficient
+  std::vector<double> lut;
+  int l_dist = 0, l_angle = 0;
+  double start_dist = 0, start_angle = 0, d_dist = 0, d_angle = 0, c6 = 0;
   double n = 0, m = 0, ean = 0, ecam = 0;
   // NN
   std::vector<SF> sf;
@@ -166,6 +192,44 @@ double elj_even(const double* c, int K, double r2) {
   }
   return s;
 }
+// dimer_energy ELJPotentialB (EnergyEvaluation.jl:943-958): terms r^-6, r^-8,
+// then one more power of 1/r each, scaled by 1 + a cos 2theta + b cos 4theta
+double eljb(const Pot& p, double r2, double tn) {
+  if (!(r2 >= 5.30)) return 0.1;
+  double r6inv = 1 / (r2 * r2 * r2);
+  const double t2 = 2 / (tn * tn + 1) - 1;  // cos(2 theta)
+  const double t4 = 2 * (t2 * t2) - 1;
+  double s = p.c[0] * r6inv * (1 + p.a[0] * t2 + p.b[0] * t4);
+  r6inv /= r2;
+  for (size_t i = 1; i < p.c.size(); ++i) {
+    s += p.c[i] * r6inv * (1 + p.a[i] * t2 + p.b[i] * t4);
+    r6inv /= std::sqrt(r2);
+  }
+  return s;
+}
+// dimer_energy LookupTablePotential (EnergyEvaluation.jl:277-298); Julia's
+// round is half-to-even (nearbyint); the indices are kept inside the table
+double lut_energy(const Pot& p, double r2, double tn) {
+  int ia = 1;
+  const double at = std::fabs(tn);
+  if (at > 0.00872687153 && at <= 114.592845357)
+    ia = (int)std::nearbyint(std::atan(at) / p.d_angle * 180.0 / M_PI + 1.0);
+  else if (at > 114.592845357)
+    ia = 91;
+  ia = std::min(std::max(ia, 1), p.l_angle);
+  const double r0 = p.start_dist + 0.5 * p.d_dist, r1 = p.start_dist + p.l_dist * p.d_dist;
+  if (r2 <= r0 * r0) return p.lut[(size_t)(ia - 1)];
+  if (r2 <= r1 * r1) {
+    int id = (int)std::nearbyint((std::sqrt(r2) - p.start_dist) / p.d_dist);
+    id = std::min(std::max(id, 1), p.l_dist);
+    return p.lut[(size_t)(id - 1) * p.l_angle + (ia - 1)];
+  }
+  return p.c6 / (r2 * r2 * r2);
+}
+inline bool is_b(const Pot& p) { return p.kind == ORC_POT_ELJB || p.kind == ORC_POT_LUT; }
+inline double dimer_b(const Pot& p, double r2, double tn) {
+  return p.kind == ORC_POT_ELJB ? eljb(p, r2, tn) : lut_energy(p, r2, tn);
+}
 inline double dimer(const Pot& p, double r2) {
   return p.kind == ORC_POT_ELJ ? elj_all(p.c.data(), (int)p.c.size(), r2)
                                : elj_even(p.c.data(), (int)p.c.size(), r2);
@@ -181,6 +245,64 @@ double lrc_even(int N, double r_cut, const double* c, int K) {
     rc3 *= r_cut;
   }
   e *= M_PI * (double)(N * N) / 4 / (rcs * rcs * rcs);
+  return e;
+}
+// lrc of ELJPotentialB (EnergyEvaluation.jl:983-998): fixed coefficients
+double lrc_eljb(int N, double r_cut) {
+  static const double cf[4] = {-0.1279111890228638, -1.328138539967966, 12.260941135261255,
+                               41.12212408251662};
+  if (r_cut <= 16) return 0.0;
+  double rcs = std::sqrt(r_cut);
+  double rc3 = r_cut * rcs;
+  double e = 0.0;
+  for (int i = 1; i <= 4; ++i) {
+    e += cf[i - 1] / rc3 / (2 * i + 1);
+    rc3 *= r_cut;
+  }
+  e *= M_PI * (double)(N * N) / 4 / (rcs * rcs * rcs);
+  return e;
+}
+// lrc of LookupTablePotential (EnergyEvaluation.jl:999-1009): 1.0 below r_cut = 10
+double lrc_lut(int N, double r_cut, double c6) {
+  if (r_cut <= 10) return 1.0;
+  double rcs = std::sqrt(r_cut);
+  double rc3 = r_cut * rcs;
+  double e = c6 / rc3 / 3;
+  e *= M_PI * (double)(N * N) / 4 / (rcs * rcs * rcs);
+  return e;
+}
+// the potential's long-range correction with the box factor of
+// dimer_energy_config (EnergyEvaluation.jl:419, 444, 469-472, 587, 634-637, 743)
+double lrc_pot(const Pot& p, int N, double rc2, int bc, double L, double H) {
+  double l = p.kind == ORC_POT_ELJB  ? lrc_eljb(N, rc2)
+             : p.kind == ORC_POT_LUT ? lrc_lut(N, rc2, p.c6)
+                                     : lrc_even(N, rc2, p.c.data(), (int)p.c.size());
+  if (bc == ORC_BC_RHOMBIC) l = l * 3 / 4 * L / H;
+  else if (bc == ORC_BC_RECT) l = L < H ? l * L / H : l * (H * H) / (L * L);
+  return l;
+}
+// dimer_energy_atom with the tangent row (EnergyEvaluation.jl:334-361)
+double dimer_atom_b(const Pot& p, int i, const double* d2, const double* tn, int N, bool cut,
+                    double rc2) {
+  double s = 0.0;
+  for (int j = 0; j < N; ++j) {
+    if (j == i) continue;
+    if (cut && !(d2[j] <= rc2)) continue;
+    s += dimer_b(p, d2[j], tn[j]);
+  }
+  return s;
+}
+// dimer_energy_config with the tangent matrix (EnergyEvaluation.jl:476-640, 657-780)
+double dimer_config_b(const Pot& p, const double* d2, const double* tn, int N, bool cut,
+                      double rc2, int bc, double L, double H) {
+  double e = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int j = i + 1; j < N; ++j) {
+      const double x = d2[(size_t)i * N + j];
+      if (cut && !(x <= rc2)) continue;
+      e += dimer_b(p, x, tn[(size_t)i * N + j]);
+    }
+  if (cut) e = e + lrc_pot(p, N, rc2, bc, L, H);
   return e;
 }
 // dimer_energy_atom (EnergyEvaluation.jl:313-345): sum over j != i in order
@@ -207,10 +329,7 @@ double dimer_config(const Pot& p, const double* d2, int N, bool cut,
       e += dimer(p, x);
     }
   if (cut) {
-    double l = lrc_even(N, rc2, p.c.data(), (int)p.c.size());
-    if (bc == ORC_BC_RHOMBIC) l = l * 3 / 4 * L / H;
-    else if (bc == ORC_BC_RECT) l = L < H ? l * L / H : l * (H * H) / (L * L);
-    e = e + l;
+    e = e + lrc_pot(p, N, rc2, bc, L, H);
   }
   return e;
 }
@@ -418,6 +537,7 @@ struct orc_run {
   // walker-bound
   std::vector<double> pos;    // R*N*3
   std::vector<double> d2;     // R*N*N
+  std::vector<double> tn;     // R*N*N tangent matrix (ELJPotentialB, LookupTablePotential)
   std::vector<double> en;     // R
   std::vector<double> box;    // R (cubic side, box_length of the other boxes)
   std::vector<double> boxh;   // R (box_height of RectangularBC / RhombicBC)
@@ -450,6 +570,7 @@ struct orc_run {
   std::vector<double> rdf;   // R * 5 n_bin
   bool inited = false;
   // scratch
+  std::vector<double> trial_trow, sc_tn;
   std::vector<double> trial_row, new_comp, newG, newF, new_eatom, sc_pos,
       sc_d2;
 
@@ -461,6 +582,7 @@ struct orc_run {
   }
   double* P(int w) { return &pos[(size_t)w * N * 3]; }
   double* D(int w) { return &d2[(size_t)w * N * N]; }
+  double* TN(int w) { return &tn[(size_t)w * N * N]; }
 };
 
 namespace {
@@ -479,6 +601,17 @@ void build_d2(orc_run* r, int w) {
       d[(size_t)j * N + i] = x;
     }
   for (int i = 0; i < N; ++i) d[(size_t)i * N + i] = 0;
+  if (is_b(r->pot)) {  // get_tantheta_mat! (Configurations.jl:225-240)
+    double* t = r->TN(w);
+    for (int i = 0; i < N; ++i) {
+      t[(size_t)i * N + i] = 0;
+      for (int j = i + 1; j < N; ++j) {
+        double x = tan_bc(r->bc, p + 3 * i, p + 3 * j, r->box[w], r->boxh[w]);
+        t[(size_t)i * N + j] = x;
+        t[(size_t)j * N + i] = x;
+      }
+    }
+  }
 }
 
 // total_symm_calc (SymmFunc.jl:494-510), all angular rows computed (the
@@ -566,6 +699,7 @@ double init_energy(orc_run* r, int w) {
     return nn_energy(r, &r->G[(size_t)w * nsf(r) * N], &r->eatom[(size_t)w * N]);
   }
   bool cut = r->ens == ORC_NPT;
+  if (is_b(p)) return dimer_config_b(p, r->D(w), r->TN(w), N, cut, r->rcut2[w], r->bc, r->box[w], r->boxh[w]);
   return dimer_config(p, r->D(w), N, cut, r->rcut2[w], r->bc, r->box[w], r->boxh[w]);
 }
 
@@ -727,6 +861,15 @@ int atom_move(orc_run* r, int w, int slot, int i) {
       }
       new_en = nn_energy(r, nG, r->new_eatom.data());
     }
+  } else if (is_b(pot)) {  // energy_update! for the B potentials (:1508-1564)
+    double* trow = r->trial_trow.data();
+    for (int j = 0; j < N; ++j) trow[j] = tan_bc(r->bc, t, p + 3 * j, r->box[w], r->boxh[w]);
+    trow[i] = 0.0;
+    const bool cut = r->ens == ORC_NPT;
+    const double rc2 = r->rcut2[w];
+    const double* told = r->TN(w) + (size_t)i * N;
+    double dE = dimer_atom_b(pot, i, row, trow, N, cut, rc2) - dimer_atom_b(pot, i, old, told, N, cut, rc2);
+    new_en = dE + r->en[w];
   } else {  // dimer_energy_update! (:804-821)
     bool cut = r->ens == ORC_NPT;
     double rc2 = r->rcut2[w];
@@ -750,6 +893,13 @@ int atom_move(orc_run* r, int w, int slot, int i) {
     r->en[w] = new_en;
     r->cnt_atom[2 * slot] += 1;
     r->cnt_atom[2 * slot + 1] += 1;
+    if (is_b(pot)) {  // swap_vars! B potentials (swap_config.jl:198-206)
+      double* tm = r->TN(w);
+      for (int j = 0; j < N; ++j) {
+        tm[(size_t)i * N + j] = r->trial_trow[j];
+        tm[(size_t)j * N + i] = r->trial_trow[j];
+      }
+    }
     if (pot.kind == ORC_POT_EAM) {  // swap_vars! EAM (:208-211)
       std::memcpy(&r->comp[(size_t)w * N * 2], r->new_comp.data(), sizeof(double) * 2 * N);
     } else if (pot.kind == ORC_POT_NN && !hard) {  // swap_vars! NNP (:213-221)
@@ -819,6 +969,14 @@ int volume_move(orc_run* r, int w, int slot) {
   std::vector<double>& nd = r->sc_d2;
   std::vector<double>& np = r->sc_pos;
   const double* p = r->P(w);
+  const bool bpot = is_b(r->pot);
+  // tangents of the trial: recomputed for separated z / xy moves
+  // (get_tantheta_mat!, MCMoves.jl:336-341), unchanged otherwise
+  std::vector<double>& nt = r->sc_tn;
+  if (bpot) {
+    nt.resize((size_t)N * N);
+    std::memcpy(nt.data(), r->TN(w), sizeof(double) * N * N);
+  }
   if (r->sep) {  // get_distance2_mat! of the trial configuration
     np.resize((size_t)3 * N);
     for (int a = 0; a < N; ++a) {
@@ -832,6 +990,11 @@ int volume_move(orc_run* r, int w, int slot) {
         double x = dist2_bc(r->bc, &np[3 * i], &np[3 * j], Ln, Hn);
         nd[(size_t)i * N + j] = x;
         nd[(size_t)j * N + i] = x;
+        if (bpot && xy_or_z != 0) {
+          double y = tan_bc(r->bc, &np[3 * i], &np[3 * j], Ln, Hn);
+          nt[(size_t)i * N + j] = y;
+          nt[(size_t)j * N + i] = y;
+        }
       }
     }
   } else {  // dist2_mat .* scale^2
@@ -839,7 +1002,8 @@ int volume_move(orc_run* r, int w, int slot) {
     const double* d = r->D(w);
     for (size_t k = 0; k < (size_t)N * N; ++k) nd[k] = d[k] * s2;
   }
-  double new_en = dimer_config(r->pot, nd.data(), N, true, rc_new, r->bc, Ln, Hn);
+  double new_en = bpot ? dimer_config_b(r->pot, nd.data(), nt.data(), N, true, rc_new, r->bc, Ln, Hn)
+                       : dimer_config(r->pot, nd.data(), N, true, rc_new, r->bc, Ln, Hn);
   double Vn = box_volume(r->bc, Ln, Hn), Vo = box_volume(r->bc, L, H);
   double dh = (new_en - r->en[w]) + r->pressure * (Vn - Vo);
   double prob = std::exp(-dh * r->beta[slot] + (double)N * std::log(Vn / Vo));
@@ -855,6 +1019,7 @@ int volume_move(orc_run* r, int w, int slot) {
     r->box[w] = Ln;
     r->boxh[w] = Hn;
     std::memcpy(r->D(w), nd.data(), sizeof(double) * N * N);
+    if (bpot) std::memcpy(r->TN(w), nt.data(), sizeof(double) * N * N);
     r->en[w] = new_en;
     std::vector<long>& cv = xy_or_z == 0 ? r->cnt_vol : xy_or_z == 1 ? r->cnt_xy : r->cnt_z;
     cv[2 * slot] += 1;
@@ -1044,6 +1209,7 @@ orc_run* orc_create(int N, int R, int ensemble, double pressure, int bc_kind,
   r->wos.resize(R);
   for (int s = 0; s < R; ++s) r->wos[s] = s;
   r->trial_row.resize(N);
+  r->trial_trow.resize(N);
   r->new_comp.resize(2 * N);
   r->sc_d2.resize((size_t)N * N);
   r->newF.resize(N);
@@ -1085,6 +1251,31 @@ int orc_set_pot_elj(orc_run* r, const double* c, int K, int even) {
   r->pot.c.assign(c, c + K);
   if (r->ens == ORC_NPT && !even)
     return fail("NPT long-range correction is defined for ELJPotentialEven only");
+  return 0;
+}
+int orc_set_pot_eljb(orc_run* r, const double* a, const double* b, const double* c, int K) {
+  if (K < 2) return fail("ELJPotentialB needs at least two coefficients");
+  r->pot.kind = ORC_POT_ELJB;
+  r->pot.a.assign(a, a + K);
+  r->pot.b.assign(b, b + K);
+  r->pot.c.assign(c, c + K);
+  r->tn.assign((size_t)r->R * r->N * r->N, 0.0);
+  return 0;
+}
+int orc_set_pot_lut(orc_run* r, const double* table, int l_angle, int l_dist, double start_dist,
+                    double start_angle, double d_dist, double d_angle, double c6) {
+  if (l_angle < 1 || l_dist < 1 || !(d_dist > 0) || !(d_angle > 0))
+    return fail("lookup table: bad dimensions");
+  r->pot.kind = ORC_POT_LUT;
+  r->pot.lut.assign(table, table + (size_t)l_angle * l_dist);
+  r->pot.l_angle = l_angle;
+  r->pot.l_dist = l_dist;
+  r->pot.start_dist = start_dist;
+  r->pot.start_angle = start_angle;
+  r->pot.d_dist = d_dist;
+  r->pot.d_angle = d_angle;
+  r->pot.c6 = c6;
+  r->tn.assign((size_t)r->R * r->N * r->N, 0.0);
   return 0;
 }
 int orc_set_pot_eam(orc_run* r, double n, double m, double ean, double ecam) {
@@ -1285,6 +1476,31 @@ double orc_distance2_box(const double* a, const double* b, int bc_kind, double L
   return dist2_bc(bc_kind, a, b, L, H);
 }
 double orc_box_rcut(int bc_kind, double L, double H) { return box_rcut(bc_kind, L, H); }
+double orc_get_tan(const double* a, const double* b, int bc_kind, double L, double H) {
+  return tan_bc(bc_kind, a, b, L, H);
+}
+double orc_eljb_energy(const double* a, const double* b, const double* c, int K, double r2,
+                       double tn) {
+  Pot p;
+  p.kind = ORC_POT_ELJB;
+  p.a.assign(a, a + K);
+  p.b.assign(b, b + K);
+  p.c.assign(c, c + K);
+  return eljb(p, r2, tn);
+}
+double orc_lut_energy(const double* table, int l_angle, int l_dist, double start_dist,
+                      double d_dist, double d_angle, double c6, double r2, double tn) {
+  Pot p;
+  p.kind = ORC_POT_LUT;
+  p.lut.assign(table, table + (size_t)l_angle * l_dist);
+  p.l_angle = l_angle;
+  p.l_dist = l_dist;
+  p.start_dist = start_dist;
+  p.d_dist = d_dist;
+  p.d_angle = d_angle;
+  p.c6 = c6;
+  return lut_energy(p, r2, tn);
+}
 double orc_box_volume(int bc_kind, double L, double H) { return box_volume(bc_kind, L, H); }
 double orc_lrc(int N, double r_cut2, const double* c, int K) {
   return lrc_even(N, r_cut2, c, K);

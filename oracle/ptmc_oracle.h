@@ -33,6 +33,8 @@ typedef struct orc_run orc_run;
 #define ORC_POT_ELJEVEN 1  /* ELJPotentialEven  :934 */
 #define ORC_POT_EAM 2      /* EmbeddedAtomPotential :1059 */
 #define ORC_POT_NN 3       /* RuNNerPotential   :1182 */
+#define ORC_POT_ELJB 4     /* ELJPotentialB     :161 */
+#define ORC_POT_LUT 5      /* LookupTablePotential :210 */
 /* boundary kinds (src/BoundaryConditions.jl) */
 #define ORC_BC_SPHERE 0
 #define ORC_BC_CUBIC 1
@@ -63,6 +65,13 @@ const char* orc_last_error(void);
 
 int orc_set_pot_elj(orc_run* r, const double* c, int K, int even);
 int orc_set_pot_eam(orc_run* r, double n, double m, double ean, double ecam);
+/* ELJPotentialB(a, b, c) (EnergyEvaluation.jl:161-183) */
+int orc_set_pot_eljb(orc_run* r, const double* a, const double* b, const double* c, int K);
+/* LookupTablePotential (EnergyEvaluation.jl:210-260); table is Julia's
+ * Matrix(l_angle, l_dist), column-major: entry (angle a, distance d) at
+ * (d-1)*l_angle + (a-1) */
+int orc_set_pot_lut(orc_run* r, const double* table, int l_angle, int l_dist, double start_dist,
+                    double start_angle, double d_dist, double d_angle, double c6);
 /* sf: nsf rows of 8 doubles {kind(0 radial,1 angular), type, eta, lambda,
  * zeta, rcut, gmin, gmax}; weights: our layout (per layer: W[n_in][n_out]
  * input-major, then b[n_out]); nodes: n_layers node counts; boundary: hard-core
@@ -106,6 +115,12 @@ double orc_lrc(int N, double r_cut2, const double* c, int K);
 /* distance2, get_r_cut, get_volume of a box with length L and height H */
 double orc_distance2_box(const double* a, const double* b, int bc_kind, double L, double H);
 double orc_box_rcut(int bc_kind, double L, double H);
+/* get_tan, dimer_energy of ELJPotentialB and LookupTablePotential */
+double orc_get_tan(const double* a, const double* b, int bc_kind, double L, double H);
+double orc_eljb_energy(const double* a, const double* b, const double* c, int K, double r2,
+                       double tn);
+double orc_lut_energy(const double* table, int l_angle, int l_dist, double start_dist,
+                      double d_dist, double d_angle, double c6, double r2, double tn);
 double orc_box_volume(int bc_kind, double L, double H);
 /* dimer_energy_config over all pairs; cut != 0 applies get_r_cut and the
  * box-scaled long-range correction */

@@ -30,7 +30,8 @@ kB = 3.16681196e-6  # Hartree/K, src/InputParams.jl:19
 
 __all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "RectangularBC", "RhombicBC",
            "Config", "NVT", "NPT",
-           "ELJPotential", "ELJPotentialEven", "EmbeddedAtomPotential", "RuNNerPotential",
+           "ELJPotential", "ELJPotentialEven", "ELJPotentialB", "LookupTablePotential",
+           "read_lookuptable", "EmbeddedAtomPotential", "RuNNerPotential",
            "Output", "MCState", "PairSurrogate",
            "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
            "multihistogram", "postprocess",
@@ -220,6 +221,59 @@ class ELJPotential:
     coeff: list
 
     even = False
+
+
+@dataclass
+class ELJPotentialB:
+    """ELJPotentialB(a, b, c) (src/EnergyEvaluation.jl:161-183): the extended
+    Lennard-Jones dimer in a magnetic field; its energy depends on |tan| of
+    the pair angle to z (dimer_energy, :943-958)."""
+    coeff_a: list
+    coeff_b: list
+    coeff_c: list
+
+
+@dataclass
+class LookupTablePotential:
+    """LookupTablePotential (src/EnergyEvaluation.jl:210-260): table[angle,
+    distance] (l_angle x l_dist) of dimer energies; LookupTablePotential(path)
+    reads the reference's table format (read_lookuptable)."""
+    table: np.ndarray
+    start_dist: float
+    start_angle: float
+    l_dist: int
+    l_angle: int
+    d_dist: float
+    d_angle: float
+    c6coeff: float
+
+    @classmethod
+    def from_file(cls, path):
+        return cls(*read_lookuptable(path))
+
+
+def read_lookuptable(path):
+    """read_lookuptable (src/EnergyEvaluation.jl:227-256): line 1 "l_dist,
+    start_dist, d_dist", line 2 "l_angle, start_angle, d_angle" ('!' starts a
+    comment), then l_angle x l_dist values, angle-major; c6coeff = the mean
+    over angles of table[:, 1000] times (start_dist + 1000 d_dist)^6."""
+    with open(path) as f:
+        def line():
+            return f.readline().split("!")[0]
+        h = line().split(", ")
+        l_dist, start_dist, d_dist = int(h[0]), float(h[1]), float(h[2])
+        h = line().split(", ")
+        l_angle, start_angle, d_angle = int(h[0]), float(h[1]), float(h[2])
+        table = np.empty((l_angle, l_dist))
+        for i in range(l_angle):
+            for j in range(l_dist):
+                table[i, j] = float(line())
+    avg = 0.0
+    for i in range(l_angle):
+        avg += table[i, 999]
+    avg /= l_angle
+    c6 = avg * (start_dist + 1000 * d_dist) ** 6
+    return table, start_dist, start_angle, l_dist, l_angle, d_dist, d_angle, c6
 
 
 @dataclass
@@ -428,6 +482,16 @@ class Engine:
         if isinstance(potential, (ELJPotential, ELJPotentialEven)):
             c = np.ascontiguousarray(potential.coeff, dtype=np.float64)
             self._ck(self.L.ptmc_set_potential_elj(h, _dptr(c), len(c), int(potential.even)))
+        elif isinstance(potential, ELJPotentialB):
+            a, b, c = (np.ascontiguousarray(v, dtype=np.float64)
+                       for v in (potential.coeff_a, potential.coeff_b, potential.coeff_c))
+            self._ck(self.L.ptmc_set_potential_eljb(h, _dptr(a), _dptr(b), _dptr(c), len(c)))
+        elif isinstance(potential, LookupTablePotential):
+            t = np.asarray(potential.table, dtype=np.float64)
+            flat = np.ascontiguousarray(t.reshape(-1, order="F"))  # Julia's column-major
+            self._ck(self.L.ptmc_set_potential_lookup(
+                h, _dptr(flat), t.shape[0], t.shape[1], potential.start_dist,
+                potential.start_angle, potential.d_dist, potential.d_angle, potential.c6coeff))
         elif isinstance(potential, EmbeddedAtomPotential):
             self._ck(self.L.ptmc_set_potential_eam(h, potential.n, potential.m, potential.ean,
                                                    potential.eCam))

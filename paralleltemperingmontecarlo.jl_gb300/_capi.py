@@ -59,6 +59,9 @@ SIGNATURES = {
     "ptmc_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Params)]),
     "ptmc_set_potential_elj": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]),
     "ptmc_set_potential_eam": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_double] * 4),
+    "ptmc_set_potential_eljb": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int]),
+    "ptmc_set_potential_lookup": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]
+                                  + [ctypes.c_double] * 5),
     "ptmc_set_potential_nn": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, _dp,
                                              ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double]),
     "ptmc_set_run_configs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,

@@ -141,6 +141,11 @@ struct ptmc_ctx {
   bool sep_vol = false;        // NPT.separated_volume
   DBuf<double> d_boxh, d_maxboxh, d_maxd_sep;  // box height, max_boxheight, max_displ[3:4]
   DBuf<long long> d_cnt_sep;   // count_vol_xy[1:2], count_vol_z[1:2] per slot
+  // ELJPotentialB (coeff_c in coeff) and LookupTablePotential
+  std::vector<double> eljb_a, eljb_b, lut;
+  int lut_na = 0, lut_nd = 0;
+  double lut_par[4] = {0, 0, 0, 0};  // start_dist, d_dist, d_angle, c6coeff
+  DBuf<double> d_tan, d_lut;
   DBuf<unsigned long long> d_ctr;
   DBuf<int> d_status, d_wos;
   DBuf<long long> d_cnt;
@@ -411,6 +416,36 @@ int ptmc_set_potential_elj(ptmc_ctx* c, const double* coeff, int K, int even) {
   return PTMC_OK;
 }
 
+int ptmc_set_potential_eljb(ptmc_ctx* c, const double* a, const double* b, const double* cc,
+                            int K) {
+  if (!c || !a || !b || !cc) return PTMC_ERR_ARG;
+  if (K < 2 || K > MAX_COEFF) return c->fail(PTMC_ERR_ARG, "ELJPotentialB: 2..16 coefficients");
+  c->pot = POT_ELJB;
+  c->eljb_a.assign(a, a + K);
+  c->eljb_b.assign(b, b + K);
+  c->coeff.assign(cc, cc + K);
+  return PTMC_OK;
+}
+
+int ptmc_set_potential_lookup(ptmc_ctx* c, const double* table, int l_angle, int l_dist,
+                              double start_dist, double start_angle, double d_dist,
+                              double d_angle, double c6coeff) {
+  if (!c || !table) return PTMC_ERR_ARG;
+  if (l_angle < 1 || l_dist < 1 || !(d_dist > 0) || !(d_angle > 0))
+    return c->fail(PTMC_ERR_ARG, "LookupTablePotential: bad table dimensions or steps");
+  (void)start_angle;  // the angle index starts at 0 degrees (EnergyEvaluation.jl:279-285)
+  c->pot = POT_LUT;
+  c->lut.assign(table, table + (size_t)l_angle * l_dist);
+  c->lut_na = l_angle;
+  c->lut_nd = l_dist;
+  c->lut_par[0] = start_dist;
+  c->lut_par[1] = d_dist;
+  c->lut_par[2] = d_angle;
+  c->lut_par[3] = c6coeff;
+  c->coeff.clear();
+  return PTMC_OK;
+}
+
 int ptmc_set_potential_eam(ptmc_ctx* c, double n, double m, double ean, double ecam) {
   if (!c) return PTMC_ERR_ARG;
   if (c->p.ensemble == PTMC_NPT) return c->fail(PTMC_ERR_ARG, "EAM is supported in the NVT ensemble only");
@@ -558,19 +593,28 @@ int ptmc_init(ptmc_ctx* c) {
     }
   }
   const bool npt = c->p.ensemble == PTMC_NPT;
-  if (c->boxh()) {  // RectangularBC / RhombicBC: the plain FP64 form with the ELJ potentials
+  const bool bpot = pot_b(c->pot);
+  if (c->boxh()) {  // RectangularBC / RhombicBC: the plain FP64 form with the dimer potentials
     if (c->f32())
       return c->fail(PTMC_ERR_ARG,
                      "RectangularBC/RhombicBC run in the plain FP64 form (precision PTMC_FP64)");
-    if (c->pot != POT_ELJ && c->pot != POT_ELJEVEN)
-      return c->fail(PTMC_ERR_ARG, "RectangularBC/RhombicBC: ELJPotential or ELJPotentialEven only");
+    if (c->pot != POT_ELJ && c->pot != POT_ELJEVEN && !bpot)
+      return c->fail(PTMC_ERR_ARG, "RectangularBC/RhombicBC: ELJ, ELJPotentialB or "
+                                   "LookupTablePotential only");
+    if (bpot && !npt)
+      return c->fail(PTMC_ERR_ARG, "ELJPotentialB/LookupTablePotential in RectangularBC/RhombicBC: "
+                                   "NPT only");
   }
+  if (bpot && c->f32())
+    return c->fail(PTMC_ERR_ARG,
+                   "ELJPotentialB/LookupTablePotential run in the plain FP64 form (precision PTMC_FP64)");
   if (c->sep_vol && (!npt || !c->boxh()))
     return c->fail(PTMC_ERR_ARG,
                    "separated volume moves need the NPT ensemble with a RectangularBC or RhombicBC");
-  if (npt && c->pot != POT_ELJEVEN)
-    return c->fail(PTMC_ERR_ARG, "NPT: ELJPotentialEven only (its long-range correction, "
-                                 "src/EnergyEvaluation.jl:968)");
+  if (npt && c->pot != POT_ELJEVEN && !bpot)
+    return c->fail(PTMC_ERR_ARG, "NPT: ELJPotentialEven, ELJPotentialB or LookupTablePotential "
+                                 "(the potentials with a long-range correction, "
+                                 "src/EnergyEvaluation.jl:968-1009)");
   // group runs by N: device order sorted by N (stable)
   int nr = c->p.n_runs;
   c->run_of_dev.resize(nr);
@@ -617,7 +661,7 @@ int ptmc_init(ptmc_ctx* c) {
     r.cyc[0] = r.cyc[1] = r.cyc[2] = 1;
     r.run_ctr = 0;
     po += (long long)R * h.N * 3;
-    if (npt && !c->f32()) mo += (long long)R * h.N * h.N;
+    if ((npt || bpot) && !c->f32()) mo += (long long)R * h.N * h.N;
     if (c->pot == POT_EAM) co += (long long)R * h.N * 2;
     ho += (long long)R * hstride;
     wk += R;
@@ -630,7 +674,8 @@ int ptmc_init(ptmc_ctx* c) {
       c->d_ham.alloc(2 * W) || c->d_ctr.alloc(W) || c->d_status.alloc(W) ||
       c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho) ||
       (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)) || c->d_boxh.alloc(W) ||
-      c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W))
+      c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W) ||
+      (bpot && c->d_tan.alloc(mo)) || (c->pot == POT_LUT && c->d_lut.alloc(c->lut.size())))
     return c->fail(PTMC_ERR_CUDA, "device allocation failed");
   // host images
   std::vector<double> pos(po), box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W), boxh(W),
@@ -705,6 +750,22 @@ int ptmc_init(ptmc_ctx* c) {
   K.maxd_sep = c->d_maxd_sep.p;
   K.cnt_sep = c->d_cnt_sep.p;
   K.sep_vol = c->sep_vol ? 1 : 0;
+  K.tan = c->d_tan.p;
+  for (int k = 0; k < MAX_COEFF; ++k) {
+    K.ca[k] = k < (int)c->eljb_a.size() ? c->eljb_a[k] : 0.0;
+    K.cb[k] = k < (int)c->eljb_b.size() ? c->eljb_b[k] : 0.0;
+  }
+  if (c->pot == POT_LUT) {
+    CK(cudaMemcpyAsync(c->d_lut.p, c->lut.data(), sizeof(double) * c->lut.size(),
+                       cudaMemcpyHostToDevice, s));
+    K.lut = c->d_lut.p;
+    K.lut_na = c->lut_na;
+    K.lut_nd = c->lut_nd;
+    K.lut_start = c->lut_par[0];
+    K.lut_dd = c->lut_par[1];
+    K.lut_da = c->lut_par[2];
+    K.lut_c6 = c->lut_par[3];
+  }
   K.K = (int)c->coeff.size();
   for (int k = 0; k < MAX_COEFF; ++k) K.c[k] = k < K.K ? c->coeff[k] : 0.0;
   for (int k = 0; k < MAX_COEFF; ++k) K.cf[k] = (float)K.c[k];
@@ -1015,6 +1076,8 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_maxboxh.free_();
   c->d_maxd_sep.free_();
   c->d_cnt_sep.free_();
+  c->d_tan.free_();
+  c->d_lut.free_();
   c->d_nn_sf.free_();
   c->d_nn_W.free_();
   c->d_nn_G.free_();
@@ -1096,6 +1159,15 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
   if (c->pot == POT_EAM) {
     s += "EAM: " + fmt_double(c->eam[0]) + " " + fmt_double(c->eam[1]) + " " + fmt_double(c->eam[2]) +
          " " + fmt_double(c->eam[3]) + " \n";
+  } else if (c->pot == POT_NN) {
+    s += "runnerpotential \n";
+  } else if (c->pot == POT_LUT) {
+    s += "LookupTablePotential \n";
+  } else if (c->pot == POT_ELJB) {  // writepotential AbstractDimerPotentialB (:71-77)
+    s += "ELJB " + std::to_string(c->coeff.size()) + " \n";
+    for (const std::vector<double>* v : {&c->eljb_a, &c->eljb_b, &c->coeff}) {
+      for (size_t k = 0; k < v->size(); ++k) s += fmt_double((*v)[k]) + (k + 1 < v->size() ? "\t" : "\n");
+    }
   } else {
     s += std::string(c->pot == POT_ELJEVEN ? "ELJPotentialEven{" : "ELJPotential{") +
          std::to_string(c->coeff.size()) + ", Float64}";
@@ -1181,7 +1253,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       (rc = dump(c, b, c->d_status)) || (rc = dump(c, b, c->d_wos)) || (rc = dump(c, b, c->d_cnt)) ||
       (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)) ||
       (rc = dump(c, b, c->d_rdf)) || (rc = dump(c, b, c->d_boxh)) || (rc = dump(c, b, c->d_maxboxh)) ||
-      (rc = dump(c, b, c->d_maxd_sep)) || (rc = dump(c, b, c->d_cnt_sep)))
+      (rc = dump(c, b, c->d_maxd_sep)) || (rc = dump(c, b, c->d_cnt_sep)) || (rc = dump(c, b, c->d_tan)))
     return rc;
   put(b, "PTMCEND!", 8);
   if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
@@ -1230,7 +1302,7 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
       (rc = undump(c, b, at, c->d_nn_G)) || (rc = undump(c, b, at, c->d_nn_sow)) ||
       (rc = undump(c, b, at, c->d_rdf)) || (rc = undump(c, b, at, c->d_boxh)) ||
       (rc = undump(c, b, at, c->d_maxboxh)) || (rc = undump(c, b, at, c->d_maxd_sep)) ||
-      (rc = undump(c, b, at, c->d_cnt_sep)))
+      (rc = undump(c, b, at, c->d_cnt_sep)) || (rc = undump(c, b, at, c->d_tan)))
     return rc;
   c->rd = rd;
   c->equilibrated = hdr[3] != 0;
@@ -1932,6 +2004,7 @@ int snapshot(ptmc_ctx* c, Snapshot& s) {
                   &c->d_maxd_sep})
     rc |= snap_one(c, s, *b);
   rc |= snap_one(c, s, c->d_cnt_sep);
+  rc |= snap_one(c, s, c->d_tan);
   rc |= snap_one(c, s, c->d_ctr);
   rc |= snap_one(c, s, c->d_status);
   rc |= snap_one(c, s, c->d_wos);

@@ -148,6 +148,132 @@ __device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
+// ---- ELJPotentialB and LookupTablePotential: pair energies that depend on
+// |tan| of the angle between the pair vector and z
+// get_tan (src/Configurations.jl:181-215) with the minimum image of the box
+template <int BC>
+__device__ __forceinline__ double ptan(double ax, double ay, double az, const double* b,
+                                       double L, double H) {
+  double bx = b[0], by = b[1], bz = b[2];
+  if (BC == BC_CUB || BC == BC_RECT) {
+    const double Hz = BC == BC_RECT ? H : L;
+    bx = dadd(b[0], dmul(L, rint(ddiv(dsub(ax, b[0]), L))));
+    by = dadd(b[1], dmul(L, rint(ddiv(dsub(ay, b[1]), L))));
+    bz = dadd(b[2], dmul(Hz, rint(ddiv(dsub(az, b[2]), Hz))));
+  } else if (BC == BC_RHB) {
+    const double hy = dmul(SQRT3 / 2, L), is3 = 1.0 / SQRT3;
+    by = dadd(b[1], dmul(hy, rint(ddiv(dsub(ay, b[1]), hy))));
+    double q = ddiv(dsub(dsub(ax, b[0]), dmul(is3, dsub(ay, b[1]))), L);
+    bx = dadd(dadd(dsub(b[0], ddiv(b[1], SQRT3)), dmul(L, rint(q))), dmul(is3, by));
+    bz = dadd(b[2], dmul(H, rint(ddiv(dsub(az, b[2]), H))));
+  }
+  const double dx = dsub(ax, bx), dy = dsub(ay, by);
+  return fabs(ddiv(sqrt(dadd(dmul(dx, dx), dmul(dy, dy))), dsub(az, bz)));
+}
+// dimer_energy ELJPotentialB (src/EnergyEvaluation.jl:943-958)
+__device__ __forceinline__ double v_eljb(const double* a, const double* b, const double* c, int K,
+                                         double r2, double tn) {
+  if (!(r2 >= 5.30)) return 0.1;
+  double r6inv = 1.0 / (r2 * r2 * r2);
+  const double t2 = 2.0 / (tn * tn + 1.0) - 1.0;  // cos(2 theta)
+  const double t4 = 2.0 * (t2 * t2) - 1.0;
+  double s = c[0] * r6inv * (1.0 + a[0] * t2 + b[0] * t4);
+  r6inv /= r2;
+  const double r = sqrt(r2);
+  for (int i = 1; i < K; ++i) {
+    s += c[i] * r6inv * (1.0 + a[i] * t2 + b[i] * t4);
+    r6inv /= r;
+  }
+  return s;
+}
+// dimer_energy LookupTablePotential (src/EnergyEvaluation.jl:277-298): angle
+// index from atan(|tan|) in table steps, distance index from sqrt(r2), the c6
+// tail beyond the table; Julia's round is half-to-even (rint), the indices are
+// kept inside the table
+__device__ __forceinline__ double v_lut(const KParams& P, double r2, double tn) {
+  int ia = 1;
+  const double at = fabs(tn);
+  if (at > 0.00872687153 && at <= 114.592845357)
+    ia = (int)rint(atan(at) / P.lut_da * 180.0 / 3.141592653589793 + 1.0);
+  else if (at > 114.592845357)
+    ia = 91;
+  ia = min(max(ia, 1), P.lut_na);
+  const double r0 = P.lut_start + 0.5 * P.lut_dd, r1 = P.lut_start + P.lut_nd * P.lut_dd;
+  if (r2 <= r0 * r0) return __ldg(P.lut + (ia - 1));
+  if (r2 <= r1 * r1) {
+    int id = (int)rint((sqrt(r2) - P.lut_start) / P.lut_dd);
+    id = min(max(id, 1), P.lut_nd);
+    return __ldg(P.lut + (size_t)(id - 1) * P.lut_na + (ia - 1));
+  }
+  return P.lut_c6 / (r2 * r2 * r2);
+}
+template <int POT>
+__device__ __forceinline__ double vb(const KParams& P, const double* a, const double* b,
+                                     const double* c, int K, double r2, double tn) {
+  return POT == POT_ELJB ? v_eljb(a, b, c, K, r2, tn) : v_lut(P, r2, tn);
+}
+// lrc of the B potentials (src/EnergyEvaluation.jl:983-1009) with the box
+// factor of dimer_energy_config
+template <int POT, int BC>
+__device__ double lrc_b(const KParams& P, int N, double rc2, double L, double H) {
+  double l;
+  const double rcs = sqrt(rc2);
+  if (POT == POT_ELJB) {
+    const double cf[4] = {-0.1279111890228638, -1.328138539967966, 12.260941135261255,
+                          41.12212408251662};
+    if (rc2 <= 16) {
+      l = 0.0;
+    } else {
+      double rc3 = rc2 * rcs;
+      l = 0.0;
+      for (int i = 1; i <= 4; ++i) {
+        l += cf[i - 1] / rc3 / (2 * i + 1);
+        rc3 *= rc2;
+      }
+      l *= 3.141592653589793 * (double)(N * N) / 4 / (rcs * rcs * rcs);
+    }
+  } else {
+    if (rc2 <= 10) {
+      l = 1.0;
+    } else {
+      l = P.lut_c6 / (rc2 * rcs) / 3;
+      l *= 3.141592653589793 * (double)(N * N) / 4 / (rcs * rcs * rcs);
+    }
+  }
+  if (BC == BC_RHB) return l * 3 / 4 * L / H;
+  if (BC == BC_RECT) return L < H ? l * L / H : l * (H * H) / (L * L);
+  return l;
+}
+// FP64 energy of one walker for the B potentials: fills the distance and
+// tangent matrices (get_distance2_mat, get_tantheta_mat) and sums
+// dimer_energy_config (src/EnergyEvaluation.jl:476-780)
+template <int POT, int BC, int ENS>
+__device__ double walker_energy_b(const KParams& P, const double* X, int N, double L, double H,
+                                  double rc2, const double* a, const double* b, const double* c,
+                                  int K, double* M, double* T, int lane) {
+  double e = 0.0;
+  for (int i = 0; i < N; ++i) {
+    const double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+    for (int j = i + 1 + lane; j < N; j += 32) {
+      const double x = pd2<BC>(xi, yi, zi, X + 3 * j, L, H);
+      const double t = ptan<BC>(xi, yi, zi, X + 3 * j, L, H);
+      M[(size_t)i * N + j] = x;
+      M[(size_t)j * N + i] = x;
+      T[(size_t)i * N + j] = t;
+      T[(size_t)j * N + i] = t;
+      if (ENS == ENS_NPT && !(x <= rc2)) continue;
+      e += vb<POT>(P, a, b, c, K, x, t);
+    }
+    if (lane == 0) {
+      M[(size_t)i * N + i] = 0.0;
+      T[(size_t)i * N + i] = 0.0;
+    }
+  }
+  e = warp_sum(e);
+  if (ENS == ENS_NPT) e = e + lrc_b<POT, BC>(P, N, rc2, L, H);
+  return e;
+}
+
 // ------------------------------------------------------------ FP64 energy of
 // one walker from positions (init and resync).  ELJ: dimer_energy_config
 // (src/EnergyEvaluation.jl:378-420); EAM: set_variables + energy
@@ -208,12 +334,18 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
   if (w >= rd.R) return;
   const int g = rd.wk + w;
   const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
-  double* M = (ENS == ENS_NPT && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
+  double* M = ((ENS == ENS_NPT || pot_b(POT)) && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N
+                                                         : nullptr;
   double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
-  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
-                                           -0.5 * P.eam_n, -0.5 * P.eam_m,
-                                           P.eam_ean, P.eam_ecam, M, comp,
-                                           nullptr, lane);
+  double e;
+  if constexpr (pot_b(POT))
+    e = walker_energy_b<POT, BC, ENS>(P, X, N, P.box[g], P.boxh[g], P.rc2[g], P.ca, P.cb, P.c,
+                                      P.K, M, P.tan + rd.mat_off + (size_t)w * N * N, lane);
+  else
+    e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
+                                      -0.5 * P.eam_n, -0.5 * P.eam_m,
+                                      P.eam_ean, P.eam_ecam, M, comp,
+                                      nullptr, lane);
   if (lane == 0) {
     P.en[g] = e;
     P.status[g] = ST_OK;
@@ -228,6 +360,9 @@ __global__ void __launch_bounds__(1024)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
   __shared__ float s_cf[MAX_COEFF];
+  __shared__ double s_ca[pot_b(POT) ? MAX_COEFF : 1], s_cb[pot_b(POT) ? MAX_COEFF : 1];
+  constexpr bool BPOT = pot_b(POT);
+  constexpr bool KEEP_M = (ENS == ENS_NPT || BPOT) && !F32;  // stored distance matrix
   const RunDesc rd = P.runs[run0 + blockIdx.x];
   const int N = rd.N, R = rd.R;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -257,7 +392,8 @@ __global__ void __launch_bounds__(1024)
       s_d64 = (double2*)carve((long long)R * N * 16);
     }
   }
-  double* s_row = (ENS == ENS_NPT && !F32) ? (double*)carve((long long)R * N * 8) : nullptr;
+  double* s_row = KEEP_M ? (double*)carve((long long)R * N * 8) : nullptr;
+  double* s_trow = (BPOT && !F32) ? (double*)carve((long long)R * N * 8) : nullptr;
   double* s_drw = (double*)carve((long long)R * DRAW_BUF * 8);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_maxbox = (double*)carve((long long)R * 8);
@@ -276,6 +412,10 @@ __global__ void __launch_bounds__(1024)
   // ---- load the run into shared memory ----
   if (tid < K) {
     s_c[tid] = P.c[tid];
+    if (BPOT) {
+      s_ca[tid] = P.ca[tid];
+      s_cb[tid] = P.cb[tid];
+    }
     s_cf[tid] = (float)P.c[tid];
   }
   const double* gpos = P.pos + rd.pos_off;
@@ -325,8 +465,10 @@ __global__ void __launch_bounds__(1024)
   double* X = s_pos + (size_t)w * N * 3;
   float4* X32 = F32 ? s_p32 + (size_t)w * N : nullptr;
   double* drw = s_drw + w * DRAW_BUF;
-  double* M = (ENS == ENS_NPT && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
+  double* M = KEEP_M ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
+  double* TM = BPOT ? P.tan + rd.mat_off + (size_t)w * N * N : nullptr;  // tangent matrix
   double* row = s_row ? s_row + (size_t)w * N : nullptr;
+  double* trow = s_trow ? s_trow + (size_t)w * N : nullptr;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const double ean = P.eam_ean, ecam = P.eam_ecam;
   const float hnf = (float)hn, hmf = (float)hm, eanf = (float)ean, ecamf = (float)ecam;
@@ -414,7 +556,28 @@ __global__ void __launch_bounds__(1024)
     double new_en;
     double sa = 0.0, sb = 0.0;  // EAM FP64: sum of component deltas of atom i
     float saf = 0.f, sbf = 0.f;
-    if (POT == POT_ELJ || POT == POT_ELJEVEN) {
+    if (BPOT) {  // energy_update! for the B potentials (src/EnergyEvaluation.jl:1508-1564)
+      double e_n = 0.0, e_o = 0.0;
+      const double* Mi = M + (size_t)i * N;
+      const double* Ti = TM + (size_t)i * N;
+      for (int j = lane; j < N; j += 32) {
+        if (j == i) {
+          row[j] = 0.0;
+          trow[j] = 0.0;
+          continue;
+        }
+        const double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
+        const double tn = ptan<BC>(tx, ty, tz, X + 3 * j, L, H);
+        row[j] = dn;
+        trow[j] = tn;
+        const double dol = Mi[j], tol = Ti[j];
+        if (ENS != ENS_NPT || dn <= rc2) e_n += vb<POT>(P, s_ca, s_cb, s_c, K, dn, tn);
+        if (ENS != ENS_NPT || dol <= rc2) e_o += vb<POT>(P, s_ca, s_cb, s_c, K, dol, tol);
+      }
+      e_n = warp_sum(e_n);
+      e_o = warp_sum(e_o);
+      new_en = (e_n - e_o) + en;
+    } else if (POT == POT_ELJ || POT == POT_ELJEVEN) {
       if (!F32) {  // dimer_energy_update! (src/EnergyEvaluation.jl:804-821)
         double e_n = 0.0, e_o = 0.0;
         const double* Mi = M ? M + (size_t)i * N : nullptr;
@@ -536,6 +699,10 @@ __global__ void __launch_bounds__(1024)
         double v = row[j];
         M[(size_t)i * N + j] = v;
         M[(size_t)j * N + i] = v;
+        if (BPOT) {  // swap_vars! B potentials (src/swap_config.jl:198-206)
+          TM[(size_t)i * N + j] = trow[j];
+          TM[(size_t)j * N + i] = trow[j];
+        }
       }
     }
     if (POT == POT_EAM) {  // swap_vars! EAM (src/swap_config.jl:208-211)
@@ -615,24 +782,38 @@ __global__ void __launch_bounds__(1024)
     }
     const double rcn = box_rcut<BC>(Ln, Hn);
     const double s2 = fx * fx;
+    // the pair energy of a trial pair: B potentials take the tangent of the
+    // trial (separated z / xy moves, get_tantheta_mat!) or the current one
+    auto pair_e = [&](double x, int i, int j, const double* a3, const double* b3) -> double {
+      if constexpr (BPOT) {
+        const double t = (sep && kind != 0) ? ptan<BC>(a3[0], a3[1], a3[2], b3, Ln, Hn)
+                                            : TM[(size_t)i * N + j];
+        return vb<POT>(P, s_ca, s_cb, s_c, K, x, t);
+      } else {
+        return v64<POT>(s_c, K, x);
+      }
+    };
     double e = 0.0;
     if (!F32 && !sep) {
       for (int i = 0; i < N; ++i)
         for (int j = i + 1 + lane; j < N; j += 32) {
           double x = M[(size_t)i * N + j] * s2;
-          if (x <= rcn) e += v64<POT>(s_c, K, x);
+          if (x <= rcn) e += pair_e(x, i, j, nullptr, nullptr);
         }
     } else {
       for (int i = 0; i < N; ++i) {
-        const double xi = X[3 * i] * fx, yi = X[3 * i + 1] * fx, zi = X[3 * i + 2] * fz;
+        const double a3[3] = {X[3 * i] * fx, X[3 * i + 1] * fx, X[3 * i + 2] * fz};
         for (int j = i + 1 + lane; j < N; j += 32) {
           const double b[3] = {X[3 * j] * fx, X[3 * j + 1] * fx, X[3 * j + 2] * fz};
-          double x = pd2<BC>(xi, yi, zi, b, Ln, Hn);
-          if (x <= rcn) e += v64<POT>(s_c, K, x);
+          double x = pd2<BC>(a3[0], a3[1], a3[2], b, Ln, Hn);
+          if (x <= rcn) e += pair_e(x, i, j, a3, b);
         }
       }
     }
-    e = warp_sum(e) + lrc_box<BC>(N, rcn, s_c, K, Ln, Hn);
+    if constexpr (BPOT)
+      e = warp_sum(e) + lrc_b<POT, BC>(P, N, rcn, Ln, Hn);
+    else
+      e = warp_sum(e) + lrc_box<BC>(N, rcn, s_c, K, Ln, Hn);
     const double Vn = box_volume<BC>(Ln, Hn), Vo = box_volume<BC>(L, H);
     double dh = dadd(dsub(e, en), dmul(P.pressure, dsub(Vn, Vo)));
     double prob = exp(dadd(dmul(-dh, beta), dmul((double)N, log(Vn / Vo))));
@@ -653,6 +834,11 @@ __global__ void __launch_bounds__(1024)
             double x = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
             M[(size_t)i * N + j] = x;
             M[(size_t)j * N + i] = x;
+            if (BPOT && kind != 0) {  // tangents of z / xy moves
+              double t = ptan<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
+              TM[(size_t)i * N + j] = t;
+              TM[(size_t)j * N + i] = t;
+            }
           }
           if (lane == 0) M[(size_t)i * N + i] = 0.0;
         }
@@ -866,10 +1052,16 @@ __global__ void __launch_bounds__(1024) k_resync(KParams P, int run0) {
   const int g = rd.wk + w;
   const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
   double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
-  double e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
-                                           -0.5 * P.eam_n, -0.5 * P.eam_m,
-                                           P.eam_ean, P.eam_ecam, nullptr, comp,
-                                           nullptr, lane);
+  double e;
+  if constexpr (pot_b(POT))
+    e = walker_energy_b<POT, BC, ENS>(P, X, N, P.box[g], P.boxh[g], P.rc2[g], P.ca, P.cb, P.c,
+                                      P.K, P.mat + rd.mat_off + (size_t)w * N * N,
+                                      P.tan + rd.mat_off + (size_t)w * N * N, lane);
+  else
+    e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
+                                      -0.5 * P.eam_n, -0.5 * P.eam_m,
+                                      P.eam_ean, P.eam_ecam, nullptr, comp,
+                                      nullptr, lane);
   if (lane == 0) {
     P.drift[g] = fmax(P.drift[g], fabs(P.en[g] - e));
     P.en[g] = e;
@@ -947,6 +1139,17 @@ static int dispatch(int pot, int bc, int ens, bool f32, int what,
   PT_CASE64(POT_ELJEVEN, BC_RHB, ENS_NVT)
   PT_CASE64(POT_ELJEVEN, BC_RECT, ENS_NPT)
   PT_CASE64(POT_ELJEVEN, BC_RHB, ENS_NPT)
+  // ELJPotentialB and LookupTablePotential: plain FP64 form
+  PT_CASE64(POT_ELJB, BC_SPH, ENS_NVT)
+  PT_CASE64(POT_ELJB, BC_CUB, ENS_NVT)
+  PT_CASE64(POT_ELJB, BC_CUB, ENS_NPT)
+  PT_CASE64(POT_ELJB, BC_RECT, ENS_NPT)
+  PT_CASE64(POT_ELJB, BC_RHB, ENS_NPT)
+  PT_CASE64(POT_LUT, BC_SPH, ENS_NVT)
+  PT_CASE64(POT_LUT, BC_CUB, ENS_NVT)
+  PT_CASE64(POT_LUT, BC_CUB, ENS_NPT)
+  PT_CASE64(POT_LUT, BC_RECT, ENS_NPT)
+  PT_CASE64(POT_LUT, BC_RHB, ENS_NPT)
 #undef PT_CASE64
   return -1;
 }

@@ -5,7 +5,9 @@
 // runs concatenated; "walker" = configuration-bound data, "slot" =
 // temperature-bound data, see the walker/slot note in ptmc_cycles.cu):
 //   pos   f64 [sum_r R_r*N_r*3]   positions, walker-major, atom-major, xyz
-//   mat   f64 [sum_r R_r*N_r*N_r] NPT plain form: squared-distance matrix
+//   mat   f64 [sum_r R_r*N_r*N_r] NPT plain form and the B potentials:
+//                                 squared-distance matrix
+//   tan   f64 [same as mat]       B potentials: |tan| of the pair angle to z
 //   comp  f64 [sum_r R_r*N_r*2]   EAM (phi_i, rho_i) components
 //   en/box/rc2/drift f64 [W], ctr u64 [W], status i32 [W]   per walker
 //   boxh f64 [W]  box height (RectangularBC / RhombicBC)     per walker
@@ -20,7 +22,9 @@
 
 namespace ptmc {
 
-enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3 };
+enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3, POT_ELJB = 4, POT_LUT = 5 };
+// pair potentials with an angle to z (ELJPotentialB, LookupTablePotential)
+__host__ __device__ constexpr bool pot_b(int pot) { return pot == POT_ELJB || pot == POT_LUT; }
 enum { BC_SPH = 0, BC_CUB = 1, BC_RECT = 2, BC_RHB = 3 };  // RECT/RHB: length L, height H
 enum { ENS_NVT = 0, ENS_NPT = 1 };
 enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
@@ -83,6 +87,12 @@ struct KParams {
   double* maxd_sep;         // [2W] slot max_displ[3] (xy), max_displ[4] (z)
   long long* cnt_sep;       // [4W] slot count_vol_xy[1:2], count_vol_z[1:2]
   int sep_vol;              // NPT.separated_volume
+  // ELJPotentialB (coeff_c in c) and LookupTablePotential
+  double ca[MAX_COEFF], cb[MAX_COEFF];  // coeff_a, coeff_b
+  double* tan;              // tangent matrices, same offsets as mat
+  const double* lut;        // table, Julia's Matrix(l_angle, l_dist) column-major
+  int lut_na, lut_nd;       // l_angle, l_dist
+  double lut_start, lut_dd, lut_da, lut_c6;  // start_dist, d_dist, d_angle, c6coeff
   // potential
   double c[MAX_COEFF];
   int K;
@@ -111,7 +121,8 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
     b += al((long long)R * N * (f32 ? 8 : 16));      // components
     b += al((long long)R * N * (f32 ? 8 : 16));      // per-move deltas
   }
-  if (ens == ENS_NPT && !f32) b += al((long long)R * N * 8);  // trial row
+  if ((ens == ENS_NPT || pot_b(pot)) && !f32) b += al((long long)R * N * 8);  // trial row
+  if (pot_b(pot) && !f32) b += al((long long)R * N * 8);    // trial tangent row
   b += al((long long)R * DRAW_BUF * 8);              // draw buffers
   b += al((long long)R * 8) * 6;                     // beta, maxbox, en, box, ham(2)
   b += al((long long)R * 16);                        // maxd

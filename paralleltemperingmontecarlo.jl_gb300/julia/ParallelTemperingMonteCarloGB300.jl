@@ -96,6 +96,17 @@ function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential,
             coeff = collect(Float64, potential.coeff)
             check(ccall((:ptmc_set_potential_elj, libptmc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Cint),
                         c, coeff, length(coeff), potential isa ELJPotentialEven), c)
+        elseif potential isa ELJPotentialB
+            a, b, cc = (collect(Float64, v) for v in (potential.coeff_a, potential.coeff_b, potential.coeff_c))
+            check(ccall((:ptmc_set_potential_eljb, libptmc), Cint,
+                        (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Cint),
+                        c, a, b, cc, length(cc)), c)
+        elseif potential isa LookupTablePotential
+            # pot.table is Matrix{Float64}(l_angle, l_dist): passed as is (column-major)
+            check(ccall((:ptmc_set_potential_lookup, libptmc), Cint,
+                        (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Cint, Cdouble, Cdouble, Cdouble, Cdouble, Cdouble),
+                        c, potential.table, potential.l_angle, potential.l_dist, potential.start_dist,
+                        potential.start_angle, potential.d_dist, potential.d_angle, potential.c6coeff), c)
         elseif potential isa EmbeddedAtomPotential
             check(ccall((:ptmc_set_potential_eam, libptmc), Cint,
                         (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble, Cdouble),

@@ -11,6 +11,9 @@ Outputs (committed, small):
                         test/multihist_test.jl:18-32 (R=3, p=3.4439647528956955e-9)
   checkpoint_ne13.json — the Ne13 checkpoint fixture test/testing_data/checkpoint/
                         (params, hist_info, 25x102 histograms, 25 configurations)
+  lookup_table_2.json — header, c6coeff and four entries of
+                        scripts/lookup-tables/look-up_table-2.txt as read by
+                        read_lookuptable (checked against test/test_potentials.jl:58-64)
   nn_cu55.json        — the symmetry-function table of scripts/cu55.jl:55-135
                         with the min/max scaling values of scripts/data/scaling.data
                         (rows 1:88, columns 3 = min and 4 = max), and the Cu55
@@ -178,6 +181,24 @@ def nn_tables(ref):
     return {"sf": sf, "ico55_nm": pos, "nm_to_bohr": 18.8973, "cu_lattice_nm": 0.36258}
 
 
+def lookup_table(ref):
+    """scripts/lookup-tables/look-up_table-2.txt read by the package's
+    read_lookuptable (restating src/EnergyEvaluation.jl:227-256), checked
+    against the known answers of test/test_potentials.jl:58-64; the header,
+    c6coeff and a few table entries are kept (not the table)."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    import __graft_entry__ as g
+    pk = g.load_package()
+    path = os.path.join(ref, "scripts", "lookup-tables", "look-up_table-2.txt")
+    table, sd, sa, ld, la, dd, da, c6 = pk.read_lookuptable(path)
+    assert table[0, 0] == 282.19449125205114 and sd == 0.1 and sa == 0
+    assert table.size == la * ld
+    samples = [[i, j, float(table[i, j])] for i, j in ((0, 0), (0, 999), (45, 500), (90, ld - 1))]
+    return {"file": "scripts/lookup-tables/look-up_table-2.txt", "l_dist": ld, "start_dist": sd,
+            "d_dist": dd, "l_angle": la, "start_angle": sa, "d_angle": da, "c6coeff": c6,
+            "samples": samples}
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     here = os.path.dirname(os.path.abspath(__file__))
@@ -186,6 +207,7 @@ def main():
     json.dump(npt, open(os.path.join(here, "multihist_npt.json"), "w"))
     json.dump(checkpoint(ref), open(os.path.join(here, "checkpoint_ne13.json"), "w"))
     json.dump(nn_tables(ref), open(os.path.join(here, "nn_cu55.json"), "w"), indent=0)
+    json.dump(lookup_table(ref), open(os.path.join(here, "lookup_table_2.json"), "w"), indent=0)
     print("golden fixtures written to", here)
 
 

@@ -303,6 +303,56 @@ def test_oracle_rectangular_uniform_npt(orc):
         assert e[i] == pytest.approx(ref, rel=1e-9)
 
 
+def test_tangent_and_eljb_known_answers(orc):
+    """get_tan (test/runtests.jl:217-239) and ELJPotentialB in a rhombic NPT
+    state (test/separated_v_test.jl:95-114): tan_mat[1,2], tan_mat[1,3] and
+    en_tot == -0.00016263185592172208 (pair terms under the rhombic cut-off
+    plus the box-scaled ELJB long-range correction), bit for bit."""
+    from lut_synth import ELJB_A, ELJB_B, ELJB_C
+    v1, v2, v3 = [5.0, 0.0, 0.0], [-3.0, 0.0, 4.0], [-2.0, 0.0, -3.0]
+    assert orc.get_tan(v1, v3) == 7 / 3 and orc.get_tan(v2, v3) == 1 / 7
+    assert orc.get_tan(v1, v3, orc.BC_CUBIC, 10.0) == 1.0
+    assert orc.get_tan(v1, v2, orc.BC_RHOMBIC, 5.0, 5.0) == 2.0
+    assert orc.get_tan(v2, v3, orc.BC_RHOMBIC, 5.0, 5.0) == 0.5
+    x = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [0.0, 1.0, 0.0]])
+    assert orc.get_tan(x[0], x[1], orc.BC_RHOMBIC, 10.0, 10.0) == pytest.approx(0.7453559924999299)
+    assert orc.get_tan(x[0], x[2], orc.BC_RHOMBIC, 10.0, 10.0) == pytest.approx(0.47140452079103173)
+    T, _ = orc.tempgrid(10.0, 15.0, 2)
+    run = orc.Run(3, 2, np.stack([x] * 2), T, ensemble=orc.NPT,
+                  pressure=101325 * 3.398928944382626e-14, bc=orc.BC_RHOMBIC, bc_param=10.0)
+    run.set_box(10.0, separated=True)
+    run.set_eljb(ELJB_A, ELJB_B, ELJB_C)
+    run.init()
+    assert run.walkers()[1][0] == -0.00016263185592172208
+
+
+def test_lookup_table_reference_header():
+    """The reference's look-up_table-2.txt read by read_lookuptable gives the
+    known answers of test/test_potentials.jl:58-64 (fixture made by
+    tests/golden/make_golden.py)."""
+    d = json.load(open(os.path.join(GOLDEN, "lookup_table_2.json")))
+    assert d["samples"][0][2] == 282.19449125205114
+    assert d["start_dist"] == 0.1 and d["start_angle"] == 0
+    assert (d["l_angle"], d["l_dist"], d["d_dist"], d["d_angle"]) == (91, 1491, 0.01, 1.0)
+
+
+def test_lookup_parser_and_oracle_energy(orc, pk, tmp_path):
+    """read_lookuptable on a table in the reference's format, and the oracle's
+    lookup (src/EnergyEvaluation.jl:277-298) against a numpy restatement over
+    the hard-core, table and c6-tail ranges and all angle bands."""
+    from lut_synth import write_lut, lut_energy_np
+    t, sd, sa, ld, la, dd, da, c6 = pk.read_lookuptable(write_lut(str(tmp_path / "t.txt")))
+    assert t.shape == (91, 1491) and (sd, sa, ld, la, dd, da) == (0.1, 0.0, 1491, 91, 0.01, 1.0)
+    assert c6 == pytest.approx(np.mean(t[:, 999]) * (0.1 + 1000 * 0.01) ** 6, rel=1e-14)
+    lut = dict(table=t, start_dist=sd, d_dist=dd, d_angle=da, c6coeff=c6)
+    rng = np.random.default_rng(4)
+    r = np.concatenate([rng.uniform(0.05, 0.2, 50), rng.uniform(0.2, 15.0, 400),
+                        rng.uniform(15.0, 20.0, 50)])
+    tn = np.concatenate([[0.0, 0.001, 0.5, 114.0, 200.0, np.inf], rng.exponential(2.0, 494)])
+    for ri, ti in zip(r, tn):
+        assert orc.lut_energy(lut, ri * ri, ti) == lut_energy_np(t, sd, dd, da, c6, ri * ri, ti)
+
+
 # ---------------------------------------------------------------- surrogate oracle
 SUR_CFG = [2.0, 12.0, 1.125, 12.0, 0.02]
 
