@@ -47,6 +47,9 @@
 
 namespace ptmc {
 
+// draw words buffered per walker (a refill is DRW32 / 4 Philox blocks)
+constexpr uint32_t DRW32 = 128;
+
 namespace {
 
 __device__ __forceinline__ float v_even32(const float* c, int K, float r2) {
@@ -141,11 +144,13 @@ __device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
-// (hi, lo) += d, error-free two-sum followed by renormalisation
+// (hi, lo) += d for a step d much smaller than the coordinate: Dekker's
+// fast two-sum (exact when |hi| >= |d|; for the rare coordinate inside one
+// step of zero the sum is still correct to the float rounding of d), then
+// renormalisation
 __device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
   float s = hi + d;
-  float bp = s - hi;
-  float err = (hi - (s - bp)) + (d - bp);
+  float err = d - (s - hi);
   float l = lo + err;
   hi = s + l;
   lo = l - (hi - s);
@@ -170,9 +175,9 @@ __device__ __forceinline__ T seg_sum(T v, unsigned mask) {
 // FP64 energy of one walker from its fixed-point positions (resync); the
 // walker's LPR lanes share the work (glane = lane within the walker's group).
 template <int POT, int BC, int ENS, int LPR>
-__device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, double rc2,
+__device__ double energy64(float4* Xh, const float4* Xl, int N, double L, double rc2,
                            const double* c, int K, double hn, double hm, double ean,
-                           double ecam, float2* comp32, float* sq32, int lane, unsigned gmask) {
+                           double ecam, float* rho_tmp, float* sq32, int lane, unsigned gmask) {
   auto P = [&](int a, double& x, double& y, double& z) {
     float4 h = Xh[a], l = Xl[a];
     x = (double)h.x + (double)l.x;
@@ -193,10 +198,16 @@ __device__ double energy64(const float4* Xh, const float4* Xl, int N, double L, 
         A += exp(hn * lg);
         B += exp(hm * lg);
       }
-      if (comp32) comp32[a] = make_float2((float)A, (float)B);
+      if (rho_tmp) rho_tmp[a] = (float)B;
       if (sq32) sq32[a] = (float)sqrt(B);
       e += ean * A - ecam * sqrt(B);
     }
+    // the electron density goes into the w lane of the position after every
+    // lane has read the positions
+    __syncwarp(gmask);
+    if (rho_tmp)
+      for (int a = lane; a < N; a += LPR) Xh[a].w = rho_tmp[a];
+    __syncwarp(gmask);
     return seg_sum<LPR>(e, gmask);
   } else {
     for (int i = 0; i < N; ++i) {
@@ -225,8 +236,8 @@ long long cycles32_smem_bytes(int pot, int R, int N, int C) {
   long long b = 0;
   b += al(Rl * N * 16);  // float4 hi positions
   b += al(Rl * N * 16);  // float4 lo positions
-  if (pot == POT_EAM) b += 2 * al(Rl * N * 8) + al(Rl * N * 4);  // comps, deltas, sqrt(rho)
-  b += al(Rl * 32 * 4);                                          // draw words
+  if (pot == POT_EAM) b += 2 * al(Rl * N * 4);  // density deltas, sqrt(rho)
+  b += al(Rl * DRW32 * 4);                                       // draw words
   b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 4;
   b += al((long long)R * 8);                                     // per-walker accepted counts
   return b;
@@ -263,15 +274,13 @@ __global__ void __launch_bounds__(1024)
   };
   float4* s_xh = (float4*)carve((long long)Rl * N * 16);
   float4* s_xl = (float4*)carve((long long)Rl * N * 16);
-  float2* s_c32 = nullptr;
-  float2* s_d32 = nullptr;
+  float* s_d32 = nullptr;
   float* s_sq = nullptr;
   if (POT == POT_EAM) {
-    s_c32 = (float2*)carve((long long)Rl * N * 8);
-    s_d32 = (float2*)carve((long long)Rl * N * 8);
+    s_d32 = (float*)carve((long long)Rl * N * 4);
     s_sq = (float*)carve((long long)Rl * N * 4);
   }
-  uint32_t* s_drw = (uint32_t*)carve((long long)Rl * 32 * 4);
+  uint32_t* s_drw = (uint32_t*)carve((long long)Rl * DRW32 * 4);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_maxbox = (double*)carve((long long)R * 8);
   double* s_en = (double*)carve((long long)R * 8);
@@ -299,8 +308,8 @@ __global__ void __launch_bounds__(1024)
   }
   if (POT == POT_EAM) {
     const double* gc = P.comp + rdp->comp_off + (size_t)q * Rl * N * 2;
-    for (int k = tid; k < Rl * N; k += nthr) {
-      s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
+    for (int k = tid; k < Rl * N; k += nthr) {  // rho in the w lane of the position
+      s_xh[k].w = (float)gc[2 * k + 1];
       s_sq[k] = (float)sqrt(gc[2 * k + 1]);
     }
   }
@@ -326,46 +335,53 @@ __global__ void __launch_bounds__(1024)
   double en = P.en[g];
   double L = P.box[g];
   double rc2 = P.rc2[g];
-  unsigned long long ctr = P.ctr[g];
-  unsigned long long base = ctr + 32;
+  // draw words: drw[k] is word `base + k` of this walker's stream; `off` is
+  // the next one (>= DRW32: refill from the 4-aligned word at base + off,
+  // DRW32 / 4 Philox blocks spread over the walker's lanes)
+  unsigned long long base = (P.ctr[g] & ~3ull) - DRW32;
+  uint32_t off = DRW32 + (uint32_t)(P.ctr[g] & 3ull);
   int status = P.status[g];
   double drift = P.drift[g];
   float4* Xh = s_xh + (size_t)wl * N;
   float4* Xl = s_xl + (size_t)wl * N;
   float* SQ = s_sq ? s_sq + (size_t)wl * N : nullptr;
-  uint32_t* drw = s_drw + wl * 32;
+  uint32_t* drw = s_drw + wl * DRW32;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
-  const float hnf = P.f_hn, hmf = P.f_hm, eanf = P.f_ean, ecamf = P.f_ecam;
+  const float hnf = P.f_hn, hmf = P.f_hm, ecamf = P.f_ecam;
+  const float ean2f = 2.f * P.f_ean;
   const uint32_t run_word = (uint32_t)rdp->run_id;
   float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
   float Llo = (float)(L - (double)Lf);
 
-  auto word = [&]() -> uint32_t {
-    if (ctr - base >= 32ull) {
-      __syncwarp(gmask);
-      base = ctr & ~3ull;
-      if (lane < 8) {
-        uint64_t blk = (base >> 2) + lane;
-        uint32_t c4[4] = {(uint32_t)blk, (uint32_t)(blk >> 32), (uint32_t)w, run_word};
-        philox4x32_10(c4, (uint32_t)P.seed, (uint32_t)(P.seed >> 32));
-        drw[4 * lane] = c4[0];
-        drw[4 * lane + 1] = c4[1];
-        drw[4 * lane + 2] = c4[2];
-        drw[4 * lane + 3] = c4[3];
-      }
-      __syncwarp(gmask);
+  auto refill = [&]() {
+    __syncwarp(gmask);
+    base += off & ~3u;
+    off &= 3u;
+    for (int bl = lane; bl < DRW32 / 4; bl += LPR) {
+      uint64_t blk = (base >> 2) + bl;
+      uint32_t c4[4] = {(uint32_t)blk, (uint32_t)(blk >> 32), (uint32_t)w, run_word};
+      philox4x32_10(c4, (uint32_t)P.seed, (uint32_t)(P.seed >> 32));
+      *(uint4*)(drw + 4 * bl) = make_uint4(c4[0], c4[1], c4[2], c4[3]);
     }
-    uint32_t x = drw[ctr - base];
-    ++ctr;
-    return x;
+    __syncwarp(gmask);
   };
+  auto word = [&]() -> uint32_t {
+    if (off >= DRW32) refill();
+    return drw[off++];
+  };
+  // the next n words are buffered (one check for a whole atom move; a refill
+  // re-creates the unread words from their stream index)
+  auto ensure = [&](uint32_t n) {
+    if (off > DRW32 - n) refill();
+  };
+  auto word_nc = [&]() -> uint32_t { return drw[off++]; };
 
   // ---------------------------------------------------------- atom move
   auto atom_move = [&](int i, float beta_l2e, float mdf, float& de_acc) -> int {
     float4 h0 = Xh[i], l0 = Xl[i];
     float th[3], tl[3];
-    auto propose = [&]() {
-      float d0 = usymf(word()) * mdf, d1 = usymf(word()) * mdf, d2 = usymf(word()) * mdf;
+    auto propose = [&]() {  // the first attempt's words are ensured by the caller
+      float d0 = usymf(word_nc()) * mdf, d1 = usymf(word_nc()) * mdf, d2 = usymf(word_nc()) * mdf;
       th[0] = h0.x; tl[0] = l0.x; ff_add(th[0], tl[0], d0);
       th[1] = h0.y; tl[1] = l0.y; ff_add(th[1], tl[1], d1);
       th[2] = h0.z; tl[2] = l0.z; ff_add(th[2], tl[2], d2);
@@ -390,7 +406,7 @@ __global__ void __launch_bounds__(1024)
           for (int a = lane; a < N; a += LPR) {
             double x = (double)Xh[a].x + Xl[a].x - sx, y = (double)Xh[a].y + Xl[a].y - sy,
                    z = (double)Xh[a].z + Xl[a].z - sz;
-            float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
+            float4 h = make_float4((float)x, (float)y, (float)z, Xh[a].w);
             Xh[a] = h;
             Xl[a] = make_float4((float)(x - h.x), (float)(y - h.y), (float)(z - h.z), 0.f);
           }
@@ -398,6 +414,7 @@ __global__ void __launch_bounds__(1024)
           h0 = Xh[i];
           l0 = Xl[i];
         } else {
+          ensure(3);
           propose();
           if (count == 100) {
             status = ST_SPHERE;
@@ -417,40 +434,42 @@ __global__ void __launch_bounds__(1024)
     }
     const float4 tf = make_float4(th[0], th[1], th[2], 0.f);
     const float4 x4 = h0;
-    float de = 0.f, saf = 0.f, sbf = 0.f;
+    float de = 0.f, sbf = 0.f;
     if (POT == POT_EAM) {
-      const float2* C = s_c32 + (size_t)wl * N;
-      float2* D = s_d32 + (size_t)wl * N;
+      // The phi sums enter the energy linearly: the pair (i, j) changes phi_j
+      // and phi_i by the same da, so the phi part of dE is 2 ean sum_j da and
+      // no phi is kept.  rho_j is the w lane of atom j's position.
+      float* D = s_d32 + (size_t)wl * N;
       for (int j = lane; j < N; j += LPR) {
-        if (j == i) continue;
+        // the self pair (j == i: zero old distance) is masked, not branched
+        const bool self = j == i;
         float4 b = Xh[j];
         float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
         float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
         float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
         float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
-        D[j] = make_float2(da, db);
-        saf += da;
+        da = self ? 0.f : da;
+        db = self ? 0.f : db;
+        D[j] = db;
         sbf += db;
-        float rho = C[j].y;
         // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
-        de += eanf * da - ecamf * db * rcpf(SQ[j] + sqrtf_approx(rho + db));
+        de += ean2f * da - ecamf * db * rcpf(SQ[j] + sqrtf_approx(b.w + db));
       }
-      saf = seg_sum<LPR>(saf, gmask);
       sbf = seg_sum<LPR>(sbf, gmask);
       de = seg_sum<LPR>(de, gmask);
-      float rhoi = C[i].y;
-      de += eanf * saf - ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(rhoi + sbf));
+      de -= ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(x4.w + sbf));
     } else {
       for (int j = lane; j < N; j += LPR) {
-        if (j == i) continue;
+        const bool self = j == i;  // masked, not branched (its old distance is 0)
         float4 b = Xh[j];
         float dn = pf2<BC>(tf, b, Lf, iLf);
         float dol = pf2<BC>(x4, b, Lf, iLf);
         if (ENS == ENS_NPT) {
-          if (dn <= rcf) de += v32p<POT>(P, s_cf, K, dn);
-          if (dol <= rcf) de -= v32p<POT>(P, s_cf, K, dol);
+          if (!self && dn <= rcf) de += v32p<POT>(P, s_cf, K, dn);
+          if (!self && dol <= rcf) de -= v32p<POT>(P, s_cf, K, dol);
         } else {
-          de += v32p<POT>(P, s_cf, K, dn) - v32p<POT>(P, s_cf, K, dol);
+          const float t = v32p<POT>(P, s_cf, K, dn) - v32p<POT>(P, s_cf, K, dol);
+          de += self ? 0.f : t;
         }
       }
       de = seg_sum<LPR>(de, gmask);
@@ -459,17 +478,20 @@ __global__ void __launch_bounds__(1024)
     if (!(ex2f(-beta_l2e * de) >= u)) return 0;
     __syncwarp(gmask);
     if (lane == 0) {
-      Xh[i] = tf;
+      float rho_i = 0.f;
+      if (POT == POT_EAM) {
+        rho_i = x4.w + sbf;
+        SQ[i] = sqrtf_approx(rho_i);
+      }
+      Xh[i] = make_float4(tf.x, tf.y, tf.z, rho_i);
       Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
     }
     if (POT == POT_EAM) {
-      float2* C = s_c32 + (size_t)wl * N;
-      const float2* D = s_d32 + (size_t)wl * N;
+      const float* D = s_d32 + (size_t)wl * N;
       for (int k = lane; k < N; k += LPR) {
-        float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
-        float2 c = C[k];
-        float rho = c.y + d.y;
-        C[k] = make_float2(c.x + d.x, rho);
+        if (k == i) continue;
+        const float rho = Xh[k].w + D[k];
+        Xh[k].w = rho;
         SQ[k] = sqrtf_approx(rho);
       }
     }
@@ -509,7 +531,7 @@ __global__ void __launch_bounds__(1024)
     for (int a = lane; a < N; a += LPR) {
       double x = ((double)Xh[a].x + Xl[a].x) * scale, y = ((double)Xh[a].y + Xl[a].y) * scale,
              z = ((double)Xh[a].z + Xl[a].z) * scale;
-      float4 h = make_float4((float)x, (float)y, (float)z, 0.f);
+      float4 h = make_float4((float)x, (float)y, (float)z, Xh[a].w);
       Xh[a] = h;
       Xl[a] = make_float4((float)(x - h.x), (float)(y - h.y), (float)(z - h.z), 0.f);
     }
@@ -539,7 +561,8 @@ __global__ void __launch_bounds__(1024)
     if (status == ST_OK) {
       float de_acc = 0.f;
       for (int st = 0; st < n_steps; ++st) {
-        int k = (int)__umulhi(word(), (uint32_t)n_steps);  // rand(1:n_steps)
+        ensure(5);  // slot draw, three displacements, acceptance
+        int k = (int)__umulhi(word_nc(), (uint32_t)n_steps);  // rand(1:n_steps)
         if (k < N) {
           acc_a += atom_move(k, beta_l2e, mdf, de_acc);
         } else {
@@ -552,7 +575,7 @@ __global__ void __launch_bounds__(1024)
       en += (double)de_acc;
       if (P.resync_every > 0 && idx % P.resync_every == 0) {
         double e64 = energy64<POT, BC, ENS, LPR>(Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean,
-                                            P.eam_ecam, POT == POT_EAM ? s_c32 + (size_t)wl * N : nullptr,
+                                            P.eam_ecam, POT == POT_EAM ? s_d32 + (size_t)wl * N : nullptr,
                                             SQ, lane, gmask);
         drift = fmax(drift, fabs(en - e64));
         en = e64;
@@ -676,15 +699,14 @@ __global__ void __launch_bounds__(1024)
   if (POT == POT_EAM) {
     double* gc = P.comp + rdp->comp_off + (size_t)q * Rl * N * 2;
     for (int k = tid; k < Rl * N; k += nthr) {
-      gc[2 * k] = s_c32[k].x;
-      gc[2 * k + 1] = s_c32[k].y;
+      gc[2 * k + 1] = s_xh[k].w;  // rho; the FP32 form keeps no phi
     }
   }
   if (lane == 0) {
     P.en[g] = en;
     P.box[g] = L;
     P.rc2[g] = rc2;
-    P.ctr[g] = ctr;
+    P.ctr[g] = base + off;
     P.status[g] = status;
     P.drift[g] = drift;
   }
