@@ -159,9 +159,10 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
 __device__ __forceinline__ float u01f(uint32_t w) {
   return __uint_as_float(0x3F800000u | (w >> 9)) - 1.0f;
 }
-// symmetric uniform in (-1/2, 1/2): (k + 1/2) 2^-23 - 1/2
-__device__ __forceinline__ float usymf(uint32_t w) {
-  return (u01f(w) - 0.5f) + 0x1.0p-24f;
+// a step of the symmetric uniform (-md/2, md/2): md ((k + 1/2) 2^-23 - 1/2)
+// for the 23-bit k of the word, one FMA with mdc = md (3/2 - 2^-24) per slot
+__device__ __forceinline__ float stepf(uint32_t w, float md, float mdc) {
+  return fmaf(__uint_as_float(0x3F800000u | (w >> 9)), md, -mdc);
 }
 
 // sum over the LPR lanes of one walker (xor partners stay inside the group)
@@ -238,7 +239,7 @@ long long cycles32_smem_bytes(int pot, int R, int N, int C) {
   b += al(Rl * N * 16);  // float4 lo positions
   if (pot == POT_EAM) b += 2 * al(Rl * N * 4);  // density deltas, sqrt(rho)
   b += al(Rl * DRW32 * 4);                                       // draw words
-  b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 4;
+  b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 5;
   b += al((long long)R * 8);                                     // per-walker accepted counts
   return b;
 }
@@ -292,6 +293,7 @@ __global__ void __launch_bounds__(1024)
   int* s_sow = (int*)carve((long long)R * 4);
   float* s_bl2e = (float*)carve((long long)R * 4);  // beta * log2(e) per slot
   float* s_mdf = (float*)carve((long long)R * 4);   // atom step size per slot
+  float* s_mdc = (float*)carve((long long)R * 4);   // its step offset md (3/2 - 2^-24)
   int2* s_acc = (int2*)carve((long long)R * 8);     // this cycle's accepted atom/volume moves per walker
 
   if (tid < K) {
@@ -326,6 +328,7 @@ __global__ void __launch_bounds__(1024)
     s_wos[s] = P.wos[g];
     s_bl2e[s] = (float)(P.beta[g] * 1.4426950408889634);
     s_mdf[s] = (float)P.maxd[2 * g];
+    s_mdc[s] = (float)(P.maxd[2 * g] * (1.5 - 0x1.0p-24));
   }
   __syncthreads();
   for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
@@ -348,7 +351,7 @@ __global__ void __launch_bounds__(1024)
   uint32_t* drw = s_drw + wl * DRW32;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const float hnf = P.f_hn, hmf = P.f_hm, ecamf = P.f_ecam;
-  const float ean2f = 2.f * P.f_ean;
+  const float ean2f = 2.f * P.f_ean, necamf = -P.f_ecam;
   const uint32_t run_word = (uint32_t)rdp->run_id;
   float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
   float Llo = (float)(L - (double)Lf);
@@ -377,11 +380,12 @@ __global__ void __launch_bounds__(1024)
   auto word_nc = [&]() -> uint32_t { return drw[off++]; };
 
   // ---------------------------------------------------------- atom move
-  auto atom_move = [&](int i, float beta_l2e, float mdf, float& de_acc) -> int {
+  auto atom_move = [&](int i, float beta_l2e, float mdf, float mdc, float& de_acc) -> int {
     float4 h0 = Xh[i], l0 = Xl[i];
     float th[3], tl[3];
     auto propose = [&]() {  // the first attempt's words are ensured by the caller
-      float d0 = usymf(word_nc()) * mdf, d1 = usymf(word_nc()) * mdf, d2 = usymf(word_nc()) * mdf;
+      float d0 = stepf(word_nc(), mdf, mdc), d1 = stepf(word_nc(), mdf, mdc),
+            d2 = stepf(word_nc(), mdf, mdc);
       th[0] = h0.x; tl[0] = l0.x; ff_add(th[0], tl[0], d0);
       th[1] = h0.y; tl[1] = l0.y; ff_add(th[1], tl[1], d1);
       th[2] = h0.z; tl[2] = l0.z; ff_add(th[2], tl[2], d2);
@@ -453,7 +457,8 @@ __global__ void __launch_bounds__(1024)
         D[j] = db;
         sbf += db;
         // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
-        de += ean2f * da - ecamf * db * rcpf(SQ[j] + sqrtf_approx(b.w + db));
+        de = fmaf(ean2f, da, de);
+        de = fmaf(necamf * db, rcpf(SQ[j] + sqrtf_approx(b.w + db)), de);
       }
       sbf = seg_sum<LPR>(sbf, gmask);
       de = seg_sum<LPR>(de, gmask);
@@ -556,15 +561,15 @@ __global__ void __launch_bounds__(1024)
     const double mdv = s_maxd[2 * slot + 1];
     const double maxbox = s_maxbox[slot];
     const float beta_l2e = s_bl2e[slot];
-    const float mdf = s_mdf[slot];
+    const float mdf = s_mdf[slot], mdc = s_mdc[slot];
     long long acc_a = 0, acc_v = 0;
     if (status == ST_OK) {
       float de_acc = 0.f;
       for (int st = 0; st < n_steps; ++st) {
         ensure(5);  // slot draw, three displacements, acceptance
         int k = (int)__umulhi(word_nc(), (uint32_t)n_steps);  // rand(1:n_steps)
-        if (k < N) {
-          acc_a += atom_move(k, beta_l2e, mdf, de_acc);
+        if (ENS == ENS_NVT || k < N) {  // NVT: every step is an atom move
+          acc_a += atom_move(k, beta_l2e, mdf, mdc, de_acc);
         } else {
           en += (double)de_acc;  // fold the FP32 sum before the FP64 enthalpy
           de_acc = 0.f;
@@ -644,6 +649,7 @@ __global__ void __launch_bounds__(1024)
         if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
         else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
         s_mdf[s] = (float)s_maxd[2 * s];
+        s_mdc[s] = (float)(s_maxd[2 * s] * (1.5 - 0x1.0p-24));
         s_cnt[6 * s + 1] = 0;
         if (ENS == ENS_NPT) {
           double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);
