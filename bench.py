@@ -17,6 +17,7 @@ only, weak scaling; no collective on the data path), timing is max over ranks.
 """
 import argparse
 import ctypes
+import functools
 import json
 import math
 import multiprocessing as mp
@@ -39,9 +40,14 @@ P_NE = 101325 * 3.398928944382626e-14
 
 
 # --------------------------------------------------------------- workloads
-def cu55_ico():
+@functools.lru_cache(maxsize=1)
+def _cu55_ico():
     d = json.load(open(os.path.join(ROOT, "tests", "golden", "nn_cu55.json")))
     return np.array(d["ico55_nm"]) * (d["cu_lattice_nm"] * d["nm_to_bohr"])
+
+
+def cu55_ico():
+    return _cu55_ico().copy()
 
 
 def sphere_start(N, radius, min_sep, seed):
@@ -68,7 +74,11 @@ def workload(name):
                     # DRAM bytes (read + write) of one k_cycles32 launch per run: ncu capture
                     # of a 16-run launch, 1.30 MB (profiles/k_cycles32_cu55_eam.md); the
                     # state moved per launch grows with the runs
-                    dram_bytes_per_run=1.30e6 / 16)
+                    dram_bytes_per_run=1.30e6 / 16,
+                    # warp instructions per attempted move of k_cycles32 (32 lanes per
+                    # walker): smsp__inst_executed of the 16-run, 50-cycle launch over its
+                    # 1.408 M moves (profiles/k_cycles32_cu55_eam.md)
+                    inst_per_move=315.9, lanes=32)
     if name == "ne13":
         return dict(name="ne13_eljeven", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
                     bc=("sphere", 11.0), sizes=lambda B: [13] * B,
@@ -352,7 +362,7 @@ def gpu_arm(args, rank, world):
                 eng.surrogate_enable(True)
                 h2d += P.nbytes
             eng.cycles_nosample(args.cycles)
-            outs = [eng.states(r)["en_tot"] for r in range(B)]
+            outs = [eng.energies()]  # every run's slot-ordered energies, one read
             eng.close()
             t1 = time.perf_counter()
             if k >= args.warmup:
@@ -473,6 +483,8 @@ def main():
     res, peaks, B, e2e = gpu_arm(args, rank, world)
     if rank != 0:
         return
+    import torch
+    n_sm = torch.cuda.get_device_properties(0).multi_processor_count
     chosen = "fp32_da" if "fp32_da" in res else "fp32"
     ch = res[chosen]
     sizes = ch["sizes"]
@@ -508,13 +520,30 @@ def main():
                      "traffic": (W["dram_bytes_per_run"] * B if W.get("dram_bytes_per_run") else None),
                      "peak_source": "measured in-situ by ptmc_measure_peaks (FFMA chains)",
                      "ops_per_pair": W["flops_pair"], "mufu_per_pair": W["mufu_pair"],
-                     "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"]},
+                     "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"],
+                     "issue": issue_roof(W, ch, n_sm)},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": ch["launches"],
         "clocks": ch["clocks"],
     }
     print(json.dumps(line))
+
+
+def issue_roof(W, ch, n_sm):
+    """The instruction-issue roofline of the cycle kernel: warp instructions
+    per move (ncu) x moves/s against 4 issue slots per SM per clock at the SM
+    clock sampled during the timed region."""
+    ipm = W.get("inst_per_move")
+    shapes = (ch.get("launch_shapes") or {}).get("lanes_per_walker") or {}
+    if not ipm or not ch.get("clocks") or any(v != W.get("lanes") for v in shapes.values()):
+        return None  # measured for one launch shape only
+    mhz = ch["clocks"]["sm_mhz"]
+    achieved = ch["value"] * ipm / 1e9
+    peak = 4 * n_sm * mhz * 1e6 / 1e9
+    return {"warp_inst_per_move": ipm, "achieved": achieved, "peak": peak, "unit": "G warp-inst/s",
+            "frac": achieved / peak,
+            "source": "ncu smsp__inst_executed, profiles/k_cycles32_cu55_eam.md"}
 
 
 if __name__ == "__main__":

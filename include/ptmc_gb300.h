@@ -193,6 +193,8 @@ int ptmc_get_output(ptmc_ctx* c, int run, ptmc_output* out);
 int ptmc_get_states(ptmc_ctx* c, int run, double* xyz, double* en_tot,
                     double* box, double* max_displ, long long* counts,
                     double* ham);
+/* Slot-ordered energies of every run in one read: en_tot [n_runs][R]. */
+int ptmc_get_energies(ptmc_ctx* c, double* en_tot);
 /* Slot-ordered box state of RectangularBC / RhombicBC runs: box_height [R],
  * max_displ_sep [2R] = max_displ[3:4], counts_sep [R][4] = count_vol_xy[1:2],
  * count_vol_z[1:2] (src/MCStates.jl:33-47).  NULL skips an array. */

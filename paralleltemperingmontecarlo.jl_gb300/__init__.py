@@ -624,6 +624,12 @@ class Engine:
                                         _dptr(ham)))
         return dict(xyz=xyz, en_tot=en, box=box, max_displ=md, counts=cnt, ham=ham)
 
+    def energies(self):
+        """Slot-ordered energies of every run, [n_runs, R], in one read."""
+        out = np.zeros((self.n_runs, self.R))
+        self._ck(self.L.ptmc_get_energies(self.h, _dptr(out)))
+        return out
+
     def box_states(self, run=0):
         """Slot-ordered box state of RectangularBC / RhombicBC runs: box_height
         [R], max_displ_sep [R,2] (max_displ[3:4]), counts_sep [R,4]

@@ -82,6 +82,7 @@ SIGNATURES = {
     "ptmc_get_states": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp,
                                        _llp, _dp]),
     "ptmc_get_box_states": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _llp]),
+    "ptmc_get_energies": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "ptmc_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "ptmc_checkpoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "ptmc_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),

@@ -202,6 +202,21 @@ struct ptmc_ctx {
 
 namespace {
 
+// replica start positions from the runs' start configurations: walker w of a
+// run starts from configuration w mod n_start (src/Initialization.jl:88-96);
+// only the distinct configurations cross the host link
+__global__ void k_expand_starts(const RunDesc* runs, const double* starts,
+                                const long long* start_off, const int* n_start, double* pos) {
+  const RunDesc rd = runs[blockIdx.x];
+  const double* src = starts + start_off[blockIdx.x];
+  const int per = rd.N * 3, ns = n_start[blockIdx.x];
+  double* dst = pos + rd.pos_off;
+  for (long long k = threadIdx.x; k < (long long)rd.R * per; k += blockDim.x) {
+    const int w = (int)(k / per), e = (int)(k % per);
+    dst[k] = src[(long long)(w % ns) * per + e];
+  }
+}
+
 int check_status(ptmc_ctx* c) {
   std::vector<int> st(c->W);
   CK(cudaMemcpyAsync(st.data(), c->d_status.p, sizeof(int) * c->W, cudaMemcpyDeviceToHost, c->st));
@@ -677,16 +692,29 @@ int ptmc_init(ptmc_ctx* c) {
       c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W) ||
       (bpot && c->d_tan.alloc(mo)) || (c->pot == POT_LUT && c->d_lut.alloc(c->lut.size())))
     return c->fail(PTMC_ERR_CUDA, "device allocation failed");
-  // host images
-  std::vector<double> pos(po), box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W), boxh(W),
+  // host images (the start configurations go up once per run and are
+  // expanded into replicas on the device)
+  std::vector<double> box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W), boxh(W),
       maxboxh(W), maxd_sep(2 * W);
   std::vector<int> wos(W);
+  std::vector<long long> start_off(nr);
+  std::vector<int> n_start(nr);
+  long long n_starts = 0;
+  for (int d = 0; d < nr; ++d) {
+    const HostRun& h = c->runs[c->run_of_dev[d]];
+    start_off[d] = n_starts;
+    n_start[d] = h.n_start;
+    n_starts += (long long)h.n_start * h.N * 3;
+  }
+  std::vector<double> starts(n_starts);
+  for (int d = 0; d < nr; ++d) {
+    const HostRun& h = c->runs[c->run_of_dev[d]];
+    std::copy(h.xyz.begin(), h.xyz.end(), starts.begin() + start_off[d]);
+  }
   for (int d = 0; d < nr; ++d) {
     const HostRun& h = c->runs[c->run_of_dev[d]];
     const RunDesc& r = c->rd[d];
     for (int w = 0; w < R; ++w) {
-      const double* src = &h.xyz[(size_t)(w % h.n_start) * h.N * 3];
-      std::copy(src, src + (size_t)h.N * 3, &pos[r.pos_off + (size_t)w * h.N * 3]);
       int g = r.wk + w;
       const double Lb = h.bc_param, Hb = h.bc_height;
       box[g] = Lb;
@@ -708,7 +736,31 @@ int ptmc_init(ptmc_ctx* c) {
     }
   }
   cudaStream_t s = c->st;
-  CK(cudaMemcpyAsync(c->d_pos.p, pos.data(), sizeof(double) * po, cudaMemcpyHostToDevice, s));
+  int rc = push_runs(c);
+  if (rc) return rc;
+  {
+    DBuf<double> d_starts;
+    DBuf<long long> d_soff;
+    DBuf<int> d_ns;
+    if (d_starts.alloc(n_starts) || d_soff.alloc(nr) || d_ns.alloc(nr))
+      return c->fail(PTMC_ERR_CUDA, "device allocation failed");
+    cudaError_t e = cudaMemcpyAsync(d_starts.p, starts.data(), sizeof(double) * n_starts,
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_soff.p, start_off.data(), sizeof(long long) * nr, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_ns.p, n_start.data(), sizeof(int) * nr, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      k_expand_starts<<<nr, 256, 0, s>>>(c->d_runs.p, d_starts.p, d_soff.p, d_ns.p, c->d_pos.p);
+      e = cudaGetLastError();
+      c->stats.kernel_launches += 1;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the scratch is freed next
+    d_starts.free_();
+    d_soff.free_();
+    d_ns.free_();
+    if (e != cudaSuccess) return c->cuda_fail(e, "start configurations");
+  }
   CK(cudaMemcpyAsync(c->d_box.p, box.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->d_rc2.p, rc2.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->d_beta.p, beta.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
@@ -724,8 +776,6 @@ int ptmc_init(ptmc_ctx* c) {
   CK(cudaMemsetAsync(c->d_cnt.p, 0, sizeof(long long) * 6 * W, s));
   CK(cudaMemsetAsync(c->d_hist.p, 0, sizeof(unsigned int) * std::max<long long>(ho, 1), s));
   if (c->rdf_on) CK(cudaMemsetAsync(c->d_rdf.p, 0, sizeof(unsigned int) * c->d_rdf.n, s));
-  int rc = push_runs(c);
-  if (rc) return rc;
   KParams& K = c->K;
   K.runs = c->d_runs.p;
   K.pos = c->d_pos.p;
@@ -954,6 +1004,22 @@ int ptmc_get_states(ptmc_ctx* c, int run, double* xyz, double* en_tot, double* b
   if (max_displ) std::copy(md.begin(), md.end(), max_displ);
   if (counts) std::copy(cnt.begin(), cnt.end(), counts);
   if (ham) std::copy(hm.begin(), hm.end(), ham);
+  return PTMC_OK;
+}
+
+int ptmc_get_energies(ptmc_ctx* c, double* en_tot) {
+  if (!c || !en_tot) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  const int R = c->R(), W = c->W;
+  std::vector<double> en(W);
+  std::vector<int> wos(W);
+  CK(cudaMemcpyAsync(en.data(), c->d_en.p, sizeof(double) * W, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(wos.data(), c->d_wos.p, sizeof(int) * W, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int run = 0; run < c->p.n_runs; ++run) {
+    const int wk = c->rd[c->dev_of_run[run]].wk;
+    for (int s = 0; s < R; ++s) en_tot[(size_t)run * R + s] = en[wk + wos[wk + s]];
+  }
   return PTMC_OK;
 }
 

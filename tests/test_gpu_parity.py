@@ -185,9 +185,11 @@ def test_batched_uneven_runs(pk, orc):
                     bc_param=radius, exch_prob=1.0, seed=21, n_runs=len(sizes), starts=starts,
                     cycles_per_launch=7)
     eng.cycles_nosample(50)
+    en_all = eng.energies()  # ptmc_get_energies: every run in one read
     for r, o in enumerate(os_):
         o.cycles(1, 50)
         compare(eng, o, run=r)
+        assert np.array_equal(en_all[r], eng.states(r)["en_tot"])
     st = eng.stats()
     assert st["kernel_launches"] >= 8
     eng.close()
