@@ -28,9 +28,11 @@ extern "C" {
 #define PTMC_ERR_IO -5       /* checkpoint file error */
 #define PTMC_ERR_LIMIT -6    /* size beyond a documented limit */
 
-/* ensembles: NVT (src/Ensembles.jl:42), NPT (src/Ensembles.jl:75) */
+/* ensembles: NVT (src/Ensembles.jl:42), NPT (src/Ensembles.jl:75), NNVT (two
+ * species with atom swaps, src/Ensembles.jl:138-151) */
 #define PTMC_NVT 0
 #define PTMC_NPT 1
+#define PTMC_NNVT 2
 /* boundary conditions: SphericalBC (src/BoundaryConditions.jl:44),
  * CubicBC (src/BoundaryConditions.jl:72), RectangularBC (:89) and RhombicBC
  * (:110), the last two with a box length (x, y) and a height (z) */
@@ -119,6 +121,23 @@ int ptmc_set_potential_eljb(ptmc_ctx* c, const double* a, const double* b,
 int ptmc_set_potential_lookup(ptmc_ctx* c, const double* table, int l_angle,
                               int l_dist, double start_dist, double start_angle,
                               double d_dist, double d_angle, double c6coeff);
+/* RuNNerPotential2Atom (src/EnergyEvaluation.jl:1287-1314) for the NNVT
+ * ensemble: n1 atoms of species 1 (indices 0..n1-1 of every configuration),
+ * the rest species 2.  rad: nrad rows {eta, r_cut, G_offset[4], G_norm[4]}
+ * (RadialType2a, MachineLearningPotential/SymmFunc.jl:54-85); ang: nang rows
+ * {eta, lambda, zeta, r_cut, tpz[6], G_offset[6]} (AngularType3a, :114-175);
+ * w1 / w2: the two species' networks in the layout of ptmc_set_potential_nn
+ * with nodes = {2 nrad + 3 nang, H1, H2, 1}.  SphericalBC, at most 64 atoms,
+ * plain FP64 form. */
+int ptmc_set_potential_nn2(ptmc_ctx* c, const double* rad, int nrad,
+                           const double* ang, int nang, const double* w1,
+                           const double* w2, int nw, const int* nodes,
+                           int n_layers, int n1);
+/* NNVT.n_atom_swaps (src/Ensembles.jl:144-151): swaps per cycle (default 1);
+ * each picks one atom of each species (swap_atoms, src/MCMoves.jl:363-370). */
+int ptmc_set_atom_swaps(ptmc_ctx* c, int n_swaps);
+/* Accepted atom swaps of run `run` so far (all its walkers). */
+int ptmc_get_swaps(ptmc_ctx* c, int run, long long* accepted);
 /* EmbeddedAtomPotential(n, m, ean, eCam) (src/EnergyEvaluation.jl:1059-1073) */
 int ptmc_set_potential_eam(ptmc_ctx* c, double n, double m, double ean,
                            double ecam);

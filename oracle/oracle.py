@@ -16,7 +16,7 @@ SRC = os.path.join(HERE, "ptmc_oracle.cpp")
 POT_ELJ, POT_ELJEVEN, POT_EAM, POT_NN = 0, 1, 2, 3
 BC_SPHERE, BC_CUBIC, BC_RECT, BC_RHOMBIC = 0, 1, 2, 3
 POT_ELJB, POT_LUT = 4, 5
-NVT, NPT = 0, 1
+NVT, NPT, NNVT = 0, 1, 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -87,6 +87,11 @@ def lib():
         L.orc_set_pot_eljb.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int]
         L.orc_set_pot_lut.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int] + \
             [ctypes.c_double] * 5
+        L.orc_set_pot_nn2.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp,
+                                      _dp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int]
+        L.orc_get_swaps.restype = ctypes.c_long
+        L.orc_get_swaps.argtypes = [ctypes.c_void_p]
         L.orc_set_box.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, _dp]
         L.orc_get_box.argtypes = [ctypes.c_void_p, _dp, _dp, _lp, _lp]
         L.orc_eam_config_energy.restype = ctypes.c_double
@@ -301,6 +306,18 @@ class Run:
         _check(lib().orc_set_pot_lut(self.h, P(self._lut), la, ld, lut["start_dist"],
                                      lut.get("start_angle", 0.0), lut["d_dist"], lut["d_angle"],
                                      lut["c6coeff"]))
+
+    def set_nn2(self, rad, ang, w1, w2, nodes, n1, n_swaps=1):
+        """RuNNerPotential2Atom in the NNVT ensemble: rad [nrad, 10], ang [nang, 16]."""
+        self._nn2 = (_d(rad), _d(ang), _d(w1), _d(w2),
+                     np.ascontiguousarray(nodes, dtype=np.int32))
+        rd, an, a, b, nd = self._nn2
+        _check(lib().orc_set_pot_nn2(self.h, P(rd), rd.shape[0], P(an), an.shape[0] if an.size else 0,
+                                     P(a), P(b), len(a), nd.ctypes.data_as(_ip), len(nd), n1,
+                                     n_swaps))
+
+    def swaps(self):
+        return lib().orc_get_swaps(self.h)
 
     def set_eam(self, n, m, ean, ecam):
         _check(lib().orc_set_pot_eam(self.h, n, m, ean, ecam))

@@ -162,6 +162,11 @@ struct Pot {
   // Matrix(l_angle, l_dist)), first distance, steps, c6 tail coefficient
   std::vector<double> lut;
   int l_dist = 0, l_angle = 0;
+  // RuNNerPotential2Atom: species 1 = atoms 0..n1-1; radial rows {eta, r_cut,
+  // G_offset[4], G_norm[4]}, angular rows {eta, lambda, zeta, r_cut, tpz[6],
+  // G_offset[6]}; w = species-1 weights, w_b = species-2 weights
+  int n1 = 0, nrad2 = 0, nang2 = 0;
+  std::vector<double> rad2, ang2, w_b;
   double start_dist = 0, start_angle = 0, d_dist = 0, d_angle = 0, c6 = 0;
   double n = 0, m = 0, ean = 0, ecam = 0;
   // NN
@@ -376,6 +381,87 @@ inline double theta_part(double th, double lam, double zeta) {
   return std::pow(1 + lam * th, zeta);  // SymmFunc.jl:166
 }
 
+// ---- two-species RuNNer potential (EnergyEvaluation.jl:1276-1448,
+// SymmFunc.jl:326-471, 508-541): the symmetry matrix of a configuration.
+// Radial function k fills rows 2k (neighbour of species 1) and 2k+1 (species
+// 2); angular function k fills rows 2 nrad + 3k + m, m = the number of
+// species-2 atoms among the centre's two neighbours.  Each row is scaled and
+// offset by the centre atom's species.  Loops in the reference's order.
+void nn2_G(const Pot& p, const double* X, const double* D, const double* F, int N, double* G) {
+  const int n1 = p.n1, nr = p.nrad2, na = p.nang2;
+  std::fill(G, G + (size_t)(2 * nr + 3 * na) * N, 0.0);
+  for (int k = 0; k < nr; ++k) {
+    const double* q = &p.rad2[10 * (size_t)k];
+    const double eta = q[0];
+    double* g0 = G + (size_t)(2 * k) * N;
+    double* g1 = G + (size_t)(2 * k + 1) * N;
+    auto v = [&](int a, int b) {  // calc_one_symm_val (SymmFunc.jl:228-230)
+      const double fc = F[(size_t)a * N + b];
+      return (fc != 0.0 && fc != 1.0) ? fc * std::exp(-eta * D[(size_t)a * N + b]) : 0.0;
+    };
+    for (int a = 0; a < n1; ++a)
+      for (int b = a + 1; b < n1; ++b) {
+        const double x = v(a, b);
+        g0[a] += x;
+        g0[b] += x;
+      }
+    for (int a = n1; a < N; ++a)
+      for (int b = a + 1; b < N; ++b) {
+        const double x = v(a, b);
+        g1[a] += x;
+        g1[b] += x;
+      }
+    for (int a = 0; a < n1; ++a)
+      for (int b = n1; b < N; ++b) {
+        const double x = v(a, b);
+        g1[a] += x;
+        g0[b] += x;
+      }
+    for (int a = 0; a < N; ++a) {
+      const int t = a < n1 ? 0 : 2;
+      g0[a] = g0[a] * q[6 + t] + q[2 + t];
+      g1[a] = g1[a] * q[7 + t] + q[3 + t];
+    }
+  }
+  for (int k = 0; k < na; ++k) {
+    const double* q = &p.ang2[16 * (size_t)k];
+    const double eta = q[0], lam = q[1], zeta = q[2];
+    double* g = G + (size_t)(2 * nr + 3 * k) * N;  // rows m = 0, 1, 2
+    auto tri = [&](int a, int b, int c, int ma, int mb, int mc) {
+      const double rab = D[(size_t)a * N + b], rac = D[(size_t)a * N + c], rbc = D[(size_t)b * N + c];
+      double th[3];
+      angles(X + 3 * a, X + 3 * b, X + 3 * c, rab, rac, rbc, th);
+      const double e = std::exp(-eta * (rab + rac + rbc)) * F[(size_t)a * N + b] *
+                       F[(size_t)a * N + c] * F[(size_t)b * N + c];
+      g[(size_t)ma * N + a] += e * theta_part(th[0], lam, zeta);
+      g[(size_t)mb * N + b] += e * theta_part(th[1], lam, zeta);
+      g[(size_t)mc * N + c] += e * theta_part(th[2], lam, zeta);
+    };
+    for (int a = 0; a < n1; ++a)  // 111
+      for (int b = a + 1; b < n1; ++b)
+        for (int c = b + 1; c < n1; ++c) tri(a, b, c, 0, 0, 0);
+    for (int a = n1; a < N; ++a)  // 222
+      for (int b = a + 1; b < N; ++b)
+        for (int c = b + 1; c < N; ++c) tri(a, b, c, 2, 2, 2);
+    for (int a = 0; a < n1; ++a)  // 112
+      for (int b = a + 1; b < n1; ++b)
+        for (int c = n1; c < N; ++c) tri(a, b, c, 1, 1, 0);
+    for (int a = 0; a < n1; ++a)  // 122
+      for (int b = n1; b < N; ++b)
+        for (int c = b + 1; c < N; ++c) tri(a, b, c, 2, 1, 1);
+    for (int a = 0; a < N; ++a) {
+      const int t = a < n1 ? 0 : 3;
+      for (int m = 0; m < 3; ++m) {
+        double& x = g[(size_t)m * N + a];
+        x = x * q[4 + t + m] + q[10 + t + m];
+      }
+    }
+  }
+}
+// calc_new_runner_energy! (EnergyEvaluation.jl:1419-1432): species-1 atoms
+// through nnp1, species-2 atoms through nnp2
+double nn2_energy(const Pot& p, const double* G, int N, double* eatom);
+
 // per-atom MLP forward (ForwardPass.jl:50-84 math: activations
 // linear/tanh/.../linear).  Weight layout (ours): per layer W[n_in][n_out]
 // input-major, then bias[n_out].
@@ -553,6 +639,8 @@ struct orc_run {
   // separated volume moves (NPT separated_volume): max_displ[3:4] (xy, z),
   // max_boxheight, count_vol_xy, count_vol_z (MCStates.jl:33-47)
   bool sep = false;
+  int n_swaps = 0;          // NNVT: atom swaps per cycle
+  long n_swaps_acc = 0;     // accepted swaps (all slots)
   std::vector<double> maxd_sep, max_boxh;          // 2R, R
   std::vector<long> cnt_xy, cnt_z;                 // 2R each
   std::vector<int> wos;                             // walker of slot
@@ -570,7 +658,7 @@ struct orc_run {
   std::vector<double> rdf;   // R * 5 n_bin
   bool inited = false;
   // scratch
-  std::vector<double> trial_trow, sc_tn;
+  std::vector<double> trial_trow, sc_tn, sc_f;
   std::vector<double> trial_row, new_comp, newG, newF, new_eatom, sc_pos,
       sc_d2;
 
@@ -661,6 +749,19 @@ void nn_full(orc_run* r, int w) {
   }
 }
 
+double nn2_energy(const Pot& p, const double* G, int N, double* eatom) {
+  const int Ng = 2 * p.nrad2 + 3 * p.nang2;
+  std::vector<double> x(Ng);
+  double e = 0.0;
+  for (int a = 0; a < N; ++a) {
+    for (int s = 0; s < Ng; ++s) x[s] = G[(size_t)s * N + a];
+    eatom[a] = mlp_atom(x.data(), (a < p.n1 ? p.w : p.w_b).data(), p.nodes.data(),
+                        (int)p.nodes.size());
+    e += eatom[a];
+  }
+  return e;
+}
+
 double nn_energy(orc_run* r, const double* G, double* eatom) {
   int N = r->N, S = nsf(r);
   std::vector<double> x(S);
@@ -693,6 +794,15 @@ double init_energy(orc_run* r, int w) {
       comp[2 * i + 1] = b;
     }
     return eam_energy(comp, N, p.ean, p.ecam);
+  }
+  if (p.kind == ORC_POT_NN2) {  // set_variables + initialise_energy (:1823-1849, 1750-1766)
+    const double rc = p.rad2[1];
+    double* F = &r->F[(size_t)w * N * N];
+    const double* d = r->D(w);
+    for (size_t k = 0; k < (size_t)N * N; ++k) F[k] = cutoff(std::sqrt(d[k]), rc);
+    double* G = &r->G[(size_t)w * (2 * p.nrad2 + 3 * p.nang2) * N];
+    nn2_G(p, r->P(w), d, F, N, G);
+    return nn2_energy(p, G, N, &r->eatom[(size_t)w * N]);
   }
   if (p.kind == ORC_POT_NN) {
     nn_full(r, w);
@@ -789,7 +899,27 @@ int atom_move(orc_run* r, int w, int slot, int i) {
     }
     r->da_exact += 1;
   }
-  if (pot.kind == ORC_POT_EAM) {  // energy_update! EAM (:1567-1591)
+  if (pot.kind == ORC_POT_NN2) {  // energy_update! RuNNerPotential2Atom (:1622-1642)
+    // the trial's distance and cutoff matrices (row and column i), then its
+    // symmetry matrix and energy
+    const size_t NN = (size_t)N * N;
+    const int Ng = 2 * pot.nrad2 + 3 * pot.nang2;
+    r->sc_d2.assign(r->D(w), r->D(w) + NN);
+    r->sc_f.assign(&r->F[(size_t)w * NN], &r->F[(size_t)w * NN] + NN);
+    r->sc_pos.assign(p, p + 3 * (size_t)N);
+    r->sc_pos[3 * i] = t[0];
+    r->sc_pos[3 * i + 1] = t[1];
+    r->sc_pos[3 * i + 2] = t[2];
+    for (int j = 0; j < N; ++j) {
+      if (j == i) continue;
+      const double f = cutoff(std::sqrt(row[j]), pot.rad2[1]);
+      r->sc_d2[(size_t)i * N + j] = r->sc_d2[(size_t)j * N + i] = row[j];
+      r->sc_f[(size_t)i * N + j] = r->sc_f[(size_t)j * N + i] = f;
+    }
+    r->newG.resize((size_t)Ng * N);
+    nn2_G(pot, r->sc_pos.data(), r->sc_d2.data(), r->sc_f.data(), N, r->newG.data());
+    new_en = nn2_energy(pot, r->newG.data(), N, r->new_eatom.data());
+  } else if (pot.kind == ORC_POT_EAM) {  // energy_update! EAM (:1567-1591)
     int S2 = 2 * N;
     double* nc = r->new_comp.data();
     std::memcpy(nc, &r->comp[(size_t)w * S2], sizeof(double) * S2);
@@ -899,6 +1029,13 @@ int atom_move(orc_run* r, int w, int slot, int i) {
         tm[(size_t)i * N + j] = r->trial_trow[j];
         tm[(size_t)j * N + i] = r->trial_trow[j];
       }
+    }
+    if (pot.kind == ORC_POT_NN2) {  // swap_atom_config! + swap_vars! (swap_config.jl:40-51, 213-235)
+      const size_t NN = (size_t)N * N;
+      const int Ng = 2 * pot.nrad2 + 3 * pot.nang2;
+      std::memcpy(&r->F[(size_t)w * NN], r->sc_f.data(), sizeof(double) * NN);
+      std::memcpy(&r->G[(size_t)w * Ng * N], r->newG.data(), sizeof(double) * Ng * N);
+      std::memcpy(&r->eatom[(size_t)w * N], r->new_eatom.data(), sizeof(double) * N);
     }
     if (pot.kind == ORC_POT_EAM) {  // swap_vars! EAM (:208-211)
       std::memcpy(&r->comp[(size_t)w * N * 2], r->new_comp.data(), sizeof(double) * 2 * N);
@@ -1029,15 +1166,63 @@ int volume_move(orc_run* r, int w, int slot) {
   return 0;
 }
 
+// atom swap of the NNVT ensemble: swap_atoms (MCMoves.jl:363-370) draws one
+// atom of each species, swap_energy_update (EnergyEvaluation.jl:1438-1446)
+// gives the energy with the two positions exchanged, swap_move_config!
+// (swap_config.jl:237-276) commits; swaps change no counter
+int swap_move(orc_run* r, int w, int slot) {
+  const int N = r->N;
+  const Pot& pot = r->pot;
+  const int n1 = pot.n1;
+  const int i1 = randint(r->draw(w), n1);
+  const int i2 = n1 + randint(r->draw(w), N - n1);
+  const size_t NN = (size_t)N * N;
+  const int Ng = 2 * pot.nrad2 + 3 * pot.nang2;
+  const double* p = r->P(w);
+  r->sc_pos.assign(p, p + 3 * (size_t)N);
+  for (int k = 0; k < 3; ++k) std::swap(r->sc_pos[3 * i1 + k], r->sc_pos[3 * i2 + k]);
+  // rows and columns i1 <-> i2 of the distance and cutoff matrices
+  auto swapped = [&](const double* M, std::vector<double>& out, double diag) {
+    out.assign(M, M + NN);
+    for (int j = 0; j < N; ++j) {
+      std::swap(out[(size_t)i1 * N + j], out[(size_t)i2 * N + j]);
+    }
+    for (int j = 0; j < N; ++j) {
+      std::swap(out[(size_t)j * N + i1], out[(size_t)j * N + i2]);
+    }
+    out[(size_t)i1 * N + i1] = diag;
+    out[(size_t)i2 * N + i2] = diag;
+  };
+  swapped(r->D(w), r->sc_d2, 0.0);
+  swapped(&r->F[(size_t)w * NN], r->sc_f, 1.0);
+  r->newG.resize((size_t)Ng * N);
+  nn2_G(pot, r->sc_pos.data(), r->sc_d2.data(), r->sc_f.data(), N, r->newG.data());
+  const double new_en = nn2_energy(pot, r->newG.data(), N, r->new_eatom.data());
+  double prob = std::exp(-(new_en - r->en[w]) * r->beta[slot]);  // metropolis_condition
+  if (prob > 1) prob = 1.0;
+  if (prob >= r->draw(w)) {
+    std::memcpy(r->P(w), r->sc_pos.data(), sizeof(double) * 3 * N);
+    std::memcpy(r->D(w), r->sc_d2.data(), sizeof(double) * NN);
+    std::memcpy(&r->F[(size_t)w * NN], r->sc_f.data(), sizeof(double) * NN);
+    std::memcpy(&r->G[(size_t)w * Ng * N], r->newG.data(), sizeof(double) * Ng * N);
+    std::memcpy(&r->eatom[(size_t)w * N], r->new_eatom.data(), sizeof(double) * N);
+    r->en[w] = new_en;
+    r->n_swaps_acc += 1;
+  }
+  return 0;
+}
+
 // mc_cycle! (MCRun.jl:192-213)
 int cycle(orc_run* r, long index) {
   int R = r->R, N = r->N;
-  int n_steps = r->ens == ORC_NPT ? N + 1 : N;
+  int n_steps = r->ens == ORC_NPT ? N + 1 : r->ens == ORC_NNVT ? N + r->n_swaps : N;
   for (int s = 0; s < R; ++s) {  // mc_step! over states
     int w = r->wos[s];
     for (int k = 0; k < n_steps; ++k) {
       int idx = randint(r->draw(w), n_steps);
-      int rc = idx < N ? atom_move(r, w, s, idx) : volume_move(r, w, s);
+      int rc = idx < N                 ? atom_move(r, w, s, idx)
+               : r->ens == ORC_NNVT ? swap_move(r, w, s)
+                                    : volume_move(r, w, s);
       if (rc) return rc;
     }
   }
@@ -1278,6 +1463,35 @@ int orc_set_pot_lut(orc_run* r, const double* table, int l_angle, int l_dist, do
   r->tn.assign((size_t)r->R * r->N * r->N, 0.0);
   return 0;
 }
+int orc_set_pot_nn2(orc_run* r, const double* rad, int nrad, const double* ang, int nang,
+                    const double* w1, const double* w2, int nw, const int* nodes, int n_layers,
+                    int n1, int n_swaps) {
+  if (r->ens != ORC_NNVT) return fail("RuNNerPotential2Atom runs in the NNVT ensemble");
+  if (r->bc != ORC_BC_SPHERE) return fail("RuNNerPotential2Atom: SphericalBC only");
+  if (nrad < 1 || n1 < 1 || n1 >= r->N) return fail("NNVT: need radial functions and both species");
+  const int Ng = 2 * nrad + 3 * nang;
+  if (n_layers < 2 || nodes[0] != Ng || nodes[n_layers - 1] != 1)
+    return fail("NN2: node counts must start at 2 nrad + 3 nang and end at 1");
+  long need = 0;
+  for (int l = 1; l < n_layers; ++l) need += (long)nodes[l - 1] * nodes[l] + nodes[l];
+  if (need != nw) return fail("NN2: weight count does not match the layer sizes");
+  Pot& p = r->pot;
+  p.kind = ORC_POT_NN2;
+  p.n1 = n1;
+  p.nrad2 = nrad;
+  p.nang2 = nang;
+  p.rad2.assign(rad, rad + 10 * (size_t)nrad);
+  p.ang2.assign(ang, ang + 16 * (size_t)nang);
+  p.w.assign(w1, w1 + nw);
+  p.w_b.assign(w2, w2 + nw);
+  p.nodes.assign(nodes, nodes + n_layers);
+  r->n_swaps = n_swaps;
+  r->G.assign((size_t)r->R * Ng * r->N, 0.0);
+  r->F.assign((size_t)r->R * r->N * r->N, 0.0);
+  r->eatom.assign((size_t)r->R * r->N, 0.0);
+  r->new_eatom.resize(r->N);
+  return 0;
+}
 int orc_set_pot_eam(orc_run* r, double n, double m, double ean, double ecam) {
   if (r->ens == ORC_NPT) return fail("EAM is supported in the NVT ensemble only");
   r->pot.kind = ORC_POT_EAM;
@@ -1458,9 +1672,11 @@ int orc_finalise(orc_run* r, long mc_cycles, int mc_sample, double* en_avg,
   return 0;
 }
 
+long orc_get_swaps(orc_run* r) { return r->n_swaps_acc; }
+
 int orc_get_nn_state(orc_run* r, int w, double* G, double* eatom) {
-  if (r->pot.kind != ORC_POT_NN) return fail("not an NN run");
-  int S = nsf(r), N = r->N;
+  if (r->pot.kind != ORC_POT_NN && r->pot.kind != ORC_POT_NN2) return fail("not an NN run");
+  int S = r->pot.kind == ORC_POT_NN2 ? 2 * r->pot.nrad2 + 3 * r->pot.nang2 : nsf(r), N = r->N;
   if (G) std::memcpy(G, &r->G[(size_t)w * S * N], sizeof(double) * S * N);
   if (eatom) std::memcpy(eatom, &r->eatom[(size_t)w * N], sizeof(double) * N);
   return 0;

@@ -35,6 +35,7 @@ typedef struct orc_run orc_run;
 #define ORC_POT_NN 3       /* RuNNerPotential   :1182 */
 #define ORC_POT_ELJB 4     /* ELJPotentialB     :161 */
 #define ORC_POT_LUT 5      /* LookupTablePotential :210 */
+#define ORC_POT_NN2 6      /* RuNNerPotential2Atom :1287 */
 /* boundary kinds (src/BoundaryConditions.jl) */
 #define ORC_BC_SPHERE 0
 #define ORC_BC_CUBIC 1
@@ -43,6 +44,7 @@ typedef struct orc_run orc_run;
 /* ensembles (src/Ensembles.jl) */
 #define ORC_NVT 0
 #define ORC_NPT 1
+#define ORC_NNVT 2         /* NNVT :138 (two species, atom swaps) */
 
 /* One PT run of R replicas of N atoms.  xyz holds R start configurations
  * (walker w starts from xyz[w*N*3 ...]); T holds the R temperatures (K);
@@ -65,6 +67,15 @@ const char* orc_last_error(void);
 
 int orc_set_pot_elj(orc_run* r, const double* c, int K, int even);
 int orc_set_pot_eam(orc_run* r, double n, double m, double ean, double ecam);
+/* RuNNerPotential2Atom (EnergyEvaluation.jl:1287-1314) for the NNVT ensemble:
+ * n1 atoms of species 1 (indices 0..n1-1), the rest species 2; rad: nrad rows
+ * {eta, r_cut, G_offset[4], G_norm[4]} (RadialType2a, SymmFunc.jl:54-85);
+ * ang: nang rows {eta, lambda, zeta, r_cut, tpz[6], G_offset[6]}
+ * (AngularType3a, :114-175); w1 / w2: the two species' MLP weights (our
+ * layout), nodes[0] == 2 nrad + 3 nang; n_swaps atom swaps per cycle. */
+int orc_set_pot_nn2(orc_run* r, const double* rad, int nrad, const double* ang, int nang,
+                    const double* w1, const double* w2, int nw, const int* nodes, int n_layers,
+                    int n1, int n_swaps);
 /* ELJPotentialB(a, b, c) (EnergyEvaluation.jl:161-183) */
 int orc_set_pot_eljb(orc_run* r, const double* a, const double* b, const double* c, int K);
 /* LookupTablePotential (EnergyEvaluation.jl:210-260); table is Julia's
@@ -104,6 +115,8 @@ int orc_finalise(orc_run* r, long mc_cycles, int mc_sample, double* en_avg,
  * the R x 5 n_bin histogram with its bin width delta_r2 */
 int orc_set_rdf(orc_run* r, int on);
 int orc_get_rdf(orc_run* r, double* rdf, double* dr2);
+/* NNVT: accepted atom swaps so far (all slots) */
+long orc_get_swaps(orc_run* r);
 /* NN only: G matrix (nsf x N, column per atom) of walker w */
 int orc_get_nn_state(orc_run* r, int w, double* G, double* eatom);
 

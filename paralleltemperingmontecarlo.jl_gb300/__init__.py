@@ -32,6 +32,7 @@ __all__ = ["kB", "MCParams", "TempGrid", "SphericalBC", "CubicBC", "RectangularB
            "Config", "NVT", "NPT",
            "ELJPotential", "ELJPotentialEven", "ELJPotentialB", "LookupTablePotential",
            "read_lookuptable", "EmbeddedAtomPotential", "RuNNerPotential",
+           "RuNNerPotential2Atom", "NNVT",
            "Output", "MCState", "PairSurrogate",
            "Engine", "ptmc_run", "multihistogram_NVT", "multihistogram_NPT", "read_checkpoint",
            "multihistogram", "postprocess",
@@ -216,6 +217,23 @@ class NPT:
 
 
 @dataclass
+class NNVT:
+    """NNVT(natoms; natomswaps=1) (src/Ensembles.jl:138-151): two species,
+    natoms = [n1, n2], atoms 0..n1-1 of every configuration are species 1;
+    N atom moves and natomswaps atom swaps per cycle."""
+    natoms: tuple
+    n_atom_swaps: int = 1
+
+    @property
+    def n_atoms(self):
+        return int(self.natoms[0]) + int(self.natoms[1])
+
+    @property
+    def n_atom_moves(self):
+        return self.n_atoms
+
+
+@dataclass
 class ELJPotential:
     """ELJPotential: V(r) = sum_i c_i r^-(5+i) (src/EnergyEvaluation.jl:923-932)."""
     coeff: list
@@ -231,6 +249,42 @@ class ELJPotentialB:
     coeff_a: list
     coeff_b: list
     coeff_c: list
+
+
+@dataclass
+class RuNNerPotential2Atom:
+    """RuNNerPotential2Atom(nnp1, nnp2, radsymvec, angsymvec, n1, n2)
+    (src/EnergyEvaluation.jl:1287-1314): rad [nrad, 10] rows {eta, r_cut,
+    G_offset[4], G_norm[4]} (RadialType2a), ang [nang, 16] rows {eta, lambda,
+    zeta, r_cut, tpz[6], G_offset[6]} (AngularType3a), the two species'
+    networks w1, w2 (per layer W[n_in][n_out] then b) with nodes =
+    [2 nrad + 3 nang, H1, H2, 1]; species 1 = the first n1 atoms."""
+    rad: np.ndarray
+    ang: np.ndarray
+    w1: np.ndarray
+    w2: np.ndarray
+    nodes: list
+    n1: int
+
+    @staticmethod
+    def radial(eta, r_cut, g_vals_a, g_vals_b):
+        """RadialType2a{T}(eta, r_cut, type, G_vals_a, G_vals_b)
+        (MachineLearningPotential/SymmFunc.jl:64-85): G_vals_x = [[max, min]
+        of the species-1 neighbour row, [max, min] of the species-2 row]."""
+        vals = [g_vals_a[0], g_vals_a[1], g_vals_b[0], g_vals_b[1]]
+        norm = [1 / (v[0] - v[1]) for v in vals]
+        off = [-v[1] * n for v, n in zip(vals, norm)]
+        return [eta, r_cut] + off + norm
+
+    @staticmethod
+    def angular(eta, lam, zeta, r_cut, g_vals_a, g_vals_b):
+        """AngularType3a{T}(eta, lambda, zeta, r_cut, type, G_valsa, G_valsb)
+        (SymmFunc.jl:139-175): three [max, min] per centre species."""
+        vals = list(g_vals_a) + list(g_vals_b)
+        norm = [1 / (v[0] - v[1]) for v in vals]
+        tpz = [2.0 ** (1 - zeta) * n for n in norm]
+        off = [-v[1] * n for v, n in zip(vals, norm)]
+        return [eta, lam, zeta, r_cut] + tpz + off
 
 
 @dataclass
@@ -457,7 +511,8 @@ class Engine:
         p.n_bin = mc_params.n_bin
         p.min_acc = mc_params.min_acc
         p.max_acc = mc_params.max_acc
-        p.ensemble = _capi.NPT if isinstance(ensemble, NPT) else _capi.NVT
+        p.ensemble = (_capi.NPT if isinstance(ensemble, NPT)
+                      else _capi.NNVT if isinstance(ensemble, NNVT) else _capi.NVT)
         p.pressure = ensemble.pressure if isinstance(ensemble, NPT) else 0.0
         p.t_i, p.t_f = temp.ti, temp.tf
         p.tdistr = _capi.TLINEAR if temp.tdistr == "equally_spaced" else _capi.TGEOMETRIC
@@ -476,12 +531,25 @@ class Engine:
             self._ck(self.L.ptmc_set_rdf(h, 1))
         if isinstance(ensemble, NPT) and ensemble.separated_volume:
             self._ck(self.L.ptmc_set_separated_volume(h, 1))
+        if isinstance(ensemble, NNVT):
+            self._ck(self.L.ptmc_set_atom_swaps(h, int(ensemble.n_atom_swaps)))
         self.n_runs, self.R = n_runs, mc_params.n_traj
         self.N = {}
         self.bc = {}
         if isinstance(potential, (ELJPotential, ELJPotentialEven)):
             c = np.ascontiguousarray(potential.coeff, dtype=np.float64)
             self._ck(self.L.ptmc_set_potential_elj(h, _dptr(c), len(c), int(potential.even)))
+        elif isinstance(potential, RuNNerPotential2Atom):
+            if not isinstance(ensemble, NNVT) or int(ensemble.natoms[0]) != potential.n1:
+                raise ValueError("RuNNerPotential2Atom runs in NNVT(natoms) with natoms[0] == n1")
+            rad = np.ascontiguousarray(potential.rad, dtype=np.float64)
+            ang = np.ascontiguousarray(potential.ang, dtype=np.float64).reshape(-1, 16)
+            w1 = np.ascontiguousarray(potential.w1, dtype=np.float64)
+            w2 = np.ascontiguousarray(potential.w2, dtype=np.float64)
+            nodes = np.ascontiguousarray(potential.nodes, dtype=np.int32)
+            self._ck(self.L.ptmc_set_potential_nn2(
+                h, _dptr(rad), len(rad), _dptr(ang), len(ang), _dptr(w1), _dptr(w2), len(w1),
+                nodes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(nodes), potential.n1))
         elif isinstance(potential, ELJPotentialB):
             a, b, c = (np.ascontiguousarray(v, dtype=np.float64)
                        for v in (potential.coeff_a, potential.coeff_b, potential.coeff_c))
@@ -623,6 +691,12 @@ class Engine:
                                         cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
                                         _dptr(ham)))
         return dict(xyz=xyz, en_tot=en, box=box, max_displ=md, counts=cnt, ham=ham)
+
+    def swaps(self, run=0):
+        """Accepted atom swaps of `run` so far (NNVT)."""
+        n = ctypes.c_longlong()
+        self._ck(self.L.ptmc_get_swaps(self.h, run, ctypes.byref(n)))
+        return n.value
 
     def energies(self):
         """Slot-ordered energies of every run, [n_runs, R], in one read."""

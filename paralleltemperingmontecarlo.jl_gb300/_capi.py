@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libptmc_gb300.so")
 
 PTMC_OK = 0
 ERRORS = {-1: "argument", -2: "state", -3: "cuda", -4: "sphere", -5: "io", -6: "limit"}
-NVT, NPT = 0, 1
+NVT, NPT, NNVT = 0, 1, 2
 BC_SPHERE, BC_CUBIC, BC_RECTANGULAR, BC_RHOMBIC = 0, 1, 2, 3
 FP64, FP32_RESYNC = 0, 1
 TGEOMETRIC, TLINEAR = 0, 1
@@ -59,6 +59,11 @@ SIGNATURES = {
     "ptmc_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Params)]),
     "ptmc_set_potential_elj": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]),
     "ptmc_set_potential_eam": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_double] * 4),
+    "ptmc_set_potential_nn2": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, _dp, ctypes.c_int,
+                                              _dp, _dp, ctypes.c_int, _ip, ctypes.c_int,
+                                              ctypes.c_int]),
+    "ptmc_set_atom_swaps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "ptmc_get_swaps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _llp]),
     "ptmc_set_potential_eljb": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int]),
     "ptmc_set_potential_lookup": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]
                                   + [ctypes.c_double] * 5),

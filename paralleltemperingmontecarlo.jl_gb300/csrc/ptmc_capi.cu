@@ -31,6 +31,7 @@
 #include "../../include/ptmc_gb300.h"
 #include "ptmc_engine.cuh"
 #include "ptmc_nn.cuh"
+#include "ptmc_nn2.cuh"
 #include "ptmc_surrogate.cuh"
 
 using namespace ptmc;
@@ -146,6 +147,12 @@ struct ptmc_ctx {
   int lut_na = 0, lut_nd = 0;
   double lut_par[4] = {0, 0, 0, 0};  // start_dist, d_dist, d_angle, c6coeff
   DBuf<double> d_tan, d_lut;
+  // two-species RuNNer potential (NNVT ensemble)
+  std::vector<double> nn2_rad, nn2_ang, nn2_W1, nn2_W2;
+  int nn2_n1 = 0, nn2_H1 = 0, nn2_H2 = 0, n_swaps = 1;
+  NN2Params Q2{};
+  DBuf<double> d_nn2_rad, d_nn2_ang, d_nn2_W1, d_nn2_W2;
+  DBuf<long long> d_nn2_swaps;
   DBuf<unsigned long long> d_ctr;
   DBuf<int> d_status, d_wos;
   DBuf<long long> d_cnt;
@@ -244,6 +251,15 @@ int pull_runs(ptmc_ctx* c) {
 
 // one chunk of `ncyc` cycles for every group, groups on forked streams
 int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
+  if (c->pot == POT_NN2) {  // one cycle kernel + one run epilogue per cycle
+    for (int k = 0; k < ncyc; ++k) {
+      int rc = nn2_launch_cycle(c->K, c->Q2, c->Q, c->W, (int)c->rd.size(), c->R(), c->nn_Nmax,
+                                phase, c->st);
+      if (rc) return c->cuda_fail((cudaError_t)rc, "k_nn2_cycle launch");
+      c->stats.kernel_launches += 2;
+    }
+    return PTMC_OK;
+  }
   if (c->pot == POT_NN) {  // one cycle kernel + one run epilogue per cycle
     for (int k = 0; k < ncyc; ++k) {
       int rc = nn_launch_cycle(c->K, c->Q, c->W, (int)c->rd.size(), c->R(), c->nn_Nmax,
@@ -270,7 +286,7 @@ int enqueue_chunk(ptmc_ctx* c, int ncyc, int phase) {
 
 int default_chunk(ptmc_ctx* c) {
   if (c->p.cycles_per_launch > 0) return c->p.cycles_per_launch;
-  if (c->pot == POT_NN) return 16;  // cycles per chunk (each cycle is 2 launches)
+  if (c->pot == POT_NN || c->pot == POT_NN2) return 16;  // cycles per chunk (2 launches each)
   // aim at a few milliseconds of work per launch
   int maxN = 0;
   for (auto& G : c->groups) maxN = std::max(maxN, G.N);
@@ -311,7 +327,8 @@ int run_phase(ptmc_ctx* c, long long n, int phase) {
       CK(cudaGraphLaunch(it->second, c->st));
       c->stats.graph_launches += 1;
       c->stats.kernel_launches +=
-          c->pot == POT_NN ? 2LL * reps * chunk : (long long)reps * c->groups.size();
+          (c->pot == POT_NN || c->pot == POT_NN2) ? 2LL * reps * chunk
+                                                  : (long long)reps * c->groups.size();
     }
     done = nfull * chunk * reps;
   }
@@ -370,7 +387,7 @@ int ptmc_create(ptmc_ctx** out, const ptmc_params* p) {
     g_err = "ptmc_create: invalid MCParams";
     return PTMC_ERR_ARG;
   }
-  if (p->ensemble != PTMC_NVT && p->ensemble != PTMC_NPT) {
+  if (p->ensemble != PTMC_NVT && p->ensemble != PTMC_NPT && p->ensemble != PTMC_NNVT) {
     g_err = "ptmc_create: unknown ensemble";
     return PTMC_ERR_ARG;
   }
@@ -458,6 +475,54 @@ int ptmc_set_potential_lookup(ptmc_ctx* c, const double* table, int l_angle, int
   c->lut_par[2] = d_angle;
   c->lut_par[3] = c6coeff;
   c->coeff.clear();
+  return PTMC_OK;
+}
+
+int ptmc_set_potential_nn2(ptmc_ctx* c, const double* rad, int nrad, const double* ang, int nang,
+                           const double* w1, const double* w2, int nw, const int* nodes,
+                           int n_layers, int n1) {
+  if (!c || !rad || (nang > 0 && !ang) || !w1 || !w2 || !nodes) return PTMC_ERR_ARG;
+  if (c->p.ensemble != PTMC_NNVT)
+    return c->fail(PTMC_ERR_ARG, "RuNNerPotential2Atom runs in the NNVT ensemble");
+  if (nrad < 1 || nang < 0 || n1 < 1) return c->fail(PTMC_ERR_ARG, "NNVT: bad symmetry-function counts");
+  const int Ng = 2 * nrad + 3 * nang;
+  if (n_layers != 4 || nodes[0] != Ng || nodes[3] != 1)
+    return c->fail(PTMC_ERR_ARG, "RuNNerPotential2Atom: nodes = [2 nrad + 3 nang, H1, H2, 1]");
+  if (nodes[1] < 1 || nodes[2] < 1 || nodes[1] > MAX_NN2_HIDDEN || nodes[2] > MAX_NN2_HIDDEN)
+    return c->fail(PTMC_ERR_LIMIT, "RuNNerPotential2Atom: 1..64 units per hidden layer");
+  const long need = (long)Ng * nodes[1] + nodes[1] + (long)nodes[1] * nodes[2] + nodes[2] + nodes[2] + 1;
+  if (nw != need) return c->fail(PTMC_ERR_ARG, "RuNNerPotential2Atom: weight count does not match nodes");
+  c->pot = POT_NN2;
+  c->nn2_rad.assign(rad, rad + 10 * (size_t)nrad);
+  c->nn2_ang.assign(ang, ang + 16 * (size_t)nang);
+  c->nn2_W1.assign(w1, w1 + nw);
+  c->nn2_W2.assign(w2, w2 + nw);
+  c->nn2_n1 = n1;
+  c->nn2_H1 = nodes[1];
+  c->nn2_H2 = nodes[2];
+  c->Q2.nrad = nrad;
+  c->Q2.nang = nang;
+  return PTMC_OK;
+}
+
+int ptmc_set_atom_swaps(ptmc_ctx* c, int n_swaps) {
+  if (!c) return PTMC_ERR_ARG;
+  if (c->inited) return c->fail(PTMC_ERR_STATE, "atom swaps are set before ptmc_init");
+  if (n_swaps < 0) return c->fail(PTMC_ERR_ARG, "n_atom_swaps must be >= 0");
+  c->n_swaps = n_swaps;
+  return PTMC_OK;
+}
+
+int ptmc_get_swaps(ptmc_ctx* c, int run, long long* accepted) {
+  if (!c || !accepted) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  *accepted = 0;
+  if (c->pot != POT_NN2) return PTMC_OK;
+  const RunDesc& r = c->rd[c->dev_of_run[run]];
+  std::vector<long long> sw(c->R());
+  CK(cudaMemcpy(sw.data(), c->d_nn2_swaps.p + r.wk, sizeof(long long) * c->R(), cudaMemcpyDeviceToHost));
+  for (long long v : sw) *accepted += v;
   return PTMC_OK;
 }
 
@@ -598,7 +663,19 @@ int ptmc_init(ptmc_ctx* c) {
   for (auto& r : c->runs)
     if (r.N == 0) return c->fail(PTMC_ERR_STATE, "every run needs start configurations");
   const int R = c->R();
-  const bool nn = c->pot == POT_NN;
+  const bool nn2 = c->pot == POT_NN2;
+  const bool nn = c->pot == POT_NN || nn2;  // one CTA per walker, per-cycle epilogue
+  if (c->p.ensemble == PTMC_NNVT && !nn2)
+    return c->fail(PTMC_ERR_ARG, "the NNVT ensemble needs RuNNerPotential2Atom");
+  if (nn2) {
+    if (c->f32())
+      return c->fail(PTMC_ERR_ARG, "RuNNerPotential2Atom runs in the plain FP64 form (precision PTMC_FP64)");
+    for (auto& r : c->runs) {
+      if (r.N > MAX_NN2_ATOMS) return c->fail(PTMC_ERR_LIMIT, "RuNNerPotential2Atom: at most 64 atoms");
+      if (r.N <= c->nn2_n1)
+        return c->fail(PTMC_ERR_ARG, "NNVT: every run needs atoms of both species (N > n1)");
+    }
+  }
   if (!nn && R > MAX_REPLICAS)
     return c->fail(PTMC_ERR_LIMIT, "at most 32 replicas per run (one warp per replica in one CTA)");
   if (nn) {
@@ -836,7 +913,49 @@ int ptmc_init(ptmc_ctx* c) {
   K.mc_sample = c->p.mc_sample;
   K.resync_every = c->p.resync_every;
   K.seed = c->p.seed;
-  if (nn) {
+  if (nn2) {
+    int Nmax = 0;
+    for (auto& G : c->groups) Nmax = std::max(Nmax, G.N);
+    c->nn_Nmax = Nmax;
+    std::vector<int> row(W), sow(W);
+    for (int d = 0; d < nr; ++d)
+      for (int w = 0; w < R; ++w) {
+        row[c->rd[d].wk + w] = d;
+        sow[c->rd[d].wk + w] = w;
+      }
+    if (c->d_nn_row.alloc(W) || c->d_nn_sow.alloc(W) || c->d_nn2_rad.alloc(c->nn2_rad.size()) ||
+        c->d_nn2_ang.alloc(c->nn2_ang.size()) || c->d_nn2_W1.alloc(c->nn2_W1.size()) ||
+        c->d_nn2_W2.alloc(c->nn2_W2.size()) || c->d_nn2_swaps.alloc(W))
+      return c->fail(PTMC_ERR_CUDA, "device allocation failed");
+    CK(cudaMemcpyAsync(c->d_nn_row.p, row.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_nn_sow.p, sow.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s));
+    for (auto pr : {std::make_pair(&c->d_nn2_rad, &c->nn2_rad), std::make_pair(&c->d_nn2_ang, &c->nn2_ang),
+                    std::make_pair(&c->d_nn2_W1, &c->nn2_W1), std::make_pair(&c->d_nn2_W2, &c->nn2_W2)})
+      if (!pr.second->empty())
+        CK(cudaMemcpyAsync(pr.first->p, pr.second->data(), sizeof(double) * pr.second->size(),
+                           cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(c->d_nn2_swaps.p, 0, sizeof(long long) * W, s));
+    NN2Params& Q2 = c->Q2;
+    Q2.n1 = c->nn2_n1;
+    Q2.H1 = c->nn2_H1;
+    Q2.H2 = c->nn2_H2;
+    Q2.n_swaps = c->n_swaps;
+    Q2.rcut = c->nn2_rad[1];  // r_cut of the first radial function (EnergyEvaluation.jl:1297)
+    Q2.rad = c->d_nn2_rad.p;
+    Q2.ang = c->d_nn2_ang.p;
+    Q2.W1 = c->d_nn2_W1.p;
+    Q2.W2 = c->d_nn2_W2.p;
+    Q2.run_of_walker = c->d_nn_row.p;
+    Q2.sow = c->d_nn_sow.p;
+    Q2.swaps_acc = c->d_nn2_swaps.p;
+    c->Q.run_of_walker = c->d_nn_row.p;  // the run epilogue's walker <-> slot tables
+    c->Q.sow = c->d_nn_sow.p;
+    if (nn2_smem_bytes(Q2, Nmax) > 227 * 1024)
+      return c->fail(PTMC_ERR_LIMIT, "NNVT walker state exceeds 227 KB of shared memory");
+    int e = nn2_launch_init(K, Q2, W, Nmax, s);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_nn2_init launch");
+    c->stats.kernel_launches += 1;
+  } else if (nn) {
     int S = (int)c->nn_sf.size();
     int Nmax = 0;
     for (auto& G : c->groups) Nmax = std::max(Nmax, G.N);
@@ -960,6 +1079,13 @@ int ptmc_run_cycles(ptmc_ctx* c, long long n) {
 int ptmc_resync(ptmc_ctx* c) {
   if (!c) return PTMC_ERR_ARG;
   if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (c->pot == POT_NN2) {  // recompute the energies from the positions
+    int e = nn2_launch_init(c->K, c->Q2, c->W, c->nn_Nmax, c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_nn2_init launch");
+    c->stats.kernel_launches += 1;
+    CK(cudaStreamSynchronize(c->st));
+    return PTMC_OK;
+  }
   if (c->pot == POT_NN) {  // recompute G and the energies from the positions
     int e = nn_launch_init(c->K, c->Q, c->W, c->nn_Nmax, !c->f32(), c->st);
     if (e) return c->cuda_fail((cudaError_t)e, "k_nn_init launch");
@@ -1144,6 +1270,8 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_cnt_sep.free_();
   c->d_tan.free_();
   c->d_lut.free_();
+  for (auto* b : {&c->d_nn2_rad, &c->d_nn2_ang, &c->d_nn2_W1, &c->d_nn2_W2}) b->free_();
+  c->d_nn2_swaps.free_();
   c->d_nn_sf.free_();
   c->d_nn_W.free_();
   c->d_nn_G.free_();
@@ -1218,6 +1346,10 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
     s += "ensemble n_atom_moves n_volume_moves n_atom_swaps pressure separated_volume\n";
     s += "NPT " + std::to_string(N) + " " + std::to_string(N) + " 1 0 " + fmt_double(c->p.pressure) +
          (c->sep_vol ? " true\n" : " false\n");
+  } else if (c->p.ensemble == PTMC_NNVT) {  // writeensemble NNVT (:51-55)
+    s += "ensemble n_1 n_2 n_atom_moves n_atom_swaps\n";
+    s += "NNVT " + std::to_string(c->nn2_n1) + " " + std::to_string(N - c->nn2_n1) + " " +
+         std::to_string(N) + " " + std::to_string(c->n_swaps) + "\n";
   } else {
     s += "ensemble n_atom_moves n_atom_swaps\n";
     s += "NVT " + std::to_string(N) + " " + std::to_string(N) + " 0\n";
@@ -1225,7 +1357,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
   if (c->pot == POT_EAM) {
     s += "EAM: " + fmt_double(c->eam[0]) + " " + fmt_double(c->eam[1]) + " " + fmt_double(c->eam[2]) +
          " " + fmt_double(c->eam[3]) + " \n";
-  } else if (c->pot == POT_NN) {
+  } else if (c->pot == POT_NN || c->pot == POT_NN2) {
     s += "runnerpotential \n";
   } else if (c->pot == POT_LUT) {
     s += "LookupTablePotential \n";
@@ -1319,7 +1451,8 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       (rc = dump(c, b, c->d_status)) || (rc = dump(c, b, c->d_wos)) || (rc = dump(c, b, c->d_cnt)) ||
       (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)) ||
       (rc = dump(c, b, c->d_rdf)) || (rc = dump(c, b, c->d_boxh)) || (rc = dump(c, b, c->d_maxboxh)) ||
-      (rc = dump(c, b, c->d_maxd_sep)) || (rc = dump(c, b, c->d_cnt_sep)) || (rc = dump(c, b, c->d_tan)))
+      (rc = dump(c, b, c->d_maxd_sep)) || (rc = dump(c, b, c->d_cnt_sep)) || (rc = dump(c, b, c->d_tan)) ||
+      (rc = dump(c, b, c->d_nn2_swaps)))
     return rc;
   put(b, "PTMCEND!", 8);
   if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
@@ -1368,7 +1501,8 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
       (rc = undump(c, b, at, c->d_nn_G)) || (rc = undump(c, b, at, c->d_nn_sow)) ||
       (rc = undump(c, b, at, c->d_rdf)) || (rc = undump(c, b, at, c->d_boxh)) ||
       (rc = undump(c, b, at, c->d_maxboxh)) || (rc = undump(c, b, at, c->d_maxd_sep)) ||
-      (rc = undump(c, b, at, c->d_cnt_sep)) || (rc = undump(c, b, at, c->d_tan)))
+      (rc = undump(c, b, at, c->d_cnt_sep)) || (rc = undump(c, b, at, c->d_tan)) ||
+      (rc = undump(c, b, at, c->d_nn2_swaps)))
     return rc;
   c->rd = rd;
   c->equilibrated = hdr[3] != 0;

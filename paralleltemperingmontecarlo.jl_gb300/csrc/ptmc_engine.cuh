@@ -22,7 +22,8 @@
 
 namespace ptmc {
 
-enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3, POT_ELJB = 4, POT_LUT = 5 };
+enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3, POT_ELJB = 4, POT_LUT = 5,
+       POT_NN2 = 6 };  // POT_NN2: two-species RuNNer potential (NNVT)
 // pair potentials with an angle to z (ELJPotentialB, LookupTablePotential)
 __host__ __device__ constexpr bool pot_b(int pot) { return pot == POT_ELJB || pot == POT_LUT; }
 enum { BC_SPH = 0, BC_CUB = 1, BC_RECT = 2, BC_RHB = 3 };  // RECT/RHB: length L, height H

@@ -34,6 +34,7 @@
 #include "ptmc_device.cuh"
 #include "ptmc_engine.cuh"
 #include "ptmc_nn.cuh"
+#include "ptmc_nn2.cuh"
 
 namespace ptmc {
 
@@ -1081,6 +1082,12 @@ int nn_launch_cycle(const KParams& P, const NNParams& Q, int n_walkers, int n_ru
   }
   if ((e = (int)cudaGetLastError())) return e;
   k_run_epilogue<<<n_runs, ((R + 31) / 32) * 32, 0, st>>>(P, Q, 0, phase);
+  return (int)cudaGetLastError();
+}
+
+int nn_launch_epilogue(const KParams& P, const NNParams& Q, int n_runs, int R, int phase,
+                       void* stream) {
+  k_run_epilogue<<<n_runs, ((R + 31) / 32) * 32, 0, (cudaStream_t)stream>>>(P, Q, 0, phase);
   return (int)cudaGetLastError();
 }
 
