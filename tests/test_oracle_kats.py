@@ -353,6 +353,42 @@ def test_lookup_parser_and_oracle_energy(orc, pk, tmp_path):
         assert orc.lut_energy(lut, ri * ri, ti) == lut_energy_np(t, sd, dd, da, c6, ri * ri, ti)
 
 
+def test_nnvt_oracle_chain_is_self_consistent(orc):
+    """NNVT with the two-species RuNNer potential on the oracle: after atom moves
+    and atom swaps the running energies equal a from-scratch evaluation of the
+    final configurations, swaps are accepted, and a swap keeps the species
+    composition (positions are exchanged, atoms keep their species)."""
+    import ptmc_gb300.starts as st
+    import nn2_synth as S
+    rad, ang, w1, w2, nodes = S.potential()
+    N, n1, R = 10, 6, 3
+    x0 = st.sphere_start(N, 6.5, 4.5, 4)
+    T, _ = orc.tempgrid(300.0, 900.0, R)
+    run = orc.Run(N, R, np.stack([x0] * R), T, ensemble=orc.NNVT, bc=orc.BC_SPHERE,
+                  bc_param=10.0, exch_prob=1.0, seed=2)
+    run.set_nn2(rad, ang, w1, w2, nodes, n1, n_swaps=2)
+    run.init()
+    run.cycles(1, 150)
+    x, e, _ = run.walkers()
+    assert run.swaps() > 0
+    fresh = orc.Run(N, R, x, T, ensemble=orc.NNVT, bc=orc.BC_SPHERE, bc_param=10.0, seed=2)
+    fresh.set_nn2(rad, ang, w1, w2, nodes, n1, n_swaps=2)
+    fresh.init()
+    np.testing.assert_allclose(fresh.walkers()[1], e, rtol=1e-12)
+
+
+def test_runner2atom_normalisations(pk):
+    """RadialType2a / AngularType3a constructors (SymmFunc.jl:64-85, 139-175)."""
+    r = pk.RuNNerPotential2Atom.radial(0.01, 12.0, [[3.0, 1.0], [2.0, 0.0]], [[5.0, 1.0], [4.0, 2.0]])
+    assert r[:2] == [0.01, 12.0]
+    assert r[6:] == [0.5, 0.5, 0.25, 0.5]  # G_norm = 1 / (max - min)
+    assert r[2:6] == [-0.5, -0.0, -0.25, -1.0]  # G_offset = -min G_norm
+    a = pk.RuNNerPotential2Atom.angular(0.001, -1.0, 4.0, 12.0, [[2.0, 0.0]] * 3, [[1.0, 0.5]] * 3)
+    assert a[:4] == [0.001, -1.0, 4.0, 12.0]
+    assert a[4:10] == [2.0 ** -3 * 0.5] * 3 + [2.0 ** -3 * 2.0] * 3  # tpz = 2^(1-zeta) G_norm
+    assert a[10:] == [-0.0] * 3 + [-1.0] * 3
+
+
 # ---------------------------------------------------------------- surrogate oracle
 SUR_CFG = [2.0, 12.0, 1.125, 12.0, 0.02]
 
