@@ -750,6 +750,7 @@ int ptmc_init(ptmc_ctx* c) {
     r.comp_off = co;
     r.hist_off = ho;
     r.hist_stride = hstride;
+    r.n_start = h.n_start;
     r.cyc[0] = r.cyc[1] = r.cyc[2] = 1;
     r.run_ctr = 0;
     po += (long long)R * h.N * 3;

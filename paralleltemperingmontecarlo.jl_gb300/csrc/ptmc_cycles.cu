@@ -329,27 +329,50 @@ __device__ double walker_energy64(const double* X, int N, double L, double H, do
 // variables and initial energy of every walker, in FP64, from HBM positions.
 template <int POT, int BC, int ENS, bool F32>
 __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
+  // walkers w >= n_start start from the configuration of walker w mod n_start
+  // (src/Initialization.jl:88-96): only the distinct starts are evaluated, the
+  // other walkers copy their energy and variables
   const RunDesc rd = P.runs[run0 + blockIdx.x];
   const int N = rd.N, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (w >= rd.R) return;
-  const int g = rd.wk + w;
-  const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
-  double* M = ((ENS == ENS_NPT || pot_b(POT)) && !F32) ? P.mat + rd.mat_off + (size_t)w * N * N
-                                                         : nullptr;
-  double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
-  double e;
-  if constexpr (pot_b(POT))
-    e = walker_energy_b<POT, BC, ENS>(P, X, N, P.box[g], P.boxh[g], P.rc2[g], P.ca, P.cb, P.c,
-                                      P.K, M, P.tan + rd.mat_off + (size_t)w * N * N, lane);
-  else
-    e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
-                                      -0.5 * P.eam_n, -0.5 * P.eam_m,
-                                      P.eam_ean, P.eam_ecam, M, comp,
-                                      nullptr, lane);
-  if (lane == 0) {
-    P.en[g] = e;
-    P.status[g] = ST_OK;
-    P.drift[g] = 0.0;
+  const int ns = rd.n_start > 0 && rd.n_start < rd.R ? rd.n_start : rd.R;
+  const bool keep_m = (ENS == ENS_NPT || pot_b(POT)) && !F32;
+  auto mat = [&](int v) { return P.mat + rd.mat_off + (size_t)v * N * N; };
+  auto cmp = [&](int v) { return P.comp + rd.comp_off + (size_t)v * N * 2; };
+  if (w < ns) {
+    const int g = rd.wk + w;
+    const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
+    double* M = keep_m ? mat(w) : nullptr;
+    double* comp = POT == POT_EAM ? cmp(w) : nullptr;
+    double e;
+    if constexpr (pot_b(POT))
+      e = walker_energy_b<POT, BC, ENS>(P, X, N, P.box[g], P.boxh[g], P.rc2[g], P.ca, P.cb, P.c,
+                                        P.K, M, P.tan + rd.mat_off + (size_t)w * N * N, lane);
+    else
+      e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
+                                        -0.5 * P.eam_n, -0.5 * P.eam_m,
+                                        P.eam_ean, P.eam_ecam, M, comp,
+                                        nullptr, lane);
+    if (lane == 0) {
+      P.en[g] = e;
+      P.status[g] = ST_OK;
+      P.drift[g] = 0.0;
+    }
+  }
+  __syncthreads();
+  if (w >= ns && w < rd.R) {
+    const int g = rd.wk + w, src = w % ns;
+    if (POT == POT_EAM)
+      for (int k = lane; k < 2 * N; k += 32) cmp(w)[k] = cmp(src)[k];
+    if (keep_m)
+      for (int k = lane; k < N * N; k += 32) mat(w)[k] = mat(src)[k];
+    if (pot_b(POT))
+      for (int k = lane; k < N * N; k += 32)
+        P.tan[rd.mat_off + (size_t)w * N * N + k] = P.tan[rd.mat_off + (size_t)src * N * N + k];
+    if (lane == 0) {
+      P.en[g] = P.en[rd.wk + src];
+      P.status[g] = ST_OK;
+      P.drift[g] = 0.0;
+    }
   }
 }
 

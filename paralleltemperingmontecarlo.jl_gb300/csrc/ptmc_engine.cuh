@@ -43,7 +43,7 @@ struct RunDesc {
   long long comp_off;
   long long hist_off;       // element offset of slot 0 in hist
   int hist_stride;          // hist elements per slot
-  int pad0;
+  int n_start;              // distinct start configurations (walker w starts from w mod n_start)
   double en_min, en_max, dE;  // energy histogram (Sampling.jl:141-194)
   double v_min, v_max, dV;    // volume histogram (NPT)
   long long cyc[3];         // next cycle index (1-based) per phase
