@@ -21,6 +21,8 @@ temperature, and the two means must agree within 5 combined standard errors.
     formulation overflows there.
   * NN13 (RuNNer potential, random FP32 weights), FP32 + delayed acceptance
     with a GPU-trained surrogate and calibrated screening strength
+  * Ne32 NPT (cubic box, cut-off + tail correction, 1 atm): Cp(T) from
+    multihistogram_NPT, FP32 move rows + FP64 volume-move enthalpy + resync
 """
 import json
 import os
@@ -97,6 +99,33 @@ def test_cv_cu55_eam_fp32_vs_fp64(pk):
     pre.close()
     args = (pk, pot, starts, bc, R, T, 400, 1500)
     compare(run_form(*args, "fp64", 21), run_form(*args, "fp32", 22), "Cu55 EAM FP32+resync")
+
+
+def test_cp_ne32_npt_fp32_vs_fp64(pk):
+    """Bulk Ne NPT (32 atoms, fcc start 8.4 bohr, cubic box, cut-off L/2 + tail,
+    1 atm): Cp(T) from multihistogram_NPT of the FP32 form (FP32 move rows,
+    FP64 volume-move enthalpy, FP64 resync) against the plain FP64 form, 12
+    independent runs each."""
+    import ptmc_gb300.starts as S
+    N, R, n_runs = 32, 8, 12
+    p_atm = 101325 * 3.398928944382626e-14
+    pot, ens = pk.ELJPotentialEven(C_NE), pk.NPT(N, p_atm)
+    temp = pk.TempGrid(10.0, 40.0, R)
+
+    def form(precision, seed):
+        mp = pk.MCParams(mc_cycles=6000, eq_cycles=3000, mc_sample=1, n_traj=R, n_atoms=N)
+        eng = pk.Engine(mp, temp, pot, ens, n_runs=n_runs, precision=precision, exch_prob=1.0,
+                        seed=seed, resync_every=1000)
+        for r in range(n_runs):
+            eng.set_configs(r, pk.Config(S.fcc_box(2, 8.4, 0.05, 500 + r), pk.CubicBC(16.8)))
+        eng.init()
+        eng.equilibrate()
+        eng.run_cycles(6000)
+        cp = np.array([pk.multihistogram_NPT(ens, temp, eng.output(r), 1e-4)[1] for r in range(n_runs)])
+        eng.close()
+        return cp
+
+    compare(form("fp64", 41), form("fp32", 42), "Ne32 NPT FP32+resync (Cp)")
 
 
 def test_cv_nn13_delayed_acceptance_vs_fp64(pk):
