@@ -85,7 +85,7 @@ function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential,
     npt = ensemble isa NPT
     p = PTMCParams(1, R, mc_params.mc_cycles, mc_params.eq_cycles, mc_params.mc_sample,
                    mc_params.n_adjust, mc_params.n_bin, mc_params.min_acc, mc_params.max_acc,
-                   npt ? 1 : 0, npt ? ensemble.pressure : 0.0,
+                   npt ? 1 : (ensemble isa NNVT ? 2 : 0), npt ? ensemble.pressure : 0.0,
                    first(temp.t_grid), last(temp.t_grid), 0, exch_prob,
                    precision == :fp64 ? 0 : 1, resync_every, UInt64(seed), 0, 0)
     ctx = Ref{Ptr{Cvoid}}(C_NULL)
@@ -96,6 +96,41 @@ function ptmc_run!(mc_params::MCParams, temp::TempGrid, start_config, potential,
             coeff = collect(Float64, potential.coeff)
             check(ccall((:ptmc_set_potential_elj, libptmc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Cint),
                         c, coeff, length(coeff), potential isa ELJPotentialEven), c)
+        elseif potential isa RuNNerPotential
+            # sf rows {kind, type, eta, lambda, zeta, r_cut, G_min, G_max}: the structs keep
+            # G_norm = 1/(max-min), G_offset = -min G_norm, tpz = 2^(1-zeta) G_norm
+            rows = Float64[]
+            for f in potential.radsymfunctions
+                gmin = -f.G_offset / f.G_norm
+                append!(rows, [0, f.type_vec, f.eta, 0, 0, f.r_cut, gmin, gmin + 1 / f.G_norm])
+            end
+            for f in potential.angsymfunctions
+                gnorm = f.tpz / 2.0^(1 - f.zeta)
+                gmin = -f.G_offset / gnorm
+                append!(rows, [1, f.type_vec, f.eta, f.lambda, f.zeta, f.r_cut, gmin, gmin + 1 / gnorm])
+            end
+            nnp = potential.nnp  # parameters: per layer W[n_in][n_out] then b[n_out]
+            nodes = Cint.(nnp.num_nodes)
+            check(ccall((:ptmc_set_potential_nn, libptmc), Cint,
+                        (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cint}, Cint, Cdouble),
+                        c, rows, length(rows) ÷ 8, nnp.parameters, length(nnp.parameters), nodes,
+                        length(nodes), sqrt(potential.boundary)), c)
+        elseif potential isa RuNNerPotential2Atom
+            # RadialType2a / AngularType3a fields as they are
+            rad = reduce(vcat, [[f.eta, f.r_cut, f.G_offset..., f.G_norm...] for f in potential.radsymfunctions])
+            ang = isempty(potential.angsymfunctions) ? Float64[] :
+                  reduce(vcat, [[f.eta, f.lambda, f.zeta, f.r_cut, f.tpz..., f.G_offset...]
+                                for f in potential.angsymfunctions])
+            nodes = Cint.(potential.nnp1.num_nodes)
+            n1 = typeof(potential).parameters[3]
+            check(ccall((:ptmc_set_potential_nn2, libptmc), Cint,
+                        (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Ptr{Cdouble},
+                         Cint, Ptr{Cint}, Cint, Cint),
+                        c, rad, length(potential.radsymfunctions), ang, length(potential.angsymfunctions),
+                        potential.nnp1.parameters, potential.nnp2.parameters,
+                        length(potential.nnp1.parameters), nodes, length(nodes), n1), c)
+            ensemble isa NNVT && check(ccall((:ptmc_set_atom_swaps, libptmc), Cint, (Ptr{Cvoid}, Cint),
+                                             c, ensemble.n_atom_swaps), c)
         elseif potential isa ELJPotentialB
             a, b, cc = (collect(Float64, v) for v in (potential.coeff_a, potential.coeff_b, potential.coeff_c))
             check(ccall((:ptmc_set_potential_eljb, libptmc), Cint,
