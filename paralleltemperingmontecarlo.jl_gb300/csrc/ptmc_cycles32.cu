@@ -137,6 +137,17 @@ __device__ double lrc64(int N, double rc2, const double* c, int K) {
   return e;
 }
 
+// lrc64 in FP32 (the correction is ~1e-2 of the energy, its FP32 rounding far
+// below the FP32 pair sum's): pi N^2 / 4 rc^-6 sum_i c_i rc^(-2i) / (2i + 3),
+// zero for r_c^2 <= 50 as in the FP64 form
+__device__ float lrc32(int N, double rc2, const float* c, int K) {
+  if (rc2 <= 50) return 0.f;
+  const float ir2 = 1.f / (float)rc2;
+  float e = 0.f;
+  for (int i = K - 1; i >= 0; --i) e = fmaf(e, ir2, c[i] / (float)(2 * i + 3));
+  return e * (ir2 * ir2 * ir2) * (3.14159265f * (float)(N * N) * 0.25f);
+}
+
 template <int BC>
 __device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
   float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
@@ -154,6 +165,14 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
   float l = lo + err;
   hi = s + l;
   lo = l - (hi - s);
+}
+// (hi, lo) *= s: the exact product hi s (its rounding error by FMA) plus lo s,
+// renormalised by a fast two-sum (|hi s| >= |lo s + err|)
+__device__ __forceinline__ void ff_scale(float& hi, float& lo, float s) {
+  const float p = hi * s;
+  const float q = fmaf(lo, s, fmaf(hi, s, -p));
+  hi = p + q;
+  lo = q - (hi - p);
 }
 // uniform in [0, 1) from the top 23 bits of a Philox word
 __device__ __forceinline__ float u01f(uint32_t w) {
@@ -353,8 +372,16 @@ __global__ void __launch_bounds__(1024)
   const float hnf = P.f_hn, hmf = P.f_hm, ecamf = P.f_ecam;
   const float ean2f = 2.f * P.f_ean, necamf = -P.f_ecam;
   const uint32_t run_word = (uint32_t)rdp->run_id;
-  float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
-  float Llo = (float)(L - (double)Lf);
+  const float pressf = (float)P.pressure;
+  float Lf, iLf, Llo, rcf = (float)rc2;
+  // the FP32 box: nearest float, its remainder, correctly rounded reciprocal
+  auto set_box = [&](double Lnew) {
+    L = Lnew;
+    Lf = (float)L;
+    Llo = (float)(L - (double)Lf);
+    iLf = __frcp_rn(Lf);
+  };
+  set_box(L);
 
   auto refill = [&]() {
     __syncwarp(gmask);
@@ -429,7 +456,7 @@ __global__ void __launch_bounds__(1024)
     } else {  // periodic wrap t -= L * round(t / L)
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float m = rintf(th[k] * iLf);
+        float m = rint_mul(th[k], iLf);
         if (m != 0.f) {
           ff_add(th[k], tl[k], -m * Lf);
           ff_add(th[k], tl[k], -m * Llo);
@@ -469,9 +496,10 @@ __global__ void __launch_bounds__(1024)
         float4 b = Xh[j];
         float dn = pf2<BC>(tf, b, Lf, iLf);
         float dol = pf2<BC>(x4, b, Lf, iLf);
-        if (ENS == ENS_NPT) {
-          if (!self && dn <= rcf) de += v32p<POT>(P, s_cf, K, dn);
-          if (!self && dol <= rcf) de -= v32p<POT>(P, s_cf, K, dol);
+        if (ENS == ENS_NPT) {  // the cutoff as selects, not branches
+          const float vn = v32p<POT>(P, s_cf, K, dn), vo = v32p<POT>(P, s_cf, K, dol);
+          const float t = (dn <= rcf ? vn : 0.f) - (dol <= rcf ? vo : 0.f);
+          de += self ? 0.f : t;
         } else {
           const float t = v32p<POT>(P, s_cf, K, dn) - v32p<POT>(P, s_cf, K, dol);
           de += self ? 0.f : t;
@@ -506,47 +534,64 @@ __global__ void __launch_bounds__(1024)
   };
 
   // ---------------------------------------------------------- volume move
-  auto volume_move = [&](double beta, double mdv, double maxbox) -> int {
-    double u = (double)u01f(word());
-    double scale = pow(exp((u - 0.5) * mdv), 1.0 / 3.0);
-    if (L >= maxbox && scale > 1.0) scale = 1.0;
-    double Ln = scale * L;
-    double rcn = Ln * Ln / 4;
-    const float s2 = (float)(scale * scale), rcnf = (float)rcn;
+  // volume_change (src/MCMoves.jl), every step but the box length and the
+  // energy total in FP32: the drawn ln(V_new / V_old) = (u - 1/2) max_vchange
+  // enters the acceptance as is (N log(V_new / V_old) needs no log), the scale
+  // is its cube root, the pair sum is FP32 with Kahan compensation reduced as
+  // float-float, and the accepted rescale of the float-float positions is an
+  // exact-product step.  GB300 issues FP64 at 1/64 of the FP32 rate, and a
+  // walker's volume moves (Binomial(N + 1, 1 / (N + 1)) of them in a cycle)
+  // would otherwise hold the whole CTA at the end-of-cycle barrier.
+  auto volume_move = [&](float beta_l2e, float mdvf, double maxbox) -> int {
+    float lnv = (u01f(word()) - 0.5f) * mdvf;  // ln(V_new / V_old)
+    float scale = expf(lnv * (1.f / 3.f));
+    if (L >= maxbox && scale > 1.f) {
+      scale = 1.f;
+      lnv = 0.f;
+    }
+    const double Ln = L * (double)scale;
+    const double rcn = Ln * Ln * 0.25;
+    const float s2 = scale * scale, rcnf = (float)rcn;
     float acc = 0.f, comp = 0.f;  // Kahan-compensated lane sum
     for (int i = 0; i < N; ++i) {
       float4 a = Xh[i];
       for (int j = i + 1 + lane; j < N; j += LPR) {
-        float x = pf2<BC>(a, Xh[j], Lf, iLf) * s2;
-        if (x <= rcnf) {
-          float y = v32<POT>(s_cf, K, x) - comp;
-          float tt = acc + y;
-          comp = (tt - acc) - y;
-          acc = tt;
-        }
+        const float x = pf2<BC>(a, Xh[j], Lf, iLf) * s2;
+        const float v = v32p<POT>(P, s_cf, K, x);
+        const float y = (x <= rcnf ? v : 0.f) - comp;
+        const float tt = acc + y;
+        comp = (tt - acc) - y;
+        acc = tt;
       }
     }
-    double e = seg_sum<LPR>((double)acc - (double)comp, gmask) + lrc64(N, rcn, s_c, K);
-    double Vn = Ln * Ln * Ln, Vo = L * L * L;
-    double dh = (e - en) + P.pressure * (Vn - Vo);
-    double prob = exp(-dh * beta + (double)N * log(Vn / Vo));
-    double ua = (double)u01f(word());
-    if (!(prob >= ua)) return 0;
+    float hi = acc, lo = -comp;
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {  // float-float sum; every lane ends with the same pair
+      const float oh = __shfl_xor_sync(gmask, hi, o), ol = __shfl_xor_sync(gmask, lo, o);
+      const float s = hi + oh, bb = s - hi;
+      const float err = (hi - (s - bb)) + (oh - bb);  // two-sum: exact in either operand order
+      lo = (lo + ol) + err;
+      hi = s + lo;
+      lo = lo - (hi - s);
+    }
+    const double e = ((double)hi + (double)lo) + (double)lrc32(N, rcn, s_cf, K);
+    const float vof = Lf * Lf * Lf;
+    const float dh = (float)(e - en) + pressf * vof * expm1f(lnv);
+    const float ua = u01f(word());
+    if (!(ex2f(fmaf(-dh, beta_l2e, (float)N * lnv * 1.4426950408889634f)) >= ua)) return 0;
     __syncwarp(gmask);
     for (int a = lane; a < N; a += LPR) {
-      double x = ((double)Xh[a].x + Xl[a].x) * scale, y = ((double)Xh[a].y + Xl[a].y) * scale,
-             z = ((double)Xh[a].z + Xl[a].z) * scale;
-      float4 h = make_float4((float)x, (float)y, (float)z, Xh[a].w);
+      float4 h = Xh[a], l = Xl[a];
+      ff_scale(h.x, l.x, scale);
+      ff_scale(h.y, l.y, scale);
+      ff_scale(h.z, l.z, scale);
       Xh[a] = h;
-      Xl[a] = make_float4((float)(x - h.x), (float)(y - h.y), (float)(z - h.z), 0.f);
+      Xl[a] = make_float4(l.x, l.y, l.z, 0.f);
     }
-    L = Ln;
+    set_box(Ln);
     rc2 = rcn;
+    rcf = rcnf;
     en = e;
-    Lf = (float)L;
-    Llo = (float)(L - (double)Lf);
-    iLf = (float)(1.0 / L);
-    rcf = (float)rc2;
     __syncwarp(gmask);
     return 1;
   };
@@ -557,8 +602,7 @@ __global__ void __launch_bounds__(1024)
   for (int cyc = 0; cyc < ncycles; ++cyc) {
     const long long idx = first + cyc;
     const int slot = s_sow[w];
-    const double beta = s_beta[slot];
-    const double mdv = s_maxd[2 * slot + 1];
+    const float mdvf = (float)s_maxd[2 * slot + 1];
     const double maxbox = s_maxbox[slot];
     const float beta_l2e = s_bl2e[slot];
     const float mdf = s_mdf[slot], mdc = s_mdc[slot];
@@ -573,7 +617,7 @@ __global__ void __launch_bounds__(1024)
         } else {
           en += (double)de_acc;  // fold the FP32 sum before the FP64 enthalpy
           de_acc = 0.f;
-          acc_v += volume_move(beta, mdv, maxbox);
+          acc_v += volume_move(beta_l2e, mdvf, maxbox);
         }
         if (status != ST_OK) break;
       }

@@ -108,12 +108,23 @@ __device__ __forceinline__ double d2_rhb(double ax, double ay, double az,
   return dot3(dsub(ax, ix), dsub(ay, iy), dsub(az, iz));
 }
 
-// FP32 minimum image for the FP32 form
+// rintf(x * y) for |x * y| < 2^22 on the FMA pipes: adding and subtracting
+// 1.5 * 2^23 rounds to the nearest integer, ties to even (the spacing of
+// floats in [2^23, 2^24) is 1), as rintf does; the product is rounded first,
+// as in rintf(x * y), and the _rn forms keep the three steps from being
+// contracted.  rintf is an XU-pipe instruction whose result waits on the
+// short scoreboard.
+__device__ __forceinline__ float rint_mul(float x, float y) {
+  constexpr float M = 12582912.f;  // 1.5 * 2^23
+  return __fadd_rn(__fadd_rn(__fmul_rn(x, y), M), -M);
+}
+// FP32 minimum image for the FP32 form (coordinate differences within 2^22
+// box lengths)
 __device__ __forceinline__ float f2_cub(float dx, float dy, float dz, float L,
                                         float iL) {
-  dx -= L * rintf(dx * iL);
-  dy -= L * rintf(dy * iL);
-  dz -= L * rintf(dz * iL);
+  dx -= L * rint_mul(dx, iL);
+  dy -= L * rint_mul(dy, iL);
+  dz -= L * rint_mul(dz, iL);
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 

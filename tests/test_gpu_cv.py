@@ -69,6 +69,8 @@ def compare(cv_ref, cv_x, label):
     dev = np.abs(m_x - m_ref)
     print("%s: max |dCv|/sigma_fp64 = %.3f, max z = %.3f, peak Cv %.4g vs %.4g" % (
         label, np.max(dev / sig), np.max(dev / se), m_x.max(), m_ref.max()))
+    with np.printoptions(precision=4, linewidth=200):
+        print("per-run Cv, reference form:\n", cv_ref, "\nper-run Cv, tested form:\n", cv_x)
     assert np.all(dev <= 2 * sig), (label, np.max(dev / sig))
     assert np.all(dev <= 5 * se), (label, np.max(dev / se))
 
