@@ -233,6 +233,8 @@ int check_status(ptmc_ctx* c) {
       return c->fail(PTMC_ERR_SPHERE, "Error: too many moves out of binding sphere");
     if (st[i] == ST_TIMEOUT)
       return c->fail(PTMC_ERR_CUDA, "a tensor-core completion wait ran out (surrogate stage)");
+    if (st[i] == ST_XWAIT)
+      return c->fail(PTMC_ERR_CUDA, "a wait for an exchange partner ran out (FP32 cycle kernel)");
   }
   return PTMC_OK;
 }

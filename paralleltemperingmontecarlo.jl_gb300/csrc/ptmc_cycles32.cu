@@ -52,27 +52,12 @@ constexpr uint32_t DRW32 = 128;
 
 namespace {
 
-__device__ __forceinline__ float v_even32(const float* c, int K, float r2) {
-  float inv = rcpf(r2);
-  float v = c[K - 1];
-  for (int k = K - 2; k >= 0; --k) v = fmaf(v, inv, c[k]);
-  return v * (inv * inv * inv);
-}
-__device__ __forceinline__ float v_all32(const float* c, int K, float r2) {
-  float ir = rsqrtf(r2);
-  float inv = ir * ir;
-  float v = c[K - 1];
-  for (int k = K - 2; k >= 0; --k) v = fmaf(v, ir, c[k]);
-  return v * (inv * inv * inv);
-}
-template <int POT>
-__device__ __forceinline__ float v32(const float* c, int K, float r2) {
-  return POT == POT_ELJ ? v_all32(c, K, r2) : v_even32(c, K, r2);
-}
-// Same polynomial with the coefficients read as kernel-parameter (constant
-// bank) operands and the Horner recurrence unrolled for the coefficient count
-// KK: no shared-memory loads and no loop overhead per pair term (a runtime-K
-// loop over shared-memory coefficients costs ~5 instructions per term).
+// ELJ pair energy in FP32: sum_k c_k x^k times r^-6, x = 1/r (ELJPotential)
+// or 1/r^2 (ELJPotentialEven), with the coefficients read as kernel-parameter
+// (constant bank) operands and the Horner recurrence unrolled for the
+// coefficient count KK: no shared-memory loads and no loop overhead per pair
+// term (a runtime-K loop over shared-memory coefficients costs ~5
+// instructions per term).
 template <int KK>
 __device__ __forceinline__ float horner_p(const KParams& P, float x) {
   float v = P.cf[KK - 1];
@@ -146,6 +131,35 @@ __device__ float lrc32(int N, double rc2, const float* c, int K) {
   float e = 0.f;
   for (int i = K - 1; i >= 0; --i) e = fmaf(e, ir2, c[i] / (float)(2 * i + 3));
   return e * (ir2 * ir2 * ir2) * (3.14159265f * (float)(N * N) * 0.25f);
+}
+
+// min(1, exp((beta_k - beta_k+1) (H_1 - H_2))), H = E + p L^3 (p = 0: NVT),
+// every operation rounded as written: both cycle-end forms of k_cycles32
+// evaluate it alike, whatever the compiler contracts elsewhere
+__device__ __forceinline__ double exch_acc(double bk, double bk1, double e1, double e2, double L1,
+                                           double L2, double p) {
+  if (p != 0.0) {
+    e1 = __dadd_rn(e1, __dmul_rn(p, __dmul_rn(__dmul_rn(L1, L1), L1)));
+    e2 = __dadd_rn(e2, __dmul_rn(p, __dmul_rn(__dmul_rn(L2, L2), L2)));
+  }
+  const double a = exp(__dmul_rn(__dadd_rn(bk, -bk1), __dadd_rn(e1, -e2)));
+  return a > 1.0 ? 1.0 : a;
+}
+
+// waits until *f >= v (a flag in shared memory written by another warp of the
+// CTA); false after ~2^33 clocks, or at once when another walker of the CTA
+// gave up (which then ends every other wait)
+__device__ bool wait_flag(const int* f, int v, int* abort_flag) {
+  const long long t0 = clock64();
+  while (*(const volatile int*)f < v) {
+    if (*(volatile int*)abort_flag) return false;
+    if (clock64() - t0 > (1ll << 33)) {
+      *(volatile int*)abort_flag = 1;
+      return false;
+    }
+    __nanosleep(64);
+  }
+  return true;
 }
 
 template <int BC>
@@ -596,12 +610,75 @@ __global__ void __launch_bounds__(1024)
     return 1;
   };
 
+  // ---------------------------------------------------------- cycle end
+  // update_max_stepsize! and sampling_step! of slot s, whose walker ended the
+  // cycle with energy e in a box of length Lw (one thread per slot)
+  auto slot_epilogue = [&](int s, long long idx, double e, double Lw) {
+    if (idx % P.n_adjust == 0) {  // update_max_stepsize!
+      double acc = (double)s_cnt[6 * s + 1] / (double)((long long)P.n_adjust * N);
+      if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
+      else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
+      s_mdf[s] = (float)s_maxd[2 * s];
+      s_mdc[s] = (float)(s_maxd[2 * s] * (1.5 - 0x1.0p-24));
+      s_cnt[6 * s + 1] = 0;
+      if (ENS == ENS_NPT) {
+        double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);
+        if (av < P.min_acc) s_maxd[2 * s + 1] *= 0.9;
+        else if (av > P.max_acc) s_maxd[2 * s + 1] *= 1.1;
+        s_cnt[6 * s + 3] = 0;
+      }
+    }
+    if (phase == PHASE_PROD && idx % P.mc_sample == 0) {  // sampling_step!
+      const int nb = P.n_bin;
+      unsigned int* hrow = P.hist + rdp->hist_off + (size_t)s * rdp->hist_stride;
+      auto hidx = [&](double h) -> int {
+        if (!(h >= 1)) return 1;
+        if (h > nb) return nb + 2;
+        return (int)floor(h) + 1;
+      };
+      if (ENS == ENS_NPT) {
+        double V = Lw * Lw * Lw;
+        double H = e + P.pressure * V;
+        s_ham[2 * s] += H;
+        s_ham[2 * s + 1] += H * H;
+        int ie = hidx(floor((e - rdp->en_min) / rdp->dE) + 1);
+        int iv = hidx(floor((V - rdp->v_min) / rdp->dV) + 1);
+        if (q == 0) atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
+      } else {
+        s_ham[2 * s] += e;
+        s_ham[2 * s + 1] += e * e;
+        int ie = hidx((e - rdp->en_min) / rdp->dE + 1);
+        if (q == 0) atomicAdd(hrow + (ie - 1), 1u);
+      }
+    }
+  };
+
+  // Handshake form (one CTA per run, a warp per walker): no CTA barrier per
+  // cycle.  The exchange draws do not depend on the walkers, so every walker
+  // draws them; only the two walkers of the drawn pair (k, k + 1) wait for
+  // each other, through per-slot records (energy, box, a flag = 2 cyc + 1 when
+  // written, 2 cyc + 2 once the partner's record has been read).  Slot s's
+  // counters, step sizes and sums are only touched by the walker holding s or
+  // by its partner in the exchange that hands s over, in cycle order, so the
+  // results are those of the barrier form bit for bit.
+  constexpr bool HANDSHAKE = !SPLIT && LPR == 32;
+  double* s_xen = s_en;              // slot records (the barrier form's per-walker arrays)
+  double* s_xbox = s_box;
+  int* s_xflag = (int*)s_acc;
+  __shared__ int s_abort;            // a partner wait ran out: the others stop waiting
+  if (HANDSHAKE) {
+    for (int s = tid; s < R; s += nthr) s_xflag[s] = 0;
+    if (tid == 0) s_abort = 0;
+    __syncthreads();
+  }
+  int myslot = s_sow[w];
+
   // ---------------------------------------------------------- cycles
   const long long first = rdp->cyc[phase];
   unsigned long long run_ctr = rdp->run_ctr;
   for (int cyc = 0; cyc < ncycles; ++cyc) {
     const long long idx = first + cyc;
-    const int slot = s_sow[w];
+    const int slot = HANDSHAKE ? myslot : s_sow[w];
     const float mdvf = (float)s_maxd[2 * slot + 1];
     const double maxbox = s_maxbox[slot];
     const float beta_l2e = s_bl2e[slot];
@@ -631,113 +708,120 @@ __global__ void __launch_bounds__(1024)
         __syncwarp(gmask);
       }
     }
-    if (lane == 0) {
-      s_en[w] = en;
-      s_box[w] = L;
-      s_acc[w] = make_int2((int)acc_a, (int)acc_v);
-    }
-    if constexpr (SPLIT) {  // gather the other CTAs' walkers through distributed shared memory
-      cg::cluster_group cl = cg::this_cluster();
-      cl.sync();
-      for (int v = tid; v < R; v += nthr) {
-        const int owner = v / Rl;
-        if (owner != q) {
-          s_en[v] = *cl.map_shared_rank(s_en + v, owner);
-          s_box[v] = *cl.map_shared_rank(s_box + v, owner);
-          s_acc[v] = *cl.map_shared_rank(s_acc + v, owner);
+    if constexpr (HANDSHAKE) {
+      if (lane == 0) {  // this cycle's moves were made in slot myslot
+        s_cnt[6 * myslot + 0] += acc_a;
+        s_cnt[6 * myslot + 1] += acc_a;
+        s_cnt[6 * myslot + 2] += acc_v;
+        s_cnt[6 * myslot + 3] += acc_v;
+      }
+      int k = -1;  // parallel_tempering_exchange! (src/Exchange.jl:132-180): the pair (k, k + 1)
+      double ux = 0.0;
+      if (R > 1) {
+        double u = philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++);
+        if (u < P.exch_prob) {
+          k = randint(philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++), R - 1);
+          ux = philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++);
         }
       }
-      cl.sync();  // every remote read is done before any CTA writes its next results
+      if (k >= 0 && (myslot == k || myslot == k + 1)) {
+        const int other = myslot == k ? k + 1 : k;
+        const int tag = 2 * cyc + 1;
+        if (lane == 0) {
+          s_xen[myslot] = en;
+          s_xbox[myslot] = L;
+          __threadfence_block();
+          *(volatile int*)(s_xflag + myslot) = tag;
+        }
+        __syncwarp();
+        bool ok = wait_flag(s_xflag + other, tag, &s_abort);
+        __threadfence_block();
+        const double eo = *(volatile double*)(s_xen + other), Lo = *(volatile double*)(s_xbox + other);
+        __syncwarp();  // every lane has read the partner's record
+        if (lane == 0) *(volatile int*)(s_xflag + myslot) = tag + 1;
+        ok = wait_flag(s_xflag + other, tag + 1, &s_abort) && ok;
+        if (!ok) status = ST_XWAIT;
+        const bool lo_side = myslot == k;
+        const double p = exch_acc(s_beta[k], s_beta[k + 1], lo_side ? en : eo, lo_side ? eo : en,
+                                  lo_side ? L : Lo, lo_side ? Lo : L, ENS == ENS_NPT ? P.pressure : 0.0);
+        const bool swap = p > ux;
+        if (swap) myslot = other;
+        if (lane == 0) {
+          s_cnt[6 * myslot + 4] += 1;
+          if (swap) s_cnt[6 * myslot + 5] += 1;
+        }
+      }
+      if (lane == 0) {
+        s_sow[w] = myslot;
+        s_wos[myslot] = w;
+        slot_epilogue(myslot, idx, en, L);
+      }
+      __syncwarp();
     } else {
+      if (lane == 0) {
+        s_en[w] = en;
+        s_box[w] = L;
+        s_acc[w] = make_int2((int)acc_a, (int)acc_v);
+      }
+      if constexpr (SPLIT) {  // gather the other CTAs' walkers through distributed shared memory
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        for (int v = tid; v < R; v += nthr) {
+          const int owner = v / Rl;
+          if (owner != q) {
+            s_en[v] = *cl.map_shared_rank(s_en + v, owner);
+            s_box[v] = *cl.map_shared_rank(s_box + v, owner);
+            s_acc[v] = *cl.map_shared_rank(s_acc + v, owner);
+          }
+        }
+        cl.sync();  // every remote read is done before any CTA writes its next results
+      } else {
+        __syncthreads();
+      }
+      for (int v = tid; v < R; v += nthr) {  // counters of the slot each walker occupied
+        const int sl = s_sow[v];
+        const int2 a = s_acc[v];
+        s_cnt[6 * sl + 0] += a.x;
+        s_cnt[6 * sl + 1] += a.x;
+        s_cnt[6 * sl + 2] += a.y;
+        s_cnt[6 * sl + 3] += a.y;
+      }
+      __syncthreads();
+      if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
+        double u = philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++);
+        if (u < P.exch_prob) {
+          int k = randint(philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++), R - 1);
+          s_cnt[6 * k + 4] += 1;
+          s_cnt[6 * (k + 1) + 4] += 1;
+          int w1 = s_wos[k], w2 = s_wos[k + 1];
+          double acc = exch_acc(s_beta[k], s_beta[k + 1], s_en[w1], s_en[w2], s_box[w1], s_box[w2],
+                                ENS == ENS_NPT ? P.pressure : 0.0);
+          if (acc > philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++)) {
+            s_cnt[6 * k + 5] += 1;
+            s_cnt[6 * (k + 1) + 5] += 1;
+            s_wos[k] = w2;
+            s_wos[k + 1] = w1;
+            s_sow[w2] = k;
+            s_sow[w1] = k + 1;
+          }
+        }
+      }
+      __syncthreads();
+      if (tid < R) {
+        const int wk = s_wos[tid];
+        slot_epilogue(tid, idx, s_en[wk], s_box[wk]);
+      }
       __syncthreads();
     }
-    for (int v = tid; v < R; v += nthr) {  // counters of the slot each walker occupied
-      const int sl = s_sow[v];
-      const int2 a = s_acc[v];
-      s_cnt[6 * sl + 0] += a.x;
-      s_cnt[6 * sl + 1] += a.x;
-      s_cnt[6 * sl + 2] += a.y;
-      s_cnt[6 * sl + 3] += a.y;
-    }
-    __syncthreads();
-    if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
-      double u = philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++);
-      if (u < P.exch_prob) {
-        int k = randint(philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++), R - 1);
-        s_cnt[6 * k + 4] += 1;
-        s_cnt[6 * (k + 1) + 4] += 1;
-        int w1 = s_wos[k], w2 = s_wos[k + 1];
-        double e1 = s_en[w1], e2 = s_en[w2];
-        if (ENS == ENS_NPT) {
-          double L1 = s_box[w1], L2 = s_box[w2];
-          e1 += P.pressure * (L1 * L1 * L1);
-          e2 += P.pressure * (L2 * L2 * L2);
-        }
-        double acc = exp((s_beta[k] - s_beta[k + 1]) * (e1 - e2));
-        if (acc > 1.0) acc = 1.0;
-        if (acc > philox_u01(P.seed, 0xFFFFFFFFu, run_word, run_ctr++)) {
-          s_cnt[6 * k + 5] += 1;
-          s_cnt[6 * (k + 1) + 5] += 1;
-          s_wos[k] = w2;
-          s_wos[k + 1] = w1;
-          s_sow[w2] = k;
-          s_sow[w1] = k + 1;
-        }
-      }
-    }
-    __syncthreads();
-    if (tid < R) {
-      const int s = tid;
-      if (idx % P.n_adjust == 0) {  // update_max_stepsize!
-        double acc = (double)s_cnt[6 * s + 1] / (double)((long long)P.n_adjust * N);
-        if (acc < P.min_acc) s_maxd[2 * s] *= 0.9;
-        else if (acc > P.max_acc) s_maxd[2 * s] *= 1.1;
-        s_mdf[s] = (float)s_maxd[2 * s];
-        s_mdc[s] = (float)(s_maxd[2 * s] * (1.5 - 0x1.0p-24));
-        s_cnt[6 * s + 1] = 0;
-        if (ENS == ENS_NPT) {
-          double av = (double)s_cnt[6 * s + 3] / (double)(P.n_adjust * 1);
-          if (av < P.min_acc) s_maxd[2 * s + 1] *= 0.9;
-          else if (av > P.max_acc) s_maxd[2 * s + 1] *= 1.1;
-          s_cnt[6 * s + 3] = 0;
-        }
-      }
-      if (phase == PHASE_PROD && idx % P.mc_sample == 0) {  // sampling_step!
-        const int wk = s_wos[s];
-        const double e = s_en[wk];
-        const int nb = P.n_bin;
-        unsigned int* hrow = P.hist + rdp->hist_off + (size_t)s * rdp->hist_stride;
-        auto hidx = [&](double h) -> int {
-          if (!(h >= 1)) return 1;
-          if (h > nb) return nb + 2;
-          return (int)floor(h) + 1;
-        };
-        if (ENS == ENS_NPT) {
-          double Lw = s_box[wk];
-          double V = Lw * Lw * Lw;
-          double H = e + P.pressure * V;
-          s_ham[2 * s] += H;
-          s_ham[2 * s + 1] += H * H;
-          int ie = hidx(floor((e - rdp->en_min) / rdp->dE) + 1);
-          int iv = hidx(floor((V - rdp->v_min) / rdp->dV) + 1);
-          if (q == 0) atomicAdd(hrow + (size_t)(ie - 1) * (nb + 2) + (iv - 1), 1u);
-        } else {
-          s_ham[2 * s] += e;
-          s_ham[2 * s + 1] += e * e;
-          int ie = hidx((e - rdp->en_min) / rdp->dE + 1);
-          if (q == 0) atomicAdd(hrow + (ie - 1), 1u);
-        }
-      }
-    }
-    __syncthreads();
     if (P.rdf && phase == PHASE_PROD && idx % P.mc_sample == 0 && idx % RDF_EVERY == 0) {
       // update_rdf! (src/Sampling.jl:301-316) from the FP32 positions
-      unsigned int* row = P.rdf + (size_t)(wk0 + s_sow[w]) * 5 * P.n_bin;
+      unsigned int* row = P.rdf + (size_t)(wk0 + (HANDSHAKE ? myslot : s_sow[w])) * 5 * P.n_bin;
       for (int i = 1; i < N; ++i)
         for (int k = lane; k < i; k += LPR)
           rdf_add(row, 5 * P.n_bin, (double)pf2<BC>(Xh[i], Xh[k], Lf, iLf), rdp->dr2);
     }
   }
+  if (HANDSHAKE) __syncthreads();  // every walker has finished its cycles and slot updates
 
   double* gpos_w = P.pos + rdp->pos_off + (size_t)q * Rl * N * 3;
   for (int k = tid; k < Rl * N; k += nthr) {

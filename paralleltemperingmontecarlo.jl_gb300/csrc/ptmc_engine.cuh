@@ -29,7 +29,9 @@ __host__ __device__ constexpr bool pot_b(int pot) { return pot == POT_ELJB || po
 enum { BC_SPH = 0, BC_CUB = 1, BC_RECT = 2, BC_RHB = 3 };  // RECT/RHB: length L, height H
 enum { ENS_NVT = 0, ENS_NPT = 1 };
 enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
-enum { ST_OK = 0, ST_SPHERE = 1, ST_TIMEOUT = 2 };  // TIMEOUT: a bounded tensor-core wait ran out
+// TIMEOUT: a bounded tensor-core wait ran out; XWAIT: a bounded wait for an
+// exchange partner ran out
+enum { ST_OK = 0, ST_SPHERE = 1, ST_TIMEOUT = 2, ST_XWAIT = 3 };
 constexpr int MAX_COEFF = 16;
 constexpr int MAX_REPLICAS = 32;
 constexpr int DRAW_BUF = 16;

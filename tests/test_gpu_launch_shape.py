@@ -50,8 +50,11 @@ def protocol(eng):
     return snapshot(eng)
 
 
-@pytest.mark.parametrize("ctas", [2, 4, 8])
-def test_cluster_split_ne13_bit_identical(pk, ctas):
+@pytest.mark.parametrize("ctas,lanes", [(2, 32), (4, 32), (8, 32), (1, 16)])
+def test_cluster_split_ne13_bit_identical(pk, ctas, lanes):
+    """The default shape (one CTA per run, a warp per walker) ends a cycle with
+    the pairwise exchange handshake; clusters and half-warp walkers end it with
+    CTA (cluster) barriers: the chains must agree bit for bit."""
     import ptmc_gb300.starts as S
     starts = [S.sphere_start(13, 8.0, 4.5, 40 + r) for r in range(3)]
     args = (pk, pk.ELJPotentialEven(C_NE), pk.NVT(13), starts, pk.SphericalBC(11.0), 16, (4.0, 16.0), 5)
@@ -59,7 +62,7 @@ def test_cluster_split_ne13_bit_identical(pk, ctas):
     a = protocol(ref)
     ref.close()
     eng = engine(*args)
-    eng.set_launch_shape(13, ctas)
+    eng.set_launch_shape(13, ctas, lanes)
     b = protocol(eng)
     eng.close()
     assert_identical(a, b)
