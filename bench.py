@@ -78,7 +78,7 @@ def workload(name):
                     # warp instructions per attempted move of k_cycles32 (32 lanes per
                     # walker): smsp__inst_executed of the 16-run, 50-cycle launch over its
                     # 1.408 M moves (profiles/k_cycles32_cu55_eam.md)
-                    inst_per_move=315.9, lanes=32)
+                    inst_per_move=315.9, lanes=32, inst_src="profiles/k_cycles32_cu55_eam.md")
     if name == "ne13":
         return dict(name="ne13_eljeven", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
                     bc=("sphere", 11.0), sizes=lambda B: [13] * B,
@@ -88,7 +88,9 @@ def workload(name):
         return dict(name="ne108_npt", R=32, T=(10.0, 40.0), pot="elj", ens="npt",
                     bc=("cubic", 25.2), sizes=lambda B: [108] * B,
                     start=lambda n, k: fcc(3, 8.4, 0.05, 7 + k), resync=1000,
-                    flops_pair=33, mufu_pair=1)
+                    flops_pair=33, mufu_pair=1,
+                    # warp instructions per attempted move, volume moves included
+                    inst_per_move=717.9, lanes=32, inst_src="profiles/k_cycles32_ne108_npt.md")
     if name == "nn55":
         return dict(name="nn55_runner", R=64, T=(300.0, 900.0), pot="nn", ens="nvt",
                     bc=("sphere", 14.0), sizes=lambda B: [55] * B,
@@ -552,7 +554,7 @@ def issue_roof(W, ch, n_sm):
     peak = 4 * n_sm * mhz * 1e6 / 1e9
     return {"warp_inst_per_move": ipm, "achieved": achieved, "peak": peak, "unit": "G warp-inst/s",
             "frac": achieved / peak,
-            "source": "ncu smsp__inst_executed, profiles/k_cycles32_cu55_eam.md"}
+            "source": "ncu smsp__inst_executed, " + W["inst_src"]}
 
 
 if __name__ == "__main__":
