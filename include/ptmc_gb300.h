@@ -23,7 +23,8 @@ extern "C" {
 #define PTMC_OK 0
 #define PTMC_ERR_ARG -1      /* bad argument (ArgumentError in the reference) */
 #define PTMC_ERR_STATE -2    /* call out of order */
-#define PTMC_ERR_CUDA -3     /* CUDA failure or no GPU */
+#define PTMC_ERR_CUDA -3     /* CUDA failure or no GPU; also a bounded device wait that ran out
+                                (tensor-core completion, exchange partner): see ptmc_last_error */
 #define PTMC_ERR_SPHERE -4   /* "too many moves out of binding sphere" (src/MCMoves.jl:132) */
 #define PTMC_ERR_IO -5       /* checkpoint file error */
 #define PTMC_ERR_LIMIT -6    /* size beyond a documented limit */
