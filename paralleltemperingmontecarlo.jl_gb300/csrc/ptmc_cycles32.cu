@@ -21,9 +21,15 @@
 //    `resync_every` cycles each walker recomputes its energy (and EAM
 //    components) in FP64 from hi + lo and records the drift
 //    |E_running - E_fp64|.
-//  * NPT volume moves (rare: one slot in N+1) are evaluated with FP32 pair
-//    terms, Kahan-compensated per lane, FP64 across lanes and for the
-//    enthalpy, long-range correction and acceptance.
+//  * NPT volume moves (one step in N+1) are FP32 too: ln(V_new/V_old) as
+//    drawn, FP32 pair terms with Kahan-compensated lane sums reduced as
+//    float-float, FP32 tail correction and pV, the energy total in FP64, and an
+//    exact-product float-float rescale of accepted positions.
+//  * With one CTA per run and a warp per walker there is no CTA barrier per
+//    cycle: every walker draws the run's exchange decisions, and only the two
+//    walkers of the drawn pair wait for each other (bounded handshake through
+//    per-slot records in shared memory); results equal the barrier form's bit
+//    for bit.
 //  * A run may be split over a thread-block cluster of C CTAs (C SMs): CTA
 //    rank q holds walkers q*R/C .. (q+1)*R/C - 1.  After the moves of a cycle
 //    every CTA gathers all walkers' energies, boxes and acceptance counts
@@ -553,7 +559,7 @@ __global__ void __launch_bounds__(1024)
   // enters the acceptance as is (N log(V_new / V_old) needs no log), the scale
   // is its cube root, the pair sum is FP32 with Kahan compensation reduced as
   // float-float, and the accepted rescale of the float-float positions is an
-  // exact-product step.  GB300 issues FP64 at 1/64 of the FP32 rate, and a
+  // exact-product step.  GB300 runs FP64 at ~1/70 of the FP32 rate, and a
   // walker's volume moves (Binomial(N + 1, 1 / (N + 1)) of them in a cycle)
   // would otherwise hold the whole CTA at the end-of-cycle barrier.
   auto volume_move = [&](float beta_l2e, float mdvf, double maxbox) -> int {
