@@ -1,15 +1,25 @@
 """Throughput benchmark: attempted atom moves per second on one GB300.
 
-Default workload (the Cu55 EAM configuration): Sutton-Chen EAM Cu55
-(scripts/cu55.jl:39-48 parameters), icosahedral start, SphericalBC(14 bohr),
-32 replicas geometric over 200-1000 K, the chosen form = FP32 move rows with
-an FP64 running total resynchronised by a full FP64 recompute every 1000
-cycles, batched as B independent PT runs (different Philox streams) in one
-launch.  A step is `--cycles` MC cycles of every run (all walkers make N atom
-moves per cycle).  The plain FP64 form is timed on the same batch and reported
-as `plain_fp64`.
+Every default run measures the five workloads of the engine's configuration
+set on the production path (equilibration as the warm-up, then timed
+production cycles that sample E, E^2 and the histograms every cycle):
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload cu55|ne13|npt108|batched]
+  cu55     Sutton-Chen EAM Cu55 (scripts/cu55.jl:39-48 parameters), icosahedral
+           start, SphericalBC(14 bohr), 32 replicas over 200-1000 K   (headline)
+  ne13     ELJEven Ne13, sphere 11 bohr, 16 replicas over 4-16 K
+  npt108   bulk Ne NPT, 108 atoms fcc in CubicBC(25.2), 32 replicas over 10-40 K
+  batched  256 runs of ELJEven Ne clusters, N in {13, 38, 55, 101, 147}, 16 replicas
+  nn55     RuNNer NN potential on Cu55, 64 replicas over 300-900 K, delayed
+           acceptance with a GPU-trained pair surrogate
+
+The chosen form is FP32 move rows with an FP64 running total resynchronised by
+a full FP64 recompute every 1000 cycles, batched as B independent PT runs
+(different Philox streams) per launch with an autotuned launch shape per atom
+count; the plain FP64 form is timed on the same batch.  The line's `value`,
+`roofline`, `cpu_baseline` and `e2e` are the headline workload's; `workloads`
+holds one record per workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload all|cu55|ne13|npt108|batched|nn55]
   python bench.py --impl reference ...   # the CPU oracle on all host cores
 
 Under torchrun (N>1) every rank runs its own batch on its own GPU (replicas
@@ -18,6 +28,7 @@ only, weak scaling; no collective on the data path), timing is max over ranks.
 import argparse
 import ctypes
 import functools
+import hashlib
 import json
 import math
 import multiprocessing as mp
@@ -25,6 +36,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -37,6 +49,22 @@ C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668
         -56234083.4334278, 288738837.441765]
 CU_EAM = dict(n=8.482, m=4.692, eps=0.0367493 * 0.0370, C=27.561, a=0.25 * 18.8973)
 P_NE = 101325 * 3.398928944382626e-14
+HEADLINE = "cu55"
+ALL = ["cu55", "ne13", "npt108", "batched", "nn55"]
+METRIC = "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error"
+
+# Counters of the chosen form's cycle kernel from one ncu capture per workload
+# (smsp__inst_executed over the launch's attempted moves; DRAM read + write
+# bytes of the launch per run), valid for the kernel source whose sha256 prefix
+# is given: a changed kernel drops them from the line instead of reporting
+# stale figures.
+KERNEL_SRC = os.path.join(ROOT, "paralleltemperingmontecarlo.jl_gb300", "csrc", "ptmc_cycles32.cu")
+PROFILED = {}
+
+
+@functools.lru_cache(maxsize=1)
+def kernel_sha():
+    return hashlib.sha256(open(KERNEL_SRC, "rb").read()).hexdigest()[:16]
 
 
 # --------------------------------------------------------------- workloads
@@ -66,38 +94,33 @@ def _starts():
 
 
 def workload(name):
-    """(description, N list per run, R, T0, T1, potential kind, ensemble, bc, starts fn)."""
+    """Description of one workload: replicas, temperature range, potential,
+    ensemble, boundary, per-run atom counts and start configurations, chosen
+    and plain-form cycles per timed step, and the algorithmic FP32 work per
+    pair (SURVEY-style counts: ELJ 24 ops, +9 with the minimum image; EAM 17
+    ops + 3 MUFU)."""
     if name == "cu55":
         return dict(name="cu55_eam", R=32, T=(200.0, 1000.0), pot="eam", ens="nvt",
                     bc=("sphere", 14.0), sizes=lambda B: [55] * B,
                     start=lambda n, k: cu55_ico(), resync=1000, flops_pair=17, mufu_pair=3,
-                    # DRAM bytes (read + write) of one k_cycles32 launch per run: ncu capture
-                    # of a 16-run launch, 1.30 MB (profiles/k_cycles32_cu55_eam.md); the
-                    # state moved per launch grows with the runs
-                    dram_bytes_per_run=1.30e6 / 16,
-                    # warp instructions per attempted move of k_cycles32 (32 lanes per
-                    # walker): smsp__inst_executed of the 16-run, 50-cycle launch over its
-                    # 1.408 M moves (profiles/k_cycles32_cu55_eam.md)
-                    inst_per_move=315.9, lanes=32, inst_src="profiles/k_cycles32_cu55_eam.md")
+                    cycles=200, plain_cycles=20)
     if name == "ne13":
         return dict(name="ne13_eljeven", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
                     bc=("sphere", 11.0), sizes=lambda B: [13] * B,
                     start=lambda n, k: sphere_start(13, 8.0, 4.5, 1234 + k), resync=1000,
-                    flops_pair=24, mufu_pair=1)
+                    flops_pair=24, mufu_pair=1, cycles=200, plain_cycles=100)
     if name == "npt108":
         return dict(name="ne108_npt", R=32, T=(10.0, 40.0), pot="elj", ens="npt",
                     bc=("cubic", 25.2), sizes=lambda B: [108] * B,
                     start=lambda n, k: fcc(3, 8.4, 0.05, 7 + k), resync=1000,
-                    flops_pair=33, mufu_pair=1,
-                    # warp instructions per attempted move, volume moves included
-                    inst_per_move=717.9, lanes=32, inst_src="profiles/k_cycles32_ne108_npt.md")
+                    flops_pair=33, mufu_pair=1, cycles=200, plain_cycles=20)
     if name == "nn55":
         return dict(name="nn55_runner", R=64, T=(300.0, 900.0), pot="nn", ens="nvt",
                     bc=("sphere", 14.0), sizes=lambda B: [55] * B,
                     start=lambda n, k: cu55_ico(), resync=1000,
                     # per move: 74.4 k angular triple terms x ~30 ops + 239 k MLP flops
                     flops_move=74400 * 30 + 239000, flops_pair=0, mufu_pair=0,
-                    da=True, cycles=20)
+                    da=True, cycles=20, plain_cycles=2)
     if name == "batched":
         ns = [13, 38, 55, 101, 147]
 
@@ -106,7 +129,7 @@ def workload(name):
         return dict(name="batched_uneven_elj", R=16, T=(4.0, 16.0), pot="elj", ens="nvt",
                     bc=("sphere", None), sizes=sizes,
                     start=lambda n, k: sphere_start(n, 0.9 * n ** (1 / 3) * 3, 4.3, 500 + k),
-                    resync=1000, flops_pair=24, mufu_pair=1)
+                    resync=1000, flops_pair=24, mufu_pair=1, cycles=200, plain_cycles=20)
     raise SystemExit("unknown workload " + name)
 
 
@@ -126,11 +149,12 @@ def nn_potential(pk):
                               pk.RuNNerPotential.random_weights(nodes, 3, 0.3), nodes, boundary=3.0)
 
 
-def train_surrogate(pk, eng, sizes, R, cycles=300, capacity=40000, steps=4000):
-    """Delayed acceptance set-up (outside the timed region): capture moves of
-    the exact chain, train the pair surrogate on the GPU, freeze, enable."""
-    every = max(1, (cycles * sum(sizes) * R) // capacity)
-    eng.surrogate_set(pk.PairSurrogate(2.0, 12.0, None, 12.0, 0.0), capacity=capacity,
+def train_surrogate(pk, eng, sizes, R, cycles=300, records=100000, steps=4000):
+    """Delayed acceptance set-up (outside the timed region): capture `records`
+    (configuration row, exact dE) pairs of the exact chain over `cycles`
+    cycles, train the pair surrogate on the GPU, freeze, enable."""
+    every = max(1, (cycles * sum(sizes) * R) // records)
+    eng.surrogate_set(pk.PairSurrogate(2.0, 12.0, None, 12.0, 0.0), capacity=records,
                       record_every=every)
     eng.surrogate_record(True)
     t0 = time.perf_counter()
@@ -156,13 +180,16 @@ def start_configs(W, B):
     return [W["start"](n, r) for r, n in enumerate(W["sizes"](B))]
 
 
-def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=None, xyz=None):
+def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=None, xyz=None,
+                eq_cycles=0):
     """Engine of B runs of workload W.  `starts`: per run, the slot-ordered
     states of an earlier engine (configurations and step sizes) to start from;
-    `xyz`: per run, a host start configuration made beforehand."""
+    `xyz`: per run, a host start configuration made beforehand; `eq_cycles`:
+    MCParams.eq_cycles (ptmc_equilibrate simulates half of them)."""
     R = W["R"]
     sizes = W["sizes"](B)
-    mp_ = pk.MCParams(mc_cycles=10 ** 6, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=sizes[0])
+    mp_ = pk.MCParams(mc_cycles=10 ** 6, eq_cycles=eq_cycles, mc_sample=1, n_traj=R,
+                      n_atoms=sizes[0])
     temp = pk.TempGrid(W["T"][0], W["T"][1], R)
     if W["pot"] == "eam":
         pot = pk.EmbeddedAtomPotential(**CU_EAM)
@@ -238,49 +265,54 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def time_steps(torch, eng, steps, cycles, dev):
+def time_steps(torch, eng, steps, cycles, dev, production=True):
     """K timed steps; L2 flushed between steps; device time from the engine's
-    own CUDA events on its stream."""
+    own CUDA events on its stream.  A production step samples every cycle
+    (ptmc_run_cycles)."""
     ms = []
     for _ in range(steps):
         flush_l2(torch, dev)
-        eng.cycles_nosample(cycles)
+        if production:
+            eng.run_cycles(cycles)
+        else:
+            eng.cycles_nosample(cycles)
         ms.append(eng.stats()["last_cycles_ms"])
     return ms
 
 
-def gpu_arm(args, rank, world):
-    import torch
-    import __graft_entry__ as g
-    pk = g.load_package()
-    dev = torch.device("cuda", args.local_rank)
-    torch.cuda.set_device(dev)
-    L = pk._capi.load()
-    W = workload(args.workload)
-    if args.atoms > 0 and args.workload == "batched":
+def _accepted(eng, B):
+    return sum(int(eng.states(r)["counts"][:, 0].sum()) for r in range(B))
+
+
+def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, e2e_on):
+    """One workload: the chosen form (and the plain FP64 form unless
+    --only-chosen) timed on the production path; returns its record."""
+    W = workload(name)
+    if args.atoms > 0 and name == "batched":
         W["sizes"] = lambda B, n=args.atoms: [n] * B
-    B = args.runs or default_runs(args.workload, torch.cuda.get_device_properties(dev).multi_processor_count)
-    # measured in-situ peaks (FMA/MUFU-bound kernels)
-    f32, f64, mufu = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-    pk._capi.check(L.ptmc_measure_peaks(args.local_rank, ctypes.byref(f32), ctypes.byref(f64),
-                                        ctypes.byref(mufu)))
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    B = args.runs or default_runs(name, n_sm)
+    cycles = args.cycles or W["cycles"]
+    pcycles = max(1, args.plain_cycles or W["plain_cycles"])
+    seed = 1234 + 7919 * rank
     res = {}
 
-    def timed(eng, form, sizes):
-        """K timed steps of `eng` (barrier + synchronize on both sides)."""
+    def timed(eng, form, sizes, cyc, k_steps):
+        """k_steps timed production steps of `eng` (barrier + synchronize on both sides)."""
         st0 = eng.stats()
-        acc0 = sum(int(eng.states(r)["counts"][:, 0].sum()) for r in range(B))
+        acc0 = _accepted(eng, B)
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        clk = ClockSampler(os.path.join(args.outdir, "clocks_%s_r%d.csv" % (form, rank)), args.local_rank)
+        clk = ClockSampler(os.path.join(args.outdir, "clocks_%s_%s_r%d.csv" % (name, form, rank)),
+                           args.local_rank)
         with clk:
-            ms = time_steps(torch, eng, args.steps, args.cycles, dev)
+            ms = time_steps(torch, eng, k_steps, cyc, dev)
         torch.cuda.synchronize(dev)
         wall = time.perf_counter() - t0
         st1 = eng.stats()
-        moves = sum(sizes) * W["R"] * args.cycles * args.steps
+        moves = sum(sizes) * W["R"] * cyc * k_steps
         dev_s = sum(ms) / 1e3
         if world > 1:
             t = torch.tensor([dev_s], device=dev)
@@ -291,30 +323,31 @@ def gpu_arm(args, rank, world):
             moves_all = float(m.item())
         else:
             moves_all = float(moves)
-        acc = sum(int(eng.states(r)["counts"][:, 0].sum()) for r in range(B))
-        return dict(value=moves_all / dev_s, ms_per_step=1e3 * dev_s / args.steps, wall=wall,
+        acc = _accepted(eng, B)
+        return dict(value=moves_all / dev_s, ms_per_step=1e3 * dev_s / k_steps, wall=wall,
+                    steps=k_steps, cycles_per_step=cyc,
                     launches=st1["kernel_launches"] - st0["kernel_launches"],
                     drift=st1["max_drift"], clocks=clk.summary(), moves=moves, sizes=sizes,
                     acceptance=(acc - acc0) / moves)
 
-    seed = 1234 + 7919 * rank
     if W.get("da"):
-        # delayed acceptance: one FP32 chain is equilibrated and its surrogate
-        # trained (untimed); then the exact FP32 form, the surrogate-screened form
-        # and (from the same configurations and step sizes) the plain FP64 form
-        # are timed from the same chain state
-        eng, sizes = make_engine(pk, W, B, "fp32", args.cycles, seed, args.local_rank)
-        for _ in range(args.warmup):
-            eng.cycles_nosample(args.cycles)
-        da = train_surrogate(pk, eng, sizes, W["R"])
+        # delayed acceptance: one FP32 chain is warmed up and its surrogate
+        # trained (untimed), then equilibrated with screening on; the exact FP32
+        # form and the screened form are timed from that chain state, and the
+        # plain FP64 form from the same configurations and step sizes
+        eng, sizes = make_engine(pk, W, B, "fp32", cycles, seed, args.local_rank,
+                                 eq_cycles=2 * warmup * cycles)
+        eng.cycles_nosample(cycles)
+        da = train_surrogate(pk, eng, sizes, W["R"], records=args.da_records)
         trained = eng.surrogate_state()[:2]
+        eng.equilibrate()
         starts = [eng.states(r) for r in range(B)]
         if not args.only_chosen:
             eng.surrogate_enable(False)
-            res["fp32"] = timed(eng, "fp32", sizes)
+            res["fp32"] = timed(eng, "fp32", sizes, cycles, steps)
             eng.surrogate_enable(True)
         sur0 = eng.surrogate_state()[2]
-        res["fp32_da"] = timed(eng, "fp32_da", sizes)
+        res["fp32_da"] = timed(eng, "fp32_da", sizes, cycles, steps)
         sur1 = eng.surrogate_state()[2]
         moves = res["fp32_da"]["moves"]
         da.update(stage1_reject_frac=(sur1["stage1_rejects"] - sur0["stage1_rejects"]) / moves,
@@ -327,61 +360,123 @@ def gpu_arm(args, rank, world):
         res["fp32_da"]["da"] = da
         eng.close()
         if not args.only_chosen:
-            eng, _ = make_engine(pk, W, B, "fp64", args.cycles, seed + 1, args.local_rank, starts=starts)
-            eng.cycles_nosample(args.cycles)
-            res["fp64"] = timed(eng, "fp64", sizes)
+            eng, _ = make_engine(pk, W, B, "fp64", pcycles, seed + 1, args.local_rank,
+                                 starts=starts, eq_cycles=2 * 3 * pcycles)
+            eng.equilibrate()
+            res["fp64"] = timed(eng, "fp64", sizes, pcycles, 3)
             eng.close()
     else:
-        for form in (["fp64", "fp32"] if not args.only_chosen else ["fp32"]):
-            eng, sizes = make_engine(pk, W, B, form, args.cycles, seed, args.local_rank)
+        forms = ["fp32"] if args.only_chosen else ["fp64", "fp32"]
+        for form in forms:
+            cyc = cycles if form == "fp32" else pcycles
+            k_steps = steps if form == "fp32" else 3
+            k_warm = warmup if form == "fp32" else 3
+            eng, sizes = make_engine(pk, W, B, form, cyc, seed, args.local_rank,
+                                     eq_cycles=2 * k_warm * cyc)
             shapes = None
             if form == "fp32" and not args.no_tune:
-                # launch shape per atom count (CTAs per run), untimed set-up; the
-                # autotuner restores the chain after its trials
+                # launch shape per atom count, untimed set-up; the autotuner
+                # restores the chain after its trials
                 t0 = time.perf_counter()
-                shapes = eng.autotune(trial_cycles=max(2, min(20, args.cycles // 4)),
+                shapes = eng.autotune(trial_cycles=max(2, min(20, cyc // 4)),
                                       cache=os.path.join(args.outdir, "autotune_r%d.json" % rank))
                 tune_s = time.perf_counter() - t0
-            for _ in range(args.warmup):
-                eng.cycles_nosample(args.cycles)
-            res[form] = timed(eng, form, sizes)
+            eng.equilibrate()           # the warm-up: k_warm steps' worth of cycles
+            res[form] = timed(eng, form, sizes, cyc, k_steps)
             if shapes is not None:
                 res[form]["launch_shapes"] = {
                     "ctas_per_run": {str(k): v[0] for k, v in sorted(shapes.items())},
                     "lanes_per_walker": {str(k): v[1] for k, v in sorted(shapes.items())},
                     "autotune_s": round(tune_s, 3)}
             eng.close()
+    chosen = "fp32_da" if "fp32_da" in res else "fp32"
+    ch = res[chosen]
+    sizes = ch["sizes"]
+    if W.get("flops_move"):
+        flops_launch = W["flops_move"] * sum(sizes) * W["R"] * ch["cycles_per_step"]
+    else:
+        flops_launch = sum((W["flops_pair"] * (n - 1) + 2 * n) * n * W["R"]
+                           for n in sizes) * ch["cycles_per_step"]
+    # the cycle kernels are ~all of a step's device time
+    achieved = flops_launch / (ch["ms_per_step"] / 1e3) / 1e12
+    prof = PROFILED.get(name)
+    fresh = prof is not None and prof["src_sha"] == kernel_sha()
+    roof = {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
+            "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"],
+            "traffic": prof["dram_bytes_per_run"] * B if fresh else None,
+            "peak_source": "measured in-situ by ptmc_measure_peaks (FFMA chains)",
+            "ops_per_pair": W["flops_pair"], "mufu_per_pair": W["mufu_pair"],
+            "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"],
+            "issue": issue_roof(prof if fresh else None, ch, n_sm)}
+    if prof is not None and not fresh:
+        roof["counters_note"] = "ncu counters predate kernel source %s; not reported" % kernel_sha()
+    rec = {"workload": W["name"], "value": ch["value"], "unit": "atom-moves/s",
+           "ms_per_step": ch["ms_per_step"], "steps": ch["steps"],
+           "cycles_per_step": ch["cycles_per_step"], "runs": B, "replicas": W["R"],
+           "atoms": sorted(set(sizes)), "path": "production (ptmc_run_cycles: E, E^2, histograms)",
+           "form": "fp32resync_batched" + ("_da" if chosen == "fp32_da" else ""),
+           "launch_shapes": ch.get("launch_shapes"), "acceptance": ch["acceptance"],
+           "fp32_max_drift_eh": ch["drift"], "gpu_launches": ch["launches"],
+           "clocks": ch["clocks"], "roofline": roof,
+           "plain_fp64": ({"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
+                           "cycles_per_step": res["fp64"]["cycles_per_step"],
+                           "chosen_over_plain": ch["value"] / res["fp64"]["value"]}
+                          if "fp64" in res else None),
+           "fp32_exact": ({"value": res["fp32"]["value"], "ms_per_step": res["fp32"]["ms_per_step"]}
+                          if chosen != "fp32" and "fp32" in res else None),
+           "delayed_acceptance": ch.get("da")}
     # e2e through the public API with host buffers, one engine per step
-    e2e = None
-    if rank == 0 and not args.no_e2e:
+    if e2e_on and rank == 0:
         # per step: a context from host arrays (start configurations; with delayed
-        # acceptance also the trained surrogate's parameters), the step's cycles,
-        # every run's energies read back
+        # acceptance also the trained surrogate's parameters), equilibration
+        # cycles, the step's production cycles, every run's energies read back
         ts = []
         h2d = d2h = 0
-        # the step's inputs: host start configurations made before the clock starts
-        host_xyz = start_configs(W, B)
-        for k in range(args.warmup + args.steps):
+        host_xyz = start_configs(W, B)   # the step's inputs, made before the clock
+        for k in range(warmup + steps):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
-            eng, sizes = make_engine(pk, W, B, "fp32", args.cycles, 99 + k, args.local_rank,
-                                     xyz=host_xyz)
+            eng, sizes = make_engine(pk, W, B, "fp32", cycles, 99 + k, args.local_rank,
+                                     xyz=host_xyz, eq_cycles=2)
             h2d = sum(n * 3 * 8 for n in sizes)  # start configurations (one per run)
             if W.get("da"):
                 P, sur = trained
                 eng.surrogate_set(sur, capacity=1, params=P)
                 eng.surrogate_enable(True)
                 h2d += P.nbytes
-            eng.cycles_nosample(args.cycles)
+            eng.equilibrate()
+            eng.run_cycles(cycles)
             outs = [eng.energies()]  # every run's slot-ordered energies, one read
             eng.close()
             t1 = time.perf_counter()
-            if k >= args.warmup:
+            if k >= warmup:
                 ts.append(t1 - t0)
             d2h = sum(o.nbytes for o in outs)
-        e2e = dict(value=sum(sizes) * W["R"] * args.cycles / statistics.mean(ts),
-                   unit="atom-moves/s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h)
-    return res, dict(fp32_tflops=f32.value, fp64_tflops=f64.value, mufu_tops=mufu.value), B, e2e
+        rec["e2e"] = dict(value=sum(sizes) * W["R"] * cycles / statistics.mean(ts),
+                          unit="atom-moves/s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h)
+    return rec
+
+
+def gpu_arm(args, rank, world, names):
+    import torch
+    import __graft_entry__ as g
+    pk = g.load_package()
+    dev = torch.device("cuda", args.local_rank)
+    torch.cuda.set_device(dev)
+    L = pk._capi.load()
+    # measured in-situ peaks (FMA/MUFU-bound kernels)
+    f32, f64, mufu = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    pk._capi.check(L.ptmc_measure_peaks(args.local_rank, ctypes.byref(f32), ctypes.byref(f64),
+                                        ctypes.byref(mufu)))
+    peaks = dict(fp32_tflops=f32.value, fp64_tflops=f64.value, mufu_tops=mufu.value)
+    recs = {}
+    for name in names:
+        head = name == names[0]
+        steps = args.steps if head else max(3, args.steps // 4)
+        warmup = args.warmup if head else 3
+        recs[name] = run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup,
+                                  e2e_on=head and not args.no_e2e)
+    return recs, peaks
 
 
 # --------------------------------------------------------------- CPU oracle arm
@@ -436,11 +531,18 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="cu55", choices=["cu55", "ne13", "npt108", "batched", "nn55"])
+    ap.add_argument("--workload", default="all", choices=["all"] + ALL,
+                    help="all: every workload, the headline (cu55) first")
     ap.add_argument("--runs", type=int, default=0, help="independent PT runs batched (0 = fill the GPU)")
-    ap.add_argument("--cycles", type=int, default=0, help="MC cycles per step (0: 200, NN: 20)")
+    ap.add_argument("--cycles", type=int, default=0,
+                    help="chosen-form MC cycles per step (0: the workload's, 200; NN: 20)")
+    ap.add_argument("--plain-cycles", type=int, default=0,
+                    help="plain FP64 form MC cycles per step (0: the workload's)")
+    ap.add_argument("--da-records", type=int, default=100000,
+                    help="delayed acceptance: (configuration, dE) records the surrogate trains on")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--outdir", default=os.path.join(tempfile.gettempdir(), "ptmc_bench"),
+                    help="clock samples and the autotuner cache")
     ap.add_argument("--only-chosen", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -452,22 +554,23 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     args.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    W = workload(args.workload)
-    if args.atoms > 0 and args.workload == "batched":
-        W["sizes"] = lambda B, n=args.atoms: [n] * B
-    if args.cycles <= 0:
-        args.cycles = W.get("cycles", 200)
+    names = ALL if args.workload == "all" else [args.workload]
+    head = names[0]
+    W = workload(head)
     cores = os.cpu_count() or 1
 
     if args.impl == "reference":
+        # the reference's CPU path on all host cores: the oracle port, a
+        # restatement of the reference's hot path (no Julia here), on the
+        # headline workload
         if rank != 0:
             return
         per_step = []
         for _ in range(args.warmup + args.steps):
-            v, cyc = cpu_baseline(args.workload, cores, max(2.0, args.cpu_seconds / 4))
+            v, cyc = cpu_baseline(head, cores, max(2.0, args.cpu_seconds / 4))
             per_step.append(v)
         v = statistics.mean(per_step[args.warmup:])
-        line = {"metric": "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error",
+        line = {"metric": METRIC,
                 "value": v, "unit": "atom-moves/s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -487,74 +590,56 @@ def main():
     # CPU baseline first (spawned workers, before any GPU work in this process)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, cyc = cpu_baseline(args.workload, cores, args.cpu_seconds)
+        v, cyc = cpu_baseline(head, cores, args.cpu_seconds)
         cpu = {"value": v, "unit": "atom-moves/s", "cores": cores, "kind": "port",
                "sample": "%d spawn workers, one %s PT run each (R=%d), %.0f s, %d cycles in total"
                          % (cores, W["name"], W["R"], args.cpu_seconds, cyc)}
-    res, peaks, B, e2e = gpu_arm(args, rank, world)
+    recs, peaks = gpu_arm(args, rank, world, names)
     if rank != 0:
         return
-    import torch
-    n_sm = torch.cuda.get_device_properties(0).multi_processor_count
-    chosen = "fp32_da" if "fp32_da" in res else "fp32"
-    ch = res[chosen]
-    sizes = ch["sizes"]
-    # roofline of the dominant kernel (k_cycles): algorithmic FP32 ops per launch
-    pairs_per_move = [n - 1 for n in sizes]
-    if W.get("flops_move"):
-        flops_launch = W["flops_move"] * sum(sizes) * W["R"] * args.cycles
-    else:
-        flops_launch = sum((W["flops_pair"] * (n - 1) + 2 * n) * n * W["R"] for n in sizes) * args.cycles
-    # the cycle kernels are ~all of a step's device time (launch list in profiles/)
-    achieved = flops_launch / (ch["ms_per_step"] / 1e3) / 1e12
+    h = recs[head]
     line = {
-        "metric": "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) error",
-        "value": ch["value"], "unit": "atom-moves/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ch["ms_per_step"], "higher_is_better": True,
+        "metric": METRIC,
+        "value": h["value"], "unit": "atom-moves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64+bf16" if chosen == "fp32_da" else "f32+f64", "data": "synthetic",
-        "config": {"workload": W["name"] + ("_fp32resync_batched_da" if chosen == "fp32_da"
-                                            else "_fp32resync_batched"), "runs_per_gpu": B,
-                   "replicas": W["R"], "atoms": sorted(set(sizes)), "cycles_per_step": args.cycles,
-                   "resync_every": W["resync"], "exchange": "every cycle",
-                   "launch_shapes": ch.get("launch_shapes"),
+        "dtype": "f32+f64+bf16" if h["delayed_acceptance"] else "f32+f64", "data": "synthetic",
+        "config": {"workload": h["workload"] + "_" + h["form"], "runs_per_gpu": h["runs"],
+                   "replicas": h["replicas"], "atoms": h["atoms"],
+                   "cycles_per_step": h["cycles_per_step"], "resync_every": W["resync"],
+                   "exchange": "every cycle", "path": h["path"],
+                   "launch_shapes": h["launch_shapes"],
                    "l2": "flushed between steps (256 MB write)"},
-        "plain_fp64": ({"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
-                        "chosen_over_plain": ch["value"] / res["fp64"]["value"]}
-                       if "fp64" in res else None),
-        "fp32_exact": ({"value": res["fp32"]["value"], "ms_per_step": res["fp32"]["ms_per_step"]}
-                       if chosen != "fp32" and "fp32" in res else None),
-        "delayed_acceptance": ch.get("da"),
-        "fp32_max_drift_eh": ch["drift"],
-        "roofline": {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
-                     "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"],
-                     "traffic": (W["dram_bytes_per_run"] * B if W.get("dram_bytes_per_run") else None),
-                     "peak_source": "measured in-situ by ptmc_measure_peaks (FFMA chains)",
-                     "ops_per_pair": W["flops_pair"], "mufu_per_pair": W["mufu_pair"],
-                     "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"],
-                     "issue": issue_roof(W, ch, n_sm)},
+        "plain_fp64": h["plain_fp64"],
+        "fp32_exact": h["fp32_exact"],
+        "delayed_acceptance": h["delayed_acceptance"],
+        "fp32_max_drift_eh": h["fp32_max_drift_eh"],
+        "roofline": h["roofline"],
         "cpu_baseline": cpu,
-        "e2e": e2e,
-        "gpu_launches": ch["launches"],
-        "clocks": ch["clocks"],
+        "e2e": h.get("e2e"),
+        "gpu_launches": h["gpu_launches"],
+        "clocks": h["clocks"],
+        "workloads": {k: {kk: vv for kk, vv in r.items() if kk != "e2e"} for k, r in recs.items()},
     }
     print(json.dumps(line))
 
 
-def issue_roof(W, ch, n_sm):
+def issue_roof(prof, ch, n_sm):
     """The instruction-issue roofline of the cycle kernel: warp instructions
-    per move (ncu) x moves/s against 4 issue slots per SM per clock at the SM
-    clock sampled during the timed region."""
-    ipm = W.get("inst_per_move")
+    per move (ncu, for the profiled launch shape) x moves/s against 4 issue
+    slots per SM per clock at the SM clock sampled during the timed region."""
+    if not prof or not ch.get("clocks"):
+        return None
     shapes = (ch.get("launch_shapes") or {}).get("lanes_per_walker") or {}
-    if not ipm or not ch.get("clocks") or any(v != W.get("lanes") for v in shapes.values()):
+    if any(v != prof["lanes"] for v in shapes.values()):
         return None  # measured for one launch shape only
     mhz = ch["clocks"]["sm_mhz"]
+    ipm = prof["inst_per_move"]
     achieved = ch["value"] * ipm / 1e9
     peak = 4 * n_sm * mhz * 1e6 / 1e9
     return {"warp_inst_per_move": ipm, "achieved": achieved, "peak": peak, "unit": "G warp-inst/s",
             "frac": achieved / peak,
-            "source": "ncu smsp__inst_executed, " + W["inst_src"]}
+            "source": "ncu smsp__inst_executed, kernel source %s" % prof["src_sha"]}
 
 
 if __name__ == "__main__":

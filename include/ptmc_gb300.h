@@ -348,7 +348,10 @@ int ptmc_multihist_linear(int R, int n_bin, const double* en_hist, const double*
  * that array, so calls that overlap on the GPU race.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress); make
  * that first call before any stream capture.  Results equal
- * ptmc_multihist_nvt's to rounding. */
+ * ptmc_multihist_nvt's to rounding.  Every failure sets the message of
+ * ptmc_last_error(NULL); a CUDA error left pending by an earlier launch of the
+ * caller's makes the call return PTMC_ERR_CUDA before it launches anything,
+ * and that error stays pending for the caller. */
 #define PTMC_NOALLOC_SCRATCH_DOUBLES 16384
 int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist,
                                const double* d_t_grid, const double* d_beta,
@@ -362,15 +365,18 @@ int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist,
  * spread over a thread-block cluster of C CTAs (C SMs, R/C walkers each); the
  * replica exchange, step adaptation and sampling then read the other CTAs'
  * walkers through distributed shared memory; results are bit-identical for
- * every C.  L: lanes per walker, 32 (one warp per walker) or 16 (two walkers
- * per warp, for small N); the pair sums then add in another order (FP32
- * rounding), the chains stay statistically equivalent.  Default C = 1, L = 32. */
-/* Set (C, L) for the runs with N atoms (C <= 8, R % C == 0, L in {32, 16},
- * (R / C) % (32 / L) == 0). */
+ * every C.  L: lanes per walker, 32 (one warp per walker), 16 (two walkers per
+ * warp), 8 or 4 (four or eight walkers per warp, NVT with C = 1: the move's
+ * scalar work is shared by the warp's walkers and a walker needs less shared
+ * memory, so more walkers fit an SM); the pair sums then add in another order
+ * (FP32 rounding), the chains stay statistically equivalent and every L
+ * consumes the same draw streams.  Default C = 1, L = 32. */
+/* Set (C, L) for the runs with N atoms (C <= 8, R % C == 0, L in {32, 16, 8, 4},
+ * (R / C) % (32 / L) == 0; L <= 8 only with C = 1 in NVT). */
 int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run, int lanes_per_walker);
 /* Pick (C, L) per atom count by timing `trial_cycles` plain cycles of the whole
  * batch for candidate shapes (coordinate descent over C in {1, 2, 4, 8} x L
- * in {32, 16} per atom count, largest N first) on a snapshot of the device
+ * in {32, 16, 8, 4} per atom count, largest N first) on a snapshot of the device
  * state that is restored after every trial, so the chain is not advanced.
  * cache_path (may be NULL): JSON-lines file of earlier choices, keyed by
  * device, potential, boundary, ensemble, R and the (N, runs) mix; a hit skips
@@ -384,6 +390,22 @@ int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_path,
  * denominators of the replica-cycle kernels. */
 int ptmc_measure_peaks(int device, double* fp32_tflops, double* fp64_tflops,
                        double* mufu_tops);
+
+/* --- diagnostics of the bounded device waits (no counterpart in the
+ *     reference, which has no device code) ---
+ * The FP32 form's exchange handshake waits for the partner walker with a
+ * bounded spin (default 2^33 clocks); when it runs out the walker stops with
+ * status 3, both walkers of the pair keep their slots, and the call returns
+ * PTMC_ERR_CUDA naming the wait.  The context's chains are then incomplete:
+ * destroy it and build a new one.  Test hook: `clocks` > 0 sets the limit
+ * (0 restores the default); never_set = 1 makes every partner wait target a
+ * flag value that no walker writes, so the failure path runs without any
+ * fault.  Takes effect at the next launch. */
+int ptmc_set_wait_test(ptmc_ctx* c, long long clocks, int never_set);
+/* Walker status words of run `run` in walker order, status[R]: 0 running,
+ * 1 too many moves out of the sphere, 2 a tensor-core wait ran out, 3 an
+ * exchange-partner wait ran out. */
+int ptmc_get_walker_status(ptmc_ctx* c, int run, int* status);
 
 const char* ptmc_last_error(ptmc_ctx* c); /* c may be NULL (global last error) */
 void ptmc_destroy(ptmc_ctx* c);

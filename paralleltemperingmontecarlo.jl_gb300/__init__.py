@@ -626,6 +626,21 @@ class Engine:
                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return {int(self.N[r]): (int(out[2 * r]), int(out[2 * r + 1])) for r in range(self.n_runs)}
 
+    # ---- bounded device waits
+    def set_wait_test(self, clocks=0, never_set=False):
+        """Exchange-partner wait limit of the FP32 form in clocks (0 = the
+        default 2^33) and the test switch that makes every such wait target a
+        flag value nobody writes (the failure path, without a fault)."""
+        self._ck(self.L.ptmc_set_wait_test(self.h, int(clocks), int(bool(never_set))))
+
+    def walker_status(self, run=0):
+        """Status word of every walker of `run` (walker order): 0 running,
+        1 out of the sphere, 2 tensor-core wait ran out, 3 exchange wait ran out."""
+        st = np.zeros(self.R, dtype=np.int32)
+        self._ck(self.L.ptmc_get_walker_status(self.h, int(run),
+                                               st.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return st
+
     # ---- delayed acceptance with the learned pair surrogate (NN potential)
     def surrogate_set(self, surrogate, capacity=100000, record_every=1, params=None):
         """Attach a PairSurrogate (configuration and, unless `params` is given,

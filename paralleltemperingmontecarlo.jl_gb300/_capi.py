@@ -126,6 +126,8 @@ SIGNATURES = {
     "ptmc_set_launch_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int]),
     "ptmc_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, _ip]),
+    "ptmc_set_wait_test": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int]),
+    "ptmc_get_walker_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip]),
     "ptmc_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "ptmc_destroy": (None, [ctypes.c_void_p]),
     "ptmc_version": (ctypes.c_char_p, []),

@@ -147,6 +147,8 @@ struct ptmc_ctx {
   int lut_na = 0, lut_nd = 0;
   double lut_par[4] = {0, 0, 0, 0};  // start_dist, d_dist, d_angle, c6coeff
   DBuf<double> d_tan, d_lut;
+  DBuf<double> d_pe;           // plain form, NVT: pair cache (pair_cache in ptmc_engine.cuh)
+  DBuf<float> d_lo;            // FP32 form: lo halves of positions during a narrow launch
   // two-species RuNNer potential (NNVT ensemble)
   std::vector<double> nn2_rad, nn2_ang, nn2_W1, nn2_W2;
   int nn2_n1 = 0, nn2_H1 = 0, nn2_H2 = 0, n_swaps = 1;
@@ -157,6 +159,9 @@ struct ptmc_ctx {
   DBuf<int> d_status, d_wos;
   DBuf<long long> d_cnt;
   DBuf<unsigned int> d_hist;
+  // exchange-partner wait of the FP32 form: limit in clocks, test switch
+  long long xwait_clocks = XWAIT_CLOCKS;
+  int xwait_never = 0;
   bool rdf_on = false;         // radial distribution sampling (rdfsave of ptmc_run!)
   DBuf<unsigned int> d_rdf;    // [W][5 n_bin]
   KParams K{};
@@ -736,7 +741,10 @@ int ptmc_init(ptmc_ctx* c) {
   }
   // offsets
   c->rd.assign(nr, RunDesc{});
-  long long po = 0, mo = 0, co = 0, ho = 0;
+  long long po = 0, mo = 0, co = 0, ho = 0, peo = 0;
+  // the plain form's NVT pair cache: N x N values (ELJ) or pairs (EAM) per walker
+  const int pe_w = (!c->f32() && !nn && pair_cache(c->pot, npt ? ENS_NPT : ENS_NVT))
+                       ? (c->pot == POT_EAM ? 2 : 1) : 0;
   int wk = 0;
   int nb = c->p.n_bin + 2;
   int hstride = npt ? nb * nb : nb;
@@ -750,6 +758,7 @@ int ptmc_init(ptmc_ctx* c) {
     r.pos_off = po;
     r.mat_off = mo;
     r.comp_off = co;
+    r.pe_off = peo;
     r.hist_off = ho;
     r.hist_stride = hstride;
     r.n_start = h.n_start;
@@ -758,6 +767,7 @@ int ptmc_init(ptmc_ctx* c) {
     po += (long long)R * h.N * 3;
     if ((npt || bpot) && !c->f32()) mo += (long long)R * h.N * h.N;
     if (c->pot == POT_EAM) co += (long long)R * h.N * 2;
+    peo += (long long)R * h.N * h.N * pe_w;
     ho += (long long)R * hstride;
     wk += R;
   }
@@ -770,7 +780,8 @@ int ptmc_init(ptmc_ctx* c) {
       c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho) ||
       (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)) || c->d_boxh.alloc(W) ||
       c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W) ||
-      (bpot && c->d_tan.alloc(mo)) || (c->pot == POT_LUT && c->d_lut.alloc(c->lut.size())))
+      (bpot && c->d_tan.alloc(mo)) || (c->pot == POT_LUT && c->d_lut.alloc(c->lut.size())) ||
+      c->d_pe.alloc(peo) || c->d_lo.alloc(c->f32() && !nn ? po / 3 * 4 : 0))
     return c->fail(PTMC_ERR_CUDA, "device allocation failed");
   // host images (the start configurations go up once per run and are
   // expanded into replicas on the device)
@@ -861,6 +872,8 @@ int ptmc_init(ptmc_ctx* c) {
   K.pos = c->d_pos.p;
   K.mat = c->d_mat.p;
   K.comp = c->d_comp.p;
+  K.pe = c->d_pe.p;
+  K.lo = c->d_lo.p;
   K.en = c->d_en.p;
   K.box = c->d_box.p;
   K.rc2 = c->d_rc2.p;
@@ -916,6 +929,8 @@ int ptmc_init(ptmc_ctx* c) {
   K.mc_sample = c->p.mc_sample;
   K.resync_every = c->p.resync_every;
   K.seed = c->p.seed;
+  K.xwait_clocks = c->xwait_clocks;
+  K.xwait_never = c->xwait_never;
   if (nn2) {
     int Nmax = 0;
     for (auto& G : c->groups) Nmax = std::max(Nmax, G.N);
@@ -1273,6 +1288,8 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_cnt_sep.free_();
   c->d_tan.free_();
   c->d_lut.free_();
+  c->d_pe.free_();
+  c->d_lo.free_();
   for (auto* b : {&c->d_nn2_rad, &c->d_nn2_ang, &c->d_nn2_W1, &c->d_nn2_W2}) b->free_();
   c->d_nn2_swaps.free_();
   c->d_nn_sf.free_();
@@ -1442,7 +1459,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       return c->fail(PTMC_ERR_IO, "cannot write configT.xyz");
   }
   // engine.bin: complete state
-  std::string b = "PTMCGB02";
+  std::string b = "PTMCGB03";
   unsigned long long hdr[4] = {(unsigned long long)c->p.n_runs, (unsigned long long)R,
                                (unsigned long long)c->W, (unsigned long long)c->equilibrated};
   put(b, hdr, 4);
@@ -1455,7 +1472,7 @@ int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
       (rc = dump(c, b, c->d_hist)) || (rc = dump(c, b, c->d_nn_G)) || (rc = dump(c, b, c->d_nn_sow)) ||
       (rc = dump(c, b, c->d_rdf)) || (rc = dump(c, b, c->d_boxh)) || (rc = dump(c, b, c->d_maxboxh)) ||
       (rc = dump(c, b, c->d_maxd_sep)) || (rc = dump(c, b, c->d_cnt_sep)) || (rc = dump(c, b, c->d_tan)) ||
-      (rc = dump(c, b, c->d_nn2_swaps)))
+      (rc = dump(c, b, c->d_nn2_swaps)) || (rc = dump(c, b, c->d_pe)))
     return rc;
   put(b, "PTMCEND!", 8);
   if (!write_file_atomic(d + "/engine.bin", b)) return c->fail(PTMC_ERR_IO, "cannot write engine.bin");
@@ -1473,9 +1490,10 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
   size_t k;
   while ((k = std::fread(buf, 1, sizeof(buf), f)) > 0) b.append(buf, k);
   std::fclose(f);
-  if (b.size() >= 8 && b.compare(0, 8, "PTMCGB01") == 0)
-    return c->fail(PTMC_ERR_IO, "engine.bin: written by an earlier format (PTMCGB01), not restorable");
-  if (b.size() < 8 + 32 || b.compare(0, 8, "PTMCGB02") != 0)
+  if (b.size() >= 8 && (b.compare(0, 8, "PTMCGB01") == 0 || b.compare(0, 8, "PTMCGB02") == 0))
+    return c->fail(PTMC_ERR_IO, "engine.bin: written by an earlier format (" + b.substr(0, 8) +
+                                    "), not restorable");
+  if (b.size() < 8 + 32 || b.compare(0, 8, "PTMCGB03") != 0)
     return c->fail(PTMC_ERR_IO, "engine.bin: bad magic");
   if (b.size() < 8 || b.compare(b.size() - 8, 8, "PTMCEND!") != 0)
     return c->fail(PTMC_ERR_IO, "engine.bin truncated (no end marker)");
@@ -1505,7 +1523,7 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
       (rc = undump(c, b, at, c->d_rdf)) || (rc = undump(c, b, at, c->d_boxh)) ||
       (rc = undump(c, b, at, c->d_maxboxh)) || (rc = undump(c, b, at, c->d_maxd_sep)) ||
       (rc = undump(c, b, at, c->d_cnt_sep)) || (rc = undump(c, b, at, c->d_tan)) ||
-      (rc = undump(c, b, at, c->d_nn2_swaps)))
+      (rc = undump(c, b, at, c->d_nn2_swaps)) || (rc = undump(c, b, at, c->d_pe)))
     return rc;
   c->rd = rd;
   c->equilibrated = hdr[3] != 0;
@@ -2279,10 +2297,13 @@ extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_pa
           int pick = best[N];
           double t_pick = t_best;
           for (int cc : {1, 2, 4, 8})
-            for (int ll : {32, 16}) {
+            for (int ll : {32, 16, 8, 4}) {
               const int code = 100 * cc + ll;
               if (code == best[N] || R % cc != 0 || (R / cc) % (32 / ll) != 0) continue;
-              if (cycles32_smem_bytes(c->pot, R, N, cc) > optin) continue;
+              if (ll <= 8 && (cc != 1 || c->p.ensemble != PTMC_NVT || R > 32)) continue;
+              const long long smem = ll <= 8 ? cycles32n_smem_bytes(c->pot, R, N, ll)
+                                             : cycles32_smem_bytes(c->pot, R, N, cc);
+              if (smem > optin) continue;
               std::map<int, int> cand = best;
               cand[N] = code;
               double t = 0;
@@ -2326,23 +2347,49 @@ extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run, int l
   const int R = c->R();
   if (ctas_per_run < 1 || ctas_per_run > 8 || R % ctas_per_run != 0)
     return c->fail(PTMC_ERR_ARG, "ctas_per_run must divide the replica count and be <= 8");
-  if (lanes_per_walker != 32 && lanes_per_walker != 16)
-    return c->fail(PTMC_ERR_ARG, "lanes_per_walker must be 32 or 16");
+  if (lanes_per_walker != 32 && lanes_per_walker != 16 && lanes_per_walker != 8 &&
+      lanes_per_walker != 4)
+    return c->fail(PTMC_ERR_ARG, "lanes_per_walker must be 32, 16, 8 or 4");
   if ((R / ctas_per_run) % (32 / lanes_per_walker) != 0)
-    return c->fail(PTMC_ERR_ARG, "16 lanes per walker need an even number of walkers per CTA");
+    return c->fail(PTMC_ERR_ARG, "the walkers of a CTA must fill whole warps (R / C a multiple of "
+                                 "32 / lanes_per_walker)");
+  if (lanes_per_walker <= 8 && (ctas_per_run != 1 || c->p.ensemble != PTMC_NVT))
+    return c->fail(PTMC_ERR_ARG, "8 or 4 lanes per walker: NVT with one CTA per run");
   int optin = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   bool found = false;
   for (auto& G : c->groups) {
     if (G.N != N) continue;
-    if (cycles32_smem_bytes(c->pot, R, N, ctas_per_run) > optin)
-      return c->fail(PTMC_ERR_LIMIT, "launch shape exceeds the shared memory of a CTA");
+    const long long smem = lanes_per_walker <= 8 ? cycles32n_smem_bytes(c->pot, R, N, lanes_per_walker)
+                                                 : cycles32_smem_bytes(c->pot, R, N, ctas_per_run);
+    if (smem > optin) return c->fail(PTMC_ERR_LIMIT, "launch shape exceeds the shared memory of a CTA");
     G.ncta = ctas_per_run;
     G.lpr = lanes_per_walker;
     found = true;
   }
   if (!found) return c->fail(PTMC_ERR_ARG, "no run with that atom count");
   drop_graphs(c);
+  return PTMC_OK;
+}
+
+extern "C" int ptmc_set_wait_test(ptmc_ctx* c, long long clocks, int never_set) {
+  if (!c) return PTMC_ERR_ARG;
+  if (clocks < 0) return c->fail(PTMC_ERR_ARG, "ptmc_set_wait_test: clocks must be >= 0");
+  c->xwait_clocks = clocks == 0 ? XWAIT_CLOCKS : clocks;
+  c->xwait_never = never_set ? 1 : 0;
+  c->K.xwait_clocks = c->xwait_clocks;
+  c->K.xwait_never = c->xwait_never;
+  drop_graphs(c);  // captured launches hold the old kernel parameters
+  return PTMC_OK;
+}
+
+extern "C" int ptmc_get_walker_status(ptmc_ctx* c, int run, int* status) {
+  if (!c || !status) return PTMC_ERR_ARG;
+  if (!c->inited) return c->fail(PTMC_ERR_STATE, "ptmc_init not called");
+  if (run < 0 || run >= c->p.n_runs) return c->fail(PTMC_ERR_ARG, "run index out of range");
+  const RunDesc& r = c->rd[c->dev_of_run[run]];
+  CK(cudaMemcpyAsync(status, c->d_status.p + r.wk, sizeof(int) * c->R(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return PTMC_OK;
 }

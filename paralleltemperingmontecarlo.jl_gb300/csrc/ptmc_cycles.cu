@@ -22,13 +22,23 @@
 // (rand(1:n_steps)), 3 displacement draws (+3 per spherical retry), the
 // acceptance draw; volume move: scale draw, acceptance draw.
 //
-// Forms.  FP64 (plain): every quantity in FP64; proposals and squared
-// distances use non-contracted IEEE operations, so they are bit-identical to
-// the reference's; pair energies use FMA Horner forms (agree to ~1e-16
-// relative).  FP32_RESYNC: positions stay FP64 (exact proposals), the pair
-// terms of a move are FP32 (MUFU lg2/ex2 for the EAM powers), the running
-// total is FP64, and every `resync_every` cycles each walker recomputes its
-// energy (and EAM components) in FP64, recording the drift.
+// This file holds the plain FP64 form: every quantity in FP64; proposals and
+// squared distances use non-contracted IEEE operations, so they are
+// bit-identical to the reference's; pair energies use FMA Horner forms (agree
+// to ~1e-16 relative).  The FP32_RESYNC form's cycle kernel is in
+// ptmc_cycles32.cu; k_init and k_resync here serve both forms.
+//
+// Pair cache.  The reference keeps each state's squared-distance matrix and
+// recomputes the old pair energies of a moved atom from it
+// (dimer_energy_update!, src/EnergyEvaluation.jl:804-821; EAM
+// calc_components, :1105-1148).  In NVT the plain form keeps the pair energies
+// themselves in HBM (ELJ: V(r_ij); EAM: (r_ij^-n, r_ij^-m)), one N x N matrix
+// per walker, so a move evaluates only its N - 1 trial pairs and reads the old
+// row; an accepted move writes the row and the column.  A cached value is the
+// value computed from the distance the reference stores for the pair, so the
+// chain is the reference's arithmetic.  NPT and the angle-dependent
+// potentials keep the squared-distance matrix (volume moves rescale it) and
+// evaluate the old pair energies from it, as the reference does.
 #include <cuda_runtime.h>
 
 #include "ptmc_device.cuh"
@@ -52,26 +62,9 @@ __device__ __forceinline__ double v_all64(const double* c, int K, double r2) {
   for (int k = K - 2; k >= 0; --k) v = fma(v, ir, c[k]);
   return v * (inv * inv * inv);
 }
-__device__ __forceinline__ float v_even32(const float* c, int K, float r2) {
-  float inv = rcpf(r2);
-  float v = c[K - 1];
-  for (int k = K - 2; k >= 0; --k) v = fmaf(v, inv, c[k]);
-  return v * (inv * inv * inv);
-}
-__device__ __forceinline__ float v_all32(const float* c, int K, float r2) {
-  float ir = rsqrtf(r2);
-  float inv = ir * ir;
-  float v = c[K - 1];
-  for (int k = K - 2; k >= 0; --k) v = fmaf(v, ir, c[k]);
-  return v * (inv * inv * inv);
-}
 template <int POT>
 __device__ __forceinline__ double v64(const double* c, int K, double r2) {
   return POT == POT_ELJ ? v_all64(c, K, r2) : v_even64(c, K, r2);
-}
-template <int POT>
-__device__ __forceinline__ float v32(const float* c, int K, float r2) {
-  return POT == POT_ELJ ? v_all32(c, K, r2) : v_even32(c, K, r2);
 }
 // lrc (src/EnergyEvaluation.jl:968-982); rc2 is the squared cut-off
 __device__ double lrc64(int N, double rc2, const double* c, int K) {
@@ -140,12 +133,6 @@ template <int BC>
 __device__ __forceinline__ double hist_volume(double L, double H) {
   if (BC == BC_RHB) return dmul(dmul(L, L), dmul(3.0, sqrt(H))) / 2;
   return box_volume<BC>(L, H);
-}
-template <int BC>
-__device__ __forceinline__ float pf2(float4 a, float4 b, float L, float iL) {
-  float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-  if (BC == BC_CUB) return f2_cub(dx, dy, dz, L, iL);
-  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
 // ---- ELJPotentialB and LookupTablePotential: pair energies that depend on
@@ -278,21 +265,28 @@ __device__ double walker_energy_b(const KParams& P, const double* X, int N, doub
 // one walker from positions (init and resync).  ELJ: dimer_energy_config
 // (src/EnergyEvaluation.jl:378-420); EAM: set_variables + energy
 // (src/EnergyEvaluation.jl:1800-1810, 1156-1162).  Writes the NPT distance
-// matrix (plain form) and the EAM components when the pointers are given.
+// matrix, the EAM components and the NVT pair cache (PE: ELJ V(r_ij) as N x N
+// doubles, EAM (r_ij^-n, r_ij^-m) as N x N double pairs, zero diagonal) when
+// the pointers are given.
 template <int POT, int BC, int ENS>
 __device__ double walker_energy64(const double* X, int N, double L, double H, double rc2,
                                   const double* c, int K, double hn, double hm,
                                   double ean, double ecam, double* M,
-                                  double* comp64, float2* comp32, int lane) {
+                                  double* comp64, double* PE, int lane) {
   double e = 0.0;
   if constexpr (POT == POT_EAM) {
+    double2* PE2 = (double2*)PE;
     for (int k = lane; k < N; k += 32) {
       double a = 0.0, b = 0.0;
       for (int j = 0; j < N; ++j) {
-        if (j == k) continue;
+        if (j == k) {
+          if (PE2) PE2[(size_t)k * N + k] = make_double2(0.0, 0.0);
+          continue;
+        }
         double x = pd2<BC>(X[3 * k], X[3 * k + 1], X[3 * k + 2], X + 3 * j, L, H);
         double pa, pb;
         invrexp64(x, hn, hm, pa, pb);
+        if (PE2) PE2[(size_t)k * N + j] = make_double2(pa, pb);
         a += pa;
         b += pb;
       }
@@ -300,7 +294,6 @@ __device__ double walker_energy64(const double* X, int N, double L, double H, do
         comp64[2 * k] = a;
         comp64[2 * k + 1] = b;
       }
-      if (comp32) comp32[k] = make_float2((float)a, (float)b);
       e += ean * a - ecam * sqrt(b);
     }
     return warp_sum(e);
@@ -314,9 +307,15 @@ __device__ double walker_energy64(const double* X, int N, double L, double H, do
           M[(size_t)j * N + i] = x;
         }
         if (ENS == ENS_NPT && !(x <= rc2)) continue;
-        e += v64<POT>(c, K, x);
+        const double v = v64<POT>(c, K, x);
+        if (PE) {
+          PE[(size_t)i * N + j] = v;
+          PE[(size_t)j * N + i] = v;
+        }
+        e += v;
       }
       if (M && lane == 0) M[(size_t)i * N + i] = 0.0;
+      if (PE && lane == 0) PE[(size_t)i * N + i] = 0.0;
     }
     e = warp_sum(e);
     if (ENS == ENS_NPT) e = e + lrc_box<BC>(N, rc2, c, K, L, H);
@@ -336,8 +335,11 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
   const int N = rd.N, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ns = rd.n_start > 0 && rd.n_start < rd.R ? rd.n_start : rd.R;
   const bool keep_m = (ENS == ENS_NPT || pot_b(POT)) && !F32;
+  constexpr bool keep_pe = pair_cache(POT, ENS) && !F32;  // plain form's NVT pair cache
+  constexpr int pe_w = POT == POT_EAM ? 2 : 1;            // doubles per cached pair
   auto mat = [&](int v) { return P.mat + rd.mat_off + (size_t)v * N * N; };
   auto cmp = [&](int v) { return P.comp + rd.comp_off + (size_t)v * N * 2; };
+  auto pe = [&](int v) { return P.pe + rd.pe_off + (size_t)v * N * N * pe_w; };
   if (w < ns) {
     const int g = rd.wk + w;
     const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
       e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
                                         -0.5 * P.eam_n, -0.5 * P.eam_m,
                                         P.eam_ean, P.eam_ecam, M, comp,
-                                        nullptr, lane);
+                                        keep_pe ? pe(w) : nullptr, lane);
     if (lane == 0) {
       P.en[g] = e;
       P.status[g] = ST_OK;
@@ -365,6 +367,8 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
       for (int k = lane; k < 2 * N; k += 32) cmp(w)[k] = cmp(src)[k];
     if (keep_m)
       for (int k = lane; k < N * N; k += 32) mat(w)[k] = mat(src)[k];
+    if (keep_pe)
+      for (int k = lane; k < N * N * pe_w; k += 32) pe(w)[k] = pe(src)[k];
     if (pot_b(POT))
       for (int k = lane; k < N * N; k += 32)
         P.tan[rd.mat_off + (size_t)w * N * N + k] = P.tan[rd.mat_off + (size_t)src * N * N + k];
@@ -377,15 +381,15 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
 }
 
 // ------------------------------------------------------------ cycle kernel
-template <int POT, int BC, int ENS, bool F32>
+template <int POT, int BC, int ENS>
 __global__ void __launch_bounds__(1024)
     k_cycles(KParams P, int run0, int ncycles, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
-  __shared__ float s_cf[MAX_COEFF];
   __shared__ double s_ca[pot_b(POT) ? MAX_COEFF : 1], s_cb[pot_b(POT) ? MAX_COEFF : 1];
   constexpr bool BPOT = pot_b(POT);
-  constexpr bool KEEP_M = (ENS == ENS_NPT || BPOT) && !F32;  // stored distance matrix
+  constexpr bool KEEP_M = ENS == ENS_NPT || BPOT;  // stored distance matrix
+  constexpr bool PEC = pair_cache(POT, ENS);        // NVT pair cache in HBM
   const RunDesc rd = P.runs[run0 + blockIdx.x];
   const int N = rd.N, R = rd.R;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -401,22 +405,15 @@ __global__ void __launch_bounds__(1024)
     return p;
   };
   double* s_pos = (double*)carve((long long)R * N * 3 * 8);
-  float4* s_p32 = F32 ? (float4*)carve((long long)R * N * 16) : nullptr;
   double2* s_c64 = nullptr;
-  double2* s_d64 = nullptr;
-  float2* s_c32 = nullptr;
-  float2* s_d32 = nullptr;
+  double2* s_t64 = nullptr;  // EAM: the trial row's (r^-n, r^-m)
   if (POT == POT_EAM) {
-    if (F32) {
-      s_c32 = (float2*)carve((long long)R * N * 8);
-      s_d32 = (float2*)carve((long long)R * N * 8);
-    } else {
-      s_c64 = (double2*)carve((long long)R * N * 16);
-      s_d64 = (double2*)carve((long long)R * N * 16);
-    }
+    s_c64 = (double2*)carve((long long)R * N * 16);
+    s_t64 = (double2*)carve((long long)R * N * 16);
   }
-  double* s_row = KEEP_M ? (double*)carve((long long)R * N * 8) : nullptr;
-  double* s_trow = (BPOT && !F32) ? (double*)carve((long long)R * N * 8) : nullptr;
+  // trial row: squared distances (NPT, B potentials) or pair energies (NVT ELJ)
+  double* s_row = (KEEP_M || POT != POT_EAM) ? (double*)carve((long long)R * N * 8) : nullptr;
+  double* s_trow = BPOT ? (double*)carve((long long)R * N * 8) : nullptr;
   double* s_drw = (double*)carve((long long)R * DRAW_BUF * 8);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_maxbox = (double*)carve((long long)R * 8);
@@ -439,16 +436,12 @@ __global__ void __launch_bounds__(1024)
       s_ca[tid] = P.ca[tid];
       s_cb[tid] = P.cb[tid];
     }
-    s_cf[tid] = (float)P.c[tid];
   }
   const double* gpos = P.pos + rd.pos_off;
   for (int k = tid; k < R * N * 3; k += nthr) s_pos[k] = gpos[k];
   if (POT == POT_EAM) {
     const double* gc = P.comp + rd.comp_off;
-    for (int k = tid; k < R * N; k += nthr) {
-      if (F32) s_c32[k] = make_float2((float)gc[2 * k], (float)gc[2 * k + 1]);
-      else s_c64[k] = make_double2(gc[2 * k], gc[2 * k + 1]);
-    }
+    for (int k = tid; k < R * N; k += nthr) s_c64[k] = make_double2(gc[2 * k], gc[2 * k + 1]);
   }
   for (int s = tid; s < R; s += nthr) {
     int g = rd.wk + s;
@@ -468,10 +461,6 @@ __global__ void __launch_bounds__(1024)
     }
   }
   __syncthreads();
-  if (F32)
-    for (int k = tid; k < R * N; k += nthr)
-      s_p32[k] = make_float4((float)s_pos[3 * k], (float)s_pos[3 * k + 1],
-                             (float)s_pos[3 * k + 2], 0.f);
   for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
   __syncthreads();
 
@@ -486,15 +475,15 @@ __global__ void __launch_bounds__(1024)
   int status = P.status[g];
   double drift = P.drift[g];
   double* X = s_pos + (size_t)w * N * 3;
-  float4* X32 = F32 ? s_p32 + (size_t)w * N : nullptr;
   double* drw = s_drw + w * DRAW_BUF;
   double* M = KEEP_M ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
+  // NVT pair cache of this walker: ELJ V(r_ij), EAM (r_ij^-n, r_ij^-m)
+  double* PE = PEC ? P.pe + rd.pe_off + (size_t)w * N * N * (POT == POT_EAM ? 2 : 1) : nullptr;
   double* TM = BPOT ? P.tan + rd.mat_off + (size_t)w * N * N : nullptr;  // tangent matrix
   double* row = s_row ? s_row + (size_t)w * N : nullptr;
   double* trow = s_trow ? s_trow + (size_t)w * N : nullptr;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const double ean = P.eam_ean, ecam = P.eam_ecam;
-  const float hnf = (float)hn, hmf = (float)hm, eanf = (float)ean, ecamf = (float)ecam;
   const uint32_t run_word = (uint32_t)rd.run_id;
 
   // draw from this walker's stream (all lanes in lockstep)
@@ -547,7 +536,6 @@ __global__ void __launch_bounds__(1024)
             X[3 * a] -= sx;
             X[3 * a + 1] -= sy;
             X[3 * a + 2] -= sz;
-            if (F32) X32[a] = make_float4((float)X[3 * a], (float)X[3 * a + 1], (float)X[3 * a + 2], 0.f);
           }
           __syncwarp();
           xi = X[3 * i];
@@ -577,8 +565,7 @@ __global__ void __launch_bounds__(1024)
     }
 
     double new_en;
-    double sa = 0.0, sb = 0.0;  // EAM FP64: sum of component deltas of atom i
-    float saf = 0.f, sbf = 0.f;
+    double sa = 0.0, sb = 0.0;  // EAM: sum of component deltas of atom i
     if (BPOT) {  // energy_update! for the B potentials (src/EnergyEvaluation.jl:1508-1564)
       double e_n = 0.0, e_o = 0.0;
       const double* Mi = M + (size_t)i * N;
@@ -601,107 +588,66 @@ __global__ void __launch_bounds__(1024)
       e_o = warp_sum(e_o);
       new_en = (e_n - e_o) + en;
     } else if (POT == POT_ELJ || POT == POT_ELJEVEN) {
-      if (!F32) {  // dimer_energy_update! (src/EnergyEvaluation.jl:804-821)
-        double e_n = 0.0, e_o = 0.0;
-        const double* Mi = M ? M + (size_t)i * N : nullptr;
-        for (int j = lane; j < N; j += 32) {
-          if (j == i) {
-            if (row) row[j] = 0.0;
-            continue;
-          }
-          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
-          double dol = Mi ? Mi[j] : pd2<BC>(xi, yi, zi, X + 3 * j, L, H);
-          if (ENS == ENS_NPT) {
-            row[j] = dn;
-            if (dn <= rc2) e_n += v64<POT>(s_c, K, dn);
-            if (dol <= rc2) e_o += v64<POT>(s_c, K, dol);
-          } else {
-            e_n += v64<POT>(s_c, K, dn);
-            e_o += v64<POT>(s_c, K, dol);
-          }
+      // dimer_energy_update! (src/EnergyEvaluation.jl:804-821)
+      double e_n = 0.0, e_o = 0.0;
+      const double* Mi = M ? M + (size_t)i * N : nullptr;
+      const double* Ei = PE ? PE + (size_t)i * N : nullptr;
+      for (int j = lane; j < N; j += 32) {
+        if (j == i) {
+          row[j] = 0.0;
+          continue;
         }
-        e_n = warp_sum(e_n);
-        e_o = warp_sum(e_o);
-        new_en = (e_n - e_o) + en;
-      } else {
-        const float Lf = (float)L, iLf = (float)(1.0 / L), rcf = (float)rc2;
-        float4 t4 = make_float4((float)tx, (float)ty, (float)tz, 0.f);
-        float4 x4 = X32[i];
-        float de = 0.f;
-        for (int j = lane; j < N; j += 32) {
-          if (j == i) continue;
-          float4 b = X32[j];
-          float dn = pf2<BC>(t4, b, Lf, iLf);
-          float dol = pf2<BC>(x4, b, Lf, iLf);
-          if (ENS == ENS_NPT) {
-            if (dn <= rcf) de += v32<POT>(s_cf, K, dn);
-            if (dol <= rcf) de -= v32<POT>(s_cf, K, dol);
-          } else {
-            de += v32<POT>(s_cf, K, dn) - v32<POT>(s_cf, K, dol);
-          }
+        const double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
+        if (ENS == ENS_NPT) {
+          const double dol = Mi[j];
+          row[j] = dn;
+          if (dn <= rc2) e_n += v64<POT>(s_c, K, dn);
+          if (dol <= rc2) e_o += v64<POT>(s_c, K, dol);
+        } else if (PEC) {  // trial pair energies; the old ones from the cache
+          const double vn = v64<POT>(s_c, K, dn);
+          row[j] = vn;
+          e_n += vn;
+          e_o += Ei[j];
+        } else {  // RectangularBC / RhombicBC in NVT: old distances from positions
+          e_n += v64<POT>(s_c, K, dn);
+          e_o += v64<POT>(s_c, K, pd2<BC>(xi, yi, zi, X + 3 * j, L, H));
         }
-        de = warp_sum(de);
-        new_en = en + (double)de;
       }
+      e_n = warp_sum(e_n);
+      e_o = warp_sum(e_o);
+      new_en = (e_n - e_o) + en;
     } else {  // EAM energy_update! (src/EnergyEvaluation.jl:1567-1591)
-      if (!F32) {
-        double2* C = s_c64 + (size_t)w * N;
-        double2* D = s_d64 + (size_t)w * N;
-        for (int j = lane; j < N; j += 32) {
-          if (j == i) {
-            D[j] = make_double2(0.0, 0.0);
-            continue;
-          }
-          double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
-          double dol = pd2<BC>(xi, yi, zi, X + 3 * j, L, H);
-          double a1, b1, a0, b0;
-          invrexp64(dn, hn, hm, a1, b1);
-          invrexp64(dol, hn, hm, a0, b0);
-          double da = a1 - a0, db = b1 - b0;
-          D[j] = make_double2(da, db);
-          sa += da;
-          sb += db;
+      // calc_components (:1105-1148): the trial row's (r^-n, r^-m); the old
+      // ones from the pair cache
+      double2* C = s_c64 + (size_t)w * N;
+      double2* T2 = s_t64 + (size_t)w * N;
+      const double2* Ei = (const double2*)PE + (size_t)i * N;
+      for (int j = lane; j < N; j += 32) {
+        if (j == i) {
+          T2[j] = make_double2(0.0, 0.0);
+          continue;
         }
-        sa = warp_sum(sa);
-        sb = warp_sum(sb);
-        __syncwarp();
-        double e = 0.0;  // calc_energies_from_components (:1156-1162)
-        for (int k = lane; k < N; k += 32) {
-          double2 c = C[k];
-          double2 d = (k == i) ? make_double2(sa, sb) : D[k];
-          e += ean * (c.x + d.x) - ecam * sqrt(c.y + d.y);
-        }
-        new_en = warp_sum(e);
-      } else {
-        const float Lf = (float)L, iLf = (float)(1.0 / L);
-        float2* C = s_c32 + (size_t)w * N;
-        float2* D = s_d32 + (size_t)w * N;
-        float4 t4 = make_float4((float)tx, (float)ty, (float)tz, 0.f);
-        float4 x4 = X32[i];
-        float de = 0.f;
-        for (int j = lane; j < N; j += 32) {
-          if (j == i) continue;
-          float4 b = X32[j];
-          float ln_ = lg2f(pf2<BC>(t4, b, Lf, iLf));
-          float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
-          float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
-          float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
-          D[j] = make_float2(da, db);
-          saf += da;
-          sbf += db;
-          float2 c = C[j];
-          // sqrt(rho+d) - sqrt(rho) in the cancellation-free form
-          float s0 = sqrtf_approx(c.y), s1 = sqrtf_approx(c.y + db);
-          de += eanf * da - ecamf * __fdividef(db, s0 + s1);
-        }
-        saf = warp_sum(saf);
-        sbf = warp_sum(sbf);
-        de = warp_sum(de);
-        float2 ci = C[i];
-        float s0 = sqrtf_approx(ci.y), s1 = sqrtf_approx(ci.y + sbf);
-        de += eanf * saf - ecamf * __fdividef(sbf, s0 + s1);
-        new_en = en + (double)de;
+        double dn = pd2<BC>(tx, ty, tz, X + 3 * j, L, H);
+        double a1, b1;
+        invrexp64(dn, hn, hm, a1, b1);
+        const double2 o = Ei[j];
+        T2[j] = make_double2(a1, b1);
+        sa += a1 - o.x;
+        sb += b1 - o.y;
       }
+      sa = warp_sum(sa);
+      sb = warp_sum(sb);
+      double e = 0.0;  // calc_energies_from_components (:1156-1162)
+      for (int k = lane; k < N; k += 32) {  // lane k reads only what lane k wrote
+        double2 c = C[k];
+        double2 d = make_double2(sa, sb);
+        if (k != i) {
+          const double2 t = T2[k], o = Ei[k];
+          d = make_double2(t.x - o.x, t.y - o.y);
+        }
+        e += ean * (c.x + d.x) - ecam * sqrt(c.y + d.y);
+      }
+      new_en = warp_sum(e);
     }
 
     // acc_test! / metropolis_condition (src/MCRun.jl:122-132, Exchange.jl:53-57)
@@ -715,7 +661,6 @@ __global__ void __launch_bounds__(1024)
       X[3 * i] = tx;
       X[3 * i + 1] = ty;
       X[3 * i + 2] = tz;
-      if (F32) X32[i] = make_float4((float)tx, (float)ty, (float)tz, 0.f);
     }
     if (M) {
       for (int j = lane; j < N; j += 32) {
@@ -729,22 +674,27 @@ __global__ void __launch_bounds__(1024)
       }
     }
     if (POT == POT_EAM) {  // swap_vars! EAM (src/swap_config.jl:208-211)
-      if (!F32) {
-        double2* C = s_c64 + (size_t)w * N;
-        const double2* D = s_d64 + (size_t)w * N;
-        for (int k = lane; k < N; k += 32) {
-          double2 d = (k == i) ? make_double2(sa, sb) : D[k];
-          double2 c = C[k];
-          C[k] = make_double2(c.x + d.x, c.y + d.y);
+      double2* C = s_c64 + (size_t)w * N;
+      const double2* T2 = s_t64 + (size_t)w * N;
+      double2* PE2 = (double2*)PE;
+      for (int k = lane; k < N; k += 32) {
+        double2 c = C[k];
+        if (k == i) {
+          C[k] = make_double2(c.x + sa, c.y + sb);
+          continue;
         }
-      } else {
-        float2* C = s_c32 + (size_t)w * N;
-        const float2* D = s_d32 + (size_t)w * N;
-        for (int k = lane; k < N; k += 32) {
-          float2 d = (k == i) ? make_float2(saf, sbf) : D[k];
-          float2 c = C[k];
-          C[k] = make_float2(c.x + d.x, c.y + d.y);
-        }
+        // each lane reads its old cache entries before it overwrites them
+        const double2 t = T2[k], o = PE2[(size_t)i * N + k];
+        C[k] = make_double2(c.x + (t.x - o.x), c.y + (t.y - o.y));
+        PE2[(size_t)i * N + k] = t;  // pair cache: row and column of atom i
+        PE2[(size_t)k * N + i] = t;
+      }
+    } else if (PEC) {
+      for (int j = lane; j < N; j += 32) {
+        if (j == i) continue;
+        const double v = row[j];
+        PE[(size_t)i * N + j] = v;
+        PE[(size_t)j * N + i] = v;
       }
     }
     en = new_en;
@@ -817,7 +767,7 @@ __global__ void __launch_bounds__(1024)
       }
     };
     double e = 0.0;
-    if (!F32 && !sep) {
+    if (!sep) {
       for (int i = 0; i < N; ++i)
         for (int j = i + 1 + lane; j < N; j += 32) {
           double x = M[(size_t)i * N + j] * s2;
@@ -850,29 +800,24 @@ __global__ void __launch_bounds__(1024)
       X[3 * a + 2] = X[3 * a + 2] * fz;
     }
     __syncwarp();
-    if (!F32) {
-      if (sep) {  // get_distance2_mat! of the accepted configuration
-        for (int i = 0; i < N; ++i) {
-          for (int j = i + 1 + lane; j < N; j += 32) {
-            double x = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
-            M[(size_t)i * N + j] = x;
-            M[(size_t)j * N + i] = x;
-            if (BPOT && kind != 0) {  // tangents of z / xy moves
-              double t = ptan<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
-              TM[(size_t)i * N + j] = t;
-              TM[(size_t)j * N + i] = t;
-            }
+    if (sep) {  // get_distance2_mat! of the accepted configuration
+      for (int i = 0; i < N; ++i) {
+        for (int j = i + 1 + lane; j < N; j += 32) {
+          double x = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
+          M[(size_t)i * N + j] = x;
+          M[(size_t)j * N + i] = x;
+          if (BPOT && kind != 0) {  // tangents of z / xy moves
+            double t = ptan<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * j, Ln, Hn);
+            TM[(size_t)i * N + j] = t;
+            TM[(size_t)j * N + i] = t;
           }
-          if (lane == 0) M[(size_t)i * N + i] = 0.0;
         }
-      } else {
-        for (int k = lane; k < N * N; k += 32) M[k] = M[k] * s2;
+        if (lane == 0) M[(size_t)i * N + i] = 0.0;
       }
+    } else {
+      for (int k = lane; k < N * N; k += 32) M[k] = M[k] * s2;
     }
     __syncwarp();
-    if (F32)
-      for (int a = lane; a < N; a += 32)
-        X32[a] = make_float4((float)X[3 * a], (float)X[3 * a + 1], (float)X[3 * a + 2], 0.f);
     L = Ln;
     H = Hn;
     rc2 = rcn;
@@ -903,14 +848,6 @@ __global__ void __launch_bounds__(1024)
           acc_z += v == 3;
         }
         if (status != ST_OK) break;
-      }
-      if (F32 && P.resync_every > 0 && idx % P.resync_every == 0) {
-        double e64 = walker_energy64<POT, BC, ENS>(
-            X, N, L, H, rc2, s_c, K, hn, hm, ean, ecam, nullptr, nullptr,
-            POT == POT_EAM ? s_c32 + (size_t)w * N : nullptr, lane);
-        drift = fmax(drift, fabs(en - e64));
-        en = e64;
-        __syncwarp();
       }
     }
     if (lane == 0) {
@@ -1028,13 +965,8 @@ __global__ void __launch_bounds__(1024)
   if (POT == POT_EAM) {
     double* gc = P.comp + rd.comp_off;
     for (int k = tid; k < R * N; k += nthr) {
-      if (F32) {
-        gc[2 * k] = s_c32[k].x;
-        gc[2 * k + 1] = s_c32[k].y;
-      } else {
-        gc[2 * k] = s_c64[k].x;
-        gc[2 * k + 1] = s_c64[k].y;
-      }
+      gc[2 * k] = s_c64[k].x;
+      gc[2 * k + 1] = s_c64[k].y;
     }
   }
   if (lane == 0) {
@@ -1099,24 +1031,28 @@ static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
   if constexpr (F32) {
     if (what == 0) return (int)cudaErrorInvalidValue;  // FP32 form: ptmc_cycles32.cu
   } else if (what == 0) {
-    long long smem = cycles_smem_bytes(POT, ENS, F32, R, maxN);
+    long long smem = cycles_smem_bytes(POT, ENS, false, R, maxN);
     // opt in to more than 48 KB of dynamic shared memory when needed, within
-    // the device limit minus the kernel's static shared memory
-    static long long attr_set = 48 * 1024;
-    if (smem > attr_set) {
-      int dev = 0, optin = 0;
-      cudaGetDevice(&dev);
+    // the device limit minus the kernel's static shared memory; the attribute
+    // belongs to the current device's context, so it is recorded per device
+    static long long attr_set[MAX_DEVICES] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= MAX_DEVICES) return (int)cudaErrorInvalidDevice;
+    if (smem > 48 * 1024 && smem > attr_set[dev]) {
+      int optin = 0;
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
       cudaFuncAttributes fa;
-      cudaError_t e = cudaFuncGetAttributes(&fa, k_cycles<POT, BC, ENS, F32>);
+      e = cudaFuncGetAttributes(&fa, k_cycles<POT, BC, ENS>);
       if (e != cudaSuccess) return (int)e;
       if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
-      e = cudaFuncSetAttribute(k_cycles<POT, BC, ENS, F32>,
+      e = cudaFuncSetAttribute(k_cycles<POT, BC, ENS>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return (int)e;
-      attr_set = smem;
+      attr_set[dev] = smem;
     }
-    k_cycles<POT, BC, ENS, F32><<<grid, block, (size_t)smem, st>>>(P, run0, ncycles, phase);
+    k_cycles<POT, BC, ENS><<<grid, block, (size_t)smem, st>>>(P, run0, ncycles, phase);
     return (int)cudaGetLastError();
   }
   if (what == 1) {

@@ -9,6 +9,8 @@
 //                                 squared-distance matrix
 //   tan   f64 [same as mat]       B potentials: |tan| of the pair angle to z
 //   comp  f64 [sum_r R_r*N_r*2]   EAM (phi_i, rho_i) components
+//   pe    f64 [sum_r R_r*N_r*N_r*w] plain form, NVT: pair cache (w = 1 ELJ V(r_ij),
+//                                 w = 2 EAM (r_ij^-n, r_ij^-m))
 //   en/box/rc2/drift f64 [W], ctr u64 [W], status i32 [W]   per walker
 //   boxh f64 [W]  box height (RectangularBC / RhombicBC)     per walker
 //   beta/maxbox f64 [W], maxd f64 [2W], ham f64 [2W], cnt i64 [6W],
@@ -28,6 +30,11 @@ enum { POT_ELJ = 0, POT_ELJEVEN = 1, POT_EAM = 2, POT_NN = 3, POT_ELJB = 4, POT_
 __host__ __device__ constexpr bool pot_b(int pot) { return pot == POT_ELJB || pot == POT_LUT; }
 enum { BC_SPH = 0, BC_CUB = 1, BC_RECT = 2, BC_RHB = 3 };  // RECT/RHB: length L, height H
 enum { ENS_NVT = 0, ENS_NPT = 1 };
+// the plain form keeps an NVT pair cache (pair energies in HBM) for the ELJ
+// and EAM potentials; NPT and the angle-dependent potentials keep distances
+__host__ __device__ constexpr bool pair_cache(int pot, int ens) {
+  return ens == ENS_NVT && (pot == POT_ELJ || pot == POT_ELJEVEN || pot == POT_EAM);
+}
 enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
 // TIMEOUT: a bounded tensor-core wait ran out; XWAIT: a bounded wait for an
 // exchange partner ran out
@@ -35,6 +42,8 @@ enum { ST_OK = 0, ST_SPHERE = 1, ST_TIMEOUT = 2, ST_XWAIT = 3 };
 constexpr int MAX_COEFF = 16;
 constexpr int MAX_REPLICAS = 32;
 constexpr int DRAW_BUF = 16;
+// devices whose per-kernel attributes (shared-memory opt-in) are tracked
+constexpr int MAX_DEVICES = 64;
 
 struct RunDesc {
   int N, R;                 // atoms, replicas
@@ -51,7 +60,7 @@ struct RunDesc {
   long long cyc[3];         // next cycle index (1-based) per phase
   unsigned long long run_ctr;  // run-level draw counter
   double dr2;               // radial-distribution bin width in r^2 (Sampling.jl:151,185)
-  double pad1;
+  long long pe_off;         // element offset of walker 0 in pe (plain form, NVT pair cache)
 };
 
 // update_rdf! (src/Sampling.jl:282, 301-316): bin = floor(r2 / delta_r2), kept
@@ -69,6 +78,11 @@ struct KParams {
   double* pos;
   double* mat;
   double* comp;
+  float* lo;                // FP32 form, 4 or 8 lanes per walker: lo halves of the
+                            // float-float positions during a launch, float4 per
+                            // atom at (pos_off / 3 + walker * N)
+  double* pe;               // plain form, NVT: pair cache, ELJ N x N V(r_ij) or EAM
+                            // N x N (r_ij^-n, r_ij^-m) per walker (see pair_cache)
   double* en;
   double* box;
   double* rc2;
@@ -112,7 +126,21 @@ struct KParams {
   // expression, and an FP64 -> FP32 conversion issues to the FP64 pipe.
   float f_hn, f_hm, f_ean, f_ecam;  // -n/2, -m/2, ean, eCam
   float cf[MAX_COEFF];              // ELJ coefficients in FP32 (constant-bank operands)
+  // bounded exchange-partner waits of the FP32 form: the limit in clocks, and
+  // a test switch that makes every such wait target a flag value nobody writes
+  long long xwait_clocks;
+  int xwait_never;
 };
+// default limit of an exchange-partner wait (~4 s at 2 GHz; legitimate waits
+// last a few cycles)
+constexpr long long XWAIT_CLOCKS = 1ll << 33;
+
+// walker stride (atoms) of the FP32 form's shared position array with 4 or 8
+// lanes per walker: stride = lpr mod 2 lpr, so that the walkers read by one
+// 128-byte shared-memory wavefront fall into disjoint banks
+__host__ __device__ inline int narrow_stride(int N, int lpr) {
+  return (N + lpr - 1) / (2 * lpr) * (2 * lpr) + lpr;
+}
 
 // shared-memory bytes of one run CTA
 inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
@@ -122,9 +150,10 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
   if (f32) b += al((long long)R * N * 16);           // FP32 positions (float4)
   if (pot == POT_EAM) {
     b += al((long long)R * N * (f32 ? 8 : 16));      // components
-    b += al((long long)R * N * (f32 ? 8 : 16));      // per-move deltas
+    b += al((long long)R * N * (f32 ? 8 : 16));      // per-move trial pair terms
   }
-  if ((ens == ENS_NPT || pot_b(pot)) && !f32) b += al((long long)R * N * 8);  // trial row
+  if ((ens == ENS_NPT || pot_b(pot) || pot != POT_EAM) && !f32)
+    b += al((long long)R * N * 8);                   // trial row (distances or pair energies)
   if (pot_b(pot) && !f32) b += al((long long)R * N * 8);    // trial tangent row
   b += al((long long)R * DRAW_BUF * 8);              // draw buffers
   b += al((long long)R * 8) * 6;                     // beta, maxbox, en, box, ham(2)
@@ -142,6 +171,11 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
 // kernel launch entry points (ptmc_cycles.cu, ptmc_cycles32.cu)
 namespace ptmc {
 long long cycles32_smem_bytes(int pot, int R, int N, int ncta);
+// FP32 form with lpr = 4 or 8 lanes per walker (NVT, one CTA of R * lpr
+// threads per run, ptmc_cycles32n.cu)
+long long cycles32n_smem_bytes(int pot, int R, int N, int lpr);
+int launch_cycles32n(int pot, int bc, const KParams& P, int run0, int nruns, int R, int maxN,
+                     int ncycles, int phase, int lpr, void* stream);
 // ncta: CTAs per run (a thread-block cluster when > 1; FP32 form only)
 // lpr: lanes per walker (32 or 16; FP32 form only)
 int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,

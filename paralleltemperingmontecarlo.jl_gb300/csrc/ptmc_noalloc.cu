@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <mutex>
+#include <string>
 
 #include "../../include/ptmc_gb300.h"
 #include "ptmc_engine.cuh"
@@ -46,6 +47,13 @@ __global__ void k_tgrid(const double* t_grid, int R, int n_out, double* tb, doub
   T_out[i] = T;
 }
 
+// every failure return names the entry point in the global last error
+// (ptmc_last_error(NULL)), as the allocating entry points do
+int fail(int code, const std::string& msg) {
+  ptmc::set_last_error("ptmc_multihist_nvt_noalloc: " + msg);
+  return code;
+}
+
 }  // namespace
 
 extern "C" int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist,
@@ -54,19 +62,33 @@ extern "C" int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist
                                           double* d_T_out, double* d_cv_out, int* d_iters,
                                           void* stream) {
   if (R < 1 || n_bin < 1 || !d_hist || !d_t_grid || !d_beta || !d_T_out || !d_cv_out || !d_iters)
-    return PTMC_ERR_ARG;
+    return fail(PTMC_ERR_ARG, "need R >= 1, n_bin >= 1 and non-null device buffers");
   const long long n_out = 10LL * R;
   const long long need = ptmc::wham_work_doubles(R, n_bin) + 2 * n_out;
-  if (need > PTMC_NOALLOC_SCRATCH_DOUBLES) return PTMC_ERR_LIMIT;
+  if (need > PTMC_NOALLOC_SCRATCH_DOUBLES)
+    return fail(PTMC_ERR_LIMIT, "R = " + std::to_string(R) + ", n_bin = " + std::to_string(n_bin) +
+                                    " need " + std::to_string(need) + " scratch doubles, the fixed array holds " +
+                                    std::to_string(PTMC_NOALLOC_SCRATCH_DOUBLES));
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PTMC_ERR_CUDA;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(PTMC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail(PTMC_ERR_CUDA, "device ordinal beyond 63");
+  // An error left pending by an earlier launch of the caller's is reported,
+  // not consumed: the launch checks below would otherwise read (and clear) it
+  // as if this call had caused it.
+  e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return fail(PTMC_ERR_CUDA, std::string("a CUDA error was pending before the call (left for the caller): ") +
+                                   cudaGetErrorString(e));
   double* base;
   {
     // once per device, with that device current: the array's device address
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_scratch_ptr[dev]) {
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_wham_scratch) != cudaSuccess || !p) return PTMC_ERR_CUDA;
+      e = cudaGetSymbolAddress(&p, g_wham_scratch);
+      if (e != cudaSuccess || !p)
+        return fail(PTMC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       g_scratch_ptr[dev] = (double*)p;
     }
     base = g_scratch_ptr[dev];
@@ -75,8 +97,11 @@ extern "C" int ptmc_multihist_nvt_noalloc(int R, int n_bin, const double* d_hist
   double* tb = base + ptmc::wham_work_doubles(R, n_bin);
   cudaStream_t st = (cudaStream_t)stream;
   k_tgrid<<<(int)((n_out + 127) / 128), 128, 0, st>>>(d_t_grid, R, (int)n_out, tb, d_T_out);
-  if (cudaGetLastError() != cudaSuccess) return PTMC_ERR_CUDA;
+  e = cudaGetLastError();  // nothing was pending, so an error here is this launch's
+  if (e != cudaSuccess) return fail(PTMC_ERR_CUDA, std::string("k_tgrid launch: ") + cudaGetErrorString(e));
   int rc = ptmc::wham_nvt_device(R, n_bin, d_hist, d_beta, en_min, en_max, thr, tb, (int)n_out,
                                  work, d_cv_out, d_iters, stream);
-  return rc == 0 ? PTMC_OK : PTMC_ERR_CUDA;
+  if (rc != 0)
+    return fail(PTMC_ERR_CUDA, std::string("k_wham launch: ") + cudaGetErrorString((cudaError_t)rc));
+  return PTMC_OK;
 }

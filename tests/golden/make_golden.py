@@ -1,8 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own files.
 
-Run once, in a container where the reference checkout exists:
+Run once, in a container where the reference checkout exists, with the path
+of that checkout (the ParallelTemperingMonteCarlo.jl package root):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference package root>
 
 Outputs (committed, small):
   multihist_nvt.json  — the NVT Output literal and expected Cv values embedded in
@@ -200,7 +201,9 @@ def lookup_table(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py <reference package root>")
+    ref = sys.argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     nvt, npt = multihist(ref)
     json.dump(nvt, open(os.path.join(here, "multihist_nvt.json"), "w"))

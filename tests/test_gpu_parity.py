@@ -355,3 +355,73 @@ def test_gpu_linear_multihistogram(pk, orc, tmp_path):
     a = np.loadtxt(os.path.join(wd, "analysis.NVT"), skiprows=1)
     np.testing.assert_allclose(a[:, 2], Cv, rtol=1e-12)
     assert np.all(np.isfinite(Cv)) and Cv.max() > 0 and len(hd) == 8
+
+
+# ------------------------------------------------------------------
+# The benchmarked configurations at their benched sizes (plain FP64 form)
+
+def test_batched_uneven_benched_sizes(pk, orc):
+    """The batched uneven-N workload's atom counts N in {13, 38, 55, 101, 147}
+    (2 runs each, R = 16, sphere starts of radius 0.9 N^(1/3) 3 bohr in a
+    container 3 bohr wider), in one context: one launch group per N on forked
+    streams, chunks of 3 cycles replayed from a CUDA graph (8 chunks per
+    replay).  N = 101 and 147 need the shared-memory opt-in of the FP64 form."""
+    sizes = [13, 38, 55, 101, 147] * 2
+    R = 16
+    starts = [sphere_start(n, 0.9 * n ** (1 / 3) * 3, 4.3, 500 + k) for k, n in enumerate(sizes)]
+    radii = [0.9 * n ** (1 / 3) * 3 + 3.0 for n in sizes]
+    mp = pk.MCParams(mc_cycles=1000, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=13)
+    temp = pk.TempGrid(4.0, 16.0, R)
+    pot = pk.ELJPotentialEven(C_NE)
+    eng = pk.Engine(mp, temp, pot, pk.NVT(13), n_runs=len(sizes), exch_prob=1.0, seed=77,
+                    cycles_per_launch=3)
+    os_ = []
+    for r, (x, rad) in enumerate(zip(starts, radii)):
+        eng.set_configs(r, pk.Config(x, pk.SphericalBC(rad)))
+        o = orc.Run(len(x), R, np.stack([x] * R), temp.t_grid, bc=orc.BC_SPHERE, bc_param=rad,
+                    exch_prob=1.0, seed=77, run_index=r)
+        o.set_elj(C_NE, True)
+        o.init()
+        os_.append(o)
+    eng.init()
+    n = 3 * 8 * 2 + 5          # two graph replays and a remainder of 5 cycles
+    eng.cycles_nosample(n)
+    assert eng.stats()["graph_launches"] == 2
+    for r, o in enumerate(os_):
+        o.cycles(1, n)
+        g = compare(eng, o, run=r)
+        assert g["counts"][:, 0].sum() > 0
+    eng.close()
+
+
+def test_cu55_eam_fp64_parity_r32(pk, orc):
+    """Cu55 EAM with the benched replica count, R = 32 over 200-1000 K, one
+    exchange attempted every cycle."""
+    pot = pk.EmbeddedAtomPotential(**CU_EAM)
+    eng, (o,) = pair(pk, orc, N=55, R=32, x0=cu55_ico(), T0=200.0, T1=1000.0, pot=pot,
+                     bc_param=14.0, exch_prob=1.0, seed=12)
+    eng.cycles_nosample(40)
+    o.cycles(1, 40)
+    g = compare(eng, o)
+    assert g["counts"][:, 5].sum() > 0, "some exchanges accepted"
+    eng.close()
+
+
+def test_ne108_npt_fp64_parity(pk, orc):
+    """Bulk Ne NPT at the benched size: 108 atoms (fcc 3x3x3, a = 8.4 bohr,
+    0.05 bohr jitter) in CubicBC(25.2), R = 32 over 10-40 K, 1 atm; volume moves
+    (one slot in N + 1), equilibration and production with the E x V histogram."""
+    x0 = fcc(3, 8.4, 0.05, 7)
+    p = 101325 * 3.398928944382626e-14
+    eng, (o,) = pair(pk, orc, N=108, R=32, x0=x0, T0=10.0, T1=40.0, pot=pk.ELJPotentialEven(C_NE),
+                     ens="npt", bc_param=25.2, exch_prob=1.0, seed=9, pressure=p, eq=20)
+    eng.equilibrate()
+    o.equilibrate(20)
+    eng.run_cycles(30)
+    o.production(1, 30)
+    g = compare(eng, o, positions_exact=False)
+    assert g["counts"][:, 2].sum() > 0, "some volume moves accepted"
+    out = eng.output(0)
+    _, ev, hp = o.hist()
+    assert np.array_equal(out.ev_histogram, ev)
+    eng.close()

@@ -57,3 +57,8 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(pk):
     # 3R + 3 n_bin + 20R + 2 > 16384 doubles
     rc = L.ptmc_multihist_nvt_noalloc(32, 6000, 1, 1, 1, -1.0, 0.0, 1e-3, 1, 1, 1, None)
     assert rc == -6
+    msg = L.ptmc_last_error(None).decode()
+    assert "ptmc_multihist_nvt_noalloc" in msg and "16384" in msg, msg
+    rc = L.ptmc_multihist_nvt_noalloc(0, 100, 1, 1, 1, -1.0, 0.0, 1e-3, 1, 1, 1, None)
+    assert rc == -1
+    assert "ptmc_multihist_nvt_noalloc" in L.ptmc_last_error(None).decode()
