@@ -181,7 +181,7 @@ def start_configs(W, B):
 
 
 def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=None, xyz=None,
-                eq_cycles=0):
+                eq_cycles=0, init=True):
     """Engine of B runs of workload W.  `starts`: per run, the slot-ordered
     states of an earlier engine (configurations and step sizes) to start from;
     `xyz`: per run, a host start configuration made beforehand; `eq_cycles`:
@@ -212,8 +212,42 @@ def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=Non
         else:
             st = starts[r]
             eng.set_configs(r, [pk.Config(x, bc) for x in st["xyz"]], max_displ=st["max_displ"])
-    eng.init()
+    if init:
+        eng.init()
     return eng, sizes
+
+
+def fill_batch(pk, W, form, n_sm, cycles, seed, device):
+    """Runs per batch and FP32 launch shape for a workload of one atom count:
+    every candidate shape gets the batch that fills the GPU in whole waves
+    (ptmc_occupancy x SMs), a short untimed trial of that batch, and the best
+    rate wins.  Returns (runs, (C, L) or None, record)."""
+    N, R = W["sizes"](1)[0], W["R"]
+    probe, _ = make_engine(pk, W, 1, form, cycles, seed, device, init=False)
+    if form == "fp64":
+        occ = probe.occupancy(N)
+        probe.close()
+        return max(1, occ) * n_sm, None, {"ctas_per_sm": occ}
+    shapes = [(1, 32), (1, 16)] + ([(1, 8), (1, 4)] if W["ens"] == "nvt" and N <= 64 else [])
+    trials = {}
+    for C, L in shapes:
+        if (R // C) % (32 // L):
+            continue
+        occ = probe.occupancy(N, C, L)
+        if occ < 1:
+            continue
+        B = occ * n_sm // C
+        eng, sizes = make_engine(pk, W, B, form, cycles, seed, device)
+        eng.set_launch_shape(N, C, L)
+        eng.cycles_nosample(4)
+        eng.cycles_nosample(20)
+        rate = B * R * N * 20 / (eng.stats()["last_cycles_ms"] / 1e3)
+        eng.close()
+        trials["%d,%d" % (C, L)] = dict(ctas_per_sm=occ, runs=B, trial_rate=rate)
+    probe.close()
+    best = max(trials, key=lambda k: trials[k]["trial_rate"])
+    C, L = (int(v) for v in best.split(","))
+    return trials[best]["runs"], (C, L), {"shape": best, "trials": trials}
 
 
 def flush_l2(torch, dev):
@@ -297,10 +331,10 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
     seed = 1234 + 7919 * rank
     res = {}
 
-    def timed(eng, form, sizes, cyc, k_steps):
+    def timed(eng, form, sizes, cyc, k_steps, nruns=B):
         """k_steps timed production steps of `eng` (barrier + synchronize on both sides)."""
         st0 = eng.stats()
-        acc0 = _accepted(eng, B)
+        acc0 = _accepted(eng, nruns)
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
@@ -323,8 +357,8 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
             moves_all = float(m.item())
         else:
             moves_all = float(moves)
-        acc = _accepted(eng, B)
-        return dict(value=moves_all / dev_s, ms_per_step=1e3 * dev_s / k_steps, wall=wall,
+        acc = _accepted(eng, nruns)
+        return dict(value=moves_all / dev_s, runs=nruns, ms_per_step=1e3 * dev_s / k_steps, wall=wall,
                     steps=k_steps, cycles_per_step=cyc,
                     launches=st1["kernel_launches"] - st0["kernel_launches"],
                     drift=st1["max_drift"], clocks=clk.summary(), moves=moves, sizes=sizes,
@@ -367,22 +401,34 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
             eng.close()
     else:
         forms = ["fp32"] if args.only_chosen else ["fp64", "fp32"]
+        uniform = name != "batched" and not args.runs
         for form in forms:
             cyc = cycles if form == "fp32" else pcycles
             k_steps = steps if form == "fp32" else 3
             k_warm = warmup if form == "fp32" else 3
-            eng, sizes = make_engine(pk, W, B, form, cyc, seed, args.local_rank,
+            Bf, shape, fill = B, None, None
+            if args.shape and form == "fp32":
+                shape = tuple(int(v) for v in args.shape.split(","))
+            elif uniform:  # the batch that fills the GPU in whole waves (untimed set-up)
+                t0 = time.perf_counter()
+                Bf, shape, fill = fill_batch(pk, W, form, n_sm, cyc, seed, args.local_rank)
+                fill["fill_s"] = round(time.perf_counter() - t0, 3)
+            eng, sizes = make_engine(pk, W, Bf, form, cyc, seed, args.local_rank,
                                      eq_cycles=2 * k_warm * cyc)
             shapes = None
-            if form == "fp32" and not args.no_tune:
+            t0 = time.perf_counter()
+            if shape is not None:
+                eng.set_launch_shape(sizes[0], *shape)
+                shapes = {sizes[0]: shape}
+            elif form == "fp32" and not args.no_tune:
                 # launch shape per atom count, untimed set-up; the autotuner
                 # restores the chain after its trials
-                t0 = time.perf_counter()
                 shapes = eng.autotune(trial_cycles=max(2, min(20, cyc // 4)),
                                       cache=os.path.join(args.outdir, "autotune_r%d.json" % rank))
-                tune_s = time.perf_counter() - t0
+            tune_s = time.perf_counter() - t0
             eng.equilibrate()           # the warm-up: k_warm steps' worth of cycles
-            res[form] = timed(eng, form, sizes, cyc, k_steps)
+            res[form] = timed(eng, form, sizes, cyc, k_steps, Bf)
+            res[form]["fill"] = fill
             if shapes is not None:
                 res[form]["launch_shapes"] = {
                     "ctas_per_run": {str(k): v[0] for k, v in sorted(shapes.items())},
@@ -403,7 +449,7 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
     fresh = prof is not None and prof["src_sha"] == kernel_sha()
     roof = {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
             "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"],
-            "traffic": prof["dram_bytes_per_run"] * B if fresh else None,
+            "traffic": prof["dram_bytes_per_run"] * ch["runs"] if fresh else None,
             "peak_source": "measured in-situ by ptmc_measure_peaks (FFMA chains)",
             "ops_per_pair": W["flops_pair"], "mufu_per_pair": W["mufu_pair"],
             "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"],
@@ -412,14 +458,18 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
         roof["counters_note"] = "ncu counters predate kernel source %s; not reported" % kernel_sha()
     rec = {"workload": W["name"], "value": ch["value"], "unit": "atom-moves/s",
            "ms_per_step": ch["ms_per_step"], "steps": ch["steps"],
-           "cycles_per_step": ch["cycles_per_step"], "runs": B, "replicas": W["R"],
+           "cycles_per_step": ch["cycles_per_step"], "runs": ch["runs"], "replicas": W["R"],
            "atoms": sorted(set(sizes)), "path": "production (ptmc_run_cycles: E, E^2, histograms)",
            "form": "fp32resync_batched" + ("_da" if chosen == "fp32_da" else ""),
-           "launch_shapes": ch.get("launch_shapes"), "acceptance": ch["acceptance"],
-           "fp32_max_drift_eh": ch["drift"], "gpu_launches": ch["launches"],
+           "launch_shapes": ch.get("launch_shapes"), "batch_fill": ch.get("fill"),
+           "acceptance": ch["acceptance"],
+           # largest |E_running - E_fp64| at a resync so far (null: no resync yet)
+           "fp32_max_drift_eh": ch["drift"] if ch["drift"] > 0 else None,
+           "gpu_launches": ch["launches"],
            "clocks": ch["clocks"], "roofline": roof,
            "plain_fp64": ({"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
                            "cycles_per_step": res["fp64"]["cycles_per_step"],
+                           "runs": res["fp64"]["runs"],
                            "chosen_over_plain": ch["value"] / res["fp64"]["value"]}
                           if "fp64" in res else None),
            "fp32_exact": ({"value": res["fp32"]["value"], "ms_per_step": res["fp32"]["ms_per_step"]}
@@ -432,12 +482,16 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
         # cycles, the step's production cycles, every run's energies read back
         ts = []
         h2d = d2h = 0
-        host_xyz = start_configs(W, B)   # the step's inputs, made before the clock
+        Be = ch["runs"]
+        host_xyz = start_configs(W, Be)   # the step's inputs, made before the clock
+        lshape = ch.get("launch_shapes") or {}
         for k in range(warmup + steps):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
-            eng, sizes = make_engine(pk, W, B, "fp32", cycles, 99 + k, args.local_rank,
+            eng, sizes = make_engine(pk, W, Be, "fp32", cycles, 99 + k, args.local_rank,
                                      xyz=host_xyz, eq_cycles=2)
+            for n, c_ in (lshape.get("ctas_per_run") or {}).items():  # the tuned launch shapes
+                eng.set_launch_shape(int(n), c_, lshape["lanes_per_walker"][n])
             h2d = sum(n * 3 * 8 for n in sizes)  # start configurations (one per run)
             if W.get("da"):
                 P, sur = trained
@@ -547,6 +601,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep one CTA per run (no autotuning)")
+    ap.add_argument("--shape", default="",
+                    help="C,L: force the FP32 launch shape (CTAs per run, lanes per walker); "
+                         "with --runs, no batch sizing or autotuning (profiling one kernel)")
     ap.add_argument("--atoms", type=int, default=0,
                     help="batched workload: every run with this atom count (profiling one group)")
     args = ap.parse_args()

@@ -385,6 +385,15 @@ int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run, int lanes_per_wa
 int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_path,
                   int* shape_out);
 
+/* Resident CTAs per SM of the cycle kernel for runs of N atoms in this
+ * context's form, with launch shape (C, L) in the FP32 form (ignored by the
+ * plain form): a batch of a multiple of ctas_per_sm x SMs / C runs fills the
+ * GPU in whole waves.  Pair and EAM potentials; callable before ptmc_init
+ * once the potential and the first run's configurations are set.  No
+ * counterpart in the reference (one CPU thread per replica there). */
+int ptmc_occupancy(ptmc_ctx* c, int N, int ctas_per_run, int lanes_per_walker,
+                   int* ctas_per_sm);
+
 /* Engine utility, no counterpart in the reference: measured FP32 FMA, FP64
  * FMA (TFLOP/s) and MUFU ex2 (Tops/s) peaks of `device`, the roofline
  * denominators of the replica-cycle kernels. */

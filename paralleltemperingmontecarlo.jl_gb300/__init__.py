@@ -626,6 +626,14 @@ class Engine:
                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return {int(self.N[r]): (int(out[2 * r]), int(out[2 * r + 1])) for r in range(self.n_runs)}
 
+    def occupancy(self, N, ctas_per_run=1, lanes_per_walker=32):
+        """Resident CTAs per SM of the cycle kernel for runs of N atoms with the
+        launch shape (C, L) (FP32 form; the plain form ignores the shape)."""
+        n = ctypes.c_int()
+        self._ck(self.L.ptmc_occupancy(self.h, int(N), int(ctas_per_run), int(lanes_per_walker),
+                                       ctypes.byref(n)))
+        return n.value
+
     # ---- bounded device waits
     def set_wait_test(self, clocks=0, never_set=False):
         """Exchange-partner wait limit of the FP32 form in clocks (0 = the

@@ -127,6 +127,7 @@ SIGNATURES = {
                                              ctypes.c_int]),
     "ptmc_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, _ip]),
     "ptmc_set_wait_test": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int]),
+    "ptmc_occupancy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip]),
     "ptmc_get_walker_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip]),
     "ptmc_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "ptmc_destroy": (None, [ctypes.c_void_p]),

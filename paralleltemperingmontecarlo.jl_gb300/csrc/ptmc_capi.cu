@@ -2393,3 +2393,20 @@ extern "C" int ptmc_get_walker_status(ptmc_ctx* c, int run, int* status) {
   CK(cudaStreamSynchronize(c->st));
   return PTMC_OK;
 }
+
+extern "C" int ptmc_occupancy(ptmc_ctx* c, int N, int ctas_per_run, int lanes_per_walker,
+                              int* ctas_per_sm) {
+  if (!c || !ctas_per_sm) return PTMC_ERR_ARG;
+  if (c->pot < 0) return c->fail(PTMC_ERR_STATE, "no potential set");
+  if (c->pot == POT_NN || c->pot == POT_NN2 || pot_b(c->pot))
+    return c->fail(PTMC_ERR_ARG, "ptmc_occupancy: pair and EAM potentials only");
+  if (N < 2) return c->fail(PTMC_ERR_ARG, "ptmc_occupancy: N >= 2");
+  const int bc = c->runs.empty() ? PTMC_BC_SPHERE : c->runs[0].bc;
+  *ctas_per_sm = 0;
+  int e = c->f32() ? occupancy_cycles32(c->pot, bc, c->p.ensemble, c->R(), N, ctas_per_run,
+                                        lanes_per_walker, ctas_per_sm)
+                   : occupancy_cycles(c->pot, bc, c->p.ensemble, c->R(), N, ctas_per_sm);
+  if (e < 0) return c->fail(PTMC_ERR_ARG, "ptmc_occupancy: no cycle kernel for this combination");
+  if (e) return c->cuda_fail((cudaError_t)e, "ptmc_occupancy");
+  return PTMC_OK;
+}

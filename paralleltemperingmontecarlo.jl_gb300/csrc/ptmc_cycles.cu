@@ -1024,34 +1024,46 @@ __global__ void __launch_bounds__(1024) k_resync(KParams P, int run0) {
 }
 
 // ------------------------------------------------------------ dispatch
+// opt in to more than 48 KB of dynamic shared memory when needed, within the
+// device limit minus the kernel's static shared memory; the attribute belongs
+// to the current device's context, so it is recorded per device, and it is
+// only ever raised (a later launch with more shared memory raises it again)
+template <int POT, int BC, int ENS>
+static int opt_in64(long long smem) {
+  static long long attr_set[MAX_DEVICES] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  if (dev < 0 || dev >= MAX_DEVICES) return (int)cudaErrorInvalidDevice;
+  if (smem <= 48 * 1024 || smem <= attr_set[dev]) return 0;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, k_cycles<POT, BC, ENS>);
+  if (e != cudaSuccess) return (int)e;
+  if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(k_cycles<POT, BC, ENS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  attr_set[dev] = smem;
+  return 0;
+}
+
+// what: 0 cycle kernel launch, 1 k_init, 2 k_resync, 3 occupancy query of the
+// cycle kernel (resident CTAs per SM into *occ)
 template <int POT, int BC, int ENS, bool F32>
 static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
-                        int maxN, int ncycles, int phase, cudaStream_t st) {
+                        int maxN, int ncycles, int phase, cudaStream_t st, int* occ) {
   dim3 grid(nruns), block(R * 32);
   if constexpr (F32) {
-    if (what == 0) return (int)cudaErrorInvalidValue;  // FP32 form: ptmc_cycles32.cu
-  } else if (what == 0) {
-    long long smem = cycles_smem_bytes(POT, ENS, false, R, maxN);
-    // opt in to more than 48 KB of dynamic shared memory when needed, within
-    // the device limit minus the kernel's static shared memory; the attribute
-    // belongs to the current device's context, so it is recorded per device
-    static long long attr_set[MAX_DEVICES] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return (int)e;
-    if (dev < 0 || dev >= MAX_DEVICES) return (int)cudaErrorInvalidDevice;
-    if (smem > 48 * 1024 && smem > attr_set[dev]) {
-      int optin = 0;
-      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-      cudaFuncAttributes fa;
-      e = cudaFuncGetAttributes(&fa, k_cycles<POT, BC, ENS>);
-      if (e != cudaSuccess) return (int)e;
-      if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
-      e = cudaFuncSetAttribute(k_cycles<POT, BC, ENS>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return (int)e;
-      attr_set[dev] = smem;
-    }
+    if (what == 0 || what == 3) return (int)cudaErrorInvalidValue;  // FP32 form: ptmc_cycles32.cu
+  } else if (what == 0 || what == 3) {
+    const long long smem = cycles_smem_bytes(POT, ENS, false, R, maxN);
+    const int e = opt_in64<POT, BC, ENS>(smem);
+    if (e) return e;
+    if (what == 3)
+      return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cycles<POT, BC, ENS>, R * 32,
+                                                                (size_t)smem);
     k_cycles<POT, BC, ENS><<<grid, block, (size_t)smem, st>>>(P, run0, ncycles, phase);
     return (int)cudaGetLastError();
   }
@@ -1065,19 +1077,19 @@ static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
 
 template <int POT, int BC, int ENS>
 static int run_prec(bool f32, int what, const KParams& P, int run0, int nruns,
-                    int R, int maxN, int ncycles, int phase, cudaStream_t st) {
-  return f32 ? run_instance<POT, BC, ENS, true>(what, P, run0, nruns, R, maxN, ncycles, phase, st)
-             : run_instance<POT, BC, ENS, false>(what, P, run0, nruns, R, maxN, ncycles, phase, st);
+                    int R, int maxN, int ncycles, int phase, cudaStream_t st, int* occ) {
+  return f32 ? run_instance<POT, BC, ENS, true>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ)
+             : run_instance<POT, BC, ENS, false>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ);
 }
 
 static int dispatch(int pot, int bc, int ens, bool f32, int what,
                     const KParams& P, int run0, int nruns, int R, int maxN,
-                    int ncycles, int phase, void* stream) {
+                    int ncycles, int phase, void* stream, int* occ = nullptr) {
   cudaStream_t st = (cudaStream_t)stream;
 #define PT_CASE(PO, B, E)                                                  \
   if (pot == PO && bc == B && ens == E)                                    \
     return run_prec<PO, B, E>(f32, what, P, run0, nruns, R, maxN, ncycles, \
-                              phase, st);
+                              phase, st, occ);
   PT_CASE(POT_ELJ, BC_SPH, ENS_NVT)
   PT_CASE(POT_ELJEVEN, BC_SPH, ENS_NVT)
   PT_CASE(POT_EAM, BC_SPH, ENS_NVT)
@@ -1091,7 +1103,7 @@ static int dispatch(int pot, int bc, int ens, bool f32, int what,
   if (pot == PO && bc == B && ens == E)                                                  \
     return f32 ? (int)cudaErrorInvalidValue                                              \
                : run_instance<PO, B, E, false>(what, P, run0, nruns, R, maxN, ncycles,   \
-                                               phase, st);
+                                               phase, st, occ);
   PT_CASE64(POT_ELJ, BC_RECT, ENS_NVT)
   PT_CASE64(POT_ELJEVEN, BC_RECT, ENS_NVT)
   PT_CASE64(POT_ELJ, BC_RHB, ENS_NVT)
@@ -1126,6 +1138,10 @@ int launch_init(int pot, int bc, int ens, bool f32, const KParams& P, int run0,
 int launch_resync(int pot, int bc, int ens, bool f32, const KParams& P,
                   int run0, int nruns, int R, void* stream) {
   return dispatch(pot, bc, ens, f32, 2, P, run0, nruns, R, 0, 0, 0, stream);
+}
+int occupancy_cycles(int pot, int bc, int ens, int R, int N, int* ctas_per_sm) {
+  KParams P{};
+  return dispatch(pot, bc, ens, false, 3, P, 0, 0, R, N, 0, 0, nullptr, ctas_per_sm);
 }
 
 }  // namespace ptmc

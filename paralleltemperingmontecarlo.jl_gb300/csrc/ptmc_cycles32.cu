@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(1024)
           const float t = (dn <= rcf ? vn : 0.f) - (dol <= rcf ? vo : 0.f);
           de += self ? 0.f : t;
         } else {
-          const float t = v32p<POT>(P, s_cf, K, dn) - v32p<POT>(P, s_cf, K, dol);
+          const float t = __fsub_rn(v32p<POT>(P, s_cf, K, dn), v32p<POT>(P, s_cf, K, dol));
           de += self ? 0.f : t;
         }
       }
@@ -713,7 +713,7 @@ static int set_smem32(long long smem) {
 
 template <int POT, int BC, int ENS, int LPR>
 static int launch32l(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
-                     int phase, int ncta, cudaStream_t st) {
+                     int phase, int ncta, cudaStream_t st, int* occ = nullptr) {
   constexpr int WPW = 32 / LPR;
   if (ncta < 1 || ncta > 8 || R % ncta != 0 || (R / ncta) % WPW != 0)
     return (int)cudaErrorInvalidValue;
@@ -721,6 +721,13 @@ static int launch32l(const KParams& P, int run0, int nruns, int R, int maxN, int
   int e = set_smem32<POT, BC, ENS, LPR>(smem);
   if (e) return e;
   const unsigned threads = (unsigned)(R / ncta * LPR);
+  if (occ) {  // resident CTAs per SM (a cluster's CTAs count one each)
+    if (ncta == 1)
+      return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          occ, k_cycles32<POT, BC, ENS, false, LPR>, (int)threads, (size_t)smem);
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        occ, k_cycles32<POT, BC, ENS, true, LPR>, (int)threads, (size_t)smem);
+  }
   if (ncta == 1) {
     k_cycles32<POT, BC, ENS, false, LPR><<<nruns, threads, (size_t)smem, st>>>(P, run0, ncycles,
                                                                                phase, 1);
@@ -746,9 +753,11 @@ static int launch32l(const KParams& P, int run0, int nruns, int R, int maxN, int
 
 template <int POT, int BC, int ENS>
 static int launch32(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
-                    int phase, int ncta, int lpr, cudaStream_t st) {
-  if (lpr == 16) return launch32l<POT, BC, ENS, 16>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st);
-  if (lpr == 32) return launch32l<POT, BC, ENS, 32>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st);
+                    int phase, int ncta, int lpr, cudaStream_t st, int* occ = nullptr) {
+  if (lpr == 16)
+    return launch32l<POT, BC, ENS, 16>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st, occ);
+  if (lpr == 32)
+    return launch32l<POT, BC, ENS, 32>(P, run0, nruns, R, maxN, ncycles, phase, ncta, st, occ);
   return (int)cudaErrorInvalidValue;
 }
 
@@ -769,6 +778,25 @@ int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nr
   PT32(POT_EAM, BC_CUB, ENS_NVT)
   PT32(POT_ELJEVEN, BC_CUB, ENS_NPT)
 #undef PT32
+  return -1;
+}
+
+int occupancy_cycles32(int pot, int bc, int ens, int R, int N, int ncta, int lpr, int* ctas_per_sm) {
+  if (lpr == 4 || lpr == 8) {
+    if (ncta != 1 || ens != ENS_NVT) return (int)cudaErrorInvalidValue;
+    return occupancy_cycles32n(pot, bc, R, N, lpr, ctas_per_sm);
+  }
+  KParams P{};
+#define OC32(PO, B, E) \
+  if (pot == PO && bc == B && ens == E) return launch32<PO, B, E>(P, 0, 0, R, N, 0, 0, ncta, lpr, nullptr, ctas_per_sm);
+  OC32(POT_ELJ, BC_SPH, ENS_NVT)
+  OC32(POT_ELJEVEN, BC_SPH, ENS_NVT)
+  OC32(POT_EAM, BC_SPH, ENS_NVT)
+  OC32(POT_ELJ, BC_CUB, ENS_NVT)
+  OC32(POT_ELJEVEN, BC_CUB, ENS_NVT)
+  OC32(POT_EAM, BC_CUB, ENS_NVT)
+  OC32(POT_ELJEVEN, BC_CUB, ENS_NPT)
+#undef OC32
   return -1;
 }
 

@@ -13,11 +13,17 @@
 //    and the pair sums need 2 (3) shuffle levels instead of 5.  The walkers of
 //    a warp make their moves in lockstep (same N, same step count); they
 //    diverge only on accept vs reject and on the rare spherical retry.
+//  * The pair and commit loops are unrolled (at most JPL terms per lane,
+//    N <= 64) in chunks of NARROW_CH terms under one warp-uniform test each;
+//    inside a chunk the terms carry no branch, so the compiler overlaps their
+//    MUFU and shared-memory chains, and the EAM density deltas stay in
+//    registers.
 //  * Shared memory per walker is small, so more walkers share an SM: FP32 hi
-//    positions (float4, the EAM density rho in w), sqrt(rho) and the move's
-//    density deltas (EAM), 32 buffered draw words.  The lo halves of the
-//    float-float positions are touched only by the moved atom's proposal and
-//    commit, so they live in HBM (L2): one 16-byte load per move.
+//    positions (float4, the EAM density rho in w; padded with far-away
+//    sentinel atoms to whole chunks) and sqrt(rho) (EAM), 32 buffered draw
+//    words.  The lo halves of the float-float positions are touched only by
+//    the moved atom's proposal and commit, so they live in HBM (L2): one
+//    16-byte load per move, issued one move ahead.
 //  * Draw words are refilled for the whole warp at once (when any walker needs
 //    words at the start of a step): a refill re-creates a walker's buffer from
 //    its stream index, so an early refill changes no draw.
@@ -28,6 +34,8 @@
 // the run), so a chain differs from the 16/32-lane form only by the order in
 // which FP32 pair terms are added.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "ptmc_device.cuh"
 #include "ptmc_engine.cuh"
@@ -40,11 +48,17 @@ using namespace f32k;
 
 // draw words buffered per walker (a refill is DRWN / 4 Philox blocks)
 constexpr uint32_t DRWN = 32;
+// pair terms per unrolled chunk
+constexpr int CH = NARROW_CH;
+// a position no atom comes near: a pair with it has r^2 ~ 3e36, whose FP32
+// ELJ and EAM terms (r^-6 and beyond; r^-n, r^-m) underflow to exactly zero
+constexpr float FAR = 1.0e18f;
 
-// at most 32 walkers (R * LPR threads); the register cap keeps 5 CTAs of 32
-// walkers per SM at LPR = 4 (96 registers) and 3 at LPR = 8 (80 registers)
-template <int POT, int BC, int LPR>
-__global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
+// JPL: pair terms per lane at most (N <= JPL * LPR = 64).
+// At most 32 walkers (R * LPR threads); the register cap keeps 4 CTAs of 32
+// walkers per SM at LPR = 4 (128 registers) and 3 at LPR = 8 (80 registers).
+template <int POT, int BC, int LPR, int JPL>
+__global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 4 : 3)
     k_cycles32n(KParams P, int run0, int ncycles, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
@@ -67,11 +81,7 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
   // order and sizes as in cycles32n_smem_bytes
   float4* s_xh = (float4*)carve((long long)R * Ns * 16);
   float* s_sq = nullptr;
-  float* s_d = nullptr;
-  if (POT == POT_EAM) {
-    s_sq = (float*)carve((long long)R * Ns * 4);
-    s_d = (float*)carve((long long)R * Ns * 4);
-  }
+  if (POT == POT_EAM) s_sq = (float*)carve((long long)R * Ns * 4);
   uint32_t* s_drw = (uint32_t*)carve((long long)R * DRWN * 4);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_en = (double*)carve((long long)R * 8);
@@ -98,6 +108,14 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
     s_xh[v * Ns + a] = h;
     glo[k] = make_float4((float)(x - (double)h.x), (float)(y - (double)h.y),
                          (float)(z - (double)h.z), 0.f);
+  }
+  // the pad atoms N .. Ns - 1 of every walker are far-away sentinels (their
+  // pair terms are zero; EAM density and its root 1 keep the embedding term
+  // of a zero delta finite)
+  for (int k = tid; k < R * (Ns - N); k += nthr) {
+    const int v = k / (Ns - N), a = N + (k - v * (Ns - N));
+    s_xh[v * Ns + a] = make_float4(FAR, FAR, FAR, 1.f);
+    if (POT == POT_EAM) s_sq[v * Ns + a] = 1.f;
   }
   if (POT == POT_EAM) {
     const double* gc = P.comp + rdp->comp_off;
@@ -139,13 +157,14 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
   float4* Xh = s_xh + (size_t)w * Ns;
   float4* Xl = glo + (size_t)w * N;
   float* SQ = s_sq ? s_sq + (size_t)w * Ns : nullptr;
-  float* D = s_d ? s_d + (size_t)w * Ns : nullptr;
   uint32_t* drw = s_drw + w * DRWN;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const float hnf = P.f_hn, hmf = P.f_hm, ecamf = P.f_ecam;
   const float ean2f = 2.f * P.f_ean, necamf = -P.f_ecam;
   const uint32_t run_word = (uint32_t)rdp->run_id;
   const float Lf = (float)L, Llo = (float)(L - (double)Lf), iLf = __frcp_rn(Lf);
+  // pair-term chunks per lane: warp-uniform
+  const int qmax = (N + LPR - 1) / LPR;
 
   // refill of this walker's buffer by its own lanes (spherical retries)
   auto refill = [&]() {
@@ -170,8 +189,12 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
   auto word_nc = [&]() -> uint32_t { return drw[off++]; };
 
   // ---------------------------------------------------------- atom move
-  auto atom_move = [&](int i, float beta_l2e, float mdf, float mdc, float& de_acc) -> int {
-    float4 h0 = Xh[i], l0 = Xl[i];
+  // l0: the lo half of atom i (from the prefetch register or a load)
+  int kpre = -1;  // atom whose lo half is in lpre (-1: none)
+  float4 lpre = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto atom_move = [&](int i, float4 l0, float beta_l2e, float mdf, float mdc,
+                       float& de_acc) -> int {
+    float4 h0 = Xh[i];
     float th[3], tl[3];
     auto propose = [&]() {  // the first attempt's words are ensured by the caller
       const float d0 = stepf(word_nc(), mdf, mdc), d1 = stepf(word_nc(), mdf, mdc),
@@ -209,6 +232,7 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
           __syncwarp(gmask);
           h0 = Xh[i];
           l0 = Xl[i];
+          kpre = -1;  // every lo half moved
         } else {
           ensure(3);
           propose();
@@ -230,42 +254,98 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
     }
     const float4 tf = make_float4(th[0], th[1], th[2], 0.f);
     const float4 x4 = h0;
+    // Spherical container: during the pair loop atom i itself is a far-away
+    // sentinel, so its pair term, like the pad atoms', is exactly zero and no
+    // term needs a mask.  A periodic box would fold the sentinel back into the
+    // box by the minimum image, so the cube masks the self pair and the pads.
+    constexpr bool SENT = BC == BC_SPH;
+    const int own = i & (LPR - 1);  // the lane that holds atom i in the loops
+    if (SENT) {
+      __syncwarp(gmask);  // every lane has read atom i
+      if (lane == own) Xh[i] = make_float4(FAR, FAR, FAR, 1.f);
+      __syncwarp(gmask);
+    }
     float de = 0.f, sbf = 0.f;
+    float dreg[POT == POT_EAM ? JPL : 1];  // this lane's density deltas db_j
     if (POT == POT_EAM) {
       // the phi part of dE is 2 ean sum_j da (the pair changes phi_i and phi_j
       // alike); rho_j is the w lane of atom j's position
-#pragma unroll 2
-      for (int j = lane; j < N; j += LPR) {
-        const bool self = j == i;  // masked, not branched (its old distance is 0)
-        const float4 b = Xh[j];
-        const float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
-        const float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
-        float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
-        float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
-        da = self ? 0.f : da;
-        db = self ? 0.f : db;
-        D[j] = db;
-        sbf += db;
-        // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
-        de = fmaf(ean2f, da, de);
-        de = fmaf(necamf * db, rcpf(SQ[j] + sqrtf_approx(b.w + db)), de);
+#pragma unroll
+      for (int c = 0; c < JPL; c += CH) {
+        if (c < qmax) {
+#pragma unroll
+          for (int u = 0; u < CH; ++u) {
+            const int j = lane + (c + u) * LPR;
+            const float4 b = Xh[j];
+            const float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
+            const float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
+            float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
+            float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
+            if (!SENT) {  // the self pair (zero old distance) and the pads
+              const bool skip = j == i || j >= N;
+              da = skip ? 0.f : da;
+              db = skip ? 0.f : db;
+            }
+            dreg[c + u] = db;
+            sbf += db;
+            // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
+            de = fmaf(ean2f, da, de);
+            de = fmaf(necamf * db, rcpf(SQ[j] + sqrtf_approx(b.w + db)), de);
+          }
+        }
       }
       sbf = seg_sum<LPR>(sbf, gmask);
       de = seg_sum<LPR>(de, gmask);
       de -= ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(x4.w + sbf));
     } else {
-#pragma unroll 2
-      for (int j = lane; j < N; j += LPR) {
-        const bool self = j == i;
-        const float4 b = Xh[j];
-        const float t = v32p<POT>(P, s_cf, K, pf2<BC>(tf, b, Lf, iLf)) -
-                        v32p<POT>(P, s_cf, K, pf2<BC>(x4, b, Lf, iLf));
-        de += self ? 0.f : t;
-      }
+      // ELJ pair terms with the coefficient count as a compile-time constant
+      // (the neon coefficients have 6) or a runtime loop
+      auto rows = [&](auto kk) {
+        constexpr int KK = decltype(kk)::value;
+        auto v = [&](float r2) -> float {
+          float x, s3;
+          if (POT == POT_ELJ) {
+            const float ir = rsqrtf(r2);
+            const float inv = ir * ir;
+            x = ir;
+            s3 = inv * inv * inv;
+          } else {
+            const float inv = rcpf(r2);
+            x = inv;
+            s3 = inv * inv * inv;
+          }
+          float p;
+          if constexpr (KK > 0) {
+            p = horner_p<KK>(P, x);
+          } else {
+            p = s_cf[K - 1];
+            for (int k = K - 2; k >= 0; --k) p = fmaf(p, x, s_cf[k]);
+          }
+          return __fmul_rn(p, s3);  // rounded as in v32p of the 16/32-lane kernel
+        };
+#pragma unroll
+        for (int c = 0; c < JPL; c += CH) {
+          if (c < qmax) {
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+              const int j = lane + (c + u) * LPR;
+              const float4 b = Xh[j];
+              const float t = __fsub_rn(v(pf2<BC>(tf, b, Lf, iLf)), v(pf2<BC>(x4, b, Lf, iLf)));
+              if (SENT) de += t;
+              else de += (j == i || j >= N) ? 0.f : t;
+            }
+          }
+        }
+      };
+      if (K == 6) rows(std::integral_constant<int, 6>{});
+      else rows(std::integral_constant<int, 0>{});
       de = seg_sum<LPR>(de, gmask);
     }
     const float u = u01f(word());
-    if (!(ex2f(-beta_l2e * de) >= u)) return 0;
+    if (!(ex2f(-beta_l2e * de) >= u)) {
+      if (SENT && lane == own) Xh[i] = h0;  // rejected: atom i back in place
+      return 0;
+    }
     __syncwarp(gmask);
     if (lane == 0) {
       float rho_i = 0.f;
@@ -277,11 +357,19 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
       Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
     }
     if (POT == POT_EAM) {
-      for (int k = lane; k < N; k += LPR) {
-        if (k == i) continue;
-        const float rho = Xh[k].w + D[k];
-        Xh[k].w = rho;
-        SQ[k] = sqrtf_approx(rho);
+#pragma unroll
+      for (int c = 0; c < JPL; c += CH) {
+        if (c < qmax) {
+#pragma unroll
+          for (int u = 0; u < CH; ++u) {
+            const int k = lane + (c + u) * LPR;
+            if (k < N && k != i) {
+              const float rho = Xh[k].w + dreg[c + u];
+              Xh[k].w = rho;
+              SQ[k] = sqrtf_approx(rho);
+            }
+          }
+        }
       }
     }
     de_acc += de;
@@ -322,6 +410,7 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
     const float mdf = s_mdf[slot], mdc = s_mdc[slot];
     int acc_a = 0;
     float de_acc = 0.f;
+    kpre = -1;
     for (int st = 0; st < N; ++st) {
       // every walker of the warp is at the same step: one refill decision for
       // the warp (slot draw, three displacements, acceptance: 5 words)
@@ -339,13 +428,28 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
       }
       if (status == ST_OK) {
         const int k = (int)__umulhi(word_nc(), (uint32_t)N);  // rand(1:N)
-        acc_a += atom_move(k, beta_l2e, mdf, mdc, de_acc);
+        const float4 l0 = k == kpre ? lpre : Xl[k];
+        // The lo halves live in L2: the load for the next move's atom is
+        // issued now, from the slot word that follows this move's three
+        // displacements and acceptance draw (the next slot word unless a
+        // spherical retry draws more; a refill re-creates the same word).
+        kpre = -1;
+        if (off + 4 < DRWN) {
+          kpre = (int)__umulhi(drw[off + 4], (uint32_t)N);
+          lpre = Xl[kpre];
+        }
+        const int a = atom_move(k, l0, beta_l2e, mdf, mdc, de_acc);
+        if (a && kpre == k) kpre = -1;  // the prefetched lo half was just replaced
+        acc_a += a;
       }
     }
     en += (double)de_acc;
     if (status == ST_OK && P.resync_every > 0 && idx % P.resync_every == 0) {
-      const double e64 = energy64<POT, BC, ENS_NVT, LPR>(Xh, Xl, N, L, rc2, s_c, K, hn, hm,
-                                                         P.eam_ean, P.eam_ecam, D, SQ, lane, gmask);
+      // EAM: the recomputed densities are staged in the w lanes of the lo
+      // halves (unused otherwise)
+      const double e64 = energy64<POT, BC, ENS_NVT, LPR>(
+          Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean, P.eam_ecam,
+          POT == POT_EAM ? &Xl[0].w : nullptr, SQ, lane, gmask, 4);
       drift = fmax(drift, fabs(en - e64));
       en = e64;
       __syncwarp(gmask);
@@ -430,12 +534,9 @@ __global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 5 : 3)
   }
 }
 
-template <int POT, int BC, int LPR>
-int launch_n(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles, int phase,
-             cudaStream_t st) {
-  if ((R * LPR) % 32 != 0 || R > 32) return (int)cudaErrorInvalidValue;
-  const long long smem = cycles32n_smem_bytes(POT, R, maxN, LPR);
-  // shared-memory opt-in, per instantiation and per device
+// shared-memory opt-in, per instantiation and per device; only ever raised
+template <int POT, int BC, int LPR, int JPL>
+int opt_in_n(long long smem) {
   static long long attr_set[MAX_DEVICES] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -445,44 +546,46 @@ int launch_n(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, k_cycles32n<POT, BC, LPR>);
+    e = cudaFuncGetAttributes(&fa, k_cycles32n<POT, BC, LPR, JPL>);
     if (e != cudaSuccess) return (int)e;
     if (smem + (long long)fa.sharedSizeBytes > optin) return (int)cudaErrorInvalidValue;
-    e = cudaFuncSetAttribute(k_cycles32n<POT, BC, LPR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+    e = cudaFuncSetAttribute(k_cycles32n<POT, BC, LPR, JPL>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     attr_set[dev] = smem;
   }
-  k_cycles32n<POT, BC, LPR><<<nruns, (unsigned)(R * LPR), (size_t)smem, st>>>(P, run0, ncycles, phase);
+  return 0;
+}
+
+// what = 0: launch; what = 1: resident CTAs per SM into *occ
+template <int POT, int BC, int LPR, int JPL>
+int launch_n(int what, const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
+             int phase, cudaStream_t st, int* occ) {
+  if ((R * LPR) % 32 != 0 || R > 32 || maxN > JPL * LPR) return (int)cudaErrorInvalidValue;
+  const long long smem = cycles32n_smem_bytes(POT, R, maxN, LPR);
+  int e = opt_in_n<POT, BC, LPR, JPL>(smem);
+  if (e) return e;
+  if (what == 1)
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cycles32n<POT, BC, LPR, JPL>,
+                                                              R * LPR, (size_t)smem);
+  k_cycles32n<POT, BC, LPR, JPL><<<nruns, (unsigned)(R * LPR), (size_t)smem, st>>>(P, run0, ncycles,
+                                                                                   phase);
   return (int)cudaGetLastError();
 }
 
+// N <= 64 atoms: 16 pair terms per lane at 4 lanes, 8 at 8 lanes
 template <int POT, int BC>
-int launch_nl(const KParams& P, int run0, int nruns, int R, int maxN, int ncycles, int phase,
-              int lpr, cudaStream_t st) {
-  if (lpr == 4) return launch_n<POT, BC, 4>(P, run0, nruns, R, maxN, ncycles, phase, st);
-  if (lpr == 8) return launch_n<POT, BC, 8>(P, run0, nruns, R, maxN, ncycles, phase, st);
+int launch_nl(int what, const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
+              int phase, int lpr, cudaStream_t st, int* occ) {
+  if (lpr == 4) return launch_n<POT, BC, 4, 16>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ);
+  if (lpr == 8) return launch_n<POT, BC, 8, 8>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ);
   return (int)cudaErrorInvalidValue;
 }
 
-}  // namespace
-
-long long cycles32n_smem_bytes(int pot, int R, int N, int lpr) {
-  auto al = [](long long b) { return (b + 15) / 16 * 16; };
-  const long long Ns = narrow_stride(N, lpr);
-  long long b = al(R * Ns * 16);                           // float4 hi positions (+ rho)
-  if (pot == POT_EAM) b += 2 * al(R * Ns * 4);             // sqrt(rho), density deltas
-  b += al(R * (long long)DRWN * 4);                        // draw words
-  b += 2 * al(R * 8LL) + 2 * al(R * 16LL) + al(R * 48LL);  // beta, en, ham, maxd, counters
-  b += 6 * al(R * 4LL);                                    // wos, sow, bl2e, mdf, mdc, acc
-  return b;
-}
-
-int launch_cycles32n(int pot, int bc, const KParams& P, int run0, int nruns, int R, int maxN,
-                     int ncycles, int phase, int lpr, void* stream) {
-  cudaStream_t st = (cudaStream_t)stream;
+int dispatch_n(int what, int pot, int bc, const KParams& P, int run0, int nruns, int R, int maxN,
+               int ncycles, int phase, int lpr, cudaStream_t st, int* occ) {
 #define PT32N(PO, B) \
-  if (pot == PO && bc == B) return launch_nl<PO, B>(P, run0, nruns, R, maxN, ncycles, phase, lpr, st);
+  if (pot == PO && bc == B) return launch_nl<PO, B>(what, P, run0, nruns, R, maxN, ncycles, phase, lpr, st, occ);
   PT32N(POT_ELJ, BC_SPH)
   PT32N(POT_ELJEVEN, BC_SPH)
   PT32N(POT_EAM, BC_SPH)
@@ -491,6 +594,30 @@ int launch_cycles32n(int pot, int bc, const KParams& P, int run0, int nruns, int
   PT32N(POT_EAM, BC_CUB)
 #undef PT32N
   return -1;
+}
+
+}  // namespace
+
+long long cycles32n_smem_bytes(int pot, int R, int N, int lpr) {
+  auto al = [](long long b) { return (b + 15) / 16 * 16; };
+  const long long Ns = narrow_stride(N, lpr);
+  long long b = al(R * Ns * 16);                           // float4 hi positions (+ rho)
+  if (pot == POT_EAM) b += al(R * Ns * 4);                 // sqrt(rho)
+  b += al(R * (long long)DRWN * 4);                        // draw words
+  b += 2 * al(R * 8LL) + 2 * al(R * 16LL) + al(R * 48LL);  // beta, en, ham, maxd, counters
+  b += 6 * al(R * 4LL);                                    // wos, sow, bl2e, mdf, mdc, acc
+  return b;
+}
+
+int launch_cycles32n(int pot, int bc, const KParams& P, int run0, int nruns, int R, int maxN,
+                     int ncycles, int phase, int lpr, void* stream) {
+  return dispatch_n(0, pot, bc, P, run0, nruns, R, maxN, ncycles, phase, lpr, (cudaStream_t)stream,
+                    nullptr);
+}
+
+int occupancy_cycles32n(int pot, int bc, int R, int N, int lpr, int* ctas_per_sm) {
+  KParams P{};
+  return dispatch_n(1, pot, bc, P, 0, 0, R, N, 0, 0, lpr, nullptr, ctas_per_sm);
 }
 
 }  // namespace ptmc

@@ -135,11 +135,15 @@ struct KParams {
 // last a few cycles)
 constexpr long long XWAIT_CLOCKS = 1ll << 33;
 
-// walker stride (atoms) of the FP32 form's shared position array with 4 or 8
-// lanes per walker: stride = lpr mod 2 lpr, so that the walkers read by one
+// pair terms per unrolled chunk of the FP32 form with 4 or 8 lanes per walker
+constexpr int NARROW_CH = 4;
+// walker stride (atoms) of that form's shared position array: N padded to
+// whole chunks (NARROW_CH * lpr atoms; the pad atoms are far-away sentinels),
+// plus lpr, so that the stride is lpr mod 2 lpr and the walkers read by one
 // 128-byte shared-memory wavefront fall into disjoint banks
 __host__ __device__ inline int narrow_stride(int N, int lpr) {
-  return (N + lpr - 1) / (2 * lpr) * (2 * lpr) + lpr;
+  const int q = NARROW_CH * lpr;
+  return (N + q - 1) / q * q + lpr;
 }
 
 // shared-memory bytes of one run CTA
@@ -176,6 +180,10 @@ long long cycles32_smem_bytes(int pot, int R, int N, int ncta);
 long long cycles32n_smem_bytes(int pot, int R, int N, int lpr);
 int launch_cycles32n(int pot, int bc, const KParams& P, int run0, int nruns, int R, int maxN,
                      int ncycles, int phase, int lpr, void* stream);
+// resident CTAs per SM of a cycle kernel (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
+int occupancy_cycles(int pot, int bc, int ens, int R, int N, int* ctas_per_sm);
+int occupancy_cycles32(int pot, int bc, int ens, int R, int N, int ncta, int lpr, int* ctas_per_sm);
+int occupancy_cycles32n(int pot, int bc, int R, int N, int lpr, int* ctas_per_sm);
 // ncta: CTAs per run (a thread-block cluster when > 1; FP32 form only)
 // lpr: lanes per walker (32 or 16; FP32 form only)
 int launch_cycles32(int pot, int bc, int ens, const KParams& P, int run0, int nruns, int R,

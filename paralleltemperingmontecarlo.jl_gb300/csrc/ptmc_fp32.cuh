@@ -50,7 +50,9 @@ __device__ __forceinline__ float v32p(const KParams& P, const float* c, int K, f
       v = c[K - 1];
       for (int k = K - 2; k >= 0; --k) v = fmaf(v, x, c[k]);
   }
-  return v * s;
+  // rounded as written: a pair term is the same float in every kernel of
+  // the form (no contraction into the caller's difference)
+  return __fmul_rn(v, s);
 }
 __device__ __forceinline__ double v_even64(const double* c, int K, double r2) {
   double inv = 1.0 / r2;
@@ -150,12 +152,16 @@ __device__ __forceinline__ T seg_sum(T v, unsigned mask) {
   return v;
 }
 
-// FP64 energy of one walker from its fixed-point positions (resync); the
-// walker's LPR lanes share the work (glane = lane within the walker's group).
+// FP64 energy of one walker from its float-float positions (resync); the
+// walker's LPR lanes share the work (lane = lane within the walker's group).
+// EAM: the recomputed densities are staged in rho_tmp[a * rho_stride] and go
+// into the w lanes of Xh once every lane has read the positions; sqrt(rho)
+// into sq32.
 template <int POT, int BC, int ENS, int LPR>
 __device__ double energy64(float4* Xh, const float4* Xl, int N, double L, double rc2,
                            const double* c, int K, double hn, double hm, double ean,
-                           double ecam, float* rho_tmp, float* sq32, int lane, unsigned gmask) {
+                           double ecam, float* rho_tmp, float* sq32, int lane, unsigned gmask,
+                           int rho_stride = 1) {
   auto P = [&](int a, double& x, double& y, double& z) {
     float4 h = Xh[a], l = Xl[a];
     x = (double)h.x + (double)l.x;
@@ -176,7 +182,7 @@ __device__ double energy64(float4* Xh, const float4* Xl, int N, double L, double
         A += exp(hn * lg);
         B += exp(hm * lg);
       }
-      if (rho_tmp) rho_tmp[a] = (float)B;
+      if (rho_tmp) rho_tmp[a * rho_stride] = (float)B;
       if (sq32) sq32[a] = (float)sqrt(B);
       e += ean * A - ecam * sqrt(B);
     }
@@ -184,7 +190,7 @@ __device__ double energy64(float4* Xh, const float4* Xl, int N, double L, double
     // lane has read the positions
     __syncwarp(gmask);
     if (rho_tmp)
-      for (int a = lane; a < N; a += LPR) Xh[a].w = rho_tmp[a];
+      for (int a = lane; a < N; a += LPR) Xh[a].w = rho_tmp[a * rho_stride];
     __syncwarp(gmask);
     return seg_sum<LPR>(e, gmask);
   } else {
