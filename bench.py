@@ -55,16 +55,24 @@ METRIC = "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) er
 
 # Counters of the chosen form's cycle kernel from one ncu capture per workload
 # (smsp__inst_executed over the launch's attempted moves; DRAM read + write
-# bytes of the launch per run), valid for the kernel source whose sha256 prefix
-# is given: a changed kernel drops them from the line instead of reporting
-# stale figures.
-KERNEL_SRC = os.path.join(ROOT, "paralleltemperingmontecarlo.jl_gb300", "csrc", "ptmc_cycles32.cu")
-PROFILED = {}
+# bytes of the launch per run), valid for the launch shape (lanes per walker)
+# and the kernel sources whose sha256 prefix is given: a changed kernel drops
+# them from the line instead of reporting stale figures.
+CSRC = os.path.join(ROOT, "paralleltemperingmontecarlo.jl_gb300", "csrc")
+NARROW_SRC = ("ptmc_cycles32n.cu", "ptmc_fp32.cuh")
+PROFILED = {
+    # 608 runs x 32 replicas of Cu55, 4 lanes per walker, one 20-cycle launch
+    # (21.4 M attempted moves): 2.318e9 warp instructions, 54.2 MB DRAM
+    "cu55": dict(inst_per_move=108.3, lanes=4, dram_bytes_per_run=54.24e6 / 608,
+                 src=NARROW_SRC, src_sha="3e18449cfa42b697"),
+}
 
 
-@functools.lru_cache(maxsize=1)
-def kernel_sha():
-    return hashlib.sha256(open(KERNEL_SRC, "rb").read()).hexdigest()[:16]
+def kernel_sha(files):
+    h = hashlib.sha256()
+    for f in files:
+        h.update(open(os.path.join(CSRC, f), "rb").read())
+    return h.hexdigest()[:16]
 
 
 # --------------------------------------------------------------- workloads
@@ -446,7 +454,7 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
     # the cycle kernels are ~all of a step's device time
     achieved = flops_launch / (ch["ms_per_step"] / 1e3) / 1e12
     prof = PROFILED.get(name)
-    fresh = prof is not None and prof["src_sha"] == kernel_sha()
+    fresh = prof is not None and prof["src_sha"] == kernel_sha(prof["src"])
     roof = {"bound": "fp32_fma", "achieved": achieved, "peak": peaks["fp32_tflops"],
             "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"],
             "traffic": prof["dram_bytes_per_run"] * ch["runs"] if fresh else None,
@@ -455,7 +463,8 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
             "fp64_peak_tflops": peaks["fp64_tflops"], "mufu_peak_tops": peaks["mufu_tops"],
             "issue": issue_roof(prof if fresh else None, ch, n_sm)}
     if prof is not None and not fresh:
-        roof["counters_note"] = "ncu counters predate kernel source %s; not reported" % kernel_sha()
+        roof["counters_note"] = ("ncu counters predate kernel source %s; not reported"
+                                 % kernel_sha(prof["src"]))
     rec = {"workload": W["name"], "value": ch["value"], "unit": "atom-moves/s",
            "ms_per_step": ch["ms_per_step"], "steps": ch["steps"],
            "cycles_per_step": ch["cycles_per_step"], "runs": ch["runs"], "replicas": W["R"],
