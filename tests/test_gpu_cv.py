@@ -13,7 +13,8 @@ means must agree within 5 combined standard errors.
 
   * Ne13 (ELJEven, the neon coefficients of examples/ne13.jl), FP32 move rows
     + FP64 resync
-  * Cu55 (Sutton-Chen EAM of scripts/cu55.jl), FP32 move rows + FP64 resync;
+  * Cu55 (Sutton-Chen EAM of scripts/cu55.jl), FP32 move rows + FP64 resync,
+    10^4 production cycles of 16 runs x 32 replicas per form;
     both forms start from the same configurations, relaxed beforehand by the
     FP32 form (the icosahedral start relaxes for longer than a short
     equilibration, and the reference protocol fixes the histogram range at the
@@ -41,8 +42,9 @@ C_NE = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668
         -56234083.4334278, 288738837.441765]
 
 
-def run_form(pk, pot, starts, bc, R, T, eq, prod, precision, seed, da=None):
-    """starts: per run, one configuration or a list of R (one per replica)."""
+def run_form(pk, pot, starts, bc, R, T, eq, prod, precision, seed, da=None, shape=None):
+    """starts: per run, one configuration or a list of R (one per replica);
+    shape: the FP32 launch shape (CTAs per run, lanes per walker) to run."""
     n_runs = len(starts)
     first = starts[0][0] if isinstance(starts[0], list) else starts[0]
     N = len(first)
@@ -54,6 +56,8 @@ def run_form(pk, pot, starts, bc, R, T, eq, prod, precision, seed, da=None):
         cfg = [pk.Config(c, bc) for c in x] if isinstance(x, list) else pk.Config(x, bc)
         eng.set_configs(r, cfg)
     eng.init()
+    if shape is not None:
+        eng.set_launch_shape(N, *shape)
     if da is not None:
         da(eng)
     eng.equilibrate()
@@ -90,7 +94,9 @@ def test_cv_ne13_fp32_vs_fp64(pk):
     R = 16
     starts = [S.sphere_start(13, 8.0, 4.5, 1234 + r) for r in range(16)]
     args = (pk, pk.ELJPotentialEven(C_NE), starts, pk.SphericalBC(11.0), R, (4.0, 16.0), 4000, 20000)
-    compare(run_form(*args, "fp64", 11), run_form(*args, "fp32", 12), "Ne13 FP32+resync")
+    # the FP32 form with 4 lanes per walker, the shape the benchmark runs
+    compare(run_form(*args, "fp64", 11), run_form(*args, "fp32", 12, shape=(1, 4)),
+            "Ne13 FP32+resync (4 lanes per walker)")
 
 
 def test_cv_cu55_eam_fp32_vs_fp64(pk):
@@ -109,8 +115,11 @@ def test_cv_cu55_eam_fp32_vs_fp64(pk):
     pre.cycles_nosample(4000)
     starts = [list(pre.states(r)["xyz"]) for r in range(n_runs)]
     pre.close()
-    args = (pk, pot, starts, bc, R, T, 400, 1500)
-    compare(run_form(*args, "fp64", 21), run_form(*args, "fp32", 22), "Cu55 EAM FP32+resync")
+    # 10^4 production cycles per run, both forms (the plain form's pair cache
+    # makes this a ~1-minute check)
+    args = (pk, pot, starts, bc, R, T, 800, 10000)
+    compare(run_form(*args, "fp64", 21), run_form(*args, "fp32", 22, shape=(1, 4)),
+            "Cu55 EAM FP32+resync (4 lanes per walker)")
 
 
 def test_cp_ne32_npt_fp32_vs_fp64(pk):

@@ -99,3 +99,25 @@ def test_fp32_matches_fp64_statistically(pk):
         se = np.sqrt(a.var(0, ddof=1) / n + b.var(0, ddof=1) / n)
         z = np.abs(a.mean(0) - b.mean(0)) / se
         assert np.all(z < 4.0), z
+
+
+def test_n147_cluster8_energy_tracks_fp64(pk, orc):
+    """The largest atom count of the batched workload (147 atoms, 16 replicas)
+    under the cluster shape the autotuner picks for it (8 CTAs per run, 2
+    walkers each): the running FP32 energy stays within 1e-6 relative of the
+    oracle's FP64 energy of the returned positions, across resyncs."""
+    import ptmc_gb300.starts as S
+    n = 147
+    rad = 0.9 * n ** (1 / 3) * 3
+    starts = [S.sphere_start(n, rad, 4.3, 700 + r) for r in range(2)]
+    e = engine(pk, N=n, R=16, starts=starts, T=(4.0, 16.0), pot=pk.ELJPotentialEven(C_NE),
+               bc=pk.SphericalBC(rad + 3.0), precision="fp32", resync=50, n_runs=2, seed=17)
+    e.set_launch_shape(n, 8, 32)
+    e.cycles_nosample(130)          # resyncs at 50 and 100, then 30 cycles of FP32 drift
+    for r in range(2):
+        st = e.states(r)
+        ref = np.array([orc.elj_config_energy(x, orc.POT_ELJEVEN, C_NE) for x in st["xyz"]])
+        assert np.all(np.abs(st["en_tot"] - ref) <= 1e-6 * np.abs(ref)), r
+        assert st["counts"][:, 0].sum() > 0 and st["counts"][:, 5].sum() > 0
+    assert 0 < e.stats()["max_drift"]
+    e.close()
