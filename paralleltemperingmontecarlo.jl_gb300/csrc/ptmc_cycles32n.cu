@@ -55,10 +55,13 @@ constexpr int CH = NARROW_CH;
 constexpr float FAR = 1.0e18f;
 
 // JPL: pair terms per lane at most (N <= JPL * LPR = 64).
-// At most 32 walkers (R * LPR threads); the register cap keeps 4 CTAs of 32
-// walkers per SM at LPR = 4 (128 registers) and 3 at LPR = 8 (80 registers).
+// At most 32 walkers (R * LPR threads).  The register cap keeps, for 32
+// walkers per CTA, 4 CTAs per SM with EAM at LPR = 4 (128 registers; its
+// shared memory allows no more) and 3 at LPR = 8 (80 registers), and 8 / 4
+// CTAs (64 registers) with the pair potentials, whose small-N runs need
+// little shared memory and gain from more resident warps.
 template <int POT, int BC, int LPR, int JPL>
-__global__ void __launch_bounds__(32 * LPR, LPR == 4 ? 4 : 3)
+__global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) : (LPR == 4 ? 6 : 4))
     k_cycles32n(KParams P, int run0, int ncycles, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];

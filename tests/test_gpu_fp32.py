@@ -101,11 +101,22 @@ def test_fp32_matches_fp64_statistically(pk):
         assert np.all(z < 4.0), z
 
 
+def _abs_pair_sum(x):
+    """sum over pairs of |V(r_ij)| for the ELJEven neon coefficients"""
+    d = x[:, None, :] - x[None, :, :]
+    r2 = np.sum(d * d, axis=2)[np.triu_indices(len(x), 1)]
+    inv = 1.0 / r2
+    v = sum(c * inv ** (3 + k) for k, c in enumerate(C_NE))
+    return float(np.sum(np.abs(v)))
+
+
 def test_n147_cluster8_energy_tracks_fp64(pk, orc):
     """The largest atom count of the batched workload (147 atoms, 16 replicas)
     under the cluster shape the autotuner picks for it (8 CTAs per run, 2
-    walkers each): the running FP32 energy stays within 1e-6 relative of the
-    oracle's FP64 energy of the returned positions, across resyncs."""
+    walkers each): the running FP32 energy stays within 1e-6 of the oracle's
+    FP64 energy of the returned positions, across resyncs, relative to the sum
+    of the pair terms' magnitudes (the scale of an FP32 pair sum's error: the
+    dilute start clusters' net energy is a small difference of large terms)."""
     import ptmc_gb300.starts as S
     n = 147
     rad = 0.9 * n ** (1 / 3) * 3
@@ -117,7 +128,8 @@ def test_n147_cluster8_energy_tracks_fp64(pk, orc):
     for r in range(2):
         st = e.states(r)
         ref = np.array([orc.elj_config_energy(x, orc.POT_ELJEVEN, C_NE) for x in st["xyz"]])
-        assert np.all(np.abs(st["en_tot"] - ref) <= 1e-6 * np.abs(ref)), r
+        scale = np.array([_abs_pair_sum(x) for x in st["xyz"]])
+        assert np.all(np.abs(st["en_tot"] - ref) <= 1e-6 * scale), r
         assert st["counts"][:, 0].sum() > 0 and st["counts"][:, 5].sum() > 0
     assert 0 < e.stats()["max_drift"]
     e.close()
