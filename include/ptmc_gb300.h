@@ -54,7 +54,9 @@ typedef struct ptmc_ctx ptmc_ctx;
  * + ensemble + engine options. */
 typedef struct ptmc_params {
   int n_runs;         /* independent PT runs batched in one context (>= 1) */
-  int n_traj;         /* replicas per run, MCParams.n_traj (1..32) */
+  int n_traj;         /* replicas per run, MCParams.n_traj (1..1024; the FP32 form of the
+                         pair and EAM potentials runs R > 32 on a cluster of C <= 8 CTAs,
+                         so R needs a divisor C with R / C <= 32) */
   long long mc_cycles;/* MCParams.mc_cycles */
   long long eq_cycles;/* MCParams.eq_cycles (round(eq_percentage*cycles)) */
   int mc_sample;      /* MCParams.mc_sample */

@@ -57,7 +57,7 @@ struct Group {
   int nruns;
   cudaStream_t st = nullptr;
   int ncta = 1;  // CTAs per run (thread-block cluster size; FP32 form), set by ptmc_autotune
-  int lpr = 32;  // lanes per walker (32 or 16; FP32 form)
+  int lpr = 32;  // lanes per walker (32, 16, 8 or 4; FP32 form)
 };
 
 template <typename T>
@@ -683,8 +683,15 @@ int ptmc_init(ptmc_ctx* c) {
         return c->fail(PTMC_ERR_ARG, "NNVT: every run needs atoms of both species (N > n1)");
     }
   }
-  if (!nn && R > MAX_REPLICAS)
-    return c->fail(PTMC_ERR_LIMIT, "at most 32 replicas per run (one warp per replica in one CTA)");
+  // the FP32 form runs more than 32 replicas of a run on a thread-block
+  // cluster of C CTAs (R / C <= 32 walkers each): the smallest such C <= 8
+  int ncta0 = 1;
+  if (!nn && c->f32()) {
+    while (ncta0 <= 8 && (R % ncta0 != 0 || R / ncta0 > 32)) ++ncta0;
+    if (ncta0 > 8)
+      return c->fail(PTMC_ERR_LIMIT, "FP32 form: the replica count needs a divisor C <= 8 with "
+                                     "R / C <= 32 (one thread-block cluster of C CTAs per run)");
+  }
   if (nn) {
     for (auto& r : c->runs) {
       if (r.N > MAX_NN_ATOMS) return c->fail(PTMC_ERR_LIMIT, "NN potential: at most 64 atoms");
@@ -729,8 +736,9 @@ int ptmc_init(ptmc_ctx* c) {
     c->groups.back().nruns++;
   }
   for (auto& G : c->groups) {
+    G.ncta = ncta0;
     long long smem = nn ? 0
-                     : c->f32() ? cycles32_smem_bytes(c->pot, R, G.N, 1)
+                     : c->f32() ? cycles32_smem_bytes(c->pot, R, G.N, G.ncta)
                               : cycles_smem_bytes(c->pot, c->p.ensemble, false, R, G.N);
     if (smem > 227 * 1024)
       return c->fail(PTMC_ERR_LIMIT, "replica state of a run exceeds 227 KB of shared memory (R*N too large)");
@@ -2253,7 +2261,7 @@ extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_pa
   const int R = c->R();
   // shape code: 100 * CTAs per run + lanes per walker
   std::map<int, int> best;  // N -> shape code
-  for (auto& G : c->groups) best[G.N] = 100 + 32;
+  for (auto& G : c->groups) best[G.N] = 100 * G.ncta + G.lpr;
   auto apply = [&](const std::map<int, int>& m) {
     for (auto& G : c->groups) {
       G.ncta = m.at(G.N) / 100;
@@ -2300,6 +2308,7 @@ extern "C" int ptmc_autotune(ptmc_ctx* c, int trial_cycles, const char* cache_pa
             for (int ll : {32, 16, 8, 4}) {
               const int code = 100 * cc + ll;
               if (code == best[N] || R % cc != 0 || (R / cc) % (32 / ll) != 0) continue;
+              if (R / cc * ll > 1024) continue;  // threads of a CTA
               if (ll <= 8 && (cc != 1 || c->p.ensemble != PTMC_NVT || R > 32)) continue;
               const long long smem = ll <= 8 ? cycles32n_smem_bytes(c->pot, R, N, ll)
                                              : cycles32_smem_bytes(c->pot, R, N, cc);
@@ -2353,8 +2362,11 @@ extern "C" int ptmc_set_launch_shape(ptmc_ctx* c, int N, int ctas_per_run, int l
   if ((R / ctas_per_run) % (32 / lanes_per_walker) != 0)
     return c->fail(PTMC_ERR_ARG, "the walkers of a CTA must fill whole warps (R / C a multiple of "
                                  "32 / lanes_per_walker)");
-  if (lanes_per_walker <= 8 && (ctas_per_run != 1 || c->p.ensemble != PTMC_NVT))
-    return c->fail(PTMC_ERR_ARG, "8 or 4 lanes per walker: NVT with one CTA per run");
+  if (R / ctas_per_run * lanes_per_walker > 1024)
+    return c->fail(PTMC_ERR_ARG, "a CTA holds at most 1024 threads (R / C * lanes_per_walker)");
+  if (lanes_per_walker <= 8 && (ctas_per_run != 1 || c->p.ensemble != PTMC_NVT || R > 32))
+    return c->fail(PTMC_ERR_ARG, "8 or 4 lanes per walker: NVT with one CTA of at most 32 "
+                                 "walkers per run");
   int optin = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

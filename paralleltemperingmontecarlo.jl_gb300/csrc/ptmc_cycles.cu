@@ -331,8 +331,10 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
   // walkers w >= n_start start from the configuration of walker w mod n_start
   // (src/Initialization.jl:88-96): only the distinct starts are evaluated, the
   // other walkers copy their energy and variables
+  // a warp per walker; with more than 32 walkers (R > blockDim / 32) each
+  // warp takes every nw-th walker
   const RunDesc rd = P.runs[run0 + blockIdx.x];
-  const int N = rd.N, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int N = rd.N, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int ns = rd.n_start > 0 && rd.n_start < rd.R ? rd.n_start : rd.R;
   const bool keep_m = (ENS == ENS_NPT || pot_b(POT)) && !F32;
   constexpr bool keep_pe = pair_cache(POT, ENS) && !F32;  // plain form's NVT pair cache
@@ -340,7 +342,7 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
   auto mat = [&](int v) { return P.mat + rd.mat_off + (size_t)v * N * N; };
   auto cmp = [&](int v) { return P.comp + rd.comp_off + (size_t)v * N * 2; };
   auto pe = [&](int v) { return P.pe + rd.pe_off + (size_t)v * N * N * pe_w; };
-  if (w < ns) {
+  for (int w = warp; w < ns; w += nw) {
     const int g = rd.wk + w;
     const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
     double* M = keep_m ? mat(w) : nullptr;
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
     }
   }
   __syncthreads();
-  if (w >= ns && w < rd.R) {
+  for (int w = ns + warp; w < rd.R; w += nw) {
     const int g = rd.wk + w, src = w % ns;
     if (POT == POT_EAM)
       for (int k = lane; k < 2 * N; k += 32) cmp(w)[k] = cmp(src)[k];
@@ -392,8 +394,11 @@ __global__ void __launch_bounds__(1024)
   constexpr bool PEC = pair_cache(POT, ENS);        // NVT pair cache in HBM
   const RunDesc rd = P.runs[run0 + blockIdx.x];
   const int N = rd.N, R = rd.R;
-  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-  const int nthr = blockDim.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nthr = blockDim.x, nw = nthr >> 5;
+  // a warp per walker; with more walkers than warps (R > 32) each warp makes
+  // the moves of every nw-th walker in turn, its state parked in shared memory
+  const bool multi = R > nw;
   const int K = P.K;
   const int n_steps = ENS == ENS_NPT ? N + 1 : N;
 
@@ -428,6 +433,12 @@ __global__ void __launch_bounds__(1024)
   double* s_maxboxh = (double*)carve((long long)R * 8);
   double* s_maxd_sep = (double*)carve((long long)R * 16);
   long long* s_cnt_sep = (long long*)carve((long long)R * 32);
+  // walker state besides en / box / box height (s_en, s_box, s_boxh)
+  double* s_wrc2 = (double*)carve((long long)R * 8);
+  double* s_wdrift = (double*)carve((long long)R * 8);
+  unsigned long long* s_wctr = (unsigned long long*)carve((long long)R * 8);
+  unsigned long long* s_wbase = (unsigned long long*)carve((long long)R * 8);
+  int* s_wst = (int*)carve((long long)R * 4);
 
   // ---- load the run into shared memory ----
   if (tid < K) {
@@ -453,6 +464,15 @@ __global__ void __launch_bounds__(1024)
     s_maxd[2 * s + 1] = P.maxd[2 * g + 1];
     for (int q = 0; q < 6; ++q) s_cnt[6 * s + q] = P.cnt[6 * (size_t)g + q];
     s_wos[s] = P.wos[g];
+    // walker s's state
+    s_en[s] = P.en[g];
+    s_box[s] = P.box[g];
+    s_boxh[s] = has_height<BC>() ? P.boxh[g] : P.box[g];
+    s_wrc2[s] = P.rc2[g];
+    s_wdrift[s] = P.drift[g];
+    s_wctr[s] = P.ctr[g];
+    s_wbase[s] = P.ctr[g] + DRAW_BUF;  // forces a refill on the first draw
+    s_wst[s] = P.status[g];
     if (has_height<BC>()) {
       s_maxboxh[s] = P.maxboxh[g];
       s_maxd_sep[2 * s] = P.maxd_sep[2 * g];
@@ -464,24 +484,48 @@ __global__ void __launch_bounds__(1024)
   for (int s = tid; s < R; s += nthr) s_sow[s_wos[s]] = s;
   __syncthreads();
 
-  // ---- walker registers (warp-uniform) ----
-  const int g = rd.wk + w;
-  double en = P.en[g];
-  double L = P.box[g];
-  double H = has_height<BC>() ? P.boxh[g] : L;  // box height (RectangularBC, RhombicBC)
-  double rc2 = P.rc2[g];
-  unsigned long long ctr = P.ctr[g];
-  unsigned long long base = ctr + DRAW_BUF;  // forces a refill on first draw
-  int status = P.status[g];
-  double drift = P.drift[g];
-  double* X = s_pos + (size_t)w * N * 3;
-  double* drw = s_drw + w * DRAW_BUF;
-  double* M = KEEP_M ? P.mat + rd.mat_off + (size_t)w * N * N : nullptr;
-  // NVT pair cache of this walker: ELJ V(r_ij), EAM (r_ij^-n, r_ij^-m)
-  double* PE = PEC ? P.pe + rd.pe_off + (size_t)w * N * N * (POT == POT_EAM ? 2 : 1) : nullptr;
-  double* TM = BPOT ? P.tan + rd.mat_off + (size_t)w * N * N : nullptr;  // tangent matrix
-  double* row = s_row ? s_row + (size_t)w * N : nullptr;
-  double* trow = s_trow ? s_trow + (size_t)w * N : nullptr;
+  // ---- the current walker's registers (warp-uniform) ----
+  int w = warp;  // walker within the run
+  double en, L, H, rc2, drift;  // H: box height (RectangularBC, RhombicBC)
+  unsigned long long ctr, base;
+  int status;
+  double *X, *drw, *M, *PE, *TM, *row, *trow;
+  auto bind = [&](int v) {  // pointers of walker v
+    w = v;
+    X = s_pos + (size_t)v * N * 3;
+    drw = s_drw + v * DRAW_BUF;
+    M = KEEP_M ? P.mat + rd.mat_off + (size_t)v * N * N : nullptr;
+    // NVT pair cache of this walker: ELJ V(r_ij), EAM (r_ij^-n, r_ij^-m)
+    PE = PEC ? P.pe + rd.pe_off + (size_t)v * N * N * (POT == POT_EAM ? 2 : 1) : nullptr;
+    TM = BPOT ? P.tan + rd.mat_off + (size_t)v * N * N : nullptr;  // tangent matrix
+    row = s_row ? s_row + (size_t)v * N : nullptr;
+    trow = s_trow ? s_trow + (size_t)v * N : nullptr;
+  };
+  auto load = [&](int v) {  // walker v's state from shared memory
+    bind(v);
+    en = s_en[v];
+    L = s_box[v];
+    H = s_boxh[v];
+    rc2 = s_wrc2[v];
+    drift = s_wdrift[v];
+    ctr = s_wctr[v];
+    base = s_wbase[v];
+    status = s_wst[v];
+  };
+  auto save = [&]() {  // the current walker's state to shared memory (lane 0)
+    if (lane == 0) {
+      s_en[w] = en;
+      s_box[w] = L;
+      s_boxh[w] = H;
+      s_wrc2[w] = rc2;
+      s_wdrift[w] = drift;
+      s_wctr[w] = ctr;
+      s_wbase[w] = base;
+      s_wst[w] = status;
+    }
+    __syncwarp();
+  };
+  if (warp < R) load(warp);
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const double ean = P.eam_ean, ecam = P.eam_ecam;
   const uint32_t run_word = (uint32_t)rd.run_id;
@@ -831,39 +875,43 @@ __global__ void __launch_bounds__(1024)
   unsigned long long run_ctr = rd.run_ctr;
   for (int cyc = 0; cyc < ncycles; ++cyc) {
     const long long idx = first + cyc;
-    const int slot = s_sow[w];
-    const double beta = s_beta[slot];
-    const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
-    const double maxbox = s_maxbox[slot];
-    long long acc_a = 0, acc_v = 0, acc_xy = 0, acc_z = 0;
-    if (status == ST_OK) {
-      for (int st = 0; st < n_steps; ++st) {
-        int k = randint(draw(), n_steps);
-        if (k < N) {
-          acc_a += atom_move(k, beta, md);
-        } else {
-          const int v = volume_move(beta, slot, mdv, maxbox);
-          acc_v += v == 1;
-          acc_xy += v == 2;
-          acc_z += v == 3;
+    for (int wv = warp; wv < R; wv += nw) {  // this warp's walkers (one unless R > 32)
+      if (multi) load(wv);
+      const int slot = s_sow[w];
+      const double beta = s_beta[slot];
+      const double md = s_maxd[2 * slot], mdv = s_maxd[2 * slot + 1];
+      const double maxbox = s_maxbox[slot];
+      long long acc_a = 0, acc_v = 0, acc_xy = 0, acc_z = 0;
+      if (status == ST_OK) {
+        for (int st = 0; st < n_steps; ++st) {
+          int k = randint(draw(), n_steps);
+          if (k < N) {
+            acc_a += atom_move(k, beta, md);
+          } else {
+            const int v = volume_move(beta, slot, mdv, maxbox);
+            acc_v += v == 1;
+            acc_xy += v == 2;
+            acc_z += v == 3;
+          }
+          if (status != ST_OK) break;
         }
-        if (status != ST_OK) break;
       }
-    }
-    if (lane == 0) {
-      s_en[w] = en;
-      s_box[w] = L;
-      s_boxh[w] = H;
-      s_cnt[6 * slot + 0] += acc_a;
-      s_cnt[6 * slot + 1] += acc_a;
-      s_cnt[6 * slot + 2] += acc_v;
-      s_cnt[6 * slot + 3] += acc_v;
-      if (has_height<BC>()) {  // count_vol_xy, count_vol_z
-        s_cnt_sep[4 * slot + 0] += acc_xy;
-        s_cnt_sep[4 * slot + 1] += acc_xy;
-        s_cnt_sep[4 * slot + 2] += acc_z;
-        s_cnt_sep[4 * slot + 3] += acc_z;
+      if (lane == 0) {
+        s_en[w] = en;
+        s_box[w] = L;
+        s_boxh[w] = H;
+        s_cnt[6 * slot + 0] += acc_a;
+        s_cnt[6 * slot + 1] += acc_a;
+        s_cnt[6 * slot + 2] += acc_v;
+        s_cnt[6 * slot + 3] += acc_v;
+        if (has_height<BC>()) {  // count_vol_xy, count_vol_z
+          s_cnt_sep[4 * slot + 0] += acc_xy;
+          s_cnt_sep[4 * slot + 1] += acc_xy;
+          s_cnt_sep[4 * slot + 2] += acc_z;
+          s_cnt_sep[4 * slot + 3] += acc_z;
+        }
       }
+      if (multi) save();
     }
     __syncthreads();
     if (tid == 0 && R > 1) {  // parallel_tempering_exchange! (src/Exchange.jl:132-180)
@@ -945,21 +993,26 @@ __global__ void __launch_bounds__(1024)
     }
     __syncthreads();
     if (P.rdf && phase == PHASE_PROD && idx % P.mc_sample == 0 && idx % RDF_EVERY == 0) {
-      // update_rdf!: pairs k < i of this walker into the row of its slot; NPT
+      // update_rdf!: pairs k < i of each walker into the row of its slot; NPT
       // reads the distance matrix (scaled on volume moves, as the reference's)
-      unsigned int* row = P.rdf + (size_t)(rd.wk + s_sow[w]) * 5 * P.n_bin;
-      for (int i = 1; i < N; ++i)
-        for (int k = lane; k < i; k += 32) {
-          double r2;
-          if (M) r2 = M[(size_t)i * N + k];
-          else
-            r2 = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * k, L, H);
-          rdf_add(row, 5 * P.n_bin, r2, rd.dr2);
-        }
+      for (int wv = warp; wv < R; wv += nw) {
+        if (multi) load(wv);
+        unsigned int* hrow = P.rdf + (size_t)(rd.wk + s_sow[w]) * 5 * P.n_bin;
+        for (int i = 1; i < N; ++i)
+          for (int k = lane; k < i; k += 32) {
+            double r2;
+            if (M) r2 = M[(size_t)i * N + k];
+            else
+              r2 = pd2<BC>(X[3 * i], X[3 * i + 1], X[3 * i + 2], X + 3 * k, L, H);
+            rdf_add(hrow, 5 * P.n_bin, r2, rd.dr2);
+          }
+      }
     }
   }
 
   // ---- store the run back to HBM ----
+  if (!multi) save();  // the warps' walker registers to shared memory
+  __syncthreads();
   double* gpos_w = P.pos + rd.pos_off;
   for (int k = tid; k < R * N * 3; k += nthr) gpos_w[k] = s_pos[k];
   if (POT == POT_EAM) {
@@ -969,14 +1022,15 @@ __global__ void __launch_bounds__(1024)
       gc[2 * k + 1] = s_c64[k].y;
     }
   }
-  if (lane == 0) {
-    P.en[g] = en;
-    P.box[g] = L;
-    if (has_height<BC>()) P.boxh[g] = H;
-    P.rc2[g] = rc2;
-    P.ctr[g] = ctr;
-    P.status[g] = status;
-    P.drift[g] = drift;
+  for (int s = tid; s < R; s += nthr) {  // walker s's state
+    const int gw = rd.wk + s;
+    P.en[gw] = s_en[s];
+    P.box[gw] = s_box[s];
+    if (has_height<BC>()) P.boxh[gw] = s_boxh[s];
+    P.rc2[gw] = s_wrc2[s];
+    P.ctr[gw] = s_wctr[s];
+    P.status[gw] = s_wst[s];
+    P.drift[gw] = s_wdrift[s];
   }
   for (int s = tid; s < R; s += nthr) {
     int gs = rd.wk + s;
@@ -1002,24 +1056,25 @@ __global__ void __launch_bounds__(1024)
 template <int POT, int BC, int ENS, bool F32>
 __global__ void __launch_bounds__(1024) k_resync(KParams P, int run0) {
   const RunDesc rd = P.runs[run0 + blockIdx.x];
-  const int N = rd.N, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (w >= rd.R) return;
-  const int g = rd.wk + w;
-  const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
-  double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
-  double e;
-  if constexpr (pot_b(POT))
-    e = walker_energy_b<POT, BC, ENS>(P, X, N, P.box[g], P.boxh[g], P.rc2[g], P.ca, P.cb, P.c,
-                                      P.K, P.mat + rd.mat_off + (size_t)w * N * N,
-                                      P.tan + rd.mat_off + (size_t)w * N * N, lane);
-  else
-    e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
-                                      -0.5 * P.eam_n, -0.5 * P.eam_m,
-                                      P.eam_ean, P.eam_ecam, nullptr, comp,
-                                      nullptr, lane);
-  if (lane == 0) {
-    P.drift[g] = fmax(P.drift[g], fabs(P.en[g] - e));
-    P.en[g] = e;
+  const int N = rd.N, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int w = warp; w < rd.R; w += nw) {  // every nw-th walker
+    const int g = rd.wk + w;
+    const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
+    double* comp = POT == POT_EAM ? P.comp + rd.comp_off + (size_t)w * N * 2 : nullptr;
+    double e;
+    if constexpr (pot_b(POT))
+      e = walker_energy_b<POT, BC, ENS>(P, X, N, P.box[g], P.boxh[g], P.rc2[g], P.ca, P.cb, P.c,
+                                        P.K, P.mat + rd.mat_off + (size_t)w * N * N,
+                                        P.tan + rd.mat_off + (size_t)w * N * N, lane);
+    else
+      e = walker_energy64<POT, BC, ENS>(X, N, P.box[g], P.boxh[g], P.rc2[g], P.c, P.K,
+                                        -0.5 * P.eam_n, -0.5 * P.eam_m,
+                                        P.eam_ean, P.eam_ecam, nullptr, comp,
+                                        nullptr, lane);
+    if (lane == 0) {
+      P.drift[g] = fmax(P.drift[g], fabs(P.en[g] - e));
+      P.en[g] = e;
+    }
   }
 }
 
@@ -1054,7 +1109,8 @@ static int opt_in64(long long smem) {
 template <int POT, int BC, int ENS, bool F32>
 static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
                         int maxN, int ncycles, int phase, cudaStream_t st, int* occ) {
-  dim3 grid(nruns), block(R * 32);
+  // a warp per walker, at most 32 warps (a warp then serves several walkers)
+  dim3 grid(nruns), block((R < 32 ? R : 32) * 32);
   if constexpr (F32) {
     if (what == 0 || what == 3) return (int)cudaErrorInvalidValue;  // FP32 form: ptmc_cycles32.cu
   } else if (what == 0 || what == 3) {
@@ -1062,8 +1118,8 @@ static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
     const int e = opt_in64<POT, BC, ENS>(smem);
     if (e) return e;
     if (what == 3)
-      return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cycles<POT, BC, ENS>, R * 32,
-                                                                (size_t)smem);
+      return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cycles<POT, BC, ENS>,
+                                                                (int)block.x, (size_t)smem);
     k_cycles<POT, BC, ENS><<<grid, block, (size_t)smem, st>>>(P, run0, ncycles, phase);
     return (int)cudaGetLastError();
   }

@@ -40,7 +40,6 @@ enum { PHASE_PLAIN = 0, PHASE_EQ = 1, PHASE_PROD = 2 };
 // exchange partner ran out
 enum { ST_OK = 0, ST_SPHERE = 1, ST_TIMEOUT = 2, ST_XWAIT = 3 };
 constexpr int MAX_COEFF = 16;
-constexpr int MAX_REPLICAS = 32;
 constexpr int DRAW_BUF = 16;
 // devices whose per-kernel attributes (shared-memory opt-in) are tracked
 constexpr int MAX_DEVICES = 64;
@@ -167,6 +166,7 @@ inline long long cycles_smem_bytes(int pot, int ens, bool f32, int R, int N) {
   b += al((long long)R * 16);                        // maxd_sep
   b += al((long long)R * 4 * 8);                     // cnt_sep
   b += al((long long)R * 4) * 2;                     // wos, sow
+  b += al((long long)R * 8) * 4 + al((long long)R * 4);  // walker rc2, drift, ctr, base, status
   return b;
 }
 

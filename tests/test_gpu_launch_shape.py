@@ -303,3 +303,33 @@ def test_occupancy_query_keeps_launch_limits(pk, precision):
         e.cycles_nosample(3)
         assert e.states(0)["counts"][:, 0].sum() > 0
         e.close()
+
+
+def test_r64_fp32_cluster_shapes(pk, orc):
+    """64 replicas in the FP32 form: by default a cluster of 2 CTAs of 32
+    walkers; the chains are bit-identical for clusters of 2, 4 and 8 CTAs and
+    track the oracle's FP64 energy of the returned positions."""
+    import ptmc_gb300.starts as S
+    starts = [S.sphere_start(13, 8.0, 4.5, 90 + r) for r in range(2)]
+    args = (pk, pk.ELJPotentialEven(C_NE), pk.NVT(13), starts, pk.SphericalBC(11.0), 64,
+            (4.0, 40.0), 9)
+    ref = engine(*args)
+    a = protocol(ref)
+    for r in range(2):
+        st = ref.states(r)
+        e64 = np.array([orc.elj_config_energy(x, orc.POT_ELJEVEN, C_NE) for x in st["xyz"]])
+        assert np.all(np.abs(st["en_tot"] - e64) <= 1e-6 * np.abs(e64))
+        assert st["counts"][:, 5].sum() > 0
+    ref.close()
+    for c in (4, 8):
+        eng = engine(*args)
+        eng.set_launch_shape(13, c, 32)
+        b = protocol(eng)
+        eng.close()
+        assert_identical(a, b)
+    with pytest.raises(pk.PTMCError):  # 64 walkers do not fit one CTA
+        eng = engine(*args)
+        try:
+            eng.set_launch_shape(13, 1, 32)
+        finally:
+            eng.close()

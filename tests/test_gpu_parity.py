@@ -425,3 +425,45 @@ def test_ne108_npt_fp64_parity(pk, orc):
     _, ev, hp = o.hist()
     assert np.array_equal(out.ev_histogram, ev)
     eng.close()
+
+
+# ------------------------------------------------------------------
+# More than 32 replicas per run (MCParams.n_traj has no bound in the reference)
+
+def test_ne13_r64_fp64_parity(pk, orc):
+    """64 replicas of Ne13: the plain form's warps each make the moves of two
+    walkers in turn; same chain as the oracle (positions bitwise)."""
+    x0 = sphere_start(13, 8.0, 4.5, 64)
+    eng, (o,) = pair(pk, orc, N=13, R=64, x0=x0, T0=4.0, T1=40.0, pot=pk.ELJPotentialEven(C_NE),
+                     bc_param=11.0, exch_prob=1.0, seed=64, eq=100)
+    eng.equilibrate()
+    o.equilibrate(100)
+    eng.run_cycles(150)
+    o.production(1, 150)
+    g = compare(eng, o)
+    assert g["counts"][:, 5].sum() > 0
+    out = eng.output(0)
+    eh, _, _ = o.hist()
+    assert np.array_equal(out.en_histogram, eh)
+    eng.close()
+
+
+def test_cu55_eam_r64_and_npt_r48_fp64_parity(pk, orc):
+    """Cu55 EAM with 64 replicas (the pair cache, two walkers per warp) and
+    Ne32 NPT with 48 replicas (warps serving one or two walkers)."""
+    pot = pk.EmbeddedAtomPotential(**CU_EAM)
+    eng, (o,) = pair(pk, orc, N=55, R=64, x0=cu55_ico(), T0=200.0, T1=1000.0, pot=pot,
+                     bc_param=14.0, exch_prob=1.0, seed=65)
+    eng.cycles_nosample(25)
+    o.cycles(1, 25)
+    compare(eng, o)
+    eng.close()
+    x0 = fcc(2, 8.4, 0.05, 48)
+    p = 101325 * 3.398928944382626e-14
+    eng, (o,) = pair(pk, orc, N=32, R=48, x0=x0, T0=10.0, T1=40.0, pot=pk.ELJPotentialEven(C_NE),
+                     ens="npt", bc_param=16.8, exch_prob=1.0, seed=66, pressure=p)
+    eng.cycles_nosample(40)
+    o.cycles(1, 40)
+    g = compare(eng, o, positions_exact=False)
+    assert g["counts"][:, 2].sum() > 0
+    eng.close()
