@@ -149,6 +149,8 @@ struct ptmc_ctx {
   DBuf<double> d_tan, d_lut;
   DBuf<double> d_pe;           // plain form, NVT: pair cache (pair_cache in ptmc_engine.cuh)
   DBuf<float> d_lo;            // FP32 form: lo halves of positions during a narrow launch
+  bool glob = false;           // plain form: per-atom state in HBM (runs beyond shared memory)
+  DBuf<double> d_scr;          // its per-walker trial-row scratch
   // two-species RuNNer potential (NNVT ensemble)
   std::vector<double> nn2_rad, nn2_ang, nn2_W1, nn2_W2;
   int nn2_n1 = 0, nn2_H1 = 0, nn2_H2 = 0, n_swaps = 1;
@@ -735,13 +737,27 @@ int ptmc_init(ptmc_ctx* c) {
     if (c->groups.empty() || c->groups.back().N != N) c->groups.push_back({N, d, 0, nullptr});
     c->groups.back().nruns++;
   }
+  // Replica state beyond a CTA's shared memory: the FP32 form spreads the run
+  // over a larger cluster (fewer walkers per CTA); the plain form keeps the
+  // per-atom state in HBM (glob).
+  const long long smem_cap = 227 * 1024;
+  c->glob = false;
   for (auto& G : c->groups) {
     G.ncta = ncta0;
-    long long smem = nn ? 0
-                     : c->f32() ? cycles32_smem_bytes(c->pot, R, G.N, G.ncta)
-                              : cycles_smem_bytes(c->pot, c->p.ensemble, false, R, G.N);
-    if (smem > 227 * 1024)
-      return c->fail(PTMC_ERR_LIMIT, "replica state of a run exceeds 227 KB of shared memory (R*N too large)");
+    if (!nn && c->f32()) {
+      while (G.ncta <= 8 && (R % G.ncta != 0 || R / G.ncta > 32 ||
+                             cycles32_smem_bytes(c->pot, R, G.N, G.ncta) > smem_cap))
+        ++G.ncta;
+      if (G.ncta > 8)
+        return c->fail(PTMC_ERR_LIMIT, "FP32 form: the replica state of a run does not fit a "
+                                       "cluster of 8 CTAs (R * N too large)");
+    } else if (!nn && cycles_smem_bytes(c->pot, c->p.ensemble, false, R, G.N) > smem_cap) {
+      c->glob = true;
+    }
+  }
+  if (c->glob && cycles_smem_bytes(c->pot, c->p.ensemble, false, R, 0) > smem_cap)
+    return c->fail(PTMC_ERR_LIMIT, "the slot tables of a run exceed a CTA's shared memory");
+  for (auto& G : c->groups) {
     CK(cudaStreamCreateWithFlags(&G.st, cudaStreamNonBlocking));
     cudaEvent_t e;
     CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -781,6 +797,8 @@ int ptmc_init(ptmc_ctx* c) {
   }
   c->W = wk;
   int W = wk;
+  int maxN_all = 0;
+  for (auto& G : c->groups) maxN_all = std::max(maxN_all, G.N);
   if (c->d_runs.alloc(nr) || c->d_pos.alloc(po) || c->d_mat.alloc(mo) || c->d_comp.alloc(co) ||
       c->d_en.alloc(W) || c->d_box.alloc(W) || c->d_rc2.alloc(W) || c->d_drift.alloc(W) ||
       c->d_beta.alloc(W) || c->d_maxd.alloc(2 * W) || c->d_maxbox.alloc(W) ||
@@ -789,7 +807,8 @@ int ptmc_init(ptmc_ctx* c) {
       (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)) || c->d_boxh.alloc(W) ||
       c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W) ||
       (bpot && c->d_tan.alloc(mo)) || (c->pot == POT_LUT && c->d_lut.alloc(c->lut.size())) ||
-      c->d_pe.alloc(peo) || c->d_lo.alloc(c->f32() && !nn ? po / 3 * 4 : 0))
+      c->d_pe.alloc(peo) || c->d_lo.alloc(c->f32() && !nn ? po / 3 * 4 : 0) ||
+      c->d_scr.alloc(c->glob ? (size_t)W * 4 * maxN_all : 0))
     return c->fail(PTMC_ERR_CUDA, "device allocation failed");
   // host images (the start configurations go up once per run and are
   // expanded into replicas on the device)
@@ -882,6 +901,9 @@ int ptmc_init(ptmc_ctx* c) {
   K.comp = c->d_comp.p;
   K.pe = c->d_pe.p;
   K.lo = c->d_lo.p;
+  K.glob = c->glob ? 1 : 0;
+  K.scr = c->d_scr.p;
+  K.scr_stride = 4LL * maxN_all;  // trial row, tangent row, EAM trial terms (2 N)
   K.en = c->d_en.p;
   K.box = c->d_box.p;
   K.rc2 = c->d_rc2.p;
@@ -1298,6 +1320,7 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_lut.free_();
   c->d_pe.free_();
   c->d_lo.free_();
+  c->d_scr.free_();
   for (auto* b : {&c->d_nn2_rad, &c->d_nn2_ang, &c->d_nn2_W1, &c->d_nn2_W2}) b->free_();
   c->d_nn2_swaps.free_();
   c->d_nn_sf.free_();
@@ -2415,9 +2438,12 @@ extern "C" int ptmc_occupancy(ptmc_ctx* c, int N, int ctas_per_run, int lanes_pe
   if (N < 2) return c->fail(PTMC_ERR_ARG, "ptmc_occupancy: N >= 2");
   const int bc = c->runs.empty() ? PTMC_BC_SPHERE : c->runs[0].bc;
   *ctas_per_sm = 0;
+  // the plain form keeps the per-atom state in HBM when it exceeds a CTA's
+  // shared memory: then only the tables (N = 0) are in shared memory
+  const int Nq = cycles_smem_bytes(c->pot, c->p.ensemble, false, c->R(), N) > 227 * 1024 ? 0 : N;
   int e = c->f32() ? occupancy_cycles32(c->pot, bc, c->p.ensemble, c->R(), N, ctas_per_run,
                                         lanes_per_walker, ctas_per_sm)
-                   : occupancy_cycles(c->pot, bc, c->p.ensemble, c->R(), N, ctas_per_sm);
+                   : occupancy_cycles(c->pot, bc, c->p.ensemble, c->R(), Nq, ctas_per_sm);
   if (e < 0) return c->fail(PTMC_ERR_ARG, "ptmc_occupancy: no cycle kernel for this combination");
   if (e) return c->cuda_fail((cudaError_t)e, "ptmc_occupancy");
   return PTMC_OK;

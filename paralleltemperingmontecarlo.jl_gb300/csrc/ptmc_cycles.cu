@@ -409,16 +409,22 @@ __global__ void __launch_bounds__(1024)
     sp += (bytes + 15) / 16 * 16;
     return p;
   };
-  double* s_pos = (double*)carve((long long)R * N * 3 * 8);
+  // Per-atom state (positions, EAM components, trial rows) sits in shared
+  // memory, or, when a run's replicas do not fit a CTA (P.glob), in HBM:
+  // the positions and components in place, the trial rows in the per-walker
+  // scratch P.scr (L1/L2 serve the rows a move touches).
+  const bool glob = P.glob != 0;
+  const long long NA = glob ? 0 : N;  // atoms held in shared memory per walker
+  double* s_pos = (double*)carve((long long)R * NA * 3 * 8);
   double2* s_c64 = nullptr;
   double2* s_t64 = nullptr;  // EAM: the trial row's (r^-n, r^-m)
   if (POT == POT_EAM) {
-    s_c64 = (double2*)carve((long long)R * N * 16);
-    s_t64 = (double2*)carve((long long)R * N * 16);
+    s_c64 = (double2*)carve((long long)R * NA * 16);
+    s_t64 = (double2*)carve((long long)R * NA * 16);
   }
   // trial row: squared distances (NPT, B potentials) or pair energies (NVT ELJ)
-  double* s_row = (KEEP_M || POT != POT_EAM) ? (double*)carve((long long)R * N * 8) : nullptr;
-  double* s_trow = BPOT ? (double*)carve((long long)R * N * 8) : nullptr;
+  double* s_row = (KEEP_M || POT != POT_EAM) ? (double*)carve((long long)R * NA * 8) : nullptr;
+  double* s_trow = BPOT ? (double*)carve((long long)R * NA * 8) : nullptr;
   double* s_drw = (double*)carve((long long)R * DRAW_BUF * 8);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_maxbox = (double*)carve((long long)R * 8);
@@ -449,8 +455,8 @@ __global__ void __launch_bounds__(1024)
     }
   }
   const double* gpos = P.pos + rd.pos_off;
-  for (int k = tid; k < R * N * 3; k += nthr) s_pos[k] = gpos[k];
-  if (POT == POT_EAM) {
+  if (!glob) for (int k = tid; k < R * N * 3; k += nthr) s_pos[k] = gpos[k];
+  if (POT == POT_EAM && !glob) {
     const double* gc = P.comp + rd.comp_off;
     for (int k = tid; k < R * N; k += nthr) s_c64[k] = make_double2(gc[2 * k], gc[2 * k + 1]);
   }
@@ -490,16 +496,24 @@ __global__ void __launch_bounds__(1024)
   unsigned long long ctr, base;
   int status;
   double *X, *drw, *M, *PE, *TM, *row, *trow;
+  double2 *C2 = nullptr, *T2w = nullptr;  // EAM components and trial terms of the walker
   auto bind = [&](int v) {  // pointers of walker v
     w = v;
-    X = s_pos + (size_t)v * N * 3;
+    X = glob ? P.pos + rd.pos_off + (size_t)v * N * 3 : s_pos + (size_t)v * N * 3;
     drw = s_drw + v * DRAW_BUF;
     M = KEEP_M ? P.mat + rd.mat_off + (size_t)v * N * N : nullptr;
     // NVT pair cache of this walker: ELJ V(r_ij), EAM (r_ij^-n, r_ij^-m)
     PE = PEC ? P.pe + rd.pe_off + (size_t)v * N * N * (POT == POT_EAM ? 2 : 1) : nullptr;
     TM = BPOT ? P.tan + rd.mat_off + (size_t)v * N * N : nullptr;  // tangent matrix
-    row = s_row ? s_row + (size_t)v * N : nullptr;
-    trow = s_trow ? s_trow + (size_t)v * N : nullptr;
+    // HBM scratch of walker v: trial row [N], tangent row [N], EAM trial terms [2N]
+    double* scr = glob ? P.scr + (size_t)(rd.wk + v) * P.scr_stride : nullptr;
+    if (KEEP_M || POT != POT_EAM) row = glob ? scr : s_row + (size_t)v * N;
+    else row = nullptr;
+    trow = BPOT ? (glob ? scr + N : s_trow + (size_t)v * N) : nullptr;
+    if (POT == POT_EAM) {
+      C2 = glob ? (double2*)(P.comp + rd.comp_off) + (size_t)v * N : s_c64 + (size_t)v * N;
+      T2w = glob ? (double2*)(scr + 2 * (size_t)N) : s_t64 + (size_t)v * N;
+    }
   };
   auto load = [&](int v) {  // walker v's state from shared memory
     bind(v);
@@ -663,8 +677,8 @@ __global__ void __launch_bounds__(1024)
     } else {  // EAM energy_update! (src/EnergyEvaluation.jl:1567-1591)
       // calc_components (:1105-1148): the trial row's (r^-n, r^-m); the old
       // ones from the pair cache
-      double2* C = s_c64 + (size_t)w * N;
-      double2* T2 = s_t64 + (size_t)w * N;
+      double2* C = C2;
+      double2* T2 = T2w;
       const double2* Ei = (const double2*)PE + (size_t)i * N;
       for (int j = lane; j < N; j += 32) {
         if (j == i) {
@@ -718,8 +732,8 @@ __global__ void __launch_bounds__(1024)
       }
     }
     if (POT == POT_EAM) {  // swap_vars! EAM (src/swap_config.jl:208-211)
-      double2* C = s_c64 + (size_t)w * N;
-      const double2* T2 = s_t64 + (size_t)w * N;
+      double2* C = C2;
+      const double2* T2 = T2w;
       double2* PE2 = (double2*)PE;
       for (int k = lane; k < N; k += 32) {
         double2 c = C[k];
@@ -1014,8 +1028,8 @@ __global__ void __launch_bounds__(1024)
   if (!multi) save();  // the warps' walker registers to shared memory
   __syncthreads();
   double* gpos_w = P.pos + rd.pos_off;
-  for (int k = tid; k < R * N * 3; k += nthr) gpos_w[k] = s_pos[k];
-  if (POT == POT_EAM) {
+  if (!glob) for (int k = tid; k < R * N * 3; k += nthr) gpos_w[k] = s_pos[k];
+  if (POT == POT_EAM && !glob) {
     double* gc = P.comp + rd.comp_off;
     for (int k = tid; k < R * N; k += nthr) {
       gc[2 * k] = s_c64[k].x;
@@ -1114,7 +1128,9 @@ static int run_instance(int what, const KParams& P, int run0, int nruns, int R,
   if constexpr (F32) {
     if (what == 0 || what == 3) return (int)cudaErrorInvalidValue;  // FP32 form: ptmc_cycles32.cu
   } else if (what == 0 || what == 3) {
-    const long long smem = cycles_smem_bytes(POT, ENS, false, R, maxN);
+    // with the per-atom state in HBM (P.glob) only the slot and walker tables
+    // are in shared memory
+    const long long smem = cycles_smem_bytes(POT, ENS, false, R, P.glob ? 0 : maxN);
     const int e = opt_in64<POT, BC, ENS>(smem);
     if (e) return e;
     if (what == 3)

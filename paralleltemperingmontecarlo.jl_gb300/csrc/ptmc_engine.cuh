@@ -80,6 +80,12 @@ struct KParams {
   float* lo;                // FP32 form, 4 or 8 lanes per walker: lo halves of the
                             // float-float positions during a launch, float4 per
                             // atom at (pos_off / 3 + walker * N)
+  // plain form, runs whose replica state exceeds a CTA's shared memory: the
+  // per-atom state stays in HBM (glob = 1) and each walker has scr_stride
+  // doubles of scratch for its trial rows
+  int glob;
+  long long scr_stride;
+  double* scr;
   double* pe;               // plain form, NVT: pair cache, ELJ N x N V(r_ij) or EAM
                             // N x N (r_ij^-n, r_ij^-m) per walker (see pair_cache)
   double* en;

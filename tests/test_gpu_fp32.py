@@ -133,3 +133,22 @@ def test_n147_cluster8_energy_tracks_fp64(pk, orc):
         assert st["counts"][:, 0].sum() > 0 and st["counts"][:, 5].sum() > 0
     assert 0 < e.stats()["max_drift"]
     e.close()
+
+
+def test_large_n_fp32_spreads_over_a_cluster(pk, orc):
+    """300 atoms x 32 replicas exceed one CTA's shared memory in the FP32 form:
+    the run is spread over a cluster (C = 2 by default); the running energy
+    tracks the oracle's FP64 energy of the returned positions."""
+    import ptmc_gb300.starts as S
+    n = 300
+    rad = 0.9 * n ** (1 / 3) * 3
+    e = engine(pk, N=n, R=32, starts=[S.sphere_start(n, rad, 4.3, 301)], T=(4.0, 16.0),
+               pot=pk.ELJPotentialEven(C_NE), bc=pk.SphericalBC(rad + 3.0), precision="fp32",
+               resync=20, seed=31)
+    e.cycles_nosample(30)
+    st = e.states(0)
+    ref = np.array([orc.elj_config_energy(x, orc.POT_ELJEVEN, C_NE) for x in st["xyz"]])
+    scale = np.array([_abs_pair_sum(x) for x in st["xyz"]])
+    assert np.all(np.abs(st["en_tot"] - ref) <= 1e-6 * scale)
+    assert st["counts"][:, 0].sum() > 0
+    e.close()

@@ -467,3 +467,39 @@ def test_cu55_eam_r64_and_npt_r48_fp64_parity(pk, orc):
     g = compare(eng, o, positions_exact=False)
     assert g["counts"][:, 2].sum() > 0
     eng.close()
+
+
+# ------------------------------------------------------------------
+# Replica state beyond a CTA's shared memory (the reference has no size limit)
+
+def test_large_n_hbm_state_fp64_parity(pk, orc):
+    """32 replicas of 300 (ELJ) and 200 (EAM) atoms and of a 256-atom NPT box
+    need more than 227 KB of per-atom state per run: the plain form keeps
+    positions, EAM components and trial rows in HBM; same chain as the oracle."""
+    n = 300
+    rad = 0.9 * n ** (1 / 3) * 3
+    x0 = sphere_start(n, rad, 4.3, 300)
+    eng, (o,) = pair(pk, orc, N=n, R=32, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                     bc_param=rad + 3.0, exch_prob=1.0, seed=300)
+    eng.cycles_nosample(6)
+    o.cycles(1, 6)
+    g = compare(eng, o)
+    assert g["counts"][:, 0].sum() > 0
+    eng.close()
+    n = 200
+    x0 = sphere_start(n, 0.9 * n ** (1 / 3) * 3, 3.5, 200)
+    pot = pk.EmbeddedAtomPotential(**CU_EAM)
+    eng, (o,) = pair(pk, orc, N=n, R=32, x0=x0, T0=200.0, T1=1000.0, pot=pot,
+                     bc_param=0.9 * n ** (1 / 3) * 3 + 3.0, exch_prob=1.0, seed=201)
+    eng.cycles_nosample(4)
+    o.cycles(1, 4)
+    compare(eng, o)
+    eng.close()
+    x0 = fcc(4, 8.4, 0.05, 256)
+    p = 101325 * 3.398928944382626e-14
+    eng, (o,) = pair(pk, orc, N=256, R=32, x0=x0, T0=10.0, T1=40.0, pot=pk.ELJPotentialEven(C_NE),
+                     ens="npt", bc_param=33.6, exch_prob=1.0, seed=256, pressure=p)
+    eng.cycles_nosample(5)
+    o.cycles(1, 5)
+    compare(eng, o, positions_exact=False)
+    eng.close()
