@@ -816,19 +816,32 @@ class Engine:
         self.close()
 
 
-def ptmc_run(mc_params, temp, start_config, potential, ensemble, *, rdfsave=False,
-             restart=False, save=False, saveconfigs=False, configsname="configuration",
-             workingdirectory=None, precision="fp64", resync_every=1000, exch_prob=0.1,
-             seed=1234, max_displ=None):
+def ptmc_run(mc_params, temp=None, start_config=None, potential=None, ensemble=None, *,
+             rdfsave=False, restart=False, save=False, saveconfigs=False,
+             configsname="configuration", workingdirectory=None, precision="fp64",
+             resync_every=1000, exch_prob=0.1, seed=1234, max_displ=None, eq_cycles=0.2):
     """ptmc_run! (src/MCRun.jl:363-432): initialise, equilibrate, run
     mc_params.mc_cycles production cycles with optional checkpoints every
     `save` cycles into <workingdirectory>/checkpoint, finalise.
+
+    ptmc_run(True, ...) is the reference's resume method (src/MCRun.jl:435-481):
+    parameters, ensemble and potential come from checkpoint/params.data, the
+    states from the checkpoint (the engine's own engine.bin, exact; or the text
+    files a reference run wrote, rebuilt as rebuild_states does), and the run
+    continues to mc_cycles.
 
     Returns (mc_states, results) with slot-ordered states and an Output; with
     rdfsave the radial distribution (Output.rdf) is sampled every 1000th
     production cycle (src/Sampling.jl:341-345)."""
     wd = workingdirectory or os.getcwd()
     ckdir = os.path.join(wd, "checkpoint")
+    if isinstance(mc_params, bool):  # ptmc_run!(restart::Bool; ...)
+        if not mc_params:
+            raise ValueError("ptmc_run(False) has no meaning: pass the run's parameters")
+        restart = True
+        mc_params, temp, ensemble, potential = read_params(ckdir, eq_cycles)
+        ck = read_checkpoint(ckdir)
+        start_config = ck["configs"][0]["config"]
     eng = Engine(mc_params, temp, potential, ensemble, precision=precision,
                  resync_every=resync_every, exch_prob=exch_prob, seed=seed, rdfsave=rdfsave)
     try:
@@ -837,6 +850,10 @@ def ptmc_run(mc_params, temp, start_config, potential, ensemble, *, rdfsave=Fals
         if restart:
             eng.restore(ckdir)
             done = _restored_index(ckdir)
+            if not os.path.exists(os.path.join(ckdir, "engine.bin")):
+                # a reference checkpoint: its loop resumes at the saved index,
+                # so cycle `index` runs again (src/MCRun.jl:455)
+                done -= 1
         else:
             eng.equilibrate()
             done = 0
@@ -862,6 +879,51 @@ def ptmc_run(mc_params, temp, start_config, potential, ensemble, *, rdfsave=Fals
         return states, results
     finally:
         eng.close()
+
+
+def read_params(ckdir, eq_cycles=0.2):
+    """read_init (src/ReadSave.jl:330-345) of checkpoint/params.data: MCParams
+    (with eq_cycles = floor(eq_cycles * cycles) as on restart, :310-320),
+    TempGrid, the ensemble and the potential (ELJ, ELJEven, EAM, ELJB)."""
+    with open(os.path.join(ckdir, "params.data")) as f:
+        rows = [ln.split() for ln in f.read().strip().split("\n")]
+    pv = [float(x) for x in rows[1]]
+    mp = MCParams(int(pv[0]), int(math.floor(eq_cycles * pv[0])), int(pv[1]), int(pv[2]),
+                  int(pv[3]), int(pv[4]), int(pv[5]), pv[6], pv[7])
+    temp = TempGrid(pv[8], pv[9], int(pv[2]))
+    ens = rows[3]
+    if ens[0] == "NVT":
+        ensemble = NVT(int(ens[1]))
+    elif ens[0].startswith("NPT"):
+        ensemble = NPT(int(ens[1]), float(ens[5]), ens[6] == "true")
+    else:
+        raise ValueError("params.data: ensemble %s cannot be rebuilt here" % ens[0])
+    pot = rows[4]
+    # "ELJPotentialEven{6, Float64} c1 ... c6": the type's tokens are not numbers
+    coeff = [float(x) for x in pot[1:] if _is_number(x)]
+    if pot[0].startswith("ELJPotentialEven"):
+        potential = ELJPotentialEven(coeff)
+    elif pot[0].startswith("ELJPotential"):
+        potential = ELJPotential(coeff)
+    elif pot[0] == "EAM:":
+        n, m, ean, ecam = (float(x) for x in pot[1:5])
+        potential = EmbeddedAtomPotential(n, m, ean=ean, eCam=ecam)
+    elif pot[0] == "ELJB":
+        a = [float(x) for x in rows[5]]
+        b = [float(x) for x in rows[6]]
+        c = [float(x) for x in rows[7]]
+        potential = ELJPotentialB(a, b, c)
+    else:
+        raise ValueError("params.data: potential %s cannot be rebuilt here" % pot[0])
+    return mp, temp, ensemble, potential
+
+
+def _is_number(t):
+    try:
+        float(t)
+        return True
+    except ValueError:
+        return False
 
 
 def _restored_index(ckdir):

@@ -1373,6 +1373,235 @@ int undump(ptmc_ctx* c, const std::string& b, size_t& at, DBuf<T>& d) {
 }
 }  // namespace
 
+// ------------------------------------------------------- reference restart
+// rebuild_states (src/ReadSave.jl:436-481) with initialisation's restart
+// branch (src/Initialization.jl:103-119): the states of run 0 from the text
+// files a reference checkpoint holds, when the directory has no engine.bin.
+namespace {
+
+void drop_graphs(ptmc_ctx* c);  // captured launches hold the old kernel parameters
+
+// whitespace-separated tokens of every line of a text file
+bool read_table(const std::string& path, std::vector<std::vector<std::string>>& rows) {
+  std::ifstream f(path);
+  if (!f) return false;
+  rows.clear();
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream ls(line);
+    std::vector<std::string> t;
+    std::string tok;
+    while (ls >> tok) t.push_back(tok);
+    if (!t.empty()) rows.push_back(t);
+  }
+  return true;
+}
+
+bool to_double(std::string t, double& v) {
+  while (!t.empty() && t.back() == ',') t.pop_back();  // "box_dims: L, H" (src/ReadSave.jl:133-135)
+  char* end = nullptr;
+  v = std::strtod(t.c_str(), &end);
+  return end && *end == '\0' && !t.empty();
+}
+
+// launches the kernels that evaluate every walker's energy (and the potential
+// variables: EAM components, distance matrices, pair caches, symmetry
+// functions) from the positions on the device
+int init_energies(ptmc_ctx* c) {
+  const int W = c->W, R = c->R();
+  if (c->pot == POT_NN2) {
+    int e = nn2_launch_init(c->K, c->Q2, W, c->nn_Nmax, c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_nn2_init launch");
+  } else if (c->pot == POT_NN) {
+    int e = nn_launch_init(c->K, c->Q, W, c->nn_Nmax, !c->f32(), c->st);
+    if (e) return c->cuda_fail((cudaError_t)e, "k_nn_init launch");
+  } else {
+    for (auto& G : c->groups) {
+      int e = launch_init(c->pot, c->bc(), c->p.ensemble, c->f32(), c->K, G.dev0, G.nruns, R, c->st);
+      if (e) return c->cuda_fail((cudaError_t)e, "k_init launch");
+    }
+  }
+  c->stats.kernel_launches += c->groups.size();
+  CK(cudaStreamSynchronize(c->st));
+  return PTMC_OK;
+}
+
+int restore_reference_text(ptmc_ctx* c, const std::string& d) {
+  if (c->p.n_runs != 1)
+    return c->fail(PTMC_ERR_STATE, "a reference checkpoint holds one run: restore it into a context "
+                                   "with n_runs = 1");
+  const int R = c->R(), W = c->W;
+  RunDesc& r = c->rd[0];
+  const int N = r.N, nb = c->p.n_bin + 2;
+  const bool npt = c->p.ensemble == PTMC_NPT;
+  std::vector<std::vector<std::string>> t;
+  // hist_info.data: header row, then e_min e_max v_min v_max dE dV dr2
+  double hi[7];
+  if (!read_table(d + "/hist_info.data", t) || t.size() < 2 || t[1].size() < 7)
+    return c->fail(PTMC_ERR_IO, "cannot read " + d + "/hist_info.data");
+  for (int k = 0; k < 7; ++k)
+    if (!to_double(t[1][k], hi[k])) return c->fail(PTMC_ERR_IO, "hist_info.data: bad number");
+  // histograms.data: one row of n_bin + 2 counts per state
+  std::vector<unsigned int> hist((size_t)R * r.hist_stride, 0u);
+  if (!read_table(d + "/histograms.data", t) || (int)t.size() != R)
+    return c->fail(PTMC_ERR_IO, "histograms.data: need " + std::to_string(R) + " rows");
+  if (!npt)
+    for (int s = 0; s < R; ++s) {
+      if ((int)t[s].size() != nb) return c->fail(PTMC_ERR_IO, "histograms.data: row length is not n_bin + 2");
+      for (int k = 0; k < nb; ++k) {
+        double v;
+        if (!to_double(t[s][k], v)) return c->fail(PTMC_ERR_IO, "histograms.data: bad number");
+        hist[(size_t)s * r.hist_stride + k] = (unsigned int)std::llround(v);
+      }
+    }
+  if (npt) {  // volume_hist.data: each state's E x V matrix, column-major (V index outer)
+    if (!read_table(d + "/volume_hist.data", t) || (int)t.size() != R)
+      return c->fail(PTMC_ERR_IO, "volume_hist.data: need " + std::to_string(R) + " rows");
+    for (int s = 0; s < R; ++s) {
+      if ((long long)t[s].size() != (long long)nb * nb)
+        return c->fail(PTMC_ERR_IO, "volume_hist.data: row length is not (n_bin + 2)^2");
+      for (int iv = 0; iv < nb; ++iv)
+        for (int ie = 0; ie < nb; ++ie) {
+          double v;
+          if (!to_double(t[s][(size_t)iv * nb + ie], v))
+            return c->fail(PTMC_ERR_IO, "volume_hist.data: bad number");
+          hist[(size_t)s * r.hist_stride + (size_t)ie * nb + iv] = (unsigned int)std::llround(v);
+        }
+    }
+  }
+  std::vector<unsigned int> rdf;
+  if (c->rdf_on && read_table(d + "/rdf.data", t)) {
+    const int nr = 5 * c->p.n_bin;
+    if ((int)t.size() != R) return c->fail(PTMC_ERR_IO, "rdf.data: need one row per state");
+    rdf.assign((size_t)W * nr, 0u);
+    for (int s = 0; s < R; ++s)
+      for (int k = 0; k < nr && k < (int)t[s].size(); ++k) {
+        double v;
+        if (!to_double(t[s][k], v)) return c->fail(PTMC_ERR_IO, "rdf.data: bad number");
+        rdf[(size_t)(r.wk + s) * nr + k] = (unsigned int)std::llround(v);
+      }
+  }
+  long long index = 1;
+  if (read_table(d + "/index.txt", t) && !t.empty()) {
+    double v;
+    if (!to_double(t[0][0], v)) return c->fail(PTMC_ERR_IO, "index.txt: bad number");
+    index = (long long)v;
+  }
+  // configT<i>.xyz: N, then "<BC type> <label> <bc values> max_displ[1:3]
+  // count_atom count_vol", then N rows "1 x y z" (src/ReadSave.jl:142-165,
+  // read_checkpoint_config :371-396)
+  std::vector<double> pos((size_t)R * N * 3), box(R), boxh(R), rc2(R), maxd(2 * R), maxbox(R),
+      maxboxh(R), maxd_sep(2 * R);
+  std::vector<long long> cnt(6 * (size_t)R, 0);
+  const int bc = c->bc();
+  for (int s = 0; s < R; ++s) {
+    const std::string path = d + "/configT" + std::to_string(s + 1) + ".xyz";
+    if (!read_table(path, t) || t.size() < 2) return c->fail(PTMC_ERR_IO, "cannot read " + path);
+    double nv;
+    if (!to_double(t[0][0], nv) || (int)nv != N || (int)t.size() < 2 + N)
+      return c->fail(PTMC_ERR_IO, path + ": not " + std::to_string(N) + " atoms");
+    const std::vector<std::string>& h = t[1];
+    const bool two = bc == PTMC_BC_RECTANGULAR || bc == PTMC_BC_RHOMBIC;
+    const char* want = bc == PTMC_BC_SPHERE ? "SphericalBC" : bc == PTMC_BC_CUBIC ? "CubicBC"
+                       : bc == PTMC_BC_RECTANGULAR ? "RectangularBC" : "RhombicBC";
+    if (h[0].compare(0, std::strlen(want), want) != 0)
+      return c->fail(PTMC_ERR_IO, path + ": boundary condition is not " + want);
+    const size_t nv_needed = two ? 9 : 8;
+    if (h.size() < nv_needed) return c->fail(PTMC_ERR_IO, path + ": short comment line");
+    double b0, b1 = 0.0, md[3], ca, cv;
+    bool ok = to_double(h[2], b0);
+    size_t at = 3;
+    if (two) ok = ok && to_double(h[at++], b1);
+    for (int k = 0; k < 3; ++k) ok = ok && to_double(h[at++], md[k]);
+    ok = ok && to_double(h[at++], ca) && to_double(h[at++], cv);
+    if (!ok) return c->fail(PTMC_ERR_IO, path + ": bad comment line");
+    const double L = bc == PTMC_BC_SPHERE ? std::sqrt(b0) : b0;  // the sphere line holds r^2
+    box[s] = L;
+    boxh[s] = two ? b1 : 0.0;
+    rc2[s] = bc == PTMC_BC_CUBIC         ? L * L / 4
+             : bc == PTMC_BC_RECTANGULAR ? std::min(L * L / 4, b1 * b1 / 4)
+             : bc == PTMC_BC_RHOMBIC     ? std::min(L * L * 3 / 16, b1 * b1 / 4)
+                                         : 0.0;
+    // MCState(...; max_displ, count_atom = [count, 0], count_vol = [count, 0]):
+    // the totals are kept, the adaptation counters start at zero, and the
+    // state's box limits follow from the restored box (MCStates.jl:63-87)
+    maxd[2 * s] = md[0];
+    maxd[2 * s + 1] = md[1];
+    maxd_sep[2 * s] = md[2];
+    maxd_sep[2 * s + 1] = 0.1;
+    maxbox[s] = bc == PTMC_BC_SPHERE ? 30.0 : L * 1.8;
+    maxboxh[s] = bc == PTMC_BC_SPHERE ? 30.0 : b1 * 1.8;
+    cnt[6 * (size_t)s + 0] = (long long)ca;
+    cnt[6 * (size_t)s + 2] = (long long)cv;
+    // recentre! of every state (src/Initialization.jl:114-116)
+    double cx = 0, cy = 0, cz = 0;
+    double* X = &pos[(size_t)s * N * 3];
+    for (int a = 0; a < N; ++a) {
+      const std::vector<std::string>& row = t[2 + a];
+      if (row.size() < 4 || !to_double(row[1], X[3 * a]) || !to_double(row[2], X[3 * a + 1]) ||
+          !to_double(row[3], X[3 * a + 2]))
+        return c->fail(PTMC_ERR_IO, path + ": bad position row");
+      cx += X[3 * a];
+      cy += X[3 * a + 1];
+      cz += X[3 * a + 2];
+    }
+    cx /= N;
+    cy /= N;
+    cz /= N;
+    for (int a = 0; a < N; ++a) {
+      X[3 * a] -= cx;
+      X[3 * a + 1] -= cy;
+      X[3 * a + 2] -= cz;
+    }
+  }
+  // device state of run 0: walker s in slot s, fresh draw streams
+  const int wk = r.wk;
+  std::vector<int> wos(R);
+  for (int s = 0; s < R; ++s) wos[s] = s;
+  std::vector<double> zero2(2 * (size_t)R, 0.0);
+  std::vector<unsigned long long> ctr(R, 0ull);
+  std::vector<int> st(R, 0);
+  cudaStream_t q = c->st;
+  CK(cudaMemcpyAsync(c->d_pos.p + r.pos_off, pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_box.p + wk, box.data(), sizeof(double) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_boxh.p + wk, boxh.data(), sizeof(double) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_rc2.p + wk, rc2.data(), sizeof(double) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_maxd.p + 2 * wk, maxd.data(), sizeof(double) * 2 * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_maxd_sep.p + 2 * wk, maxd_sep.data(), sizeof(double) * 2 * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_maxbox.p + wk, maxbox.data(), sizeof(double) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_maxboxh.p + wk, maxboxh.data(), sizeof(double) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_cnt.p + 6 * (size_t)wk, cnt.data(), sizeof(long long) * cnt.size(), cudaMemcpyHostToDevice, q));
+  CK(cudaMemsetAsync(c->d_cnt_sep.p + 4 * (size_t)wk, 0, sizeof(long long) * 4 * R, q));
+  CK(cudaMemcpyAsync(c->d_ham.p + 2 * wk, zero2.data(), sizeof(double) * 2 * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_hist.p + r.hist_off, hist.data(), sizeof(unsigned int) * hist.size(), cudaMemcpyHostToDevice, q));
+  if (!rdf.empty())
+    CK(cudaMemcpyAsync(c->d_rdf.p, rdf.data(), sizeof(unsigned int) * rdf.size(), cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_wos.p + wk, wos.data(), sizeof(int) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_ctr.p + wk, ctr.data(), sizeof(unsigned long long) * R, cudaMemcpyHostToDevice, q));
+  CK(cudaMemcpyAsync(c->d_status.p + wk, st.data(), sizeof(int) * R, cudaMemcpyHostToDevice, q));
+  r.n_start = R;  // every walker has its own configuration
+  r.en_min = hi[0];
+  r.en_max = hi[1];
+  r.v_min = hi[2];
+  r.v_max = hi[3];
+  r.dE = hi[4];
+  r.dV = hi[5];
+  r.dr2 = hi[6];
+  // the reference's loop resumes at the saved index (src/MCRun.jl:455: i in
+  // start_counter:mc_cycles), so cycle `index` runs again
+  r.cyc[PHASE_PROD] = index;
+  r.run_ctr = 0;
+  int rc = push_runs(c);
+  if (rc) return rc;
+  rc = init_energies(c);
+  if (rc) return rc;
+  c->equilibrated = true;
+  drop_graphs(c);
+  return PTMC_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int ptmc_checkpoint(ptmc_ctx* c, const char* dir) {
@@ -1515,7 +1744,12 @@ int ptmc_restore(ptmc_ctx* c, const char* dir) {
   if (!c->inited) return c->fail(PTMC_ERR_STATE, "call ptmc_init before ptmc_restore");
   std::string path = std::string(dir) + "/engine.bin";
   FILE* f = std::fopen(path.c_str(), "rb");
-  if (!f) return c->fail(PTMC_ERR_IO, "cannot open " + path);
+  if (!f) {
+    struct stat sb;
+    if (::stat((std::string(dir) + "/hist_info.data").c_str(), &sb) == 0)
+      return restore_reference_text(c, dir);  // a checkpoint the reference wrote
+    return c->fail(PTMC_ERR_IO, "cannot open " + path + " (and no reference checkpoint files)");
+  }
   std::string b;
   char buf[1 << 16];
   size_t k;

@@ -133,3 +133,32 @@ def test_julia_float_text(pk):
              3.166811429e-6: "3.166811429e-6", -0.00123: "-0.00123"}
     for x, t in cases.items():
         assert pk._jl(x) == t, (x, pk._jl(x), t)
+
+
+def test_read_params_of_a_reference_checkpoint(pk, tmp_path):
+    """read_init's params.data (src/ReadSave.jl:280-345): MCParams with the
+    restart's eq_cycles = floor(0.2 cycles), TempGrid, ensemble, potential."""
+    ck = tmp_path / "checkpoint"
+    ck.mkdir()
+    (ck / "params.data").write_text(
+        "cycles: sample_rate: n_traj: n_atoms: n_adjust n_bins min_acc: max_acc t_i: t_f\n"
+        "1.0e6 1.0 24.0 55.0 100.0 100.0 0.4 0.6 6.0 20.0\n"
+        "ensemble n_atom_moves n_atom_swaps\n"
+        "NVT 55 55 0\n"
+        "ELJPotentialEven{6, Float64} -10.5097942564988 989.725135614556 -101383.865938807 "
+        "3.91884612841668e6 -5.62340834334278e7 2.88738837441765e8\n")
+    mp, temp, ens, pot = pk.read_params(str(ck))
+    assert (mp.mc_cycles, mp.eq_cycles, mp.n_traj, mp.n_atoms, mp.n_bin) == (10 ** 6, 200000, 24, 55, 100)
+    assert temp.t_grid[0] == 6.0 and temp.t_grid[-1] == pytest.approx(20.0, rel=1e-15)
+    assert isinstance(ens, pk.NVT) and ens.n_atoms == 55
+    assert isinstance(pot, pk.ELJPotentialEven) and pot.coeff[3] == 3.91884612841668e6
+    (ck / "params.data").write_text(
+        "cycles: sample_rate: n_traj: n_atoms: n_adjust n_bins min_acc: max_acc t_i: t_f\n"
+        "1000.0 1.0 8.0 32.0 100.0 50.0 0.4 0.6 10.0 40.0\n"
+        "ensemble n_atom_moves n_volume_moves n_atom_swaps pressure separated_volume\n"
+        "NPT 32 32 1 0 3.4439647528956955e-9 false\n"
+        "EAM: 8.482 4.692 1.23 4.56 \n")
+    mp, temp, ens, pot = pk.read_params(str(ck))
+    assert isinstance(ens, pk.NPT) and ens.pressure == 3.4439647528956955e-9
+    assert not ens.separated_volume and mp.n_bin == 50
+    assert isinstance(pot, pk.EmbeddedAtomPotential) and (pot.n, pot.ean, pot.eCam) == (8.482, 1.23, 4.56)
