@@ -84,3 +84,39 @@ def test_nn_cu55_initial_energy_fp32_vs_fp64(pk, orc):
     assert st["counts"][:, 0].sum() > 0
     e64.close()
     e32.close()
+
+
+def _pin_clusters():
+    import symm_restatement as SR
+    rng = np.random.default_rng(7)
+    x = [np.zeros(3)]
+    while len(x) < 5:                      # a scalene 5-atom cluster, r >= 3.6 bohr
+        p = rng.uniform(-6.0, 6.0, 3)
+        if np.linalg.norm(np.array(x) - p, axis=1).min() > 3.6:
+            x.append(p)
+    return {"tetra": SR.tetrahedron(4.8), "right+far": SR.right_triangle_plus_far(4.8, 20.0),
+            "scalene5": np.array(x)}
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-12), ("fp32", 1e-5)])
+@pytest.mark.parametrize("name", ["tetra", "right+far", "scalene5"])
+def test_nn_energy_pinned_by_restatement(pk, orc, precision, rtol, name):
+    """The engine's initial energies against the independent numpy restatement of
+    SymmFunc.jl (tests/symm_restatement.py: hand-checked closed forms on the
+    tetrahedron and the right triangle), not against the oracle; then a short
+    chain, and the running energies against the restatement's energies of the
+    engine's own final positions."""
+    import symm_restatement as SR
+    pot, _ = nn_potential(pk)
+    x = _pin_clusters()[name]
+    eng, _ = setup(pk, orc, pot, x, 2, precision, 30.0)
+    ea = SR.mlp(SR.g_matrix(x, pot.sf), pot.weights, pot.nodes)
+    tol = rtol * np.abs(ea).sum()
+    np.testing.assert_allclose(eng.states(0)["en_tot"], ea.sum(), rtol=0, atol=tol)
+    eng.cycles_nosample(20)
+    st = eng.states(0)
+    assert st["counts"][:, 0].sum() > 0
+    for s in range(2):
+        e = SR.energy(st["xyz"][s], pot.sf, pot.weights, pot.nodes)
+        assert abs(st["en_tot"][s] - e) <= (1e-10 if precision == "fp64" else 1e-4) * np.abs(ea).sum()
+    eng.close()

@@ -108,3 +108,30 @@ def test_nnvt_argument_errors(pk):
     e.close()
     with pytest.raises(ValueError, match="NNVT"):
         pk.Engine(mp, temp, pot, pk.NVT(12))
+
+
+@pytest.mark.parametrize("N,n1", [(4, 2), (4, 1), (9, 5)])
+def test_nnvt_energy_pinned_by_restatement(pk, orc, N, n1):
+    """Initial and running energies against the independent numpy restatement of
+    the two-species symmetry functions (tests/symm_restatement.py; SymmFunc.jl:
+    318-541) instead of the oracle: the regular tetrahedron (closed form) and a
+    9-atom cluster, before and after a chain with atom moves and swaps."""
+    import symm_restatement as SR
+    import ptmc_gb300.starts as st
+    rad, ang, w1, w2, nodes = S.potential()
+    x0 = SR.tetrahedron(4.8) if N == 4 else st.sphere_start(N, 6.0, 4.2, 3)
+    mp = pk.MCParams(mc_cycles=100, eq_cycles=0, mc_sample=1, n_traj=3, n_atoms=N)
+    temp = pk.TempGrid(300.0, 900.0, 3)
+    pot = pk.RuNNerPotential2Atom(rad, ang, w1, w2, nodes, n1)
+    eng = pk.Engine(mp, temp, pot, pk.NNVT((n1, N - n1), 1), exch_prob=1.0, seed=4)
+    eng.set_configs(0, pk.Config(x0, pk.SphericalBC(9.0)))
+    eng.init()
+    e0 = SR.energy2(x0, rad, ang, w1, w2, nodes, n1)
+    np.testing.assert_allclose(eng.states(0)["en_tot"], e0, rtol=1e-12)
+    eng.cycles_nosample(60)
+    g = eng.states(0)
+    assert g["counts"][:, 0].sum() > 0 and eng.swaps(0) > 0
+    for s in range(3):
+        np.testing.assert_allclose(g["en_tot"][s], SR.energy2(g["xyz"][s], rad, ang, w1, w2, nodes, n1),
+                                   rtol=1e-10)
+    eng.close()
