@@ -399,6 +399,15 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
                   accepted_per_s=res["fp32_da"]["acceptance"] * res["fp32_da"]["value"],
                   accepted_per_s_exact=(res["fp32"]["acceptance"] * res["fp32"]["value"]
                                         if "fp32" in res else None))
+        if "fp32" in res:
+            # time per attempted move under screening = (r + p1) x exact time per
+            # move, p1 = fraction evaluated exactly: r is the stage-1 cost as a
+            # fraction of an exact move; with stage 1 free (r = 0) accepted moves
+            # per second could rise at most (a / a0) / p1
+            p1 = da["exact_eval_frac"]
+            da.update(stage1_cost_frac=res["fp32"]["value"] / res["fp32_da"]["value"] - p1,
+                      accepted_gain=da["accepted_per_s"] / da["accepted_per_s_exact"],
+                      accepted_gain_bound_free_stage1=(da["acceptance"] / da["acceptance_exact"]) / p1)
         res["fp32_da"]["da"] = da
         eng.close()
         if not args.only_chosen:

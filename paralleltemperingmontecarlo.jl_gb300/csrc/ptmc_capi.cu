@@ -556,7 +556,8 @@ int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf, const double* 
   if (H1 < 1 || H2 < 1 || H1 > 64 || H2 > 64) return c->fail(PTMC_ERR_LIMIT, "NN: hidden layers of 1..64 nodes");
   long long need = (long long)nsf * H1 + H1 + (long long)H1 * H2 + H2 + H2 + 1;
   if (need != nw) return c->fail(PTMC_ERR_ARG, "NN: weight count does not match the layer sizes");
-  // active functions: radial type 11 in table order, angular type 111 sorted by eta
+  // active functions: radial type 11 in table order, angular type 111 sorted by
+  // (eta, lambda, zeta)
   std::vector<int> rad, ang;
   double rc = -1;
   for (int k = 0; k < nsf; ++k) {
@@ -567,7 +568,13 @@ int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf, const double* 
     if (kind == 0 && type == 11) rad.push_back(k);
     if (kind == 1 && type == 111) ang.push_back(k);
   }
-  std::stable_sort(ang.begin(), ang.end(), [&](int a, int b) { return sf[8 * a + 2] < sf[8 * b + 2]; });
+  std::stable_sort(ang.begin(), ang.end(), [&](int a, int b) {
+    const double* x = sf + 8 * a;
+    const double* y = sf + 8 * b;
+    if (x[2] != y[2]) return x[2] < y[2];
+    if (x[3] != y[3]) return x[3] < y[3];
+    return x[4] < y[4];
+  });
   if ((int)ang.size() > MAX_NN_ANG) return c->fail(PTMC_ERR_LIMIT, "NN: at most 32 active angular functions");
   std::vector<int> act(rad);
   act.insert(act.end(), ang.begin(), ang.end());
@@ -599,6 +606,33 @@ int ptmc_set_potential_nn(ptmc_ctx* c, const double* sf, int nsf, const double* 
   c->nn_boundary2 = boundary * boundary;
   c->Q.SR = (int)rad.size();
   c->Q.SA = (int)ang.size();
+  // a sorted angular set whose structure (eta groups, lambda signs, zeta
+  // powers) matches a compiled pattern runs the table-specialised FP32 kernel;
+  // the eta values themselves are runtime parameters
+  c->Q.ang_pat = NN_PAT_GENERIC;
+  for (int pat : {NN_PAT_CU55}) {
+    const int n = nn_pat_sa(pat);
+    if ((int)ang.size() != n) continue;
+    bool ok = true;
+    int g = -1;
+    float nle[8] = {};
+    for (int q = 0; q < n && ok; ++q) {
+      const double* r = sf + 8 * ang[q];
+      const double eta = r[2], lam = r[3], zeta = r[4];
+      if (q == 0 || eta != sf[8 * ang[q - 1] + 2]) {
+        if (++g >= 8) break;
+        nle[g] = (float)(-eta * 1.4426950408889634);
+      }
+      const int e = zeta == 1 ? 0 : zeta == 2 ? 1 : zeta == 4 ? 2 : zeta == 8 ? 3 : zeta == 16 ? 4 : -1;
+      ok = e >= 0 && (lam == 1.0 || lam == -1.0) &&
+           nn_pat_term(pat, q) == (g | ((lam < 0 ? 1 : 0) << 4) | (e << 5));
+    }
+    if (ok && g + 1 == nn_pat_ng(pat)) {
+      c->Q.ang_pat = pat;
+      for (int k = 0; k < 8; ++k) c->Q.ang_nle[k] = nle[k];
+      break;
+    }
+  }
   c->pot = POT_NN;
   return PTMC_OK;
 }

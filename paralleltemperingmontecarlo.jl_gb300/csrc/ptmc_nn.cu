@@ -90,8 +90,8 @@ template <typename Real>
 struct NNSmem {
   double* Xd;  // [N][3] positions (FP64 master: proposals and commits)
   Real* X;     // [N][3] positions in the arithmetic type
-  Real* D2;    // [N][N]
-  Real* F;     // [N][N]
+  Real* D2;    // [N][ld]
+  Real* F;     // [N][ld]
   Real* G;     // [S][N]
   Real* dG;    // [S][N]
   Real* part;  // [NCH][SA][64]
@@ -108,6 +108,13 @@ struct NNSmem {
   double* drw; // draw buffer [16]
   double* tpos;// trial position [3]
   int* flags;  // [4]
+  int ld;      // row stride of D2 and F: N rounded up to even, so that lanes
+               // reading (j, j + d) pairs (stride ld + 1) hit distinct banks
+  // FP32 form: per-move rows packed for the table-specialised angular loop
+  float4* pr4;  // [64] {d2n, fn, d2o, fo}
+  float4* vn4;  // [64] {t - x_j, 1 / r_new}
+  float4* vo4;  // [64] {x_i - x_j, 1 / r_old}
+  float* tpzf;  // [MAX_NN_ANG] tpz of the angular functions
 };
 
 template <typename Real>
@@ -121,23 +128,39 @@ __device__ size_t nn_carve(NNSmem<Real>& s, unsigned char* base, int N, int S, i
   };
   s.Xd = (double*)take(sizeof(double) * N * 3);
   s.X = (Real*)take(sizeof(Real) * N * 3);
-  s.D2 = (Real*)take(sizeof(Real) * N * N);
-  s.F = (Real*)take(sizeof(Real) * N * N);
+  s.ld = N + (N & 1);
+  s.D2 = (Real*)take(sizeof(Real) * N * s.ld);
+  s.F = (Real*)take(sizeof(Real) * N * s.ld);
   s.G = (Real*)take(sizeof(Real) * S * N);
   s.dG = (Real*)take(sizeof(Real) * S * N);
-  s.part = (Real*)take(sizeof(Real) * NCH * (SA > 0 ? SA : 1) * 64);
+  // the FP32 form runs the MLP on the tensor cores (weights staged straight
+  // from global memory into its tiles) and keeps the angular partial sums in
+  // the MLP input tile, which is free until the MLP phase of the move: only
+  // the FP64 form carves the weights, hidden activations and partial sums
+  s.part = s.W = s.h1 = s.h2 = nullptr;
+  if constexpr (sizeof(Real) == 8) s.part = (Real*)take(sizeof(Real) * NCH * (SA > 0 ? SA : 1) * 64);
   s.rows = (Real*)take(sizeof(Real) * 8 * 64);
   s.vn = (Real*)take(sizeof(Real) * 64 * 3);
   s.vo = (Real*)take(sizeof(Real) * 64 * 3);
-  s.W = (Real*)take(sizeof(Real) * nW);
-  s.h1 = (Real*)take(sizeof(Real) * N * H1);
-  s.h2 = (Real*)take(sizeof(Real) * N * H2);
+  if constexpr (sizeof(Real) == 8) {
+    s.W = (Real*)take(sizeof(Real) * nW);
+    s.h1 = (Real*)take(sizeof(Real) * N * H1);
+    s.h2 = (Real*)take(sizeof(Real) * N * H2);
+  }
   s.red = (Real*)take(sizeof(Real) * 64);
   s.dGi = (Real*)take(sizeof(Real) * (S > 0 ? S : 1));
   s.sfp = (Real*)take(sizeof(Real) * 4 * MAX_NN_ANG);
   s.drw = (double*)take(sizeof(double) * DRAW_BUF);
   s.tpos = (double*)take(sizeof(double) * 4);
   s.flags = (int*)take(sizeof(int) * 4);
+  s.pr4 = s.vn4 = s.vo4 = nullptr;
+  s.tpzf = nullptr;
+  if constexpr (sizeof(Real) == 4) {
+    s.pr4 = (float4*)take(sizeof(float4) * 64);
+    s.vn4 = (float4*)take(sizeof(float4) * 64);
+    s.vo4 = (float4*)take(sizeof(float4) * 64);
+    s.tpzf = (float*)take(sizeof(float) * MAX_NN_ANG);
+  }
   return off;
 }
 
@@ -204,10 +227,12 @@ __device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X,
     s.Xd[k] = X[k];
     s.X[k] = (Real)X[k];
   }
-  for (int k = threadIdx.x; k < Q.nW; k += blockDim.x) s.W[k] = (Real)Q.W[k];
+  if (s.W)
+    for (int k = threadIdx.x; k < Q.nW; k += blockDim.x) s.W[k] = (Real)Q.W[k];
   for (int q = threadIdx.x; q < Q.SA; q += blockDim.x) {
     const NNSF& f = Q.sf[Q.SR + q];
     if constexpr (sizeof(Real) == 4) {  // exponent form of the FP32 path
+      s.tpzf[q] = (float)f.tpz;
       s.sfp[4 * q] = (Real)(-f.eta * 1.4426950408889634);
       s.sfp[4 * q + 1] = (Real)f.zeta;
       s.sfp[4 * q + 2] = (Real)log2(f.tpz);
@@ -227,8 +252,9 @@ __device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X,
     Real dx = s.X[3 * a] - s.X[3 * b], dy = s.X[3 * a + 1] - s.X[3 * b + 1],
          dz = s.X[3 * a + 2] - s.X[3 * b + 2];
     Real d2 = (dx * dx + dy * dy) + dz * dz;
-    s.D2[t] = a == b ? Real(0) : d2;
-    s.F[t] = cutoff<Real>(sqrt(s.D2[t]), (Real)Q.rcut);
+    if (a == b) d2 = Real(0);
+    s.D2[a * s.ld + b] = d2;
+    s.F[a * s.ld + b] = cutoff<Real>(sqrt(d2), (Real)Q.rcut);
   }
   __syncthreads();
 }
@@ -244,6 +270,8 @@ __device__ void load_walker(const NNParams& Q, NNSmem<Real>& s, const double* X,
 // form keeps the CUDA-core MLP.
 constexpr uint32_t MLP_LBO = 128, MLP_SBO = 1024;  // K = 32 TF32: 8 core matrices per row group
 constexpr size_t MLP_TC_BYTES = 2 * 16384 + 4 * 4096 + 512 + 16;
+static_assert(NCH * MAX_NN_ANG * 64 * sizeof(float) <= 2 * 16384,
+              "angular partial sums must fit the MLP input tile");
 
 struct MlpSmem {
   unsigned char *Ah, *Al;              // 128 x 32 TF32 inputs (hi, lo)
@@ -265,14 +293,15 @@ __device__ __forceinline__ void mlp_carve(MlpSmem& m, unsigned char* base) {
   m.tslot = (uint32_t*)(base + 49152 + 520);
 }
 
-// W: gathered parameters W1[S][H1], b1, W2[H1][H2], b2, w3[H2], b3
-__device__ void mlp_stage(const MlpSmem& m, const float* W, int S, int H1, int H2) {
-  const float* W2 = W + S * H1 + H1;
+// W: gathered parameters W1[S][H1], b1, W2[H1][H2], b2, w3[H2], b3 (global
+// memory, rounded to FP32 here)
+__device__ void mlp_stage(const MlpSmem& m, const double* W, int S, int H1, int H2) {
+  const double* W2 = W + S * H1 + H1;
   for (int e = threadIdx.x; e < 2 * 16384 / 4; e += blockDim.x) ((float*)m.Ah)[e] = 0.f;
   for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
     const int n = e / 32, k = e % 32;
-    const float x1 = (k < S && n < H1) ? W[k * H1 + n] : 0.f;
-    const float x2 = (k < H1 && n < H2) ? W2[k * H2 + n] : 0.f;
+    const float x1 = (k < S && n < H1) ? (float)W[k * H1 + n] : 0.f;
+    const float x2 = (k < H1 && n < H2) ? (float)W2[k * H2 + n] : 0.f;
     const uint32_t o = umma_off32(n, k, MLP_LBO, MLP_SBO);
     const float h1 = tf32_hi(x1), h2 = tf32_hi(x2);
     *(float*)(m.B1h + o) = h1;
@@ -281,12 +310,12 @@ __device__ void mlp_stage(const MlpSmem& m, const float* W, int S, int H1, int H
     *(float*)(m.B2l + o) = x2 - h2;
   }
   for (int n = threadIdx.x; n < 32; n += blockDim.x) {
-    m.vec[n] = n < H1 ? W[S * H1 + n] : 0.f;
-    m.vec[32 + n] = n < H2 ? W2[H1 * H2 + n] : 0.f;
-    m.vec[64 + n] = n < H2 ? W2[H1 * H2 + H2 + n] : 0.f;
+    m.vec[n] = n < H1 ? (float)W[S * H1 + n] : 0.f;
+    m.vec[32 + n] = n < H2 ? (float)W2[H1 * H2 + n] : 0.f;
+    m.vec[64 + n] = n < H2 ? (float)W2[H1 * H2 + H2 + n] : 0.f;
   }
   if (threadIdx.x == 0) {
-    m.vec[96] = W2[H1 * H2 + 2 * H2];
+    m.vec[96] = (float)W2[H1 * H2 + 2 * H2];
     mbar_init(smem_u32(m.mbar), 1);
   }
   fence_async_smem();
@@ -311,21 +340,32 @@ __device__ __forceinline__ void mlp_issue(uint32_t tbase, const unsigned char* A
 // E = sum_a MLP(G[:, a] (+ dG[:, a])); every thread calls it.  `ph` is the
 // mbarrier parity (flipped twice); *bad is set (uniformly) when a
 // tensor-core wait ran out.
+// tanh(x) = 1 - 2 / (1 + 2^(2 log2(e) x)) with MUFU ex2 and rcp: absolute
+// error ~3e-7 (the FP32 form's MLP; saturates to +-1 without overflow)
+__device__ __forceinline__ float tanh_mufu(float x) {
+  return 1.f - __fdividef(2.f, 1.f + ex2f(x * 2.8853900817779268f));
+}
+
 __device__ float mlp_energy_tc(const NNSmem<float>& s, const MlpSmem& m, int N, int S, int H1,
                                int H2, bool with_delta, uint32_t tbase, uint32_t& ph, int* bad) {
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mb = smem_u32(m.mbar);
-  for (int t = tid; t < 32 * N; t += blockDim.x) {  // inputs, columns S..31 zero
-    const int q = t / N, a = t % N;
-    float x = 0.f;
-    if (q < S) {
-      x = s.G[q * N + a];
-      if (with_delta) x += s.dG[q * N + a];
+  {  // inputs: thread (atom a = tid % 64, columns q = tid / 64, + 4, ...), columns S..31 zero
+    const int a = tid & 63;
+    if (a < N) {
+      const uint32_t ob = umma_off32(a, 0, MLP_LBO, MLP_SBO);
+      for (int q = tid >> 6; q < 32; q += NN_THREADS / 64) {
+        float x = 0.f;
+        if (q < S) {
+          x = s.G[q * N + a];
+          if (with_delta) x += s.dG[q * N + a];
+        }
+        const uint32_t o = ob + (uint32_t)(q >> 2) * MLP_LBO + (uint32_t)(q & 3) * 4u;
+        const float h = tf32_hi(x);
+        *(float*)(m.Ah + o) = h;
+        *(float*)(m.Al + o) = x - h;
+      }
     }
-    const uint32_t o = umma_off32(a, q, MLP_LBO, MLP_SBO);
-    const float h = tf32_hi(x);
-    *(float*)(m.Ah + o) = h;
-    *(float*)(m.Al + o) = x - h;
   }
   fence_async_smem();
   tc_fence_before();
@@ -335,25 +375,28 @@ __device__ float mlp_energy_tc(const NNSmem<float>& s, const MlpSmem& m, int N, 
     mlp_issue(tbase, m.Ah, m.Al, m.B1h, m.B1l);
     umma_commit(mb);
   }
+  // accumulator rows = atoms 0..63 live in TMEM lanes 0-63, readable by warps
+  // 0, 1 (and 4, 5: a warp reads the lane quarter warp % 4); warps 4, 5 take
+  // the second half of the 32 columns
+  const bool tw = (warp & 3) < 2;
+  const int a = 32 * (warp & 1) + lane, half = warp >> 2;
+  const uint32_t taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 16u * (uint32_t)half;
   int b = 0;
   float acc[16];
-  if (warp < 2) {
+  if (tw) {
     if (!mbar_wait(mb, ph)) b = 1;
     tc_fence_after();
-    const int a = tid;
-#pragma unroll 1
-    for (int half = 0; half < 2; ++half) {  // 16 columns at a time (register pressure)
-      tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 16u * half, acc);
-      if (a < N) {
+    tmem_ld16(taddr, acc);
+    if (a < N) {
+      const uint32_t ob = umma_off32(a, 0, MLP_LBO, MLP_SBO);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {  // first hidden layer -> second GEMM's input (hi, lo)
-          const int n = 16 * half + c;
-          const float h = n < H1 ? tanhf(acc[c] + m.vec[n]) : 0.f;
-          const uint32_t o = umma_off32(a, n, MLP_LBO, MLP_SBO);
-          const float hh = tf32_hi(h);
-          *(float*)(m.Ah + o) = hh;
-          *(float*)(m.Al + o) = h - hh;
-        }
+      for (int c = 0; c < 16; ++c) {  // first hidden layer -> second GEMM's input (hi, lo)
+        const int n = 16 * half + c;
+        const float h = n < H1 ? tanh_mufu(acc[c] + m.vec[n]) : 0.f;
+        const uint32_t o = ob + (uint32_t)(n >> 2) * MLP_LBO + (uint32_t)(n & 3) * 4u;
+        const float hh = tf32_hi(h);
+        *(float*)(m.Ah + o) = hh;
+        *(float*)(m.Al + o) = h - hh;
       }
     }
   }
@@ -369,21 +412,21 @@ __device__ float mlp_energy_tc(const NNSmem<float>& s, const MlpSmem& m, int N, 
     mlp_issue(tbase, m.Ah, m.Al, m.B2h, m.B2l);
     umma_commit(mb);
   }
-  float e = 0.f;
-  if (warp < 2) {
+  if (tw) {
+    float e = 0.f;
     if (!mbar_wait(mb, ph)) b = 1;
     tc_fence_after();
-    const int a = tid;
-#pragma unroll 1
-    for (int half = 0; half < 2; ++half) {
-      tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 16u * half, acc);
+    tmem_ld16(taddr, acc);
+    if (a < N) {
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
         const int n = 16 * half + c;
-        if (a < N && n < H2) e += m.vec[64 + n] * tanhf(acc[c] + m.vec[32 + n]);
+        if (n < H2) e += m.vec[64 + n] * tanh_mufu(acc[c] + m.vec[32 + n]);
       }
+      if (half == 0) e += m.vec[96];
     }
-    if (a < N) e += m.vec[96];
+    e = warp_sum(e);
+    if (lane == 0) s.red[warp] = e;
   }
   ph ^= 1u;
   tc_fence_before();
@@ -391,7 +434,7 @@ __device__ float mlp_energy_tc(const NNSmem<float>& s, const MlpSmem& m, int N, 
     *bad = 1;
     return 0.f;
   }
-  return block_sum(e, s.red);
+  return (s.red[0] + s.red[1]) + (s.red[4] + s.red[5]);
 }
 
 // tensor-core state of a walker CTA: MLP tiles (FP32 form), surrogate tiles
@@ -414,7 +457,7 @@ __device__ void tc_setup(TcState<Real>& t, unsigned char* smem_raw, size_t off, 
   if constexpr (sizeof(Real) == 4) {
     mlp_carve(t.m, smem_raw + off);
     off += MLP_TC_BYTES;
-    mlp_stage(t.m, s.W, Q.S, Q.H1, Q.H2);
+    mlp_stage(t.m, Q.W, Q.S, Q.H1, Q.H2);
     slot = t.m.tslot;
   }
   if (want_sur) {
@@ -441,6 +484,33 @@ __device__ void tc_teardown(const TcState<Real>& t) {
   if ((threadIdx.x >> 5) == 0) tmem_dealloc(t.tbase, 32);
 }
 
+// acc[q] += E_g (1 + lambda cos_new)^zeta - E'_g (1 + lambda cos_old)^zeta for
+// every function q of pattern PAT (mapping fixed at compile time; powers 2^e of
+// both signs by repeated squaring, the unused ones are never formed)
+template <int PAT>
+__device__ __forceinline__ void pat_accumulate(float* acc, const float* En, const float* Eo,
+                                               float cn, float co) {
+  float pn[2][5], po[2][5];
+  pn[0][0] = 1.f + cn;
+  pn[1][0] = 1.f - cn;
+  po[0][0] = 1.f + co;
+  po[1][0] = 1.f - co;
+#pragma unroll
+  for (int e = 1; e < 5; ++e)
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+      pn[sg][e] = pn[sg][e - 1] * pn[sg][e - 1];
+      po[sg][e] = po[sg][e - 1] * po[sg][e - 1];
+    }
+#pragma unroll
+  for (int q = 0; q < nn_pat_sa(PAT); ++q) {
+    const int t = nn_pat_term(PAT, q);
+    const int g = t & 15, sg = (t >> 4) & 1, e = t >> 5;
+    acc[q] = fmaf(En[g], pn[sg][e], acc[q]);
+    acc[q] = fmaf(-Eo[g], po[sg][e], acc[q]);
+  }
+}
+
 }  // namespace
 
 // --------------------------------------------------------------- init kernel
@@ -459,7 +529,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
   load_walker(Q, s, X, nullptr, N);
   TcState<Real> tc;
   tc_setup(tc, smem_raw, nn_off, Q, s, false);
-  const int S = Q.S, SR = Q.SR;
+  const int S = Q.S, SR = Q.SR, ld = s.ld;
   for (int t = threadIdx.x; t < S * N; t += blockDim.x) s.G[t] = 0;
   __syncthreads();
   // radial: G_s[a] = sum_b gnorm f_ab exp(-eta r2_ab) (fc != 0, 1 excluded, SymmFunc.jl:234)
@@ -469,9 +539,9 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
     Real g = 0;
     for (int b = 0; b < N; ++b) {
       if (b == a) continue;
-      Real fc = s.F[a * N + b];
+      Real fc = s.F[a * ld + b];
       if (fc != Real(0) && fc != Real(1))
-        g += fc * rexp<Real>(-(Real)f.eta * s.D2[a * N + b]) * (Real)f.gnorm;
+        g += fc * rexp<Real>(-(Real)f.eta * s.D2[a * ld + b]) * (Real)f.gnorm;
     }
     s.G[q * N + a] = g + (Real)f.goffset;
   }
@@ -484,9 +554,9 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
       if (b == a) continue;
       for (int c = b + 1; c < N; ++c) {
         if (c == a) continue;
-        Real rab = s.D2[a * N + b], rac = s.D2[a * N + c], rbc = s.D2[b * N + c];
-        Real ex = rexp<Real>(-(Real)f.eta * (rab + rac + rbc)) * s.F[a * N + b] * s.F[a * N + c] *
-                  s.F[b * N + c];
+        Real rab = s.D2[a * ld + b], rac = s.D2[a * ld + c], rbc = s.D2[b * ld + c];
+        Real ex = rexp<Real>(-(Real)f.eta * (rab + rac + rbc)) * s.F[a * ld + b] * s.F[a * ld + c] *
+                  s.F[b * ld + c];
         if (ex == Real(0)) continue;
         Real abx = s.X[3 * a] - s.X[3 * b], aby = s.X[3 * a + 1] - s.X[3 * b + 1],
              abz = s.X[3 * a + 2] - s.X[3 * b + 2];
@@ -516,7 +586,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
 }
 
 // --------------------------------------------------------------- cycle kernel
-template <typename Real>
+template <typename Real, int PAT>
 __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
     k_nn_cycle(KParams P, NNParams Q, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -528,6 +598,7 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
   const int S = Q.S, SR = Q.SR, SA = Q.SA;
   NNSmem<Real> s;
   const size_t nn_off = nn_carve(s, smem_raw, N, S, SA, Q.H1, Q.H2, Q.nW);
+  const int ld = s.ld;
   double* Xg = P.pos + rd->pos_off + (size_t)w * N * 3;
   double* Gg = Q.G + (size_t)gw * S * Q.Nmax;
   load_walker(Q, s, Xg, Gg, N);
@@ -535,6 +606,11 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
   // tensor-core tiles after the walker state: MLP (FP32 form), surrogate (delayed acceptance)
   TcState<Real> tc;
   tc_setup(tc, smem_raw, nn_off, Q, s, Q.da != 0);
+  // FP32: angular partial sums in the MLP input tile (Ah, Al: 32 KB >= NCH x
+  // MAX_NN_ANG x 64 floats); rows of that tile beyond N are then not zero, but
+  // each row of an MMA product depends on its own row only and rows >= N are
+  // never read back
+  if constexpr (sizeof(Real) == 4) s.part = (Real*)tc.m.Ah;
   const SurSmem& ss = tc.ss;
   const uint32_t tbase = tc.tbase;
   uint32_t& mphase = tc.sph;
@@ -550,6 +626,7 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
   int status = ST_OK;
   long long acc = 0;
   const Real rc = (Real)Q.rcut;
+  const float pirc = (float)(3.141592653589793 / Q.rcut);
   const uint32_t run_word = (uint32_t)rd->run_id;
   const double R2 = P.box[g] * P.box[g];
 
@@ -676,8 +753,14 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
       Real d = (vx * vx + vy * vy) + vz * vz;
       if (j == i) d = 0;
       d2n[j] = d;
-      rn[j] = sqrt(d);
-      fn[j] = cutoff<Real>(rn[j], rc);
+      if constexpr (sizeof(Real) == 4) {  // MUFU rsqrt and cos (argument in [0, pi])
+        rin[j] = j == i ? 0.f : rsqrtf(d);
+        rn[j] = d * rin[j];
+        fn[j] = rn[j] < rc ? 0.5f * (__cosf(rn[j] * pirc) + 1.f) : 0.f;
+      } else {
+        rn[j] = sqrt(d);
+        fn[j] = cutoff<Real>(rn[j], rc);
+      }
       s.vn[3 * j] = vx;
       s.vn[3 * j + 1] = vy;
       s.vn[3 * j + 2] = vz;
@@ -686,11 +769,21 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
       s.vo[3 * j] = ox;
       s.vo[3 * j + 1] = oy;
       s.vo[3 * j + 2] = oz;
-      d2o[j] = s.D2[i * N + j];
-      ro[j] = sqrt(d2o[j]);
-      rin[j] = Real(1) / rn[j];
-      rio[j] = Real(1) / ro[j];
-      fo[j] = s.F[i * N + j];
+      d2o[j] = s.D2[i * ld + j];
+      if constexpr (sizeof(Real) == 4) {
+        rio[j] = j == i ? 0.f : rsqrtf(d2o[j]);
+        ro[j] = d2o[j] * rio[j];
+      } else {
+        ro[j] = sqrt(d2o[j]);
+        rin[j] = Real(1) / rn[j];
+        rio[j] = Real(1) / ro[j];
+      }
+      fo[j] = s.F[i * ld + j];
+      if constexpr (sizeof(Real) == 4) {
+        s.pr4[j] = make_float4(d, fn[j], d2o[j], fo[j]);
+        s.vn4[j] = make_float4(vx, vy, vz, rin[j]);
+        s.vo4[j] = make_float4(ox, oy, oz, rio[j]);
+      }
       if (j != i && d < (Real)Q.boundary2) hard = 1;
     }
     hard = __syncthreads_or(hard);
@@ -717,8 +810,13 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
       dEs = (double)(kap * ((ss.vec[100] + ss.vec[101]) + (ss.vec[102] + ss.vec[103])));
       int pass = 0;
       if (warp == 0) {
-        double p1 = exp(-dEs * beta);
-        if (p1 > 1) p1 = 1.0;
+        double p1;
+        if constexpr (sizeof(Real) == 4) {  // MUFU exp, min(1, exp(x)) = 2^(min(x, 0) log2 e)
+          p1 = (double)ex2f(fminf((float)(-dEs * beta), 0.f) * 1.4426950408889634f);
+        } else {
+          p1 = exp(-dEs * beta);
+          if (p1 > 1) p1 = 1.0;
+        }
         pass = p1 >= draw();
       }
       if (!__syncthreads_or(warp == 0 && lane == 0 && pass)) {
@@ -747,7 +845,73 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
         s.dG[q * N + j] = d;
       }
       // ---- 4. angular deltas (angular_symmetry_calculation!, DeltaMatrix.jl:827-871)
-      {
+      if constexpr (sizeof(Real) == 4 && PAT != NN_PAT_GENERIC) {
+        // Table-specialised FP32 form.  Every function q is (eta group g,
+        // lambda sign, zeta = 2^e) with the mapping known at compile time, so a
+        // triangle costs one exponential per eta group for its new and its old
+        // shape, E_g = f_ij f_ik f_jk 2^(-eta_g log2(e) s), and the powers
+        // (1 +- cos)^(2^e) by repeated squaring, shared by all functions; each
+        // function adds E_g P to its accumulator with one FMA, and tpz scales
+        // the sums.  Lanes jj = 0 .. N-2 of a 64-lane group run over the atoms
+        // j != i, chunk c over the cyclic offsets d = c+1, c+1+NCH, ... < N-1 of
+        // k = jj + d (mod N-1).  The centre-i term of an unordered pair {j, k}
+        // is taken at 2d < N-1 (and at 2d = N-1 by the lower index): the same
+        // for every lane of a warp at a given d.
+        constexpr int SAp = nn_pat_sa(PAT), NGp = nn_pat_ng(PAT);
+        static_assert(SAp <= MAX_NN_ANG && NGp <= 8, "pattern sizes");
+        const int Np = N - 1, jj = tid & 63, c = tid >> 6;
+        float accj[SAp], acci[SAp];
+#pragma unroll
+        for (int q = 0; q < SAp; ++q) {
+          accj[q] = 0.f;
+          acci[q] = 0.f;
+        }
+        int j = -1;
+        if (jj < Np) {
+          j = jj + (jj >= i);
+          const float4 vj = s.vn4[j], wj = s.vo4[j], pj = s.pr4[j];
+          const float* D2j = s.D2 + j * ld;
+          const float* Fj = s.F + j * ld;
+          int kk = jj + c + 1;
+          if (kk >= Np) kk -= Np;
+          for (int d = c + 1; d < Np; d += NCH) {
+            const int k = kk + (kk >= i);
+            const bool ci = 2 * d < Np || (2 * d == Np && jj < kk);
+            kk += NCH;
+            if (kk >= Np) kk -= Np;
+            const float rjk2 = D2j[k], fjk = Fj[k];
+            const float4 pk = s.pr4[k], vk = s.vn4[k];
+            // f products folded into the exponent (lg2 0 = -inf gives E = 0)
+            const float lfn = lg2f((pj.y * pk.y) * fjk), lfo = lg2f((pj.w * pk.w) * fjk);
+            const float sn = (pj.x + pk.x) + rjk2, so = (pj.z + pk.z) + rjk2;
+            float En[NGp], Eo[NGp];
+#pragma unroll
+            for (int g = 0; g < NGp; ++g) {
+              En[g] = ex2f(fmaf(Q.ang_nle[g], sn, lfn));
+              Eo[g] = ex2f(fmaf(Q.ang_nle[g], so, lfo));
+            }
+            const float rjki = rsqrtf(rjk2);
+            const float ux = vj.x - vk.x, uy = vj.y - vk.y, uz = vj.z - vk.z;  // x_k - x_j
+            // angle at j: (t - x_j).(x_k - x_j) / (r_new,j r_jk), old: (x_i - x_j)
+            const float cjn = ((vj.x * ux + vj.y * uy) + vj.z * uz) * (vj.w * rjki);
+            const float cjo = ((wj.x * ux + wj.y * uy) + wj.z * uz) * (wj.w * rjki);
+            pat_accumulate<PAT>(accj, En, Eo, cjn, cjo);
+            if (ci) {  // angle at the moved atom: (x_j - t).(x_k - t) / (r_j r_k)
+              const float4 wk = s.vo4[k];
+              const float cin = ((vj.x * vk.x + vj.y * vk.y) + vj.z * vk.z) * (vj.w * vk.w);
+              const float cio = ((wj.x * wk.x + wj.y * wk.y) + wj.z * wk.z) * (wj.w * wk.w);
+              pat_accumulate<PAT>(acci, En, Eo, cin, cio);
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < SAp; ++q) {
+          const float tz = s.tpzf[q];
+          if (j >= 0) s.part[(c * SAp + q) * 64 + j] = accj[q] * tz;
+          const float v = warp_sum(acci[q]);
+          if (lane == 0 && v != 0.f) atomicAdd(&s.dGi[SR + q], v * tz);
+        }
+      } else {
         const int j = tid % 64, c = tid / 64;
         Real accj[MAX_NN_ANG], acci[MAX_NN_ANG];
 #pragma unroll
@@ -769,7 +933,7 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
             const float4* sf4 = reinterpret_cast<const float4*>(s.sfp);
             for (int k = k0; k < k1; ++k) {
               if (k == i || k == j) continue;
-              const float rjk2 = s.D2[j * N + k], fjk = s.F[j * N + k];
+              const float rjk2 = s.D2[j * ld + k], fjk = s.F[j * ld + k];
               const float fpn = fnj * fn[k] * fjk, fpo = foj * fo[k] * fjk;
               if (fpn == 0.f && fpo == 0.f) continue;
               const float rjki = rsqrtf(rjk2);
@@ -810,7 +974,7 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
           } else
           for (int k = k0; k < k1; ++k) {
             if (k == i || k == j) continue;
-            const Real rjk2 = s.D2[j * N + k], fjk = s.F[j * N + k];
+            const Real rjk2 = s.D2[j * ld + k], fjk = s.F[j * ld + k];
             const Real fpn = fnj * fn[k] * fjk, fpo = foj * fo[k] * fjk;
             if (fpn == Real(0) && fpo == Real(0)) continue;
             const Real rjk = sqrt(rjk2);
@@ -857,12 +1021,15 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
         }
       }
       __syncthreads();
-      for (int t = tid; t < SA * N; t += blockDim.x) {
-        int q = t / N, j = t % N;
-        Real v = 0;
-        if (j != i)
-          for (int c = 0; c < NCH; ++c) v += s.part[(c * SA + q) * 64 + j];
-        s.dG[(SR + q) * N + j] = v;
+      {  // thread: atom j = tid % 64, functions q = tid / 64, + 4, ...
+        const int j = tid & 63;
+        if (j < N)
+          for (int q = tid >> 6; q < SA; q += NN_THREADS / 64) {
+            Real v = 0;
+            if (j != i)
+              for (int c = 0; c < NCH; ++c) v += s.part[(c * SA + q) * 64 + j];
+            s.dG[(SR + q) * N + j] = v;
+          }
       }
       for (int q = warp; q < SR; q += NN_THREADS / 32) {  // centre-i radial deltas
         Real v = 0;
@@ -907,8 +1074,14 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
     // ---- 6. Metropolis (src/MCRun.jl:122-132) and commit (swap_vars!, swap_config.jl:213-221);
     // with delayed acceptance this is the second stage, exp(-beta (dE - dE_s))
     if (warp == 0) {
-      double prob = exp(-(((double)new_en - en) - dEs) * beta);
-      if (prob > 1) prob = 1.0;
+      const double x = -(((double)new_en - en) - dEs) * beta;
+      double prob;
+      if constexpr (sizeof(Real) == 4) {  // FP32 form: MUFU exp, as the pair kernels
+        prob = (double)ex2f(fminf((float)x, 0.f) * 1.4426950408889634f);
+      } else {
+        prob = exp(x);
+        if (prob > 1) prob = 1.0;
+      }
       double u = draw();
       if (lane == 0) s.flags[3] = (prob >= u) ? 1 : 0;
     }
@@ -916,12 +1089,12 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
     if (s.flags[3]) {
       for (int j = tid; j < N; j += blockDim.x) {
         Real d = d2n[j];
-        s.D2[i * N + j] = d;
-        s.D2[j * N + i] = d;
+        s.D2[i * ld + j] = d;
+        s.D2[j * ld + i] = d;
         if (!hard) {  // the hard-core branch computes no new cut-off row or G
           Real f = fn[j];
-          s.F[i * N + j] = f;
-          s.F[j * N + i] = f;
+          s.F[i * ld + j] = f;
+          s.F[j * ld + i] = f;
         }
       }
       if (!hard)
@@ -1029,11 +1202,15 @@ size_t nn_smem_bytes(const NNParams& Q, int N, bool f64) {
   size_t es = f64 ? 8 : 4;
   auto al = [](size_t b) { return (b + 15) / 16 * 16; };
   size_t b = 0;
-  b += al(8 * N * 3) + al(es * N * 3) + 2 * al(es * N * N) + 2 * al(es * Q.S * N);
-  b += al(es * NCH * (Q.SA > 0 ? Q.SA : 1) * 64) + al(es * 8 * 64) + 2 * al(es * 64 * 3);
-  b += al(es * Q.nW) + al(es * N * Q.H1) + al(es * N * Q.H2) + al(es * 64) + al(es * (Q.S > 0 ? Q.S : 1));
+  const size_t ld = (size_t)N + (N & 1);
+  b += al(8 * N * 3) + al(es * N * 3) + 2 * al(es * N * ld) + 2 * al(es * Q.S * N);
+  if (f64) b += al(es * NCH * (Q.SA > 0 ? Q.SA : 1) * 64);
+  b += al(es * 8 * 64) + 2 * al(es * 64 * 3);
+  if (f64) b += al(es * Q.nW) + al(es * N * Q.H1) + al(es * N * Q.H2);
+  b += al(es * 64) + al(es * (Q.S > 0 ? Q.S : 1));
   b += al(es * 4 * MAX_NN_ANG);
   b += al(8 * DRAW_BUF) + al(8 * 4) + al(4 * 4);
+  if (!f64) b += 3 * al(16 * 64) + al(4 * MAX_NN_ANG);  // packed rows, tpz
   b += 128;                                 // alignment of the tensor-core tiles
   if (!f64) b += MLP_TC_BYTES;              // FP32 form: tensor-core MLP tiles
   if (Q.da) b += SUR_SMEM_BYTES;            // surrogate tiles
@@ -1074,11 +1251,16 @@ int nn_launch_cycle(const KParams& P, const NNParams& Q, int n_walkers, int n_ru
   cudaStream_t st = (cudaStream_t)stream;
   int e;
   if (f64) {
-    if ((e = set_smem(k_nn_cycle<double>, smem))) return e;
-    k_nn_cycle<double><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
+    if ((e = set_smem(k_nn_cycle<double, NN_PAT_GENERIC>, smem))) return e;
+    k_nn_cycle<double, NN_PAT_GENERIC><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
   } else {
-    if ((e = set_smem(k_nn_cycle<float>, smem))) return e;
-    k_nn_cycle<float><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
+    if (Q.ang_pat == NN_PAT_CU55) {
+      if ((e = set_smem(k_nn_cycle<float, NN_PAT_CU55>, smem))) return e;
+      k_nn_cycle<float, NN_PAT_CU55><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
+    } else {
+      if ((e = set_smem(k_nn_cycle<float, NN_PAT_GENERIC>, smem))) return e;
+      k_nn_cycle<float, NN_PAT_GENERIC><<<n_walkers, NN_THREADS, smem, st>>>(P, Q, phase);
+    }
   }
   if ((e = (int)cudaGetLastError())) return e;
   k_run_epilogue<<<n_runs, ((R + 31) / 32) * 32, 0, st>>>(P, Q, 0, phase);

@@ -17,6 +17,29 @@ struct NNSF {
   int pad;
 };
 
+// Angular function sets with a compiled cycle kernel.  Active angular
+// functions are ordered by (eta, lambda, zeta); a set whose structure matches
+// one below runs the table-specialised FP32 kernel: term q of a set is
+// (eta group g, lambda sign, zeta = 2^e), packed as g | (lambda < 0) << 4 | e << 5.
+// NN_PAT_CU55: the 26 type-111 functions of scripts/cu55.jl, eta groups
+// 1e-4, 3e-3, 8e-3, 0.015, 0.025, 0.045, 0.08.
+constexpr int NN_PAT_GENERIC = 0, NN_PAT_CU55 = 1;
+__host__ __device__ constexpr int nn_pat_sa(int pat) { return pat == NN_PAT_CU55 ? 26 : 0; }
+__host__ __device__ constexpr int nn_pat_ng(int pat) { return pat == NN_PAT_CU55 ? 7 : 0; }
+__host__ __device__ constexpr int nn_pat_term(int pat, int q) {
+#define T(g, neg, e) ((g) | ((neg) << 4) | ((e) << 5))
+  constexpr int cu55[26] = {
+      T(0, 1, 1), T(0, 0, 0),                                      // eta 1e-4
+      T(1, 1, 0), T(1, 1, 1),                                      // 3e-3
+      T(2, 1, 0), T(2, 1, 1), T(2, 0, 1),                          // 8e-3
+      T(3, 1, 1), T(3, 1, 2), T(3, 1, 4), T(3, 0, 0),              // 0.015
+      T(4, 1, 0), T(4, 1, 2), T(4, 1, 4), T(4, 0, 0), T(4, 0, 1), T(4, 0, 4),  // 0.025
+      T(5, 1, 1), T(5, 1, 2), T(5, 0, 0), T(5, 0, 2), T(5, 0, 4),  // 0.045
+      T(6, 1, 1), T(6, 1, 2), T(6, 0, 0), T(6, 0, 2)};             // 0.08
+#undef T
+  return pat == NN_PAT_CU55 && q >= 0 && q < 26 ? cu55[q] : -1;
+}
+
 struct NNParams {
   int S, SR, SA;      // active functions: all, radial (first), angular (sorted by eta)
   int H1, H2;         // hidden layer widths
@@ -41,6 +64,9 @@ struct NNParams {
   int* rec_slot;      // [rec_cap] temperature slot (within its run) of the move
   unsigned long long* rec_n;  // records written so far
   int rec_cap, rec_every;
+  // table-specialised angular kernel (FP32 form): pattern, -eta*log2(e) per eta group
+  int ang_pat;
+  float ang_nle[8];
 };
 
 size_t nn_smem_bytes(const NNParams& Q, int N, bool f64);

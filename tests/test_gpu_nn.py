@@ -98,16 +98,24 @@ def _pin_clusters():
             "scalene5": np.array(x)}
 
 
-@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-12), ("fp32", 1e-5)])
+@pytest.mark.parametrize("precision,rtol,table", [("fp64", 1e-12, "cu55"), ("fp32", 1e-5, "cu55"),
+                                                   ("fp32", 1e-5, "generic")])
 @pytest.mark.parametrize("name", ["tetra", "right+far", "scalene5"])
-def test_nn_energy_pinned_by_restatement(pk, orc, precision, rtol, name):
+def test_nn_energy_pinned_by_restatement(pk, orc, precision, rtol, table, name):
     """The engine's initial energies against the independent numpy restatement of
     SymmFunc.jl (tests/symm_restatement.py: hand-checked closed forms on the
     tetrahedron and the right triangle), not against the oracle; then a short
     chain, and the running energies against the restatement's energies of the
-    engine's own final positions."""
+    engine's own final positions.  "cu55": the table of scripts/cu55.jl, whose
+    26 angular functions run the table-specialised FP32 kernel; "generic": the
+    same table with one angular function switched off (type 100), which runs
+    the generic FP32 angular loop."""
     import symm_restatement as SR
     pot, _ = nn_potential(pk)
+    if table == "generic":
+        sf = pot.sf.copy()
+        sf[np.flatnonzero((sf[:, 0] == 1) & (sf[:, 1] == 111))[7], 1] = 100
+        pot = pk.RuNNerPotential(sf, pot.weights, pot.nodes, pot.boundary)
     x = _pin_clusters()[name]
     eng, _ = setup(pk, orc, pot, x, 2, precision, 30.0)
     ea = SR.mlp(SR.g_matrix(x, pot.sf), pot.weights, pot.nodes)
