@@ -318,6 +318,11 @@ int ptmc_surrogate_get(ptmc_ctx* c, float* params, ptmc_surrogate_cfg* cfg,
  * choice.  The delayed-acceptance on/off state is left as it was. */
 int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles,
                              double* kappa_out);
+/* Set the screening strength per temperature slot directly: kappa [R], each in
+ * [0, 1], the same for every run (for instance a choice ptmc_surrogate_calibrate
+ * made on an earlier engine).  No counterpart in the reference (delayed
+ * acceptance is this engine's addition). */
+int ptmc_surrogate_set_kappa(ptmc_ctx* c, const double* kappa);
 /* Copy up to max_n captured records (rows [n][128], targets [n]); *n_out = count. */
 int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n,
                            int* n_out);

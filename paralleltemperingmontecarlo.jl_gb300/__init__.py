@@ -682,6 +682,13 @@ class Engine:
                                                  _dptr(k)))
         return k
 
+    def surrogate_set_kappa(self, kappa):
+        """Screening strength per temperature slot (R values in [0, 1])."""
+        k = np.ascontiguousarray(kappa, dtype=np.float64)
+        if k.shape != (self.R,):
+            raise ValueError("kappa: one value per temperature slot")
+        self._ck(self.L.ptmc_surrogate_set_kappa(self.h, _dptr(k)))
+
     def surrogate_state(self):
         """(parameters, PairSurrogate config, stats dict)."""
         P = np.zeros(_capi.SUR_NPARAMS, dtype=np.float32)

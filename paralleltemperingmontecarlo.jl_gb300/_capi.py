@@ -123,6 +123,7 @@ SIGNATURES = {
     "ptmc_surrogate_records": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int, _ip]),
     "ptmc_surrogate_calibrate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                                 _dp]),
+    "ptmc_surrogate_set_kappa": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "ptmc_set_launch_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int]),
     "ptmc_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, _ip]),

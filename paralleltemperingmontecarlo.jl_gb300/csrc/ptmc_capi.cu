@@ -185,6 +185,7 @@ struct ptmc_ctx {
   DBuf<long long> d_da_cnt;
   DBuf<int> d_sur_err, d_rec_slot;
   DBuf<float> d_da_kappa;
+  DBuf<float> d_sur_tab;  // phi on the grid (first stage of screened moves)
   std::vector<double> sur_kappa;  // per slot index
   int sur_step = 0;  // Adam steps taken
   cudaStream_t st = nullptr;
@@ -1363,7 +1364,7 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_nn_row.free_();
   c->d_nn_sow.free_();
   for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_rec_rows, &c->d_rec_y,
-                  &c->d_da_kappa})
+                  &c->d_da_kappa, &c->d_sur_tab})
     b->free_();
   c->d_sur_loss.free_();
   c->d_rec_n.free_();
@@ -1972,6 +1973,18 @@ int sur_err_check(ptmc_ctx* c) {
   return PTMC_OK;
 }
 
+// phi of the frozen surrogate on the grid of the first stage (built whenever
+// screening is switched on: the parameters cannot change while it is on)
+int build_sur_table(ptmc_ctx* c) {
+  int e = sur_launch_table(sur_dev(c->sur_cfg), c->d_sur_P.p, c->d_sur_tab.p, c->d_sur_err.p, c->st);
+  if (e) return c->cuda_fail((cudaError_t)e, "k_sur_table launch");
+  int rc = sur_err_check(c);
+  if (rc) return rc;
+  c->Q.sur_tab = c->d_sur_tab.p;
+  c->Q.sur_tab_inv_h = (float)((SUR_TAB_N - 1) / (double)c->sur_cfg.r_cut);
+  return PTMC_OK;
+}
+
 int sm_count() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -2123,7 +2136,8 @@ int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg, const float* 
   // the record ring survives a new set-up with the same capacity (re-training
   // from other initial parameters on the same records)
   const bool keep_ring = c->sur_set && c->Q.rec_cap == capacity;
-  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_da_kappa}) b->free_();
+  for (auto* b : {&c->d_sur_P, &c->d_sur_m, &c->d_sur_v, &c->d_sur_g, &c->d_da_kappa, &c->d_sur_tab})
+    b->free_();
   c->d_sur_loss.free_();
   c->d_da_cnt.free_();
   c->d_sur_err.free_();
@@ -2135,7 +2149,7 @@ int ptmc_surrogate_set(ptmc_ctx* c, const ptmc_surrogate_cfg* cfg, const float* 
   }
   if (c->d_sur_P.alloc(SUR_NP) || c->d_sur_m.alloc(SUR_NP) || c->d_sur_v.alloc(SUR_NP) ||
       c->d_sur_g.alloc(SUR_NP) || c->d_sur_loss.alloc(1) || c->d_da_cnt.alloc(2 * (size_t)W) ||
-      c->d_sur_err.alloc(1) || c->d_da_kappa.alloc(W))
+      c->d_sur_err.alloc(1) || c->d_da_kappa.alloc(W) || c->d_sur_tab.alloc(SUR_TAB_N))
     return c->fail(PTMC_ERR_CUDA, "surrogate: device allocation failed");
   if (!keep_ring && (c->d_rec_rows.alloc((size_t)capacity * SUR_ROWS) ||
                      c->d_rec_y.alloc(capacity) || c->d_rec_n.alloc(1) ||
@@ -2244,10 +2258,8 @@ int ptmc_surrogate_enable(ptmc_ctx* c, int on) {
     if (c->Q.rec_rows) return c->fail(PTMC_ERR_STATE, "stop recording before enabling delayed acceptance");
     if (!(c->sur_cfg.escale > 0))
       return c->fail(PTMC_ERR_STATE, "surrogate output scale unset: train first or give escale");
-    NNParams Q = c->Q;
-    Q.da = 1;
-    if (nn_smem_bytes(Q, c->nn_Nmax, !c->f32()) > 227 * 1024)
-      return c->fail(PTMC_ERR_LIMIT, "NN walker state plus surrogate tiles exceed 227 KB of shared memory");
+    int rc = build_sur_table(c);
+    if (rc) return rc;
   }
   c->Q.da = on ? 1 : 0;
   drop_graphs(c);
@@ -2294,6 +2306,22 @@ int ptmc_surrogate_records(ptmc_ctx* c, float* rows, float* targets, int max_n, 
 }
 
 
+int ptmc_surrogate_set_kappa(ptmc_ctx* c, const double* kappa) {
+  if (!c || !kappa) return PTMC_ERR_ARG;
+  if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
+  const int R = c->R(), W = c->W;
+  for (int s2 = 0; s2 < R; ++s2)
+    if (!(kappa[s2] >= 0.0 && kappa[s2] <= 1.0))
+      return c->fail(PTMC_ERR_ARG, "kappa must lie in [0, 1]");
+  std::vector<float> kw(W);
+  for (const auto& r : c->rd)
+    for (int s2 = 0; s2 < R; ++s2) kw[r.wk + s2] = (float)kappa[s2];
+  CK(cudaMemcpyAsync(c->d_da_kappa.p, kw.data(), sizeof(float) * W, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->sur_kappa.assign(kappa, kappa + R);
+  return PTMC_OK;
+}
+
 int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, double* kappa_out) {
   if (!c) return PTMC_ERR_ARG;
   if (!c->sur_set) return c->fail(PTMC_ERR_STATE, "ptmc_surrogate_set not called");
@@ -2306,6 +2334,10 @@ int ptmc_surrogate_calibrate(ptmc_ctx* c, double cost_ratio, int timing_cycles, 
   if (n < 1) return c->fail(PTMC_ERR_STATE, "surrogate: no records to calibrate on");
   const int R = c->R(), W = c->W;
   const int da_before = c->Q.da;
+  {
+    int rc = build_sur_table(c);
+    if (rc) return rc;
+  }
   auto set_kappa = [&](const std::vector<double>& k) -> int {
     std::vector<float> kw(W);
     for (const auto& r : c->rd)

@@ -54,8 +54,6 @@ template <typename Real>
 __device__ __forceinline__ Real rtanh(Real x);
 template <>
 __device__ __forceinline__ double rtanh<double>(double x) { return tanh(x); }
-template <>
-__device__ __forceinline__ float rtanh<float>(float x) { return tanhf(x); }
 
 // cutoff_function (MachineLearningPotential/Cutoff.jl:79-90)
 template <typename Real>
@@ -376,102 +374,96 @@ __device__ float mlp_energy_tc(const NNSmem<float>& s, const MlpSmem& m, int N, 
     umma_commit(mb);
   }
   // accumulator rows = atoms 0..63 live in TMEM lanes 0-63, readable by warps
-  // 0, 1 (and 4, 5: a warp reads the lane quarter warp % 4); warps 4, 5 take
-  // the second half of the 32 columns
+  // 0, 1 and 4, 5 (a warp reads the lane quarter warp % 4), columns 16 (warp / 4)
+  // .. +15; they are staged column-major in the upper half of the A hi tile
+  // (rows 64-127, whose products are never read back), and all 8 warps apply
+  // the activations: thread (atom a = tid % 64, columns 8 (tid / 64) .. +7)
+  float* stg = (float*)(m.Ah + 8192);
   const bool tw = (warp & 3) < 2;
-  const int a = 32 * (warp & 1) + lane, half = warp >> 2;
+  const int ta = 32 * (warp & 1) + lane, half = warp >> 2;
   const uint32_t taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 16u * (uint32_t)half;
   int b = 0;
-  float acc[16];
-  if (tw) {
-    if (!mbar_wait(mb, ph)) b = 1;
-    tc_fence_after();
-    tmem_ld16(taddr, acc);
-    if (a < N) {
-      const uint32_t ob = umma_off32(a, 0, MLP_LBO, MLP_SBO);
+  auto stage = [&]() {
+    if (tw) {
+      if (!mbar_wait(mb, ph)) b = 1;
+      tc_fence_after();
+      float acc[16];
+      tmem_ld16(taddr, acc);
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {  // first hidden layer -> second GEMM's input (hi, lo)
-        const int n = 16 * half + c;
-        const float h = n < H1 ? tanh_mufu(acc[c] + m.vec[n]) : 0.f;
-        const uint32_t o = ob + (uint32_t)(n >> 2) * MLP_LBO + (uint32_t)(n & 3) * 4u;
-        const float hh = tf32_hi(h);
-        *(float*)(m.Ah + o) = hh;
-        *(float*)(m.Al + o) = h - hh;
-      }
+      for (int c = 0; c < 16; ++c) stg[(16 * half + c) * 64 + ta] = acc[c];
     }
-  }
-  ph ^= 1u;
-  fence_async_smem();
-  tc_fence_before();
+    ph ^= 1u;
+    tc_fence_before();
+  };
+  const int a = tid & 63, c0 = 8 * (tid >> 6);
+  stage();
   if (__syncthreads_or(b)) {
     *bad = 1;
     return 0.f;
   }
+  if (a < N) {  // first hidden layer -> second GEMM's input (hi, lo)
+    const uint32_t ob = umma_off32(a, 0, MLP_LBO, MLP_SBO);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int n = c0 + c;
+      const float h = n < H1 ? tanh_mufu(stg[n * 64 + a] + m.vec[n]) : 0.f;
+      const uint32_t o = ob + (uint32_t)(n >> 2) * MLP_LBO + (uint32_t)(n & 3) * 4u;
+      const float hh = tf32_hi(h);
+      *(float*)(m.Ah + o) = hh;
+      *(float*)(m.Al + o) = h - hh;
+    }
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
   if (tid == 0) {
     tc_fence_after();
     mlp_issue(tbase, m.Ah, m.Al, m.B2h, m.B2l);
     umma_commit(mb);
   }
-  if (tw) {
-    float e = 0.f;
-    if (!mbar_wait(mb, ph)) b = 1;
-    tc_fence_after();
-    tmem_ld16(taddr, acc);
-    if (a < N) {
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int n = 16 * half + c;
-        if (n < H2) e += m.vec[64 + n] * tanh_mufu(acc[c] + m.vec[32 + n]);
-      }
-      if (half == 0) e += m.vec[96];
-    }
-    e = warp_sum(e);
-    if (lane == 0) s.red[warp] = e;
-  }
-  ph ^= 1u;
-  tc_fence_before();
+  stage();
   if (__syncthreads_or(b)) {
     *bad = 1;
     return 0.f;
   }
-  return (s.red[0] + s.red[1]) + (s.red[4] + s.red[5]);
+  float e = 0.f;
+  if (a < N) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int n = c0 + c;
+      if (n < H2) e += m.vec[64 + n] * tanh_mufu(stg[n * 64 + a] + m.vec[32 + n]);
+    }
+    if (c0 == 0) e += m.vec[96];
+  }
+  e = warp_sum(e);
+  if (lane == 0) s.red[warp] = e;
+  __syncthreads();
+  return ((s.red[0] + s.red[1]) + (s.red[2] + s.red[3])) +
+         ((s.red[4] + s.red[5]) + (s.red[6] + s.red[7]));
 }
 
-// tensor-core state of a walker CTA: MLP tiles (FP32 form), surrogate tiles
-// (delayed acceptance), one 32-column TMEM allocation shared by both (they are
-// used one after the other within a move)
+// tensor-core state of a walker CTA (FP32 form): the MLP tiles and one
+// 32-column TMEM allocation; the FP64 form has none
 template <typename Real>
 struct TcState {
   MlpSmem m{};
-  SurSmem ss{};
-  uint32_t tbase = 0, mph = 0, sph = 0;
+  uint32_t tbase = 0, mph = 0;
   bool on = false;
 };
 
 template <typename Real>
-__device__ void tc_setup(TcState<Real>& t, unsigned char* smem_raw, size_t off, const NNParams& Q,
-                         const NNSmem<Real>& s, bool want_sur) {
-  const uint32_t a = smem_u32(smem_raw) + (uint32_t)off;
-  off += (128u - (a & 127u)) & 127u;
-  uint32_t* slot = nullptr;
+__device__ void tc_setup(TcState<Real>& t, unsigned char* smem_raw, size_t off, const NNParams& Q) {
   if constexpr (sizeof(Real) == 4) {
+    const uint32_t a = smem_u32(smem_raw) + (uint32_t)off;
+    off += (128u - (a & 127u)) & 127u;
     mlp_carve(t.m, smem_raw + off);
-    off += MLP_TC_BYTES;
     mlp_stage(t.m, Q.W, Q.S, Q.H1, Q.H2);
-    slot = t.m.tslot;
-  }
-  if (want_sur) {
-    sur_carve(t.ss, smem_raw + off);
-    sur_stage(t.ss, Q.surP);
-    if (!slot) slot = t.ss.tslot;
-  }
-  t.on = slot != nullptr;
-  if (t.on) {
-    if ((threadIdx.x >> 5) == 0) tmem_alloc(smem_u32(slot), 32);
+    t.on = true;
+    if ((threadIdx.x >> 5) == 0) tmem_alloc(smem_u32(t.m.tslot), 32);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    t.tbase = *slot;
+    t.tbase = *t.m.tslot;
   }
 }
 
@@ -528,7 +520,7 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn_init(KParams P, NNParams Q) {
   const double* X = P.pos + rd->pos_off + (size_t)w * N * 3;
   load_walker(Q, s, X, nullptr, N);
   TcState<Real> tc;
-  tc_setup(tc, smem_raw, nn_off, Q, s, false);
+  tc_setup(tc, smem_raw, nn_off, Q);
   const int S = Q.S, SR = Q.SR, ld = s.ld;
   for (int t = threadIdx.x; t < S * N; t += blockDim.x) s.G[t] = 0;
   __syncthreads();
@@ -605,15 +597,13 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
   if (P.status[g] != ST_OK) return;
   // tensor-core tiles after the walker state: MLP (FP32 form), surrogate (delayed acceptance)
   TcState<Real> tc;
-  tc_setup(tc, smem_raw, nn_off, Q, s, Q.da != 0);
+  tc_setup(tc, smem_raw, nn_off, Q);
   // FP32: angular partial sums in the MLP input tile (Ah, Al: 32 KB >= NCH x
   // MAX_NN_ANG x 64 floats); rows of that tile beyond N are then not zero, but
   // each row of an MMA product depends on its own row only and rows >= N are
   // never read back
   if constexpr (sizeof(Real) == 4) s.part = (Real*)tc.m.Ah;
-  const SurSmem& ss = tc.ss;
   const uint32_t tbase = tc.tbase;
-  uint32_t& mphase = tc.sph;
   long long n_rej1 = 0, n_exact = 0;
   const int slot = Q.sow[g];
   const int gs = rd->wk + slot;
@@ -680,7 +670,6 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
         s.flags[0] = i;
         s.flags[1] = err;
         s.flags[2] = rec;
-        s.flags[3] = 0;
       }
     }
     __syncthreads();
@@ -792,22 +781,18 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
     // exact evaluation
     double dEs = 0.0;
     if (kap > 0.f) {
-      float r = -1.f;
-      if (tid < SUR_ROWS) {
-        const int j = tid & (SUR_ROWS / 2 - 1);
-        if (j < N && j != i) r = (float)(tid < SUR_ROWS / 2 ? rn[j] : ro[j]);
-      }
-      float phi = 0.f;
-      if (!sur_tile_forward<true>(ss, Q.sc, tbase, mphase, r, phi, nullptr, nullptr)) {
-        status = ST_TIMEOUT;
-        break;
-      }
-      float v = warp_sum(r >= 0.f ? (tid < SUR_ROWS / 2 ? phi : -phi) : 0.f);
-      if (lane == 0 && warp < SUR_ROWS / 32) ss.vec[100 + warp] = v;
+      // dE_s = sum_j phi(|t - x_j|) - phi(|x_i - x_j|), phi from the frozen
+      // surrogate's table (threads j < N <= 64: warps 0 and 1)
+      float v = 0.f;
+      if (tid < N && tid != i)
+        v = sur_tab_phi(Q.sur_tab, Q.sur_tab_inv_h, (float)rn[tid]) -
+            sur_tab_phi(Q.sur_tab, Q.sur_tab_inv_h, (float)ro[tid]);
+      v = warp_sum(v);
+      if (lane == 0 && warp < 2) s.red[16 + warp] = v;
       __syncthreads();
       // screening strength kappa: stage 1 on exp(-kappa beta dE_s), stage 2 on
       // exp(-beta (dE - kappa dE_s)); exact for any fixed kappa
-      dEs = (double)(kap * ((ss.vec[100] + ss.vec[101]) + (ss.vec[102] + ss.vec[103])));
+      dEs = (double)(kap * (float)(s.red[16] + s.red[17]));
       int pass = 0;
       if (warp == 0) {
         double p1;
@@ -1086,31 +1071,38 @@ __global__ void __launch_bounds__(NN_THREADS, sizeof(Real) == 4 ? 2 : 1)
       if (lane == 0) s.flags[3] = (prob >= u) ? 1 : 0;
     }
     __syncthreads();
+    // commit on acceptance: warp 0 moves the atom and goes on to the next
+    // proposal (which reads positions only) while warps 1-7 update the distance
+    // and cut-off rows and G; the next proposal's barrier orders both before
+    // any use.  flags[3] is written only here, by the Metropolis step.
     if (s.flags[3]) {
-      for (int j = tid; j < N; j += blockDim.x) {
-        Real d = d2n[j];
-        s.D2[i * ld + j] = d;
-        s.D2[j * ld + i] = d;
-        if (!hard) {  // the hard-core branch computes no new cut-off row or G
-          Real f = fn[j];
-          s.F[i * ld + j] = f;
-          s.F[j * ld + i] = f;
+      if (warp == 0) {
+        if (lane == 0)
+          for (int k = 0; k < 3; ++k) {
+            s.Xd[3 * i + k] = s.tpos[k];
+            s.X[3 * i + k] = (Real)s.tpos[k];
+          }
+        __syncwarp();
+      } else {
+        const int ct = tid - 32, cn = NN_THREADS - 32;
+        for (int j = ct; j < N; j += cn) {
+          Real d = d2n[j];
+          s.D2[i * ld + j] = d;
+          s.D2[j * ld + i] = d;
+          if (!hard) {  // the hard-core branch computes no new cut-off row or G
+            Real f = fn[j];
+            s.F[i * ld + j] = f;
+            s.F[j * ld + i] = f;
+          }
         }
-      }
-      if (!hard)
-        for (int t = tid; t < S * N; t += blockDim.x) s.G[t] += s.dG[t];
-      __syncthreads();
-      if (tid == 0) {
-        for (int k = 0; k < 3; ++k) {
-          s.Xd[3 * i + k] = s.tpos[k];
-          s.X[3 * i + k] = (Real)s.tpos[k];
-        }
+        if (!hard)
+          for (int t = ct; t < S * N; t += cn) s.G[t] += s.dG[t];
       }
       en = (double)new_en;
       ++acc;
     }
-    __syncthreads();
   }
+  __syncthreads();
   // store back
   for (int k = tid; k < 3 * N; k += blockDim.x) Xg[k] = s.Xd[k];
   for (int t = tid; t < S * N; t += blockDim.x) Gg[t] = (double)s.G[t];
@@ -1213,7 +1205,6 @@ size_t nn_smem_bytes(const NNParams& Q, int N, bool f64) {
   if (!f64) b += 3 * al(16 * 64) + al(4 * MAX_NN_ANG);  // packed rows, tpz
   b += 128;                                 // alignment of the tensor-core tiles
   if (!f64) b += MLP_TC_BYTES;              // FP32 form: tensor-core MLP tiles
-  if (Q.da) b += SUR_SMEM_BYTES;            // surrogate tiles
   return b;
 }
 

@@ -55,6 +55,8 @@ struct NNParams {
   int da;             // 1: on
   SurCfgDev sc;
   const float* surP;  // [SUR_NP] surrogate parameters
+  const float* sur_tab;  // [SUR_TAB_N] phi on the grid (first stage of a move)
+  float sur_tab_inv_h;   // (SUR_TAB_N - 1) / r_cut
   long long* da_cnt;  // [walkers][2]: first-stage rejections, exact evaluations
   const float* da_kappa;  // [slots] screening strength per temperature slot (0 = no screening)
   // training-record capture (exact moves only): move m of a walker in cycle c

@@ -87,6 +87,28 @@ __global__ void __launch_bounds__(SUR_THREADS) k_sur_eval(SurCfgDev c, const flo
   sur_epilogue(s, tbase, err_flag);
 }
 
+// phi at the SUR_TAB_N grid distances, 128 per tile (accurate forward)
+__global__ void __launch_bounds__(SUR_THREADS) k_sur_table(SurCfgDev c, const float* __restrict__ P,
+                                                           float* __restrict__ tab, int* err_flag) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  SurSmem s;
+  uint32_t tbase;
+  sur_prologue(s, smem, P, tbase);
+  uint32_t phase = 0;
+  const float h = c.r_cut / (float)(SUR_TAB_N - 1);
+  for (int b = blockIdx.x; b * SUR_ROWS < SUR_TAB_N; b += gridDim.x) {
+    const int k = b * SUR_ROWS + (int)threadIdx.x;
+    const float r = k < SUR_TAB_N ? (float)k * h : -1.f;
+    float phi = 0.f;
+    if (!sur_tile_forward(s, c, tbase, phase, r, phi, nullptr, nullptr)) {
+      if (threadIdx.x == 0) *s.err = 1;
+      break;
+    }
+    if (k < SUR_TAB_N) tab[k] = phi;
+  }
+  sur_epilogue(s, tbase, err_flag);
+}
+
 // one parameter's column sum over the 128 rows of the current tile
 __device__ __forceinline__ float sur_param_grad(int p, const SurSmem& s, const GradSmem& g) {
   float acc = 0.f;
@@ -237,6 +259,12 @@ int sur_launch_eval(const SurCfgDev& c, const float* P, const float* rows, int n
   if (grid <= 0 || grid > n) grid = n;
   k_sur_eval<<<grid, SUR_THREADS, SUR_SMEM_BYTES, (cudaStream_t)stream>>>(c, P, rows, n, out,
                                                                          err_flag);
+  return (int)cudaGetLastError();
+}
+
+int sur_launch_table(const SurCfgDev& c, const float* P, float* tab, int* err_flag, void* stream) {
+  const int grid = (SUR_TAB_N + SUR_ROWS - 1) / SUR_ROWS;
+  k_sur_table<<<grid, SUR_THREADS, SUR_SMEM_BYTES, (cudaStream_t)stream>>>(c, P, tab, err_flag);
   return (int)cudaGetLastError();
 }
 

@@ -202,7 +202,22 @@ __device__ __forceinline__ bool sur_tile_forward(const SurSmem& s, const SurCfgD
   return !__syncthreads_or(bad);
 }
 
+// The frozen surrogate of a screening chain as a table: phi at the n grid
+// distances r_k = k r_cut / (n - 1) from the accurate tile forward (the
+// function training, evaluation and calibration use); beyond r_cut every
+// feature is zero and phi is the constant phi(r_cut).  The first stage of a
+// move interpolates linearly between grid points: a fixed pair function of
+// the distance, so dE_s stays an exact difference of a state function.
+constexpr int SUR_TAB_N = 4097;
+__device__ __forceinline__ float sur_tab_phi(const float* __restrict__ tab, float inv_h, float r) {
+  const float x = fminf(r * inv_h, (float)(SUR_TAB_N - 1));
+  const int k = min((int)x, SUR_TAB_N - 2);
+  const float a = __ldg(tab + k), b = __ldg(tab + k + 1);
+  return fmaf(x - (float)k, b - a, a);
+}
+
 // launchers (ptmc_surrogate.cu); every pointer is device memory
+int sur_launch_table(const SurCfgDev& c, const float* P, float* tab, int* err_flag, void* stream);
 size_t sur_grad_smem_bytes();
 int sur_launch_eval(const SurCfgDev& c, const float* P, const float* rows, int n, double* out,
                     int* err_flag, int grid, void* stream);

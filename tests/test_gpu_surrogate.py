@@ -212,3 +212,45 @@ def test_trained_surrogate_gain_and_exactness(pk):
         se_x = e_x.mean(axis=0).std(axis=0, ddof=1) / np.sqrt(runs)
         z = np.abs(m_ref - m_x) / np.sqrt(se_ref ** 2 + se_x ** 2)
         assert np.all(z < 5), z
+
+
+def test_set_kappa_zero_is_the_exact_chain(pk):
+    """ptmc_surrogate_set_kappa: screening strength 0 on every slot skips the
+    first stage (no draw), so the delayed-acceptance chain is the exact chain
+    bit for bit (FP64 form, same seed); strengths outside [0, 1] and a wrong
+    count are refused."""
+    import ptmc_gb300.starts as S
+    pot = nn_potential(pk)
+    N, R = 13, 4
+    x0 = S.sphere_start(N, 7.0, 4.0, 11)
+
+    def engine():
+        mp = pk.MCParams(mc_cycles=100, eq_cycles=0, mc_sample=1, n_traj=R, n_atoms=N)
+        e = pk.Engine(mp, pk.TempGrid(300.0, 900.0, R), pot, pk.NVT(N), precision="fp64",
+                      exch_prob=1.0, seed=5)
+        e.set_configs(0, pk.Config(x0, pk.SphericalBC(10.0)))
+        e.init()
+        return e
+
+    ref = engine()
+    ref.cycles_nosample(8)
+    g_ref = ref.states(0)
+    ref.close()
+    eng = engine()
+    rng = np.random.default_rng(1)
+    eng.surrogate_set(pk.PairSurrogate(2.0, 12.0, None, 12.0, 1.0), capacity=16,
+                      params=(rng.standard_normal(NP) * 0.1).astype(np.float32))
+    with pytest.raises(pk.PTMCError, match="kappa"):
+        eng.surrogate_set_kappa(np.full(R, 1.5))
+    with pytest.raises(ValueError):
+        eng.surrogate_set_kappa(np.zeros(R + 1))
+    eng.surrogate_set_kappa(np.zeros(R))
+    eng.surrogate_enable(True)
+    eng.cycles_nosample(8)
+    g = eng.states(0)
+    _, _, st = eng.surrogate_state()
+    eng.close()
+    assert st["stage1_rejects"] == 0 and st["exact_evals"] == 8 * N * R
+    assert np.array_equal(g["xyz"], g_ref["xyz"])
+    assert np.array_equal(g["counts"], g_ref["counts"])
+    np.testing.assert_array_equal(g["en_tot"], g_ref["en_tot"])
