@@ -212,17 +212,22 @@ def make_engine(pk, W, B, precision, cycles_per_launch, seed, device, starts=Non
     eng = pk.Engine(mp_, temp, pot, ens, n_runs=B, precision=precision,
                     resync_every=W["resync"], exch_prob=1.0, seed=seed,
                     cycles_per_launch=cycles_per_launch, device=device)
-    for r, n in enumerate(sizes):
+    def bc_of(n):
         if W["bc"][0] == "cubic":
-            bc = pk.CubicBC(W["bc"][1])
-        else:
-            rad = W["bc"][1] if W["bc"][1] else 0.9 * n ** (1 / 3) * 3 + 3.0
-            bc = pk.SphericalBC(rad)
-        if starts is None:
-            eng.set_configs(r, pk.Config(W["start"](n, r) if xyz is None else xyz[r], bc))
-        else:
-            st = starts[r]
-            eng.set_configs(r, [pk.Config(x, bc) for x in st["xyz"]], max_displ=st["max_displ"])
+            return pk.CubicBC(W["bc"][1])
+        return pk.SphericalBC(W["bc"][1] if W["bc"][1] else 0.9 * n ** (1 / 3) * 3 + 3.0)
+
+    if starts is None and len(set(sizes)) == 1:  # one atom count: one call for every run
+        eng.set_configs_batch(np.stack([W["start"](n, r) if xyz is None else xyz[r]
+                                        for r, n in enumerate(sizes)]), bc_of(sizes[0]))
+    else:
+        for r, n in enumerate(sizes):
+            if starts is None:
+                eng.set_configs(r, pk.Config(W["start"](n, r) if xyz is None else xyz[r], bc_of(n)))
+            else:
+                st = starts[r]
+                eng.set_configs(r, [pk.Config(x, bc_of(n)) for x in st["xyz"]],
+                                max_displ=st["max_displ"])
     if init:
         eng.init()
     return eng, sizes

@@ -170,6 +170,13 @@ int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N,
 int ptmc_set_run_configs_box(ptmc_ctx* c, int run, const double* xyz, int N,
                              int n_start, int bc_kind, double box_length,
                              double box_height);
+/* Start configurations of the n_runs runs first .. first + n_runs - 1 in one
+ * call: one configuration of N atoms per run (xyz [n_runs][N][3], bohr), all
+ * with the same boundary; the same as ptmc_set_run_configs_box with n_start = 1
+ * for each run (the batched form of the per-run call that
+ * src/Initialization.jl:88-96 replaces). */
+int ptmc_set_runs_configs(ptmc_ctx* c, int first, int n_runs, const double* xyz, int N,
+                          int bc_kind, double box_length, double box_height);
 /* NPT(n_atoms, pressure, separated_volume) (src/Ensembles.jl:75-86): volume
  * moves change z (probability 1/6), x and y (1/3) or all directions (1/2)
  * (volume_change_separated, src/MCMoves.jl:298-343) with their own step sizes

@@ -595,6 +595,18 @@ class Engine:
                 self._ck(self.L.ptmc_set_max_displ_sep(
                     self.h, run, _dptr(np.ascontiguousarray(md[:, 2:]))))
 
+    def set_configs_batch(self, xyz, bc, first=0):
+        """One start configuration per run for runs first .. first + len(xyz) - 1
+        in one call: xyz [n_runs, N, 3] (bohr), one boundary condition for all."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        if x.ndim != 3 or x.shape[2] != 3:
+            raise ValueError("xyz: [n_runs, N, 3]")
+        n, N = x.shape[0], x.shape[1]
+        kind, par, height = _bc_kind(bc)
+        self._ck(self.L.ptmc_set_runs_configs(self.h, int(first), n, _dptr(x), N, kind, par, height))
+        for r in range(first, first + n):
+            self.N[r], self.bc[r] = N, bc
+
     def init(self):
         self._ck(self.L.ptmc_init(self.h))
 

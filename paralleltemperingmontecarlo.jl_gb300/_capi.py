@@ -74,6 +74,9 @@ SIGNATURES = {
     "ptmc_set_run_configs_box": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                 ctypes.c_double]),
+    "ptmc_set_runs_configs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                             ctypes.c_double]),
     "ptmc_set_separated_volume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ptmc_set_max_displ": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "ptmc_set_max_displ_sep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),

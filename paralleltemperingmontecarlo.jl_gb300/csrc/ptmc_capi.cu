@@ -643,6 +643,51 @@ int ptmc_set_run_configs(ptmc_ctx* c, int run, const double* xyz, int N, int n_s
   return ptmc_set_run_configs_box(c, run, xyz, N, n_start, bc_kind, bc_param, bc_param);
 }
 
+namespace {
+// the checks of a start-configuration call that do not depend on the run
+int check_configs(ptmc_ctx* c, const double* xyz, int N, int n_start, int bc_kind,
+                  double bc_param, double box_height) {
+  if (!c || !xyz) return PTMC_ERR_ARG;
+  if (c->inited) return c->fail(PTMC_ERR_STATE, "configurations must be set before ptmc_init");
+  if (N < 2) return c->fail(PTMC_ERR_ARG, "need at least 2 atoms");
+  if (N > 1024) return c->fail(PTMC_ERR_LIMIT, "at most 1024 atoms per configuration");
+  if (n_start < 1) return c->fail(PTMC_ERR_ARG, "need at least one start configuration");
+  if (bc_kind != PTMC_BC_SPHERE && bc_kind != PTMC_BC_CUBIC && bc_kind != PTMC_BC_RECTANGULAR &&
+      bc_kind != PTMC_BC_RHOMBIC)
+    return c->fail(PTMC_ERR_ARG, "unknown boundary condition");
+  if (!(bc_param > 0)) return c->fail(PTMC_ERR_ARG, "boundary parameter must be positive");
+  if (!(box_height > 0)) return c->fail(PTMC_ERR_ARG, "box height must be positive");
+  if (c->p.ensemble == PTMC_NPT && bc_kind == PTMC_BC_SPHERE)
+    return c->fail(PTMC_ERR_ARG, "SphericalBC cannot be used in an NPT ensemble.");  // Ensembles.jl:192
+  for (auto& r : c->runs)
+    if (r.bc >= 0 && r.bc != bc_kind)
+      return c->fail(PTMC_ERR_ARG, "all runs of a context share one boundary kind");
+  return PTMC_OK;
+}
+
+void store_configs(HostRun& h, const double* xyz, int N, int n_start, int bc_kind,
+                   double bc_param, double box_height) {
+  h.N = N;
+  h.n_start = n_start;
+  h.bc = bc_kind;
+  h.bc_param = bc_param;
+  h.bc_height = (bc_kind == PTMC_BC_RECTANGULAR || bc_kind == PTMC_BC_RHOMBIC) ? box_height : bc_param;
+  h.xyz.assign(xyz, xyz + (size_t)n_start * N * 3);
+}
+}  // namespace
+
+int ptmc_set_runs_configs(ptmc_ctx* c, int first, int n_runs, const double* xyz, int N,
+                          int bc_kind, double box_length, double box_height) {
+  int rc = check_configs(c, xyz, N, 1, bc_kind, box_length, box_height);
+  if (rc) return rc;
+  if (n_runs < 1 || first < 0 || first + n_runs > c->p.n_runs)
+    return c->fail(PTMC_ERR_ARG, "run range out of bounds");
+  for (int r = 0; r < n_runs; ++r)
+    store_configs(c->runs[first + r], xyz + (size_t)r * N * 3, N, 1, bc_kind, box_length,
+                  box_height);
+  return PTMC_OK;
+}
+
 int ptmc_set_run_configs_box(ptmc_ctx* c, int run, const double* xyz, int N, int n_start,
                              int bc_kind, double box_length, double box_height) {
   const double bc_param = box_length;

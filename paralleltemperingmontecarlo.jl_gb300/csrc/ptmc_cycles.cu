@@ -323,6 +323,75 @@ __device__ double walker_energy64(const double* X, int N, double L, double H, do
   }
 }
 
+// FP64 energy (and EAM components) of one configuration with every thread of
+// the CTA, for a run whose replicas all start from one configuration: thread
+// (row k, group g) sums the pair terms of row k over j = g, g + G, ... (the
+// pair potentials: j > k only), the groups of a row are added in order and
+// the rows by a fixed tree, so the result does not depend on the timing.
+// Needs blockDim.x >= N.
+template <int POT, int BC, int ENS>
+__device__ double start_energy_cta(const KParams& P, const double* X, int N, double L, double H,
+                                   double rc2, double* comp64) {
+  __shared__ double s_pa[1024], s_pb[1024];
+  const int T = blockDim.x, t = threadIdx.x;
+  const int G = T / N;
+  double a = 0.0, b = 0.0;
+  if (t < G * N) {
+    const int k = t % N, g = t / N;
+    const double xk = X[3 * k], yk = X[3 * k + 1], zk = X[3 * k + 2];
+    if constexpr (POT == POT_EAM) {
+      for (int j = g; j < N; j += G) {
+        if (j == k) continue;
+        double pa, pb;
+        invrexp64(pd2<BC>(xk, yk, zk, X + 3 * j, L, H), -0.5 * P.eam_n, -0.5 * P.eam_m, pa, pb);
+        a += pa;
+        b += pb;
+      }
+    } else {
+      for (int j = k + 1 + g; j < N; j += G) {
+        const double x = pd2<BC>(xk, yk, zk, X + 3 * j, L, H);
+        if (ENS == ENS_NPT && !(x <= rc2)) continue;
+        a += v64<POT>(P.c, P.K, x);
+      }
+    }
+  }
+  s_pa[t] = a;
+  s_pb[t] = b;
+  __syncthreads();
+  double e = 0.0;
+  if (t < N) {
+    double ra = 0.0, rb = 0.0;
+    for (int g = 0; g < G; ++g) {
+      ra += s_pa[g * N + t];
+      rb += s_pb[g * N + t];
+    }
+    if constexpr (POT == POT_EAM) {
+      if (comp64) {
+        comp64[2 * t] = ra;
+        comp64[2 * t + 1] = rb;
+      }
+      e = P.eam_ean * ra - P.eam_ecam * sqrt(rb);
+    } else {
+      e = ra;
+    }
+  }
+  __syncthreads();
+  s_pa[t] = e;
+  __syncthreads();
+  int p2 = 1;  // the largest power of two <= T: fold the rest onto it, then a tree
+  while (2 * p2 <= T) p2 *= 2;
+  if (t >= p2) s_pa[t - p2] += s_pa[t];
+  __syncthreads();
+  for (int h = p2 >> 1; h > 0; h >>= 1) {
+    if (t < h) s_pa[t] += s_pa[t + h];
+    __syncthreads();
+  }
+  e = s_pa[0];
+  __syncthreads();
+  if constexpr (ENS == ENS_NPT && POT != POT_EAM) e = e + lrc_box<BC>(N, rc2, P.c, P.K, L, H);
+  return e;
+}
+
 // ------------------------------------------------------------ init kernel
 // MCState constructor (src/MCStates.jl:137-162): distance matrix, potential
 // variables and initial energy of every walker, in FP64, from HBM positions.
@@ -342,7 +411,22 @@ __global__ void __launch_bounds__(1024) k_init(KParams P, int run0) {
   auto mat = [&](int v) { return P.mat + rd.mat_off + (size_t)v * N * N; };
   auto cmp = [&](int v) { return P.comp + rd.comp_off + (size_t)v * N * 2; };
   auto pe = [&](int v) { return P.pe + rd.pe_off + (size_t)v * N * N * pe_w; };
-  for (int w = warp; w < ns; w += nw) {
+  // FP32 form, one start for every replica: the whole CTA evaluates it (a
+  // single warp would leave the SM's FP64 pipes mostly idle)
+  const bool cta = F32 && !pot_b(POT) && ns == 1 && N <= (int)blockDim.x;
+  if constexpr (F32 && !pot_b(POT)) {
+    if (cta) {
+      const int g = rd.wk;
+      const double e = start_energy_cta<POT, BC, ENS>(
+          P, P.pos + rd.pos_off, N, P.box[g], P.boxh[g], P.rc2[g], POT == POT_EAM ? cmp(0) : nullptr);
+      if (threadIdx.x == 0) {
+        P.en[g] = e;
+        P.status[g] = ST_OK;
+        P.drift[g] = 0.0;
+      }
+    }
+  }
+  for (int w = cta ? ns : warp; w < ns; w += nw) {
     const int g = rd.wk + w;
     const double* X = P.pos + rd.pos_off + (size_t)w * N * 3;
     double* M = keep_m ? mat(w) : nullptr;

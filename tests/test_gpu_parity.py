@@ -503,3 +503,41 @@ def test_large_n_hbm_state_fp64_parity(pk, orc):
     o.cycles(1, 5)
     compare(eng, o, positions_exact=False)
     eng.close()
+
+
+def test_set_configs_batch_equals_per_run(pk):
+    """ptmc_set_runs_configs (one configuration for each of many runs in one call)
+    gives the same engine state as one ptmc_set_run_configs call per run; a run
+    range beyond n_runs and a wrong array shape are refused."""
+    import ptmc_gb300.starts as S
+    C = [-10.5097942564988, 989.725135614556, -101383.865938807, 3918846.12841668,
+         -56234083.4334278, 288738837.441765]
+    B, N, R = 5, 13, 4
+    xs = np.stack([S.sphere_start(N, 8.0, 4.5, 40 + r) for r in range(B)])
+
+    def engine(batch):
+        mp = pk.MCParams(mc_cycles=100, eq_cycles=20, mc_sample=1, n_traj=R, n_atoms=N)
+        e = pk.Engine(mp, pk.TempGrid(4.0, 16.0, R), pk.ELJPotentialEven(C), pk.NVT(N),
+                      n_runs=B, precision="fp32", exch_prob=1.0, seed=3)
+        if batch:
+            with pytest.raises(pk.PTMCError, match="run range"):
+                e.set_configs_batch(xs, pk.SphericalBC(11.0), first=1)
+            with pytest.raises(ValueError):
+                e.set_configs_batch(xs[:, :, :2], pk.SphericalBC(11.0))
+            e.set_configs_batch(xs, pk.SphericalBC(11.0))
+        else:
+            for r in range(B):
+                e.set_configs(r, pk.Config(xs[r], pk.SphericalBC(11.0)))
+        e.init()
+        e.equilibrate()
+        e.run_cycles(30)
+        return e
+
+    a, b = engine(True), engine(False)
+    for r in range(B):
+        sa, sb = a.states(r), b.states(r)
+        assert np.array_equal(sa["xyz"], sb["xyz"])
+        assert np.array_equal(sa["en_tot"], sb["en_tot"])
+        assert np.array_equal(a.output(r).en_histogram, b.output(r).en_histogram)
+    a.close()
+    b.close()
