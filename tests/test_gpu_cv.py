@@ -26,7 +26,7 @@ means must agree within 5 combined standard errors.
     with a GPU-trained surrogate and calibrated screening strength
   * Ne32 NPT (cubic box, cut-off + tail correction, 1 atm): Cp(T) from
     multihistogram_NPT, FP32 move rows and volume moves (FP64 energy total)
-    + resync
+    + resync; and the benchmarked Ne108 NPT configuration (32 replicas)
 """
 import json
 import os
@@ -147,6 +147,34 @@ def test_cp_ne32_npt_fp32_vs_fp64(pk):
         return cp
 
     compare(form("fp64", 41), form("fp32", 42), "Ne32 NPT FP32+resync (Cp)")
+
+
+def test_cp_ne108_npt_benched_size_fp32_vs_fp64(pk):
+    """The benchmarked NPT configuration itself: bulk Ne, 108 atoms (fcc 3x3x3
+    cells of 8.4 bohr, +-0.05 bohr jitter, CubicBC(25.2)), 32 replicas over
+    10-40 K, 1 atm, one volume move per 108 atom moves; Cp(T) of the FP32 form
+    against the plain FP64 form, 12 independent runs each (800 equilibration
+    + 2000 production cycles)."""
+    import ptmc_gb300.starts as S
+    N, R, n_runs, prod = 108, 32, 12, 2000
+    p_atm = 101325 * 3.398928944382626e-14
+    pot, ens = pk.ELJPotentialEven(C_NE), pk.NPT(N, p_atm)
+    temp = pk.TempGrid(10.0, 40.0, R)
+
+    def form(precision, seed):
+        mp = pk.MCParams(mc_cycles=prod, eq_cycles=1600, mc_sample=1, n_traj=R, n_atoms=N)
+        eng = pk.Engine(mp, temp, pot, ens, n_runs=n_runs, precision=precision, exch_prob=1.0,
+                        seed=seed, resync_every=1000)
+        for r in range(n_runs):
+            eng.set_configs(r, pk.Config(S.fcc_box(3, 8.4, 0.05, 700 + r), pk.CubicBC(25.2)))
+        eng.init()
+        eng.equilibrate()
+        eng.run_cycles(prod)
+        cp = np.array([pk.multihistogram_NPT(ens, temp, eng.output(r), 1e-4)[1] for r in range(n_runs)])
+        eng.close()
+        return cp
+
+    compare(form("fp64", 51), form("fp32", 52), "Ne108 NPT FP32+resync (Cp), benched size")
 
 
 def test_cv_nn13_delayed_acceptance_vs_fp64(pk):
