@@ -64,14 +64,27 @@ template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  bool own = true;  // false: a slice of the context's state block
   int alloc(size_t count) {
     n = count;
+    own = true;
     if (count == 0) count = 1;
     return (int)cudaMalloc(&p, count * sizeof(T));
   }
   void free_() {
-    if (p) cudaFree(p);
+    if (p && own) cudaFree(p);
     p = nullptr;
+    own = true;
+  }
+  // bytes of a slice of `count` elements (at least one), 256-byte aligned
+  static size_t span(size_t count) {
+    return ((count ? count : 1) * sizeof(T) + 255) / 256 * 256;
+  }
+  void place(unsigned char*& cur, size_t count) {
+    n = count;
+    p = (T*)cur;
+    own = false;
+    cur += span(count);
   }
 };
 
@@ -123,6 +136,7 @@ bool write_file_atomic(const std::string& path, const std::string& data) {
 }  // namespace
 
 struct ptmc_ctx {
+  void* state_block = nullptr;  // one device allocation for the state set up by ptmc_init
   ptmc_params p{};
   std::string err;
   int pot = -1;
@@ -879,22 +893,8 @@ int ptmc_init(ptmc_ctx* c) {
   int W = wk;
   int maxN_all = 0;
   for (auto& G : c->groups) maxN_all = std::max(maxN_all, G.N);
-  if (c->d_runs.alloc(nr) || c->d_pos.alloc(po) || c->d_mat.alloc(mo) || c->d_comp.alloc(co) ||
-      c->d_en.alloc(W) || c->d_box.alloc(W) || c->d_rc2.alloc(W) || c->d_drift.alloc(W) ||
-      c->d_beta.alloc(W) || c->d_maxd.alloc(2 * W) || c->d_maxbox.alloc(W) ||
-      c->d_ham.alloc(2 * W) || c->d_ctr.alloc(W) || c->d_status.alloc(W) ||
-      c->d_wos.alloc(W) || c->d_cnt.alloc(6 * (size_t)W) || c->d_hist.alloc(ho) ||
-      (c->rdf_on && c->d_rdf.alloc((size_t)W * 5 * c->p.n_bin)) || c->d_boxh.alloc(W) ||
-      c->d_maxboxh.alloc(W) || c->d_maxd_sep.alloc(2 * W) || c->d_cnt_sep.alloc(4 * (size_t)W) ||
-      (bpot && c->d_tan.alloc(mo)) || (c->pot == POT_LUT && c->d_lut.alloc(c->lut.size())) ||
-      c->d_pe.alloc(peo) || c->d_lo.alloc(c->f32() && !nn ? po / 3 * 4 : 0) ||
-      c->d_scr.alloc(c->glob ? (size_t)W * 4 * maxN_all : 0))
-    return c->fail(PTMC_ERR_CUDA, "device allocation failed");
-  // host images (the start configurations go up once per run and are
+  // host images of the start configurations (they go up once per run and are
   // expanded into replicas on the device)
-  std::vector<double> box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W), boxh(W),
-      maxboxh(W), maxd_sep(2 * W);
-  std::vector<int> wos(W);
   std::vector<long long> start_off(nr);
   std::vector<int> n_start(nr);
   long long n_starts = 0;
@@ -904,6 +904,63 @@ int ptmc_init(ptmc_ctx* c) {
     n_start[d] = h.n_start;
     n_starts += (long long)h.n_start * h.N * 3;
   }
+  // the context's device state as slices of one allocation (a cudaMalloc per
+  // buffer costs tens of microseconds at creation and again at destruction)
+  DBuf<double> d_starts;
+  DBuf<long long> d_soff;
+  DBuf<int> d_ns;
+  {
+    size_t total = 0;
+    unsigned char* cur = nullptr;
+    auto take = [&](auto& b, size_t count) {
+      if (cur) b.place(cur, count);
+      else total += b.span(count);
+    };
+    auto plan = [&]() {
+      take(c->d_runs, nr);
+      take(c->d_pos, po);
+      take(c->d_mat, mo);
+      take(c->d_comp, co);
+      take(c->d_en, W);
+      take(c->d_box, W);
+      take(c->d_rc2, W);
+      take(c->d_drift, W);
+      take(c->d_beta, W);
+      take(c->d_maxd, 2 * (size_t)W);
+      take(c->d_maxbox, W);
+      take(c->d_ham, 2 * (size_t)W);
+      take(c->d_ctr, W);
+      take(c->d_status, W);
+      take(c->d_wos, W);
+      take(c->d_cnt, 6 * (size_t)W);
+      take(c->d_hist, ho);
+      if (c->rdf_on) take(c->d_rdf, (size_t)W * 5 * c->p.n_bin);
+      take(c->d_boxh, W);
+      take(c->d_maxboxh, W);
+      take(c->d_maxd_sep, 2 * (size_t)W);
+      take(c->d_cnt_sep, 4 * (size_t)W);
+      if (bpot) take(c->d_tan, mo);
+      if (c->pot == POT_LUT) take(c->d_lut, c->lut.size());
+      take(c->d_pe, peo);
+      take(c->d_lo, c->f32() && !nn ? po / 3 * 4 : 0);
+      take(c->d_scr, c->glob ? (size_t)W * 4 * maxN_all : 0);
+      take(d_starts, n_starts);
+      take(d_soff, nr);
+      take(d_ns, nr);
+    };
+    plan();
+    if (cudaMalloc(&c->state_block, total) != cudaSuccess) {
+      c->state_block = nullptr;
+      return c->fail(PTMC_ERR_CUDA, "device allocation failed");
+    }
+    cur = (unsigned char*)c->state_block;
+    plan();
+  }
+  // host images (the start configurations go up once per run and are
+  // expanded into replicas on the device)
+  std::vector<double> box(W), rc2(W), beta(W), maxd(2 * W), maxbox(W), boxh(W),
+      maxboxh(W), maxd_sep(2 * W);
+  std::vector<int> wos(W);
   std::vector<double> starts(n_starts);
   for (int d = 0; d < nr; ++d) {
     const HostRun& h = c->runs[c->run_of_dev[d]];
@@ -937,11 +994,6 @@ int ptmc_init(ptmc_ctx* c) {
   int rc = push_runs(c);
   if (rc) return rc;
   {
-    DBuf<double> d_starts;
-    DBuf<long long> d_soff;
-    DBuf<int> d_ns;
-    if (d_starts.alloc(n_starts) || d_soff.alloc(nr) || d_ns.alloc(nr))
-      return c->fail(PTMC_ERR_CUDA, "device allocation failed");
     cudaError_t e = cudaMemcpyAsync(d_starts.p, starts.data(), sizeof(double) * n_starts,
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
@@ -953,10 +1005,6 @@ int ptmc_init(ptmc_ctx* c) {
       e = cudaGetLastError();
       c->stats.kernel_launches += 1;
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the scratch is freed next
-    d_starts.free_();
-    d_soff.free_();
-    d_ns.free_();
     if (e != cudaSuccess) return c->cuda_fail(e, "start configurations");
   }
   CK(cudaMemcpyAsync(c->d_box.p, box.data(), sizeof(double) * W, cudaMemcpyHostToDevice, s));
@@ -1401,6 +1449,8 @@ void ptmc_destroy(ptmc_ctx* c) {
   c->d_pe.free_();
   c->d_lo.free_();
   c->d_scr.free_();
+  if (c->state_block) cudaFree(c->state_block);
+  c->state_block = nullptr;
   for (auto* b : {&c->d_nn2_rad, &c->d_nn2_ang, &c->d_nn2_W1, &c->d_nn2_W2}) b->free_();
   c->d_nn2_swaps.free_();
   c->d_nn_sf.free_();
