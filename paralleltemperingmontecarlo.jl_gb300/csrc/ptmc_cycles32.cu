@@ -84,7 +84,7 @@ long long cycles32_smem_bytes(int pot, int R, int N, int C) {
   long long b = 0;
   b += al(Rl * N * 16);  // float4 hi positions
   b += al(Rl * N * 16);  // float4 lo positions
-  if (pot == POT_EAM) b += 2 * al(Rl * N * 4);  // density deltas, sqrt(rho)
+  if (pot == POT_EAM) b += al(Rl * N * 4);  // density deltas
   b += al(Rl * DRW32 * 4);                                       // draw words
   b += al((long long)R * 8) * 6 + al((long long)R * 16) + al((long long)R * 48) + al((long long)R * 4) * 5;
   b += al((long long)R * 8);                                     // per-walker accepted counts
@@ -123,11 +123,7 @@ __global__ void __launch_bounds__(1024)
   float4* s_xh = (float4*)carve((long long)Rl * N * 16);
   float4* s_xl = (float4*)carve((long long)Rl * N * 16);
   float* s_d32 = nullptr;
-  float* s_sq = nullptr;
-  if (POT == POT_EAM) {
-    s_d32 = (float*)carve((long long)Rl * N * 4);
-    s_sq = (float*)carve((long long)Rl * N * 4);
-  }
+  if (POT == POT_EAM) s_d32 = (float*)carve((long long)Rl * N * 4);
   uint32_t* s_drw = (uint32_t*)carve((long long)Rl * DRW32 * 4);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_maxbox = (double*)carve((long long)R * 8);
@@ -159,7 +155,6 @@ __global__ void __launch_bounds__(1024)
     const double* gc = P.comp + rdp->comp_off + (size_t)q * Rl * N * 2;
     for (int k = tid; k < Rl * N; k += nthr) {  // rho in the w lane of the position
       s_xh[k].w = (float)gc[2 * k + 1];
-      s_sq[k] = (float)sqrt(gc[2 * k + 1]);
     }
   }
   const int wk0 = rdp->wk;
@@ -194,7 +189,6 @@ __global__ void __launch_bounds__(1024)
   double drift = P.drift[g];
   float4* Xh = s_xh + (size_t)wl * N;
   float4* Xl = s_xl + (size_t)wl * N;
-  float* SQ = s_sq ? s_sq + (size_t)wl * N : nullptr;
   uint32_t* drw = s_drw + wl * DRW32;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const float hnf = P.f_hn, hmf = P.f_hm, ecamf = P.f_ecam;
@@ -313,11 +307,11 @@ __global__ void __launch_bounds__(1024)
         sbf += db;
         // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
         de = fmaf(ean2f, da, de);
-        de = fmaf(necamf * db, rcpf(SQ[j] + sqrtf_approx(b.w + db)), de);
+        de = fmaf(necamf * db, rcpf(sqrtf_approx(b.w) + sqrtf_approx(b.w + db)), de);
       }
       sbf = seg_sum<LPR>(sbf, gmask);
       de = seg_sum<LPR>(de, gmask);
-      de -= ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(x4.w + sbf));
+      de -= ecamf * sbf * rcpf(sqrtf_approx(x4.w) + sqrtf_approx(x4.w + sbf));
     } else {
       for (int j = lane; j < N; j += LPR) {
         const bool self = j == i;  // masked, not branched (its old distance is 0)
@@ -342,7 +336,6 @@ __global__ void __launch_bounds__(1024)
       float rho_i = 0.f;
       if (POT == POT_EAM) {
         rho_i = x4.w + sbf;
-        SQ[i] = sqrtf_approx(rho_i);
       }
       Xh[i] = make_float4(tf.x, tf.y, tf.z, rho_i);
       Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
@@ -351,9 +344,7 @@ __global__ void __launch_bounds__(1024)
       const float* D = s_d32 + (size_t)wl * N;
       for (int k = lane; k < N; k += LPR) {
         if (k == i) continue;
-        const float rho = Xh[k].w + D[k];
-        Xh[k].w = rho;
-        SQ[k] = sqrtf_approx(rho);
+        Xh[k].w += D[k];
       }
     }
     de_acc += de;
@@ -516,7 +507,7 @@ __global__ void __launch_bounds__(1024)
       if (P.resync_every > 0 && idx % P.resync_every == 0) {
         double e64 = energy64<POT, BC, ENS, LPR>(Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean,
                                             P.eam_ecam, POT == POT_EAM ? s_d32 + (size_t)wl * N : nullptr,
-                                            SQ, lane, gmask);
+                                            nullptr, lane, gmask);
         drift = fmax(drift, fabs(en - e64));
         en = e64;
         __syncwarp(gmask);

@@ -20,8 +20,10 @@
 //    registers.
 //  * Shared memory per walker is small, so more walkers share an SM: FP32 hi
 //    positions (float4, the EAM density rho in w; padded with far-away
-//    sentinel atoms to whole chunks) and sqrt(rho) (EAM), 32 buffered draw
-//    words.  The lo halves of the float-float positions are touched only by
+//    sentinel atoms to whole chunks) and 32 buffered draw words.  sqrt(rho_j)
+//    of the embedding term is taken per pair (one MUFU op) rather than kept
+//    per atom: at Cu55 the 8.7 KB it took per 32 walkers decided between 4
+//    and 5 CTAs per SM.  The lo halves of the float-float positions are touched only by
 //    the moved atom's proposal and commit, so they live in HBM (L2): one
 //    16-byte load per move, issued one move ahead.
 //  * Draw words are refilled for the whole warp at once (when any walker needs
@@ -61,7 +63,7 @@ constexpr float FAR = 1.0e18f;
 // CTAs (64 registers) with the pair potentials, whose small-N runs need
 // little shared memory and gain from more resident warps.
 template <int POT, int BC, int LPR, int JPL>
-__global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) : (LPR == 4 ? 6 : 4))
+__global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 5 : 3) : (LPR == 4 ? 6 : 4))
     k_cycles32n(KParams P, int run0, int ncycles, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
@@ -83,8 +85,6 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
   };
   // order and sizes as in cycles32n_smem_bytes
   float4* s_xh = (float4*)carve((long long)R * Ns * 16);
-  float* s_sq = nullptr;
-  if (POT == POT_EAM) s_sq = (float*)carve((long long)R * Ns * 4);
   uint32_t* s_drw = (uint32_t*)carve((long long)R * DRWN * 4);
   double* s_beta = (double*)carve((long long)R * 8);
   double* s_en = (double*)carve((long long)R * 8);
@@ -118,7 +118,6 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
   for (int k = tid; k < R * (Ns - N); k += nthr) {
     const int v = k / (Ns - N), a = N + (k - v * (Ns - N));
     s_xh[v * Ns + a] = make_float4(FAR, FAR, FAR, 1.f);
-    if (POT == POT_EAM) s_sq[v * Ns + a] = 1.f;
   }
   if (POT == POT_EAM) {
     const double* gc = P.comp + rdp->comp_off;
@@ -126,7 +125,6 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
     for (int k = tid; k < R * N; k += nthr) {  // rho in the w lane of the position
       const int v = k / N, a = k - v * N;
       s_xh[v * Ns + a].w = (float)gc[2 * k + 1];
-      s_sq[v * Ns + a] = (float)sqrt(gc[2 * k + 1]);
     }
   }
   const int wk0 = rdp->wk;
@@ -159,7 +157,6 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
   double drift = P.drift[g];
   float4* Xh = s_xh + (size_t)w * Ns;
   float4* Xl = glo + (size_t)w * N;
-  float* SQ = s_sq ? s_sq + (size_t)w * Ns : nullptr;
   uint32_t* drw = s_drw + w * DRWN;
   const double hn = -0.5 * P.eam_n, hm = -0.5 * P.eam_m;
   const float hnf = P.f_hn, hmf = P.f_hm, ecamf = P.f_ecam;
@@ -293,13 +290,13 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
             sbf += db;
             // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
             de = fmaf(ean2f, da, de);
-            de = fmaf(necamf * db, rcpf(SQ[j] + sqrtf_approx(b.w + db)), de);
+            de = fmaf(necamf * db, rcpf(sqrtf_approx(b.w) + sqrtf_approx(b.w + db)), de);
           }
         }
       }
       sbf = seg_sum<LPR>(sbf, gmask);
       de = seg_sum<LPR>(de, gmask);
-      de -= ecamf * sbf * rcpf(SQ[i] + sqrtf_approx(x4.w + sbf));
+      de -= ecamf * sbf * rcpf(sqrtf_approx(x4.w) + sqrtf_approx(x4.w + sbf));
     } else {
       // ELJ pair terms with the coefficient count as a compile-time constant
       // (the neon coefficients have 6) or a runtime loop
@@ -354,7 +351,6 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
       float rho_i = 0.f;
       if (POT == POT_EAM) {
         rho_i = x4.w + sbf;
-        SQ[i] = sqrtf_approx(rho_i);
       }
       Xh[i] = make_float4(tf.x, tf.y, tf.z, rho_i);
       Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
@@ -366,11 +362,7 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
 #pragma unroll
           for (int u = 0; u < CH; ++u) {
             const int k = lane + (c + u) * LPR;
-            if (k < N && k != i) {
-              const float rho = Xh[k].w + dreg[c + u];
-              Xh[k].w = rho;
-              SQ[k] = sqrtf_approx(rho);
-            }
+            if (k < N && k != i) Xh[k].w += dreg[c + u];
           }
         }
       }
@@ -452,7 +444,7 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 4 : 3) 
       // halves (unused otherwise)
       const double e64 = energy64<POT, BC, ENS_NVT, LPR>(
           Xh, Xl, N, L, rc2, s_c, K, hn, hm, P.eam_ean, P.eam_ecam,
-          POT == POT_EAM ? &Xl[0].w : nullptr, SQ, lane, gmask, 4);
+          POT == POT_EAM ? &Xl[0].w : nullptr, nullptr, lane, gmask, 4);
       drift = fmax(drift, fabs(en - e64));
       en = e64;
       __syncwarp(gmask);
@@ -605,7 +597,6 @@ long long cycles32n_smem_bytes(int pot, int R, int N, int lpr) {
   auto al = [](long long b) { return (b + 15) / 16 * 16; };
   const long long Ns = narrow_stride(N, lpr);
   long long b = al(R * Ns * 16);                           // float4 hi positions (+ rho)
-  if (pot == POT_EAM) b += al(R * Ns * 4);                 // sqrt(rho)
   b += al(R * (long long)DRWN * 4);                        // draw words
   b += 2 * al(R * 8LL) + 2 * al(R * 16LL) + al(R * 48LL);  // beta, en, ham, maxd, counters
   b += 6 * al(R * 4LL);                                    // wos, sow, bl2e, mdf, mdc, acc
