@@ -61,10 +61,10 @@ METRIC = "atom-moves/sec on 1 GB300, chosen vs plain FP64 form at equal Cv(T) er
 CSRC = os.path.join(ROOT, "paralleltemperingmontecarlo.jl_gb300", "csrc")
 NARROW_SRC = ("ptmc_cycles32n.cu", "ptmc_fp32.cuh")
 PROFILED = {
-    # 608 runs x 32 replicas of Cu55, 4 lanes per walker, one 20-cycle launch
-    # (21.4 M attempted moves): 2.318e9 warp instructions, 54.2 MB DRAM
-    "cu55": dict(inst_per_move=108.3, lanes=4, dram_bytes_per_run=54.24e6 / 608,
-                 src=NARROW_SRC, src_sha="3e18449cfa42b697"),
+    # 760 runs x 32 replicas of Cu55, 4 lanes per walker, one 20-cycle launch
+    # (26.8 M attempted moves): 2.830e9 warp instructions, 79.9 MB DRAM
+    "cu55": dict(inst_per_move=105.8, lanes=4, dram_bytes_per_run=79.92e6 / 760,
+                 src=NARROW_SRC, src_sha="fee4d7e58adce072"),
 }
 
 
