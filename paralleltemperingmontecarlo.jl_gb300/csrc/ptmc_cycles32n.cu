@@ -63,7 +63,7 @@ constexpr float FAR = 1.0e18f;
 // CTAs (64 registers) with the pair potentials, whose small-N runs need
 // little shared memory and gain from more resident warps.
 template <int POT, int BC, int LPR, int JPL>
-__global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 5 : 3) : (LPR == 4 ? 6 : 4))
+__global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 5 : 3) : (LPR == 4 ? 7 : 4))
     k_cycles32n(KParams P, int run0, int ncycles, int phase) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_c[MAX_COEFF];
