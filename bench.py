@@ -64,7 +64,7 @@ PROFILED = {
     # 760 runs x 32 replicas of Cu55, 4 lanes per walker, one 20-cycle launch
     # (26.8 M attempted moves): 2.830e9 warp instructions, 79.9 MB DRAM
     "cu55": dict(inst_per_move=105.8, lanes=4, dram_bytes_per_run=79.92e6 / 760,
-                 src=NARROW_SRC, src_sha="fee4d7e58adce072"),
+                 src=NARROW_SRC, src_sha="8a9b5ad680ec6033"),
 }
 
 
