@@ -270,28 +270,36 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 5 : 3) 
     if (POT == POT_EAM) {
       // the phi part of dE is 2 ean sum_j da (the pair changes phi_i and phi_j
       // alike); rho_j is the w lane of atom j's position
+      auto term = [&](int c, int u) {
+        const int j = lane + (c + u) * LPR;
+        const float4 b = Xh[j];
+        const float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
+        const float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
+        float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
+        float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
+        if (!SENT) {  // the self pair (zero old distance) and the pads
+          const bool skip = j == i || j >= N;
+          da = skip ? 0.f : da;
+          db = skip ? 0.f : db;
+        }
+        dreg[c + u] = db;
+        sbf += db;
+        // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
+        de = fmaf(ean2f, da, de);
+        de = fmaf(necamf * db, rcpf(sqrtf_approx(b.w) + sqrtf_approx(b.w + db)), de);
+      };
+      // whole chunks without a test per term; the last, partial chunk tests
+      // each term against qmax (the same for every lane of the warp), so the
+      // pad terms beyond it (exactly zero) are not evaluated
 #pragma unroll
       for (int c = 0; c < JPL; c += CH) {
-        if (c < qmax) {
+        if (c + CH <= qmax) {
 #pragma unroll
-          for (int u = 0; u < CH; ++u) {
-            const int j = lane + (c + u) * LPR;
-            const float4 b = Xh[j];
-            const float ln_ = lg2f(pf2<BC>(tf, b, Lf, iLf));
-            const float lo_ = lg2f(pf2<BC>(x4, b, Lf, iLf));
-            float da = ex2f(hnf * ln_) - ex2f(hnf * lo_);
-            float db = ex2f(hmf * ln_) - ex2f(hmf * lo_);
-            if (!SENT) {  // the self pair (zero old distance) and the pads
-              const bool skip = j == i || j >= N;
-              da = skip ? 0.f : da;
-              db = skip ? 0.f : db;
-            }
-            dreg[c + u] = db;
-            sbf += db;
-            // sqrt(rho + db) - sqrt(rho) in the cancellation-free form
-            de = fmaf(ean2f, da, de);
-            de = fmaf(necamf * db, rcpf(sqrtf_approx(b.w) + sqrtf_approx(b.w + db)), de);
-          }
+          for (int u = 0; u < CH; ++u) term(c, u);
+        } else if (c < qmax) {
+#pragma unroll
+          for (int u = 0; u < CH; ++u)
+            if (c + u < qmax) term(c, u);
         }
       }
       sbf = seg_sum<LPR>(sbf, gmask);
@@ -323,6 +331,8 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 5 : 3) 
           }
           return __fmul_rn(p, s3);  // rounded as in v32p of the 16/32-lane kernel
         };
+        // whole chunks only (a partial last chunk, as in the EAM loop, made the
+        // Ne13 kernel slower: its 13 atoms fill one chunk of 4 terms per lane)
 #pragma unroll
         for (int c = 0; c < JPL; c += CH) {
           if (c < qmax) {
