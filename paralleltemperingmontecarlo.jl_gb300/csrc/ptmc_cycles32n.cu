@@ -357,25 +357,28 @@ __global__ void __launch_bounds__(32 * LPR, POT == POT_EAM ? (LPR == 4 ? 5 : 3) 
       return 0;
     }
     __syncwarp(gmask);
-    if (lane == 0) {
-      float rho_i = 0.f;
-      if (POT == POT_EAM) {
-        rho_i = x4.w + sbf;
-      }
-      Xh[i] = make_float4(tf.x, tf.y, tf.z, rho_i);
-      Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
-    }
     if (POT == POT_EAM) {
+      // density deltas of every slot up to the lane's term count, without a
+      // test per slot: the pads and atom i itself (a sentinel during the pair
+      // loop, or masked in the cube) carry an exact zero, and atom i's record
+      // is written after a warp barrier
 #pragma unroll
       for (int c = 0; c < JPL; c += CH) {
-        if (c < qmax) {
+        if (c + CH <= qmax) {
 #pragma unroll
-          for (int u = 0; u < CH; ++u) {
-            const int k = lane + (c + u) * LPR;
-            if (k < N && k != i) Xh[k].w += dreg[c + u];
-          }
+          for (int u = 0; u < CH; ++u) Xh[lane + (c + u) * LPR].w += dreg[c + u];
+        } else if (c < qmax) {
+#pragma unroll
+          for (int u = 0; u < CH; ++u)
+            if (c + u < qmax) Xh[lane + (c + u) * LPR].w += dreg[c + u];
         }
       }
+      __syncwarp(gmask);
+    }
+    if (lane == 0) {
+      const float rho_i = POT == POT_EAM ? x4.w + sbf : 0.f;
+      Xh[i] = make_float4(tf.x, tf.y, tf.z, rho_i);
+      Xl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
     }
     de_acc += de;
     __syncwarp(gmask);
