@@ -27,6 +27,8 @@ means must agree within 5 combined standard errors.
   * Ne32 NPT (cubic box, cut-off + tail correction, 1 atm): Cp(T) from
     multihistogram_NPT, FP32 move rows and volume moves (FP64 energy total)
     + resync; and the benchmarked Ne108 NPT configuration (32 replicas)
+  * Ne147, the batched workload's largest runs, in their benchmarked launch
+    shape (a cluster of 8 CTAs per run)
 """
 import json
 import os
@@ -97,6 +99,22 @@ def test_cv_ne13_fp32_vs_fp64(pk):
     # the FP32 form with 4 lanes per walker, the shape the benchmark runs
     compare(run_form(*args, "fp64", 11), run_form(*args, "fp32", 12, shape=(1, 4)),
             "Ne13 FP32+resync (4 lanes per walker)")
+
+
+def test_cv_ne147_cluster_shape_fp32_vs_fp64(pk):
+    """The largest runs of the batched workload: Ne147 (ELJEven, sphere start of
+    radius 0.9 N^(1/3) 3 bohr, container 3 bohr wider), 16 replicas over 4-16 K,
+    the FP32 form in the benchmark's launch shape for N = 147 (a cluster of 8
+    CTAs, 2 walkers each, 32 lanes per walker) against the plain FP64 form,
+    8 runs each (600 equilibration + 1500 production cycles)."""
+    import ptmc_gb300.starts as S
+    N, R = 147, 16
+    rad = 0.9 * N ** (1 / 3) * 3
+    starts = [S.sphere_start(N, rad, 4.3, 900 + r) for r in range(8)]
+    args = (pk, pk.ELJPotentialEven(C_NE), starts, pk.SphericalBC(rad + 3.0), R, (4.0, 16.0),
+            1200, 1500)
+    compare(run_form(*args, "fp64", 61), run_form(*args, "fp32", 62, shape=(8, 32)),
+            "Ne147 FP32+resync (8-CTA cluster)")
 
 
 def test_cv_cu55_eam_fp32_vs_fp64(pk):
