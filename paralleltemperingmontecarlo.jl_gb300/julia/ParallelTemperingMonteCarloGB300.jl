@@ -288,14 +288,18 @@ function multihistogram(output::Output, temp::TempGrid; outdir=pwd(), NPoints=10
 end
 
 """
-    train_surrogate!(ctx; cycles=300, capacity=40000, steps=4000, batch=512, lr=2e-3)
+    train_surrogate!(ctx; cycles=300, capacity=40000, steps=4000, batch=512, lr=2e-3,
+                     calibrate=false)
 
 Delayed-acceptance set-up on an initialised NN context (no counterpart in the
 reference): capture `cycles` of exact moves, train the pair surrogate on the
-GPU, calibrate the per-temperature screening strength, enable screening.
+GPU, enable screening. Screening strength 1 on every temperature (the standard
+two-stage test) unless `calibrate` asks for the per-temperature choice of
+`ptmc_surrogate_calibrate`.
 """
 function train_surrogate!(ctx::Ptr{Cvoid}; cycles=300, capacity=40000, steps=4000, batch=512,
-                          lr=2e-3, cfg=PTMCSurrogateCfg(2.0, 12.0, 0.5625, 12.0, 0.0))
+                          lr=2e-3, calibrate::Bool=false,
+                          cfg=PTMCSurrogateCfg(2.0, 12.0, 0.5625, 12.0, 0.0))
     check(ccall((:ptmc_surrogate_set, libptmc), Cint,
                 (Ptr{Cvoid}, Ref{PTMCSurrogateCfg}, Ptr{Cfloat}, Cint, Cint),
                 ctx, cfg, C_NULL, capacity, 1), ctx)
@@ -305,8 +309,8 @@ function train_surrogate!(ctx::Ptr{Cvoid}; cycles=300, capacity=40000, steps=400
     loss = Ref{Cdouble}(0)
     check(ccall((:ptmc_surrogate_train, libptmc), Cint, (Ptr{Cvoid}, Cint, Cint, Cdouble, Ref{Cdouble}),
                 ctx, steps, batch, lr, loss), ctx)
-    check(ccall((:ptmc_surrogate_calibrate, libptmc), Cint, (Ptr{Cvoid}, Cdouble, Cint, Ptr{Cdouble}),
-                ctx, 0.0, 10, C_NULL), ctx)
+    calibrate && check(ccall((:ptmc_surrogate_calibrate, libptmc), Cint,
+                             (Ptr{Cvoid}, Cdouble, Cint, Ptr{Cdouble}), ctx, 0.0, 10, C_NULL), ctx)
     check(ccall((:ptmc_surrogate_enable, libptmc), Cint, (Ptr{Cvoid}, Cint), ctx, 1), ctx)
     return loss[]
 end
