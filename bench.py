@@ -62,9 +62,9 @@ CSRC = os.path.join(ROOT, "paralleltemperingmontecarlo.jl_gb300", "csrc")
 NARROW_SRC = ("ptmc_cycles32n.cu", "ptmc_fp32.cuh")
 PROFILED = {
     # 760 runs x 32 replicas of Cu55, 4 lanes per walker, one 20-cycle launch
-    # (26.8 M attempted moves): 2.633e9 warp instructions, 80.4 MB DRAM
-    "cu55": dict(inst_per_move=98.4, lanes=4, dram_bytes_per_run=80.42e6 / 760,
-                 src=NARROW_SRC, src_sha="d7defd3a9fbb806e"),
+    # (26.8 M attempted moves): 2.511e9 warp instructions, 78.8 MB DRAM
+    "cu55": dict(inst_per_move=93.9, lanes=4, dram_bytes_per_run=78.85e6 / 760,
+                 src=NARROW_SRC, src_sha="c03d02f04a2d7d8a"),
 }
 
 
