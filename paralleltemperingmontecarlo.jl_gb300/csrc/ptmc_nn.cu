@@ -12,23 +12,32 @@
 // Execution: one CTA of 256 threads per walker (a move is ~10^5 FLOP, far too
 // much for one warp), one launch per MC cycle (N moves per walker), then a
 // per-run epilogue kernel does the exchange, step adaptation and sampling of
-// the cycle.  The host captures [cycle, epilogue] x C in one CUDA graph.
+// the cycle.  The host captures [cycle, epilogue] x C in one CUDA graph.  The
+// FP32 form fits two walker CTAs per SM (98 KB at N = 55).
 //
 // Per move:
 //   1. warp 0 draws the proposal (walker stream, reference draw order),
-//   2. threads over j: new/old distance rows, cut-off rows, hard-core test,
+//   2. threads over j: new/old distance rows, cut-off rows, hard-core test
+//      (with delayed acceptance the first stage follows: the frozen surrogate's
+//      tabulated pair function of the new and old distances),
 //   3. radial deltas: threads over (sf, j),
-//   4. angular deltas: threads over (j, k-chunk); each ordered pair (j, k)
-//      evaluates the old and new triangle (i, j, k) once and adds the centre-j
-//      term; one of (j, k) and (k, j) also adds the centre-i term.  FP64:
-//      exponentials shared by the functions with equal eta, powers
-//      (1 + lambda cos)^zeta by repeated squaring for zeta in {1, 2, 4, 8, 16};
-//      FP32: one ex2(zeta lg2(1 + lambda cos) + lg2(tpz) - eta log2(e) s) per
-//      function and term, branch-free,
-//   5. the MLP on every atom (every column of G changes): threads over
-//      (atom, hidden unit), layer by layer, block sum of the atom energies,
-//   6. Metropolis on thread 0, commit (positions, distance and cut-off
-//      matrices, G += dG) on acceptance.
+//   4. angular deltas.  FP32, table-specialised (a compiled pattern of eta
+//      groups, lambda signs and zeta powers, NN_PAT_CU55 for scripts/cu55.jl):
+//      lanes over the atoms j != i, chunks over cyclic offsets d of k; a
+//      triangle costs one exponential per eta group for its new and old shape
+//      and shared powers (1 +- cos)^(2^e), every function one FMA.  Otherwise
+//      (generic tables, FP64): threads over (j, k-chunk), each ordered pair
+//      (j, k) evaluates the old and new triangle once and adds the centre-j
+//      term, one of (j, k) and (k, j) also the centre-i term; FP64:
+//      exponentials shared by the functions with equal eta, powers by repeated
+//      squaring; FP32: one ex2(zeta lg2(1 + lambda cos) + lg2(tpz) - eta
+//      log2(e) s) per function and term,
+//   5. the MLP on every atom (every column of G changes): FP32 on the tensor
+//      cores (two 3xTF32 tcgen05 GEMMs, rows = atoms, activations on all 8
+//      warps), FP64 on the CUDA cores, threads over (atom, hidden unit),
+//   6. Metropolis on warp 0; on acceptance warp 0 moves the atom and goes on
+//      to the next proposal while warps 1-7 commit the distance and cut-off
+//      rows and G += dG.
 #include <cuda_runtime.h>
 
 #include "ptmc_device.cuh"
