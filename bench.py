@@ -334,6 +334,19 @@ def _accepted(eng, B):
     return sum(int(eng.states(r)["counts"][:, 0].sum()) for r in range(B))
 
 
+def combine_ranks(torch, dev_s, moves, device, world):
+    """Whole-job figures of a timed segment: under torchrun every rank runs its
+    own batch (replicas only, weak scaling), the job takes as long as its
+    slowest rank and makes the moves of all ranks."""
+    if world <= 1:
+        return dev_s, float(moves)
+    t = torch.tensor([dev_s], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    m = torch.tensor([float(moves)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(m)
+    return float(t.item()), float(m.item())
+
+
 def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, e2e_on):
     """One workload: the chosen form (and the plain FP64 form unless
     --only-chosen) timed on the production path; returns its record."""
@@ -363,16 +376,7 @@ def run_workload(args, name, pk, torch, dev, rank, world, peaks, steps, warmup, 
         wall = time.perf_counter() - t0
         st1 = eng.stats()
         moves = sum(sizes) * W["R"] * cyc * k_steps
-        dev_s = sum(ms) / 1e3
-        if world > 1:
-            t = torch.tensor([dev_s], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            dev_s = float(t.item())
-            m = torch.tensor([float(moves)], device=dev)
-            torch.distributed.all_reduce(m)
-            moves_all = float(m.item())
-        else:
-            moves_all = float(moves)
+        dev_s, moves_all = combine_ranks(torch, sum(ms) / 1e3, moves, dev, world)
         acc = _accepted(eng, nruns)
         return dict(value=moves_all / dev_s, runs=nruns, ms_per_step=1e3 * dev_s / k_steps, wall=wall,
                     steps=k_steps, cycles_per_step=cyc,
