@@ -105,8 +105,7 @@ def workload(name):
     """Description of one workload: replicas, temperature range, potential,
     ensemble, boundary, per-run atom counts and start configurations, chosen
     and plain-form cycles per timed step, and the algorithmic FP32 work per
-    pair (SURVEY-style counts: ELJ 24 ops, +9 with the minimum image; EAM 17
-    ops + 3 MUFU)."""
+    pair (ELJ 24 ops, +9 with the minimum image; EAM 17 ops + 3 MUFU)."""
     if name == "cu55":
         return dict(name="cu55_eam", R=32, T=(200.0, 1000.0), pot="eam", ens="nvt",
                     bc=("sphere", 14.0), sizes=lambda B: [55] * B,
