@@ -302,7 +302,10 @@ int ptmc_surrogate_record(ptmc_ctx* c, int on);
 int ptmc_surrogate_train(ptmc_ctx* c, int steps, int batch, double lr,
                          double* loss_out);
 /* Switch delayed-acceptance moves on (1) or off (0); the surrogate is frozen
- * while on. */
+ * while on.  Switching on tabulates the network's pair function phi(r) on 4097
+ * grid distances over [0, r_cut] (phi is constant beyond r_cut); the first
+ * stage of a move interpolates linearly in that table, a fixed pair function of
+ * the distance, so the two-stage chain stays exact. */
 int ptmc_surrogate_enable(ptmc_ctx* c, int on);
 /* Current parameters (params may be NULL), the configuration in use (cfg may
  * be NULL) and counters stats[4] = {records captured, first-stage
