@@ -72,7 +72,9 @@ class TempGrid:
         if tdistr not in ("geometric", "equally_spaced"):
             raise ValueError("chosen temperature distribution %s does not exist" % tdistr)
         i = np.arange(N, dtype=np.float64)
-        if tdistr == "equally_spaced":
+        if N == 1:  # the reference's formulas divide 0 / 0 here (NaN); one temperature, ti
+            self.t_grid = np.array([float(ti)])
+        elif tdistr == "equally_spaced":
             delta = (tf - ti) / (N - 1)
             self.t_grid = ti + i * delta
         else:

@@ -541,3 +541,33 @@ def test_set_configs_batch_equals_per_run(pk):
         assert np.array_equal(a.output(r).en_histogram, b.output(r).en_histogram)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("R", [1, 3])
+def test_one_replica_and_two_atoms(pk, orc, R):
+    """Edge cases against the oracle (plain FP64 form): one replica, where the
+    exchange step has no partner (the reference's rand(1:n_traj - 1) has nothing to
+    draw; engine and oracle skip the step and its draws), and the smallest
+    configuration, two atoms (one pair); equilibration, then production with
+    histograms.  The FP32 form runs the same cases."""
+    for N, x0 in ((2, np.array([[0.0, 0.0, 0.0], [5.5, 0.0, 0.0]])), (13, sphere_start(13, 8.0, 4.5, 3))):
+        eng, (o,) = pair(pk, orc, N=N, R=R, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                         bc_param=11.0, exch_prob=1.0, seed=5, eq=40)
+        eng.equilibrate()
+        o.equilibrate(40)
+        eng.run_cycles(100)
+        o.production(1, 100)
+        g = compare(eng, o)
+        assert g["counts"][:, 0].sum() > 0
+        if R == 1:
+            assert g["counts"][:, 4].sum() == 0  # no exchange attempted
+        eh, _, _ = o.hist()
+        assert np.array_equal(eng.output(0).en_histogram, eh)
+        eng.close()
+        e32, _ = pair(pk, orc, N=N, R=R, x0=x0, T0=4.0, T1=16.0, pot=pk.ELJPotentialEven(C_NE),
+                      bc_param=11.0, exch_prob=1.0, seed=5, eq=40, precision="fp32")
+        e32.equilibrate()
+        e32.run_cycles(100)
+        s32 = e32.states(0)
+        assert np.all(np.isfinite(s32["en_tot"])) and s32["counts"][:, 0].sum() > 0
+        e32.close()
