@@ -23,7 +23,8 @@ means must agree within 5 combined standard errors.
     GPU multihistogram's energy origin at en_min matters: the reference's
     formulation overflows there.
   * NN13 (RuNNer potential, random FP32 weights), FP32 + delayed acceptance
-    with a GPU-trained surrogate and calibrated screening strength
+    with a GPU-trained surrogate and calibrated screening strength; and NN55,
+    the benchmarked configuration, delayed acceptance against the exact FP32 form
   * Ne32 NPT (cubic box, cut-off + tail correction, 1 atm): Cp(T) from
     multihistogram_NPT, FP32 move rows and volume moves (FP64 energy total)
     + resync; and the benchmarked Ne108 NPT configuration (32 replicas)
@@ -226,3 +227,39 @@ def test_cv_nn13_delayed_acceptance_vs_fp64(pk):
     args = (pk, pot, starts, pk.SphericalBC(10.0), 8, (300.0, 900.0), 2000, 4000)
     compare(run_form(*args, "fp64", 31, da=pre), run_form(*args, "fp32", 32, da=da),
             "NN13 FP32+delayed acceptance", spread="both")
+
+
+def test_cv_nn55_delayed_acceptance_vs_exact_fp32(pk):
+    """Delayed acceptance on the benchmarked NN55 configuration itself (88 symmetry
+    functions of scripts/cu55.jl, r_c 12 bohr, MLP 88-20-20-1 with seeded FP32
+    weights, output layer x0.3, 3-bohr hard core; Cu55 icosahedral start in
+    SphericalBC(14); 64 replicas over 300-900 K): Cv(T) of the screened chain
+    (surrogate trained on the GPU from 300 cycles of the chain's own records,
+    strength 1 on every temperature, the benchmark's chosen form) against the
+    exact FP32 chain, 8 runs each.  The plain FP64 form is too slow at this size
+    for a spread of independent runs (0.15 M atom-moves/s on the whole GPU); the
+    exact FP32 form is itself checked against FP64 (energies to 1e-5, the NN13 Cv
+    test)."""
+    tables = json.load(open(os.path.join(GOLDEN, "nn_cu55.json")))
+    nodes = [88, 20, 20, 1]
+    pot = pk.RuNNerPotential(pk.RuNNerPotential.sf_table(tables, 12.0),
+                             pk.RuNNerPotential.random_weights(nodes, 3, 0.3), nodes, boundary=3.0)
+    x0 = np.array(tables["ico55_nm"]) * (tables["cu_lattice_nm"] * tables["nm_to_bohr"])
+    starts = [x0.copy() for _ in range(8)]
+
+    def pre(eng):  # the same cycles before equilibration as the screened form
+        eng.cycles_nosample(400)
+
+    def da(eng):
+        eng.cycles_nosample(100)
+        eng.surrogate_set(pk.PairSurrogate(2.0, 12.0, None, 12.0, 0.0), capacity=100000,
+                          record_every=4)
+        eng.surrogate_record(True)
+        eng.cycles_nosample(300)
+        eng.surrogate_record(False)
+        eng.surrogate_train(4000, batch=512, lr=2e-3)
+        eng.surrogate_enable(True)
+
+    args = (pk, pot, starts, pk.SphericalBC(14.0), 64, (300.0, 900.0), 1000, 2000)
+    compare(run_form(*args, "fp32", 71, da=pre), run_form(*args, "fp32", 72, da=da),
+            "NN55 FP32+delayed acceptance vs exact FP32", spread="both")
