@@ -585,6 +585,10 @@ int launch_n(int what, const KParams& P, int run0, int nruns, int R, int maxN, i
 template <int POT, int BC>
 int launch_nl(int what, const KParams& P, int run0, int nruns, int R, int maxN, int ncycles,
               int phase, int lpr, cudaStream_t st, int* occ) {
+  // pair-potential runs of at most 16 atoms (Ne13): one chunk of 4 terms per
+  // lane, without the tests of the three chunks such runs never reach
+  if (POT != POT_EAM && lpr == 4 && maxN <= 16)
+    return launch_n<POT, BC, 4, 4>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ);
   if (lpr == 4) return launch_n<POT, BC, 4, 16>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ);
   if (lpr == 8) return launch_n<POT, BC, 8, 8>(what, P, run0, nruns, R, maxN, ncycles, phase, st, occ);
   return (int)cudaErrorInvalidValue;
