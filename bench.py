@@ -64,7 +64,7 @@ PROFILED = {
     # 760 runs x 32 replicas of Cu55, 4 lanes per walker, one 20-cycle launch
     # (26.8 M attempted moves): 2.511e9 warp instructions, 78.8 MB DRAM
     "cu55": dict(inst_per_move=93.9, lanes=4, dram_bytes_per_run=78.85e6 / 760,
-                 src=NARROW_SRC, src_sha="c03d02f04a2d7d8a"),
+                 src=NARROW_SRC, src_sha="6e43710641953936"),
 }
 
 
